@@ -1,0 +1,225 @@
+/*
+ * mfgpu.h -- C ABI of the GB300 matched-filtering library (libmfgpu.so).
+ *
+ * The library is a drop-in for mflib's matched-filtering hot path: every
+ * entry point below replaces one method of the reference's C++ classes,
+ * cited as file:line within the mflib project.  Plain pointers and sizes
+ * only; no exception crosses this boundary.  Every function returns an
+ * mfgpu_status; on failure mfgpu_last_error() holds a message for the
+ * calling thread.  MFGPU_EINVAL maps to the reference's
+ * std::invalid_argument, MFGPU_ESTATE to std::runtime_error.
+ *
+ * Threading: an object (matched filter, peak finder, DBSCAN) is used by one
+ * host thread at a time, like the reference classes.  Each object owns its
+ * own CUDA stream on the current device.  All host buffers passed in are
+ * copied (the reference copies every input, e.g. src/matchedFilter.cpp:896-904).
+ *
+ * Sample type: a matched filter or peak finder is created for
+ * MFGPU_FLOAT32 or MFGPU_FLOAT64 (MFLib::MatchedFilter<float|double>);
+ * `const void *` sample arguments point at that type.
+ */
+#ifndef MFGPU_H
+#define MFGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum
+{
+    MFGPU_OK = 0,
+    MFGPU_EINVAL = 1,   /* invalid argument   (reference: std::invalid_argument) */
+    MFGPU_ESTATE = 2,   /* invalid state      (reference: std::runtime_error)    */
+    MFGPU_ENOMEM = 3,   /* device or pinned host allocation failed               */
+    MFGPU_ECUDA = 4,    /* CUDA runtime error                                    */
+    MFGPU_ETIMEOUT = 5  /* a bounded device-side wait gave up                    */
+} mfgpu_status;
+
+enum { MFGPU_FLOAT32 = 4, MFGPU_FLOAT64 = 8 };
+
+/* MFLib::MatchedFilterDetectionMode, include/mflib/enums.hpp:24-32 */
+enum { MFGPU_SINGLE_CHANNEL = 0, MFGPU_MULTI_CHANNEL = 1 };
+
+/* Message for the last failed call on this thread ("" if none). */
+const char *mfgpu_last_error(void);
+
+/* Library version (major*10000 + minor*100 + patch). */
+int mfgpu_version(void);
+
+/* Number of visible CUDA devices (0 when none). */
+mfgpu_status mfgpu_device_count(int *count);
+
+/* MFLib::computeOptimalFFTAndBlockLength(nb, nx),
+ * include/mflib/matchedFilterParameters.hpp:208, src/matchedFilterParameters.cpp:371-385.
+ * Returns the reference's FFT length and overlap-add block length. */
+mfgpu_status mfgpu_fft_sizes(int nb, int nx, int *fft_length, int *block_length);
+
+/* ------------------------------------------------------------------------ */
+/* Matched filter: MFLib::MatchedFilter<T> (include/mflib/matchedFilter.hpp:28-178)
+ * and its SINGLE_CHANNEL facade MFLib::SingleChannel::MatchedFilter<T>
+ * (include/mflib/singleChannel/matchedFilter.hpp). */
+typedef struct mfgpu_mf mfgpu_mf;
+
+/* Everything MatchedFilter<T>::initialize reads from MatchedFilterParameters
+ * (src/matchedFilter.cpp:507-593): templates (FP64 samples, as stored by
+ * WaveformTemplate), signal size, detection mode, and the per-template
+ * shift/weight that shiftAndStack uses (:577-592). */
+typedef struct
+{
+    int detection_mode;             /* MFGPU_SINGLE_CHANNEL or MFGPU_MULTI_CHANNEL */
+    int n_templates;                /* >= 1 */
+    const int *template_lengths;    /* [n_templates], each >= 1 */
+    const double *const *templates; /* [n_templates] pointers to FP64 samples */
+    int signal_size;                /* samples per signal, >= 1 */
+    /* shift-and-stack inputs, may be NULL: the reference stacks only when
+       every template has an onset and a travel time (:581-592) */
+    const int *stack_shifts;        /* round((travel - onset) * fs) per template */
+    const double *stack_weights;    /* per template weight in [0,1] */
+    int stack_absolute_values;      /* MatchedFilterParameters::getStackAbsoluteValues */
+    /* Extension (no reference counterpart): share one signal between
+       several templates.  n_channels = 0 keeps the reference layout (one
+       signal per template in MULTI_CHANNEL, one signal in SINGLE_CHANNEL).
+       Otherwise template t reads channel template_channel[t]. */
+    int n_channels;
+    const int *template_channel;
+    /* Extension: FFT length for the overlap-save blocks; 0 = autotune. */
+    int fft_length;
+} mfgpu_mf_params;
+
+/* MatchedFilter<T>::MatchedFilter(); precision MFGPU_FLOAT32 | MFGPU_FLOAT64 */
+mfgpu_status mfgpu_mf_create(int precision, mfgpu_mf **mf);
+/* ~MatchedFilter() */
+mfgpu_status mfgpu_mf_destroy(mfgpu_mf *mf);
+/* MatchedFilter<T>::initialize, src/matchedFilter.cpp:507-821 */
+mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *params);
+/* MatchedFilter<T>::clear, src/matchedFilter.cpp:501-504 */
+mfgpu_status mfgpu_mf_clear(mfgpu_mf *mf);
+/* MatchedFilter<T>::isInitialized, src/matchedFilter.cpp:1367-1371 */
+mfgpu_status mfgpu_mf_is_initialized(const mfgpu_mf *mf, int *flag);
+/* MatchedFilter<T>::getNumberOfTemplates, src/matchedFilter.cpp:1374-1382 */
+mfgpu_status mfgpu_mf_get_number_of_templates(const mfgpu_mf *mf, int *n);
+/* MatchedFilter<T>::getSignalLength, src/matchedFilter.cpp:1385-1393 */
+mfgpu_status mfgpu_mf_get_signal_length(const mfgpu_mf *mf, int *n);
+/* MatchedFilter<T>::getFilteredSignalLength (n - maxLen + 1), src/matchedFilter.cpp:1396-1402 */
+mfgpu_status mfgpu_mf_get_filtered_signal_length(const mfgpu_mf *mf, int *n);
+/* MatchedFilter<T>::setSignal(it, n, x) (host samples), src/matchedFilter.cpp:863-921.
+ * MULTI_CHANNEL: signal of template `it`; SINGLE_CHANNEL: it must be 0
+ * (SingleChannel::MatchedFilter::setSignal, src/singleChannel/matchedFilter.cpp:62-67). */
+mfgpu_status mfgpu_mf_set_signal(mfgpu_mf *mf, int it, int n, const void *x);
+/* MatchedFilter<T>::zeroSignal, src/matchedFilter.cpp:824-845 */
+mfgpu_status mfgpu_mf_zero_signal(mfgpu_mf *mf, int it);
+/* MatchedFilter<T>::getSignalPointer, src/matchedFilter.cpp:924-938: copies the
+ * stored signal of `it` (n samples) to host memory `dst` (capacity maxn). */
+mfgpu_status mfgpu_mf_get_signal(const mfgpu_mf *mf, int it, int maxn, void *dst);
+/* MatchedFilter<T>::apply, src/matchedFilter.cpp:972-1316.  Enqueues the
+ * work on the object's stream; getters synchronise. */
+mfgpu_status mfgpu_mf_apply(mfgpu_mf *mf);
+/* MatchedFilter<T>::haveMatchedFilteredSignals, src/matchedFilter.cpp:1405-1409 */
+mfgpu_status mfgpu_mf_have_matched_filtered_signals(const mfgpu_mf *mf, int *flag);
+/* MatchedFilter<T>::getMatchedFilteredSignal, src/matchedFilter.cpp:941-948:
+ * copies the first getFilteredSignalLength() coefficients of template `it`
+ * into `dst` (capacity maxn); *nout receives the count. */
+mfgpu_status mfgpu_mf_get_matched_filtered_signal(mfgpu_mf *mf, int it, int maxn, void *dst, int *nout);
+/* MatchedFilter<T>::shiftAndStack, src/matchedFilter.cpp:1319-1364 */
+mfgpu_status mfgpu_mf_shift_and_stack(mfgpu_mf *mf, int maxn, void *dst, int *nout);
+/* MatchedFilter<T>::getSpectraOfTemplate, src/matchedFilter.cpp:1412-1431: the
+ * reference's debug view, rfft of the reversed, demeaned, unit-norm template
+ * at the reference's FFT length (computed on the device on request);
+ * dst holds 2*(nfft/2+1) interleaved re/im values of the object's type. */
+mfgpu_status mfgpu_mf_get_spectra_of_template(mfgpu_mf *mf, int it, int maxn, void *dst, int *nout);
+
+/* Extensions (no reference counterpart) --------------------------------- */
+/* Signal of channel c (n_channels > 0 layout), host samples. */
+mfgpu_status mfgpu_mf_set_channel_signal(mfgpu_mf *mf, int channel, int n, const void *x);
+/* Signal of channel c from device memory (same type, n samples). */
+mfgpu_status mfgpu_mf_set_channel_signal_device(mfgpu_mf *mf, int channel, int n, const void *dx);
+/* Full valid coefficient range of template it: lags 0..n-L_t (n - L_t + 1
+ * values), host copy. */
+mfgpu_status mfgpu_mf_get_valid_signal(mfgpu_mf *mf, int it, int maxn, void *dst, int *nout);
+/* Device pointer to template it's coefficients (lag k at p[k]) and the
+ * number of valid lags; valid until the next apply/initialize/clear. */
+mfgpu_status mfgpu_mf_get_device_signal(mfgpu_mf *mf, int it, const void **dptr, int *nvalid);
+/* Overlap-save plan chosen at initialize. */
+mfgpu_status mfgpu_mf_get_plan(const mfgpu_mf *mf, int *fft_length, int *lags_per_block, int *n_blocks);
+/* Block until the object's stream is idle; reports device-side errors. */
+mfgpu_status mfgpu_mf_synchronize(mfgpu_mf *mf);
+/* Device time (ms) of the last apply's correlation kernel and of the whole
+ * apply (correlation + dead-trace checks), measured with CUDA events on
+ * the object's stream. */
+mfgpu_status mfgpu_mf_get_last_timings(mfgpu_mf *mf, float *xcorr_ms, float *apply_ms);
+/* Number of kernel launches issued by the object since it was created. */
+mfgpu_status mfgpu_mf_get_launch_count(const mfgpu_mf *mf, long long *count);
+
+/* Batched peak finding on the device over every template's coefficients
+ * (PeakFinder<T>::apply, src/peakFinder.cpp:329-446, applied per template
+ * as SingleChannel::Detector does, src/singleChannel/detector.cpp:466-489).
+ * trace_length: lags searched per template; 0 = getFilteredSignalLength().
+ * Results stay on the device; read them with mfgpu_mf_get_peaks. */
+mfgpu_status mfgpu_mf_find_peaks(mfgpu_mf *mf, double threshold, int min_distance, int trace_length);
+/* Peaks of template it (ascending lag indices). */
+mfgpu_status mfgpu_mf_get_peaks(mfgpu_mf *mf, int it, int maxn, int *dst, int *nout);
+/* Total peaks over all templates, and all of them at once: counts[nt] and
+ * indices[sum counts] (template-major, ascending within a template). */
+mfgpu_status mfgpu_mf_get_all_peaks(mfgpu_mf *mf, int nt, int *counts, int max_total, int *indices,
+                                    int *total);
+
+/* ------------------------------------------------------------------------ */
+/* Peak finder: MFLib::PeakFinder<T> (include/private/peakFinder.hpp:12-138). */
+typedef struct mfgpu_peaks mfgpu_peaks;
+mfgpu_status mfgpu_peaks_create(int precision, mfgpu_peaks **pf);
+mfgpu_status mfgpu_peaks_destroy(mfgpu_peaks *pf);
+/* PeakFinder<T>::setThreshold (must be in [0,1]), src/peakFinder.cpp:226-235 */
+mfgpu_status mfgpu_peaks_set_threshold(mfgpu_peaks *pf, double threshold);
+mfgpu_status mfgpu_peaks_get_threshold(const mfgpu_peaks *pf, double *threshold);
+/* PeakFinder<T>::setMinimumPeakDistance, src/peakFinder.cpp:251-256 */
+mfgpu_status mfgpu_peaks_set_minimum_peak_distance(mfgpu_peaks *pf, int min_distance);
+mfgpu_status mfgpu_peaks_get_minimum_peak_distance(const mfgpu_peaks *pf, int *min_distance);
+/* PeakFinder<T>::setSignal (host samples, n >= 1), src/peakFinder.cpp:260-283 */
+mfgpu_status mfgpu_peaks_set_signal(mfgpu_peaks *pf, int n, const void *x);
+/* PeakFinder<T>::apply, src/peakFinder.cpp:329-446 */
+mfgpu_status mfgpu_peaks_apply(mfgpu_peaks *pf);
+/* PeakFinder<T>::getNumberOfPeaks, src/peakFinder.cpp:287-290 */
+mfgpu_status mfgpu_peaks_get_number_of_peaks(const mfgpu_peaks *pf, int *n);
+/* PeakFinder<T>::getPeakIndices, src/peakFinder.cpp:294-311 */
+mfgpu_status mfgpu_peaks_get_peak_indices(const mfgpu_peaks *pf, int maxn, int *dst);
+/* PeakFinder<T>::clear */
+mfgpu_status mfgpu_peaks_clear(mfgpu_peaks *pf);
+
+/* ------------------------------------------------------------------------ */
+/* DBSCAN: MFLib::DBSCAN (include/private/dbscan.hpp:10-132). */
+typedef struct mfgpu_dbscan mfgpu_dbscan;
+mfgpu_status mfgpu_dbscan_create(mfgpu_dbscan **db);
+mfgpu_status mfgpu_dbscan_destroy(mfgpu_dbscan *db);
+/* DBSCAN::initialize(epsilon >= 0, minObservations >= 1), src/dbscan.cpp:95-112 */
+mfgpu_status mfgpu_dbscan_initialize(mfgpu_dbscan *db, double epsilon, int min_observations);
+/* DBSCAN::setData, src/dbscan.cpp:115-138: row-major [n_obs x n_features] */
+mfgpu_status mfgpu_dbscan_set_data(mfgpu_dbscan *db, int n_obs, int n_features, const double *X);
+/* DBSCAN::setWeightedData, src/dbscan.cpp:141-184: weights > 0 or NULL */
+mfgpu_status mfgpu_dbscan_set_weighted_data(mfgpu_dbscan *db, int n_obs, int n_features, const double *X,
+                                            const double *weights);
+/* DBSCAN::cluster, src/dbscan.cpp:187-214 */
+mfgpu_status mfgpu_dbscan_cluster(mfgpu_dbscan *db);
+/* DBSCAN::getNumberOfClusters, src/dbscan.cpp:229-232 */
+mfgpu_status mfgpu_dbscan_get_number_of_clusters(const mfgpu_dbscan *db, int *n);
+/* DBSCAN::getLabels, src/dbscan.cpp:235-239 (-1 = noise) */
+mfgpu_status mfgpu_dbscan_get_labels(const mfgpu_dbscan *db, int maxn, int *labels);
+/* Extension: number of kernel launches issued by the object so far. */
+mfgpu_status mfgpu_dbscan_get_launch_count(const mfgpu_dbscan *db, long long *count);
+mfgpu_status mfgpu_dbscan_is_initialized(const mfgpu_dbscan *db, int *flag);
+mfgpu_status mfgpu_dbscan_have_data(const mfgpu_dbscan *db, int *flag);
+mfgpu_status mfgpu_dbscan_have_labels(const mfgpu_dbscan *db, int *flag);
+mfgpu_status mfgpu_dbscan_clear(mfgpu_dbscan *db);
+
+/* Segmented DBSCAN (extension): n_segments independent problems in one
+ * launch sequence, as SingleChannel::Associator::associate runs one DBSCAN
+ * per template id (src/singleChannel/associator.cpp:192-264).  Observations
+ * of segment s are rows seg_offsets[s]..seg_offsets[s+1]-1; labels are
+ * numbered per segment; n_clusters[s] receives each segment's count.
+ * weights may be NULL. */
+mfgpu_status mfgpu_dbscan_segmented(mfgpu_dbscan *db, int n_segments, const int *seg_offsets, int n_features,
+                                    const double *X, const double *weights, int *labels, int *n_clusters);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MFGPU_H */

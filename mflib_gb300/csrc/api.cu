@@ -1,0 +1,1189 @@
+// api.cu -- the C ABI of libmfgpu.so (declared in include/mfgpu.h).
+//
+// Host-side objects mirror the reference classes: mfgpu_mf is
+// MFLib::MatchedFilter<T> (src/matchedFilter.cpp), mfgpu_peaks is
+// MFLib::PeakFinder<T> (src/peakFinder.cpp), mfgpu_dbscan is MFLib::DBSCAN
+// (src/dbscan.cpp).  Argument checks follow the reference's exceptions:
+// std::invalid_argument -> MFGPU_EINVAL, std::runtime_error -> MFGPU_ESTATE.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+#include "mfgpu.h"
+#include "launch.h"
+
+using namespace mfgpu;
+
+namespace {
+
+thread_local std::string g_err;
+
+mfgpu_status fail(mfgpu_status s, const std::string &msg)
+{
+    g_err = msg;
+    return s;
+}
+
+mfgpu_status cuda_fail(cudaError_t e, const char *what)
+{
+    return fail(e == cudaErrorMemoryAllocation ? MFGPU_ENOMEM : MFGPU_ECUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CU(expr)                                                                                                   \
+    do                                                                                                             \
+    {                                                                                                              \
+        cudaError_t e_ = (expr);                                                                                   \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #expr);                                                        \
+    } while (0)
+
+struct DeviceGuard
+{
+    int prev = -1;
+    explicit DeviceGuard(int dev)
+    {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard()
+    {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+// computeWindowLength, src/matchedFilterParameters.cpp:47-104 (with the
+// guards of computeOptimalFFTAndBlockLength, :371-385).  The operation-count
+// table and the candidate lengths are the reference's, so the chosen
+// (FFT length, block length) pair is identical.
+const double kFftFlops[21] = {18,       59,       138,       303,       660,       1441,     3150,
+                              6875,     14952,    32373,     69762,     149647,    319644,   680105,
+                              1441974,  3047619,  6422736,   13500637,  28311786,  59244791, 59244791 * 2.09};
+
+mfgpu_status fft_sizes(int nb, int nx, int *nfft, int *L)
+{
+    if (nb < 1) return fail(MFGPU_EINVAL, "Filter length must be positive");
+    if (nx <= nb)
+        return fail(MFGPU_EINVAL, "Signal length = " + std::to_string(nx) + " must exceed filter length = " +
+                                      std::to_string(nb));
+    int start = -1;
+    for (int i = 0; i < 21; ++i)
+        if ((uint64_t) 1 << (i + 1) > (uint64_t) (nb - 1)) { start = i; break; }
+    if (start < 0)
+    {
+        int p = 1;
+        if (nx > 1) p = (int) std::pow(2.0, std::ceil(std::log2((double) nx)));
+        *nfft = p;
+        *L = p - (nb - 1);
+        return MFGPU_OK;
+    }
+    double best = std::numeric_limits<double>::max();
+    int bn = 0, bl = 0;
+    for (int i = start; i < 21; ++i)
+    {
+        int len = 1 << (i + 1);
+        int lt = len - (nb - 1);
+        double obj = std::ceil((double) nx / (double) lt) * kFftFlops[i];
+        if (obj < best) { best = obj; bn = len; bl = lt; }
+    }
+    *nfft = bn;
+    *L = bl;
+    return MFGPU_OK;
+}
+
+template <class T> void fill_twiddles(std::vector<cx<T>> &tw)
+{
+    tw.resize(kNMax);
+    const double two_pi = 6.283185307179586476925286766559;
+    for (int k = 0; k < kNMax; ++k)
+    {
+        double a = -two_pi * (double) k / (double) kNMax;
+        tw[k].x = (T) std::cos(a);
+        tw[k].y = (T) std::sin(a);
+    }
+}
+
+}  // namespace
+
+// ============================================================================
+struct mfgpu_mf
+{
+    int prec = 4;
+    int dev = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool initialized = false, have = false, timed = false;
+    int mode = MFGPU_MULTI_CHANNEL, nt = 0, n = 0, maxLen = 0, minLen = 0, nch = 0;
+    std::vector<int> lens, tchan, nvalid;
+    std::vector<double> tmpl;
+    std::vector<long> toff;
+    bool can_stack = false;
+    std::vector<int> shifts;
+    std::vector<double> weights;
+    int stack_abs = 1;
+    bool ref_layout = true;
+    // overlap-save plan
+    int nfft = 0, log2p = 0, S = 0, nblocks = 0, ngroups = 0, maxvalid = 0;
+    bool shared_den = false;
+    long ldx = 0, ldr = 0;
+    int dead_chunks = 1;
+    // device buffers
+    DevBuf x, rho, Bc, tw, grp_chan, grp_tb, grp_te, tids, tlen_d, nvalid_d, dead, err, tmpl_d, toff_d, pmin, pmax,
+        chan_list, stackbuf, shifts_d, weights_d, specbuf;
+    PeakWS pk;
+    std::vector<long long> pk_off;
+    bool have_peaks = false;
+    long long launches = 0;
+    float last_xcorr_ms = 0, last_apply_ms = 0;
+
+    size_t esz() const { return (size_t) prec; }
+    void release_device()
+    {
+        DevBuf *all[] = {&x,      &rho,      &Bc,   &tw,  &grp_chan, &grp_tb, &grp_te, &tids,      &tlen_d,
+                         &nvalid_d, &dead,   &err,  &tmpl_d, &toff_d, &pmin, &pmax,  &chan_list, &stackbuf,
+                         &shifts_d, &weights_d, &specbuf};
+        for (DevBuf *d : all) d->release();
+        pk.release();
+    }
+    void reset()
+    {
+        if (stream) cudaStreamSynchronize(stream);
+        release_device();
+        initialized = have = timed = have_peaks = false;
+        nt = n = maxLen = minLen = nch = 0;
+        lens.clear(); tchan.clear(); nvalid.clear(); tmpl.clear(); toff.clear();
+        shifts.clear(); weights.clear(); pk_off.clear();
+        can_stack = false;
+        nfft = log2p = S = nblocks = ngroups = maxvalid = 0;
+        ldx = ldr = 0;
+    }
+};
+
+static mfgpu_status mf_sync(mfgpu_mf *mf)
+{
+    CU(cudaStreamSynchronize(mf->stream));
+    if (mf->initialized && mf->err.p)
+    {
+        int e = 0;
+        CU(cudaMemcpy(&e, mf->err.p, sizeof(int), cudaMemcpyDeviceToHost));
+        if (e != 0)
+        {
+            CU(cudaMemset(mf->err.p, 0, sizeof(int)));
+            mf->have = false;
+            return fail(e == KERR_TMA_TIMEOUT ? MFGPU_ETIMEOUT : MFGPU_ECUDA,
+                        "device kernel reported error code " + std::to_string(e));
+        }
+    }
+    if (mf->timed)
+    {
+        cudaEventElapsedTime(&mf->last_xcorr_ms, mf->ev[1], mf->ev[2]);
+        cudaEventElapsedTime(&mf->last_apply_ms, mf->ev[0], mf->ev[3]);
+        mf->timed = false;
+    }
+    return MFGPU_OK;
+}
+
+
+const char *mfgpu_last_error(void) { return g_err.c_str(); }
+
+int mfgpu_version(void) { return 100; }
+
+mfgpu_status mfgpu_device_count(int *count)
+{
+    if (!count) return fail(MFGPU_EINVAL, "count is NULL");
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) n = 0;
+    *count = n;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_fft_sizes(int nb, int nx, int *fft_length, int *block_length)
+{
+    if (!fft_length || !block_length) return fail(MFGPU_EINVAL, "output is NULL");
+    return fft_sizes(nb, nx, fft_length, block_length);
+}
+
+// ---------------------------------------------------------------------------
+mfgpu_status mfgpu_mf_create(int precision, mfgpu_mf **out)
+{
+    if (!out) return fail(MFGPU_EINVAL, "mf is NULL");
+    if (precision != MFGPU_FLOAT32 && precision != MFGPU_FLOAT64)
+        return fail(MFGPU_EINVAL, "precision must be MFGPU_FLOAT32 or MFGPU_FLOAT64");
+    auto *mf = new mfgpu_mf();
+    mf->prec = precision;
+    cudaError_t e = cudaGetDevice(&mf->dev);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&mf->stream, cudaStreamNonBlocking);
+    for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreate(&mf->ev[i]);
+    if (e != cudaSuccess)
+    {
+        delete mf;
+        return cuda_fail(e, "mfgpu_mf_create");
+    }
+    *out = mf;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_destroy(mfgpu_mf *mf)
+{
+    if (!mf) return MFGPU_OK;
+    {
+        DeviceGuard g(mf->dev);
+        mf->reset();
+        for (auto &e : mf->ev)
+            if (e) cudaEventDestroy(e);
+        if (mf->stream) cudaStreamDestroy(mf->stream);
+    }
+    delete mf;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_clear(mfgpu_mf *mf)
+{
+    if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");
+    DeviceGuard g(mf->dev);
+    mf->reset();
+    return MFGPU_OK;
+}
+
+template <class T> static mfgpu_status mf_upload_tables(mfgpu_mf *mf)
+{
+    std::vector<cx<T>> tw;
+    fill_twiddles<T>(tw);
+    CU(mf->tw.ensure(sizeof(cx<T>) * tw.size()));
+    CU(cudaMemcpyAsync(mf->tw.p, tw.data(), sizeof(cx<T>) * tw.size(), cudaMemcpyHostToDevice, mf->stream));
+    SpecParams<T> sp;
+    sp.tmpl = mf->tmpl_d.as<double>();
+    sp.toff = mf->toff_d.as<long>();
+    sp.tlen = mf->tlen_d.as<int>();
+    sp.Bc = mf->Bc.as<cx<T>>();
+    sp.ldb = (1L << mf->log2p) + 2;
+    sp.tw = mf->tw.as<cx<T>>();
+    CU(launch_spectra<T>(mf->log2p, sp, mf->nt, mf->stream));
+    ++mf->launches;
+    return MFGPU_OK;
+}
+
+template <class T> static int plan_limit_lo() { return fft_limits<T>::lo; }
+template <class T> static int plan_limit_hi() { return fft_limits<T>::hi; }
+
+mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
+{
+    if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");
+    DeviceGuard g(mf->dev);
+    mf->reset();
+    if (!p) return fail(MFGPU_EINVAL, "Parameters are invalid: NULL");
+    if (p->n_templates < 1) return fail(MFGPU_EINVAL, "Parameters are invalid: no templates");
+    if (p->signal_size < 1) return fail(MFGPU_EINVAL, "Parameters are invalid: signal size not set");
+    if (!p->template_lengths || !p->templates) return fail(MFGPU_EINVAL, "Parameters are invalid: templates NULL");
+    if (p->detection_mode != MFGPU_SINGLE_CHANNEL && p->detection_mode != MFGPU_MULTI_CHANNEL)
+        return fail(MFGPU_EINVAL, "invalid detection mode");
+    const int nt = p->n_templates, n = p->signal_size;
+    int maxLen = 0, minLen = std::numeric_limits<int>::max();
+    for (int t = 0; t < nt; ++t)
+    {
+        if (p->template_lengths[t] < 1 || !p->templates[t])
+            return fail(MFGPU_EINVAL, "template " + std::to_string(t) + " has no signal");
+        maxLen = std::max(maxLen, p->template_lengths[t]);
+        minLen = std::min(minLen, p->template_lengths[t]);
+    }
+    // MatchedFilter::initialize sizes the reference's FFT from (maxLen, n+maxLen-1)
+    // and throws when the signal is not longer than that (src/matchedFilter.cpp:522-525).
+    int rn = 0, rl = 0;
+    mfgpu_status st = fft_sizes(maxLen, n + maxLen - 1, &rn, &rl);
+    if (st != MFGPU_OK) return st;
+
+    int nch;
+    std::vector<int> tchan(nt);
+    bool ref_layout = p->n_channels <= 0;
+    if (ref_layout)
+    {
+        nch = p->detection_mode == MFGPU_MULTI_CHANNEL ? nt : 1;
+        for (int t = 0; t < nt; ++t) tchan[t] = p->detection_mode == MFGPU_MULTI_CHANNEL ? t : 0;
+    }
+    else
+    {
+        if (!p->template_channel) return fail(MFGPU_EINVAL, "template_channel is NULL");
+        nch = p->n_channels;
+        for (int t = 0; t < nt; ++t)
+        {
+            if (p->template_channel[t] < 0 || p->template_channel[t] >= nch)
+                return fail(MFGPU_EINVAL, "template_channel[" + std::to_string(t) + "] out of range");
+            tchan[t] = p->template_channel[t];
+        }
+    }
+    if (nch > 65535 * 64) return fail(MFGPU_EINVAL, "too many channels");
+
+    mf->mode = p->detection_mode;
+    mf->nt = nt; mf->n = n; mf->maxLen = maxLen; mf->minLen = minLen; mf->nch = nch;
+    mf->ref_layout = ref_layout;
+    mf->tchan = tchan;
+    mf->lens.assign(p->template_lengths, p->template_lengths + nt);
+    mf->nvalid.resize(nt);
+    int maxvalid = 0;
+    for (int t = 0; t < nt; ++t)
+    {
+        mf->nvalid[t] = std::max(0, n - mf->lens[t] + 1);
+        maxvalid = std::max(maxvalid, mf->nvalid[t]);
+    }
+    mf->maxvalid = maxvalid;
+    mf->toff.resize(nt);
+    long tot = 0;
+    for (int t = 0; t < nt; ++t) { mf->toff[t] = tot; tot += mf->lens[t]; }
+    mf->tmpl.resize(tot);
+    for (int t = 0; t < nt; ++t)
+        std::memcpy(&mf->tmpl[mf->toff[t]], p->templates[t], sizeof(double) * mf->lens[t]);
+    mf->stack_abs = p->stack_absolute_values ? 1 : 0;
+    if (p->stack_shifts && p->stack_weights)
+    {
+        mf->can_stack = true;
+        mf->shifts.assign(p->stack_shifts, p->stack_shifts + nt);
+        mf->weights.assign(p->stack_weights, p->stack_weights + nt);
+    }
+
+    // ---- plan: FFT length (autotuned unless given), lags per block, groups
+    std::vector<int> per_chan(nch, 0);
+    for (int t = 0; t < nt; ++t) per_chan[tchan[t]]++;
+    int used_ch = 0, max_tpc = 0;
+    for (int c = 0; c < nch; ++c) if (per_chan[c]) { ++used_ch; max_tpc = std::max(max_tpc, per_chan[c]); }
+    const double tpc = (double) nt / std::max(1, used_ch);
+    const int lo = mf->prec == 4 ? plan_limit_lo<float>() : plan_limit_lo<double>();
+    const int hi = mf->prec == 4 ? plan_limit_hi<float>() : plan_limit_hi<double>();
+    bool all_equal = minLen == maxLen;
+    mf->shared_den = all_equal;
+    auto smem_of = [&](int l2p, int S) {
+        return mf->prec == 4 ? xcorr_smem_bytes<float>(l2p, all_equal, S)
+                             : xcorr_smem_bytes<double>(l2p, all_equal, S);
+    };
+    int dev_smem = 0;
+    CU(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, mf->dev));
+    int best_l2p = -1, best_S = 0;
+    double best_cost = 0;
+    for (int l2p = lo; l2p <= hi; ++l2p)
+    {
+        int N = 2 << l2p;
+        if (p->fft_length > 0 && p->fft_length != N) continue;
+        int S = ((N - maxLen + 1) / 32) * 32;
+        if (S < 32) continue;
+        if ((int) smem_of(l2p, S) > dev_smem) continue;
+        double nb = std::ceil((double) std::max(1, maxvalid) / S);
+        double cost = nb * N * (l2p + 1) * (1.0 + 1.15 * tpc);
+        if (best_l2p < 0 || cost < best_cost) { best_l2p = l2p; best_S = S; best_cost = cost; }
+    }
+    if (best_l2p < 0)
+    {
+        if (p->fft_length > 0)
+            return fail(MFGPU_EINVAL, "fft_length " + std::to_string(p->fft_length) +
+                                          " is not a supported power of two for templates of length " +
+                                          std::to_string(maxLen));
+        return fail(MFGPU_EINVAL, "template length " + std::to_string(maxLen) + " exceeds the supported maximum (" +
+                                      std::to_string((2 << hi) - 31) + ")");
+    }
+    mf->log2p = best_l2p;
+    mf->nfft = 2 << best_l2p;
+    mf->S = best_S;
+    mf->nblocks = (maxvalid + best_S - 1) / best_S;
+    mf->ldx = ((long) mf->nblocks * best_S + mf->nfft + 63) / 64 * 64;
+    mf->ldx = std::max<long>(mf->ldx, (n + 63) / 64 * 64);
+    mf->ldr = ((long) std::max(1, maxvalid) + 63) / 64 * 64;
+    // work groups: split each channel's templates so the grid has enough CTAs
+    int G = std::max(1, max_tpc);
+    auto count_groups = [&](int gsz) {
+        long ng = 0;
+        for (int c = 0; c < nch; ++c) ng += (per_chan[c] + gsz - 1) / gsz;
+        return ng;
+    };
+    while (G > 1 && ((long) mf->nblocks * count_groups(G) < 4L * 152 * 2 || count_groups(G) > 65535)) G = (G + 1) / 2;
+    if (count_groups(G) > 65535) return fail(MFGPU_EINVAL, "too many template groups");
+    std::vector<std::vector<int>> chan_t(nch);
+    for (int t = 0; t < nt; ++t) chan_t[tchan[t]].push_back(t);
+    std::vector<int> gch, gtb, gte, tids;
+    for (int c = 0; c < nch; ++c)
+    {
+        for (size_t i = 0; i < chan_t[c].size(); i += G)
+        {
+            gch.push_back(c);
+            gtb.push_back((int) tids.size());
+            for (size_t j = i; j < std::min(chan_t[c].size(), i + (size_t) G); ++j) tids.push_back(chan_t[c][j]);
+            gte.push_back((int) tids.size());
+        }
+    }
+    mf->ngroups = (int) gch.size();
+    mf->dead_chunks = (int) std::min<long>(1024, std::max<long>(1, (n + 65535) / 65536));
+
+    // ---- device memory
+    const size_t es = mf->esz();
+    const int P = 1 << mf->log2p;
+    CU(mf->x.ensure(es * (size_t) nch * mf->ldx));
+    CU(cudaMemsetAsync(mf->x.p, 0, mf->x.bytes, mf->stream));
+    CU(mf->rho.ensure(es * (size_t) nt * mf->ldr));
+    CU(cudaMemsetAsync(mf->rho.p, 0, mf->rho.bytes, mf->stream));
+    CU(mf->Bc.ensure(2 * es * (size_t) nt * (P + 2)));
+    CU(mf->grp_chan.ensure(sizeof(int) * gch.size()));
+    CU(mf->grp_tb.ensure(sizeof(int) * gch.size()));
+    CU(mf->grp_te.ensure(sizeof(int) * gch.size()));
+    CU(mf->tids.ensure(sizeof(int) * tids.size()));
+    CU(mf->tlen_d.ensure(sizeof(int) * nt));
+    CU(mf->nvalid_d.ensure(sizeof(int) * nt));
+    CU(mf->dead.ensure((size_t) nch));
+    CU(cudaMemsetAsync(mf->dead.p, 0, mf->dead.bytes, mf->stream));
+    CU(mf->err.ensure(sizeof(int)));
+    CU(cudaMemsetAsync(mf->err.p, 0, sizeof(int), mf->stream));
+    CU(mf->tmpl_d.ensure(sizeof(double) * (size_t) tot));
+    CU(mf->toff_d.ensure(sizeof(long) * nt));
+    CU(mf->pmin.ensure(es * (size_t) nch * mf->dead_chunks));
+    CU(mf->pmax.ensure(es * (size_t) nch * mf->dead_chunks));
+    CU(mf->chan_list.ensure(sizeof(int) * nch));
+    std::vector<int> all_ch(nch);
+    for (int c = 0; c < nch; ++c) all_ch[c] = c;
+    CU(cudaMemcpyAsync(mf->chan_list.p, all_ch.data(), sizeof(int) * nch, cudaMemcpyHostToDevice, mf->stream));
+    CU(cudaMemcpyAsync(mf->grp_chan.p, gch.data(), sizeof(int) * gch.size(), cudaMemcpyHostToDevice, mf->stream));
+    CU(cudaMemcpyAsync(mf->grp_tb.p, gtb.data(), sizeof(int) * gtb.size(), cudaMemcpyHostToDevice, mf->stream));
+    CU(cudaMemcpyAsync(mf->grp_te.p, gte.data(), sizeof(int) * gte.size(), cudaMemcpyHostToDevice, mf->stream));
+    CU(cudaMemcpyAsync(mf->tids.p, tids.data(), sizeof(int) * tids.size(), cudaMemcpyHostToDevice, mf->stream));
+    CU(cudaMemcpyAsync(mf->tlen_d.p, mf->lens.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, mf->stream));
+    CU(cudaMemcpyAsync(mf->nvalid_d.p, mf->nvalid.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, mf->stream));
+    CU(cudaMemcpyAsync(mf->tmpl_d.p, mf->tmpl.data(), sizeof(double) * tot, cudaMemcpyHostToDevice, mf->stream));
+    CU(cudaMemcpyAsync(mf->toff_d.p, mf->toff.data(), sizeof(long) * nt, cudaMemcpyHostToDevice, mf->stream));
+    mfgpu_status s2 = mf->prec == 4 ? mf_upload_tables<float>(mf) : mf_upload_tables<double>(mf);
+    if (s2 != MFGPU_OK) return s2;
+    CU(cudaStreamSynchronize(mf->stream));
+    CU(cudaGetLastError());
+    mf->initialized = true;
+    return MFGPU_OK;
+}
+
+#define MF_CHECK_INIT(mf)                                                                                          \
+    do                                                                                                             \
+    {                                                                                                              \
+        if (!(mf)) return fail(MFGPU_EINVAL, "mf is NULL");                                                        \
+        if (!(mf)->initialized) return fail(MFGPU_ESTATE, "Class not initialized");                                \
+    } while (0)
+
+mfgpu_status mfgpu_mf_is_initialized(const mfgpu_mf *mf, int *flag)
+{
+    if (!mf || !flag) return fail(MFGPU_EINVAL, "NULL argument");
+    *flag = mf->initialized ? 1 : 0;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_get_number_of_templates(const mfgpu_mf *mf, int *n)
+{
+    MF_CHECK_INIT(mf);
+    if (!n) return fail(MFGPU_EINVAL, "n is NULL");
+    *n = mf->nt;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_get_signal_length(const mfgpu_mf *mf, int *n)
+{
+    MF_CHECK_INIT(mf);
+    if (!n) return fail(MFGPU_EINVAL, "n is NULL");
+    *n = mf->n;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_get_filtered_signal_length(const mfgpu_mf *mf, int *n)
+{
+    MF_CHECK_INIT(mf);
+    if (!n) return fail(MFGPU_EINVAL, "n is NULL");
+    *n = mf->n - mf->maxLen + 1;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_get_plan(const mfgpu_mf *mf, int *fft_length, int *lags_per_block, int *n_blocks)
+{
+    MF_CHECK_INIT(mf);
+    if (fft_length) *fft_length = mf->nfft;
+    if (lags_per_block) *lags_per_block = mf->S;
+    if (n_blocks) *n_blocks = mf->nblocks;
+    return MFGPU_OK;
+}
+
+static mfgpu_status mf_channel_of(mfgpu_mf *mf, int it, int *c)
+{
+    if (it < 0 || it >= mf->nt)
+        return fail(MFGPU_EINVAL, "it = " + std::to_string(it) + " must be in the range [0," +
+                                      std::to_string(mf->nt - 1) + "]");
+    if (mf->ref_layout && mf->mode == MFGPU_SINGLE_CHANNEL && it != 0)
+        return fail(MFGPU_EINVAL, "single-channel mode has one signal: it must be 0");
+    *c = mf->tchan[it];
+    return MFGPU_OK;
+}
+
+static mfgpu_status mf_store_signal(mfgpu_mf *mf, int c, int n, const void *x, cudaMemcpyKind kind)
+{
+    if (n != mf->n)
+        return fail(MFGPU_EINVAL, "Number of samples = " + std::to_string(n) + " must equal" + std::to_string(mf->n));
+    if (!x) return fail(MFGPU_EINVAL, "x is NULL");
+    mf->have = false;
+    mf->have_peaks = false;
+    const size_t es = mf->esz();
+    char *row = mf->x.as<char>() + es * (size_t) c * mf->ldx;
+    CU(cudaMemcpyAsync(row, x, es * (size_t) n, kind, mf->stream));
+    unsigned char *dflag = mf->dead.as<unsigned char>() + c;
+    const size_t poff = (size_t) c * mf->dead_chunks;
+    if (mf->prec == 4)
+        CU(launch_dead<float>(reinterpret_cast<const float *>(row), mf->n, dflag, mf->pmin.as<float>() + poff,
+                              mf->pmax.as<float>() + poff, mf->dead_chunks, mf->stream));
+    else
+        CU(launch_dead<double>(reinterpret_cast<const double *>(row), mf->n, dflag, mf->pmin.as<double>() + poff,
+                               mf->pmax.as<double>() + poff, mf->dead_chunks, mf->stream));
+    mf->launches += 2;
+    // the reference copies the caller's samples before returning
+    CU(cudaStreamSynchronize(mf->stream));
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_set_signal(mfgpu_mf *mf, int it, int n, const void *x)
+{
+    MF_CHECK_INIT(mf);
+    DeviceGuard g(mf->dev);
+    int c;
+    mfgpu_status st = mf_channel_of(mf, it, &c);
+    if (st != MFGPU_OK) return st;
+    return mf_store_signal(mf, c, n, x, cudaMemcpyHostToDevice);
+}
+
+mfgpu_status mfgpu_mf_set_channel_signal(mfgpu_mf *mf, int channel, int n, const void *x)
+{
+    MF_CHECK_INIT(mf);
+    DeviceGuard g(mf->dev);
+    if (channel < 0 || channel >= mf->nch) return fail(MFGPU_EINVAL, "channel out of range");
+    return mf_store_signal(mf, channel, n, x, cudaMemcpyHostToDevice);
+}
+
+mfgpu_status mfgpu_mf_set_channel_signal_device(mfgpu_mf *mf, int channel, int n, const void *dx)
+{
+    MF_CHECK_INIT(mf);
+    DeviceGuard g(mf->dev);
+    if (channel < 0 || channel >= mf->nch) return fail(MFGPU_EINVAL, "channel out of range");
+    return mf_store_signal(mf, channel, n, dx, cudaMemcpyDeviceToDevice);
+}
+
+mfgpu_status mfgpu_mf_zero_signal(mfgpu_mf *mf, int it)
+{
+    MF_CHECK_INIT(mf);
+    DeviceGuard g(mf->dev);
+    int c;
+    mfgpu_status st = mf_channel_of(mf, it, &c);
+    if (st != MFGPU_OK) return st;
+    mf->have = false;
+    mf->have_peaks = false;
+    const size_t es = mf->esz();
+    CU(cudaMemsetAsync(mf->x.as<char>() + es * (size_t) c * mf->ldx, 0, es * (size_t) mf->n, mf->stream));
+    CU(cudaMemsetAsync(mf->dead.as<unsigned char>() + c, 1, 1, mf->stream));
+    CU(cudaStreamSynchronize(mf->stream));
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_get_signal(const mfgpu_mf *cmf, int it, int maxn, void *dst)
+{
+    auto *mf = const_cast<mfgpu_mf *>(cmf);
+    MF_CHECK_INIT(mf);
+    DeviceGuard g(mf->dev);
+    int c;
+    mfgpu_status st = mf_channel_of(mf, it, &c);
+    if (st != MFGPU_OK) return st;
+    if (!dst || maxn < mf->n) return fail(MFGPU_EINVAL, "destination too small");
+    const size_t es = mf->esz();
+    CU(cudaMemcpyAsync(dst, mf->x.as<char>() + es * (size_t) c * mf->ldx, es * (size_t) mf->n,
+                       cudaMemcpyDeviceToHost, mf->stream));
+    CU(cudaStreamSynchronize(mf->stream));
+    return MFGPU_OK;
+}
+
+template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
+{
+    XcorrParams<T> p;
+    p.x = mf->x.as<T>(); p.ldx = mf->ldx;
+    p.Bc = mf->Bc.as<cx<T>>(); p.ldb = (1L << mf->log2p) + 2;
+    p.rho = mf->rho.as<T>(); p.ldr = mf->ldr;
+    p.grp_chan = mf->grp_chan.as<int>(); p.grp_tb = mf->grp_tb.as<int>(); p.grp_te = mf->grp_te.as<int>();
+    p.tids = mf->tids.as<int>();
+    p.tlen = mf->tlen_d.as<int>(); p.nvalid = mf->nvalid_d.as<int>();
+    p.dead = mf->dead.as<unsigned char>();
+    p.tw = mf->tw.as<cx<T>>();
+    p.S = mf->S;
+    p.tol = sizeof(T) == 4 ? (T) 1.e-6 : (T) 1.e-12;  // src/matchedFilter.cpp:1287 / :1115
+    p.err = mf->err.as<int>();
+    CU(launch_xcorr<T>(mf->log2p, mf->shared_den, p, mf->nblocks, mf->ngroups, mf->stream));
+    ++mf->launches;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_apply(mfgpu_mf *mf)
+{
+    if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");
+    if (!mf->initialized) return fail(MFGPU_ESTATE, "Class is not initialized");
+    DeviceGuard g(mf->dev);
+    mf->have = false;
+    mf->have_peaks = false;
+    CU(cudaEventRecord(mf->ev[0], mf->stream));
+    CU(cudaEventRecord(mf->ev[1], mf->stream));
+    if (mf->nblocks > 0)
+    {
+        mfgpu_status st = mf->prec == 4 ? mf_launch_xcorr<float>(mf) : mf_launch_xcorr<double>(mf);
+        if (st != MFGPU_OK) return st;
+    }
+    CU(cudaEventRecord(mf->ev[2], mf->stream));
+    CU(cudaEventRecord(mf->ev[3], mf->stream));
+    mf->timed = true;
+    mf->have = true;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_synchronize(mfgpu_mf *mf)
+{
+    if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");
+    DeviceGuard g(mf->dev);
+    return mf_sync(mf);
+}
+
+mfgpu_status mfgpu_mf_have_matched_filtered_signals(const mfgpu_mf *mf, int *flag)
+{
+    if (!mf || !flag) return fail(MFGPU_EINVAL, "NULL argument");
+    *flag = mf->have ? 1 : 0;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_get_last_timings(mfgpu_mf *mf, float *xcorr_ms, float *apply_ms)
+{
+    if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");
+    DeviceGuard g(mf->dev);
+    mfgpu_status st = mf_sync(mf);
+    if (st != MFGPU_OK) return st;
+    if (xcorr_ms) *xcorr_ms = mf->last_xcorr_ms;
+    if (apply_ms) *apply_ms = mf->last_apply_ms;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_get_launch_count(const mfgpu_mf *mf, long long *count)
+{
+    if (!mf || !count) return fail(MFGPU_EINVAL, "NULL argument");
+    *count = mf->launches;
+    return MFGPU_OK;
+}
+
+static mfgpu_status mf_check_template(mfgpu_mf *mf, int it)
+{
+    if (it < 0 || it >= mf->nt)
+        return fail(MFGPU_EINVAL, "it = " + std::to_string(it) + " must be in the range [0," +
+                                      std::to_string(mf->nt - 1) + "]");
+    return MFGPU_OK;
+}
+
+static mfgpu_status mf_copy_rho(mfgpu_mf *mf, int it, int count, int maxn, void *dst, int *nout)
+{
+    if (!mf->have) return fail(MFGPU_ESTATE, "Matched filtering not yet applied");
+    mfgpu_status st = mf_check_template(mf, it);
+    if (st != MFGPU_OK) return st;
+    st = mf_sync(mf);
+    if (st != MFGPU_OK) return st;
+    count = std::max(0, count);
+    if (count > 0 && (!dst || maxn < count))
+        return fail(MFGPU_EINVAL, "maxn = " + std::to_string(maxn) + " must be at least " + std::to_string(count));
+    const size_t es = mf->esz();
+    if (count > 0)
+        CU(cudaMemcpy(dst, mf->rho.as<char>() + es * (size_t) it * mf->ldr, es * (size_t) count,
+                      cudaMemcpyDeviceToHost));
+    if (nout) *nout = count;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_get_matched_filtered_signal(mfgpu_mf *mf, int it, int maxn, void *dst, int *nout)
+{
+    MF_CHECK_INIT(mf);
+    DeviceGuard g(mf->dev);
+    return mf_copy_rho(mf, it, mf->n - mf->maxLen + 1, maxn, dst, nout);
+}
+
+mfgpu_status mfgpu_mf_get_valid_signal(mfgpu_mf *mf, int it, int maxn, void *dst, int *nout)
+{
+    MF_CHECK_INIT(mf);
+    DeviceGuard g(mf->dev);
+    mfgpu_status st = mf_check_template(mf, it);
+    if (st != MFGPU_OK) return st;
+    return mf_copy_rho(mf, it, mf->nvalid[it], maxn, dst, nout);
+}
+
+mfgpu_status mfgpu_mf_get_device_signal(mfgpu_mf *mf, int it, const void **dptr, int *nvalid)
+{
+    MF_CHECK_INIT(mf);
+    mfgpu_status st = mf_check_template(mf, it);
+    if (st != MFGPU_OK) return st;
+    if (!dptr) return fail(MFGPU_EINVAL, "dptr is NULL");
+    *dptr = mf->rho.as<char>() + mf->esz() * (size_t) it * mf->ldr;
+    if (nvalid) *nvalid = mf->nvalid[it];
+    return MFGPU_OK;
+}
+
+template <class T> static mfgpu_status mf_stack(mfgpu_mf *mf, int maxn, void *dst, int *nout)
+{
+    const int nfilt = mf->n - mf->maxLen + 1;
+    int smax = mf->shifts[0];
+    T xnorm = 0;
+    for (int t = 0; t < mf->nt; ++t)
+    {
+        smax = std::max(smax, mf->shifts[t]);
+        xnorm = xnorm + (T) mf->weights[t];
+    }
+    if (xnorm > 0) xnorm = 1 / xnorm;
+    const int outlen = nfilt - smax;
+    if (nout) *nout = std::max(0, outlen);
+    if (outlen <= 0) return MFGPU_OK;
+    if (!dst || maxn < outlen)
+        return fail(MFGPU_EINVAL, "maxn = " + std::to_string(maxn) + " must be at least " + std::to_string(outlen));
+    std::vector<T> w(mf->nt);
+    for (int t = 0; t < mf->nt; ++t) w[t] = xnorm * (T) mf->weights[t];
+    CU(mf->shifts_d.ensure(sizeof(int) * mf->nt));
+    CU(mf->weights_d.ensure(sizeof(T) * mf->nt));
+    CU(mf->stackbuf.ensure(sizeof(T) * (size_t) outlen));
+    CU(cudaMemcpyAsync(mf->shifts_d.p, mf->shifts.data(), sizeof(int) * mf->nt, cudaMemcpyHostToDevice, mf->stream));
+    CU(cudaMemcpyAsync(mf->weights_d.p, w.data(), sizeof(T) * mf->nt, cudaMemcpyHostToDevice, mf->stream));
+    CU(launch_stack<T>(mf->rho.as<T>(), mf->ldr, mf->nt, mf->shifts_d.as<int>(), mf->weights_d.as<T>(),
+                       mf->stack_abs, outlen, mf->stackbuf.as<T>(), mf->stream));
+    ++mf->launches;
+    CU(cudaMemcpyAsync(dst, mf->stackbuf.p, sizeof(T) * (size_t) outlen, cudaMemcpyDeviceToHost, mf->stream));
+    CU(cudaStreamSynchronize(mf->stream));
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_shift_and_stack(mfgpu_mf *mf, int maxn, void *dst, int *nout)
+{
+    MF_CHECK_INIT(mf);
+    DeviceGuard g(mf->dev);
+    if (!mf->have) return fail(MFGPU_ESTATE, "Matched filtered signals not yet computed");
+    if (!mf->can_stack) return fail(MFGPU_ESTATE, "Templates missing info - can't shift");
+    mfgpu_status st = mf_sync(mf);
+    if (st != MFGPU_OK) return st;
+    return mf->prec == 4 ? mf_stack<float>(mf, maxn, dst, nout) : mf_stack<double>(mf, maxn, dst, nout);
+}
+
+mfgpu_status mfgpu_mf_get_spectra_of_template(mfgpu_mf *mf, int it, int maxn, void *dst, int *nout)
+{
+    MF_CHECK_INIT(mf);
+    DeviceGuard g(mf->dev);
+    mfgpu_status st = mf_check_template(mf, it);
+    if (st != MFGPU_OK) return st;
+    int rn = 0, rl = 0;
+    st = fft_sizes(mf->maxLen, mf->n + mf->maxLen - 1, &rn, &rl);
+    if (st != MFGPU_OK) return st;
+    const int ns = rn / 2 + 1;
+    if (!dst || maxn < 2 * ns) return fail(MFGPU_EINVAL, "maxn must be at least 2*(nfft/2+1)");
+    const size_t es = mf->esz();
+    CU(mf->specbuf.ensure(es * 2 * (size_t) ns));
+    const double *tp = mf->tmpl_d.as<double>() + mf->toff[it];
+    if (mf->prec == 4) CU(launch_ref_spectrum<float>(tp, mf->lens[it], rn, mf->specbuf.as<float>(), mf->stream));
+    else CU(launch_ref_spectrum<double>(tp, mf->lens[it], rn, mf->specbuf.as<double>(), mf->stream));
+    ++mf->launches;
+    CU(cudaMemcpyAsync(dst, mf->specbuf.p, es * 2 * (size_t) ns, cudaMemcpyDeviceToHost, mf->stream));
+    CU(cudaStreamSynchronize(mf->stream));
+    if (nout) *nout = 2 * ns;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_find_peaks(mfgpu_mf *mf, double threshold, int min_distance, int trace_length)
+{
+    MF_CHECK_INIT(mf);
+    DeviceGuard g(mf->dev);
+    if (!mf->have) return fail(MFGPU_ESTATE, "Matched filtering not yet applied");
+    if (threshold < 0 || threshold > 1)
+        return fail(MFGPU_EINVAL, "Threshold = " + std::to_string(threshold) + " must be in the range [0,1]");
+    int len = trace_length > 0 ? trace_length : mf->n - mf->maxLen + 1;
+    if (len > mf->maxvalid) return fail(MFGPU_EINVAL, "trace_length exceeds the valid lags");
+    mfgpu_status st = mf_sync(mf);
+    if (st != MFGPU_OK) return st;
+    mf->have_peaks = false;
+    std::vector<int> rows(mf->nt);
+    for (int t = 0; t < mf->nt; ++t) rows[t] = t;
+    mf->pk_off.assign(mf->nt + 1, 0);
+    std::string err;
+    int rc = mf->prec == 4
+                 ? run_peaks<float>(mf->rho.as<float>(), mf->ldr, rows.data(), mf->nt, len, threshold, min_distance,
+                                    mf->pk, mf->stream, &mf->launches, mf->pk_off.data(), err)
+                 : run_peaks<double>(mf->rho.as<double>(), mf->ldr, rows.data(), mf->nt, len, threshold,
+                                     min_distance, mf->pk, mf->stream, &mf->launches, mf->pk_off.data(), err);
+    if (rc != 0) return fail(MFGPU_ECUDA, err);
+    mf->have_peaks = true;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_get_peaks(mfgpu_mf *mf, int it, int maxn, int *dst, int *nout)
+{
+    MF_CHECK_INIT(mf);
+    DeviceGuard g(mf->dev);
+    if (!mf->have_peaks) return fail(MFGPU_ESTATE, "peaks not computed");
+    mfgpu_status st = mf_check_template(mf, it);
+    if (st != MFGPU_OK) return st;
+    long long cnt = mf->pk_off[it + 1] - mf->pk_off[it];
+    if (cnt > 0 && (!dst || maxn < cnt)) return fail(MFGPU_EINVAL, "destination too small");
+    if (cnt > 0)
+        CU(cudaMemcpy(dst, mf->pk.peaks.as<int>() + mf->pk_off[it], sizeof(int) * (size_t) cnt,
+                      cudaMemcpyDeviceToHost));
+    if (nout) *nout = (int) cnt;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_get_all_peaks(mfgpu_mf *mf, int nt, int *counts, int max_total, int *indices, int *total)
+{
+    MF_CHECK_INIT(mf);
+    DeviceGuard g(mf->dev);
+    if (!mf->have_peaks) return fail(MFGPU_ESTATE, "peaks not computed");
+    if (nt != mf->nt || !counts) return fail(MFGPU_EINVAL, "counts must hold one entry per template");
+    long long tot = mf->pk_off[mf->nt];
+    if (total) *total = (int) tot;
+    for (int t = 0; t < mf->nt; ++t) counts[t] = (int) (mf->pk_off[t + 1] - mf->pk_off[t]);
+    if (tot > 0)
+    {
+        if (!indices || max_total < tot) return fail(MFGPU_EINVAL, "indices too small");
+        CU(cudaMemcpy(indices, mf->pk.peaks.p, sizeof(int) * (size_t) tot, cudaMemcpyDeviceToHost));
+    }
+    return MFGPU_OK;
+}
+
+
+// ============================================================================
+struct mfgpu_peaks
+{
+    int prec = 4;
+    int dev = 0;
+    cudaStream_t stream = nullptr;
+    double thr = 0.7;  // DEFAULT_THRESH, src/peakFinder.cpp:24
+    int dist = 0;      // src/peakFinder.cpp:167
+    int n = 0;
+    DevBuf x;
+    PeakWS ws;
+    std::vector<int> peaks;
+    int npeaks = 0;
+    long long launches = 0;
+};
+
+
+mfgpu_status mfgpu_peaks_create(int precision, mfgpu_peaks **out)
+{
+    if (!out) return fail(MFGPU_EINVAL, "pf is NULL");
+    if (precision != MFGPU_FLOAT32 && precision != MFGPU_FLOAT64)
+        return fail(MFGPU_EINVAL, "precision must be MFGPU_FLOAT32 or MFGPU_FLOAT64");
+    auto *pf = new mfgpu_peaks();
+    pf->prec = precision;
+    cudaError_t e = cudaGetDevice(&pf->dev);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&pf->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess)
+    {
+        delete pf;
+        return cuda_fail(e, "mfgpu_peaks_create");
+    }
+    *out = pf;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_peaks_destroy(mfgpu_peaks *pf)
+{
+    if (!pf) return MFGPU_OK;
+    {
+        DeviceGuard g(pf->dev);
+        cudaStreamSynchronize(pf->stream);
+        pf->x.release();
+        pf->ws.release();
+        cudaStreamDestroy(pf->stream);
+    }
+    delete pf;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_peaks_clear(mfgpu_peaks *pf)
+{
+    if (!pf) return fail(MFGPU_EINVAL, "pf is NULL");
+    DeviceGuard g(pf->dev);
+    cudaStreamSynchronize(pf->stream);
+    pf->x.release();
+    pf->ws.release();
+    pf->thr = 0.7;
+    pf->dist = 0;
+    pf->n = 0;
+    pf->npeaks = 0;
+    pf->peaks.clear();
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_peaks_set_threshold(mfgpu_peaks *pf, double threshold)
+{
+    if (!pf) return fail(MFGPU_EINVAL, "pf is NULL");
+    pf->npeaks = 0;
+    if (threshold < 0 || threshold > 1)
+        return fail(MFGPU_EINVAL, "Threshold = " + std::to_string(threshold) + " must be in the range [0,1]");
+    pf->thr = threshold;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_peaks_get_threshold(const mfgpu_peaks *pf, double *threshold)
+{
+    if (!pf || !threshold) return fail(MFGPU_EINVAL, "NULL argument");
+    *threshold = pf->thr;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_peaks_set_minimum_peak_distance(mfgpu_peaks *pf, int min_distance)
+{
+    if (!pf) return fail(MFGPU_EINVAL, "pf is NULL");
+    pf->npeaks = 0;
+    pf->dist = min_distance;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_peaks_get_minimum_peak_distance(const mfgpu_peaks *pf, int *min_distance)
+{
+    if (!pf || !min_distance) return fail(MFGPU_EINVAL, "NULL argument");
+    *min_distance = pf->dist;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_peaks_set_signal(mfgpu_peaks *pf, int n, const void *x)
+{
+    if (!pf) return fail(MFGPU_EINVAL, "pf is NULL");
+    pf->npeaks = 0;
+    if (n < 1) return fail(MFGPU_EINVAL, "No points in x");
+    if (!x) return fail(MFGPU_EINVAL, "x is NULL");
+    DeviceGuard g(pf->dev);
+    CU(pf->x.ensure((size_t) pf->prec * n));
+    CU(cudaMemcpyAsync(pf->x.p, x, (size_t) pf->prec * n, cudaMemcpyHostToDevice, pf->stream));
+    CU(cudaStreamSynchronize(pf->stream));
+    pf->n = n;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_peaks_apply(mfgpu_peaks *pf)
+{
+    if (!pf) return fail(MFGPU_EINVAL, "pf is NULL");
+    DeviceGuard g(pf->dev);
+    pf->npeaks = 0;
+    pf->peaks.clear();
+    if (pf->n < 1) return MFGPU_OK;
+    int row = 0;
+    long long off[2] = {0, 0};
+    std::string err;
+    int rc = pf->prec == 4 ? run_peaks<float>(pf->x.as<float>(), 0, &row, 1, pf->n, pf->thr, pf->dist, pf->ws,
+                                              pf->stream, &pf->launches, off, err)
+                           : run_peaks<double>(pf->x.as<double>(), 0, &row, 1, pf->n, pf->thr, pf->dist, pf->ws,
+                                               pf->stream, &pf->launches, off, err);
+    if (rc != 0) return fail(MFGPU_ECUDA, err);
+    pf->npeaks = (int) (off[1] - off[0]);
+    pf->peaks.resize(pf->npeaks);
+    if (pf->npeaks > 0)
+        CU(cudaMemcpy(pf->peaks.data(), pf->ws.peaks.p, sizeof(int) * pf->npeaks, cudaMemcpyDeviceToHost));
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_peaks_get_number_of_peaks(const mfgpu_peaks *pf, int *n)
+{
+    if (!pf || !n) return fail(MFGPU_EINVAL, "NULL argument");
+    *n = pf->npeaks;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_peaks_get_peak_indices(const mfgpu_peaks *pf, int maxn, int *dst)
+{
+    if (!pf) return fail(MFGPU_EINVAL, "pf is NULL");
+    if (maxn < pf->npeaks)
+        return fail(MFGPU_EINVAL, "maxx = " + std::to_string(maxn) + " must be at least = " +
+                                      std::to_string(pf->npeaks));
+    if (!dst) return fail(MFGPU_EINVAL, "peaks is NULL");
+    if (pf->npeaks > 0) std::memcpy(dst, pf->peaks.data(), sizeof(int) * pf->npeaks);
+    return MFGPU_OK;
+}
+
+
+// ============================================================================
+struct mfgpu_dbscan
+{
+    int dev = 0;
+    cudaStream_t stream = nullptr;
+    double eps = 3;     // src/dbscan.cpp:56
+    int min_obs = 5;    // src/dbscan.cpp:58
+    bool init = false, have_data = false, have_labels = false, have_weights = false;
+    int nobs = 0, nf = 0, ncl = 0;
+    std::vector<double> X, w;
+    std::vector<int> labels;
+    DbWS ws;
+    long long launches = 0;
+};
+
+
+mfgpu_status mfgpu_dbscan_create(mfgpu_dbscan **out)
+{
+    if (!out) return fail(MFGPU_EINVAL, "db is NULL");
+    auto *db = new mfgpu_dbscan();
+    cudaError_t e = cudaGetDevice(&db->dev);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&db->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess)
+    {
+        delete db;
+        return cuda_fail(e, "mfgpu_dbscan_create");
+    }
+    *out = db;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_dbscan_destroy(mfgpu_dbscan *db)
+{
+    if (!db) return MFGPU_OK;
+    {
+        DeviceGuard g(db->dev);
+        cudaStreamSynchronize(db->stream);
+        db->ws.release();
+        cudaStreamDestroy(db->stream);
+    }
+    delete db;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_dbscan_clear(mfgpu_dbscan *db)
+{
+    if (!db) return fail(MFGPU_EINVAL, "db is NULL");
+    db->eps = 3;
+    db->min_obs = 5;
+    db->init = db->have_data = db->have_labels = db->have_weights = false;
+    db->nobs = db->nf = db->ncl = 0;
+    db->X.clear(); db->w.clear(); db->labels.clear();
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_dbscan_initialize(mfgpu_dbscan *db, double epsilon, int min_observations)
+{
+    if (!db) return fail(MFGPU_EINVAL, "db is NULL");
+    mfgpu_dbscan_clear(db);
+    if (epsilon < 0) return fail(MFGPU_EINVAL, "epsilon = " + std::to_string(epsilon) + " must be non-negative");
+    if (min_observations < 1)
+        return fail(MFGPU_EINVAL, "minObservations = " + std::to_string(min_observations) + " must be positive");
+    db->eps = epsilon;
+    db->min_obs = min_observations;
+    db->init = true;
+    return MFGPU_OK;
+}
+
+static mfgpu_status db_set(mfgpu_dbscan *db, int n_obs, int n_features, const double *X, const double *w)
+{
+    if (!db) return fail(MFGPU_EINVAL, "db is NULL");
+    db->have_data = db->have_labels = db->have_weights = false;
+    if (!db->init) return fail(MFGPU_ESTATE, "Class not initialized");
+    if (n_obs < 1) return fail(MFGPU_EINVAL, "No observations");
+    if (n_features < 1) return fail(MFGPU_EINVAL, "No features");
+    if (!X) return fail(MFGPU_EINVAL, "X is NULL");
+    if (w)
+    {
+        double mn = *std::min_element(w, w + n_obs);
+        if (!(mn > 0)) return fail(MFGPU_EINVAL, "All weights must be positive");
+    }
+    db->X.assign(X, X + (size_t) n_obs * n_features);
+    if (w) db->w.assign(w, w + n_obs);
+    else db->w.clear();
+    db->nobs = n_obs;
+    db->nf = n_features;
+    db->have_weights = w != nullptr;
+    db->have_data = true;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_dbscan_set_data(mfgpu_dbscan *db, int n_obs, int n_features, const double *X)
+{
+    return db_set(db, n_obs, n_features, X, nullptr);
+}
+
+mfgpu_status mfgpu_dbscan_set_weighted_data(mfgpu_dbscan *db, int n_obs, int n_features, const double *X,
+                                            const double *weights)
+{
+    return db_set(db, n_obs, n_features, X, weights);
+}
+
+mfgpu_status mfgpu_dbscan_cluster(mfgpu_dbscan *db)
+{
+    if (!db) return fail(MFGPU_EINVAL, "db is NULL");
+    db->have_labels = false;
+    db->labels.clear();
+    if (!db->init) return fail(MFGPU_ESTATE, "Class not initialized");
+    if (!db->have_data) return fail(MFGPU_ESTATE, "Data not yet set");
+    DeviceGuard g(db->dev);
+    int seg[2] = {0, db->nobs};
+    db->labels.resize(db->nobs);
+    std::string err;
+    int rc = run_dbscan(db->nobs, db->nf, db->X.data(), db->have_weights ? db->w.data() : nullptr, db->eps,
+                        db->min_obs, 1, seg, db->labels.data(), &db->ncl, db->ws, db->stream, &db->launches, err);
+    if (rc != 0) return fail(MFGPU_ECUDA, err);
+    db->have_labels = true;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_dbscan_get_number_of_clusters(const mfgpu_dbscan *db, int *n)
+{
+    if (!db || !n) return fail(MFGPU_EINVAL, "NULL argument");
+    *n = db->ncl;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_dbscan_get_labels(const mfgpu_dbscan *db, int maxn, int *labels)
+{
+    if (!db) return fail(MFGPU_EINVAL, "db is NULL");
+    if (!db->have_labels) return fail(MFGPU_ESTATE, "clustering not yet done");
+    if (!labels || maxn < (int) db->labels.size()) return fail(MFGPU_EINVAL, "labels too small");
+    std::memcpy(labels, db->labels.data(), sizeof(int) * db->labels.size());
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_dbscan_get_launch_count(const mfgpu_dbscan *db, long long *count)
+{
+    if (!db || !count) return fail(MFGPU_EINVAL, "NULL argument");
+    *count = db->launches;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_dbscan_is_initialized(const mfgpu_dbscan *db, int *flag)
+{
+    if (!db || !flag) return fail(MFGPU_EINVAL, "NULL argument");
+    *flag = db->init;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_dbscan_have_data(const mfgpu_dbscan *db, int *flag)
+{
+    if (!db || !flag) return fail(MFGPU_EINVAL, "NULL argument");
+    *flag = db->have_data;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_dbscan_have_labels(const mfgpu_dbscan *db, int *flag)
+{
+    if (!db || !flag) return fail(MFGPU_EINVAL, "NULL argument");
+    *flag = db->have_labels;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_dbscan_segmented(mfgpu_dbscan *db, int n_segments, const int *seg_offsets, int n_features,
+                                    const double *X, const double *weights, int *labels, int *n_clusters)
+{
+    if (!db) return fail(MFGPU_EINVAL, "db is NULL");
+    if (!db->init) return fail(MFGPU_ESTATE, "Class not initialized");
+    if (n_segments < 1 || !seg_offsets || !labels || !n_clusters) return fail(MFGPU_EINVAL, "NULL argument");
+    if (n_features < 1) return fail(MFGPU_EINVAL, "No features");
+    if (seg_offsets[0] != 0) return fail(MFGPU_EINVAL, "seg_offsets[0] must be 0");
+    for (int s = 0; s < n_segments; ++s)
+        if (seg_offsets[s + 1] < seg_offsets[s]) return fail(MFGPU_EINVAL, "seg_offsets must be non-decreasing");
+    const int n = seg_offsets[n_segments];
+    if (n > 0 && !X) return fail(MFGPU_EINVAL, "X is NULL");
+    if (weights && n > 0)
+    {
+        double mn = *std::min_element(weights, weights + n);
+        if (!(mn > 0)) return fail(MFGPU_EINVAL, "All weights must be positive");
+    }
+    DeviceGuard g(db->dev);
+    std::string err;
+    int rc = run_dbscan(n, n_features, X, weights, db->eps, db->min_obs, n_segments, seg_offsets, labels,
+                        n_clusters, db->ws, db->stream, &db->launches, err);
+    if (rc != 0) return fail(MFGPU_ECUDA, err);
+    return MFGPU_OK;
+}
+

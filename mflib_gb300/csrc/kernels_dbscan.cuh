@@ -1,0 +1,136 @@
+// kernels_dbscan.cuh -- DBSCAN (MFLib::DBSCAN::cluster, src/dbscan.cpp:187-214,
+// which calls Intel DAAL dbscan::Batch<double>) on the device, for one or
+// many independent segments.
+//
+// Semantics (DAAL's published algorithm):
+//   N(i) = { j in segment(i) : ||x_i - x_j||_2 <= eps } including i;
+//   core(i) iff sum_{j in N(i)} w_j >= minObservations (w = 1 unweighted);
+//   clusters are the connected components of core points under the
+//   eps-neighbour relation; DAAL visits observations in index order and
+//   opens a new cluster at the first unassigned core point, so cluster ids
+//   are ordered by each component's lowest core index;
+//   a non-core point with a core neighbour takes the smallest id among its
+//   neighbours' clusters (the first cluster to reach it); others are -1.
+//
+// Device formulation: weighted neighbour sums, union-find with atomic CAS
+// that always hooks the larger root under the smaller (so every component's
+// root is its lowest core index), exclusive scan of root flags for the ids,
+// then labels.
+#pragma once
+#include <cstdint>
+#include "kernels_util.cuh"
+
+namespace mfgpu {
+
+constexpr int kDbThreads = 256;
+
+struct DbParams
+{
+    const double *X;        // [n x nf] row-major
+    int nf;
+    const double *w;        // weights or null
+    double eps;
+    double min_obs;
+    const int *seg_of;      // segment of each point
+    const int *seg_off;     // [nseg + 1]
+    int n;
+};
+
+__device__ __forceinline__ bool db_near(const DbParams &p, int i, int j)
+{
+    const double *a = p.X + (long) i * p.nf, *b = p.X + (long) j * p.nf;
+    double s = 0;
+    for (int f = 0; f < p.nf; ++f)
+    {
+        double d = a[f] - b[f];
+        s = fma(d, d, s);
+    }
+    return sqrt(s) <= p.eps;
+}
+
+static __global__ void __launch_bounds__(kDbThreads) db_core_kernel(DbParams p, unsigned char *core, int *parent)
+{
+    int i = blockIdx.x * kDbThreads + threadIdx.x;
+    if (i >= p.n) return;
+    int s = p.seg_of[i];
+    int jb = p.seg_off[s], je = p.seg_off[s + 1];
+    double acc = 0;
+    for (int j = jb; j < je; ++j)
+        if (db_near(p, i, j)) acc += p.w ? p.w[j] : 1.0;
+    core[i] = acc >= p.min_obs ? 1 : 0;
+    parent[i] = i;
+}
+
+__device__ __forceinline__ int db_find(volatile int *parent, int x)
+{
+    int p = parent[x];
+    while (p != x)
+    {
+        x = p;
+        p = parent[x];
+    }
+    return x;
+}
+
+static __global__ void __launch_bounds__(kDbThreads) db_union_kernel(DbParams p, const unsigned char *core, int *parent)
+{
+    int i = blockIdx.x * kDbThreads + threadIdx.x;
+    if (i >= p.n || !core[i]) return;
+    int s = p.seg_of[i];
+    int je = p.seg_off[s + 1];
+    volatile int *vp = parent;
+    for (int j = i + 1; j < je; ++j)
+    {
+        if (!core[j] || !db_near(p, i, j)) continue;
+        int a = i, b = j;
+        for (int guard = 0; guard < (1 << 30); ++guard)
+        {
+            a = db_find(vp, a);
+            b = db_find(vp, b);
+            if (a == b) break;
+            if (a > b) { int t = a; a = b; b = t; }
+            int old = atomicCAS(parent + b, b, a);  // hook larger root under smaller
+            if (old == b) break;
+            b = old;
+        }
+    }
+}
+
+static __global__ void db_roots_kernel(int n, const unsigned char *core, int *parent, int *is_root)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (!core[i]) { is_root[i] = 0; return; }
+    int r = db_find(parent, i);
+    parent[i] = r;
+    is_root[i] = r == i ? 1 : 0;
+}
+
+// labels: core -> id of its root; border -> smallest id among core neighbours
+static __global__ void __launch_bounds__(kDbThreads) db_label_kernel(DbParams p, const unsigned char *core, const int *root,
+                                                             const long long *root_pos, int *labels)
+{
+    int i = blockIdx.x * kDbThreads + threadIdx.x;
+    if (i >= p.n) return;
+    int s = p.seg_of[i];
+    int jb = p.seg_off[s], je = p.seg_off[s + 1];
+    long long base = root_pos[jb];
+    if (core[i]) { labels[i] = (int) (root_pos[root[i]] - base); return; }
+    long long best = -1;
+    for (int j = jb; j < je; ++j)
+    {
+        if (!core[j] || !db_near(p, i, j)) continue;
+        long long id = root_pos[root[j]] - base;
+        if (best < 0 || id < best) best = id;
+    }
+    labels[i] = (int) best;
+}
+
+static __global__ void db_count_kernel(int nseg, const int *seg_off, const long long *root_pos, int *n_clusters)
+{
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nseg) return;
+    n_clusters[s] = (int) (root_pos[seg_off[s + 1]] - root_pos[seg_off[s]]);
+}
+
+}  // namespace mfgpu

@@ -1,0 +1,215 @@
+// kernels_peaks.cuh -- peak finder (PeakFinder<T>::apply, src/peakFinder.cpp:329-446)
+// over many traces at once.
+//
+// Candidates follow the reference's sign-of-difference rules
+// (:345-381): i = 0 if sign(x[1]-x[0]) < 0; 0 < i < n-1 if
+// sign(x[i]-x[i-1]) >= 0 and sign(x[i+1]-x[i]) < 0 (right end of a
+// plateau); i = n-1 if sign(x[n-1]-x[n-2]) > 0; always x[i] > threshold.
+//
+// Minimum-separation pruning (:396-433) is a greedy pass in value order.
+// Here it runs as rounds over all traces in parallel: an undecided
+// candidate is accepted when no undecided candidate within min_distance
+// has a higher priority (value descending, then index ascending), and the
+// undecided candidates within min_distance of an accepted one are
+// rejected.  By induction on priority this accepts exactly the candidates
+// the sequential greedy pass accepts under the same total order.
+#pragma once
+#include <cstdint>
+#include "kernels_util.cuh"
+
+namespace mfgpu {
+
+constexpr int kPkThreads = 256;
+constexpr int kPkPer = 16;                          // lags per thread
+constexpr int kPkChunk = kPkThreads * kPkPer;       // lags per CTA
+constexpr int kPkCap = 32;                          // slot capacity per chunk
+
+template <class T> struct PeakTraces
+{
+    const T *x;       // trace i starts at x + row[i] * ldx
+    long ldx;
+    const int *row;   // row of each trace
+    int len;          // lags per trace
+    T thr;
+};
+
+template <class T> __device__ __forceinline__ int sgn(T d) { return d > (T) 0 ? 1 : (d < (T) 0 ? -1 : 0); }
+
+template <class T> __device__ __forceinline__ bool is_candidate(const T *x, int i, int n, T thr)
+{
+    if (i >= n) return false;
+    T xi = x[i];
+    if (!(xi > thr)) return false;
+    if (n == 1) return xi > (T) 0;  // reference reads x[1] out of bounds; 0 assumed
+    if (i == 0) return sgn<T>(x[1] - x[0]) < 0;
+    if (i == n - 1) return sgn<T>(x[n - 1] - x[n - 2]) > 0;
+    return sgn<T>(xi - x[i - 1]) >= 0 && sgn<T>(x[i + 1] - xi) < 0;
+}
+
+// Phase 1: find candidates of one chunk; write up to kPkCap of them into the
+// chunk's slot, and the exact count.
+template <class T>
+static __global__ void __launch_bounds__(kPkThreads) peak_cand_kernel(PeakTraces<T> tr, int nchunks, int *counts,
+                                                               int *slot_idx, T *slot_val)
+{
+    __shared__ long long sh[32];
+    const int trace = blockIdx.y, chunk = blockIdx.x;
+    const T *x = tr.x + (long) tr.row[trace] * tr.ldx;
+    const int n = tr.len;
+    const int i0 = chunk * kPkChunk + threadIdx.x * kPkPer;
+    unsigned mask = 0;
+#pragma unroll
+    for (int q = 0; q < kPkPer; ++q)
+        if (is_candidate<T>(x, i0 + q, n, tr.thr)) mask |= 1u << q;
+    long long tot;
+    long long r = block_excl_scan((long long) __popc(mask), sh, &tot);
+    const long slot = (long) trace * nchunks + chunk;
+    while (mask)
+    {
+        int q = __ffs(mask) - 1;
+        mask &= mask - 1;
+        if (r < kPkCap)
+        {
+            slot_idx[slot * kPkCap + r] = i0 + q;
+            slot_val[slot * kPkCap + r] = x[i0 + q];
+        }
+        ++r;
+    }
+    if (threadIdx.x == 0) counts[slot] = (int) tot;
+}
+
+// Phase 3: gather the slots (or re-scan overflowed chunks) into the packed,
+// index-ordered candidate arrays.
+template <class T>
+static __global__ void __launch_bounds__(kPkThreads) peak_gather_kernel(PeakTraces<T> tr, int nchunks, const int *counts,
+                                                                 const long long *offs, const int *slot_idx,
+                                                                 const T *slot_val, int *cidx, T *cval, int *ctr)
+{
+    __shared__ long long sh[32];
+    const int trace = blockIdx.y, chunk = blockIdx.x;
+    const long slot = (long) trace * nchunks + chunk;
+    const int cnt = counts[slot];
+    const long long off = offs[slot];
+    if (cnt == 0) return;
+    if (cnt <= kPkCap)
+    {
+        for (int r = threadIdx.x; r < cnt; r += kPkThreads)
+        {
+            cidx[off + r] = slot_idx[slot * kPkCap + r];
+            cval[off + r] = slot_val[slot * kPkCap + r];
+            ctr[off + r] = trace;
+        }
+        return;
+    }
+    const T *x = tr.x + (long) tr.row[trace] * tr.ldx;
+    const int n = tr.len;
+    const int i0 = chunk * kPkChunk + threadIdx.x * kPkPer;
+    unsigned mask = 0;
+#pragma unroll
+    for (int q = 0; q < kPkPer; ++q)
+        if (is_candidate<T>(x, i0 + q, n, tr.thr)) mask |= 1u << q;
+    long long tot;
+    long long r = block_excl_scan((long long) __popc(mask), sh, &tot);
+    while (mask)
+    {
+        int q = __ffs(mask) - 1;
+        mask &= mask - 1;
+        cidx[off + r] = i0 + q;
+        cval[off + r] = x[i0 + q];
+        ctr[off + r] = trace;
+        ++r;
+    }
+}
+
+// candidate states
+enum : unsigned char { PK_UNDECIDED = 0, PK_ACCEPTED = 1, PK_NEW = 2, PK_REJECTED = 3 };
+
+template <class T> __device__ __forceinline__ bool higher(T vj, int ij, T vg, int ig)
+{
+    return vj > vg || (vj == vg && ij < ig);
+}
+
+// Round step 1: accept undecided candidates that have no undecided
+// higher-priority neighbour within dist.  PK_NEW counts as undecided for
+// the neighbours' tests, so the outcome does not depend on timing.
+template <class T>
+static __global__ void __launch_bounds__(kPkThreads) peak_decide_kernel(long long ncand, const int *cidx, const T *cval,
+                                                                 const int *ctr, const long long *trace_beg,
+                                                                 unsigned char *state, int dist, int *n_undecided)
+{
+    long long g = (long long) blockIdx.x * kPkThreads + threadIdx.x;
+    if (g >= ncand) return;
+    if (state[g] != PK_UNDECIDED) return;
+    const int t = ctr[g];
+    const long long tb = trace_beg[t], te = trace_beg[t + 1];
+    const int ig = cidx[g];
+    const T vg = cval[g];
+    bool best = true;
+    for (long long j = g - 1; j >= tb && ig - cidx[j] <= dist; --j)
+    {
+        unsigned char s = state[j];
+        if ((s == PK_UNDECIDED || s == PK_NEW) && higher<T>(cval[j], cidx[j], vg, ig)) { best = false; break; }
+    }
+    if (best)
+        for (long long j = g + 1; j < te && cidx[j] - ig <= dist; ++j)
+        {
+            unsigned char s = state[j];
+            if ((s == PK_UNDECIDED || s == PK_NEW) && higher<T>(cval[j], cidx[j], vg, ig)) { best = false; break; }
+        }
+    if (best) state[g] = PK_NEW;
+    else atomicAdd(n_undecided, 1);
+}
+
+// Round step 2: newly accepted candidates reject their undecided neighbours.
+template <class T>
+static __global__ void __launch_bounds__(kPkThreads) peak_suppress_kernel(long long ncand, const int *cidx, const int *ctr,
+                                                                   const long long *trace_beg, unsigned char *state,
+                                                                   int dist)
+{
+    long long g = (long long) blockIdx.x * kPkThreads + threadIdx.x;
+    if (g >= ncand) return;
+    if (state[g] != PK_NEW) return;
+    const int t = ctr[g];
+    const long long tb = trace_beg[t], te = trace_beg[t + 1];
+    const int ig = cidx[g];
+    for (long long j = g - 1; j >= tb && ig - cidx[j] <= dist; --j)
+        if (state[j] == PK_UNDECIDED) state[j] = PK_REJECTED;
+    for (long long j = g + 1; j < te && cidx[j] - ig <= dist; ++j)
+        if (state[j] == PK_UNDECIDED) state[j] = PK_REJECTED;
+    state[g] = PK_ACCEPTED;
+}
+
+// accepted flag (as int) for the final compaction
+static __global__ void peak_flags_kernel(long long ncand, const unsigned char *state, int all, int *flags)
+{
+    long long g = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ncand) return;
+    flags[g] = (all || state[g] == PK_ACCEPTED) ? 1 : 0;
+}
+
+static __global__ void peak_compact_kernel(long long ncand, const int *flags, const long long *pos, const int *cidx,
+                                    int *peaks)
+{
+    long long g = (long long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ncand) return;
+    if (flags[g]) peaks[pos[g]] = cidx[g];
+}
+
+// per-trace peak offsets: peak_off[t] = pos[trace_beg[t]]
+static __global__ void peak_trace_offsets_kernel(int ntr, const long long *trace_beg, const long long *pos,
+                                          long long *peak_off)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t > ntr) return;
+    peak_off[t] = pos[trace_beg[t]];
+}
+
+// trace_beg[t] = offs[t * nchunks] (candidate offsets of each trace)
+static __global__ void peak_trace_beg_kernel(int ntr, int nchunks, const long long *offs, long long *trace_beg)
+{
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t > ntr) return;
+    trace_beg[t] = offs[(long) t * nchunks];
+}
+
+}  // namespace mfgpu

@@ -1,0 +1,103 @@
+// launch.h -- host-side launchers for the device kernels (one definition per
+// sample type lives in mf_f32.cu / mf_f64.cu; peaks and DBSCAN in
+// peaks_dbscan.cu).  Used by the C ABI in api.cu.
+#pragma once
+#include <cstddef>
+#include <string>
+#include <cuda_runtime.h>
+#include "kernels_mf.cuh"
+#include "kernels_util.cuh"
+
+namespace mfgpu {
+
+// Largest supported twiddle table / FFT length.
+constexpr int kNMax = 16384;
+
+// Supported range of log2(N/2) for the overlap-save correlator.
+template <class T> struct fft_limits;
+template <> struct fft_limits<float> { static constexpr int lo = 5, hi = 12; };   // N = 64 .. 8192
+template <> struct fft_limits<double> { static constexpr int lo = 5, hi = 11; };  // N = 64 .. 4096
+
+template <class T> size_t xcorr_smem_bytes(int log2p, bool shared_den, int S);
+template <class T> cudaError_t launch_xcorr(int log2p, bool shared_den, const XcorrParams<T> &p, int nblocks,
+                                            int ngroups, cudaStream_t s);
+template <class T> cudaError_t launch_spectra(int log2p, const SpecParams<T> &p, int nt, cudaStream_t s);
+// dead-trace flag of one channel (row of n samples): two launches;
+// pmin/pmax are scratch of nchunks entries each
+template <class T> cudaError_t launch_dead(const T *x_row, long n, unsigned char *dead, T *pmin, T *pmax,
+                                           int nchunks, cudaStream_t s);
+// reference debug spectrum of one prepared template at FFT length nfft
+template <class T> cudaError_t launch_ref_spectrum(const double *tmpl, int L, int nfft, T *out, cudaStream_t s);
+// shift and stack (src/matchedFilter.cpp:1319-1364)
+template <class T> cudaError_t launch_stack(const T *rho, long ldr, int nt, const int *shifts, const T *weights,
+                                            int stack_abs, int outlen, T *out, cudaStream_t s);
+
+// ---------------------------------------------------------------------------
+// grow-only device buffer
+struct DevBuf
+{
+    void *p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t need)
+    {
+        if (p && need <= bytes) return cudaSuccess;
+        release();
+        size_t b = (need < 64 ? 64 : need);
+        b += b / 4;
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e == cudaSuccess) bytes = b;
+        else p = nullptr;
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class U> U *as() const { return static_cast<U *>(p); }
+};
+
+// peak finder pipeline over ntr traces (rows of a matrix)
+struct PeakWS
+{
+    DevBuf counts, offs, slot_idx, slot_val, cidx, cval, ctr, state, flags, pos, tiles, trace_beg, peak_off, peaks,
+        counter, row;
+    long long npeaks = 0;
+    void release()
+    {
+        DevBuf *all[] = {&counts, &offs, &slot_idx, &slot_val, &cidx, &cval, &ctr, &state,
+                         &flags, &pos, &tiles, &trace_beg, &peak_off, &peaks, &counter, &row};
+        for (DevBuf *d : all) d->release();
+        npeaks = 0;
+    }
+};
+
+// Runs candidates + pruning + compaction; on return (stream synchronised)
+// ws.peaks / ws.peak_off hold the result and host_peak_off (ntr+1) is filled.
+template <class T>
+int run_peaks(const T *x, long ldx, const int *host_rows, int ntr, int len, double thr, int dist, PeakWS &ws,
+              cudaStream_t s, long long *launches, long long *host_peak_off, std::string &err);
+
+// ---------------------------------------------------------------------------
+// DBSCAN over segments
+struct DbWS
+{
+    DevBuf X, w, seg_of, seg_off, parent, is_root, labels, nclusters, core, pos, tiles;
+    void release()
+    {
+        DevBuf *all[] = {&X, &w, &seg_of, &seg_off, &parent, &is_root, &labels, &nclusters, &core, &pos, &tiles};
+        for (DevBuf *d : all) d->release();
+    }
+};
+
+int run_dbscan(int n, int nf, const double *X, const double *w, double eps, int min_obs, int nseg,
+               const int *seg_off_host, int *labels_host, int *nclusters_host, DbWS &ws, cudaStream_t s,
+               long long *launches, std::string &err);
+
+// device scan helper: out[0..n] = exclusive scan of in[0..n) (+ total)
+cudaError_t device_excl_scan(const int *in, long n, long long *out, long long *tiles, cudaStream_t s,
+                             long long *launches);
+inline long scan_tiles_needed(long n) { return (n + kScanTile - 1) / kScanTile + 1; }
+
+}  // namespace mfgpu

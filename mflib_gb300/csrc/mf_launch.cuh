@@ -1,0 +1,176 @@
+// mf_launch.cuh -- launchers of the matched-filter kernels for one sample
+// type; included once by mf_f32.cu and once by mf_f64.cu so the two
+// precisions compile in parallel.
+#pragma once
+#include "launch.h"
+
+namespace mfgpu {
+
+template <class T, int LOG2P> struct XcorrTable
+{
+    static size_t smem(bool shared_den, int S)
+    {
+        using acc = typename acc_t<T>::type;
+        constexpr int P = 1 << LOG2P, N = 2 * P, NCH = N / 32;
+        auto up = [](size_t v) { return (v + 127) & ~size_t(127); };
+        size_t b = 16 + 32 * sizeof(T) + 2 * sizeof(acc) * (NCH + 1);
+        b = up(b);
+        size_t seg = sizeof(T) * N, fft = sizeof(cx<T>) * spad_size(P);
+        b += up(shared_den ? (seg > fft ? seg : fft) : seg);
+        b += up(fft);
+        if (!shared_den) b += up(fft);
+        b += sizeof(T) * (size_t) S;
+        return b;
+    }
+    static cudaError_t launch(bool shared_den, const XcorrParams<T> &p, int nblocks, int ngroups, cudaStream_t s)
+    {
+        size_t bytes = smem(shared_den, p.S);
+        dim3 grid(nblocks, ngroups);
+        cudaError_t e;
+        if (shared_den)
+        {
+            auto k = xcorr_kernel<T, LOG2P, kNMax, true>;
+            e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+            if (e != cudaSuccess) return e;
+            k<<<grid, kThreads, bytes, s>>>(p);
+        }
+        else
+        {
+            auto k = xcorr_kernel<T, LOG2P, kNMax, false>;
+            e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+            if (e != cudaSuccess) return e;
+            k<<<grid, kThreads, bytes, s>>>(p);
+        }
+        return cudaGetLastError();
+    }
+    static cudaError_t spectra(const SpecParams<T> &p, int nt, cudaStream_t s)
+    {
+        constexpr int P = 1 << LOG2P;
+        size_t bytes = sizeof(cx<T>) * spad_size(P) + 64 * sizeof(double);
+        auto k = template_spectra_kernel<T, LOG2P, kNMax>;
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+        if (e != cudaSuccess) return e;
+        k<<<nt, kThreads, bytes, s>>>(p);
+        return cudaGetLastError();
+    }
+};
+
+template <class T, int LO, int HI> struct XcorrDispatch
+{
+    static size_t smem(int log2p, bool sd, int S)
+    {
+        if (log2p == LO) return XcorrTable<T, LO>::smem(sd, S);
+        if constexpr (LO < HI) return XcorrDispatch<T, LO + 1, HI>::smem(log2p, sd, S);
+        return 0;
+    }
+    static cudaError_t launch(int log2p, bool sd, const XcorrParams<T> &p, int nb, int ng, cudaStream_t s)
+    {
+        if (log2p == LO) return XcorrTable<T, LO>::launch(sd, p, nb, ng, s);
+        if constexpr (LO < HI) return XcorrDispatch<T, LO + 1, HI>::launch(log2p, sd, p, nb, ng, s);
+        return cudaErrorInvalidValue;
+    }
+    static cudaError_t spectra(int log2p, const SpecParams<T> &p, int nt, cudaStream_t s)
+    {
+        if (log2p == LO) return XcorrTable<T, LO>::spectra(p, nt, s);
+        if constexpr (LO < HI) return XcorrDispatch<T, LO + 1, HI>::spectra(log2p, p, nt, s);
+        return cudaErrorInvalidValue;
+    }
+};
+
+template <>
+size_t xcorr_smem_bytes<MFGPU_T>(int log2p, bool shared_den, int S)
+{
+    return XcorrDispatch<MFGPU_T, fft_limits<MFGPU_T>::lo, fft_limits<MFGPU_T>::hi>::smem(log2p, shared_den, S);
+}
+
+template <>
+cudaError_t launch_xcorr<MFGPU_T>(int log2p, bool shared_den, const XcorrParams<MFGPU_T> &p, int nblocks,
+                                  int ngroups, cudaStream_t s)
+{
+    return XcorrDispatch<MFGPU_T, fft_limits<MFGPU_T>::lo, fft_limits<MFGPU_T>::hi>::launch(log2p, shared_den, p,
+                                                                                        nblocks, ngroups, s);
+}
+
+template <>
+cudaError_t launch_spectra<MFGPU_T>(int log2p, const SpecParams<MFGPU_T> &p, int nt, cudaStream_t s)
+{
+    return XcorrDispatch<MFGPU_T, fft_limits<MFGPU_T>::lo, fft_limits<MFGPU_T>::hi>::spectra(log2p, p, nt, s);
+}
+
+template <>
+cudaError_t launch_dead<MFGPU_T>(const MFGPU_T *x_row, long n, unsigned char *dead, MFGPU_T *pmin, MFGPU_T *pmax,
+                                 int nchunks, cudaStream_t s)
+{
+    int chunk = (int) ((n + nchunks - 1) / nchunks);
+    dim3 grid(nchunks, 1);
+    minmax_partial_kernel<MFGPU_T><<<grid, kThreads, 0, s>>>(x_row, 0, n, chunk, pmin, pmax, nchunks);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    minmax_final_kernel<MFGPU_T><<<1, 256, 0, s>>>(pmin, pmax, nchunks, dead);
+    return cudaGetLastError();
+}
+
+// Reference debug spectrum: X[k] = sum_j brev[j] exp(-2 pi i j k / nfft),
+// brev = reverse((b - mean)/||b - mean||) (src/matchedFilter.cpp:168-190,
+// :595-620), evaluated directly in FP64 with exact integer phase reduction.
+template <class T>
+__global__ void ref_spectrum_kernel(const double *b, int L, int nfft, T *out)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > nfft / 2) return;
+    double mean = 0;
+    for (int j = 0; j < L; ++j) mean += b[j];
+    mean /= (double) L;
+    double nrm = 0;
+    for (int j = 0; j < L; ++j) { double d = b[j] - mean; nrm += d * d; }
+    double inv = nrm > 0 ? 1.0 / sqrt(nrm) : 0.0;
+    double re = 0, im = 0;
+    for (int j = 0; j < L; ++j)
+    {
+        double v = (b[L - 1 - j] - mean) * inv;
+        long long m = ((long long) j * k) % nfft;
+        double sn, cs;
+        sincospi(2.0 * (double) m / (double) nfft, &sn, &cs);
+        re += v * cs;
+        im -= v * sn;
+    }
+    out[2 * k] = (T) re;
+    out[2 * k + 1] = (T) im;
+}
+
+template <>
+cudaError_t launch_ref_spectrum<MFGPU_T>(const double *tmpl, int L, int nfft, MFGPU_T *out, cudaStream_t s)
+{
+    ref_spectrum_kernel<MFGPU_T><<<(nfft / 2 + 1 + 127) / 128, 128, 0, s>>>(tmpl, L, nfft, out);
+    return cudaGetLastError();
+}
+
+// Shift and stack, src/matchedFilter.cpp:1341-1362: out[k] = sum_t w_t |rho_t[k + shift_t]|
+// (or without the absolute value), templates accumulated in index order.
+// Lags before 0 contribute nothing.
+template <class T>
+__global__ void stack_kernel(const T *rho, long ldr, int nt, const int *shifts, const T *weights, int stack_abs,
+                             int outlen, T *out)
+{
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= outlen) return;
+    T acc = 0;
+    for (int t = 0; t < nt; ++t)
+    {
+        long lag = (long) k + shifts[t];
+        T v = lag >= 0 ? rho[(long) t * ldr + lag] : (T) 0;
+        acc = acc + weights[t] * (stack_abs ? (T) fabs(v) : v);
+    }
+    out[k] = acc;
+}
+
+template <>
+cudaError_t launch_stack<MFGPU_T>(const MFGPU_T *rho, long ldr, int nt, const int *shifts, const MFGPU_T *weights,
+                                  int stack_abs, int outlen, MFGPU_T *out, cudaStream_t s)
+{
+    stack_kernel<MFGPU_T><<<(outlen + 255) / 256, 256, 0, s>>>(rho, ldr, nt, shifts, weights, stack_abs, outlen,
+                                                              out);
+    return cudaGetLastError();
+}
+
+}  // namespace mfgpu

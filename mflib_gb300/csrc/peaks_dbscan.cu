@@ -1,0 +1,213 @@
+// peaks_dbscan.cu -- host drivers of the peak-finder and DBSCAN pipelines
+// (kernels in kernels_peaks.cuh / kernels_dbscan.cuh) and the device scan.
+#include <algorithm>
+#include <string>
+#include <vector>
+#include "launch.h"
+#include "kernels_peaks.cuh"
+#include "kernels_dbscan.cuh"
+
+namespace mfgpu {
+
+#define MF_TRY(expr)                                                                                               \
+    do                                                                                                             \
+    {                                                                                                              \
+        cudaError_t e_ = (expr);                                                                                   \
+        if (e_ != cudaSuccess)                                                                                     \
+        {                                                                                                          \
+            err = std::string(#expr) + ": " + cudaGetErrorString(e_);                                              \
+            return -1;                                                                                             \
+        }                                                                                                          \
+    } while (0)
+
+cudaError_t device_excl_scan(const int *in, long n, long long *out, long long *tiles, cudaStream_t s,
+                             long long *launches)
+{
+    long nt = (n + kScanTile - 1) / kScanTile;
+    if (nt == 0) return cudaMemsetAsync(out, 0, sizeof(long long), s);
+    scan_tile_sums_kernel<<<(unsigned) nt, kScanThreads, 0, s>>>(in, n, tiles);
+    scan_tile_offsets_kernel<<<1, kScanThreads, 0, s>>>(tiles, nt);
+    scan_apply_kernel<<<(unsigned) nt, kScanThreads, 0, s>>>(in, n, tiles, out);
+    if (launches) *launches += 3;
+    return cudaGetLastError();
+}
+
+template <class T>
+int run_peaks(const T *x, long ldx, const int *host_rows, int ntr, int len, double thr, int dist, PeakWS &ws,
+              cudaStream_t s, long long *launches, long long *host_peak_off, std::string &err)
+{
+    ws.npeaks = 0;
+    if (ntr <= 0) return 0;
+    if (len <= 0)
+    {
+        for (int t = 0; t <= ntr; ++t) host_peak_off[t] = 0;
+        return 0;
+    }
+    const int nchunks = (len + kPkChunk - 1) / kPkChunk;
+    const size_t nslots = (size_t) ntr * nchunks;
+    MF_TRY(ws.row.ensure(sizeof(int) * ntr));
+    MF_TRY(ws.trace_beg.ensure(sizeof(long long) * (ntr + 1)));
+    MF_TRY(ws.peak_off.ensure(sizeof(long long) * (ntr + 1)));
+    MF_TRY(ws.counts.ensure(sizeof(int) * nslots));
+    MF_TRY(ws.offs.ensure(sizeof(long long) * (nslots + 1)));
+    MF_TRY(ws.slot_idx.ensure(sizeof(int) * nslots * kPkCap));
+    MF_TRY(ws.slot_val.ensure(sizeof(T) * nslots * kPkCap));
+    MF_TRY(ws.tiles.ensure(sizeof(long long) * (scan_tiles_needed((long) nslots + 1) + 8)));
+    MF_TRY(ws.counter.ensure(sizeof(int)));
+    MF_TRY(cudaMemcpyAsync(ws.row.p, host_rows, sizeof(int) * ntr, cudaMemcpyHostToDevice, s));
+
+    PeakTraces<T> tr;
+    tr.x = x; tr.ldx = ldx; tr.row = ws.row.as<int>(); tr.len = len; tr.thr = (T) thr;
+    dim3 grid(nchunks, ntr);
+    peak_cand_kernel<T><<<grid, kPkThreads, 0, s>>>(tr, nchunks, ws.counts.as<int>(), ws.slot_idx.as<int>(),
+                                                    ws.slot_val.as<T>());
+    ++*launches;
+    MF_TRY(cudaGetLastError());
+    MF_TRY(device_excl_scan(ws.counts.as<int>(), (long) nslots, ws.offs.as<long long>(),
+                            ws.tiles.as<long long>(), s, launches));
+    long long ncand = 0;
+    MF_TRY(cudaMemcpyAsync(&ncand, ws.offs.as<long long>() + nslots, sizeof(long long), cudaMemcpyDeviceToHost, s));
+    MF_TRY(cudaStreamSynchronize(s));
+    MF_TRY(ws.cidx.ensure(sizeof(int) * ncand));
+    MF_TRY(ws.cval.ensure(sizeof(T) * ncand));
+    MF_TRY(ws.ctr.ensure(sizeof(int) * ncand));
+    MF_TRY(ws.state.ensure((size_t) ncand));
+    MF_TRY(ws.flags.ensure(sizeof(int) * ncand));
+    MF_TRY(ws.pos.ensure(sizeof(long long) * (ncand + 1)));
+    MF_TRY(ws.tiles.ensure(sizeof(long long) * (scan_tiles_needed((long) ncand + 1) + 8)));
+
+    peak_trace_beg_kernel<<<(ntr + 1 + 127) / 128, 128, 0, s>>>(ntr, nchunks, ws.offs.as<long long>(),
+                                                                ws.trace_beg.as<long long>());
+    ++*launches;
+    if (ncand > 0)
+    {
+        peak_gather_kernel<T><<<grid, kPkThreads, 0, s>>>(tr, nchunks, ws.counts.as<int>(), ws.offs.as<long long>(),
+                                                          ws.slot_idx.as<int>(), ws.slot_val.as<T>(),
+                                                          ws.cidx.as<int>(), ws.cval.as<T>(), ws.ctr.as<int>());
+        ++*launches;
+        MF_TRY(cudaGetLastError());
+    }
+    const unsigned gblocks = (unsigned) ((ncand + kPkThreads - 1) / kPkThreads);
+    const bool prune = dist > 0 && ncand > 0;
+    if (prune)
+    {
+        MF_TRY(cudaMemsetAsync(ws.state.p, PK_UNDECIDED, (size_t) ncand, s));
+        // Rounds until no candidate is left undecided; every round accepts at
+        // least the highest-priority undecided candidate of each trace, so
+        // ncand rounds always suffice.  The host checks every 4 rounds.
+        bool done = false;
+        for (long long round = 0; round <= ncand && !done; round += 4)
+        {
+            for (int r = 0; r < 4; ++r)
+            {
+                MF_TRY(cudaMemsetAsync(ws.counter.p, 0, sizeof(int), s));
+                peak_decide_kernel<T><<<gblocks, kPkThreads, 0, s>>>(ncand, ws.cidx.as<int>(), ws.cval.as<T>(),
+                                                                     ws.ctr.as<int>(), ws.trace_beg.as<long long>(),
+                                                                     ws.state.as<unsigned char>(), dist,
+                                                                     ws.counter.as<int>());
+                peak_suppress_kernel<T><<<gblocks, kPkThreads, 0, s>>>(
+                    ncand, ws.cidx.as<int>(), ws.ctr.as<int>(), ws.trace_beg.as<long long>(),
+                    ws.state.as<unsigned char>(), dist);
+                *launches += 2;
+            }
+            MF_TRY(cudaGetLastError());
+            int left = 0;
+            MF_TRY(cudaMemcpyAsync(&left, ws.counter.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+            MF_TRY(cudaStreamSynchronize(s));
+            done = left == 0;
+        }
+        if (!done)
+        {
+            err = "peak pruning did not converge";
+            return -1;
+        }
+    }
+    if (ncand > 0)
+    {
+        peak_flags_kernel<<<gblocks, kPkThreads, 0, s>>>(ncand, ws.state.as<unsigned char>(), prune ? 0 : 1,
+                                                         ws.flags.as<int>());
+        ++*launches;
+    }
+    MF_TRY(device_excl_scan(ws.flags.as<int>(), (long) ncand, ws.pos.as<long long>(), ws.tiles.as<long long>(), s,
+                            launches));
+    long long npk = 0;
+    MF_TRY(cudaMemcpyAsync(&npk, ws.pos.as<long long>() + ncand, sizeof(long long), cudaMemcpyDeviceToHost, s));
+    MF_TRY(cudaStreamSynchronize(s));
+    MF_TRY(ws.peaks.ensure(sizeof(int) * npk));
+    if (ncand > 0)
+    {
+        peak_compact_kernel<<<gblocks, kPkThreads, 0, s>>>(ncand, ws.flags.as<int>(), ws.pos.as<long long>(),
+                                                           ws.cidx.as<int>(), ws.peaks.as<int>());
+        ++*launches;
+    }
+    peak_trace_offsets_kernel<<<(ntr + 1 + 127) / 128, 128, 0, s>>>(ntr, ws.trace_beg.as<long long>(),
+                                                                    ws.pos.as<long long>(),
+                                                                    ws.peak_off.as<long long>());
+    ++*launches;
+    MF_TRY(cudaGetLastError());
+    MF_TRY(cudaMemcpyAsync(host_peak_off, ws.peak_off.p, sizeof(long long) * (ntr + 1), cudaMemcpyDeviceToHost, s));
+    MF_TRY(cudaStreamSynchronize(s));
+    ws.npeaks = npk;
+    return 0;
+}
+
+template int run_peaks<float>(const float *, long, const int *, int, int, double, int, PeakWS &, cudaStream_t,
+                              long long *, long long *, std::string &);
+template int run_peaks<double>(const double *, long, const int *, int, int, double, int, PeakWS &, cudaStream_t,
+                               long long *, long long *, std::string &);
+
+int run_dbscan(int n, int nf, const double *X, const double *w, double eps, int min_obs, int nseg,
+               const int *seg_off_host, int *labels_host, int *nclusters_host, DbWS &ws, cudaStream_t s,
+               long long *launches, std::string &err)
+{
+    if (n <= 0)
+    {
+        for (int i = 0; i < nseg; ++i) nclusters_host[i] = 0;
+        return 0;
+    }
+    MF_TRY(ws.X.ensure(sizeof(double) * (size_t) n * nf));
+    MF_TRY(ws.w.ensure(sizeof(double) * (size_t) n));
+    MF_TRY(ws.seg_of.ensure(sizeof(int) * (size_t) n));
+    MF_TRY(ws.seg_off.ensure(sizeof(int) * (size_t) (nseg + 1)));
+    MF_TRY(ws.parent.ensure(sizeof(int) * (size_t) n));
+    MF_TRY(ws.is_root.ensure(sizeof(int) * (size_t) n));
+    MF_TRY(ws.labels.ensure(sizeof(int) * (size_t) n));
+    MF_TRY(ws.nclusters.ensure(sizeof(int) * (size_t) nseg));
+    MF_TRY(ws.core.ensure((size_t) n));
+    MF_TRY(ws.pos.ensure(sizeof(long long) * (size_t) (n + 1)));
+    MF_TRY(ws.tiles.ensure(sizeof(long long) * (scan_tiles_needed(n + 1) + 8)));
+
+    std::vector<int> seg_of(n);
+    for (int sg = 0; sg < nseg; ++sg)
+        for (int i = seg_off_host[sg]; i < seg_off_host[sg + 1]; ++i) seg_of[i] = sg;
+    MF_TRY(cudaMemcpyAsync(ws.X.p, X, sizeof(double) * (size_t) n * nf, cudaMemcpyHostToDevice, s));
+    if (w) MF_TRY(cudaMemcpyAsync(ws.w.p, w, sizeof(double) * (size_t) n, cudaMemcpyHostToDevice, s));
+    MF_TRY(cudaMemcpyAsync(ws.seg_of.p, seg_of.data(), sizeof(int) * (size_t) n, cudaMemcpyHostToDevice, s));
+    MF_TRY(cudaMemcpyAsync(ws.seg_off.p, seg_off_host, sizeof(int) * (size_t) (nseg + 1), cudaMemcpyHostToDevice,
+                           s));
+
+    DbParams p;
+    p.X = ws.X.as<double>(); p.nf = nf; p.w = w ? ws.w.as<double>() : nullptr; p.eps = eps;
+    p.min_obs = (double) min_obs; p.seg_of = ws.seg_of.as<int>(); p.seg_off = ws.seg_off.as<int>(); p.n = n;
+    const unsigned blocks = (unsigned) ((n + kDbThreads - 1) / kDbThreads);
+    db_core_kernel<<<blocks, kDbThreads, 0, s>>>(p, ws.core.as<unsigned char>(), ws.parent.as<int>());
+    db_union_kernel<<<blocks, kDbThreads, 0, s>>>(p, ws.core.as<unsigned char>(), ws.parent.as<int>());
+    db_roots_kernel<<<blocks, kDbThreads, 0, s>>>(n, ws.core.as<unsigned char>(), ws.parent.as<int>(),
+                                                  ws.is_root.as<int>());
+    *launches += 3;
+    MF_TRY(cudaGetLastError());
+    MF_TRY(device_excl_scan(ws.is_root.as<int>(), n, ws.pos.as<long long>(), ws.tiles.as<long long>(), s,
+                            launches));
+    db_label_kernel<<<blocks, kDbThreads, 0, s>>>(p, ws.core.as<unsigned char>(), ws.parent.as<int>(),
+                                                  ws.pos.as<long long>(), ws.labels.as<int>());
+    db_count_kernel<<<(nseg + 127) / 128, 128, 0, s>>>(nseg, ws.seg_off.as<int>(), ws.pos.as<long long>(),
+                                                       ws.nclusters.as<int>());
+    *launches += 2;
+    MF_TRY(cudaGetLastError());
+    MF_TRY(cudaMemcpyAsync(labels_host, ws.labels.p, sizeof(int) * (size_t) n, cudaMemcpyDeviceToHost, s));
+    MF_TRY(cudaMemcpyAsync(nclusters_host, ws.nclusters.p, sizeof(int) * (size_t) nseg, cudaMemcpyDeviceToHost, s));
+    MF_TRY(cudaStreamSynchronize(s));
+    return 0;
+}
+
+}  // namespace mfgpu

@@ -1,0 +1,401 @@
+"""Matched-filter parameters and engines with the pymflib interface.
+
+``MultiChannel.MatchedFilterParameters`` / ``MultiChannel.MatchedFilter``
+mirror python/multiChannelMatchedFilterParameters.cpp and
+python/multiChannelMatchedFilter.cpp (MFLib::MatchedFilterParameters and
+MFLib::MatchedFilter<T> in MULTI_CHANNEL mode); the ``SingleChannel``
+versions mirror python/singleChannel/matchedFilter*.cpp
+(MFLib::SingleChannel::*).  The compute runs in libmfgpu on the GPU; this
+module only marshals arguments through the C ABI.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from .waveform import MatchedFilterDetectionMode, MatchedFilterImplementation, WaveformTemplate
+
+
+def compute_optimal_fft_and_block_length(nb, nx):
+    """MFLib::computeOptimalFFTAndBlockLength (src/matchedFilterParameters.cpp:371-385)."""
+    a, b = C.c_int(), C.c_int()
+    _lib.call("mfgpu_fft_sizes", int(nb), int(nx), C.byref(a), C.byref(b))
+    return a.value, b.value
+
+
+class MatchedFilterParameters:
+    """MFLib::MatchedFilterParameters (src/matchedFilterParameters.cpp:108-369)."""
+
+    def __init__(self, detection_mode=MatchedFilterDetectionMode.multi_channel):
+        self._mode = MatchedFilterDetectionMode(detection_mode)
+        self.clear()
+
+    def clear(self):
+        mode = self._mode
+        self._templates = []
+        self._fs = -1.0
+        self._signal_size = 0
+        self._fft = 0
+        self._block = 0
+        self._impl = MatchedFilterImplementation.direct
+        self._stack_abs = True
+        self._mode = mode
+
+    def add_template(self, wt):
+        """:199-219 -- the template must have a signal; sampling rates must agree to 1e-4."""
+        self._fft = self._block = 0
+        if not isinstance(wt, WaveformTemplate) or not wt.have_signal():
+            raise ValueError("Waveform not yet set on template")
+        df = wt.get_sampling_rate()
+        if self._fs < 0:
+            self._fs = df
+        if abs(df - self._fs) > 1.e-4:
+            raise ValueError("Template sampling rate = %f must equal %f" % (df, self._fs))
+        self._templates.append(wt.copy())
+
+    def get_template(self, it):
+        nt = len(self._templates)
+        if it < 0 or it >= nt:
+            raise ValueError("template index = %d must be in range [0,%d]" % (it, nt - 1))
+        return self._templates[it].copy()
+
+    def get_number_of_templates(self):
+        return len(self._templates)
+
+    def clear_templates(self):
+        self._fs = -1.0
+        self._templates = []
+
+    def get_max_template_length(self):
+        if not self._templates:
+            raise RuntimeError("No templates set")
+        return max(t.get_signal_length() for t in self._templates)
+
+    def set_signal_size(self, n):
+        self._fft = self._block = 0
+        if n < 1:
+            raise ValueError("Signal size must be positive")
+        self._signal_size = int(n)
+
+    def get_signal_size(self):
+        if self._signal_size < 1:
+            raise RuntimeError("Signal size not set")
+        return self._signal_size
+
+    def set_fft_length(self, n):
+        """:250-265 -- stored only: like the reference, initialize() picks its own sizes."""
+        if not self._templates:
+            raise RuntimeError("No templates set")
+        nb = self.get_max_template_length()
+        if n < nb:
+            raise ValueError("fftLength = %d must be at least %d" % (n, nb))
+        self._fft = int(n)
+        self._block = self._fft - nb + 1
+
+    def _sizes(self):
+        if not self._templates:
+            raise RuntimeError("Templates must be set prior to calling this")
+        if self._fft < 1:
+            self._fft, self._block = compute_optimal_fft_and_block_length(
+                self.get_max_template_length(), self.get_signal_size())
+        return self._fft, self._block
+
+    def get_fft_length(self):
+        return self._sizes()[0]
+
+    def get_block_length(self):
+        return self._sizes()[1]
+
+    def block_length(self):
+        """pymflib binds this name to getFFTLength (python/multiChannelMatchedFilterParameters.cpp:160-162);
+        here it returns the overlap-add block length its docstring describes."""
+        return self.get_block_length()
+
+    def set_matched_filter_implementation(self, impl):
+        self._impl = MatchedFilterImplementation(impl)
+
+    def get_matched_filter_implementation(self):
+        return self._impl
+
+    def set_detection_mode(self, mode):
+        self._mode = MatchedFilterDetectionMode(mode)
+
+    def get_detection_mode(self):
+        return self._mode
+
+    def set_stack_absolute_values(self, flag):
+        self._stack_abs = bool(flag)
+
+    def get_stack_absolute_values(self):
+        return self._stack_abs
+
+    def is_valid(self):
+        if not self._templates or self._signal_size < 1:
+            return False
+        return self.get_max_template_length() >= 1
+
+
+class MatchedFilter:
+    """MFLib::MatchedFilter<T> (include/mflib/matchedFilter.hpp:28-178) on the GPU.
+
+    ``dtype`` selects the instantiation (numpy.float64 is the one pymflib
+    exposes; numpy.float32 is the FP32 engine)."""
+
+    def __init__(self, dtype=np.float64):
+        self._dtype = np.dtype(dtype)
+        if self._dtype not in (np.dtype(np.float32), np.dtype(np.float64)):
+            raise ValueError("dtype must be float32 or float64")
+        prec = _lib.MFGPU_FLOAT32 if self._dtype == np.float32 else _lib.MFGPU_FLOAT64
+        h = C.c_void_p()
+        _lib.call("mfgpu_mf_create", prec, C.byref(h))
+        self._h = h
+        self._params = None
+        self._nt = 0
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.lib().mfgpu_mf_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    @property
+    def dtype(self):
+        return self._dtype
+
+    def initialize(self, params, template_channels=None, n_channels=None, fft_length=0):
+        """MatchedFilter<T>::initialize (src/matchedFilter.cpp:507-821).
+
+        Extensions: ``template_channels`` (one channel index per template,
+        with ``n_channels`` channels) lets several templates share one
+        signal; ``fft_length`` forces the overlap-save FFT length."""
+        if not isinstance(params, MatchedFilterParameters) or not params.is_valid():
+            raise ValueError("Parameters are invalid")
+        tmpls = [params.get_template(i) for i in range(params.get_number_of_templates())]
+        nt = len(tmpls)
+        arrs = [np.ascontiguousarray(t.get_signal(), dtype=np.float64) for t in tmpls]
+        lens = (C.c_int * nt)(*[a.size for a in arrs])
+        ptrs = (C.POINTER(C.c_double) * nt)(*[a.ctypes.data_as(C.POINTER(C.c_double)) for a in arrs])
+        p = _lib.MfgpuParams()
+        p.detection_mode = int(params.get_detection_mode())
+        p.n_templates = nt
+        p.template_lengths = lens
+        p.templates = ptrs
+        p.signal_size = params.get_signal_size()
+        # shift-and-stack inputs exist only when every template has an onset
+        # and a travel time (src/matchedFilter.cpp:577-592)
+        if all(t.have_phase_onset_time() and t.have_travel_time() for t in tmpls):
+            sh = (C.c_int * nt)(*[int((t.get_phase_travel_time() - t.get_phase_onset_time())
+                                      * t.get_sampling_rate() + 0.5) for t in tmpls])
+            w = (C.c_double * nt)(*[t.get_shift_and_stack_weight() for t in tmpls])
+            p.stack_shifts = sh
+            p.stack_weights = w
+        p.stack_absolute_values = 1 if params.get_stack_absolute_values() else 0
+        chans = None
+        if template_channels is not None:
+            chans = np.ascontiguousarray(template_channels, dtype=np.int32)
+            if chans.size != nt:
+                raise ValueError("template_channels needs one entry per template")
+            p.n_channels = int(n_channels if n_channels is not None else chans.max() + 1)
+            p.template_channel = chans.ctypes.data_as(C.POINTER(C.c_int))
+        p.fft_length = int(fft_length)
+        _lib.call("mfgpu_mf_initialize", self._h, C.byref(p))
+        self._params = params
+        self._nt = nt
+        self._templates = tmpls
+        self._n = params.get_signal_size()
+
+    def clear(self):
+        _lib.call("mfgpu_mf_clear", self._h)
+        self._params = None
+        self._nt = 0
+
+    def is_initialized(self):
+        f = C.c_int()
+        _lib.call("mfgpu_mf_is_initialized", self._h, C.byref(f))
+        return bool(f.value)
+
+    def _int(self, name):
+        v = C.c_int()
+        _lib.call(name, self._h, C.byref(v))
+        return v.value
+
+    def get_number_of_templates(self):
+        return self._int("mfgpu_mf_get_number_of_templates")
+
+    def get_signal_length(self):
+        return self._int("mfgpu_mf_get_signal_length")
+
+    def get_filtered_signal_length(self):
+        return self._int("mfgpu_mf_get_filtered_signal_length")
+
+    def _samples(self, x):
+        if x is None:
+            raise ValueError("x is null")
+        return np.ascontiguousarray(x, dtype=self._dtype).ravel()
+
+    def set_signal(self, it, x):
+        """MatchedFilter<T>::setSignal (src/matchedFilter.cpp:863-921)."""
+        x = self._samples(x)
+        _lib.call("mfgpu_mf_set_signal", self._h, int(it), int(x.size), x.ctypes.data_as(C.c_void_p))
+
+    def set_channel_signal(self, channel, x):
+        """Extension: signal of a shared channel (see initialize)."""
+        x = self._samples(x)
+        _lib.call("mfgpu_mf_set_channel_signal", self._h, int(channel), int(x.size),
+                  x.ctypes.data_as(C.c_void_p))
+
+    def zero_signal(self, it):
+        _lib.call("mfgpu_mf_zero_signal", self._h, int(it))
+
+    def get_signal(self, it):
+        """Copy of the stored signal (MatchedFilter<T>::getSignalPointer)."""
+        out = np.empty(self.get_signal_length(), dtype=self._dtype)
+        _lib.call("mfgpu_mf_get_signal", self._h, int(it), int(out.size), out.ctypes.data_as(C.c_void_p))
+        return out
+
+    def apply(self):
+        _lib.call("mfgpu_mf_apply", self._h)
+
+    def synchronize(self):
+        _lib.call("mfgpu_mf_synchronize", self._h)
+
+    def have_matched_filtered_signals(self):
+        f = C.c_int()
+        _lib.call("mfgpu_mf_have_matched_filtered_signals", self._h, C.byref(f))
+        return bool(f.value)
+
+    def get_matched_filtered_signal(self, it):
+        """Coefficients of template it at lags 0..getFilteredSignalLength()-1."""
+        n = max(0, self.get_filtered_signal_length())
+        out = np.empty(max(n, 1), dtype=self._dtype)
+        cnt = C.c_int()
+        _lib.call("mfgpu_mf_get_matched_filtered_signal", self._h, int(it), int(out.size),
+                  out.ctypes.data_as(C.c_void_p), C.byref(cnt))
+        return out[: cnt.value]
+
+    def get_valid_matched_filtered_signal(self, it):
+        """Extension: every valid lag of template it (n - L_t + 1 values)."""
+        out = np.empty(max(self.get_signal_length(), 1), dtype=self._dtype)
+        cnt = C.c_int()
+        _lib.call("mfgpu_mf_get_valid_signal", self._h, int(it), int(out.size), out.ctypes.data_as(C.c_void_p),
+                  C.byref(cnt))
+        return out[: cnt.value]
+
+    def shift_and_stack(self):
+        out = np.empty(max(self.get_filtered_signal_length(), 1), dtype=self._dtype)
+        cnt = C.c_int()
+        _lib.call("mfgpu_mf_shift_and_stack", self._h, int(out.size), out.ctypes.data_as(C.c_void_p),
+                  C.byref(cnt))
+        return out[: cnt.value]
+
+    def get_spectra_of_template(self, it):
+        """Debug view (src/matchedFilter.cpp:1412-1431): rfft of the reversed,
+        demeaned, unit-norm template at the reference's FFT length."""
+        nfft, _ = compute_optimal_fft_and_block_length(self._templates and max(
+            t.get_signal_length() for t in self._templates), self._n + max(
+            t.get_signal_length() for t in self._templates) - 1)
+        buf = np.empty(2 * (nfft // 2 + 1), dtype=self._dtype)
+        cnt = C.c_int()
+        _lib.call("mfgpu_mf_get_spectra_of_template", self._h, int(it), int(buf.size),
+                  buf.ctypes.data_as(C.c_void_p), C.byref(cnt))
+        return buf[0::2] + 1j * buf[1::2]
+
+    def get_waveform_template(self, it):
+        if it < 0 or it >= self._nt:
+            raise ValueError("it = %d must be in the range [0,%d]" % (it, self._nt - 1))
+        return self._templates[it].copy()
+
+    # -- extensions ---------------------------------------------------------
+    def get_plan(self):
+        a, b, c = C.c_int(), C.c_int(), C.c_int()
+        _lib.call("mfgpu_mf_get_plan", self._h, C.byref(a), C.byref(b), C.byref(c))
+        return {"fft_length": a.value, "lags_per_block": b.value, "n_blocks": c.value}
+
+    def last_timings(self):
+        a, b = C.c_float(), C.c_float()
+        _lib.call("mfgpu_mf_get_last_timings", self._h, C.byref(a), C.byref(b))
+        return {"xcorr_ms": a.value, "apply_ms": b.value}
+
+    def launch_count(self):
+        v = C.c_longlong()
+        _lib.call("mfgpu_mf_get_launch_count", self._h, C.byref(v))
+        return v.value
+
+    def find_peaks(self, threshold, min_distance, trace_length=0):
+        """PeakFinder<T>::apply on every template's coefficients, on the device."""
+        _lib.call("mfgpu_mf_find_peaks", self._h, float(threshold), int(min_distance), int(trace_length))
+
+    def get_peaks(self, it):
+        cap = max(1, self.get_signal_length())
+        out = np.empty(cap, dtype=np.int32)
+        cnt = C.c_int()
+        _lib.call("mfgpu_mf_get_peaks", self._h, int(it), cap, out.ctypes.data_as(C.POINTER(C.c_int)),
+                  C.byref(cnt))
+        return out[: cnt.value].copy()
+
+    def get_all_peaks(self):
+        """(counts[nt], concatenated indices) of the last find_peaks."""
+        nt = self._nt
+        counts = np.zeros(nt, dtype=np.int32)
+        tot = C.c_int()
+        _lib.call("mfgpu_mf_get_all_peaks", self._h, nt, counts.ctypes.data_as(C.POINTER(C.c_int)), 0, None,
+                  C.byref(tot))
+        idx = np.empty(max(1, tot.value), dtype=np.int32)
+        _lib.call("mfgpu_mf_get_all_peaks", self._h, nt, counts.ctypes.data_as(C.POINTER(C.c_int)), int(idx.size),
+                  idx.ctypes.data_as(C.POINTER(C.c_int)), C.byref(tot))
+        return counts, idx[: tot.value].copy()
+
+
+class _MultiChannel:
+    """pymflib.MultiChannel (python/pymflib.cpp:68-70)."""
+
+    class MatchedFilterParameters(MatchedFilterParameters):
+        def __init__(self):
+            super().__init__(MatchedFilterDetectionMode.multi_channel)
+
+        def set_detection_mode(self, mode):
+            raise AttributeError("MultiChannel parameters are always MULTI_CHANNEL")
+
+    class MatchedFilter(MatchedFilter):
+        """Multi-channel engine: signal it feeds template it."""
+
+        def initialize(self, params, **kw):
+            if params.get_detection_mode() != MatchedFilterDetectionMode.multi_channel:
+                raise ValueError("Parameters are invalid")
+            super().initialize(params, **kw)
+
+
+class _SingleChannel:
+    """pymflib.SingleChannel matched filter (python/singleChannel/matchedFilter*.cpp,
+    src/singleChannel/matchedFilter*.cpp): many templates against one signal."""
+
+    class MatchedFilterParameters(MatchedFilterParameters):
+        def __init__(self):
+            # src/singleChannel/matchedFilterParameters.cpp:20-25 forces SINGLE_CHANNEL
+            super().__init__(MatchedFilterDetectionMode.single_channel)
+
+        def set_detection_mode(self, mode):
+            raise AttributeError("SingleChannel parameters are always SINGLE_CHANNEL")
+
+    class MatchedFilter(MatchedFilter):
+        def initialize(self, params, **kw):
+            if params.get_detection_mode() != MatchedFilterDetectionMode.single_channel:
+                raise ValueError("Parameters are invalid")
+            super().initialize(params, **kw)
+
+        def set_signal(self, x):
+            """src/singleChannel/matchedFilter.cpp:62-67: always signal slot 0."""
+            super().set_signal(0, x)
+
+        def zero_signal(self):
+            super().zero_signal(0)
+
+        def get_signal(self):
+            return super().get_signal(0)
+
+
+MultiChannel = _MultiChannel
+SingleChannel = _SingleChannel

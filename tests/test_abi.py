@@ -1,0 +1,147 @@
+"""The C ABI library loads and exports every entry point include/mfgpu.h
+declares; host-side API logic that needs no GPU.  No compute calls."""
+import ctypes
+import os
+import pickle
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "mfgpu.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(mfgpu_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol(mflib):
+    from mflib_gb300 import _lib
+    lib = ctypes.CDLL(_lib.LIB_PATH)
+    syms = header_symbols()
+    assert len(syms) > 40
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+    # the Python binding covers the whole header
+    assert sorted(_lib.exported_symbols()) == syms
+
+
+def test_fft_sizes_through_abi(mflib, oracle, rng):
+    for nb, nx, expect in ((4500, 75000, (32768, 28269)), (4500, 8640000, (65536, 61037)),
+                           (101, 1024, (512, 412))):
+        assert mflib.compute_optimal_fft_and_block_length(nb, nx) == expect
+    for _ in range(300):
+        nb = int(rng.integers(1, 5000))
+        nx = int(rng.integers(nb + 1, 20_000_000))
+        assert mflib.compute_optimal_fft_and_block_length(nb, nx) == oracle.fft_sizes(nb, nx)
+    with pytest.raises(ValueError):
+        mflib.compute_optimal_fft_and_block_length(10, 10)
+    with pytest.raises(ValueError):
+        mflib.compute_optimal_fft_and_block_length(0, 10)
+
+
+def test_network_station_phase(mflib):
+    # python/unit_tests.py:8-35
+    nsp = mflib.NetworkStationPhase()
+    nsp.set_network("UU")
+    nsp.set_station("ALT")
+    nsp.set_channel("EHN")
+    nsp.set_location_code("01")
+    nsp.set_phase("P")
+    assert (nsp.get_network(), nsp.get_station(), nsp.get_channel(), nsp.get_location_code(),
+            nsp.get_phase()) == ("UU", "ALT", "EHN", "01", "P")
+    p = pickle.loads(pickle.dumps(nsp, 2))
+    assert p == nsp and p.get_station() == "ALT"
+    q = mflib.NetworkStationPhase()
+    q.set_network(" uu")
+    assert q.get_network() == "UU"
+
+
+def test_waveform_template(mflib):
+    # python/unit_tests.py:37-117
+    wt = mflib.WaveformTemplate()
+    sig = np.arange(1, 400, 1)
+    wt.set_signal(sig)
+    assert np.max(np.abs(wt.get_signal() - sig)) == 0
+    wt.set_sampling_rate(100)
+    assert wt.get_sampling_rate() == 100
+    wt.set_shift_and_stack_weight(0.8)
+    assert wt.get_shift_and_stack_weight() == 0.8
+    wt.set_phase_travel_time(9)
+    assert wt.get_phase_travel_time() == 9
+    wt.set_phase_onset_time_in_signal(0.5)
+    assert wt.get_phase_onset_time_in_signal() == 0.5
+    wt.set_magnitude(6)
+    assert wt.get_magnitude() == 6
+    wt.set_polarity(mflib.Polarity.compression)
+    assert wt.get_polarity() == mflib.Polarity.compression
+    nsp = mflib.NetworkStationPhase()
+    nsp.set_station("FORU")
+    wt.set_identifier([nsp, 4])
+    idb = wt.get_identifier()
+    assert idb[0].get_station() == "FORU" and idb[1] == 4
+    cp = pickle.loads(pickle.dumps(wt))
+    assert np.max(np.abs(cp.get_signal() - sig)) == 0
+    assert cp.get_phase_onset_time_in_signal() == 0.5 and cp.get_identifier()[1] == 4
+    wt.clear()
+    assert wt.get_shift_and_stack_weight() == 1
+    with pytest.raises(ValueError):
+        wt.set_sampling_rate(0)
+    with pytest.raises(ValueError):
+        wt.set_shift_and_stack_weight(1.5)
+    with pytest.raises(RuntimeError):
+        wt.get_signal()
+
+
+def test_matched_filter_parameters(mflib):
+    # python/unit_tests.py:121-180
+    wf1, wf2 = mflib.WaveformTemplate(), mflib.WaveformTemplate()
+    p = mflib.MultiChannel.MatchedFilterParameters()
+    t1, t2 = np.arange(1, 100, 1), np.arange(1, 95, 1)
+    wf1.set_signal(t1)
+    wf2.set_signal(t2)
+    for w in (wf1, wf2):
+        w.set_sampling_rate(100)
+        w.set_shift_and_stack_weight(0.8)
+        w.set_phase_onset_time_in_signal(0.05)
+        w.set_phase_travel_time(4)
+    p.add_template(wf1)
+    p.add_template(wf2)
+    p.set_signal_size(1024)
+    assert p.get_number_of_templates() == 2
+    assert p.get_fft_length() == 512
+    p.set_fft_length(550)
+    assert p.get_fft_length() == 550
+    for i, t in enumerate((t1, t2)):
+        wb = p.get_template(i)
+        assert wb.get_sampling_rate() == 100 and wb.get_shift_and_stack_weight() == 0.8
+        assert wb.get_phase_onset_time_in_signal() == 0.05 and wb.get_phase_travel_time() == 4
+        assert np.max(np.abs(wb.get_signal() - t)) == 0
+    p.clear_templates()
+    assert p.get_number_of_templates() == 0
+    bad = mflib.WaveformTemplate()
+    bad.set_signal(t1)
+    bad.set_sampling_rate(50)
+    p.add_template(wf1)
+    with pytest.raises(ValueError):
+        p.add_template(bad)
+
+
+def test_single_channel_parameters(mflib, rng):
+    # testing/singleChannel.cpp:28-102
+    p = mflib.SingleChannel.MatchedFilterParameters()
+    p.set_signal_size(3823)
+    assert p.get_detection_mode() == mflib.MatchedFilterDetectionMode.single_channel
+    assert not p.is_valid()
+    for L in (410, 411):
+        wt = mflib.WaveformTemplate()
+        wt.set_signal(rng.uniform(-1, 1, L))
+        wt.set_sampling_rate(1)
+        p.add_template(wt)
+    assert p.get_max_template_length() == 411 and p.is_valid()
+    p.clear_templates()
+    assert p.get_number_of_templates() == 0
+    p.clear()
+    assert not p.is_valid()

@@ -1,0 +1,180 @@
+"""Peak finder and DBSCAN on the GPU against the oracle and the reference's
+golden vectors.  Indices and labels are compared exactly."""
+import numpy as np
+import pytest
+
+from test_oracle import DBSCAN_X, PEAKS_13, PEAKS_21, peak_signal
+
+pytestmark = pytest.mark.gpu
+
+
+def _peaks(mf, x, thr, md, dtype=np.float64):
+    pf = mf.PeakFinder(dtype=dtype)
+    pf.set_threshold(thr)
+    pf.set_minimum_peak_distance(md)
+    pf.set_signal(x)
+    pf.apply()
+    return pf.get_peak_indices()
+
+
+def test_peak_finder_golden(gpu):
+    # testing/peakFinder.cpp:16-143
+    mf = gpu
+    pf = mf.PeakFinder()
+    assert abs(pf.get_threshold() - 0.7) < 1e-14
+    pf.set_threshold(0.8)
+    pf.set_minimum_peak_distance(52)
+    assert pf.get_minimum_peak_distance() == 52
+    pf.set_signal(np.full(4000, 0.4))
+    pf.apply()
+    assert pf.get_number_of_peaks() == 0
+    sig = peak_signal()
+    np.testing.assert_array_equal(_peaks(mf, sig, 0.8, 52), PEAKS_13)
+    np.testing.assert_array_equal(_peaks(mf, sig, 0.8, 0), PEAKS_21)
+    np.testing.assert_array_equal(_peaks(mf, sig.astype(np.float32), 0.8, 52, np.float32), PEAKS_13)
+
+
+def test_peak_finder_errors(gpu):
+    mf = gpu
+    pf = mf.PeakFinder()
+    with pytest.raises(ValueError):
+        pf.set_threshold(1.5)
+    with pytest.raises(ValueError):
+        pf.set_threshold(-0.1)
+    with pytest.raises(ValueError):
+        pf.set_signal(np.zeros(0))
+    pf.apply()  # no signal: no peaks
+    assert pf.get_number_of_peaks() == 0
+
+
+@pytest.mark.parametrize("thr,md", [(0.5, 50), (0.0, 0), (0.0, 3), (0.9, 1000), (0.3, 250), (0.2, 1)])
+def test_peaks_random_vs_oracle(gpu, oracle, rng, thr, md):
+    mf = gpu
+    for n in (1, 2, 3, 17, 4096, 4097, 100_000):
+        x = np.clip(rng.standard_normal(n) * 0.6, -1, 1)
+        np.testing.assert_array_equal(_peaks(mf, x, thr, md), oracle.peaks(x, thr, md))
+
+
+def test_peaks_plateaus_and_ties(gpu, oracle, rng):
+    mf = gpu
+    # quantised values give plateaus and equal-valued candidates
+    x = np.round(rng.uniform(0, 1, 50_000) * 8) / 8
+    for thr, md in ((0.1, 0), (0.1, 5), (0.5, 40)):
+        np.testing.assert_array_equal(_peaks(mf, x, thr, md), oracle.peaks(x, thr, md))
+    x = np.zeros(10)
+    x[3:6] = 0.9
+    np.testing.assert_array_equal(_peaks(mf, x, 0.5, 0), oracle.peaks(x, 0.5, 0))
+
+
+def test_peaks_dense_long_chain(gpu, oracle):
+    """A damped oscillation gives a long run of candidates whose values fall
+    with index: the pruning rounds must still match the greedy pass."""
+    mf = gpu
+    t = np.arange(200_000)
+    x = np.exp(-t / 60_000.0) * np.abs(np.sin(t * 0.31)) * 0.99
+    for md in (3, 10, 100):
+        np.testing.assert_array_equal(_peaks(mf, x, 0.01, md), oracle.peaks(x, 0.01, md))
+
+
+def test_batched_peaks_on_rho(gpu, oracle, rng):
+    mf = gpu
+    n = 200_000
+    sig = rng.standard_normal(n).astype(np.float32)
+    tps = [sig[i:i + 300].astype(np.float64) for i in (1000, 50_000, 123_456)]
+    p = mf.SingleChannel.MatchedFilterParameters()
+    for t in tps:
+        wt = mf.WaveformTemplate()
+        wt.set_signal(t)
+        wt.set_sampling_rate(100.0)
+        p.add_template(wt)
+    p.set_signal_size(n)
+    f = mf.SingleChannel.MatchedFilter(dtype=np.float32)
+    f.initialize(p)
+    f.set_signal(sig)
+    f.apply()
+    for thr, md in ((0.3, 100), (0.1, 0)):
+        f.find_peaks(thr, md)
+        counts, allidx = f.get_all_peaks()
+        off = 0
+        for i in range(len(tps)):
+            rho = f.get_matched_filtered_signal(i).astype(np.float64)
+            ref = oracle.peaks(rho, thr, md)
+            got = f.get_peaks(i)
+            np.testing.assert_array_equal(got, ref)
+            np.testing.assert_array_equal(allidx[off:off + counts[i]], ref)
+            off += counts[i]
+    f.find_peaks(0.5, 200)
+    for i, start in enumerate((1000, 50_000, 123_456)):
+        assert start in set(f.get_peaks(i).tolist())
+
+
+def test_dbscan_golden(gpu):
+    # testing/dbscan.cpp:8-60
+    mf = gpu
+    db = mf.DBSCAN()
+    db.initialize(3, 2)
+    db.set_data(DBSCAN_X)
+    db.cluster()
+    assert db.get_number_of_clusters() == 2
+    np.testing.assert_array_equal(db.get_labels(), [0, 0, 0, 1, 1, -1])
+    db.set_data(DBSCAN_X[:5])
+    db.cluster()
+    assert db.get_number_of_clusters() == 2
+    np.testing.assert_array_equal(db.get_labels(), [0, 0, 0, 1, 1])
+
+
+def test_dbscan_errors(gpu):
+    mf = gpu
+    db = mf.DBSCAN()
+    with pytest.raises(RuntimeError):
+        db.set_data(DBSCAN_X)
+    with pytest.raises(ValueError):
+        db.initialize(-1, 2)
+    with pytest.raises(ValueError):
+        db.initialize(1, 0)
+    db.initialize(1, 2)
+    with pytest.raises(RuntimeError):
+        db.cluster()
+    with pytest.raises(ValueError):
+        db.set_weighted_data(DBSCAN_X, np.zeros(6))
+
+
+@pytest.mark.parametrize("nf", [1, 2, 3])
+def test_dbscan_random_vs_oracle(gpu, oracle, rng, nf):
+    mf = gpu
+    db = mf.DBSCAN()
+    for _ in range(6):
+        X = rng.uniform(0, 30, (int(rng.integers(1, 2000)), nf))
+        if nf == 1:
+            X = np.round(X * 4) / 4  # exact ties at the eps boundary
+        eps = float(rng.uniform(0.25, 2.5))
+        mo = int(rng.integers(1, 8))
+        w = rng.uniform(0.1, 3.0, X.shape[0])
+        for weights in (None, w):
+            db.initialize(eps, mo)
+            if weights is None:
+                db.set_data(X)
+            else:
+                db.set_weighted_data(X, weights)
+            db.cluster()
+            ncl, lab = oracle.dbscan(X, eps, mo, weights)
+            assert db.get_number_of_clusters() == ncl
+            np.testing.assert_array_equal(db.get_labels(), lab)
+
+
+def test_dbscan_segmented(gpu, oracle, rng):
+    mf = gpu
+    db = mf.DBSCAN()
+    db.initialize(50.0, 3)
+    sizes = [0, 5, 300, 1, 1200]
+    segs = [rng.uniform(0, 20_000, s) for s in sizes]
+    X = np.concatenate(segs) if sum(sizes) else np.zeros(0)
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int32)
+    labels, ncl = db.cluster_segments(X, off)
+    for s, seg in enumerate(segs):
+        if seg.size == 0:
+            assert ncl[s] == 0
+            continue
+        n_ref, lab_ref = oracle.dbscan(seg, 50.0, 3)
+        assert ncl[s] == n_ref
+        np.testing.assert_array_equal(labels[off[s]:off[s + 1]], lab_ref)

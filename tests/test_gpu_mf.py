@@ -1,0 +1,351 @@
+"""Matched filter on the GPU (through the C ABI) against the CPU oracle and
+the reference's own known-answer tests.
+
+Tolerances: FP64 engine at the reference tests' own bounds (1e-13 .. 1e-14
+versus the naive two-pass Pearson correlation); FP32 engine within 1e-5
+absolute of the FP64 oracle, the bound stated for the FP32 path."""
+import numpy as np
+import pytest
+
+from test_oracle import damped_case
+
+pytestmark = pytest.mark.gpu
+
+FP32_TOL = 1e-5
+
+
+def _params(mf, templates, n, mode="multi", fs=1.0):
+    p = mf.MultiChannel.MatchedFilterParameters() if mode == "multi" else mf.SingleChannel.MatchedFilterParameters()
+    for t in templates:
+        wt = mf.WaveformTemplate()
+        wt.set_signal(t)
+        wt.set_sampling_rate(fs)
+        p.add_template(wt)
+    p.set_signal_size(n)
+    return p
+
+
+def test_basic_double(gpu, oracle):
+    # testing/matchedFilter.cpp:58-168
+    mf = gpu
+    x, x2, b, b2 = damped_case()
+    f = mf.MultiChannel.MatchedFilter()
+    f.initialize(_params(mf, [b], x.size))
+    f.set_signal(0, x)
+    np.testing.assert_array_equal(f.get_signal(0), x)
+    assert not f.have_matched_filtered_signals()
+    f.apply()
+    assert f.have_matched_filtered_signals()
+    r = f.get_matched_filtered_signal(0)
+    assert r.size == x.size - b.size + 1
+    assert np.max(np.abs(r - oracle.pearson_naive(b, x))) < 1e-13
+    f.initialize(_params(mf, [b, b2, b, b2], x.size))
+    for i, s in enumerate([x, x2, x, x2]):
+        f.set_signal(i, s)
+    f.apply()
+    for i, (tp, s) in enumerate(zip([b, b2, b, b2], [x, x2, x, x2])):
+        assert np.max(np.abs(f.get_matched_filtered_signal(i) - oracle.pearson_naive(tp, s))) < 1e-13
+
+
+def test_basic_float(gpu, oracle):
+    # testing/matchedFilter.cpp:172-271 (< 2e-6)
+    mf = gpu
+    x, x2, b, b2 = damped_case()
+    f = mf.MultiChannel.MatchedFilter(dtype=np.float32)
+    f.initialize(_params(mf, [b, b2, b, b2], x.size))
+    for i, s in enumerate([x, x2, x, x2]):
+        f.set_signal(i, s.astype(np.float32))
+    f.apply()
+    for i, (tp, s) in enumerate(zip([b, b2, b, b2], [x, x2, x, x2])):
+        ref = oracle.pearson_naive(tp.astype(np.float32), s.astype(np.float32))
+        assert np.max(np.abs(f.get_matched_filtered_signal(i).astype(np.float64) - ref)) < 2e-6
+
+
+def test_shift_and_stack(gpu, oracle):
+    # testing/matchedFilter.cpp:275-465
+    mf = gpu
+    df = 100.0
+    dt = 1 / df
+    n = int(120 / dt + 0.5) + 1
+    tsz = int(4 / dt + 0.5) + 1
+    toffs = [1.0, 2.0, 1.5]
+    extras = [int(t / dt + 0.5) for t in toffs]
+    tts = [20.0, 40.0, 80.0]
+    amps = [(2.0, 1.0), (1.5, 1.5), (1.2, 2.5)]
+    sigs = []
+    tps = []
+    base = np.where(np.arange(n) % 2 == 0, -0.001, 0.001)
+    t = np.arange(tsz) * dt
+    for (a, d), ex, tt in zip(amps, extras, tts):
+        w = a * np.exp(-d * t) * np.sin(2 * np.pi * t / 4.0)
+        w[0] = 0
+        w[-1] = 0
+        tp = np.zeros(tsz + ex)
+        tp[ex:] = w
+        s = base.copy()
+        i0 = int((8.0 + tt) / dt + 0.5)
+        s[i0:i0 + tsz] = w
+        tps.append(tp)
+        sigs.append(s)
+    p = mf.MultiChannel.MatchedFilterParameters()
+    for tp, to, tt in zip(tps, toffs, tts):
+        wt = mf.WaveformTemplate()
+        wt.set_signal(tp)
+        wt.set_sampling_rate(df)
+        wt.set_phase_travel_time(tt)
+        wt.set_phase_onset_time_in_signal(to)
+        p.add_template(wt)
+    p.set_signal_size(n)
+    f = mf.MultiChannel.MatchedFilter()
+    f.initialize(p)
+    for i, s in enumerate(sigs):
+        f.set_signal(i, s)
+    f.apply()
+    for i in range(3):
+        r = f.get_matched_filtered_signal(i)
+        ref = oracle.pearson_naive(tps[i], sigs[i])[: r.size]
+        assert np.max(np.abs(r - ref)) <= 1e-11
+    stack = f.shift_and_stack()
+    imax = int(np.argmax(stack))
+    assert abs(stack[imax] - 1.0) < 1e-3
+    assert abs(imax / df - 8.0) <= 1 / df / 2
+    # the same stack from the oracle's restatement of shiftAndStack
+    rows = [f.get_matched_filtered_signal(i) for i in range(3)]
+    shifts = [int((tt - to) * df + 0.5) for tt, to in zip(tts, toffs)]
+    ref_stack = oracle.shift_and_stack(rows, rows[0].size, shifts, [1, 1, 1])
+    assert np.max(np.abs(stack - ref_stack)) < 1e-14
+
+
+def test_single_channel_double(gpu, oracle, rng):
+    # testing/singleChannel.cpp:104-160 (< 1e-12)
+    mf = gpu
+    wave = rng.uniform(2, 3, 4000)
+    tps = [wave[25:155], wave[1124:1264], wave[3601:3726]]
+    f = mf.SingleChannel.MatchedFilter()
+    f.initialize(_params(mf, tps, wave.size, mode="single"))
+    f.set_signal(wave)
+    np.testing.assert_array_equal(f.get_signal(), wave)
+    f.apply()
+    for i, tp in enumerate(tps):
+        r = f.get_matched_filtered_signal(i)
+        ref = oracle.pearson_naive(tp, wave)[: r.size]
+        assert np.max(np.abs(r - ref)) < 1e-12
+
+
+def test_pymflib_multichannel(gpu, oracle):
+    # python/unit_tests.py:198-246 (< 1e-14)
+    mf = gpu
+    n = 3000
+    tmax = 8
+    f0 = 4 / tmax
+    dt = tmax / (n - 1)
+    times = np.linspace(0, tmax, n, endpoint=False)
+    s1 = np.exp(-0.1 * times) * np.sin(2 * np.pi * f0 * times)
+    s2 = np.exp(-0.15 * times) * np.cos(2 * np.pi * f0 * times)
+    nb = int(2 / dt + 0.5)
+    tt = np.linspace(0, 2, nb, endpoint=False)
+    t1 = np.sin(2 * np.pi * f0 * tt)
+    t2 = np.cos(2 * np.pi * f0 * tt)
+    f = mf.MultiChannel.MatchedFilter()
+    f.initialize(_params(mf, [t1, t2], n, fs=1 / dt))
+    f.set_signal(0, s1)
+    f.set_signal(1, s2)
+    f.apply()
+    assert np.max(np.abs(f.get_matched_filtered_signal(0) - oracle.pearson_naive(t1, s1))) < 1e-14
+    assert np.max(np.abs(f.get_matched_filtered_signal(1) - oracle.pearson_naive(t2, s2))) < 1e-14
+
+
+def test_pymflib_single_channel(gpu, oracle, rng):
+    # python/unit_tests.py:250-299 (< 1e-14)
+    mf = gpu
+    fs = 100.0
+    n = int(fs * 60 * 3) + 1
+    L = int(fs * 10) + 1
+    sig = rng.uniform(-3, 4, n)
+    tps = [sig[int(n * a):int(n * a) + L] for a in (0.25, 0.05, 0.8)]
+    f = mf.SingleChannel.MatchedFilter()
+    f.initialize(_params(mf, tps, n, mode="single", fs=fs))
+    f.set_signal(sig)
+    f.apply()
+    lags = rng.integers(0, n - L + 1, 3000)
+    for i, tp in enumerate(tps):
+        r = f.get_matched_filtered_signal(i)
+        ref = oracle.pearson_naive(tp, sig, lags)
+        assert np.max(np.abs(r[lags] - ref)) < 1e-14
+
+
+@pytest.mark.parametrize("mode", ["multi", "single"])
+@pytest.mark.parametrize("lens", [(400,), (200, 200, 200), (37, 500, 130, 999)])
+def test_fp32_vs_fp64_oracle(gpu, oracle, rng, mode, lens):
+    mf = gpu
+    n = 50_000
+    nsig = len(lens) if mode == "multi" else 1
+    sigs = [(rng.standard_normal(n) * 2 + 3).astype(np.float32) for _ in range(nsig)]
+    tps = [rng.standard_normal(L) for L in lens]
+    f = mf.MatchedFilter(dtype=np.float32)
+    p = mf.MatchedFilterParameters(0 if mode == "single" else 1)
+    for t in tps:
+        wt = mf.WaveformTemplate()
+        wt.set_signal(t)
+        wt.set_sampling_rate(100.0)
+        p.add_template(wt)
+    p.set_signal_size(n)
+    f.initialize(p)
+    for i, s in enumerate(sigs):
+        f.set_signal(i, s)
+    f.apply()
+    ref = oracle.matched_filter(tps, sigs, multi=(mode == "multi"), fp64_from_f32=True)
+    for i in range(len(tps)):
+        r = f.get_valid_matched_filtered_signal(i).astype(np.float64)
+        assert r.size == ref[i].size
+        assert np.max(np.abs(r - ref[i])) < FP32_TOL
+        short = f.get_matched_filtered_signal(i)
+        assert short.size == n - max(lens) + 1
+        np.testing.assert_array_equal(short, r[: short.size].astype(np.float32))
+
+
+@pytest.mark.parametrize("fft_length", [1024, 2048, 4096, 8192])
+def test_forced_fft_lengths(gpu, oracle, rng, fft_length):
+    mf = gpu
+    n = 30_001
+    sig = rng.standard_normal(n).astype(np.float32)
+    tps = [rng.standard_normal(300), rng.standard_normal(300)]
+    p = _params(mf, tps, n, mode="single")
+    f = mf.SingleChannel.MatchedFilter(dtype=np.float32)
+    f.initialize(p, fft_length=fft_length)
+    assert f.get_plan()["fft_length"] == fft_length
+    f.set_signal(sig)
+    f.apply()
+    ref = oracle.matched_filter(tps, [sig], multi=False, fp64_from_f32=True)
+    for i in range(2):
+        assert np.max(np.abs(f.get_valid_matched_filtered_signal(i) - ref[i])) < FP32_TOL
+
+
+def test_shared_channels_extension(gpu, oracle, rng):
+    """Several templates reading one channel (template_channels) give the
+    same coefficients as one signal copy per template."""
+    mf = gpu
+    n = 40_000
+    chans = [rng.standard_normal(n).astype(np.float32) for _ in range(3)]
+    assign = [0, 0, 1, 2, 2, 2]
+    tps = [rng.standard_normal(250) for _ in assign]
+    p = _params(mf, tps, n)
+    f = mf.MultiChannel.MatchedFilter(dtype=np.float32)
+    f.initialize(p, template_channels=assign, n_channels=3)
+    for c, s in enumerate(chans):
+        f.set_channel_signal(c, s)
+    f.apply()
+    g = mf.MultiChannel.MatchedFilter(dtype=np.float32)
+    g.initialize(p)
+    for i, c in enumerate(assign):
+        g.set_signal(i, chans[c])
+    g.apply()
+    ref = oracle.matched_filter(tps, [chans[c] for c in assign], multi=True, fp64_from_f32=True)
+    for i in range(len(assign)):
+        a = f.get_matched_filtered_signal(i)
+        np.testing.assert_array_equal(a, g.get_matched_filtered_signal(i))
+        assert np.max(np.abs(a - ref[i][: a.size])) < FP32_TOL
+
+
+def test_dc_offset_fp32(gpu, oracle, rng):
+    """A large DC offset (1e4) barely moves the FP32 engine's error: the
+    block mean is removed before the FFT and the sliding sums."""
+    mf = gpu
+    n = 60_000
+    sig = (rng.standard_normal(n) + 1e4).astype(np.float32)
+    tp = rng.standard_normal(500)
+    f = mf.SingleChannel.MatchedFilter(dtype=np.float32)
+    f.initialize(_params(mf, [tp], n, mode="single"))
+    f.set_signal(sig)
+    f.apply()
+    lags = rng.integers(0, n - 500 + 1, 2000)
+    ref = oracle.pearson_naive(tp, sig.astype(np.float64), lags)
+    r = f.get_matched_filtered_signal(0)
+    assert np.max(np.abs(r[lags] - ref)) < 5e-4
+
+
+def test_dead_and_zero_signals(gpu, rng):
+    mf = gpu
+    n = 5000
+    tps = [rng.standard_normal(100), rng.standard_normal(100)]
+    f = mf.MultiChannel.MatchedFilter()
+    f.initialize(_params(mf, tps, n))
+    f.set_signal(0, np.full(n, 3.0))        # dead: |min| == |max|
+    f.set_signal(1, rng.standard_normal(n))
+    f.apply()
+    assert np.all(f.get_matched_filtered_signal(0) == 0)
+    assert np.any(f.get_matched_filtered_signal(1) != 0)
+    f.zero_signal(1)
+    f.apply()
+    assert np.all(f.get_matched_filtered_signal(1) == 0)
+    np.testing.assert_array_equal(f.get_signal(1), np.zeros(n))
+
+
+def test_errors(gpu, rng):
+    mf = gpu
+    f = mf.MultiChannel.MatchedFilter()
+    with pytest.raises(RuntimeError):
+        f.apply()
+    with pytest.raises(RuntimeError):
+        f.get_number_of_templates()
+    tps = [rng.standard_normal(50)]
+    f.initialize(_params(mf, tps, 1000))
+    with pytest.raises(ValueError):
+        f.set_signal(1, np.zeros(1000))
+    with pytest.raises(ValueError):
+        f.set_signal(0, np.zeros(999))
+    with pytest.raises(RuntimeError):
+        f.get_matched_filtered_signal(0)
+    with pytest.raises(RuntimeError):
+        f.shift_and_stack()
+    p = mf.MultiChannel.MatchedFilterParameters()
+    with pytest.raises(ValueError):
+        f.initialize(p)
+
+
+def test_short_signal_edge(gpu, oracle, rng):
+    """Signal shorter than the longest template: the common filtered length
+    is empty; shorter templates keep their valid lags."""
+    mf = gpu
+    n = 300
+    tps = [rng.standard_normal(40), rng.standard_normal(400)]
+    f = mf.SingleChannel.MatchedFilter()
+    f.initialize(_params(mf, tps, n, mode="single"))
+    sig = rng.standard_normal(n)
+    f.set_signal(sig)
+    f.apply()
+    assert f.get_matched_filtered_signal(0).size == 0
+    r = f.get_valid_matched_filtered_signal(0)
+    assert r.size == n - 40 + 1
+    assert np.max(np.abs(r - oracle.pearson_naive(tps[0], sig))) < 1e-12
+    assert f.get_valid_matched_filtered_signal(1).size == 0
+
+
+def test_spectra_of_template(gpu, reference, rng):
+    """getSpectraOfTemplate is the reference's rfft of the reversed,
+    demeaned, unit-norm template at its own FFT length."""
+    mf = gpu
+    tp = rng.standard_normal(120)
+    f = mf.MultiChannel.MatchedFilter()
+    f.initialize(_params(mf, [tp], 2000))
+    spec = f.get_spectra_of_template(0)
+    nfft, _ = mf.compute_optimal_fft_and_block_length(120, 2000 + 119)
+    b = tp - tp.mean()
+    b = b[::-1] / np.linalg.norm(b)
+    ref = np.fft.rfft(b, nfft)
+    assert np.max(np.abs(spec - ref)) < 1e-12
+
+
+def test_repeat_apply_and_reinitialize(gpu, oracle, rng):
+    mf = gpu
+    n = 20_000
+    f = mf.SingleChannel.MatchedFilter(dtype=np.float32)
+    for L in (64, 700, 2500):
+        tp = rng.standard_normal(L)
+        f.initialize(_params(mf, [tp], n, mode="single"))
+        for _ in range(2):
+            sig = rng.standard_normal(n).astype(np.float32)
+            f.set_signal(sig)
+            f.apply()
+            ref = oracle.matched_filter([tp], [sig], multi=False, fp64_from_f32=True)[0]
+            assert np.max(np.abs(f.get_matched_filtered_signal(0) - ref)) < FP32_TOL

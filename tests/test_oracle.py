@@ -1,0 +1,163 @@
+"""The CPU oracle pinned against the reference's own golden vectors and
+known-answer tests (and, where it was compiled here, against the reference
+itself).  No GPU."""
+import numpy as np
+import pytest
+
+
+# FFT sizing: testing/matchedFilterParameters.cpp:14-33, :82-89; python/unit_tests.py:159
+@pytest.mark.parametrize("nb,nx,expect", [
+    (4500, 75000, (32768, 28269)),
+    (4500, 8640000, (65536, 61037)),
+    (101, 1024, (512, 412)),
+    (99, 1024, (512, 414)),
+])
+def test_fft_sizes_golden(oracle, nb, nx, expect):
+    assert oracle.fft_sizes(nb, nx) == expect
+
+
+def test_fft_sizes_errors(oracle):
+    with pytest.raises(ValueError):
+        oracle.fft_sizes(0, 10)
+    with pytest.raises(ValueError):
+        oracle.fft_sizes(10, 10)
+
+
+def test_fft_sizes_vs_reference(oracle, reference, rng):
+    for _ in range(200):
+        nb = int(rng.integers(1, 5000))
+        nx = int(rng.integers(nb + 1, 10_000_000))
+        assert oracle.fft_sizes(nb, nx) == reference.fft_sizes(nb, nx)
+
+
+def damped_case(signal_size=1000):
+    """testing/matchedFilter.cpp:63-90 (damped sine/cosine, 2 s template)."""
+    tmax = 8.0
+    dt = tmax / (signal_size - 1)
+    f0 = 4.0 / tmax
+    t = np.arange(signal_size) * dt
+    x = 2 * np.exp(-0.1 * t) * np.sin(2 * np.pi * f0 * t)
+    x2 = 2 * np.exp(-0.15 * t) * np.cos(2 * np.pi * f0 * t)
+    nb = int(2.0 / dt + 0.5) + 1
+    tb = np.arange(nb) * dt
+    return x, x2, np.sin(2 * np.pi * f0 * tb), np.cos(2 * np.pi * f0 * tb)
+
+
+def test_mf_double_known_answer(oracle):
+    # testing/matchedFilter.cpp:58-168: < 1e-13 vs the naive Pearson correlation
+    x, x2, b, b2 = damped_case()
+    out = oracle.matched_filter([b, b2, b, b2], [x, x2, x, x2], multi=True)
+    for r, tp, sg in zip(out, [b, b2, b, b2], [x, x2, x, x2]):
+        ref = oracle.pearson_naive(tp, sg)
+        assert np.max(np.abs(r - ref)) < 1e-13
+
+
+def test_mf_float_known_answer(oracle):
+    # testing/matchedFilter.cpp:172-271: < 2e-6 in float
+    x, x2, b, b2 = damped_case()
+    out = oracle.matched_filter([b, b2], [x, x2], multi=True, dtype=np.float32)
+    for r, tp, sg in zip(out, [b, b2], [x, x2]):
+        ref = oracle.pearson_naive(tp.astype(np.float32), sg.astype(np.float32))
+        assert np.max(np.abs(r.astype(np.float64) - ref)) < 2e-6
+
+
+def test_mf_single_channel_uneven(oracle, rng):
+    # testing/singleChannel.cpp:104-160 (U(2,3) signal, templates cut from it)
+    wave = rng.uniform(2, 3, 4000)
+    tps = [wave[25:155], wave[1124:1264], wave[3601:3726]]
+    out = oracle.matched_filter(tps, [wave], multi=False)
+    for r, tp in zip(out, tps):
+        assert np.max(np.abs(r - oracle.pearson_naive(tp, wave))) < 1e-12
+
+
+def test_mf_vs_reference(oracle, reference, rng):
+    for multi in (True, False):
+        sig = [rng.standard_normal(3000) + 5.0 for _ in range(3 if multi else 1)]
+        tps = [rng.standard_normal(L) for L in (90, 150, 200)]
+        a = oracle.matched_filter(tps, sig, multi=multi)
+        b = reference.matched_filter(tps, sig, multi=multi)
+        for x, y in zip(a, b):
+            assert np.max(np.abs(x - y)) < 1e-12
+        af = oracle.matched_filter(tps[:1] * 2, [s.astype(np.float32) for s in sig[:2]] if multi else
+                                   [sig[0].astype(np.float32)], multi=multi, dtype=np.float32)
+        bf = reference.matched_filter(tps[:1] * 2, [s.astype(np.float32) for s in sig[:2]] if multi else
+                                      [sig[0].astype(np.float32)], multi=multi, dtype=np.float32)
+        for x, y in zip(af, bf):
+            assert np.max(np.abs(x - y)) < 1e-5
+
+
+def gaussian_sine(tdur=4.0, dt=0.01, sigma=1.2, freq=12.0):
+    """testing/peakFinder.cpp:145-170."""
+    t0, t1 = -tdur / 2, tdur / 2
+    npts = int((t1 - t0) / dt + 0.5) + 1
+    t = t0 + np.arange(npts) * dt
+    y = np.exp(-((t / sigma) ** 2) ** 2) * np.cos(2 * np.pi * (t - t0) / tdur * freq)
+    y = y / np.max(np.abs(y))
+    y[0] = 0
+    y[-1] = 0
+    return y
+
+
+def peak_signal(n=4000):
+    """Signal layout of testing/peakFinder.cpp:38-54."""
+    tp = gaussian_sine()
+    sig = np.zeros(n)
+    ih = tp.size // 2
+    sig[: tp.size - ih] = tp[ih:]
+    for frac in (0.25, 0.5, 0.75):
+        i1 = int(n * frac) - ih
+        sig[i1:i1 + tp.size] = tp
+    i1 = n - ih
+    sig[i1:i1 + ih] = tp[1:ih + 1]
+    return sig
+
+
+PEAKS_13 = [0, 67, 1000 - 67, 1000, 1000 + 67, 2000 - 67, 2000, 2000 + 67, 3000 - 67, 3000, 3000 + 67,
+            4000 - 1 - 67, 4000 - 1]
+PEAKS_21 = [0, 33, 67, 1000 - 67, 1000 - 33, 1000, 1000 + 33, 1000 + 67, 2000 - 67, 2000 - 33, 2000, 2000 + 33,
+            2000 + 67, 3000 - 67, 3000 - 33, 3000, 3000 + 33, 3000 + 67, 4000 - 1 - 67, 4000 - 1 - 33, 4000 - 1]
+
+
+def test_peaks_golden(oracle):
+    # testing/peakFinder.cpp:16-143
+    assert oracle.peaks(np.full(4000, 0.4), 0.8, 52).size == 0
+    sig = peak_signal()
+    np.testing.assert_array_equal(oracle.peaks(sig, 0.8, int(0.5 / 0.01 + 1) + 1), PEAKS_13)
+    np.testing.assert_array_equal(oracle.peaks(sig, 0.8, 0), PEAKS_21)
+
+
+def test_peaks_vs_reference(oracle, reference, rng):
+    for _ in range(20):
+        n = int(rng.integers(2, 20000))
+        x = rng.standard_normal(n)
+        thr = float(rng.uniform(0, 1))
+        md = int(rng.integers(0, 300))
+        np.testing.assert_array_equal(oracle.peaks(x, thr, md), reference.peaks(x, thr, md))
+
+
+DBSCAN_X = np.array([[1, 2], [2, 2], [2, 2], [8, 7], [8, 8], [25, 80]], dtype=float)
+
+
+def test_dbscan_golden(oracle):
+    # testing/dbscan.cpp:8-60
+    ncl, lab = oracle.dbscan(DBSCAN_X, 3, 2)
+    assert ncl == 2
+    np.testing.assert_array_equal(lab, [0, 0, 0, 1, 1, -1])
+    ncl, lab = oracle.dbscan(DBSCAN_X[:5], 3, 2)
+    assert ncl == 2
+    np.testing.assert_array_equal(lab, [0, 0, 0, 1, 1])
+
+
+def test_dbscan_vs_sklearn(oracle, rng):
+    sk = pytest.importorskip("sklearn.cluster")
+    for nf in (1, 2, 3):
+        for _ in range(5):
+            X = rng.uniform(0, 20, (int(rng.integers(5, 300)), nf))
+            eps = float(rng.uniform(0.5, 3))
+            mo = int(rng.integers(1, 6))
+            w = rng.uniform(0.2, 2.0, X.shape[0])
+            for weights in (None, w):
+                ncl, lab = oracle.dbscan(X, eps, mo, weights)
+                ref = sk.DBSCAN(eps=eps, min_samples=mo).fit(X, sample_weight=weights).labels_
+                assert ncl == (ref.max() + 1 if ref.size else 0)
+                np.testing.assert_array_equal(lab, ref)
