@@ -159,7 +159,8 @@ mfgpu_status mfgpu_mf_find_peaks(mfgpu_mf *mf, double threshold, int min_distanc
 /* Peaks of template it (ascending lag indices). */
 mfgpu_status mfgpu_mf_get_peaks(mfgpu_mf *mf, int it, int maxn, int *dst, int *nout);
 /* Total peaks over all templates, and all of them at once: counts[nt] and
- * indices[sum counts] (template-major, ascending within a template). */
+ * indices[sum counts] (template-major, ascending within a template).
+ * indices == NULL with max_total == 0 only fills counts and *total. */
 mfgpu_status mfgpu_mf_get_all_peaks(mfgpu_mf *mf, int nt, int *counts, int max_total, int *indices,
                                     int *total);
 

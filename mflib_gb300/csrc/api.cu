@@ -838,6 +838,7 @@ mfgpu_status mfgpu_mf_get_all_peaks(mfgpu_mf *mf, int nt, int *counts, int max_t
     long long tot = mf->pk_off[mf->nt];
     if (total) *total = (int) tot;
     for (int t = 0; t < mf->nt; ++t) counts[t] = (int) (mf->pk_off[t + 1] - mf->pk_off[t]);
+    if (tot > 0 && indices == nullptr && max_total == 0) return MFGPU_OK;  // size query
     if (tot > 0)
     {
         if (!indices || max_total < tot) return fail(MFGPU_EINVAL, "indices too small");

@@ -187,7 +187,7 @@ class MatchedFilter:
         # shift-and-stack inputs exist only when every template has an onset
         # and a travel time (src/matchedFilter.cpp:577-592)
         if all(t.have_phase_onset_time() and t.have_travel_time() for t in tmpls):
-            sh = (C.c_int * nt)(*[int((t.get_phase_travel_time() - t.get_phase_onset_time())
+            sh = (C.c_int * nt)(*[int((t.get_phase_travel_time() - t.get_phase_onset_time_in_signal())
                                       * t.get_sampling_rate() + 0.5) for t in tmpls])
             w = (C.c_double * nt)(*[t.get_shift_and_stack_weight() for t in tmpls])
             p.stack_shifts = sh

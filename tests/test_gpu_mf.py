@@ -321,7 +321,7 @@ def test_short_signal_edge(gpu, oracle, rng):
     assert f.get_valid_matched_filtered_signal(1).size == 0
 
 
-def test_spectra_of_template(gpu, reference, rng):
+def test_spectra_of_template(gpu, rng):
     """getSpectraOfTemplate is the reference's rfft of the reversed,
     demeaned, unit-norm template at its own FFT length."""
     mf = gpu
