@@ -95,18 +95,6 @@ mfgpu_status fft_sizes(int nb, int nx, int *nfft, int *L)
     return MFGPU_OK;
 }
 
-template <class T> void fill_twiddles(std::vector<cx<T>> &tw)
-{
-    tw.resize(kNMax);
-    const double two_pi = 6.283185307179586476925286766559;
-    for (int k = 0; k < kNMax; ++k)
-    {
-        double a = -two_pi * (double) k / (double) kNMax;
-        tw[k].x = (T) std::cos(a);
-        tw[k].y = (T) std::sin(a);
-    }
-}
-
 }  // namespace
 
 // ============================================================================
@@ -128,7 +116,7 @@ struct mfgpu_mf
     bool ref_layout = true;
     // overlap-save plan
     int nfft = 0, log2p = 0, S = 0, nblocks = 0, ngroups = 0, maxvalid = 0;
-    bool shared_den = false;
+    bool shared_den = false, prefetch = false;
     long ldx = 0, ldr = 0;
     int dead_chunks = 1;
     // device buffers
@@ -253,7 +241,7 @@ mfgpu_status mfgpu_mf_clear(mfgpu_mf *mf)
 template <class T> static mfgpu_status mf_upload_tables(mfgpu_mf *mf)
 {
     std::vector<cx<T>> tw;
-    fill_twiddles<T>(tw);
+    twiddle_table<T>(mf->log2p, tw);
     CU(mf->tw.ensure(sizeof(cx<T>) * tw.size()));
     CU(cudaMemcpyAsync(mf->tw.p, tw.data(), sizeof(cx<T>) * tw.size(), cudaMemcpyHostToDevice, mf->stream));
     SpecParams<T> sp;
@@ -262,7 +250,7 @@ template <class T> static mfgpu_status mf_upload_tables(mfgpu_mf *mf)
     sp.tlen = mf->tlen_d.as<int>();
     sp.Bc = mf->Bc.as<cx<T>>();
     sp.ldb = (1L << mf->log2p) + 2;
-    sp.tw = mf->tw.as<cx<T>>();
+    sp.twt = mf->tw.as<cx<T>>();
     CU(launch_spectra<T>(mf->log2p, sp, mf->nt, mf->stream));
     ++mf->launches;
     return MFGPU_OK;
@@ -355,13 +343,22 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
     const int hi = mf->prec == 4 ? plan_limit_hi<float>() : plan_limit_hi<double>();
     bool all_equal = minLen == maxLen;
     mf->shared_den = all_equal;
-    auto smem_of = [&](int l2p, int S) {
-        return mf->prec == 4 ? xcorr_smem_bytes<float>(l2p, all_equal, S)
-                             : xcorr_smem_bytes<double>(l2p, all_equal, S);
+    auto smem_of = [&](int l2p, bool pf, int S) {
+        return mf->prec == 4 ? xcorr_smem_bytes<float>(l2p, all_equal, pf, S)
+                             : xcorr_smem_bytes<double>(l2p, all_equal, pf, S);
     };
-    int dev_smem = 0;
+    int dev_smem = 0, sm_smem = 0;
     CU(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, mf->dev));
+    CU(cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, mf->dev));
+    // CTAs per SM for a given shared-memory size (the register budget caps
+    // the FP32 kernels at 2 per SM for P <= 2048 and 1 above, FP64 at 1)
+    auto occupancy = [&](int l2p, size_t bytes) {
+        int cap = (mf->prec == 4 && l2p <= 11) ? 2 : 1;
+        int occ = (int) (sm_smem / (bytes + 1024));
+        return std::min(cap, occ);
+    };
     int best_l2p = -1, best_S = 0;
+    bool best_pf = false;
     double best_cost = 0;
     for (int l2p = lo; l2p <= hi; ++l2p)
     {
@@ -369,11 +366,17 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
         if (p->fft_length > 0 && p->fft_length != N) continue;
         int S = ((N - maxLen + 1) / 32) * 32;
         if (S < 32) continue;
-        if ((int) smem_of(l2p, S) > dev_smem) continue;
+        size_t b0 = smem_of(l2p, false, S), b1 = smem_of(l2p, true, S);
+        if ((int) b0 > dev_smem) continue;
+        int occ0 = occupancy(l2p, b0), occ1 = (int) b1 <= dev_smem ? occupancy(l2p, b1) : 0;
+        bool pf = occ1 >= occ0 && occ1 > 0;
+        int occ = pf ? occ1 : occ0;
+        if (occ < 1) continue;
         double nb = std::ceil((double) std::max(1, maxvalid) / S);
-        double cost = nb * N * (l2p + 1) * (1.0 + 1.15 * tpc);
-        if (best_l2p < 0 || cost < best_cost) { best_l2p = l2p; best_S = S; best_cost = cost; }
+        double cost = nb * N * (l2p + 1) * (1.0 + 1.15 * tpc) / (occ >= 2 ? 1.4 : 1.0);
+        if (best_l2p < 0 || cost < best_cost) { best_l2p = l2p; best_S = S; best_cost = cost; best_pf = pf; }
     }
+    mf->prefetch = best_pf;
     if (best_l2p < 0)
     {
         if (p->fft_length > 0)
@@ -607,11 +610,11 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
     p.tids = mf->tids.as<int>();
     p.tlen = mf->tlen_d.as<int>(); p.nvalid = mf->nvalid_d.as<int>();
     p.dead = mf->dead.as<unsigned char>();
-    p.tw = mf->tw.as<cx<T>>();
+    p.twt = mf->tw.as<cx<T>>();
     p.S = mf->S;
     p.tol = sizeof(T) == 4 ? (T) 1.e-6 : (T) 1.e-12;  // src/matchedFilter.cpp:1287 / :1115
     p.err = mf->err.as<int>();
-    CU(launch_xcorr<T>(mf->log2p, mf->shared_den, p, mf->nblocks, mf->ngroups, mf->stream));
+    CU(launch_xcorr<T>(mf->log2p, mf->shared_den, mf->prefetch, p, mf->nblocks, mf->ngroups, mf->stream));
     ++mf->launches;
     return MFGPU_OK;
 }

@@ -139,71 +139,6 @@ template <class T, int R, bool INV> __device__ __forceinline__ void dft(cx<T> *a
 }
 
 // ----------------------------------------------------------------------------
-// Stockham autosort complex FFT of P = 2^LOG2P points held in padded shared
-// memory, NT threads.  In place: each pass loads every butterfly's inputs to
-// registers, synchronises, then stores.  Twiddle table `tw` holds
-// exp(-2 pi i m / NMAX) for m in [0, NMAX); entry m*(NMAX/(Ns*R)) is
-// W_{Ns R}^m.  The transform is unnormalised.
-template <class T, int P, int NT, int R, bool INV, int NMAX>
-__device__ __forceinline__ void fft_pass(cx<T> *s, int Ns, const cx<T> *__restrict__ tw, int tid)
-{
-    constexpr int NB = P / R;
-    constexpr int BPT = (NB + NT - 1) / NT;
-    cx<T> a[BPT][R];
-#pragma unroll
-    for (int b = 0; b < BPT; ++b)
-    {
-        int q = tid + b * NT;
-        if (NB % NT == 0 || q < NB)
-        {
-#pragma unroll
-            for (int r = 0; r < R; ++r) a[b][r] = s[spad(q + r * NB)];
-        }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int b = 0; b < BPT; ++b)
-    {
-        int q = tid + b * NT;
-        if (NB % NT == 0 || q < NB)
-        {
-            int k = q & (Ns - 1);
-            if (Ns > 1)
-            {
-                int stride = NMAX / (Ns * R);
-#pragma unroll
-                for (int r = 1; r < R; ++r)
-                {
-                    cx<T> w = tw[(r * k) * stride];
-                    if (INV) w.y = -w.y;
-                    a[b][r] = cmul(a[b][r], w);
-                }
-            }
-            dft<T, R, INV>(a[b]);
-            int base = (q - k) * R + k;
-#pragma unroll
-            for (int r = 0; r < R; ++r) s[spad(base + r * Ns)] = a[b][r];
-        }
-    }
-    __syncthreads();
-}
-
-template <int L2> struct radix_of { static constexpr int value = L2 >= 4 ? 16 : (1 << L2); };
-
-template <class T, int LOG2P, int NT, bool INV, int NMAX, int DONE = 0>
-__device__ __forceinline__ void fft_passes(cx<T> *s, const cx<T> *__restrict__ tw, int tid)
-{
-    if constexpr (DONE < LOG2P)
-    {
-        constexpr int REM = LOG2P - DONE;
-        constexpr int R = radix_of<REM>::value;
-        constexpr int LR = R == 16 ? 4 : (R == 8 ? 3 : (R == 4 ? 2 : 1));
-        fft_pass<T, (1 << LOG2P), NT, R, INV, NMAX>(s, 1 << DONE, tw, tid);
-        fft_passes<T, LOG2P, NT, INV, NMAX, DONE + LR>(s, tw, tid);
-    }
-}
-
-// ----------------------------------------------------------------------------
 // Double-float ("two FP32 values") accumulation, Knuth TwoSum / FMA TwoProd.
 // Used for the sliding-window sums of x and x^2 in the FP32 path.
 struct df { float hi, lo; };

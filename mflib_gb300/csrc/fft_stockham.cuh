@@ -1,0 +1,148 @@
+// fft_stockham.cuh -- shared-memory Stockham FFT with a compile-time radix
+// plan, per-pass twiddle tables and pluggable first-pass loads / last-pass
+// stores (so pre-processing and epilogues fuse into the transform).
+#pragma once
+#include <cmath>
+#include <vector>
+#include "device_common.cuh"
+
+namespace mfgpu {
+
+// Radix plan for P = 2^LOG2P complex points: radix-16 passes, then one
+// radix-2/4/8 pass for the remainder.  Pass p has stride Ns_p = prod of the
+// earlier radices.  Twiddles of pass p >= 1 are stored as
+// table[tw_off(p) + (r-1)*Ns_p + k] = exp(-2 pi i r k / (Ns_p R_p)), k < Ns_p,
+// 1 <= r < R_p (consecutive k are contiguous: conflict-free shared loads),
+// followed by the real-FFT post-processing twiddles exp(-2 pi i k / 2P),
+// k = 0..P/2.
+template <int LOG2P> struct FftPlan
+{
+    static constexpr int P = 1 << LOG2P;
+    static constexpr int step(int rem) { return rem >= 4 ? 4 : rem; }
+    static constexpr int npass()
+    {
+        int done = 0, n = 0;
+        while (done < LOG2P) { done += step(LOG2P - done); ++n; }
+        return n;
+    }
+    static constexpr int ns_log(int pass)
+    {
+        int done = 0;
+        for (int p = 0; p < pass; ++p) done += step(LOG2P - done);
+        return done;
+    }
+    static constexpr int radix_log(int pass) { return step(LOG2P - ns_log(pass)); }
+    static constexpr int tw_off(int pass)
+    {
+        int off = 0;
+        for (int p = 1; p < pass; ++p) off += ((1 << radix_log(p)) - 1) << ns_log(p);
+        return off;
+    }
+    static constexpr int post_off() { return tw_off(npass()); }
+    // padded to a multiple of 4 entries (16-byte multiple for TMA copies)
+    static constexpr int tw_total() { return (post_off() + P / 2 + 1 + 3) & ~3; }
+};
+
+// Host-side construction of the same table (double precision, rounded once).
+template <int LOG2P, class T> void build_twiddle_table_fixed(std::vector<cx<T>> &out)
+{
+    using PL = FftPlan<LOG2P>;
+    const double two_pi = 6.283185307179586476925286766559;
+    out.assign(PL::tw_total(), cx<T>{(T) 0, (T) 0});
+    for (int p = 1; p < PL::npass(); ++p)
+    {
+        const int R = 1 << PL::radix_log(p), NS = 1 << PL::ns_log(p);
+        for (int r = 1; r < R; ++r)
+            for (int k = 0; k < NS; ++k)
+            {
+                // exp(-2 pi i r k/(NS R)) with the phase reduced exactly in integers
+                const long long m = ((long long) r * k) % ((long long) NS * R);
+                const double a = -two_pi * (double) m / (double) (NS * R);
+                out[PL::tw_off(p) + (r - 1) * NS + k] = cx<T>{(T) std::cos(a), (T) std::sin(a)};
+            }
+    }
+    for (int k = 0; k <= PL::P / 2; ++k)
+    {
+        const double a = -two_pi * (double) k / (double) (2 * PL::P);
+        out[PL::post_off() + k] = cx<T>{(T) std::cos(a), (T) std::sin(a)};
+    }
+}
+
+template <class T, int LO = 1, int HI = 13> void build_twiddle_table(int log2p, std::vector<cx<T>> &out)
+{
+    if (log2p == LO) build_twiddle_table_fixed<LO, T>(out);
+    else if constexpr (LO < HI) build_twiddle_table<T, LO + 1, HI>(log2p, out);
+}
+
+template <class T, int LOG2P, int NT, bool INV, bool ST_BUF, int PASS, class LD, class ST>
+__device__ __forceinline__ void fft_pass_io(cx<T> *s, const cx<T> *tws, int tid, LD &ld, ST &st)
+{
+    using PL = FftPlan<LOG2P>;
+    constexpr int P = PL::P, NP = PL::npass();
+    constexpr int R = 1 << PL::radix_log(PASS), NS = 1 << PL::ns_log(PASS);
+    constexpr int NB = P / R, BPT = (NB + NT - 1) / NT;
+    constexpr bool FIRST = PASS == 0, LAST = PASS == NP - 1;
+    cx<T> a[BPT][R];
+#pragma unroll
+    for (int b = 0; b < BPT; ++b)
+    {
+        const int q = tid + b * NT;
+        if (NB % NT == 0 || q < NB)
+        {
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+            {
+                if constexpr (FIRST) a[b][r] = ld(q + r * NB);
+                else a[b][r] = s[spad(q + r * NB)];
+            }
+        }
+    }
+    if constexpr (!FIRST && (!LAST || ST_BUF)) __syncthreads();
+#pragma unroll
+    for (int b = 0; b < BPT; ++b)
+    {
+        const int q = tid + b * NT;
+        if (NB % NT == 0 || q < NB)
+        {
+            const int k = q & (NS - 1);
+            if constexpr (NS > 1)
+            {
+                const cx<T> *tp = tws + PL::tw_off(PASS) + k;
+#pragma unroll
+                for (int r = 1; r < R; ++r)
+                {
+                    cx<T> w = tp[(r - 1) * NS];
+                    if (INV) w.y = -w.y;
+                    a[b][r] = cmul(a[b][r], w);
+                }
+            }
+            dft<T, R, INV>(a[b]);
+            const int base = (q - k) * R + k;
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+            {
+                if constexpr (LAST) st(base + r * NS, a[b][r]);
+                else s[spad(base + r * NS)] = a[b][r];
+            }
+        }
+    }
+    if constexpr (!LAST) __syncthreads();
+}
+
+// Runs every pass.  The first pass reads its inputs through ld(e) (e in
+// [0, P)); the last pass hands each output element e to st(e, value).
+// ST_BUF: the last pass stores into s itself (needs the load/store barrier).
+// Intermediate results live in the padded buffer s.  The caller must make
+// sure s is free on entry; after return (with ST_BUF) the caller
+// synchronises before reading s.
+template <class T, int LOG2P, int NT, bool INV, bool ST_BUF, class LD, class ST, int PASS = 0>
+__device__ __forceinline__ void fft_run(cx<T> *s, const cx<T> *tws, int tid, LD &ld, ST &st)
+{
+    if constexpr (PASS < FftPlan<LOG2P>::npass())
+    {
+        fft_pass_io<T, LOG2P, NT, INV, ST_BUF, PASS>(s, tws, tid, ld, st);
+        fft_run<T, LOG2P, NT, INV, ST_BUF, LD, ST, PASS + 1>(s, tws, tid, ld, st);
+    }
+}
+
+}  // namespace mfgpu

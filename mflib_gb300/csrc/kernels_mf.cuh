@@ -1,14 +1,16 @@
 // kernels_mf.cuh -- matched-filter kernels (templated on the sample type).
 //
-// Design (GB300, one CTA per (signal block, channel)):
+// Design (GB300, one CTA per (signal block, channel, template group)):
 //   * Overlap-save instead of the reference's overlap-add: block b of a
 //     channel reads samples [b*S, b*S + N) and yields the S lags
 //     [b*S, b*S + S) of every template on that channel, S <= N - Lmax + 1.
 //     No block writes another block's outputs, so nothing is accumulated in
 //     HBM (the reference accumulates y[istart+i] += ... across blocks,
 //     src/matchedFilter.cpp:1093-1112).
-//   * The N-sample segment is staged into shared memory by one TMA bulk
-//     copy (cp.async.bulk + mbarrier, bounded wait).
+//   * The N-sample segment and the plan's twiddle table are staged into
+//     shared memory by TMA bulk copies (cp.async.bulk + mbarrier, bounded
+//     wait); the next template's spectrum is prefetched the same way while
+//     the current one is transformed.
 //   * The segment mean m is subtracted before both the FFT and the sliding
 //     sums.  The numerator is invariant to it (templates are zero-mean,
 //     src/matchedFilter.cpp:172-189) and so is the window variance, but the
@@ -17,13 +19,13 @@
 //     (normalizeSignal, src/matchedFilter.cpp:94-166) are accumulated in
 //     double-float for FP32 data (about 48 significant bits; GB300's FP64
 //     rate is a small fraction of its FP32 rate) and in double for FP64 data.
-//   * Forward real FFT of the segment once; per template: conj(B_t)/N
-//     multiply fused into the pre-processing of the inverse real FFT, the
-//     inverse complex FFT, and the Pearson epilogue
+//   * Forward real FFT of the segment once.  Per template the conj(B_t)/N
+//     multiply and the inverse real-FFT pre-processing are fused into the
+//     first inverse pass, and the Pearson epilogue
 //     rho = sqrt(L) num / max(tol, sqrt(max(0, L s2 - s1^2))), rho := 0 when
-//     |rho| > 1.1, written with 16-byte stores.
+//     |rho| > 1.1, is fused into the last pass (coalesced 2-lag stores).
 #pragma once
-#include "device_common.cuh"
+#include "fft_stockham.cuh"
 
 namespace mfgpu {
 
@@ -33,7 +35,7 @@ template <class T> struct XcorrParams
 {
     const T *x;               // channel signals, row stride ldx (zero padded tail)
     long ldx;
-    const cx<T> *Bc;          // conj(spectrum)/N of each template, row stride ldb
+    const cx<T> *Bc;          // conj(spectrum)/N of each template, row stride ldb = P + 2
     long ldb;
     T *rho;                   // output rows, stride ldr
     long ldr;
@@ -44,7 +46,7 @@ template <class T> struct XcorrParams
     const int *tlen;          // template lengths
     const int *nvalid;        // valid lags per template (n - L_t + 1)
     const unsigned char *dead;// dead-trace flag per channel
-    const cx<T> *tw;          // exp(-2 pi i m / NMAX) table
+    const cx<T> *twt;         // twiddle table of the plan (FftPlan layout)
     int S;                    // lags per block (multiple of 32)
     T tol;
     int *err;
@@ -57,7 +59,28 @@ template <class T> struct SpecParams
     const int *tlen;
     cx<T> *Bc;
     long ldb;
-    const cx<T> *tw;
+    const cx<T> *twt;
+};
+
+// Shared-memory carve-up of the correlator (used by host and device).
+template <class T, int LOG2P> struct XcorrLayout
+{
+    using acc = typename acc_t<T>::type;
+    static constexpr int P = 1 << LOG2P, N = 2 * P, NCH = N / 32;
+    static constexpr size_t up(size_t v) { return (v + 127) & ~size_t(127); }
+    static constexpr size_t seg = sizeof(T) * N;
+    static constexpr size_t fft = sizeof(cx<T>) * spad_size(P);
+    static constexpr size_t head = up(64 + 32 * sizeof(T) + 2 * sizeof(acc) * (NCH + 1));
+    static constexpr size_t tw = up(sizeof(cx<T>) * FftPlan<LOG2P>::tw_total());
+    static constexpr size_t brow = sizeof(cx<T>) * (P + 2);
+    static constexpr size_t xs_region(bool sd) { return up(sd ? (seg > fft ? seg : fft) : seg); }
+    static constexpr size_t off_xs = head;
+    static constexpr size_t off_A(bool sd) { return off_xs + xs_region(sd); }
+    static constexpr size_t off_W(bool sd) { return off_A(sd) + up(fft); }
+    static constexpr size_t off_tw(bool sd) { return off_A(sd) + up(fft) + (sd ? 0 : up(fft)); }
+    static constexpr size_t off_B(bool sd) { return off_tw(sd) + tw; }
+    static constexpr size_t off_invd(bool sd, bool pf) { return off_B(sd) + (pf ? 2 * up(brow) : 0); }
+    static size_t bytes(bool sd, bool pf, int S) { return off_invd(sd, pf) + sizeof(T) * (size_t) S; }
 };
 
 template <class T> __device__ __forceinline__ T block_sum(T v, T *red)
@@ -74,12 +97,37 @@ template <class T> __device__ __forceinline__ T block_sum(T v, T *red)
     return s;
 }
 
+// real-FFT post-processing in place: A[0..P-1] holds Z = FFT_P(x_even + i x_odd);
+// on return A[k] = X[k] for k = 0..P (X[P] in the spare slot spad(P)).
+template <class T, int LOG2P>
+__device__ __forceinline__ void rfft_post(cx<T> *A, const cx<T> *post, int tid)
+{
+    constexpr int P = 1 << LOG2P;
+    for (int k = tid; k <= P / 2; k += kThreads)
+    {
+        if (k == 0)
+        {
+            cx<T> z = A[0];
+            A[0] = cmk(z.x + z.y, (T) 0);
+            A[spad(P)] = cmk(z.x - z.y, (T) 0);
+            continue;
+        }
+        cx<T> zk = A[spad(k)], zp = A[spad(P - k)];
+        cx<T> E = cscale(zk + cconj(zp), (T) 0.5);
+        cx<T> D = cscale(zk - cconj(zp), (T) 0.5);
+        cx<T> O = cmk(D.y, -D.x);  // D / i
+        cx<T> wO = cmul(post[k], O);
+        A[spad(k)] = E + wO;
+        A[spad(P - k)] = cconj(E - wO);
+    }
+}
+
 // ----------------------------------------------------------------------------
 // Template spectra: demean and unit-normalise the template in FP64
 // (src/matchedFilter.cpp:168-190; the double path uses the template's own
 // length, :575), zero pad to N, forward real FFT, store conj(B)/N for
 // k = 0..P.  The template is not reversed: correlation uses conj(B).
-template <class T, int LOG2P, int NMAX>
+template <class T, int LOG2P>
 __global__ void __launch_bounds__(kThreads) template_spectra_kernel(SpecParams<T> p)
 {
     constexpr int P = 1 << LOG2P;
@@ -92,42 +140,25 @@ __global__ void __launch_bounds__(kThreads) template_spectra_kernel(SpecParams<T
     const double *b = p.tmpl + p.toff[t];
     double s = 0;
     for (int i = tid; i < L; i += kThreads) s += b[i];
-    double mean = block_sum<double>(s, red) / (double) L;
+    const double mean = block_sum<double>(s, red) / (double) L;
     double q = 0;
     for (int i = tid; i < L; i += kThreads) { double d = b[i] - mean; q += d * d; }
-    double nrm2 = block_sum<double>(q, red);
-    double inv = nrm2 > 0 ? 1.0 / sqrt(nrm2) : 0.0;
-    for (int n = tid; n < P; n += kThreads)
-    {
+    const double nrm2 = block_sum<double>(q, red);
+    const double inv = nrm2 > 0 ? 1.0 / sqrt(nrm2) : 0.0;
+    auto ld = [&](int e) -> cx<T> {
         T re = 0, im = 0;
-        if (2 * n < L) re = (T) ((b[2 * n] - mean) * inv);
-        if (2 * n + 1 < L) im = (T) ((b[2 * n + 1] - mean) * inv);
-        A[spad(n)] = cmk(re, im);
-    }
+        if (2 * e < L) re = (T) ((b[2 * e] - mean) * inv);
+        if (2 * e + 1 < L) im = (T) ((b[2 * e + 1] - mean) * inv);
+        return cmk(re, im);
+    };
+    auto st = [&](int e, cx<T> v) { A[spad(e)] = v; };
+    fft_run<T, LOG2P, kThreads, false, true>(A, p.twt, tid, ld, st);
     __syncthreads();
-    fft_passes<T, LOG2P, kThreads, false, NMAX>(A, p.tw, tid);
+    rfft_post<T, LOG2P>(A, p.twt + FftPlan<LOG2P>::post_off(), tid);
+    __syncthreads();
     const T scale = (T) (1.0 / (double) N);
     cx<T> *out = p.Bc + (long) t * p.ldb;
-    for (int k = tid; k <= P / 2; k += kThreads)
-    {
-        if (k == 0)
-        {
-            cx<T> z = A[0];
-            out[0] = cmk((z.x + z.y) * scale, (T) 0);
-            out[P] = cmk((z.x - z.y) * scale, (T) 0);
-            continue;
-        }
-        cx<T> zk = A[spad(k)], zp = A[spad(P - k)];
-        cx<T> E = cscale(zk + cconj(zp), (T) 0.5);
-        cx<T> D = cscale(zk - cconj(zp), (T) 0.5);
-        cx<T> O = cmk(D.y, -D.x);  // D / i
-        cx<T> w = p.tw[k * (NMAX / N)];
-        cx<T> wO = cmul(w, O);
-        cx<T> Xk = E + wO;
-        cx<T> Xp = cconj(E - wO);
-        out[k] = cscale(cconj(Xk), scale);
-        out[P - k] = cscale(cconj(Xp), scale);
-    }
+    for (int k = tid; k <= P; k += kThreads) out[k] = cscale(cconj(A[spad(k)]), scale);
 }
 
 // ----------------------------------------------------------------------------
@@ -247,47 +278,62 @@ __device__ __forceinline__ void seg_inv_den(SegStats<T> st, int L, int S, T tol,
     }
 }
 
-template <class T> __device__ __forceinline__ void store4(T *dst, T a, T b, T c, T d);
-template <> __device__ __forceinline__ void store4<float>(float *dst, float a, float b, float c, float d)
+template <class T> __device__ __forceinline__ void store2(T *dst, T a, T b);
+template <> __device__ __forceinline__ void store2<float>(float *dst, float a, float b)
 {
-    *reinterpret_cast<float4 *>(dst) = make_float4(a, b, c, d);
+    *reinterpret_cast<float2 *>(dst) = make_float2(a, b);
 }
-template <> __device__ __forceinline__ void store4<double>(double *dst, double a, double b, double c, double d)
+template <> __device__ __forceinline__ void store2<double>(double *dst, double a, double b)
 {
-    reinterpret_cast<double2 *>(dst)[0] = make_double2(a, b);
-    reinterpret_cast<double2 *>(dst)[1] = make_double2(c, d);
+    *reinterpret_cast<double2 *>(dst) = make_double2(a, b);
 }
 
 template <class T> __device__ __forceinline__ T clamp_rho(T v) { return fabs(v) > (T) 1.1 ? (T) 0 : v; }
 
+// Bounded wait on a TMA phase; on timeout record the error and let every
+// thread return (the caller returns when this yields false).
+__device__ __forceinline__ bool xcorr_wait(uint64_t *bar, uint32_t parity, int *err)
+{
+    bool ok = mbar_wait_bounded(bar, parity);
+    if (!__syncthreads_and(ok))
+    {
+        if (threadIdx.x == 0) atomicExch(err, KERR_TMA_TIMEOUT);
+        return false;
+    }
+    return true;
+}
+
 // ----------------------------------------------------------------------------
-// Fused overlap-save correlator: one CTA per (block, channel).
-// SHARED_DEN: every template of every channel has the same length, so the
-// normalisation is computed once per CTA and the inverse-FFT buffer reuses
-// the staged segment's shared memory (2 CTAs per SM at N = 8192 FP32).
-template <class T, int LOG2P, int NMAX, bool SHARED_DEN>
-__global__ void __launch_bounds__(kThreads, (SHARED_DEN && sizeof(T) == 4) ? 2 : 1) xcorr_kernel(XcorrParams<T> p)
+// Fused overlap-save correlator: one CTA per (block, template group).
+// SHARED_DEN: every template has the same length, so the normalisation is
+// computed once per CTA and the inverse-FFT buffer reuses the staged
+// segment's shared memory.  PREFETCH: the next template's spectrum is
+// TMA-copied into a second buffer while the current one is transformed.
+template <class T, int LOG2P, bool SHARED_DEN, bool PREFETCH>
+__global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 : 1)
+    xcorr_kernel(XcorrParams<T> p)
 {
     using Acc = acc_t<T>;
     using acc = typename Acc::type;
-    constexpr int P = 1 << LOG2P;
-    constexpr int N = 2 * P;
-    constexpr int NCH = N / 32;
+    using LY = XcorrLayout<T, LOG2P>;
+    using PL = FftPlan<LOG2P>;
+    constexpr int P = LY::P, N = LY::N, NCH = LY::NCH;
     const int tid = threadIdx.x;
     const int g = blockIdx.y;
     const int c = p.grp_chan[g];
     const long k0 = (long) blockIdx.x * p.S;
     const int S = p.S;
     const int t_begin = p.grp_tb[g], t_end = p.grp_te[g];
-    if (t_begin == t_end) return;
+    const int ntl = t_end - t_begin;
+    if (ntl <= 0) return;
 
     if (p.dead[c])
     {
         // dead trace (|min| == |max|, src/matchedFilter.cpp:886-894): rho = 0
         for (int ti = t_begin; ti < t_end; ++ti)
         {
-            int t = p.tids[ti];
-            long nv = p.nvalid[t];
+            const int t = p.tids[ti];
+            const long nv = p.nvalid[t];
             T *dst = p.rho + (long) t * p.ldr;
             for (int k = tid; k < S; k += kThreads)
                 if (k0 + k < nv) dst[k0 + k] = (T) 0;
@@ -295,133 +341,131 @@ __global__ void __launch_bounds__(kThreads, (SHARED_DEN && sizeof(T) == 4) ? 2 :
         return;
     }
 
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    unsigned char *sp = smem_raw;
-    uint64_t *bar = reinterpret_cast<uint64_t *>(sp); sp += 16;
-    T *red = reinterpret_cast<T *>(sp); sp += 32 * sizeof(T);
-    acc *c1 = reinterpret_cast<acc *>(sp); sp += sizeof(acc) * (NCH + 1);
-    acc *c2 = reinterpret_cast<acc *>(sp); sp += sizeof(acc) * (NCH + 1);
-    sp = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(sp) + 127) & ~uintptr_t(127));
-    constexpr size_t seg_bytes = sizeof(T) * N;
-    constexpr size_t fft_bytes = sizeof(cx<T>) * spad_size(P);
-    constexpr size_t xs_region = SHARED_DEN ? (seg_bytes > fft_bytes ? seg_bytes : fft_bytes) : seg_bytes;
-    T *xs = reinterpret_cast<T *>(sp); sp += (xs_region + 127) & ~size_t(127);
-    cx<T> *A = reinterpret_cast<cx<T> *>(sp); sp += (fft_bytes + 127) & ~size_t(127);
-    cx<T> *W;
-    if (SHARED_DEN) W = reinterpret_cast<cx<T> *>(xs);
-    else { W = reinterpret_cast<cx<T> *>(sp); sp += (fft_bytes + 127) & ~size_t(127); }
-    T *invd = reinterpret_cast<T *>(sp);
+    extern __shared__ __align__(128) unsigned char smem_x[];
+    uint64_t *bar = reinterpret_cast<uint64_t *>(smem_x);  // [0] segment+twiddles, [1],[2] spectra
+    T *red = reinterpret_cast<T *>(smem_x + 64);
+    acc *c1 = reinterpret_cast<acc *>(smem_x + 64 + 32 * sizeof(T));
+    acc *c2 = c1 + (NCH + 1);
+    T *xs = reinterpret_cast<T *>(smem_x + LY::off_xs);
+    cx<T> *A = reinterpret_cast<cx<T> *>(smem_x + LY::off_A(SHARED_DEN));
+    cx<T> *W = SHARED_DEN ? reinterpret_cast<cx<T> *>(xs) : reinterpret_cast<cx<T> *>(smem_x + LY::off_W(SHARED_DEN));
+    cx<T> *tws = reinterpret_cast<cx<T> *>(smem_x + LY::off_tw(SHARED_DEN));
+    cx<T> *Bs0 = reinterpret_cast<cx<T> *>(smem_x + LY::off_B(SHARED_DEN));
+    cx<T> *Bs1 = reinterpret_cast<cx<T> *>(smem_x + LY::off_B(SHARED_DEN) + LY::up(LY::brow));
+    T *invd = reinterpret_cast<T *>(smem_x + LY::off_invd(SHARED_DEN, PREFETCH));
+    const cx<T> *post = tws + PL::post_off();
+    constexpr uint32_t kTwBytes = (uint32_t) (sizeof(cx<T>) * PL::tw_total());
 
-    // ---- stage the segment with one bulk async copy
+    // ---- stage segment, twiddles and the first spectrum with bulk async copies
     if (tid == 0)
     {
-        mbar_init(bar, 1);
+        mbar_init(&bar[0], 1);
+        if (PREFETCH) { mbar_init(&bar[1], 1); mbar_init(&bar[2], 1); }
         fence_proxy_async_smem();
-        mbar_arrive_expect_tx(bar, (uint32_t) seg_bytes);
-        tma_load_1d(xs, p.x + (long) c * p.ldx + k0, (uint32_t) seg_bytes, bar);
+        mbar_arrive_expect_tx(&bar[0], (uint32_t) LY::seg + kTwBytes);
+        tma_load_1d(xs, p.x + (long) c * p.ldx + k0, (uint32_t) LY::seg, &bar[0]);
+        tma_load_1d(tws, p.twt, kTwBytes, &bar[0]);
+        if (PREFETCH)
+        {
+            mbar_arrive_expect_tx(&bar[1], (uint32_t) LY::brow);
+            tma_load_1d(Bs0, p.Bc + (long) p.tids[t_begin] * p.ldb, (uint32_t) LY::brow, &bar[1]);
+        }
     }
     __syncthreads();
-    bool ok = mbar_wait_bounded(bar, 0);
-    if (!__syncthreads_and(ok))
+    if (!xcorr_wait(&bar[0], 0, p.err))
     {
-        if (tid == 0) atomicExch(p.err, KERR_TMA_TIMEOUT);
+        if (PREFETCH) mbar_wait_bounded(&bar[1], 0);  // let the spectrum copy land before exiting
         return;
     }
 
-    // ---- segment mean
+    // ---- segment mean and sliding-window normalisation
     T s = 0;
     for (int i = tid; i < N; i += kThreads) s += xs[i];
     const T m = block_sum<T>(s, red) / (T) N;
-
     SegStats<T> st;
     st.xs = xs; st.m = m; st.c1 = c1; st.c2 = c2;
     seg_chunk_prefix<T, N>(st, tid);
     int Lcur = p.tlen[p.tids[t_begin]];
     seg_inv_den<T, N>(st, Lcur, S, p.tol, invd, tid);
 
-    // ---- forward real FFT of (x - m)
-    const cx<T> *xs2 = reinterpret_cast<const cx<T> *>(xs);
-    for (int n = tid; n < P; n += kThreads)
+    // ---- forward real FFT of (x - m), read straight from the staged segment
     {
-        cx<T> v = xs2[n];
-        A[spad(n)] = cmk(v.x - m, v.y - m);
+        const cx<T> *xs2 = reinterpret_cast<const cx<T> *>(xs);
+        auto ld = [&](int e) -> cx<T> {
+            cx<T> v = xs2[e];
+            return cmk(v.x - m, v.y - m);
+        };
+        auto stb = [&](int e, cx<T> v) { A[spad(e)] = v; };
+        fft_run<T, LOG2P, kThreads, false, true>(A, tws, tid, ld, stb);
+        __syncthreads();
+        rfft_post<T, LOG2P>(A, post, tid);
+        __syncthreads();
     }
-    __syncthreads();
-    fft_passes<T, LOG2P, kThreads, false, NMAX>(A, p.tw, tid);
-    for (int k = tid; k <= P / 2; k += kThreads)
-    {
-        if (k == 0)
-        {
-            cx<T> z = A[0];
-            A[0] = cmk(z.x + z.y, (T) 0);
-            A[spad(P)] = cmk(z.x - z.y, (T) 0);
-            continue;
-        }
-        cx<T> zk = A[spad(k)], zp = A[spad(P - k)];
-        cx<T> E = cscale(zk + cconj(zp), (T) 0.5);
-        cx<T> D = cscale(zk - cconj(zp), (T) 0.5);
-        cx<T> O = cmk(D.y, -D.x);
-        cx<T> wO = cmul(p.tw[k * (NMAX / N)], O);
-        A[spad(k)] = E + wO;
-        A[spad(P - k)] = cconj(E - wO);
-    }
-    __syncthreads();
 
-    // ---- per template: multiply, inverse FFT, normalise, store
-    for (int ti = t_begin; ti < t_end; ++ti)
+    // ---- per template: fused conj-multiply + inverse FFT + Pearson epilogue
+    for (int j = 0; j < ntl; ++j)
     {
-        const int t = p.tids[ti];
-        if (!SHARED_DEN)
+        const int t = p.tids[t_begin + j];
+        if (j > 0) __syncthreads();  // previous template finished reading W and its spectrum buffer
+        const cx<T> *B;
+        if constexpr (PREFETCH)
         {
-            int L = p.tlen[t];
+            if (tid == 0 && j + 1 < ntl)
+            {
+                fence_proxy_async_smem();
+                uint64_t *nb = &bar[1 + ((j + 1) & 1)];
+                mbar_arrive_expect_tx(nb, (uint32_t) LY::brow);
+                tma_load_1d(((j + 1) & 1) ? Bs1 : Bs0, p.Bc + (long) p.tids[t_begin + j + 1] * p.ldb,
+                            (uint32_t) LY::brow, nb);
+            }
+            if (!xcorr_wait(&bar[1 + (j & 1)], (uint32_t) ((j >> 1) & 1), p.err))
+            {
+                if (j + 1 < ntl) mbar_wait_bounded(&bar[1 + ((j + 1) & 1)], (uint32_t) (((j + 1) >> 1) & 1));
+                return;
+            }
+            B = (j & 1) ? Bs1 : Bs0;
+        }
+        else
+        {
+            B = p.Bc + (long) t * p.ldb;
+        }
+        if constexpr (!SHARED_DEN)
+        {
+            const int L = p.tlen[t];
             if (L != Lcur)
             {
                 seg_inv_den<T, N>(st, L, S, p.tol, invd, tid);
                 Lcur = L;
+                __syncthreads();
             }
         }
-        const cx<T> *B = p.Bc + (long) t * p.ldb;
-        for (int k = tid; k <= P / 2; k += kThreads)
-        {
-            cx<T> Xk = A[spad(k)];
-            if (k == 0)
-            {
-                cx<T> XP = A[spad(P)];
-                cx<T> y0 = cmul(B[0], Xk), yP = cmul(B[P], XP);
-                cx<T> e = y0 + cconj(yP), d = y0 - cconj(yP);
-                W[0] = cmk(e.x - d.y, e.y + d.x);
-                continue;
-            }
-            cx<T> Xp = A[spad(P - k)];
-            cx<T> yk = cmul(B[k], Xk), yp = cmul(B[P - k], Xp);
-            cx<T> wk = cconj(p.tw[k * (NMAX / N)]);          // exp(+2 pi i k/N)
-            cx<T> e = yk + cconj(yp), d = cmul(yk - cconj(yp), wk);
-            W[spad(k)] = cmk(e.x - d.y, e.y + d.x);             // e + i d
-            cx<T> e2 = yp + cconj(yk), d2 = cmul(yp - cconj(yk), cmk(-wk.x, wk.y));
-            W[spad(P - k)] = cmk(e2.x - d2.y, e2.y + d2.x);
-        }
-        __syncthreads();
-        fft_passes<T, LOG2P, kThreads, true, NMAX>(W, p.tw, tid);
         const long nv = p.nvalid[t];
         T *dst = p.rho + (long) t * p.ldr + k0;
-        for (int i = tid; i < S / 4; i += kThreads)
-        {
-            const int k = 4 * i;
-            if (k0 + k >= nv) continue;
-            cx<T> w0 = W[spad(2 * i)], w1 = W[spad(2 * i + 1)];
-            T r0 = clamp_rho(w0.x * invd[k]);
-            T r1 = clamp_rho(w0.y * invd[k + 1]);
-            T r2 = clamp_rho(w1.x * invd[k + 2]);
-            T r3 = clamp_rho(w1.y * invd[k + 3]);
-            if (k0 + k + 3 < nv) store4<T>(dst + k, r0, r1, r2, r3);
-            else
+        auto pre = [&](int e) -> cx<T> {
+            if (e == 0)
             {
-                dst[k] = r0;
-                if (k0 + k + 1 < nv) dst[k + 1] = r1;
-                if (k0 + k + 2 < nv) dst[k + 2] = r2;
+                cx<T> y0 = cmul(B[0], A[0]), yP = cmul(B[P], A[spad(P)]);
+                cx<T> sm = y0 + cconj(yP), df = y0 - cconj(yP);
+                return cmk(sm.x - df.y, sm.y + df.x);
             }
-        }
-        __syncthreads();
+            cx<T> yk = cmul(B[e], A[spad(e)]), yp = cmul(B[P - e], A[spad(P - e)]);
+            cx<T> wc;  // exp(+2 pi i e / N)
+            if (e <= P / 2) wc = cconj(post[e]);
+            else { cx<T> q = post[P - e]; wc = cmk(-q.x, -q.y); }
+            cx<T> sm = yk + cconj(yp), df = cmul(yk - cconj(yp), wc);
+            return cmk(sm.x - df.y, sm.y + df.x);  // sm + i df
+        };
+        auto epi = [&](int e, cx<T> z) {
+            const int k = 2 * e;
+            if (k >= S) return;
+            const long lag = k0 + k;
+            if (lag >= nv) return;
+            const T r0 = clamp_rho(z.x * invd[k]);
+            const T r1 = clamp_rho(z.y * invd[k + 1]);
+            if (lag + 1 < nv) store2<T>(dst + k, r0, r1);
+            else dst[k] = r0;
+        };
+        fft_run<T, LOG2P, kThreads, true, false>(W, tws, tid, pre, epi);
     }
 }
 

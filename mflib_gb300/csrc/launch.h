@@ -10,18 +10,17 @@
 
 namespace mfgpu {
 
-// Largest supported twiddle table / FFT length.
-constexpr int kNMax = 16384;
-
 // Supported range of log2(N/2) for the overlap-save correlator.
 template <class T> struct fft_limits;
 template <> struct fft_limits<float> { static constexpr int lo = 5, hi = 12; };   // N = 64 .. 8192
 template <> struct fft_limits<double> { static constexpr int lo = 5, hi = 11; };  // N = 64 .. 4096
 
-template <class T> size_t xcorr_smem_bytes(int log2p, bool shared_den, int S);
-template <class T> cudaError_t launch_xcorr(int log2p, bool shared_den, const XcorrParams<T> &p, int nblocks,
-                                            int ngroups, cudaStream_t s);
+template <class T> size_t xcorr_smem_bytes(int log2p, bool shared_den, bool prefetch, int S);
+template <class T> cudaError_t launch_xcorr(int log2p, bool shared_den, bool prefetch, const XcorrParams<T> &p,
+                                            int nblocks, int ngroups, cudaStream_t s);
 template <class T> cudaError_t launch_spectra(int log2p, const SpecParams<T> &p, int nt, cudaStream_t s);
+// twiddle table of the FFT plan for P = 2^log2p (FftPlan layout)
+template <class T> void twiddle_table(int log2p, std::vector<cx<T>> &out);
 // dead-trace flag of one channel (row of n samples): two launches;
 // pmin/pmax are scratch of nchunks entries each
 template <class T> cudaError_t launch_dead(const T *x_row, long n, unsigned char *dead, T *pmin, T *pmax,

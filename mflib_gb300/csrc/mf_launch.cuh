@@ -8,46 +8,29 @@ namespace mfgpu {
 
 template <class T, int LOG2P> struct XcorrTable
 {
-    static size_t smem(bool shared_den, int S)
+    static size_t smem(bool shared_den, bool prefetch, int S)
     {
-        using acc = typename acc_t<T>::type;
-        constexpr int P = 1 << LOG2P, N = 2 * P, NCH = N / 32;
-        auto up = [](size_t v) { return (v + 127) & ~size_t(127); };
-        size_t b = 16 + 32 * sizeof(T) + 2 * sizeof(acc) * (NCH + 1);
-        b = up(b);
-        size_t seg = sizeof(T) * N, fft = sizeof(cx<T>) * spad_size(P);
-        b += up(shared_den ? (seg > fft ? seg : fft) : seg);
-        b += up(fft);
-        if (!shared_den) b += up(fft);
-        b += sizeof(T) * (size_t) S;
-        return b;
+        return XcorrLayout<T, LOG2P>::bytes(shared_den, prefetch, S);
     }
-    static cudaError_t launch(bool shared_den, const XcorrParams<T> &p, int nblocks, int ngroups, cudaStream_t s)
+    template <bool SD, bool PF> static cudaError_t go(const XcorrParams<T> &p, int nblocks, int ngroups, cudaStream_t s)
     {
-        size_t bytes = smem(shared_den, p.S);
-        dim3 grid(nblocks, ngroups);
-        cudaError_t e;
-        if (shared_den)
-        {
-            auto k = xcorr_kernel<T, LOG2P, kNMax, true>;
-            e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
-            if (e != cudaSuccess) return e;
-            k<<<grid, kThreads, bytes, s>>>(p);
-        }
-        else
-        {
-            auto k = xcorr_kernel<T, LOG2P, kNMax, false>;
-            e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
-            if (e != cudaSuccess) return e;
-            k<<<grid, kThreads, bytes, s>>>(p);
-        }
+        size_t bytes = smem(SD, PF, p.S);
+        auto k = xcorr_kernel<T, LOG2P, SD, PF>;
+        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+        if (e != cudaSuccess) return e;
+        k<<<dim3(nblocks, ngroups), kThreads, bytes, s>>>(p);
         return cudaGetLastError();
+    }
+    static cudaError_t launch(bool sd, bool pf, const XcorrParams<T> &p, int nblocks, int ngroups, cudaStream_t s)
+    {
+        if (sd) return pf ? go<true, true>(p, nblocks, ngroups, s) : go<true, false>(p, nblocks, ngroups, s);
+        return pf ? go<false, true>(p, nblocks, ngroups, s) : go<false, false>(p, nblocks, ngroups, s);
     }
     static cudaError_t spectra(const SpecParams<T> &p, int nt, cudaStream_t s)
     {
         constexpr int P = 1 << LOG2P;
         size_t bytes = sizeof(cx<T>) * spad_size(P) + 64 * sizeof(double);
-        auto k = template_spectra_kernel<T, LOG2P, kNMax>;
+        auto k = template_spectra_kernel<T, LOG2P>;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
         if (e != cudaSuccess) return e;
         k<<<nt, kThreads, bytes, s>>>(p);
@@ -57,16 +40,16 @@ template <class T, int LOG2P> struct XcorrTable
 
 template <class T, int LO, int HI> struct XcorrDispatch
 {
-    static size_t smem(int log2p, bool sd, int S)
+    static size_t smem(int log2p, bool sd, bool pf, int S)
     {
-        if (log2p == LO) return XcorrTable<T, LO>::smem(sd, S);
-        if constexpr (LO < HI) return XcorrDispatch<T, LO + 1, HI>::smem(log2p, sd, S);
+        if (log2p == LO) return XcorrTable<T, LO>::smem(sd, pf, S);
+        if constexpr (LO < HI) return XcorrDispatch<T, LO + 1, HI>::smem(log2p, sd, pf, S);
         return 0;
     }
-    static cudaError_t launch(int log2p, bool sd, const XcorrParams<T> &p, int nb, int ng, cudaStream_t s)
+    static cudaError_t launch(int log2p, bool sd, bool pf, const XcorrParams<T> &p, int nb, int ng, cudaStream_t s)
     {
-        if (log2p == LO) return XcorrTable<T, LO>::launch(sd, p, nb, ng, s);
-        if constexpr (LO < HI) return XcorrDispatch<T, LO + 1, HI>::launch(log2p, sd, p, nb, ng, s);
+        if (log2p == LO) return XcorrTable<T, LO>::launch(sd, pf, p, nb, ng, s);
+        if constexpr (LO < HI) return XcorrDispatch<T, LO + 1, HI>::launch(log2p, sd, pf, p, nb, ng, s);
         return cudaErrorInvalidValue;
     }
     static cudaError_t spectra(int log2p, const SpecParams<T> &p, int nt, cudaStream_t s)
@@ -77,24 +60,28 @@ template <class T, int LO, int HI> struct XcorrDispatch
     }
 };
 
-template <>
-size_t xcorr_smem_bytes<MFGPU_T>(int log2p, bool shared_den, int S)
+using Dispatch = XcorrDispatch<MFGPU_T, fft_limits<MFGPU_T>::lo, fft_limits<MFGPU_T>::hi>;
+
+template <> size_t xcorr_smem_bytes<MFGPU_T>(int log2p, bool shared_den, bool prefetch, int S)
 {
-    return XcorrDispatch<MFGPU_T, fft_limits<MFGPU_T>::lo, fft_limits<MFGPU_T>::hi>::smem(log2p, shared_den, S);
+    return Dispatch::smem(log2p, shared_den, prefetch, S);
 }
 
 template <>
-cudaError_t launch_xcorr<MFGPU_T>(int log2p, bool shared_den, const XcorrParams<MFGPU_T> &p, int nblocks,
-                                  int ngroups, cudaStream_t s)
+cudaError_t launch_xcorr<MFGPU_T>(int log2p, bool shared_den, bool prefetch, const XcorrParams<MFGPU_T> &p,
+                                  int nblocks, int ngroups, cudaStream_t s)
 {
-    return XcorrDispatch<MFGPU_T, fft_limits<MFGPU_T>::lo, fft_limits<MFGPU_T>::hi>::launch(log2p, shared_den, p,
-                                                                                        nblocks, ngroups, s);
+    return Dispatch::launch(log2p, shared_den, prefetch, p, nblocks, ngroups, s);
 }
 
-template <>
-cudaError_t launch_spectra<MFGPU_T>(int log2p, const SpecParams<MFGPU_T> &p, int nt, cudaStream_t s)
+template <> cudaError_t launch_spectra<MFGPU_T>(int log2p, const SpecParams<MFGPU_T> &p, int nt, cudaStream_t s)
 {
-    return XcorrDispatch<MFGPU_T, fft_limits<MFGPU_T>::lo, fft_limits<MFGPU_T>::hi>::spectra(log2p, p, nt, s);
+    return Dispatch::spectra(log2p, p, nt, s);
+}
+
+template <> void twiddle_table<MFGPU_T>(int log2p, std::vector<cx<MFGPU_T>> &out)
+{
+    build_twiddle_table<MFGPU_T>(log2p, out);
 }
 
 template <>
