@@ -12,10 +12,12 @@
 //   a non-core point with a core neighbour takes the smallest id among its
 //   neighbours' clusters (the first cluster to reach it); others are -1.
 //
-// Device formulation: weighted neighbour sums, union-find with atomic CAS
-// that always hooks the larger root under the smaller (so every component's
-// root is its lowest core index), exclusive scan of root flags for the ids,
-// then labels.
+// Device formulation: one warp per point scans its segment; weighted
+// neighbour sums; union-find with atomic CAS that always hooks the larger
+// root under the smaller (so every component's root is its lowest core
+// index); exclusive scan of root flags for the ids; then labels.
+// One feature: |x_i - x_j| <= eps, which equals sqrt((x_i - x_j)^2) <= eps
+// exactly in IEEE arithmetic and avoids the FP64 square root.
 #pragma once
 #include <cstdint>
 #include "kernels_util.cuh"
@@ -23,6 +25,7 @@
 namespace mfgpu {
 
 constexpr int kDbThreads = 256;
+constexpr int kDbWarps = kDbThreads / 32;
 
 struct DbParams
 {
@@ -38,6 +41,7 @@ struct DbParams
 
 __device__ __forceinline__ bool db_near(const DbParams &p, int i, int j)
 {
+    if (p.nf == 1) return fabs(p.X[i] - p.X[j]) <= p.eps;
     const double *a = p.X + (long) i * p.nf, *b = p.X + (long) j * p.nf;
     double s = 0;
     for (int f = 0; f < p.nf; ++f)
@@ -48,17 +52,23 @@ __device__ __forceinline__ bool db_near(const DbParams &p, int i, int j)
     return sqrt(s) <= p.eps;
 }
 
+// core flags: weighted neighbourhood size >= minObservations
 static __global__ void __launch_bounds__(kDbThreads) db_core_kernel(DbParams p, unsigned char *core, int *parent)
 {
-    int i = blockIdx.x * kDbThreads + threadIdx.x;
+    const int i = blockIdx.x * kDbWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (i >= p.n) return;
-    int s = p.seg_of[i];
-    int jb = p.seg_off[s], je = p.seg_off[s + 1];
+    const int s = p.seg_of[i];
+    const int jb = p.seg_off[s], je = p.seg_off[s + 1];
     double acc = 0;
-    for (int j = jb; j < je; ++j)
+    for (int j = jb + lane; j < je; j += 32)
         if (db_near(p, i, j)) acc += p.w ? p.w[j] : 1.0;
-    core[i] = acc >= p.min_obs ? 1 : 0;
-    parent[i] = i;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0)
+    {
+        core[i] = acc >= p.min_obs ? 1 : 0;
+        parent[i] = i;
+    }
 }
 
 __device__ __forceinline__ int db_find(volatile int *parent, int x)
@@ -72,28 +82,29 @@ __device__ __forceinline__ int db_find(volatile int *parent, int x)
     return x;
 }
 
+__device__ __forceinline__ void db_unite(int *parent, int a, int b)
+{
+    volatile int *vp = parent;
+    for (int guard = 0; guard < (1 << 30); ++guard)
+    {
+        a = db_find(vp, a);
+        b = db_find(vp, b);
+        if (a == b) return;
+        if (a > b) { int t = a; a = b; b = t; }
+        int old = atomicCAS(parent + b, b, a);  // hook the larger root under the smaller
+        if (old == b) return;
+        b = old;
+    }
+}
+
 static __global__ void __launch_bounds__(kDbThreads) db_union_kernel(DbParams p, const unsigned char *core, int *parent)
 {
-    int i = blockIdx.x * kDbThreads + threadIdx.x;
+    const int i = blockIdx.x * kDbWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (i >= p.n || !core[i]) return;
-    int s = p.seg_of[i];
-    int je = p.seg_off[s + 1];
-    volatile int *vp = parent;
-    for (int j = i + 1; j < je; ++j)
-    {
-        if (!core[j] || !db_near(p, i, j)) continue;
-        int a = i, b = j;
-        for (int guard = 0; guard < (1 << 30); ++guard)
-        {
-            a = db_find(vp, a);
-            b = db_find(vp, b);
-            if (a == b) break;
-            if (a > b) { int t = a; a = b; b = t; }
-            int old = atomicCAS(parent + b, b, a);  // hook larger root under smaller
-            if (old == b) break;
-            b = old;
-        }
-    }
+    const int s = p.seg_of[i];
+    const int je = p.seg_off[s + 1];
+    for (int j = i + 1 + lane; j < je; j += 32)
+        if (core[j] && db_near(p, i, j)) db_unite(parent, i, j);
 }
 
 static __global__ void db_roots_kernel(int n, const unsigned char *core, int *parent, int *is_root)
@@ -108,22 +119,32 @@ static __global__ void db_roots_kernel(int n, const unsigned char *core, int *pa
 
 // labels: core -> id of its root; border -> smallest id among core neighbours
 static __global__ void __launch_bounds__(kDbThreads) db_label_kernel(DbParams p, const unsigned char *core, const int *root,
-                                                             const long long *root_pos, int *labels)
+                                                                     const long long *root_pos, int *labels)
 {
-    int i = blockIdx.x * kDbThreads + threadIdx.x;
+    const int i = blockIdx.x * kDbWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (i >= p.n) return;
-    int s = p.seg_of[i];
-    int jb = p.seg_off[s], je = p.seg_off[s + 1];
-    long long base = root_pos[jb];
-    if (core[i]) { labels[i] = (int) (root_pos[root[i]] - base); return; }
-    long long best = -1;
-    for (int j = jb; j < je; ++j)
+    const int s = p.seg_of[i];
+    const int jb = p.seg_off[s], je = p.seg_off[s + 1];
+    const long long base = root_pos[jb];
+    if (core[i])
+    {
+        if (lane == 0) labels[i] = (int) (root_pos[root[i]] - base);
+        return;
+    }
+    long long best = 0x7fffffffffffffffLL;
+    for (int j = jb + lane; j < je; j += 32)
     {
         if (!core[j] || !db_near(p, i, j)) continue;
         long long id = root_pos[root[j]] - base;
-        if (best < 0 || id < best) best = id;
+        best = id < best ? id : best;
     }
-    labels[i] = (int) best;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        long long v = __shfl_xor_sync(0xffffffffu, best, o);
+        best = v < best ? v : best;
+    }
+    if (lane == 0) labels[i] = best == 0x7fffffffffffffffLL ? -1 : (int) best;
 }
 
 static __global__ void db_count_kernel(int nseg, const int *seg_off, const long long *root_pos, int *n_clusters)

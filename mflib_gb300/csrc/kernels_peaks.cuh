@@ -13,6 +13,11 @@
 // undecided candidates within min_distance of an accepted one are
 // rejected.  By induction on priority this accepts exactly the candidates
 // the sequential greedy pass accepts under the same total order.
+//
+// The packed candidate arrays have a host-chosen capacity `cap`; kernels
+// read the true count from device memory and never index past `cap`.  A
+// count above `cap` raises the overflow flag and the host reruns with a
+// larger capacity, so the common path needs a single synchronisation.
 #pragma once
 #include <cstdint>
 #include "kernels_util.cuh"
@@ -50,7 +55,7 @@ template <class T> __device__ __forceinline__ bool is_candidate(const T *x, int 
 // chunk's slot, and the exact count.
 template <class T>
 static __global__ void __launch_bounds__(kPkThreads) peak_cand_kernel(PeakTraces<T> tr, int nchunks, int *counts,
-                                                               int *slot_idx, T *slot_val)
+                                                                      int *slot_idx, T *slot_val)
 {
     __shared__ long long sh[32];
     const int trace = blockIdx.y, chunk = blockIdx.x;
@@ -79,11 +84,13 @@ static __global__ void __launch_bounds__(kPkThreads) peak_cand_kernel(PeakTraces
 }
 
 // Phase 3: gather the slots (or re-scan overflowed chunks) into the packed,
-// index-ordered candidate arrays.
+// index-ordered candidate arrays (entries at or beyond cap are dropped and
+// flagged).
 template <class T>
 static __global__ void __launch_bounds__(kPkThreads) peak_gather_kernel(PeakTraces<T> tr, int nchunks, const int *counts,
-                                                                 const long long *offs, const int *slot_idx,
-                                                                 const T *slot_val, int *cidx, T *cval, int *ctr)
+                                                                        const long long *offs, const int *slot_idx,
+                                                                        const T *slot_val, int *cidx, T *cval, int *ctr,
+                                                                        long long cap, int *overflow)
 {
     __shared__ long long sh[32];
     const int trace = blockIdx.y, chunk = blockIdx.x;
@@ -91,10 +98,12 @@ static __global__ void __launch_bounds__(kPkThreads) peak_gather_kernel(PeakTrac
     const int cnt = counts[slot];
     const long long off = offs[slot];
     if (cnt == 0) return;
+    if (threadIdx.x == 0 && off + cnt > cap) *overflow = 1;
     if (cnt <= kPkCap)
     {
         for (int r = threadIdx.x; r < cnt; r += kPkThreads)
         {
+            if (off + r >= cap) break;
             cidx[off + r] = slot_idx[slot * kPkCap + r];
             cval[off + r] = slot_val[slot * kPkCap + r];
             ctr[off + r] = trace;
@@ -114,9 +123,12 @@ static __global__ void __launch_bounds__(kPkThreads) peak_gather_kernel(PeakTrac
     {
         int q = __ffs(mask) - 1;
         mask &= mask - 1;
-        cidx[off + r] = i0 + q;
-        cval[off + r] = x[i0 + q];
-        ctr[off + r] = trace;
+        if (off + r < cap)
+        {
+            cidx[off + r] = i0 + q;
+            cval[off + r] = x[i0 + q];
+            ctr[off + r] = trace;
+        }
         ++r;
     }
 }
@@ -129,14 +141,23 @@ template <class T> __device__ __forceinline__ bool higher(T vj, int ij, T vg, in
     return vj > vg || (vj == vg && ij < ig);
 }
 
+__device__ __forceinline__ long long pk_count(const long long *ncand, long long cap)
+{
+    long long n = *ncand;
+    return n < cap ? n : cap;
+}
+
 // Round step 1: accept undecided candidates that have no undecided
 // higher-priority neighbour within dist.  PK_NEW counts as undecided for
 // the neighbours' tests, so the outcome does not depend on timing.
 template <class T>
-static __global__ void __launch_bounds__(kPkThreads) peak_decide_kernel(long long ncand, const int *cidx, const T *cval,
-                                                                 const int *ctr, const long long *trace_beg,
-                                                                 unsigned char *state, int dist, int *n_undecided)
+static __global__ void __launch_bounds__(kPkThreads) peak_decide_kernel(const long long *ncand_p, long long cap,
+                                                                        const int *cidx, const T *cval, const int *ctr,
+                                                                        const long long *trace_beg,
+                                                                        unsigned char *state, int dist,
+                                                                        int *n_undecided)
 {
+    const long long ncand = pk_count(ncand_p, cap);
     long long g = (long long) blockIdx.x * kPkThreads + threadIdx.x;
     if (g >= ncand) return;
     if (state[g] != PK_UNDECIDED) return;
@@ -161,11 +182,12 @@ static __global__ void __launch_bounds__(kPkThreads) peak_decide_kernel(long lon
 }
 
 // Round step 2: newly accepted candidates reject their undecided neighbours.
-template <class T>
-static __global__ void __launch_bounds__(kPkThreads) peak_suppress_kernel(long long ncand, const int *cidx, const int *ctr,
-                                                                   const long long *trace_beg, unsigned char *state,
-                                                                   int dist)
+static __global__ void __launch_bounds__(kPkThreads) peak_suppress_kernel(const long long *ncand_p, long long cap,
+                                                                          const int *cidx, const int *ctr,
+                                                                          const long long *trace_beg,
+                                                                          unsigned char *state, int dist)
 {
+    const long long ncand = pk_count(ncand_p, cap);
     long long g = (long long) blockIdx.x * kPkThreads + threadIdx.x;
     if (g >= ncand) return;
     if (state[g] != PK_NEW) return;
@@ -179,17 +201,20 @@ static __global__ void __launch_bounds__(kPkThreads) peak_suppress_kernel(long l
     state[g] = PK_ACCEPTED;
 }
 
-// accepted flag (as int) for the final compaction
-static __global__ void peak_flags_kernel(long long ncand, const unsigned char *state, int all, int *flags)
+// accepted flag (as int) for the final compaction; zero past the count
+static __global__ void peak_flags_kernel(const long long *ncand_p, long long cap, const unsigned char *state, int all,
+                                         int *flags)
 {
+    const long long ncand = pk_count(ncand_p, cap);
     long long g = (long long) blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= ncand) return;
-    flags[g] = (all || state[g] == PK_ACCEPTED) ? 1 : 0;
+    if (g >= cap) return;
+    flags[g] = (g < ncand && (all || state[g] == PK_ACCEPTED)) ? 1 : 0;
 }
 
-static __global__ void peak_compact_kernel(long long ncand, const int *flags, const long long *pos, const int *cidx,
-                                    int *peaks)
+static __global__ void peak_compact_kernel(const long long *ncand_p, long long cap, const int *flags,
+                                           const long long *pos, const int *cidx, int *peaks)
 {
+    const long long ncand = pk_count(ncand_p, cap);
     long long g = (long long) blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= ncand) return;
     if (flags[g]) peaks[pos[g]] = cidx[g];
@@ -197,19 +222,21 @@ static __global__ void peak_compact_kernel(long long ncand, const int *flags, co
 
 // per-trace peak offsets: peak_off[t] = pos[trace_beg[t]]
 static __global__ void peak_trace_offsets_kernel(int ntr, const long long *trace_beg, const long long *pos,
-                                          long long *peak_off)
+                                                 long long *peak_off)
 {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t > ntr) return;
     peak_off[t] = pos[trace_beg[t]];
 }
 
-// trace_beg[t] = offs[t * nchunks] (candidate offsets of each trace)
-static __global__ void peak_trace_beg_kernel(int ntr, int nchunks, const long long *offs, long long *trace_beg)
+// trace_beg[t] = min(offs[t * nchunks], cap): candidate offsets of each trace
+static __global__ void peak_trace_beg_kernel(int ntr, int nchunks, const long long *offs, long long cap,
+                                             long long *trace_beg)
 {
     int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t > ntr) return;
-    trace_beg[t] = offs[(long) t * nchunks];
+    long long v = offs[(long) t * nchunks];
+    trace_beg[t] = v < cap ? v : cap;
 }
 
 }  // namespace mfgpu

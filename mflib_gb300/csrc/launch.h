@@ -63,12 +63,14 @@ struct PeakWS
     DevBuf counts, offs, slot_idx, slot_val, cidx, cval, ctr, state, flags, pos, tiles, trace_beg, peak_off, peaks,
         counter, row;
     long long npeaks = 0;
+    long long cand_cap = 1 << 16;  // capacity of the packed candidate arrays
     void release()
     {
         DevBuf *all[] = {&counts, &offs, &slot_idx, &slot_val, &cidx, &cval, &ctr, &state,
                          &flags, &pos, &tiles, &trace_beg, &peak_off, &peaks, &counter, &row};
         for (DevBuf *d : all) d->release();
         npeaks = 0;
+        cand_cap = 1 << 16;
     }
 };
 

@@ -52,105 +52,107 @@ int run_peaks(const T *x, long ldx, const int *host_rows, int ntr, int len, doub
     MF_TRY(ws.offs.ensure(sizeof(long long) * (nslots + 1)));
     MF_TRY(ws.slot_idx.ensure(sizeof(int) * nslots * kPkCap));
     MF_TRY(ws.slot_val.ensure(sizeof(T) * nslots * kPkCap));
-    MF_TRY(ws.tiles.ensure(sizeof(long long) * (scan_tiles_needed((long) nslots + 1) + 8)));
-    MF_TRY(ws.counter.ensure(sizeof(int)));
+    MF_TRY(ws.counter.ensure(4 * sizeof(int)));  // [0] undecided after the last round, [1] overflow
     MF_TRY(cudaMemcpyAsync(ws.row.p, host_rows, sizeof(int) * ntr, cudaMemcpyHostToDevice, s));
+    int *undecided = ws.counter.as<int>(), *overflow = ws.counter.as<int>() + 1;
+    const long long *ncand_dev = ws.offs.as<long long>() + nslots;
 
     PeakTraces<T> tr;
     tr.x = x; tr.ldx = ldx; tr.row = ws.row.as<int>(); tr.len = len; tr.thr = (T) thr;
-    dim3 grid(nchunks, ntr);
-    peak_cand_kernel<T><<<grid, kPkThreads, 0, s>>>(tr, nchunks, ws.counts.as<int>(), ws.slot_idx.as<int>(),
-                                                    ws.slot_val.as<T>());
-    ++*launches;
-    MF_TRY(cudaGetLastError());
-    MF_TRY(device_excl_scan(ws.counts.as<int>(), (long) nslots, ws.offs.as<long long>(),
-                            ws.tiles.as<long long>(), s, launches));
-    long long ncand = 0;
-    MF_TRY(cudaMemcpyAsync(&ncand, ws.offs.as<long long>() + nslots, sizeof(long long), cudaMemcpyDeviceToHost, s));
-    MF_TRY(cudaStreamSynchronize(s));
-    MF_TRY(ws.cidx.ensure(sizeof(int) * ncand));
-    MF_TRY(ws.cval.ensure(sizeof(T) * ncand));
-    MF_TRY(ws.ctr.ensure(sizeof(int) * ncand));
-    MF_TRY(ws.state.ensure((size_t) ncand));
-    MF_TRY(ws.flags.ensure(sizeof(int) * ncand));
-    MF_TRY(ws.pos.ensure(sizeof(long long) * (ncand + 1)));
-    MF_TRY(ws.tiles.ensure(sizeof(long long) * (scan_tiles_needed((long) ncand + 1) + 8)));
-
-    peak_trace_beg_kernel<<<(ntr + 1 + 127) / 128, 128, 0, s>>>(ntr, nchunks, ws.offs.as<long long>(),
-                                                                ws.trace_beg.as<long long>());
-    ++*launches;
-    if (ncand > 0)
+    const dim3 grid(nchunks, ntr);
+    const bool prune = dist > 0;
+    for (int attempt = 0; attempt < 4; ++attempt)
     {
-        peak_gather_kernel<T><<<grid, kPkThreads, 0, s>>>(tr, nchunks, ws.counts.as<int>(), ws.offs.as<long long>(),
-                                                          ws.slot_idx.as<int>(), ws.slot_val.as<T>(),
-                                                          ws.cidx.as<int>(), ws.cval.as<T>(), ws.ctr.as<int>());
+        const long long cap = ws.cand_cap;
+        MF_TRY(ws.cidx.ensure(sizeof(int) * cap));
+        MF_TRY(ws.cval.ensure(sizeof(T) * cap));
+        MF_TRY(ws.ctr.ensure(sizeof(int) * cap));
+        MF_TRY(ws.state.ensure((size_t) cap));
+        MF_TRY(ws.flags.ensure(sizeof(int) * cap));
+        MF_TRY(ws.pos.ensure(sizeof(long long) * (cap + 1)));
+        MF_TRY(ws.peaks.ensure(sizeof(int) * cap));
+        MF_TRY(ws.tiles.ensure(sizeof(long long) * (scan_tiles_needed(std::max<long>((long) nslots, (long) cap) + 1) + 8)));
+        MF_TRY(cudaMemsetAsync(ws.counter.p, 0, 4 * sizeof(int), s));
+
+        peak_cand_kernel<T><<<grid, kPkThreads, 0, s>>>(tr, nchunks, ws.counts.as<int>(), ws.slot_idx.as<int>(),
+                                                        ws.slot_val.as<T>());
         ++*launches;
         MF_TRY(cudaGetLastError());
-    }
-    const unsigned gblocks = (unsigned) ((ncand + kPkThreads - 1) / kPkThreads);
-    const bool prune = dist > 0 && ncand > 0;
-    if (prune)
-    {
-        MF_TRY(cudaMemsetAsync(ws.state.p, PK_UNDECIDED, (size_t) ncand, s));
-        // Rounds until no candidate is left undecided; every round accepts at
-        // least the highest-priority undecided candidate of each trace, so
-        // ncand rounds always suffice.  The host checks every 4 rounds.
-        bool done = false;
-        for (long long round = 0; round <= ncand && !done; round += 4)
+        MF_TRY(device_excl_scan(ws.counts.as<int>(), (long) nslots, ws.offs.as<long long>(),
+                                ws.tiles.as<long long>(), s, launches));
+        peak_trace_beg_kernel<<<(ntr + 1 + 127) / 128, 128, 0, s>>>(ntr, nchunks, ws.offs.as<long long>(), cap,
+                                                                    ws.trace_beg.as<long long>());
+        peak_gather_kernel<T><<<grid, kPkThreads, 0, s>>>(tr, nchunks, ws.counts.as<int>(), ws.offs.as<long long>(),
+                                                          ws.slot_idx.as<int>(), ws.slot_val.as<T>(),
+                                                          ws.cidx.as<int>(), ws.cval.as<T>(), ws.ctr.as<int>(), cap,
+                                                          overflow);
+        *launches += 2;
+        MF_TRY(cudaGetLastError());
+        const unsigned gblocks = (unsigned) ((cap + kPkThreads - 1) / kPkThreads);
+        if (prune) MF_TRY(cudaMemsetAsync(ws.state.p, PK_UNDECIDED, (size_t) cap, s));
+        // Pruning rounds, checked in batches: every round accepts at least
+        // the highest-priority undecided candidate of each trace.
+        long long rounds_done = 0;
+        int left = 0;
+        long long ncand = 0;
+        int ovf = 0;
+        for (;;)
         {
-            for (int r = 0; r < 4; ++r)
+            if (prune)
             {
-                MF_TRY(cudaMemsetAsync(ws.counter.p, 0, sizeof(int), s));
-                peak_decide_kernel<T><<<gblocks, kPkThreads, 0, s>>>(ncand, ws.cidx.as<int>(), ws.cval.as<T>(),
-                                                                     ws.ctr.as<int>(), ws.trace_beg.as<long long>(),
-                                                                     ws.state.as<unsigned char>(), dist,
-                                                                     ws.counter.as<int>());
-                peak_suppress_kernel<T><<<gblocks, kPkThreads, 0, s>>>(
-                    ncand, ws.cidx.as<int>(), ws.ctr.as<int>(), ws.trace_beg.as<long long>(),
-                    ws.state.as<unsigned char>(), dist);
-                *launches += 2;
+                const int batch = rounds_done == 0 ? 6 : 16;
+                for (int r = 0; r < batch; ++r)
+                {
+                    MF_TRY(cudaMemsetAsync(undecided, 0, sizeof(int), s));
+                    peak_decide_kernel<T><<<gblocks, kPkThreads, 0, s>>>(
+                        ncand_dev, cap, ws.cidx.as<int>(), ws.cval.as<T>(), ws.ctr.as<int>(),
+                        ws.trace_beg.as<long long>(), ws.state.as<unsigned char>(), dist, undecided);
+                    peak_suppress_kernel<<<gblocks, kPkThreads, 0, s>>>(ncand_dev, cap, ws.cidx.as<int>(),
+                                                                        ws.ctr.as<int>(), ws.trace_beg.as<long long>(),
+                                                                        ws.state.as<unsigned char>(), dist);
+                    *launches += 2;
+                }
+                rounds_done += batch;
+                MF_TRY(cudaGetLastError());
             }
+            peak_flags_kernel<<<gblocks, kPkThreads, 0, s>>>(ncand_dev, cap, ws.state.as<unsigned char>(),
+                                                             prune ? 0 : 1, ws.flags.as<int>());
+            ++*launches;
+            MF_TRY(device_excl_scan(ws.flags.as<int>(), (long) cap, ws.pos.as<long long>(), ws.tiles.as<long long>(),
+                                    s, launches));
+            peak_compact_kernel<<<gblocks, kPkThreads, 0, s>>>(ncand_dev, cap, ws.flags.as<int>(),
+                                                               ws.pos.as<long long>(), ws.cidx.as<int>(),
+                                                               ws.peaks.as<int>());
+            peak_trace_offsets_kernel<<<(ntr + 1 + 127) / 128, 128, 0, s>>>(ntr, ws.trace_beg.as<long long>(),
+                                                                            ws.pos.as<long long>(),
+                                                                            ws.peak_off.as<long long>());
+            *launches += 2;
             MF_TRY(cudaGetLastError());
-            int left = 0;
-            MF_TRY(cudaMemcpyAsync(&left, ws.counter.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+            MF_TRY(cudaMemcpyAsync(host_peak_off, ws.peak_off.p, sizeof(long long) * (ntr + 1),
+                                   cudaMemcpyDeviceToHost, s));
+            MF_TRY(cudaMemcpyAsync(&ncand, ncand_dev, sizeof(long long), cudaMemcpyDeviceToHost, s));
+            MF_TRY(cudaMemcpyAsync(&left, undecided, sizeof(int), cudaMemcpyDeviceToHost, s));
+            MF_TRY(cudaMemcpyAsync(&ovf, overflow, sizeof(int), cudaMemcpyDeviceToHost, s));
             MF_TRY(cudaStreamSynchronize(s));
-            done = left == 0;
+            if (ovf || ncand > cap) break;
+            if (!prune || left == 0) break;
+            if (rounds_done > ncand + 16)
+            {
+                err = "peak pruning did not converge";
+                return -1;
+            }
         }
-        if (!done)
+        if (ovf || ncand > cap)
         {
-            err = "peak pruning did not converge";
-            return -1;
+            ws.cand_cap = std::max<long long>(2 * cap, ncand + ncand / 4 + 1024);
+            continue;
         }
+        ws.npeaks = host_peak_off[ntr];
+        return 0;
     }
-    if (ncand > 0)
-    {
-        peak_flags_kernel<<<gblocks, kPkThreads, 0, s>>>(ncand, ws.state.as<unsigned char>(), prune ? 0 : 1,
-                                                         ws.flags.as<int>());
-        ++*launches;
-    }
-    MF_TRY(device_excl_scan(ws.flags.as<int>(), (long) ncand, ws.pos.as<long long>(), ws.tiles.as<long long>(), s,
-                            launches));
-    long long npk = 0;
-    MF_TRY(cudaMemcpyAsync(&npk, ws.pos.as<long long>() + ncand, sizeof(long long), cudaMemcpyDeviceToHost, s));
-    MF_TRY(cudaStreamSynchronize(s));
-    MF_TRY(ws.peaks.ensure(sizeof(int) * npk));
-    if (ncand > 0)
-    {
-        peak_compact_kernel<<<gblocks, kPkThreads, 0, s>>>(ncand, ws.flags.as<int>(), ws.pos.as<long long>(),
-                                                           ws.cidx.as<int>(), ws.peaks.as<int>());
-        ++*launches;
-    }
-    peak_trace_offsets_kernel<<<(ntr + 1 + 127) / 128, 128, 0, s>>>(ntr, ws.trace_beg.as<long long>(),
-                                                                    ws.pos.as<long long>(),
-                                                                    ws.peak_off.as<long long>());
-    ++*launches;
-    MF_TRY(cudaGetLastError());
-    MF_TRY(cudaMemcpyAsync(host_peak_off, ws.peak_off.p, sizeof(long long) * (ntr + 1), cudaMemcpyDeviceToHost, s));
-    MF_TRY(cudaStreamSynchronize(s));
-    ws.npeaks = npk;
-    return 0;
+    err = "peak candidate capacity could not be sized";
+    return -1;
 }
-
 template int run_peaks<float>(const float *, long, const int *, int, int, double, int, PeakWS &, cudaStream_t,
                               long long *, long long *, std::string &);
 template int run_peaks<double>(const double *, long, const int *, int, int, double, int, PeakWS &, cudaStream_t,
@@ -189,16 +191,17 @@ int run_dbscan(int n, int nf, const double *X, const double *w, double eps, int 
     DbParams p;
     p.X = ws.X.as<double>(); p.nf = nf; p.w = w ? ws.w.as<double>() : nullptr; p.eps = eps;
     p.min_obs = (double) min_obs; p.seg_of = ws.seg_of.as<int>(); p.seg_off = ws.seg_off.as<int>(); p.n = n;
-    const unsigned blocks = (unsigned) ((n + kDbThreads - 1) / kDbThreads);
-    db_core_kernel<<<blocks, kDbThreads, 0, s>>>(p, ws.core.as<unsigned char>(), ws.parent.as<int>());
-    db_union_kernel<<<blocks, kDbThreads, 0, s>>>(p, ws.core.as<unsigned char>(), ws.parent.as<int>());
+    const unsigned blocks = (unsigned) ((n + kDbThreads - 1) / kDbThreads);   // one thread per point
+    const unsigned wblocks = (unsigned) ((n + kDbWarps - 1) / kDbWarps);      // one warp per point
+    db_core_kernel<<<wblocks, kDbThreads, 0, s>>>(p, ws.core.as<unsigned char>(), ws.parent.as<int>());
+    db_union_kernel<<<wblocks, kDbThreads, 0, s>>>(p, ws.core.as<unsigned char>(), ws.parent.as<int>());
     db_roots_kernel<<<blocks, kDbThreads, 0, s>>>(n, ws.core.as<unsigned char>(), ws.parent.as<int>(),
                                                   ws.is_root.as<int>());
     *launches += 3;
     MF_TRY(cudaGetLastError());
     MF_TRY(device_excl_scan(ws.is_root.as<int>(), n, ws.pos.as<long long>(), ws.tiles.as<long long>(), s,
                             launches));
-    db_label_kernel<<<blocks, kDbThreads, 0, s>>>(p, ws.core.as<unsigned char>(), ws.parent.as<int>(),
+    db_label_kernel<<<wblocks, kDbThreads, 0, s>>>(p, ws.core.as<unsigned char>(), ws.parent.as<int>(),
                                                   ws.pos.as<long long>(), ws.labels.as<int>());
     db_count_kernel<<<(nseg + 127) / 128, 128, 0, s>>>(nseg, ws.seg_off.as<int>(), ws.pos.as<long long>(),
                                                        ws.nclusters.as<int>());
