@@ -220,6 +220,30 @@ mfgpu_status mfgpu_dbscan_clear(mfgpu_dbscan *db);
 mfgpu_status mfgpu_dbscan_segmented(mfgpu_dbscan *db, int n_segments, const int *seg_offsets, int n_features,
                                     const double *X, const double *weights, int *labels, int *n_clusters);
 
+/* Segmented DBSCAN without any device allocation.  No counterpart in the
+ * reference: it serves callers that cannot call cudaMalloc -- a host
+ * framework that has reserved all device memory for its own pools, or a
+ * real-time pipeline that must not allocate or free (and so synchronise the
+ * device) after start-up.  Same semantics as mfgpu_dbscan_segmented, but
+ * every pointer is DEVICE memory supplied by the caller (X [n_obs x
+ * n_features] FP64 row-major, weights or NULL, seg_offsets [n_segments+1]
+ * with seg_offsets[0] = 0 and seg_offsets[n_segments] = n_obs, labels
+ * [n_obs], n_clusters [n_segments]) and the work is enqueued on `stream`
+ * (a cudaStream_t, NULL = default stream); the caller synchronises.
+ * Working memory is a fixed file-scope device array sized for at most
+ * MFGPU_DBSCAN_NOALLOC_MAX_OBS observations and
+ * MFGPU_DBSCAN_NOALLOC_MAX_SEGMENTS segments (about 1.4 MB, held on every
+ * device that loads the library until the process exits); larger requests
+ * fail with MFGPU_EINVAL.  The first call on each device looks up the
+ * array's device address; make that first call before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race, so the
+ * caller must serialise them. */
+#define MFGPU_DBSCAN_NOALLOC_MAX_OBS 65536
+#define MFGPU_DBSCAN_NOALLOC_MAX_SEGMENTS 4096
+mfgpu_status mfgpu_dbscan_segmented_noalloc(int n_segments, const int *seg_offsets, int n_obs, int n_features,
+                                            const double *X, const double *weights, double epsilon,
+                                            int min_observations, int *labels, int *n_clusters, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

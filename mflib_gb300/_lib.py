@@ -102,6 +102,8 @@ _SIGS = {
     "mfgpu_dbscan_have_labels": ([_vp, _ip], C.c_int),
     "mfgpu_dbscan_clear": ([_vp], C.c_int),
     "mfgpu_dbscan_segmented": ([_vp, C.c_int, _ip, C.c_int, _vp, _vp, _ip, _ip], C.c_int),
+    "mfgpu_dbscan_segmented_noalloc": ([C.c_int, _vp, C.c_int, C.c_int, _vp, _vp, C.c_double, C.c_int, _vp, _vp,
+                                        _vp], C.c_int),
 }
 
 

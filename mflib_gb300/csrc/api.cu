@@ -97,6 +97,8 @@ mfgpu_status fft_sizes(int nb, int nx, int *nfft, int *L)
 
 }  // namespace
 
+void mfgpu::set_last_error(const std::string &msg) { g_err = msg; }
+
 // ============================================================================
 struct mfgpu_mf
 {

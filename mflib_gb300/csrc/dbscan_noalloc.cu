@@ -1,0 +1,161 @@
+// dbscan_noalloc.cu -- segmented DBSCAN that performs no device allocation.
+//
+// Some callers cannot call cudaMalloc: a host framework that has reserved
+// every byte of device memory up front for its own pools (a serving process
+// that admits work against a fixed HBM budget, for example), or a real-time
+// pipeline that must not allocate or free after start-up because
+// cudaMalloc/cudaFree can synchronise the whole device.  For them this entry
+// point runs the same DBSCAN kernels as mfgpu_dbscan_segmented, but all of its
+// working memory is one file-scope __device__ array of fixed size; the
+// caller supplies the inputs and outputs in device memory and a stream.
+//
+// The array is shared by every call in the process and on each device it
+// lives until the process exits.  Calls that overlap on the GPU (on
+// different streams, or from different host threads) race on it; callers
+// must serialise them.  Every kernel writes each scratch word it later reads,
+// so no clearing between calls is needed.
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include "mfgpu.h"
+#include "launch.h"
+#include "kernels_dbscan.cuh"
+
+namespace {
+
+using namespace mfgpu;
+
+constexpr int kMaxPoints = MFGPU_DBSCAN_NOALLOC_MAX_OBS;
+constexpr int kMaxSegments = MFGPU_DBSCAN_NOALLOC_MAX_SEGMENTS;
+constexpr long kTiles = (kMaxPoints + 1 + kScanTile - 1) / kScanTile + 2;
+
+// scratch layout (bytes, each part 256-byte aligned)
+constexpr size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
+constexpr size_t kOffSegOf = 0;
+constexpr size_t kOffParent = kOffSegOf + align256(sizeof(int) * kMaxPoints);
+constexpr size_t kOffIsRoot = kOffParent + align256(sizeof(int) * kMaxPoints);
+constexpr size_t kOffCore = kOffIsRoot + align256(sizeof(int) * kMaxPoints);
+constexpr size_t kOffPos = kOffCore + align256(kMaxPoints);
+constexpr size_t kOffTiles = kOffPos + align256(sizeof(long long) * (kMaxPoints + 1));
+constexpr size_t kOffSegOff = kOffTiles + align256(sizeof(long long) * kTiles);
+constexpr size_t kScratchBytes = kOffSegOff + align256(sizeof(int) * (kMaxSegments + 1));
+
+__device__ __align__(256) unsigned char g_dbscan_scratch[kScratchBytes];
+
+std::mutex g_mutex;
+void *g_scratch_addr[64] = {};
+
+// Device address of the scratch array on the current device, looked up
+// once per device (the host-side symbol is not a device address).
+cudaError_t scratch_address(void **out)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_mutex);
+    if (!g_scratch_addr[dev])
+    {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_dbscan_scratch);
+        if (e != cudaSuccess) return e;
+        g_scratch_addr[dev] = p;
+    }
+    *out = g_scratch_addr[dev];
+    return cudaSuccess;
+}
+
+// Copy of the caller's offsets forced into a valid partition of [0, n):
+// first 0, last n, non-decreasing and clamped to [0, n], so no later kernel
+// can index outside the caller's arrays whatever the offsets hold.
+__global__ void sanitize_offsets_kernel(int n, int nseg, const int *seg_off, int *safe)
+{
+    int prev = 0;
+    safe[0] = 0;
+    for (int s = 1; s < nseg; ++s)
+    {
+        int v = seg_off[s];
+        v = v < prev ? prev : (v > n ? n : v);
+        safe[s] = v;
+        prev = v;
+    }
+    safe[nseg] = n;
+}
+
+// segment of each point by binary search over the offsets
+__global__ void seg_of_kernel(int n, int nseg, const int *seg_off, int *seg_of)
+{
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi)
+    {
+        int mid = (lo + hi + 1) >> 1;
+        if (seg_off[mid] <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    seg_of[i] = lo;
+}
+
+mfgpu_status fail(mfgpu_status s, const std::string &m)
+{
+    mfgpu::set_last_error(m);
+    return s;
+}
+
+}  // namespace
+
+mfgpu_status mfgpu_dbscan_segmented_noalloc(int n_segments, const int *d_seg_offsets, int n_obs, int n_features,
+                                            const double *d_X, const double *d_weights, double epsilon,
+                                            int min_observations, int *d_labels, int *d_n_clusters, void *stream)
+{
+    if (n_segments < 1 || n_segments > kMaxSegments)
+        return fail(MFGPU_EINVAL, "n_segments = " + std::to_string(n_segments) + " must be in [1, " +
+                                      std::to_string(kMaxSegments) + "]");
+    if (n_obs < 0 || n_obs > kMaxPoints)
+        return fail(MFGPU_EINVAL, "n_obs = " + std::to_string(n_obs) + " exceeds the fixed scratch capacity of " +
+                                      std::to_string(kMaxPoints) + " observations");
+    if (n_features < 1) return fail(MFGPU_EINVAL, "No features");
+    if (epsilon < 0) return fail(MFGPU_EINVAL, "epsilon must be non-negative");
+    if (min_observations < 1) return fail(MFGPU_EINVAL, "minObservations must be positive");
+    if (!d_seg_offsets || !d_n_clusters || (n_obs > 0 && (!d_X || !d_labels)))
+        return fail(MFGPU_EINVAL, "NULL argument");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    void *base = nullptr;
+    cudaError_t e = scratch_address(&base);
+    if (e != cudaSuccess) return fail(MFGPU_ECUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    unsigned char *sb = static_cast<unsigned char *>(base);
+    int *seg_of = reinterpret_cast<int *>(sb + kOffSegOf);
+    int *parent = reinterpret_cast<int *>(sb + kOffParent);
+    int *is_root = reinterpret_cast<int *>(sb + kOffIsRoot);
+    unsigned char *core = sb + kOffCore;
+    long long *pos = reinterpret_cast<long long *>(sb + kOffPos);
+    long long *tiles = reinterpret_cast<long long *>(sb + kOffTiles);
+    int *seg_off = reinterpret_cast<int *>(sb + kOffSegOff);
+
+    if (n_obs == 0)
+    {
+        e = cudaMemsetAsync(d_n_clusters, 0, sizeof(int) * n_segments, s);
+        if (e != cudaSuccess) return fail(MFGPU_ECUDA, cudaGetErrorString(e));
+        return MFGPU_OK;
+    }
+    DbParams p;
+    p.X = d_X; p.nf = n_features; p.w = d_weights; p.eps = epsilon; p.min_obs = (double) min_observations;
+    p.seg_of = seg_of; p.seg_off = seg_off; p.n = n_obs;
+    const unsigned blocks = (unsigned) ((n_obs + kDbThreads - 1) / kDbThreads);
+    const unsigned wblocks = (unsigned) ((n_obs + kDbWarps - 1) / kDbWarps);
+    sanitize_offsets_kernel<<<1, 1, 0, s>>>(n_obs, n_segments, d_seg_offsets, seg_off);
+    seg_of_kernel<<<blocks, kDbThreads, 0, s>>>(n_obs, n_segments, seg_off, seg_of);
+    db_core_kernel<<<wblocks, kDbThreads, 0, s>>>(p, core, parent);
+    db_union_kernel<<<wblocks, kDbThreads, 0, s>>>(p, core, parent);
+    db_roots_kernel<<<blocks, kDbThreads, 0, s>>>(n_obs, core, parent, is_root);
+    const long nt = (n_obs + kScanTile - 1) / kScanTile;
+    scan_tile_sums_kernel<<<(unsigned) nt, kScanThreads, 0, s>>>(is_root, n_obs, tiles);
+    scan_tile_offsets_kernel<<<1, kScanThreads, 0, s>>>(tiles, nt);
+    scan_apply_kernel<<<(unsigned) nt, kScanThreads, 0, s>>>(is_root, n_obs, tiles, pos);
+    db_label_kernel<<<wblocks, kDbThreads, 0, s>>>(p, core, parent, pos, d_labels);
+    db_count_kernel<<<(n_segments + 127) / 128, 128, 0, s>>>(n_segments, seg_off, pos, d_n_clusters);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(MFGPU_ECUDA, cudaGetErrorString(e));
+    return MFGPU_OK;
+}

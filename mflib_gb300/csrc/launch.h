@@ -96,6 +96,9 @@ int run_dbscan(int n, int nf, const double *X, const double *w, double eps, int 
                const int *seg_off_host, int *labels_host, int *nclusters_host, DbWS &ws, cudaStream_t s,
                long long *launches, std::string &err);
 
+// message returned by mfgpu_last_error() on the calling thread
+void set_last_error(const std::string &msg);
+
 // device scan helper: out[0..n] = exclusive scan of in[0..n) (+ total)
 cudaError_t device_excl_scan(const int *in, long n, long long *out, long long *tiles, cudaStream_t s,
                              long long *launches);
