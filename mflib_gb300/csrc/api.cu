@@ -123,7 +123,9 @@ struct mfgpu_mf
     int dead_chunks = 1;
     // device buffers
     DevBuf x, rho, Bc, tw, grp_chan, grp_tb, grp_te, tids, tlen_d, nvalid_d, dead, err, tmpl_d, toff_d, pmin, pmax,
-        chan_list, stackbuf, shifts_d, weights_d, specbuf;
+        chan_list, stackbuf, shifts_d, weights_d, specbuf, den;
+    long ldd = 0;
+    int nden = 0;
     PeakWS pk;
     std::vector<long long> pk_off;
     bool have_peaks = false;
@@ -135,7 +137,7 @@ struct mfgpu_mf
     {
         DevBuf *all[] = {&x,      &rho,      &Bc,   &tw,  &grp_chan, &grp_tb, &grp_te, &tids,      &tlen_d,
                          &nvalid_d, &dead,   &err,  &tmpl_d, &toff_d, &pmin, &pmax,  &chan_list, &stackbuf,
-                         &shifts_d, &weights_d, &specbuf};
+                         &shifts_d, &weights_d, &specbuf, &den};
         for (DevBuf *d : all) d->release();
         pk.release();
     }
@@ -395,6 +397,14 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
     mf->ldx = ((long) mf->nblocks * best_S + mf->nfft + 63) / 64 * 64;
     mf->ldx = std::max<long>(mf->ldx, (n + 63) / 64 * 64);
     mf->ldr = ((long) std::max(1, maxvalid) + 63) / 64 * 64;
+    if (all_equal)
+    {
+        // per-channel normalisation rows read by the correlator (S lags per
+        // block) and written by den_kernel (kDenLags lags per CTA)
+        mf->nden = (std::max(1, maxvalid) + kDenLags - 1) / kDenLags;
+        mf->ldd = (std::max<long>((long) mf->nblocks * best_S, (long) mf->nden * kDenLags) + 63) / 64 * 64;
+        mf->ldx = std::max<long>(mf->ldx, ((long) mf->nden * kDenLags + maxLen + 63) / 64 * 64);
+    }
     // work groups: split each channel's templates so the grid has enough CTAs
     int G = std::max(1, max_tpc);
     auto count_groups = [&](int gsz) {
@@ -424,6 +434,7 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
     const size_t es = mf->esz();
     const int P = 1 << mf->log2p;
     CU(mf->x.ensure(es * (size_t) nch * mf->ldx));
+    if (all_equal) CU(mf->den.ensure(es * (size_t) nch * mf->ldd));
     CU(cudaMemsetAsync(mf->x.p, 0, mf->x.bytes, mf->stream));
     CU(mf->rho.ensure(es * (size_t) nt * mf->ldr));
     CU(cudaMemsetAsync(mf->rho.p, 0, mf->rho.bytes, mf->stream));
@@ -616,6 +627,15 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
     p.S = mf->S;
     p.tol = sizeof(T) == 4 ? (T) 1.e-6 : (T) 1.e-12;  // src/matchedFilter.cpp:1287 / :1115
     p.err = mf->err.as<int>();
+    p.den = mf->den.as<T>();
+    p.ldd = mf->ldd;
+    if (mf->shared_den)
+    {
+        CU(launch_den<T>(mf->x.as<T>(), mf->ldx, mf->maxLen, mf->den.as<T>(), mf->ldd, p.tol, mf->nden, mf->nch,
+                         mf->stream));
+        ++mf->launches;
+    }
+    CU(cudaEventRecord(mf->ev[1], mf->stream));
     CU(launch_xcorr<T>(mf->log2p, mf->shared_den, mf->prefetch, p, mf->nblocks, mf->ngroups, mf->stream));
     ++mf->launches;
     return MFGPU_OK;
@@ -629,11 +649,15 @@ mfgpu_status mfgpu_mf_apply(mfgpu_mf *mf)
     mf->have = false;
     mf->have_peaks = false;
     CU(cudaEventRecord(mf->ev[0], mf->stream));
-    CU(cudaEventRecord(mf->ev[1], mf->stream));
     if (mf->nblocks > 0)
     {
+        // records ev[1] between the normalisation and the correlator
         mfgpu_status st = mf->prec == 4 ? mf_launch_xcorr<float>(mf) : mf_launch_xcorr<double>(mf);
         if (st != MFGPU_OK) return st;
+    }
+    else
+    {
+        CU(cudaEventRecord(mf->ev[1], mf->stream));
     }
     CU(cudaEventRecord(mf->ev[2], mf->stream));
     CU(cudaEventRecord(mf->ev[3], mf->stream));
@@ -956,7 +980,8 @@ mfgpu_status mfgpu_peaks_set_signal(mfgpu_peaks *pf, int n, const void *x)
     if (n < 1) return fail(MFGPU_EINVAL, "No points in x");
     if (!x) return fail(MFGPU_EINVAL, "x is NULL");
     DeviceGuard g(pf->dev);
-    CU(pf->x.ensure((size_t) pf->prec * n));
+    // the candidate scan reads 16-sample vectors: pad to a multiple of 16
+    CU(pf->x.ensure((size_t) pf->prec * ((n + 15) / 16 * 16)));
     CU(cudaMemcpyAsync(pf->x.p, x, (size_t) pf->prec * n, cudaMemcpyHostToDevice, pf->stream));
     CU(cudaStreamSynchronize(pf->stream));
     pf->n = n;

@@ -47,6 +47,8 @@ template <class T> struct XcorrParams
     const int *nvalid;        // valid lags per template (n - L_t + 1)
     const unsigned char *dead;// dead-trace flag per channel
     const cx<T> *twt;         // twiddle table of the plan (FftPlan layout)
+    const T *den;             // SHARED_DEN: sqrt(L)/max(tol, den) per channel and lag, row stride ldd
+    long ldd;
     int S;                    // lags per block (multiple of 32)
     T tol;
     int *err;
@@ -356,15 +358,18 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
     const cx<T> *post = tws + PL::post_off();
     constexpr uint32_t kTwBytes = (uint32_t) (sizeof(cx<T>) * PL::tw_total());
 
-    // ---- stage segment, twiddles and the first spectrum with bulk async copies
+    // ---- stage segment, twiddles (and, with SHARED_DEN, the block's
+    //      precomputed normalisation) and the first spectrum with bulk copies
     if (tid == 0)
     {
         mbar_init(&bar[0], 1);
         if (PREFETCH) { mbar_init(&bar[1], 1); mbar_init(&bar[2], 1); }
         fence_proxy_async_smem();
-        mbar_arrive_expect_tx(&bar[0], (uint32_t) LY::seg + kTwBytes);
+        const uint32_t den_bytes = SHARED_DEN ? (uint32_t) (sizeof(T) * S) : 0u;
+        mbar_arrive_expect_tx(&bar[0], (uint32_t) LY::seg + kTwBytes + den_bytes);
         tma_load_1d(xs, p.x + (long) c * p.ldx + k0, (uint32_t) LY::seg, &bar[0]);
         tma_load_1d(tws, p.twt, kTwBytes, &bar[0]);
+        if (SHARED_DEN) tma_load_1d(invd, p.den + (long) c * p.ldd + k0, den_bytes, &bar[0]);
         if (PREFETCH)
         {
             mbar_arrive_expect_tx(&bar[1], (uint32_t) LY::brow);
@@ -378,15 +383,19 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
         return;
     }
 
-    // ---- segment mean and sliding-window normalisation
+    // ---- segment mean; sliding-window normalisation (precomputed per
+    //      channel by den_kernel when every template shares one length)
     T s = 0;
     for (int i = tid; i < N; i += kThreads) s += xs[i];
     const T m = block_sum<T>(s, red) / (T) N;
     SegStats<T> st;
     st.xs = xs; st.m = m; st.c1 = c1; st.c2 = c2;
-    seg_chunk_prefix<T, N>(st, tid);
     int Lcur = p.tlen[p.tids[t_begin]];
-    seg_inv_den<T, N>(st, Lcur, S, p.tol, invd, tid);
+    if constexpr (!SHARED_DEN)
+    {
+        seg_chunk_prefix<T, N>(st, tid);
+        seg_inv_den<T, N>(st, Lcur, S, p.tol, invd, tid);
+    }
 
     // ---- forward real FFT of (x - m), read straight from the staged segment
     {
@@ -466,6 +475,182 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
             else dst[k] = r0;
         };
         fft_run<T, LOG2P, kThreads, true, false>(W, tws, tid, pre, epi);
+    }
+}
+
+// ----------------------------------------------------------------------------
+// Per-channel normalisation for one template length L (normalizeSignal,
+// src/matchedFilter.cpp:94-166): den[c][k] = sqrt(L)/max(tol, sqrt(max(0,
+// L s2 - s1^2))) where s1, s2 are the sums of y and y^2 over [k, k+L) and
+// y = x - m (m = mean of the CTA's samples; both sums are shift-invariant in
+// the variance).  One CTA per (8192 lags, channel): the samples are staged
+// in shared memory with one pad word per 32 (conflict-free strided access),
+// exact prefix sums are formed at multiples of 32, and thread u slides over
+// lags [32u, 32u+32) in double-float (double for FP64 data).
+constexpr int kDenRun = 32;
+constexpr int kDenLags = kThreads * kDenRun;
+constexpr int kDenMaxRunsPerLane = 16;  // supports L <= 8192
+__host__ __device__ constexpr int den_pad(int i) { return i + (i >> 5); }
+
+template <class T> struct DenLayout
+{
+    using acc = typename acc_t<T>::type;
+    static constexpr int nruns(int L) { return (kDenLags + L + kDenRun - 1) / kDenRun; }
+    static constexpr size_t y_bytes(int L)
+    {
+        return ((sizeof(T) * (size_t) (den_pad(nruns(L) * kDenRun) + 32)) + 15) & ~size_t(15);
+    }
+    static constexpr size_t bytes(int L) { return y_bytes(L) + 2 * sizeof(acc) * (size_t) (nruns(L) + 1) + 32 * sizeof(T); }
+};
+
+// Sliding update of the window sums by one lag, and the normalisation of a
+// window.  FP32 data: double-float with the "sloppy" addition (one TwoSum,
+// about 44 significant bits, enough within a 32-lag run that restarts from
+// exact prefixes) and a reciprocal square root; FP64 data: plain double.
+template <class T> struct DenSlide;
+template <> struct DenSlide<float>
+{
+    static __device__ __forceinline__ df add_sloppy(df a, df b)
+    {
+        df s = two_sum(a.hi, b.hi);
+        s.lo += a.lo + b.lo;
+        return quick_two_sum(s.hi, s.lo);
+    }
+    static __device__ __forceinline__ void step(df &w1, df &w2, float vin, float vout)
+    {
+        w1 = add_sloppy(w1, two_sum(vin, -vout));
+        df pi = two_prod(vin, vin), po = two_prod(vout, vout);
+        df d = two_sum(pi.hi, -po.hi);
+        d.lo += pi.lo - po.lo;
+        w2 = add_sloppy(w2, d);
+    }
+    // sqrt(L)/max(tol, sqrt(max(0, L w2 - w1^2)))
+    static __device__ __forceinline__ float inv(df w1, df w2, int L, float sqrtL, float tol)
+    {
+        df a = two_prod((float) L, w2.hi);
+        a.lo = fmaf((float) L, w2.lo, a.lo);
+        df b = two_prod(w1.hi, w1.hi);
+        b.lo = fmaf(2.f * w1.hi, w1.lo, b.lo);
+        df v = two_sum(a.hi, -b.hi);
+        const float var = v.hi + (v.lo + (a.lo - b.lo));
+        return var > tol * tol ? sqrtL * rsqrtf(var) : sqrtL / tol;
+    }
+};
+template <> struct DenSlide<double>
+{
+    static __device__ __forceinline__ void step(double &w1, double &w2, double vin, double vout)
+    {
+        w1 += vin - vout;
+        w2 = fma(vin, vin, fma(-vout, vout, w2));
+    }
+    static __device__ __forceinline__ double inv(double w1, double w2, int L, double sqrtL, double tol)
+    {
+        const double var = (double) L * w2 - w1 * w1;
+        return sqrtL / fmax(sqrt(fmax(var, 0.0)), tol);
+    }
+};
+
+template <class T>
+__global__ void __launch_bounds__(kThreads) den_kernel(const T *x, long ldx, int L, T *den, long ldd, T tol)
+{
+    using A = acc_t<T>;
+    using acc = typename A::type;
+    extern __shared__ __align__(16) unsigned char smem_den[];
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int c = blockIdx.y;
+    const long k0 = (long) blockIdx.x * kDenLags;
+    const int nseg = kDenLags + L;
+    const int nruns = DenLayout<T>::nruns(L);
+    T *y = reinterpret_cast<T *>(smem_den);
+    acc *r1 = reinterpret_cast<acc *>(smem_den + DenLayout<T>::y_bytes(L));
+    acc *r2 = r1 + (nruns + 1);
+    T *red = reinterpret_cast<T *>(r2 + (nruns + 1));
+    const T *xr = x + (long) c * ldx + k0;
+    T s = 0;
+    for (int i = tid; i < nruns * kDenRun; i += kThreads)
+    {
+        const T v = i < nseg ? xr[i] : (T) 0;
+        y[den_pad(i)] = v;
+        s += v;
+    }
+    const T m = block_sum<T>(s, red) / (T) nseg;
+    // sums over runs of 32 samples (run j at padded offset 33 j)
+    for (int j = tid; j < nruns; j += kThreads)
+    {
+        acc a1 = A::zero(), a2 = A::zero();
+#pragma unroll 8
+        for (int q = 0; q < kDenRun; ++q)
+        {
+            const T v = y[33 * j + q] - m;
+            a1 = A::add_val(a1, v);
+            a2 = A::add_sq(a2, v);
+        }
+        r1[j + 1] = a1;
+        r2[j + 1] = a2;
+    }
+    __syncthreads();
+    // exclusive prefix over the runs (warp 0): r[j] = sum of runs < j
+    if (tid < 32)
+    {
+        const int per = (nruns + 31) / 32;
+        acc v1[kDenMaxRunsPerLane], v2[kDenMaxRunsPerLane];
+        acc t1 = A::zero(), t2 = A::zero();
+#pragma unroll
+        for (int i = 0; i < kDenMaxRunsPerLane; ++i)
+        {
+            const int j = lane * per + i;
+            const bool ok = i < per && j < nruns;
+            v1[i] = ok ? r1[j + 1] : A::zero();
+            v2[i] = ok ? r2[j + 1] : A::zero();
+            t1 = A::add(t1, v1[i]);
+            t2 = A::add(t2, v2[i]);
+        }
+        __syncwarp();
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            acc u1 = A::shfl_up(t1, o), u2 = A::shfl_up(t2, o);
+            if (lane >= o) { t1 = A::add(t1, u1); t2 = A::add(t2, u2); }
+        }
+        acc e1 = A::shfl_up(t1, 1), e2 = A::shfl_up(t2, 1);
+        if (lane == 0) { e1 = A::zero(); e2 = A::zero(); }
+#pragma unroll
+        for (int i = 0; i < kDenMaxRunsPerLane; ++i)
+        {
+            const int j = lane * per + i;
+            if (i < per && j < nruns)
+            {
+                r1[j] = e1;
+                r2[j] = e2;
+                e1 = A::add(e1, v1[i]);
+                e2 = A::add(e2, v2[i]);
+                if (j == nruns - 1) { r1[nruns] = e1; r2[nruns] = e2; }
+            }
+        }
+    }
+    __syncthreads();
+    // thread u: lags [32u, 32u + 32); first window from the prefixes plus the
+    // L % 32 samples past the last full run
+    const int ks = kDenRun * tid;
+    const int je = tid + (L >> 5), re = L & 31;
+    acc b1 = r1[je], b2 = r2[je];
+    for (int q = 0; q < re; ++q)
+    {
+        const T v = y[33 * je + q] - m;
+        b1 = A::add_val(b1, v);
+        b2 = A::add_sq(b2, v);
+    }
+    acc w1 = A::sub(b1, r1[tid]), w2 = A::sub(b2, r2[tid]);
+    T *dr = den + (long) c * ldd + k0 + ks;
+    const T sqrtL = sqrt((T) L);
+#pragma unroll
+    for (int q = 0; q < kDenRun; q += 2)
+    {
+        const T o0 = DenSlide<T>::inv(w1, w2, L, sqrtL, tol);
+        DenSlide<T>::step(w1, w2, y[den_pad(ks + q + L)] - m, y[den_pad(ks + q)] - m);
+        const T o1 = DenSlide<T>::inv(w1, w2, L, sqrtL, tol);
+        if (q + 2 < kDenRun) DenSlide<T>::step(w1, w2, y[den_pad(ks + q + 1 + L)] - m, y[den_pad(ks + q + 1)] - m);
+        store2<T>(dr + q, o0, o1);
     }
 }
 

@@ -51,6 +51,63 @@ template <class T> __device__ __forceinline__ bool is_candidate(const T *x, int 
     return sgn<T>(xi - x[i - 1]) >= 0 && sgn<T>(x[i + 1] - xi) < 0;
 }
 
+template <class T> struct vec16;
+template <> struct vec16<float>
+{
+    static __device__ __forceinline__ void load(const float *p, float *v)
+    {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+        {
+            float4 a = reinterpret_cast<const float4 *>(p)[i];
+            v[4 * i] = a.x; v[4 * i + 1] = a.y; v[4 * i + 2] = a.z; v[4 * i + 3] = a.w;
+        }
+    }
+};
+template <> struct vec16<double>
+{
+    static __device__ __forceinline__ void load(const double *p, double *v)
+    {
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+        {
+            double2 a = reinterpret_cast<const double2 *>(p)[i];
+            v[2 * i] = a.x; v[2 * i + 1] = a.y;
+        }
+    }
+};
+
+// Candidate mask of the 16 lags [i0, i0+16) of a trace of n lags (bit q set
+// when lag i0+q is a candidate).  The 16 samples are read with 16-byte
+// loads: the trace storage must be readable up to round_up(n, 16) and
+// 16-byte aligned at every multiple of 16.
+template <class T> __device__ __forceinline__ unsigned cand_mask16(const T *x, int i0, int n, T thr)
+{
+    if (i0 >= n) return 0u;
+    T v[16];
+    vec16<T>::load(x + i0, v);
+    const T left = i0 > 0 ? x[i0 - 1] : (T) 0;
+    const T right = i0 + 16 < n ? x[i0 + 16] : (T) 0;
+    unsigned mask = 0;
+#pragma unroll
+    for (int q = 0; q < 16; ++q)
+    {
+        const int i = i0 + q;
+        if (i >= n) break;
+        const T xi = v[q];
+        if (!(xi > thr)) continue;
+        const T xl = q > 0 ? v[q - 1] : left;
+        const T xr = q < 15 ? v[q + 1] : right;
+        bool cand;
+        if (n == 1) cand = xi > (T) 0;  // reference reads x[1] out of bounds; 0 assumed
+        else if (i == 0) cand = sgn<T>(xr - xi) < 0;
+        else if (i == n - 1) cand = sgn<T>(xi - xl) > 0;
+        else cand = sgn<T>(xi - xl) >= 0 && sgn<T>(xr - xi) < 0;
+        if (cand) mask |= 1u << q;
+    }
+    return mask;
+}
+
 // Phase 1: find candidates of one chunk; write up to kPkCap of them into the
 // chunk's slot, and the exact count.
 template <class T>
@@ -62,10 +119,7 @@ static __global__ void __launch_bounds__(kPkThreads) peak_cand_kernel(PeakTraces
     const T *x = tr.x + (long) tr.row[trace] * tr.ldx;
     const int n = tr.len;
     const int i0 = chunk * kPkChunk + threadIdx.x * kPkPer;
-    unsigned mask = 0;
-#pragma unroll
-    for (int q = 0; q < kPkPer; ++q)
-        if (is_candidate<T>(x, i0 + q, n, tr.thr)) mask |= 1u << q;
+    unsigned mask = cand_mask16<T>(x, i0, n, tr.thr);
     long long tot;
     long long r = block_excl_scan((long long) __popc(mask), sh, &tot);
     const long slot = (long) trace * nchunks + chunk;
@@ -113,10 +167,7 @@ static __global__ void __launch_bounds__(kPkThreads) peak_gather_kernel(PeakTrac
     const T *x = tr.x + (long) tr.row[trace] * tr.ldx;
     const int n = tr.len;
     const int i0 = chunk * kPkChunk + threadIdx.x * kPkPer;
-    unsigned mask = 0;
-#pragma unroll
-    for (int q = 0; q < kPkPer; ++q)
-        if (is_candidate<T>(x, i0 + q, n, tr.thr)) mask |= 1u << q;
+    unsigned mask = cand_mask16<T>(x, i0, n, tr.thr);
     long long tot;
     long long r = block_excl_scan((long long) __popc(mask), sh, &tot);
     while (mask)

@@ -19,6 +19,9 @@ template <class T> size_t xcorr_smem_bytes(int log2p, bool shared_den, bool pref
 template <class T> cudaError_t launch_xcorr(int log2p, bool shared_den, bool prefetch, const XcorrParams<T> &p,
                                             int nblocks, int ngroups, cudaStream_t s);
 template <class T> cudaError_t launch_spectra(int log2p, const SpecParams<T> &p, int nt, cudaStream_t s);
+// per-channel normalisation for template length L over nblocks * kDenLags lags
+template <class T> cudaError_t launch_den(const T *x, long ldx, int L, T *den, long ldd, T tol, int nblocks, int nch,
+                                          cudaStream_t s);
 // twiddle table of the FFT plan for P = 2^log2p (FftPlan layout)
 template <class T> void twiddle_table(int log2p, std::vector<cx<T>> &out);
 // dead-trace flag of one channel (row of n samples): two launches;

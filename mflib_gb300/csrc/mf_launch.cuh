@@ -79,6 +79,18 @@ template <> cudaError_t launch_spectra<MFGPU_T>(int log2p, const SpecParams<MFGP
     return Dispatch::spectra(log2p, p, nt, s);
 }
 
+template <>
+cudaError_t launch_den<MFGPU_T>(const MFGPU_T *x, long ldx, int L, MFGPU_T *den, long ldd, MFGPU_T tol, int nblocks,
+                                int nch, cudaStream_t s)
+{
+    const size_t bytes = DenLayout<MFGPU_T>::bytes(L);
+    auto k = den_kernel<MFGPU_T>;
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+    if (e != cudaSuccess) return e;
+    k<<<dim3(nblocks, nch), kThreads, bytes, s>>>(x, ldx, L, den, ldd, tol);
+    return cudaGetLastError();
+}
+
 template <> void twiddle_table<MFGPU_T>(int log2p, std::vector<cx<MFGPU_T>> &out)
 {
     build_twiddle_table<MFGPU_T>(log2p, out);
