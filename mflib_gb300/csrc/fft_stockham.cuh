@@ -8,9 +8,14 @@
 
 namespace mfgpu {
 
-// Radix plan for P = 2^LOG2P complex points: radix-16 passes, then one
-// radix-2/4/8 pass for the remainder.  Pass p has stride Ns_p = prod of the
-// earlier radices.  Twiddles of pass p >= 1 are stored as
+// Largest radix (log2) of the plan.  Radix 16 everywhere: a radix-8 plan
+// keeps all 256 threads busy at P = 2048 but executes more instructions and
+// measured slower on GB300.
+__host__ __device__ constexpr int fft_max_radix_log(int) { return 4; }
+
+// Radix plan for P = 2^LOG2P complex points: passes of the largest radix,
+// then one smaller pass for the remainder.  Pass p has stride Ns_p = product
+// of the earlier radices.  Twiddles of pass p >= 1 are stored as
 // table[tw_off(p) + (r-1)*Ns_p + k] = exp(-2 pi i r k / (Ns_p R_p)), k < Ns_p,
 // 1 <= r < R_p (consecutive k are contiguous: conflict-free shared loads),
 // followed by the real-FFT post-processing twiddles exp(-2 pi i k / 2P),
@@ -18,7 +23,8 @@ namespace mfgpu {
 template <int LOG2P> struct FftPlan
 {
     static constexpr int P = 1 << LOG2P;
-    static constexpr int step(int rem) { return rem >= 4 ? 4 : rem; }
+    static constexpr int MAXL = fft_max_radix_log(LOG2P);
+    static constexpr int step(int rem) { return rem >= MAXL ? MAXL : rem; }
     static constexpr int npass()
     {
         int done = 0, n = 0;
@@ -74,7 +80,7 @@ template <class T, int LO = 1, int HI = 13> void build_twiddle_table(int log2p, 
     else if constexpr (LO < HI) build_twiddle_table<T, LO + 1, HI>(log2p, out);
 }
 
-template <class T, int LOG2P, int NT, bool INV, bool ST_BUF, int PASS, class LD, class ST>
+template <class T, int LOG2P, int NT, bool INV, bool ST_BUF, int PASS, class LD, class ST, bool LD_ALIAS = false>
 __device__ __forceinline__ void fft_pass_io(cx<T> *s, const cx<T> *tws, int tid, LD &ld, ST &st)
 {
     using PL = FftPlan<LOG2P>;
@@ -97,7 +103,7 @@ __device__ __forceinline__ void fft_pass_io(cx<T> *s, const cx<T> *tws, int tid,
             }
         }
     }
-    if constexpr (!FIRST && (!LAST || ST_BUF)) __syncthreads();
+    if constexpr ((!FIRST && (!LAST || ST_BUF)) || (FIRST && LD_ALIAS)) __syncthreads();
 #pragma unroll
     for (int b = 0; b < BPT; ++b)
     {
@@ -132,16 +138,17 @@ __device__ __forceinline__ void fft_pass_io(cx<T> *s, const cx<T> *tws, int tid,
 // Runs every pass.  The first pass reads its inputs through ld(e) (e in
 // [0, P)); the last pass hands each output element e to st(e, value).
 // ST_BUF: the last pass stores into s itself (needs the load/store barrier).
+// LD_ALIAS: ld reads memory that overlaps s (barrier before the first stores).
 // Intermediate results live in the padded buffer s.  The caller must make
 // sure s is free on entry; after return (with ST_BUF) the caller
 // synchronises before reading s.
-template <class T, int LOG2P, int NT, bool INV, bool ST_BUF, class LD, class ST, int PASS = 0>
+template <class T, int LOG2P, int NT, bool INV, bool ST_BUF, class LD, class ST, bool LD_ALIAS = false, int PASS = 0>
 __device__ __forceinline__ void fft_run(cx<T> *s, const cx<T> *tws, int tid, LD &ld, ST &st)
 {
     if constexpr (PASS < FftPlan<LOG2P>::npass())
     {
-        fft_pass_io<T, LOG2P, NT, INV, ST_BUF, PASS>(s, tws, tid, ld, st);
-        fft_run<T, LOG2P, NT, INV, ST_BUF, LD, ST, PASS + 1>(s, tws, tid, ld, st);
+        fft_pass_io<T, LOG2P, NT, INV, ST_BUF, PASS, LD, ST, LD_ALIAS>(s, tws, tid, ld, st);
+        fft_run<T, LOG2P, NT, INV, ST_BUF, LD, ST, LD_ALIAS, PASS + 1>(s, tws, tid, ld, st);
     }
 }
 

@@ -65,6 +65,9 @@ template <class T> struct SpecParams
 };
 
 // Shared-memory carve-up of the correlator (used by host and device).
+//   head | xs (staged segment; with SD also the FFT work buffer W) | [W] |
+//   UV (per-bin U, V pairs of the block spectrum) | pass twiddles |
+//   [2 spectrum buffers] | [invd (without SD)]
 template <class T, int LOG2P> struct XcorrLayout
 {
     using acc = typename acc_t<T>::type;
@@ -72,15 +75,16 @@ template <class T, int LOG2P> struct XcorrLayout
     static constexpr size_t up(size_t v) { return (v + 127) & ~size_t(127); }
     static constexpr size_t seg = sizeof(T) * N;
     static constexpr size_t fft = sizeof(cx<T>) * spad_size(P);
-    static constexpr size_t head = up(64 + 32 * sizeof(T) + 2 * sizeof(acc) * (NCH + 1));
-    static constexpr size_t tw = up(sizeof(cx<T>) * FftPlan<LOG2P>::tw_total());
+    static constexpr size_t head(bool sd) { return up(64 + 32 * sizeof(T) + (sd ? 0 : 2 * sizeof(acc) * (NCH + 1))); }
+    static constexpr size_t tw_bytes = sizeof(cx<T>) * FftPlan<LOG2P>::post_off();  // pass twiddles only
+    static constexpr size_t uv = sizeof(cx<T>) * 2 * P;
     static constexpr size_t brow = sizeof(cx<T>) * (P + 2);
     static constexpr size_t xs_region(bool sd) { return up(sd ? (seg > fft ? seg : fft) : seg); }
-    static constexpr size_t off_xs = head;
-    static constexpr size_t off_A(bool sd) { return off_xs + xs_region(sd); }
-    static constexpr size_t off_W(bool sd) { return off_A(sd) + up(fft); }
-    static constexpr size_t off_tw(bool sd) { return off_A(sd) + up(fft) + (sd ? 0 : up(fft)); }
-    static constexpr size_t off_B(bool sd) { return off_tw(sd) + tw; }
+    static constexpr size_t off_xs(bool sd) { return head(sd); }
+    static constexpr size_t off_W(bool sd) { return off_xs(sd) + xs_region(sd); }  // only without SD
+    static constexpr size_t off_UV(bool sd) { return off_xs(sd) + xs_region(sd) + (sd ? 0 : up(fft)); }
+    static constexpr size_t off_tw(bool sd) { return off_UV(sd) + up(uv); }
+    static constexpr size_t off_B(bool sd) { return off_tw(sd) + up(tw_bytes); }
     static constexpr size_t off_invd(bool sd, bool pf) { return off_B(sd) + (pf ? 2 * up(brow) : 0); }
     static size_t bytes(bool sd, bool pf, int S) { return off_invd(sd, pf) + sizeof(T) * (size_t) S; }
 };
@@ -292,6 +296,20 @@ template <> __device__ __forceinline__ void store2<double>(double *dst, double a
 
 template <class T> __device__ __forceinline__ T clamp_rho(T v) { return fabs(v) > (T) 1.1 ? (T) 0 : v; }
 
+// two consecutive complex values in one 16-byte shared load (FP32)
+template <class T> __device__ __forceinline__ void load_pair(const cx<T> *p, cx<T> &a, cx<T> &b);
+template <> __device__ __forceinline__ void load_pair<float>(const cx<float> *p, cx<float> &a, cx<float> &b)
+{
+    const float4 q = *reinterpret_cast<const float4 *>(p);
+    a = cmk(q.x, q.y);
+    b = cmk(q.z, q.w);
+}
+template <> __device__ __forceinline__ void load_pair<double>(const cx<double> *p, cx<double> &a, cx<double> &b)
+{
+    a = p[0];
+    b = p[1];
+}
+
 // Bounded wait on a TMA phase; on timeout record the error and let every
 // thread return (the caller returns when this yields false).
 __device__ __forceinline__ bool xcorr_wait(uint64_t *bar, uint32_t parity, int *err)
@@ -346,20 +364,19 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
     extern __shared__ __align__(128) unsigned char smem_x[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem_x);  // [0] segment+twiddles, [1],[2] spectra
     T *red = reinterpret_cast<T *>(smem_x + 64);
-    acc *c1 = reinterpret_cast<acc *>(smem_x + 64 + 32 * sizeof(T));
+    acc *c1 = reinterpret_cast<acc *>(smem_x + 64 + 32 * sizeof(T));  // only without SHARED_DEN
     acc *c2 = c1 + (NCH + 1);
-    T *xs = reinterpret_cast<T *>(smem_x + LY::off_xs);
-    cx<T> *A = reinterpret_cast<cx<T> *>(smem_x + LY::off_A(SHARED_DEN));
+    T *xs = reinterpret_cast<T *>(smem_x + LY::off_xs(SHARED_DEN));
     cx<T> *W = SHARED_DEN ? reinterpret_cast<cx<T> *>(xs) : reinterpret_cast<cx<T> *>(smem_x + LY::off_W(SHARED_DEN));
+    cx<T> *UV = reinterpret_cast<cx<T> *>(smem_x + LY::off_UV(SHARED_DEN));
     cx<T> *tws = reinterpret_cast<cx<T> *>(smem_x + LY::off_tw(SHARED_DEN));
     cx<T> *Bs0 = reinterpret_cast<cx<T> *>(smem_x + LY::off_B(SHARED_DEN));
     cx<T> *Bs1 = reinterpret_cast<cx<T> *>(smem_x + LY::off_B(SHARED_DEN) + LY::up(LY::brow));
-    T *invd = reinterpret_cast<T *>(smem_x + LY::off_invd(SHARED_DEN, PREFETCH));
-    const cx<T> *post = tws + PL::post_off();
-    constexpr uint32_t kTwBytes = (uint32_t) (sizeof(cx<T>) * PL::tw_total());
+    T *invd_s = reinterpret_cast<T *>(smem_x + LY::off_invd(SHARED_DEN, PREFETCH));
+    const cx<T> *post = p.twt + PL::post_off();  // real-FFT twiddles, read once per CTA from L2
+    constexpr uint32_t kTwBytes = (uint32_t) LY::tw_bytes;
 
-    // ---- stage segment, twiddles (and, with SHARED_DEN, the block's
-    //      precomputed normalisation) and the first spectrum with bulk copies
+    // ---- stage segment, pass twiddles and the first spectrum with bulk async copies
     if (tid == 0)
     {
         mbar_init(&bar[0], 1);
@@ -369,7 +386,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
         mbar_arrive_expect_tx(&bar[0], (uint32_t) LY::seg + kTwBytes + den_bytes);
         tma_load_1d(xs, p.x + (long) c * p.ldx + k0, (uint32_t) LY::seg, &bar[0]);
         tma_load_1d(tws, p.twt, kTwBytes, &bar[0]);
-        if (SHARED_DEN) tma_load_1d(invd, p.den + (long) c * p.ldd + k0, den_bytes, &bar[0]);
+        if (SHARED_DEN) tma_load_1d(invd_s, p.den + (long) c * p.ldd + k0, den_bytes, &bar[0]);
         if (PREFETCH)
         {
             mbar_arrive_expect_tx(&bar[1], (uint32_t) LY::brow);
@@ -394,20 +411,53 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
     if constexpr (!SHARED_DEN)
     {
         seg_chunk_prefix<T, N>(st, tid);
-        seg_inv_den<T, N>(st, Lcur, S, p.tol, invd, tid);
+        seg_inv_den<T, N>(st, Lcur, S, p.tol, invd_s, tid);
     }
 
     // ---- forward real FFT of (x - m), read straight from the staged segment
+    //      (with SHARED_DEN the work buffer overlays the segment)
     {
         const cx<T> *xs2 = reinterpret_cast<const cx<T> *>(xs);
         auto ld = [&](int e) -> cx<T> {
             cx<T> v = xs2[e];
             return cmk(v.x - m, v.y - m);
         };
-        auto stb = [&](int e, cx<T> v) { A[spad(e)] = v; };
-        fft_run<T, LOG2P, kThreads, false, true>(A, tws, tid, ld, stb);
+        auto stb = [&](int e, cx<T> v) { W[spad(e)] = v; };
+        fft_run<T, LOG2P, kThreads, false, true, decltype(ld), decltype(stb), SHARED_DEN>(W, tws, tid, ld, stb);
         __syncthreads();
-        rfft_post<T, LOG2P>(A, post, tid);
+        // Real-FFT post-processing to X[k], k = 0..P, then the per-bin pairs
+        //   U[e] = X[e] (1 + i wc_e),  V[e] = conj(X[P-e]) (1 - i wc_e),
+        // wc_e = exp(+2 pi i e/N), so that the inverse pre-processing of
+        // Y = B X becomes Z'[e] = B[e] U[e] + conj(B[P-e]) V[e].
+        for (int k = tid; k <= P / 2; k += kThreads)
+        {
+            cx<T> xk, xp;  // X[k], X[P-k]
+            if (k == 0)
+            {
+                const cx<T> z = W[0];
+                xk = cmk(z.x + z.y, (T) 0);
+                xp = cmk(z.x - z.y, (T) 0);
+            }
+            else
+            {
+                const cx<T> zk = W[spad(k)], zp = W[spad(P - k)];
+                const cx<T> E = cscale(zk + cconj(zp), (T) 0.5);
+                const cx<T> D = cscale(zk - cconj(zp), (T) 0.5);
+                const cx<T> wO = cmul(post[k], cmk(D.y, -D.x));
+                xk = E + wO;
+                xp = cconj(E - wO);
+            }
+            const cx<T> wc = cconj(post[k]);                  // exp(+2 pi i k/N)
+            const cx<T> iw = cmk(-wc.y, wc.x);                // i wc_k
+            UV[2 * k] = cmul(xk, cmk((T) 1 + iw.x, iw.y));    // U[k]
+            UV[2 * k + 1] = cmul(cconj(xp), cmk((T) 1 - iw.x, -iw.y));  // V[k]
+            if (k > 0 && k < P / 2)
+            {
+                // wc_{P-k} = -conj(wc_k), so i wc_{P-k} = (iw.x, -iw.y)
+                UV[2 * (P - k)] = cmul(xp, cmk((T) 1 + iw.x, -iw.y));
+                UV[2 * (P - k) + 1] = cmul(cconj(xk), cmk((T) 1 - iw.x, iw.y));
+            }
+        }
         __syncthreads();
     }
 
@@ -443,7 +493,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
             const int L = p.tlen[t];
             if (L != Lcur)
             {
-                seg_inv_den<T, N>(st, L, S, p.tol, invd, tid);
+                seg_inv_den<T, N>(st, L, S, p.tol, invd_s, tid);
                 Lcur = L;
                 __syncthreads();
             }
@@ -451,27 +501,23 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
         const long nv = p.nvalid[t];
         T *dst = p.rho + (long) t * p.ldr + k0;
         auto pre = [&](int e) -> cx<T> {
-            if (e == 0)
-            {
-                cx<T> y0 = cmul(B[0], A[0]), yP = cmul(B[P], A[spad(P)]);
-                cx<T> sm = y0 + cconj(yP), df = y0 - cconj(yP);
-                return cmk(sm.x - df.y, sm.y + df.x);
-            }
-            cx<T> yk = cmul(B[e], A[spad(e)]), yp = cmul(B[P - e], A[spad(P - e)]);
-            cx<T> wc;  // exp(+2 pi i e / N)
-            if (e <= P / 2) wc = cconj(post[e]);
-            else { cx<T> q = post[P - e]; wc = cmk(-q.x, -q.y); }
-            cx<T> sm = yk + cconj(yp), df = cmul(yk - cconj(yp), wc);
-            return cmk(sm.x - df.y, sm.y + df.x);  // sm + i df
+            cx<T> u, v;
+            load_pair<T>(UV + 2 * e, u, v);
+            const cx<T> b1 = B[e], b2 = B[P - e];
+            // b1 u + conj(b2) v
+            return cmk(b1.x * u.x - b1.y * u.y + b2.x * v.x + b2.y * v.y,
+                       b1.x * u.y + b1.y * u.x + b2.x * v.y - b2.y * v.x);
         };
+        // lags [k0, k0 + kmax) of this block are stored (kmax <= S, even S)
+        const int kmax = (int) (nv - k0 < (long) S ? nv - k0 : (long) S);
+        const cx<T> *invd2 = reinterpret_cast<const cx<T> *>(invd_s);
         auto epi = [&](int e, cx<T> z) {
             const int k = 2 * e;
-            if (k >= S) return;
-            const long lag = k0 + k;
-            if (lag >= nv) return;
-            const T r0 = clamp_rho(z.x * invd[k]);
-            const T r1 = clamp_rho(z.y * invd[k + 1]);
-            if (lag + 1 < nv) store2<T>(dst + k, r0, r1);
+            if (k >= kmax) return;
+            const cx<T> d = invd2[e];
+            const T r0 = clamp_rho(z.x * d.x);
+            const T r1 = clamp_rho(z.y * d.y);
+            if (k + 1 < kmax) store2<T>(dst + k, r0, r1);
             else dst[k] = r0;
         };
         fft_run<T, LOG2P, kThreads, true, false>(W, tws, tid, pre, epi);
