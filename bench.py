@@ -89,7 +89,7 @@ def make_workload(n_samples=N_SAMPLES, n_stations=N_STATIONS, n_events=N_EVENTS,
 
 
 # ---------------------------------------------------------------------------
-def build_filter(mf, w):
+def build_filter(mf, w, **kw):
     p = mf.MultiChannel.MatchedFilterParameters()
     for tp, s in zip(w["templates"], w["tshift"]):
         wt = mf.WaveformTemplate()
@@ -100,7 +100,7 @@ def build_filter(mf, w):
         p.add_template(wt)
     p.set_signal_size(w["n"])
     f = mf.MultiChannel.MatchedFilter(dtype=np.float32)
-    f.initialize(p, template_channels=w["tchan"], n_channels=w["nch"])
+    f.initialize(p, template_channels=w["tchan"], n_channels=w["nch"], **kw)
     return f
 
 

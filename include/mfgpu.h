@@ -84,6 +84,10 @@ typedef struct
     const int *template_channel;
     /* Extension: FFT length for the overlap-save blocks; 0 = autotune. */
     int fft_length;
+    /* Extension: correlator organisation; 0 = automatic, 1 = whole CTA per
+       transform, 2 = whole CTA with the next spectrum prefetched by TMA,
+       3 = two 128-thread teams per CTA (templates of one length only). */
+    int correlator_variant;
 } mfgpu_mf_params;
 
 /* MatchedFilter<T>::MatchedFilter(); precision MFGPU_FLOAT32 | MFGPU_FLOAT64 */

@@ -40,6 +40,7 @@ class MfgpuParams(C.Structure):
         ("n_channels", C.c_int),
         ("template_channel", C.POINTER(C.c_int)),
         ("fft_length", C.c_int),
+        ("correlator_variant", C.c_int),
     ]
 
 

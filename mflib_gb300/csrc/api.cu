@@ -118,7 +118,8 @@ struct mfgpu_mf
     bool ref_layout = true;
     // overlap-save plan
     int nfft = 0, log2p = 0, S = 0, nblocks = 0, ngroups = 0, maxvalid = 0;
-    bool shared_den = false, prefetch = false;
+    bool shared_den = false;
+    int mode_x = 0;  // correlator organisation (launch_xcorr mode)
     long ldx = 0, ldr = 0;
     int dead_chunks = 1;
     // device buffers
@@ -347,10 +348,15 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
     const int hi = mf->prec == 4 ? plan_limit_hi<float>() : plan_limit_hi<double>();
     bool all_equal = minLen == maxLen;
     mf->shared_den = all_equal;
-    auto smem_of = [&](int l2p, bool pf, int S) {
-        return mf->prec == 4 ? xcorr_smem_bytes<float>(l2p, all_equal, pf, S)
-                             : xcorr_smem_bytes<double>(l2p, all_equal, pf, S);
+    auto smem_of = [&](int l2p, int mode, int S) {
+        return mf->prec == 4 ? xcorr_smem_bytes<float>(l2p, all_equal, mode, S)
+                             : xcorr_smem_bytes<double>(l2p, all_equal, mode, S);
     };
+    const int forced_mode = p->correlator_variant >= 1 && p->correlator_variant <= 3 ? p->correlator_variant - 1 : -1;
+    if (p->correlator_variant < 0 || p->correlator_variant > 3)
+        return fail(MFGPU_EINVAL, "correlator_variant must be 0..3");
+    if (forced_mode == 2 && !all_equal)
+        return fail(MFGPU_EINVAL, "correlator_variant 3 (teams) needs templates of one length");
     int dev_smem = 0, sm_smem = 0;
     CU(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, mf->dev));
     CU(cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, mf->dev));
@@ -361,8 +367,7 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
         int occ = (int) (sm_smem / (bytes + 1024));
         return std::min(cap, occ);
     };
-    int best_l2p = -1, best_S = 0;
-    bool best_pf = false;
+    int best_l2p = -1, best_S = 0, best_mode = 0;
     double best_cost = 0;
     for (int l2p = lo; l2p <= hi; ++l2p)
     {
@@ -370,17 +375,33 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
         if (p->fft_length > 0 && p->fft_length != N) continue;
         int S = ((N - maxLen + 1) / 32) * 32;
         if (S < 32) continue;
-        size_t b0 = smem_of(l2p, false, S), b1 = smem_of(l2p, true, S);
-        if ((int) b0 > dev_smem) continue;
-        int occ0 = occupancy(l2p, b0), occ1 = (int) b1 <= dev_smem ? occupancy(l2p, b1) : 0;
-        bool pf = occ1 >= occ0 && occ1 > 0;
-        int occ = pf ? occ1 : occ0;
+        // organisation: forced, else two teams for a shared length when they
+        // keep the occupancy (measured 16% faster than the whole-CTA loop at
+        // N = 4096 and 5% at N = 2048, 2% slower at N = 8192), else spectrum
+        // prefetch when it keeps the occupancy
+        int mode;
+        if (forced_mode >= 0) mode = forced_mode;
+        else
+        {
+            size_t b0 = smem_of(l2p, 0, S), b1 = smem_of(l2p, 1, S);
+            int occ0 = occupancy(l2p, b0), occ1 = (int) b1 <= dev_smem ? occupancy(l2p, b1) : 0;
+            mode = (occ1 >= occ0 && occ1 > 0) ? 1 : 0;
+            if (all_equal && l2p <= 11)
+            {
+                size_t b2 = smem_of(l2p, 2, S);
+                int occ2 = (int) b2 <= dev_smem ? occupancy(l2p, b2) : 0;
+                if (occ2 >= std::max(occ0, occ1) && occ2 > 0) mode = 2;
+            }
+        }
+        size_t bytes = smem_of(l2p, mode, S);
+        if ((int) bytes > dev_smem) continue;
+        int occ = occupancy(l2p, bytes);
         if (occ < 1) continue;
         double nb = std::ceil((double) std::max(1, maxvalid) / S);
         double cost = nb * N * (l2p + 1) * (1.0 + 1.15 * tpc) / (occ >= 2 ? 1.4 : 1.0);
-        if (best_l2p < 0 || cost < best_cost) { best_l2p = l2p; best_S = S; best_cost = cost; best_pf = pf; }
+        if (best_l2p < 0 || cost < best_cost) { best_l2p = l2p; best_S = S; best_cost = cost; best_mode = mode; }
     }
-    mf->prefetch = best_pf;
+    mf->mode_x = best_mode;
     if (best_l2p < 0)
     {
         if (p->fft_length > 0)
@@ -636,7 +657,7 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
         ++mf->launches;
     }
     CU(cudaEventRecord(mf->ev[1], mf->stream));
-    CU(launch_xcorr<T>(mf->log2p, mf->shared_den, mf->prefetch, p, mf->nblocks, mf->ngroups, mf->stream));
+    CU(launch_xcorr<T>(mf->log2p, mf->shared_den, mf->mode_x, p, mf->nblocks, mf->ngroups, mf->stream));
     ++mf->launches;
     return MFGPU_OK;
 }

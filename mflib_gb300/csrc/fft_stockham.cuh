@@ -3,6 +3,7 @@
 // stores (so pre-processing and epilogues fuse into the transform).
 #pragma once
 #include <cmath>
+#include <type_traits>
 #include <vector>
 #include "device_common.cuh"
 
@@ -80,7 +81,16 @@ template <class T, int LO = 1, int HI = 13> void build_twiddle_table(int log2p, 
     else if constexpr (LO < HI) build_twiddle_table<T, LO + 1, HI>(log2p, out);
 }
 
-template <class T, int LOG2P, int NT, bool INV, bool ST_BUF, int PASS, class LD, class ST, bool LD_ALIAS = false>
+// Barrier over the NT threads that run one transform: the whole CTA
+// (BAR == 0) or a named hardware barrier shared by a team of NT threads.
+template <int BAR, int NT> __device__ __forceinline__ void team_sync()
+{
+    if constexpr (BAR == 0) __syncthreads();
+    else asm volatile("bar.sync %0, %1;" ::"n"(BAR), "n"(NT) : "memory");
+}
+
+template <class T, int LOG2P, int NT, bool INV, bool ST_BUF, int PASS, class LD, class ST, bool LD_ALIAS = false,
+          int BAR = 0>
 __device__ __forceinline__ void fft_pass_io(cx<T> *s, const cx<T> *tws, int tid, LD &ld, ST &st)
 {
     using PL = FftPlan<LOG2P>;
@@ -103,7 +113,7 @@ __device__ __forceinline__ void fft_pass_io(cx<T> *s, const cx<T> *tws, int tid,
             }
         }
     }
-    if constexpr ((!FIRST && (!LAST || ST_BUF)) || (FIRST && LD_ALIAS)) __syncthreads();
+    if constexpr ((!FIRST && (!LAST || ST_BUF)) || (FIRST && LD_ALIAS)) team_sync<BAR, NT>();
 #pragma unroll
     for (int b = 0; b < BPT; ++b)
     {
@@ -132,7 +142,7 @@ __device__ __forceinline__ void fft_pass_io(cx<T> *s, const cx<T> *tws, int tid,
             }
         }
     }
-    if constexpr (!LAST) __syncthreads();
+    if constexpr (!LAST) team_sync<BAR, NT>();
 }
 
 // Runs every pass.  The first pass reads its inputs through ld(e) (e in
@@ -142,13 +152,14 @@ __device__ __forceinline__ void fft_pass_io(cx<T> *s, const cx<T> *tws, int tid,
 // Intermediate results live in the padded buffer s.  The caller must make
 // sure s is free on entry; after return (with ST_BUF) the caller
 // synchronises before reading s.
-template <class T, int LOG2P, int NT, bool INV, bool ST_BUF, class LD, class ST, bool LD_ALIAS = false, int PASS = 0>
+template <class T, int LOG2P, int NT, bool INV, bool ST_BUF, class LD, class ST, bool LD_ALIAS = false, int BAR = 0,
+          int PASS = 0>
 __device__ __forceinline__ void fft_run(cx<T> *s, const cx<T> *tws, int tid, LD &ld, ST &st)
 {
     if constexpr (PASS < FftPlan<LOG2P>::npass())
     {
-        fft_pass_io<T, LOG2P, NT, INV, ST_BUF, PASS, LD, ST, LD_ALIAS>(s, tws, tid, ld, st);
-        fft_run<T, LOG2P, NT, INV, ST_BUF, LD, ST, LD_ALIAS, PASS + 1>(s, tws, tid, ld, st);
+        fft_pass_io<T, LOG2P, NT, INV, ST_BUF, PASS, LD, ST, LD_ALIAS, BAR>(s, tws, tid, ld, st);
+        fft_run<T, LOG2P, NT, INV, ST_BUF, LD, ST, LD_ALIAS, BAR, PASS + 1>(s, tws, tid, ld, st);
     }
 }
 

@@ -65,9 +65,12 @@ template <class T> struct SpecParams
 };
 
 // Shared-memory carve-up of the correlator (used by host and device).
-//   head | xs (staged segment; with SD also the FFT work buffer W) | [W] |
-//   UV (per-bin U, V pairs of the block spectrum) | pass twiddles |
-//   [2 spectrum buffers] | [invd (without SD)]
+//   head | xs (staged segment; with SD also the first FFT work buffer W0) |
+//   [W0] | [W1 (MODE 2)] | UV (per-bin U, V pairs of the block spectrum) |
+//   pass twiddles | [2 spectrum buffers (MODE 1)] | invd
+// MODE 0: whole CTA per transform, spectra read from L2;  MODE 1: whole CTA,
+// spectra TMA-prefetched;  MODE 2: two 128-thread teams transform different
+// templates with their own named barriers, spectra read from L2.
 template <class T, int LOG2P> struct XcorrLayout
 {
     using acc = typename acc_t<T>::type;
@@ -81,12 +84,13 @@ template <class T, int LOG2P> struct XcorrLayout
     static constexpr size_t brow = sizeof(cx<T>) * (P + 2);
     static constexpr size_t xs_region(bool sd) { return up(sd ? (seg > fft ? seg : fft) : seg); }
     static constexpr size_t off_xs(bool sd) { return head(sd); }
-    static constexpr size_t off_W(bool sd) { return off_xs(sd) + xs_region(sd); }  // only without SD
-    static constexpr size_t off_UV(bool sd) { return off_xs(sd) + xs_region(sd) + (sd ? 0 : up(fft)); }
-    static constexpr size_t off_tw(bool sd) { return off_UV(sd) + up(uv); }
-    static constexpr size_t off_B(bool sd) { return off_tw(sd) + up(tw_bytes); }
-    static constexpr size_t off_invd(bool sd, bool pf) { return off_B(sd) + (pf ? 2 * up(brow) : 0); }
-    static size_t bytes(bool sd, bool pf, int S) { return off_invd(sd, pf) + sizeof(T) * (size_t) S; }
+    static constexpr size_t off_W0(bool sd) { return off_xs(sd) + (sd ? 0 : xs_region(sd)); }
+    static constexpr size_t off_W1(bool sd) { return off_xs(sd) + xs_region(sd) + (sd ? 0 : up(fft)); }
+    static constexpr size_t off_UV(bool sd, int mode) { return off_W1(sd) + (mode == 2 ? up(fft) : 0); }
+    static constexpr size_t off_tw(bool sd, int mode) { return off_UV(sd, mode) + up(uv); }
+    static constexpr size_t off_B(bool sd, int mode) { return off_tw(sd, mode) + up(tw_bytes); }
+    static constexpr size_t off_invd(bool sd, int mode) { return off_B(sd, mode) + (mode == 1 ? 2 * up(brow) : 0); }
+    static size_t bytes(bool sd, int mode, int S) { return off_invd(sd, mode) + sizeof(T) * (size_t) S; }
 };
 
 template <class T> __device__ __forceinline__ T block_sum(T v, T *red)
@@ -325,11 +329,10 @@ __device__ __forceinline__ bool xcorr_wait(uint64_t *bar, uint32_t parity, int *
 
 // ----------------------------------------------------------------------------
 // Fused overlap-save correlator: one CTA per (block, template group).
-// SHARED_DEN: every template has the same length, so the normalisation is
-// computed once per CTA and the inverse-FFT buffer reuses the staged
-// segment's shared memory.  PREFETCH: the next template's spectrum is
-// TMA-copied into a second buffer while the current one is transformed.
-template <class T, int LOG2P, bool SHARED_DEN, bool PREFETCH>
+// SHARED_DEN: every template has the same length, so the normalisation was
+// precomputed per channel (den_kernel) and the first FFT work buffer
+// overlays the staged segment.  MODE: see XcorrLayout.
+template <class T, int LOG2P, bool SHARED_DEN, int MODE>
 __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 : 1)
     xcorr_kernel(XcorrParams<T> p)
 {
@@ -337,6 +340,8 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
     using acc = typename Acc::type;
     using LY = XcorrLayout<T, LOG2P>;
     using PL = FftPlan<LOG2P>;
+    constexpr bool PREFETCH = MODE == 1;
+    constexpr bool TEAMS = MODE == 2;
     constexpr int P = LY::P, N = LY::N, NCH = LY::NCH;
     const int tid = threadIdx.x;
     const int g = blockIdx.y;
@@ -367,12 +372,14 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
     acc *c1 = reinterpret_cast<acc *>(smem_x + 64 + 32 * sizeof(T));  // only without SHARED_DEN
     acc *c2 = c1 + (NCH + 1);
     T *xs = reinterpret_cast<T *>(smem_x + LY::off_xs(SHARED_DEN));
-    cx<T> *W = SHARED_DEN ? reinterpret_cast<cx<T> *>(xs) : reinterpret_cast<cx<T> *>(smem_x + LY::off_W(SHARED_DEN));
-    cx<T> *UV = reinterpret_cast<cx<T> *>(smem_x + LY::off_UV(SHARED_DEN));
-    cx<T> *tws = reinterpret_cast<cx<T> *>(smem_x + LY::off_tw(SHARED_DEN));
-    cx<T> *Bs0 = reinterpret_cast<cx<T> *>(smem_x + LY::off_B(SHARED_DEN));
-    cx<T> *Bs1 = reinterpret_cast<cx<T> *>(smem_x + LY::off_B(SHARED_DEN) + LY::up(LY::brow));
-    T *invd_s = reinterpret_cast<T *>(smem_x + LY::off_invd(SHARED_DEN, PREFETCH));
+    cx<T> *W0 = reinterpret_cast<cx<T> *>(smem_x + LY::off_W0(SHARED_DEN));
+    cx<T> *W1 = reinterpret_cast<cx<T> *>(smem_x + LY::off_W1(SHARED_DEN));
+    cx<T> *UV = reinterpret_cast<cx<T> *>(smem_x + LY::off_UV(SHARED_DEN, MODE));
+    cx<T> *tws = reinterpret_cast<cx<T> *>(smem_x + LY::off_tw(SHARED_DEN, MODE));
+    cx<T> *Bs0 = reinterpret_cast<cx<T> *>(smem_x + LY::off_B(SHARED_DEN, MODE));
+    cx<T> *Bs1 = reinterpret_cast<cx<T> *>(smem_x + LY::off_B(SHARED_DEN, MODE) + LY::up(LY::brow));
+    T *invd_s = reinterpret_cast<T *>(smem_x + LY::off_invd(SHARED_DEN, MODE));
+    cx<T> *W = W0;
     const cx<T> *post = p.twt + PL::post_off();  // real-FFT twiddles, read once per CTA from L2
     constexpr uint32_t kTwBytes = (uint32_t) LY::tw_bytes;
 
@@ -462,42 +469,11 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
     }
 
     // ---- per template: fused conj-multiply + inverse FFT + Pearson epilogue
-    for (int j = 0; j < ntl; ++j)
-    {
+    //      BAR/NTT select the barrier domain: the whole CTA, or one team.
+    auto template_body = [&](auto bar_tag, auto nt_tag, int j, const cx<T> *B, cx<T> *Wt, int ttid) {
+        constexpr int BAR = decltype(bar_tag)::value;
+        constexpr int NTT = decltype(nt_tag)::value;
         const int t = p.tids[t_begin + j];
-        if (j > 0) __syncthreads();  // previous template finished reading W and its spectrum buffer
-        const cx<T> *B;
-        if constexpr (PREFETCH)
-        {
-            if (tid == 0 && j + 1 < ntl)
-            {
-                fence_proxy_async_smem();
-                uint64_t *nb = &bar[1 + ((j + 1) & 1)];
-                mbar_arrive_expect_tx(nb, (uint32_t) LY::brow);
-                tma_load_1d(((j + 1) & 1) ? Bs1 : Bs0, p.Bc + (long) p.tids[t_begin + j + 1] * p.ldb,
-                            (uint32_t) LY::brow, nb);
-            }
-            if (!xcorr_wait(&bar[1 + (j & 1)], (uint32_t) ((j >> 1) & 1), p.err))
-            {
-                if (j + 1 < ntl) mbar_wait_bounded(&bar[1 + ((j + 1) & 1)], (uint32_t) (((j + 1) >> 1) & 1));
-                return;
-            }
-            B = (j & 1) ? Bs1 : Bs0;
-        }
-        else
-        {
-            B = p.Bc + (long) t * p.ldb;
-        }
-        if constexpr (!SHARED_DEN)
-        {
-            const int L = p.tlen[t];
-            if (L != Lcur)
-            {
-                seg_inv_den<T, N>(st, L, S, p.tol, invd_s, tid);
-                Lcur = L;
-                __syncthreads();
-            }
-        }
         const long nv = p.nvalid[t];
         T *dst = p.rho + (long) t * p.ldr + k0;
         auto pre = [&](int e) -> cx<T> {
@@ -520,7 +496,68 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
             if (k + 1 < kmax) store2<T>(dst + k, r0, r1);
             else dst[k] = r0;
         };
-        fft_run<T, LOG2P, kThreads, true, false>(W, tws, tid, pre, epi);
+        fft_run<T, LOG2P, NTT, true, false, decltype(pre), decltype(epi), false, BAR>(Wt, tws, ttid, pre, epi);
+    };
+
+    if constexpr (TEAMS)
+    {
+        // two teams of 128 threads; each keeps its own work buffer and barrier
+        const int team = tid >> 7, ttid = tid & 127;
+        for (int j = team; j < ntl; j += 2)
+        {
+            const cx<T> *B = p.Bc + (long) p.tids[t_begin + j] * p.ldb;
+            if (team == 0)
+            {
+                if (j > 0) team_sync<1, 128>();
+                template_body(std::integral_constant<int, 1>(), std::integral_constant<int, 128>(), j, B, W0, ttid);
+            }
+            else
+            {
+                if (j > 1) team_sync<2, 128>();
+                template_body(std::integral_constant<int, 2>(), std::integral_constant<int, 128>(), j, B, W1, ttid);
+            }
+        }
+    }
+    else
+    {
+        for (int j = 0; j < ntl; ++j)
+        {
+            const int t = p.tids[t_begin + j];
+            if (j > 0) __syncthreads();  // previous template finished reading W and its spectrum buffer
+            const cx<T> *B;
+            if constexpr (PREFETCH)
+            {
+                if (tid == 0 && j + 1 < ntl)
+                {
+                    fence_proxy_async_smem();
+                    uint64_t *nb = &bar[1 + ((j + 1) & 1)];
+                    mbar_arrive_expect_tx(nb, (uint32_t) LY::brow);
+                    tma_load_1d(((j + 1) & 1) ? Bs1 : Bs0, p.Bc + (long) p.tids[t_begin + j + 1] * p.ldb,
+                                (uint32_t) LY::brow, nb);
+                }
+                if (!xcorr_wait(&bar[1 + (j & 1)], (uint32_t) ((j >> 1) & 1), p.err))
+                {
+                    if (j + 1 < ntl) mbar_wait_bounded(&bar[1 + ((j + 1) & 1)], (uint32_t) (((j + 1) >> 1) & 1));
+                    return;
+                }
+                B = (j & 1) ? Bs1 : Bs0;
+            }
+            else
+            {
+                B = p.Bc + (long) t * p.ldb;
+            }
+            if constexpr (!SHARED_DEN)
+            {
+                const int L = p.tlen[t];
+                if (L != Lcur)
+                {
+                    seg_inv_den<T, N>(st, L, S, p.tol, invd_s, tid);
+                    Lcur = L;
+                    __syncthreads();
+                }
+            }
+            template_body(std::integral_constant<int, 0>(), std::integral_constant<int, kThreads>(), j, B, W, tid);
+        }
     }
 }
 

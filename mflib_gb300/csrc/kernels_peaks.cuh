@@ -81,13 +81,25 @@ template <> struct vec16<double>
 // when lag i0+q is a candidate).  The 16 samples are read with 16-byte
 // loads: the trace storage must be readable up to round_up(n, 16) and
 // 16-byte aligned at every multiple of 16.
+// Called by all 32 lanes of a warp with consecutive i0 (step 16): the
+// neighbours x[i0-1] and x[i0+16] come from the adjacent lanes' vectors; only
+// the first and last lane of the warp read them from memory.
 template <class T> __device__ __forceinline__ unsigned cand_mask16(const T *x, int i0, int n, T thr)
 {
-    if (i0 >= n) return 0u;
     T v[16];
-    vec16<T>::load(x + i0, v);
-    const T left = i0 > 0 ? x[i0 - 1] : (T) 0;
-    const T right = i0 + 16 < n ? x[i0 + 16] : (T) 0;
+    const bool any = i0 < n;
+    if (any) vec16<T>::load(x + i0, v);
+    else
+    {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) v[q] = (T) 0;
+    }
+    const int lane = threadIdx.x & 31;
+    T left = __shfl_up_sync(0xffffffffu, v[15], 1);
+    T right = __shfl_down_sync(0xffffffffu, v[0], 1);
+    if (lane == 0) left = (any && i0 > 0) ? x[i0 - 1] : (T) 0;
+    if (lane == 31) right = (i0 + 16 < n) ? x[i0 + 16] : (T) 0;
+    if (!any) return 0u;
     unsigned mask = 0;
 #pragma unroll
     for (int q = 0; q < 16; ++q)

@@ -8,23 +8,26 @@ namespace mfgpu {
 
 template <class T, int LOG2P> struct XcorrTable
 {
-    static size_t smem(bool shared_den, bool prefetch, int S)
+    static size_t smem(bool shared_den, int mode, int S) { return XcorrLayout<T, LOG2P>::bytes(shared_den, mode, S); }
+    template <bool SD, int MODE> static cudaError_t go(const XcorrParams<T> &p, int nblocks, int ngroups, cudaStream_t s)
     {
-        return XcorrLayout<T, LOG2P>::bytes(shared_den, prefetch, S);
-    }
-    template <bool SD, bool PF> static cudaError_t go(const XcorrParams<T> &p, int nblocks, int ngroups, cudaStream_t s)
-    {
-        size_t bytes = smem(SD, PF, p.S);
-        auto k = xcorr_kernel<T, LOG2P, SD, PF>;
+        size_t bytes = smem(SD, MODE, p.S);
+        auto k = xcorr_kernel<T, LOG2P, SD, MODE>;
         cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
         if (e != cudaSuccess) return e;
         k<<<dim3(nblocks, ngroups), kThreads, bytes, s>>>(p);
         return cudaGetLastError();
     }
-    static cudaError_t launch(bool sd, bool pf, const XcorrParams<T> &p, int nblocks, int ngroups, cudaStream_t s)
+    // MODE 2 (teams) exists only for a shared template length
+    static cudaError_t launch(bool sd, int mode, const XcorrParams<T> &p, int nblocks, int ngroups, cudaStream_t s)
     {
-        if (sd) return pf ? go<true, true>(p, nblocks, ngroups, s) : go<true, false>(p, nblocks, ngroups, s);
-        return pf ? go<false, true>(p, nblocks, ngroups, s) : go<false, false>(p, nblocks, ngroups, s);
+        if (sd)
+        {
+            if (mode == 2) return go<true, 2>(p, nblocks, ngroups, s);
+            return mode == 1 ? go<true, 1>(p, nblocks, ngroups, s) : go<true, 0>(p, nblocks, ngroups, s);
+        }
+        if (mode == 2) return cudaErrorInvalidValue;
+        return mode == 1 ? go<false, 1>(p, nblocks, ngroups, s) : go<false, 0>(p, nblocks, ngroups, s);
     }
     static cudaError_t spectra(const SpecParams<T> &p, int nt, cudaStream_t s)
     {
@@ -40,16 +43,16 @@ template <class T, int LOG2P> struct XcorrTable
 
 template <class T, int LO, int HI> struct XcorrDispatch
 {
-    static size_t smem(int log2p, bool sd, bool pf, int S)
+    static size_t smem(int log2p, bool sd, int mode, int S)
     {
-        if (log2p == LO) return XcorrTable<T, LO>::smem(sd, pf, S);
-        if constexpr (LO < HI) return XcorrDispatch<T, LO + 1, HI>::smem(log2p, sd, pf, S);
+        if (log2p == LO) return XcorrTable<T, LO>::smem(sd, mode, S);
+        if constexpr (LO < HI) return XcorrDispatch<T, LO + 1, HI>::smem(log2p, sd, mode, S);
         return 0;
     }
-    static cudaError_t launch(int log2p, bool sd, bool pf, const XcorrParams<T> &p, int nb, int ng, cudaStream_t s)
+    static cudaError_t launch(int log2p, bool sd, int mode, const XcorrParams<T> &p, int nb, int ng, cudaStream_t s)
     {
-        if (log2p == LO) return XcorrTable<T, LO>::launch(sd, pf, p, nb, ng, s);
-        if constexpr (LO < HI) return XcorrDispatch<T, LO + 1, HI>::launch(log2p, sd, pf, p, nb, ng, s);
+        if (log2p == LO) return XcorrTable<T, LO>::launch(sd, mode, p, nb, ng, s);
+        if constexpr (LO < HI) return XcorrDispatch<T, LO + 1, HI>::launch(log2p, sd, mode, p, nb, ng, s);
         return cudaErrorInvalidValue;
     }
     static cudaError_t spectra(int log2p, const SpecParams<T> &p, int nt, cudaStream_t s)
@@ -62,16 +65,16 @@ template <class T, int LO, int HI> struct XcorrDispatch
 
 using Dispatch = XcorrDispatch<MFGPU_T, fft_limits<MFGPU_T>::lo, fft_limits<MFGPU_T>::hi>;
 
-template <> size_t xcorr_smem_bytes<MFGPU_T>(int log2p, bool shared_den, bool prefetch, int S)
+template <> size_t xcorr_smem_bytes<MFGPU_T>(int log2p, bool shared_den, int mode, int S)
 {
-    return Dispatch::smem(log2p, shared_den, prefetch, S);
+    return Dispatch::smem(log2p, shared_den, mode, S);
 }
 
 template <>
-cudaError_t launch_xcorr<MFGPU_T>(int log2p, bool shared_den, bool prefetch, const XcorrParams<MFGPU_T> &p,
-                                  int nblocks, int ngroups, cudaStream_t s)
+cudaError_t launch_xcorr<MFGPU_T>(int log2p, bool shared_den, int mode, const XcorrParams<MFGPU_T> &p, int nblocks,
+                                  int ngroups, cudaStream_t s)
 {
-    return Dispatch::launch(log2p, shared_den, prefetch, p, nblocks, ngroups, s);
+    return Dispatch::launch(log2p, shared_den, mode, p, nblocks, ngroups, s);
 }
 
 template <> cudaError_t launch_spectra<MFGPU_T>(int log2p, const SpecParams<MFGPU_T> &p, int nt, cudaStream_t s)

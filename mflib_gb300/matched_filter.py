@@ -165,12 +165,15 @@ class MatchedFilter:
     def dtype(self):
         return self._dtype
 
-    def initialize(self, params, template_channels=None, n_channels=None, fft_length=0):
+    def initialize(self, params, template_channels=None, n_channels=None, fft_length=0, correlator_variant=0):
         """MatchedFilter<T>::initialize (src/matchedFilter.cpp:507-821).
 
         Extensions: ``template_channels`` (one channel index per template,
         with ``n_channels`` channels) lets several templates share one
-        signal; ``fft_length`` forces the overlap-save FFT length."""
+        signal; ``fft_length`` forces the overlap-save FFT length;
+        ``correlator_variant`` forces the correlator organisation (0 automatic,
+        1 whole CTA, 2 whole CTA with spectrum prefetch, 3 two teams per CTA,
+        templates of one length only)."""
         if not isinstance(params, MatchedFilterParameters) or not params.is_valid():
             raise ValueError("Parameters are invalid")
         tmpls = [params.get_template(i) for i in range(params.get_number_of_templates())]
@@ -201,6 +204,7 @@ class MatchedFilter:
             p.n_channels = int(n_channels if n_channels is not None else chans.max() + 1)
             p.template_channel = chans.ctypes.data_as(C.POINTER(C.c_int))
         p.fft_length = int(fft_length)
+        p.correlator_variant = int(correlator_variant)
         _lib.call("mfgpu_mf_initialize", self._h, C.byref(p))
         self._params = params
         self._nt = nt

@@ -221,6 +221,53 @@ def test_forced_fft_lengths(gpu, oracle, rng, fft_length):
         assert np.max(np.abs(f.get_valid_matched_filtered_signal(i) - ref[i])) < FP32_TOL
 
 
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("variant", [1, 2, 3])
+@pytest.mark.parametrize("fft_length", [0, 256, 2048, 4096])
+@pytest.mark.parametrize("ntpl", [1, 2, 5])
+def test_correlator_variants(gpu, oracle, rng, dtype, variant, fft_length, ntpl):
+    """Every correlator organisation (whole CTA, whole CTA with the next
+    spectrum prefetched, two teams of 128 threads) gives the oracle's
+    coefficients; 5 templates on one channel leave one team a template
+    short in the last round."""
+    mf = gpu
+    if dtype == np.float64 and fft_length > 4096:
+        pytest.skip("FP64 correlator stops at N = 4096")
+    n = 20_011
+    L = 100
+    chans = [rng.standard_normal(n) + 3.0 for _ in range(2)]
+    assign = [0] * ntpl + [1] * ntpl
+    tps = [rng.standard_normal(L) for _ in assign]
+    p = _params(mf, tps, n)
+    f = mf.MultiChannel.MatchedFilter(dtype=dtype)
+    f.initialize(p, template_channels=assign, n_channels=2, fft_length=fft_length, correlator_variant=variant)
+    if fft_length:
+        assert f.get_plan()["fft_length"] == fft_length
+    for c, s in enumerate(chans):
+        f.set_channel_signal(c, s.astype(dtype))
+    f.apply()
+    sig = [chans[c].astype(dtype) for c in assign]
+    ref = oracle.matched_filter(tps, sig, multi=True, fp64_from_f32=dtype == np.float32)
+    tol = FP32_TOL if dtype == np.float32 else 1e-11
+    for i in range(len(assign)):
+        a = f.get_valid_matched_filtered_signal(i)
+        assert a.size == ref[i].size
+        assert np.max(np.abs(a - ref[i])) < tol, (i, np.max(np.abs(a - ref[i])))
+
+
+def test_correlator_variant_errors(gpu, rng):
+    mf = gpu
+    n = 5000
+    p = _params(mf, [rng.standard_normal(100), rng.standard_normal(120)], n)
+    f = mf.MultiChannel.MatchedFilter(dtype=np.float32)
+    with pytest.raises(ValueError):
+        f.initialize(p, correlator_variant=3)  # teams need one template length
+    with pytest.raises(ValueError):
+        f.initialize(p, correlator_variant=4)
+    f.initialize(p, correlator_variant=2)
+    assert f.is_initialized()
+
+
 def test_shared_channels_extension(gpu, oracle, rng):
     """Several templates reading one channel (template_channels) give the
     same coefficients as one signal copy per template."""
