@@ -153,6 +153,9 @@ mfgpu_status mfgpu_mf_synchronize(mfgpu_mf *mf);
 mfgpu_status mfgpu_mf_get_last_timings(mfgpu_mf *mf, float *xcorr_ms, float *apply_ms);
 /* Number of kernel launches issued by the object since it was created. */
 mfgpu_status mfgpu_mf_get_launch_count(const mfgpu_mf *mf, long long *count);
+/* The object's CUDA stream (a cudaStream_t), on which every launch and
+ * copy of the object is issued; for event timing by the caller. */
+mfgpu_status mfgpu_mf_get_stream(const mfgpu_mf *mf, void **stream);
 
 /* Batched peak finding on the device over every template's coefficients
  * (PeakFinder<T>::apply, src/peakFinder.cpp:329-446, applied per template
@@ -160,6 +163,16 @@ mfgpu_status mfgpu_mf_get_launch_count(const mfgpu_mf *mf, long long *count);
  * trace_length: lags searched per template; 0 = getFilteredSignalLength().
  * Results stay on the device; read them with mfgpu_mf_get_peaks. */
 mfgpu_status mfgpu_mf_find_peaks(mfgpu_mf *mf, double threshold, int min_distance, int trace_length);
+/* Extension (no reference counterpart): from the next apply on, the
+ * correlator also gathers the peak candidates above `threshold` of the
+ * default trace length, and a find_peaks with the same
+ * threshold and the default trace length uses them instead of scanning the
+ * stored coefficients again.  The peaks are identical either way.  A
+ * negative threshold turns the gathering off (the default). */
+mfgpu_status mfgpu_mf_set_peak_threshold(mfgpu_mf *mf, double threshold);
+/* Requested gathering threshold (negative: off) and whether the last apply
+ * gathered candidates (active = 1). */
+mfgpu_status mfgpu_mf_get_peak_threshold(const mfgpu_mf *mf, double *threshold, int *active);
 /* Peaks of template it (ascending lag indices). */
 mfgpu_status mfgpu_mf_get_peaks(mfgpu_mf *mf, int it, int maxn, int *dst, int *nout);
 /* Total peaks over all templates, and all of them at once: counts[nt] and

@@ -130,6 +130,12 @@ struct mfgpu_mf
     PeakWS pk;
     std::vector<long long> pk_off;
     bool have_peaks = false;
+    // candidates gathered by the correlator (mfgpu_mf_set_peak_threshold)
+    double pk_req = -1;         // requested threshold, < 0: off
+    bool pk_fused = false;      // slots hold the current apply's candidates
+    double pk_fused_thr = 0;
+    int pk_fused_len = 0;
+    DevBuf pk_cnt, pk_idx, pk_val;
     long long launches = 0;
     float last_xcorr_ms = 0, last_apply_ms = 0;
 
@@ -138,7 +144,7 @@ struct mfgpu_mf
     {
         DevBuf *all[] = {&x,      &rho,      &Bc,   &tw,  &grp_chan, &grp_tb, &grp_te, &tids,      &tlen_d,
                          &nvalid_d, &dead,   &err,  &tmpl_d, &toff_d, &pmin, &pmax,  &chan_list, &stackbuf,
-                         &shifts_d, &weights_d, &specbuf, &den};
+                         &shifts_d, &weights_d, &specbuf, &den, &pk_cnt, &pk_idx, &pk_val};
         for (DevBuf *d : all) d->release();
         pk.release();
     }
@@ -146,7 +152,8 @@ struct mfgpu_mf
     {
         if (stream) cudaStreamSynchronize(stream);
         release_device();
-        initialized = have = timed = have_peaks = false;
+        initialized = have = timed = have_peaks = pk_fused = false;
+        pk_req = -1;
         nt = n = maxLen = minLen = nch = 0;
         lens.clear(); tchan.clear(); nvalid.clear(); tmpl.clear(); toff.clear();
         shifts.clear(); weights.clear(); pk_off.clear();
@@ -636,7 +643,7 @@ mfgpu_status mfgpu_mf_get_signal(const mfgpu_mf *cmf, int it, int maxn, void *ds
 
 template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
 {
-    XcorrParams<T> p;
+    XcorrParams<T> p{};
     p.x = mf->x.as<T>(); p.ldx = mf->ldx;
     p.Bc = mf->Bc.as<cx<T>>(); p.ldb = (1L << mf->log2p) + 2;
     p.rho = mf->rho.as<T>(); p.ldr = mf->ldr;
@@ -656,9 +663,32 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
                          mf->stream));
         ++mf->launches;
     }
+    // fused peak candidates
+    mf->pk_fused = false;
+    p.pk_on = 0;
+    if (mf->pk_req >= 0)
+    {
+        const size_t nslot = (size_t) mf->nt * mf->nblocks;
+        CU(mf->pk_cnt.ensure(sizeof(int) * nslot));
+        CU(mf->pk_idx.ensure(sizeof(int) * nslot * kPkCap));
+        CU(mf->pk_val.ensure(sizeof(T) * nslot * kPkCap));
+        CU(cudaMemsetAsync(mf->pk_cnt.p, 0, sizeof(int) * nslot, mf->stream));
+        p.pk_on = 1;
+        p.pk_len = mf->n - mf->maxLen + 1;
+        p.pk_thr = (T) mf->pk_req;
+        p.pk_cnt = mf->pk_cnt.as<int>();
+        p.pk_idx = mf->pk_idx.as<int>();
+        p.pk_val = mf->pk_val.as<T>();
+    }
     CU(cudaEventRecord(mf->ev[1], mf->stream));
     CU(launch_xcorr<T>(mf->log2p, mf->shared_den, mf->mode_x, p, mf->nblocks, mf->ngroups, mf->stream));
     ++mf->launches;
+    if (p.pk_on)
+    {
+        mf->pk_fused = true;
+        mf->pk_fused_thr = mf->pk_req;
+        mf->pk_fused_len = p.pk_len;
+    }
     return MFGPU_OK;
 }
 
@@ -716,6 +746,13 @@ mfgpu_status mfgpu_mf_get_launch_count(const mfgpu_mf *mf, long long *count)
 {
     if (!mf || !count) return fail(MFGPU_EINVAL, "NULL argument");
     *count = mf->launches;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_get_stream(const mfgpu_mf *mf, void **stream)
+{
+    if (!mf || !stream) return fail(MFGPU_EINVAL, "NULL argument");
+    *stream = (void *) mf->stream;
     return MFGPU_OK;
 }
 
@@ -853,13 +890,34 @@ mfgpu_status mfgpu_mf_find_peaks(mfgpu_mf *mf, double threshold, int min_distanc
     for (int t = 0; t < mf->nt; ++t) rows[t] = t;
     mf->pk_off.assign(mf->nt + 1, 0);
     std::string err;
+    // candidates of the last apply when it gathered them for this threshold and length
+    const bool fused = mf->pk_fused && threshold == mf->pk_fused_thr && len == mf->pk_fused_len;
+    FusedSlots<float> ff{mf->pk_cnt.as<int>(), mf->pk_idx.as<int>(), mf->pk_val.as<float>(), mf->nblocks, mf->S};
+    FusedSlots<double> fd{mf->pk_cnt.as<int>(), mf->pk_idx.as<int>(), mf->pk_val.as<double>(), mf->nblocks, mf->S};
     int rc = mf->prec == 4
                  ? run_peaks<float>(mf->rho.as<float>(), mf->ldr, rows.data(), mf->nt, len, threshold, min_distance,
-                                    mf->pk, mf->stream, &mf->launches, mf->pk_off.data(), err)
+                                    mf->pk, mf->stream, &mf->launches, mf->pk_off.data(), err, fused ? &ff : nullptr)
                  : run_peaks<double>(mf->rho.as<double>(), mf->ldr, rows.data(), mf->nt, len, threshold,
-                                     min_distance, mf->pk, mf->stream, &mf->launches, mf->pk_off.data(), err);
+                                     min_distance, mf->pk, mf->stream, &mf->launches, mf->pk_off.data(), err,
+                                     fused ? &fd : nullptr);
     if (rc != 0) return fail(MFGPU_ECUDA, err);
     mf->have_peaks = true;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_set_peak_threshold(mfgpu_mf *mf, double threshold)
+{
+    if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");
+    if (threshold > 1) return fail(MFGPU_EINVAL, "Threshold = " + std::to_string(threshold) + " must be at most 1");
+    mf->pk_req = threshold < 0 ? -1.0 : threshold;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_get_peak_threshold(const mfgpu_mf *mf, double *threshold, int *active)
+{
+    if (!mf || !threshold) return fail(MFGPU_EINVAL, "NULL argument");
+    *threshold = mf->pk_req;
+    if (active) *active = mf->pk_fused ? 1 : 0;
     return MFGPU_OK;
 }
 

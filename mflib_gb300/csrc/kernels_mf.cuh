@@ -26,6 +26,7 @@
 //     |rho| > 1.1, is fused into the last pass (coalesced 2-lag stores).
 #pragma once
 #include "fft_stockham.cuh"
+#include "kernels_util.cuh"
 
 namespace mfgpu {
 
@@ -52,6 +53,17 @@ template <class T> struct XcorrParams
     int S;                    // lags per block (multiple of 32)
     T tol;
     int *err;
+    // fused peak candidates (pk_on != 0): lags [k0+1, k0+S-2] of block b of
+    // template t that pass the candidate rule on a trace of pk_len lags with
+    // threshold pk_thr go to slot (t * gridDim.x + b): count pk_cnt (zeroed
+    // before the launch; may exceed kPkCap), up to kPkCap (index, value)
+    // pairs in pk_idx / pk_val, in no particular order.
+    int pk_on;
+    int pk_len;
+    T pk_thr;
+    int *pk_cnt;
+    int *pk_idx;
+    T *pk_val;
 };
 
 template <class T> struct SpecParams
@@ -90,7 +102,17 @@ template <class T, int LOG2P> struct XcorrLayout
     static constexpr size_t off_tw(bool sd, int mode) { return off_UV(sd, mode) + up(uv); }
     static constexpr size_t off_B(bool sd, int mode) { return off_tw(sd, mode) + up(tw_bytes); }
     static constexpr size_t off_invd(bool sd, int mode) { return off_B(sd, mode) + (mode == 1 ? 2 * up(brow) : 0); }
-    static size_t bytes(bool sd, int mode, int S) { return off_invd(sd, mode) + sizeof(T) * (size_t) S; }
+    // fused peak candidates: per team two chunk masks (one bit per 64 lags,
+    // P/32 chunks)
+    static constexpr int mask_words = (P / 32 + 31) / 32;
+    static __host__ __device__ size_t off_M(bool sd, int mode, int S)
+    {
+        return off_invd(sd, mode) + up(sizeof(T) * (size_t) S);
+    }
+    static size_t bytes(bool sd, int mode, int S)
+    {
+        return off_M(sd, mode, S) + sizeof(unsigned) * 2 * (mode == 2 ? 2 : 1) * mask_words;
+    }
 };
 
 template <class T> __device__ __forceinline__ T block_sum(T v, T *red)
@@ -300,6 +322,34 @@ template <> __device__ __forceinline__ void store2<double>(double *dst, double a
 
 template <class T> __device__ __forceinline__ T clamp_rho(T v) { return fabs(v) > (T) 1.1 ? (T) 0 : v; }
 
+// four consecutive values (16-byte aligned) in vector loads / stores
+template <class T> struct vec4;
+template <> struct vec4<float>
+{
+    static __device__ __forceinline__ void load(const float *p, float (&v)[4])
+    {
+        const float4 a = *reinterpret_cast<const float4 *>(p);
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    }
+    static __device__ __forceinline__ void store(float *p, const float (&v)[4])
+    {
+        *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    }
+};
+template <> struct vec4<double>
+{
+    static __device__ __forceinline__ void load(const double *p, double (&v)[4])
+    {
+        const double2 a = reinterpret_cast<const double2 *>(p)[0], b = reinterpret_cast<const double2 *>(p)[1];
+        v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+    }
+    static __device__ __forceinline__ void store(double *p, const double (&v)[4])
+    {
+        reinterpret_cast<double2 *>(p)[0] = make_double2(v[0], v[1]);
+        reinterpret_cast<double2 *>(p)[1] = make_double2(v[2], v[3]);
+    }
+};
+
 // two consecutive complex values in one 16-byte shared load (FP32)
 template <class T> __device__ __forceinline__ void load_pair(const cx<T> *p, cx<T> &a, cx<T> &b);
 template <> __device__ __forceinline__ void load_pair<float>(const cx<float> *p, cx<float> &a, cx<float> &b)
@@ -379,11 +429,13 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
     cx<T> *Bs0 = reinterpret_cast<cx<T> *>(smem_x + LY::off_B(SHARED_DEN, MODE));
     cx<T> *Bs1 = reinterpret_cast<cx<T> *>(smem_x + LY::off_B(SHARED_DEN, MODE) + LY::up(LY::brow));
     T *invd_s = reinterpret_cast<T *>(smem_x + LY::off_invd(SHARED_DEN, MODE));
+    unsigned *Mk = reinterpret_cast<unsigned *>(smem_x + LY::off_M(SHARED_DEN, MODE, S));
     cx<T> *W = W0;
     const cx<T> *post = p.twt + PL::post_off();  // real-FFT twiddles, read once per CTA from L2
     constexpr uint32_t kTwBytes = (uint32_t) LY::tw_bytes;
 
     // ---- stage segment, pass twiddles and the first spectrum with bulk async copies
+    if (tid < 2 * (TEAMS ? 2 : 1) * LY::mask_words) Mk[tid] = 0u;  // chunk masks of the fused peak candidates
     if (tid == 0)
     {
         mbar_init(&bar[0], 1);
@@ -470,7 +522,53 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
 
     // ---- per template: fused conj-multiply + inverse FFT + Pearson epilogue
     //      BAR/NTT select the barrier domain: the whole CTA, or one team.
-    auto template_body = [&](auto bar_tag, auto nt_tag, int j, const cx<T> *B, cx<T> *Wt, int ttid) {
+    //
+    // Fused peak candidates (p.pk_on): the last pass also sets bit c of the
+    // template's chunk mask when a lag in [64c, 64c+64) exceeds the
+    // threshold.  After the team's next barrier (the next template's, or a
+    // final one), which makes the team's global stores visible to the team,
+    // only the flagged chunks are read back (from L2) and examined: the
+    // candidate rule for the lags [k0+1, k0+S-2], whose neighbours both lie
+    // in this block.  The block's first and last lags are decided from the
+    // stored trace after the launch.
+    const bool pk = p.pk_on != 0;
+    const long pk_n = p.pk_len;
+    const T pk_thr = p.pk_thr;
+    constexpr int MW = LY::mask_words;
+    auto pk_scan = [&](auto nt_tag, const unsigned *mk, int t, int ttid) {
+        constexpr int NTT = decltype(nt_tag)::value;
+        const T *Rt = p.rho + (long) t * p.ldr + k0;
+        const long nv = p.nvalid[t];
+        const int kmax = (int) (nv - k0 < (long) S ? nv - k0 : (long) S);
+#pragma unroll 1
+        for (int w = 0; w < MW; ++w)
+        {
+            unsigned m = mk[w];
+            while (m)
+            {
+                const int c = 32 * w + __ffs(m) - 1;
+                m &= m - 1;
+                for (int l = 64 * c + ttid; l < 64 * c + 64; l += NTT)
+                {
+                    if (l < 1 || l > S - 2 || k0 + l >= pk_n) continue;  // then also l < kmax
+                    const T xi = __ldcg(Rt + l);
+                    if (!(xi > pk_thr)) continue;
+                    const T xr = l + 1 < kmax ? __ldcg(Rt + l + 1) : (T) 0;  // unused at the trace's last lag
+                    if (cand_rule<T>(__ldcg(Rt + l - 1), xi, xr, k0 + l, pk_n, pk_thr))
+                    {
+                        const long slot = (long) t * gridDim.x + blockIdx.x;
+                        const int pos = atomicAdd(p.pk_cnt + slot, 1);
+                        if (pos < kPkCap)
+                        {
+                            p.pk_idx[slot * kPkCap + pos] = (int) (k0 + l);
+                            p.pk_val[slot * kPkCap + pos] = xi;
+                        }
+                    }
+                }
+            }
+        }
+    };
+    auto template_body = [&](auto bar_tag, auto nt_tag, int j, const cx<T> *B, cx<T> *Wt, unsigned *mk, int ttid) {
         constexpr int BAR = decltype(bar_tag)::value;
         constexpr int NTT = decltype(nt_tag)::value;
         const int t = p.tids[t_begin + j];
@@ -495,27 +593,56 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
             const T r1 = clamp_rho(z.y * d.y);
             if (k + 1 < kmax) store2<T>(dst + k, r0, r1);
             else dst[k] = r0;
+            if (pk && (r0 > pk_thr || r1 > pk_thr)) atomicOr(mk + (e >> 10), 1u << ((e >> 5) & 31));
         };
         fft_run<T, LOG2P, NTT, true, false, decltype(pre), decltype(epi), false, BAR>(Wt, tws, ttid, pre, epi);
     };
 
     if constexpr (TEAMS)
     {
-        // two teams of 128 threads; each keeps its own work buffer and barrier
+        // two teams of 128 threads; each keeps its own work buffer, chunk
+        // masks and barrier
         const int team = tid >> 7, ttid = tid & 127;
-        for (int j = team; j < ntl; j += 2)
+        unsigned *mkt = Mk + team * 2 * MW;
+        int t_prev = -1, it = 0;
+        for (int j = team; j < ntl; j += 2, ++it)
         {
             const cx<T> *B = p.Bc + (long) p.tids[t_begin + j] * p.ldb;
             if (team == 0)
             {
-                if (j > 0) team_sync<1, 128>();
-                template_body(std::integral_constant<int, 1>(), std::integral_constant<int, 128>(), j, B, W0, ttid);
+                if (it > 0)
+                {
+                    team_sync<1, 128>();
+                    if (pk)
+                    {
+                        pk_scan(std::integral_constant<int, 128>(), mkt + ((it - 1) & 1) * MW, t_prev, ttid);
+                        if (ttid < MW) mkt[(it & 1) * MW + ttid] = 0u;
+                    }
+                }
+                template_body(std::integral_constant<int, 1>(), std::integral_constant<int, 128>(), j, B, W0,
+                              mkt + (it & 1) * MW, ttid);
             }
             else
             {
-                if (j > 1) team_sync<2, 128>();
-                template_body(std::integral_constant<int, 2>(), std::integral_constant<int, 128>(), j, B, W1, ttid);
+                if (it > 0)
+                {
+                    team_sync<2, 128>();
+                    if (pk)
+                    {
+                        pk_scan(std::integral_constant<int, 128>(), mkt + ((it - 1) & 1) * MW, t_prev, ttid);
+                        if (ttid < MW) mkt[(it & 1) * MW + ttid] = 0u;
+                    }
+                }
+                template_body(std::integral_constant<int, 2>(), std::integral_constant<int, 128>(), j, B, W1,
+                              mkt + (it & 1) * MW, ttid);
             }
+            t_prev = p.tids[t_begin + j];
+        }
+        if (pk && it > 0)
+        {
+            if (team == 0) team_sync<1, 128>();
+            else team_sync<2, 128>();
+            pk_scan(std::integral_constant<int, 128>(), mkt + ((it - 1) & 1) * MW, t_prev, ttid);
         }
     }
     else
@@ -523,7 +650,16 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
         for (int j = 0; j < ntl; ++j)
         {
             const int t = p.tids[t_begin + j];
-            if (j > 0) __syncthreads();  // previous template finished reading W and its spectrum buffer
+            if (j > 0)
+            {
+                __syncthreads();  // previous template finished reading W and its spectrum buffer
+                if (pk)
+                {
+                    pk_scan(std::integral_constant<int, kThreads>(), Mk + ((j - 1) & 1) * MW,
+                            p.tids[t_begin + j - 1], tid);
+                    if (tid < MW) Mk[(j & 1) * MW + tid] = 0u;
+                }
+            }
             const cx<T> *B;
             if constexpr (PREFETCH)
             {
@@ -556,7 +692,13 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
                     __syncthreads();
                 }
             }
-            template_body(std::integral_constant<int, 0>(), std::integral_constant<int, kThreads>(), j, B, W, tid);
+            template_body(std::integral_constant<int, 0>(), std::integral_constant<int, kThreads>(), j, B, W,
+                          Mk + (j & 1) * MW, tid);
+        }
+        if (pk)
+        {
+            __syncthreads();
+            pk_scan(std::integral_constant<int, kThreads>(), Mk + ((ntl - 1) & 1) * MW, p.tids[t_end - 1], tid);
         }
     }
 }

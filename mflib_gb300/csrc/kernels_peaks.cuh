@@ -27,7 +27,6 @@ namespace mfgpu {
 constexpr int kPkThreads = 256;
 constexpr int kPkPer = 16;                          // lags per thread
 constexpr int kPkChunk = kPkThreads * kPkPer;       // lags per CTA
-constexpr int kPkCap = 32;                          // slot capacity per chunk
 
 template <class T> struct PeakTraces
 {
@@ -37,8 +36,6 @@ template <class T> struct PeakTraces
     int len;          // lags per trace
     T thr;
 };
-
-template <class T> __device__ __forceinline__ int sgn(T d) { return d > (T) 0 ? 1 : (d < (T) 0 ? -1 : 0); }
 
 template <class T> __device__ __forceinline__ bool is_candidate(const T *x, int i, int n, T thr)
 {
@@ -300,6 +297,101 @@ static __global__ void peak_trace_beg_kernel(int ntr, int nchunks, const long lo
     if (t > ntr) return;
     long long v = offs[(long) t * nchunks];
     trace_beg[t] = v < cap ? v : cap;
+}
+
+// ----------------------------------------------------------------------------
+// Candidates gathered by the correlator.  Chunk b of a trace is correlator
+// block b, lags [b*S, b*S + S): the correlator decided the body lags
+// [b*S+1, b*S+S-2] from the values it stored (count body_cnt, up to kPkCap
+// unordered slot entries, indexed by row * nblk + b); the seam kernel
+// decides the first and last lag of each block from the stored trace and
+// forms the chunk's total count.
+template <class T>
+static __global__ void peak_seam_kernel(PeakTraces<T> tr, int ntr, FusedSlots<T> fs, int *counts, unsigned char *ht)
+{
+    const long g = (long) blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (long) ntr * fs.nblk) return;
+    const int trace = (int) (g / fs.nblk), b = (int) (g % fs.nblk);
+    const int row = tr.row[trace];
+    const T *x = tr.x + (long) row * tr.ldx;
+    const long n = tr.len;
+    const long i0 = (long) b * fs.S, i1 = i0 + fs.S - 1;
+    const int h = (i0 < n && is_candidate<T>(x, (int) i0, (int) n, tr.thr)) ? 1 : 0;
+    const int tl = (i1 < n && is_candidate<T>(x, (int) i1, (int) n, tr.thr)) ? 1 : 0;
+    counts[g] = h + fs.cnt[(long) row * fs.nblk + b] + tl;
+    ht[g] = (unsigned char) (h | (tl << 1));
+}
+
+// Packs chunk b of a trace in index order: first lag, body (slot entries
+// ranked by index, or a re-scan of the stored trace when more than kPkCap
+// body lags passed), last lag.
+template <class T>
+static __global__ void __launch_bounds__(kPkThreads)
+    peak_gather_fused_kernel(PeakTraces<T> tr, FusedSlots<T> fs, const int *counts, const unsigned char *ht,
+                             const long long *offs, int *cidx, T *cval, int *ctr, long long cap, int *overflow)
+{
+    __shared__ long long sh[32];
+    const int trace = blockIdx.y, b = blockIdx.x;
+    const long slot = (long) trace * fs.nblk + b;
+    const int cnt = counts[slot];
+    if (cnt == 0) return;
+    const long long off = offs[slot];
+    if (threadIdx.x == 0 && off + cnt > cap) *overflow = 1;
+    const int row = tr.row[trace];
+    const T *x = tr.x + (long) row * tr.ldx;
+    const long n = tr.len;
+    const int hv = ht[slot];
+    const long i0 = (long) b * fs.S;
+    auto put = [&](long long o, long i, T v) {
+        if (o < cap)
+        {
+            cidx[o] = (int) i;
+            cval[o] = v;
+            ctr[o] = trace;
+        }
+    };
+    if (threadIdx.x == 0)
+    {
+        if (hv & 1) put(off, i0, x[i0]);
+        if (hv & 2) put(off + cnt - 1, i0 + fs.S - 1, x[i0 + fs.S - 1]);
+    }
+    const long long boff = off + (hv & 1);
+    const long bs = (long) row * fs.nblk + b;
+    const int bc = fs.cnt[bs];
+    if (bc <= kPkCap)
+    {
+        const int *si = fs.idx + bs * kPkCap;
+        for (int r = threadIdx.x; r < bc; r += kPkThreads)
+        {
+            const int ir = si[r];
+            int rank = 0;
+            for (int q = 0; q < bc; ++q) rank += si[q] < ir ? 1 : 0;
+            put(boff + rank, ir, fs.val[bs * kPkCap + r]);
+        }
+        return;
+    }
+    const long lo = i0 + 1, hi = (i0 + fs.S - 1 < n) ? i0 + fs.S - 1 : n;
+    long long base = boff;
+    for (long c0 = lo; c0 < hi; c0 += kPkChunk)
+    {
+        const long a = c0 + (long) threadIdx.x * kPkPer;
+        unsigned mask = 0;
+#pragma unroll 4
+        for (int q = 0; q < kPkPer; ++q)
+            if (a + q < hi && cand_rule<T>(x[a + q - 1], x[a + q], a + q + 1 < n ? x[a + q + 1] : (T) 0, a + q, n,
+                                           tr.thr))
+                mask |= 1u << q;
+        long long tot;
+        long long r = block_excl_scan((long long) __popc(mask), sh, &tot);
+        while (mask)
+        {
+            const int q = __ffs(mask) - 1;
+            mask &= mask - 1;
+            put(base + r, a + q, x[a + q]);
+            ++r;
+        }
+        base += tot;
+    }
 }
 
 }  // namespace mfgpu

@@ -10,6 +10,33 @@ constexpr int kScanThreads = 256;
 constexpr int kScanPer = 8;
 constexpr int kScanTile = kScanThreads * kScanPer;
 
+// Peak candidates: slot capacity per chunk of a trace (the correlator's
+// fused scan and the stand-alone scan both write chunk slots of this size).
+constexpr int kPkCap = 32;
+
+// Candidate slots written by the correlator for chunks of S lags (one chunk
+// per correlator block): count, entries and blocks per trace.
+template <class T> struct FusedSlots
+{
+    const int *cnt;
+    const int *idx;
+    const T *val;
+    int nblk;
+    int S;
+};
+
+template <class T> __device__ __forceinline__ int sgn(T d) { return d > (T) 0 ? 1 : (d < (T) 0 ? -1 : 0); }
+
+// PeakFinder<T>::apply's candidate rule (src/peakFinder.cpp:345-381) for an
+// interior or last lag i (1 <= i <= n-1) with neighbours xl = x[i-1] and
+// xr = x[i+1] (xr unused when i == n-1).
+template <class T> __device__ __forceinline__ bool cand_rule(T xl, T xi, T xr, long i, long n, T thr)
+{
+    if (!(xi > thr)) return false;
+    if (i == n - 1) return sgn<T>(xi - xl) > 0;
+    return sgn<T>(xi - xl) >= 0 && sgn<T>(xr - xi) < 0;
+}
+
 // exclusive block scan of one int64 per thread; returns the block total
 __device__ __forceinline__ long long block_excl_scan(long long v, long long *sh, long long *total)
 {

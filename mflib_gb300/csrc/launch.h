@@ -65,13 +65,13 @@ struct DevBuf
 struct PeakWS
 {
     DevBuf counts, offs, slot_idx, slot_val, cidx, cval, ctr, state, flags, pos, tiles, trace_beg, peak_off, peaks,
-        counter, row;
+        counter, row, ht;
     long long npeaks = 0;
     long long cand_cap = 1 << 16;  // capacity of the packed candidate arrays
     void release()
     {
-        DevBuf *all[] = {&counts, &offs, &slot_idx, &slot_val, &cidx, &cval, &ctr, &state,
-                         &flags, &pos, &tiles, &trace_beg, &peak_off, &peaks, &counter, &row};
+        DevBuf *all[] = {&counts, &offs, &slot_idx, &slot_val, &cidx, &cval, &ctr, &state, &flags,
+                         &pos, &tiles, &trace_beg, &peak_off, &peaks, &counter, &row, &ht};
         for (DevBuf *d : all) d->release();
         npeaks = 0;
         cand_cap = 1 << 16;
@@ -80,9 +80,12 @@ struct PeakWS
 
 // Runs candidates + pruning + compaction; on return (stream synchronised)
 // ws.peaks / ws.peak_off hold the result and host_peak_off (ntr+1) is filled.
+// With `fused`, the candidates the correlator gathered (same threshold and
+// trace length) replace the scan over the traces.
 template <class T>
 int run_peaks(const T *x, long ldx, const int *host_rows, int ntr, int len, double thr, int dist, PeakWS &ws,
-              cudaStream_t s, long long *launches, long long *host_peak_off, std::string &err);
+              cudaStream_t s, long long *launches, long long *host_peak_off, std::string &err,
+              const FusedSlots<T> *fused = nullptr);
 
 // ---------------------------------------------------------------------------
 // DBSCAN over segments

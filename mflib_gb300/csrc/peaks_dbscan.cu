@@ -34,7 +34,8 @@ cudaError_t device_excl_scan(const int *in, long n, long long *out, long long *t
 
 template <class T>
 int run_peaks(const T *x, long ldx, const int *host_rows, int ntr, int len, double thr, int dist, PeakWS &ws,
-              cudaStream_t s, long long *launches, long long *host_peak_off, std::string &err)
+              cudaStream_t s, long long *launches, long long *host_peak_off, std::string &err,
+              const FusedSlots<T> *fused)
 {
     ws.npeaks = 0;
     if (ntr <= 0) return 0;
@@ -43,15 +44,21 @@ int run_peaks(const T *x, long ldx, const int *host_rows, int ntr, int len, doub
         for (int t = 0; t <= ntr; ++t) host_peak_off[t] = 0;
         return 0;
     }
-    const int nchunks = (len + kPkChunk - 1) / kPkChunk;
+    // chunks: kPkChunk lags for the stand-alone scan, one correlator block
+    // (fused.S lags) when the correlator gathered the candidates
+    const int nchunks = fused ? fused->nblk : (len + kPkChunk - 1) / kPkChunk;
     const size_t nslots = (size_t) ntr * nchunks;
     MF_TRY(ws.row.ensure(sizeof(int) * ntr));
     MF_TRY(ws.trace_beg.ensure(sizeof(long long) * (ntr + 1)));
     MF_TRY(ws.peak_off.ensure(sizeof(long long) * (ntr + 1)));
     MF_TRY(ws.counts.ensure(sizeof(int) * nslots));
     MF_TRY(ws.offs.ensure(sizeof(long long) * (nslots + 1)));
-    MF_TRY(ws.slot_idx.ensure(sizeof(int) * nslots * kPkCap));
-    MF_TRY(ws.slot_val.ensure(sizeof(T) * nslots * kPkCap));
+    if (fused) MF_TRY(ws.ht.ensure(nslots));
+    else
+    {
+        MF_TRY(ws.slot_idx.ensure(sizeof(int) * nslots * kPkCap));
+        MF_TRY(ws.slot_val.ensure(sizeof(T) * nslots * kPkCap));
+    }
     MF_TRY(ws.counter.ensure(4 * sizeof(int)));  // [0] undecided after the last round, [1] overflow
     MF_TRY(cudaMemcpyAsync(ws.row.p, host_rows, sizeof(int) * ntr, cudaMemcpyHostToDevice, s));
     int *undecided = ws.counter.as<int>(), *overflow = ws.counter.as<int>() + 1;
@@ -74,18 +81,27 @@ int run_peaks(const T *x, long ldx, const int *host_rows, int ntr, int len, doub
         MF_TRY(ws.tiles.ensure(sizeof(long long) * (scan_tiles_needed(std::max<long>((long) nslots, (long) cap) + 1) + 8)));
         MF_TRY(cudaMemsetAsync(ws.counter.p, 0, 4 * sizeof(int), s));
 
-        peak_cand_kernel<T><<<grid, kPkThreads, 0, s>>>(tr, nchunks, ws.counts.as<int>(), ws.slot_idx.as<int>(),
-                                                        ws.slot_val.as<T>());
+        if (fused)
+            peak_seam_kernel<T><<<(unsigned) ((nslots + 255) / 256), 256, 0, s>>>(tr, ntr, *fused, ws.counts.as<int>(),
+                                                                                ws.ht.as<unsigned char>());
+        else
+            peak_cand_kernel<T><<<grid, kPkThreads, 0, s>>>(tr, nchunks, ws.counts.as<int>(), ws.slot_idx.as<int>(),
+                                                            ws.slot_val.as<T>());
         ++*launches;
         MF_TRY(cudaGetLastError());
         MF_TRY(device_excl_scan(ws.counts.as<int>(), (long) nslots, ws.offs.as<long long>(),
                                 ws.tiles.as<long long>(), s, launches));
         peak_trace_beg_kernel<<<(ntr + 1 + 127) / 128, 128, 0, s>>>(ntr, nchunks, ws.offs.as<long long>(), cap,
                                                                     ws.trace_beg.as<long long>());
-        peak_gather_kernel<T><<<grid, kPkThreads, 0, s>>>(tr, nchunks, ws.counts.as<int>(), ws.offs.as<long long>(),
-                                                          ws.slot_idx.as<int>(), ws.slot_val.as<T>(),
-                                                          ws.cidx.as<int>(), ws.cval.as<T>(), ws.ctr.as<int>(), cap,
-                                                          overflow);
+        if (fused)
+            peak_gather_fused_kernel<T><<<grid, kPkThreads, 0, s>>>(
+                tr, *fused, ws.counts.as<int>(), ws.ht.as<unsigned char>(), ws.offs.as<long long>(), ws.cidx.as<int>(),
+                ws.cval.as<T>(), ws.ctr.as<int>(), cap, overflow);
+        else
+            peak_gather_kernel<T><<<grid, kPkThreads, 0, s>>>(tr, nchunks, ws.counts.as<int>(),
+                                                              ws.offs.as<long long>(), ws.slot_idx.as<int>(),
+                                                              ws.slot_val.as<T>(), ws.cidx.as<int>(), ws.cval.as<T>(),
+                                                              ws.ctr.as<int>(), cap, overflow);
         *launches += 2;
         MF_TRY(cudaGetLastError());
         const unsigned gblocks = (unsigned) ((cap + kPkThreads - 1) / kPkThreads);
@@ -154,9 +170,9 @@ int run_peaks(const T *x, long ldx, const int *host_rows, int ntr, int len, doub
     return -1;
 }
 template int run_peaks<float>(const float *, long, const int *, int, int, double, int, PeakWS &, cudaStream_t,
-                              long long *, long long *, std::string &);
+                              long long *, long long *, std::string &, const FusedSlots<float> *);
 template int run_peaks<double>(const double *, long, const int *, int, int, double, int, PeakWS &, cudaStream_t,
-                               long long *, long long *, std::string &);
+                               long long *, long long *, std::string &, const FusedSlots<double> *);
 
 int run_dbscan(int n, int nf, const double *X, const double *w, double eps, int min_obs, int nseg,
                const int *seg_off_host, int *labels_host, int *nclusters_host, DbWS &ws, cudaStream_t s,

@@ -328,9 +328,28 @@ class MatchedFilter:
         _lib.call("mfgpu_mf_get_launch_count", self._h, C.byref(v))
         return v.value
 
+    def stream_handle(self):
+        """The object's cudaStream_t as an integer (every launch and copy of
+        the object is issued on it)."""
+        v = C.c_void_p()
+        _lib.call("mfgpu_mf_get_stream", self._h, C.byref(v))
+        return v.value or 0
+
     def find_peaks(self, threshold, min_distance, trace_length=0):
         """PeakFinder<T>::apply on every template's coefficients, on the device."""
         _lib.call("mfgpu_mf_find_peaks", self._h, float(threshold), int(min_distance), int(trace_length))
+
+    def set_peak_threshold(self, threshold):
+        """From the next apply on, gather the peak candidates above
+        ``threshold`` inside the correlator (None or a negative value: off);
+        find_peaks with that threshold then skips its scan of the traces."""
+        _lib.call("mfgpu_mf_set_peak_threshold", self._h, -1.0 if threshold is None else float(threshold))
+
+    def get_peak_threshold(self):
+        """(requested gathering threshold or None, whether the last apply gathered)."""
+        v, a = C.c_double(), C.c_int()
+        _lib.call("mfgpu_mf_get_peak_threshold", self._h, C.byref(v), C.byref(a))
+        return (None if v.value < 0 else v.value), bool(a.value)
 
     def get_peaks(self, it):
         cap = max(1, self.get_signal_length())

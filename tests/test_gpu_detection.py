@@ -178,3 +178,126 @@ def test_dbscan_segmented(gpu, oracle, rng):
         n_ref, lab_ref = oracle.dbscan(seg, 50.0, 3)
         assert ncl[s] == n_ref
         np.testing.assert_array_equal(labels[off[s]:off[s + 1]], lab_ref)
+
+
+def _fused_case(mf, rng, dtype, lens, n=60_000, nch=2):
+    """Channels of noise with copies of the templates injected, templates
+    assigned round-robin to the channels."""
+    chans = [rng.standard_normal(n) for _ in range(nch)]
+    tps = []
+    for i, L in enumerate(lens):
+        c = i % nch
+        start = int(rng.integers(0, n - L))
+        tp = chans[c][start:start + L].copy()
+        tps.append(tp)
+        for s in rng.integers(0, n - L, 6):
+            chans[c][s:s + L] += rng.uniform(0.5, 2.0) * tp
+    p = mf.MultiChannel.MatchedFilterParameters()
+    for t in tps:
+        wt = mf.WaveformTemplate()
+        wt.set_signal(t)
+        wt.set_sampling_rate(100.0)
+        p.add_template(wt)
+    p.set_signal_size(n)
+    assign = [i % nch for i in range(len(lens))]
+    return p, [c.astype(dtype) for c in chans], assign
+
+
+def _filter(mf, p, chans, assign, dtype, **kw):
+    f = mf.MultiChannel.MatchedFilter(dtype=dtype)
+    f.initialize(p, template_channels=assign, n_channels=len(chans), **kw)
+    for c, s in enumerate(chans):
+        f.set_channel_signal(c, s)
+    return f
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("variant", [1, 2, 3])
+@pytest.mark.parametrize("fft_length", [256, 1024, 4096])
+def test_fused_peak_candidates(gpu, oracle, rng, dtype, variant, fft_length):
+    """Candidates gathered inside the correlator give exactly the peaks of
+    the stand-alone scan and of the oracle, including chunks with more
+    candidates than slots (threshold 0), block seams and the last lag."""
+    mf = gpu
+    if dtype == np.float64 and variant == 2 and fft_length == 4096:
+        pytest.skip("FP64 spectrum prefetch at N = 4096 exceeds the shared memory of a CTA")
+    lens = [150] * 6
+    p, chans, assign = _fused_case(mf, rng, dtype, lens)
+    plain = _filter(mf, p, chans, assign, dtype, fft_length=fft_length, correlator_variant=variant)
+    plain.apply()
+    for thr, md in ((0.0, 0), (0.0, 40), (0.35, 0), (0.35, 150), (0.8, 300)):
+        f = _filter(mf, p, chans, assign, dtype, fft_length=fft_length, correlator_variant=variant)
+        f.set_peak_threshold(thr)
+        f.apply()
+        assert f.get_peak_threshold() == (thr, True)
+        f.find_peaks(thr, md)
+        counts, idx = f.get_all_peaks()
+        plain.find_peaks(thr, md)
+        counts0, idx0 = plain.get_all_peaks()
+        np.testing.assert_array_equal(counts, counts0)
+        np.testing.assert_array_equal(idx, idx0)
+        off = 0
+        for i in range(len(lens)):
+            rho = f.get_matched_filtered_signal(i).astype(np.float64)
+            np.testing.assert_array_equal(rho, plain.get_matched_filtered_signal(i).astype(np.float64))
+            ref = oracle.peaks(rho, thr, md)
+            np.testing.assert_array_equal(idx[off:off + counts[i]], ref)
+            off += counts[i]
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_fused_peak_candidates_mixed_lengths(gpu, oracle, rng, dtype):
+    """Templates of several lengths: the peak trace stops at n - Lmax + 1
+    lags, inside the shorter templates' valid range."""
+    mf = gpu
+    lens = [90, 200, 333, 120, 201]
+    p, chans, assign = _fused_case(mf, rng, dtype, lens, n=45_001)
+    f = _filter(mf, p, chans, assign, dtype, fft_length=2048)
+    f.set_peak_threshold(0.0)
+    f.apply()
+    plain = _filter(mf, p, chans, assign, dtype, fft_length=2048)
+    plain.apply()
+    for md in (0, 25):
+        f.find_peaks(0.0, md)
+        plain.find_peaks(0.0, md)
+        c1, i1 = f.get_all_peaks()
+        c0, i0 = plain.get_all_peaks()
+        np.testing.assert_array_equal(c1, c0)
+        np.testing.assert_array_equal(i1, i0)
+        off = 0
+        for i in range(len(lens)):
+            rho = f.get_matched_filtered_signal(i).astype(np.float64)
+            np.testing.assert_array_equal(i1[off:off + c1[i]], oracle.peaks(rho, 0.0, md))
+            off += c1[i]
+
+
+def test_fused_peak_threshold_switching(gpu, rng):
+    """Another threshold or trace length, a short FFT, or gathering turned
+    off all fall back to the scan and give the same peaks."""
+    mf = gpu
+    p, chans, assign = _fused_case(mf, rng, np.float32, [150] * 4, n=30_000)
+    f = _filter(mf, p, chans, assign, np.float32, fft_length=1024)
+    g = _filter(mf, p, chans, assign, np.float32, fft_length=1024)
+    g.apply()
+    f.set_peak_threshold(0.4)
+    f.apply()
+    for thr, md, tl in ((0.4, 50, 0), (0.5, 50, 0), (0.4, 50, 20_000)):
+        f.find_peaks(thr, md, tl)
+        g.find_peaks(thr, md, tl)
+        for a, b in zip(f.get_all_peaks(), g.get_all_peaks()):
+            np.testing.assert_array_equal(a, b)
+    f.set_peak_threshold(None)
+    f.apply()
+    assert f.get_peak_threshold() == (None, False)
+    with pytest.raises(ValueError):
+        f.set_peak_threshold(1.5)
+    s = _filter(mf, p, chans, assign, np.float32, fft_length=256)
+    s.set_peak_threshold(0.4)
+    s.apply()
+    assert s.get_peak_threshold() == (0.4, True)
+    t = _filter(mf, p, chans, assign, np.float32, fft_length=256)
+    t.apply()
+    s.find_peaks(0.4, 50)
+    t.find_peaks(0.4, 50)
+    for a, b in zip(s.get_all_peaks(), t.get_all_peaks()):
+        np.testing.assert_array_equal(a, b)
