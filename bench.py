@@ -280,8 +280,7 @@ def main():
     host = pinned.numpy()
 
     def load_all():
-        for c in range(w["nch"]):
-            f.set_channel_signal(c, host[c])
+        f.set_channel_signals(host)
 
     def step():
         f.apply()

@@ -135,6 +135,11 @@ mfgpu_status mfgpu_mf_get_spectra_of_template(mfgpu_mf *mf, int it, int maxn, vo
 /* Extensions (no reference counterpart) --------------------------------- */
 /* Signal of channel c (n_channels > 0 layout), host samples. */
 mfgpu_status mfgpu_mf_set_channel_signal(mfgpu_mf *mf, int channel, int n, const void *x);
+/* Signals of channels [first_channel, first_channel + n_channels) from one
+ * host array: row r (n samples) starts at x + r * ld samples.  One copy and
+ * one dead-trace pass for all rows; returns when the rows are copied. */
+mfgpu_status mfgpu_mf_set_channel_signals(mfgpu_mf *mf, int first_channel, int n_channels, int n, const void *x,
+                                          long ld);
 /* Signal of channel c from device memory (same type, n samples). */
 mfgpu_status mfgpu_mf_set_channel_signal_device(mfgpu_mf *mf, int channel, int n, const void *dx);
 /* Full valid coefficient range of template it: lags 0..n-L_t (n - L_t + 1

@@ -428,10 +428,12 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
     if (all_equal)
     {
         // per-channel normalisation rows read by the correlator (S lags per
-        // block) and written by den_kernel (kDenLags lags per CTA)
-        mf->nden = (std::max(1, maxvalid) + kDenLags - 1) / kDenLags;
-        mf->ldd = (std::max<long>((long) mf->nblocks * best_S, (long) mf->nden * kDenLags) + 63) / 64 * 64;
-        mf->ldx = std::max<long>(mf->ldx, ((long) mf->nden * kDenLags + maxLen + 63) / 64 * 64);
+        // block) and written by den_kernel (den_lags_per_cta lags per CTA,
+        // reading 32 * den_tail_runs samples past them)
+        const long lpc = den_lags_per_cta(maxLen);
+        mf->nden = (int) ((std::max(1, maxvalid) + lpc - 1) / lpc);
+        mf->ldd = (std::max<long>((long) mf->nblocks * best_S + 32, (long) mf->nden * lpc) + 63) / 64 * 64;
+        mf->ldx = std::max<long>(mf->ldx, ((long) mf->nden * lpc + 32L * den_tail_runs(maxLen) + 63) / 64 * 64);
     }
     // work groups: split each channel's templates so the grid has enough CTAs
     int G = std::max(1, max_tpc);
@@ -456,7 +458,7 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
         }
     }
     mf->ngroups = (int) gch.size();
-    mf->dead_chunks = (int) std::min<long>(1024, std::max<long>(1, (n + 65535) / 65536));
+    mf->dead_chunks = (int) std::min<long>(1024, std::max<long>(1, (n + 16383) / 16384));
 
     // ---- device memory
     const size_t es = mf->esz();
@@ -559,28 +561,41 @@ static mfgpu_status mf_channel_of(mfgpu_mf *mf, int it, int *c)
     return MFGPU_OK;
 }
 
-static mfgpu_status mf_store_signal(mfgpu_mf *mf, int c, int n, const void *x, cudaMemcpyKind kind)
+// Copies nch channel rows (n samples each, source row stride ld samples)
+// into channels [c0, c0 + nch) and recomputes their dead-trace flags.
+static mfgpu_status mf_store_signals(mfgpu_mf *mf, int c0, int nch, int n, const void *x, long ld,
+                                     cudaMemcpyKind kind)
 {
     if (n != mf->n)
         return fail(MFGPU_EINVAL, "Number of samples = " + std::to_string(n) + " must equal" + std::to_string(mf->n));
     if (!x) return fail(MFGPU_EINVAL, "x is NULL");
+    if (nch > 1 && ld < n) return fail(MFGPU_EINVAL, "row stride is smaller than the number of samples");
     mf->have = false;
     mf->have_peaks = false;
     const size_t es = mf->esz();
-    char *row = mf->x.as<char>() + es * (size_t) c * mf->ldx;
-    CU(cudaMemcpyAsync(row, x, es * (size_t) n, kind, mf->stream));
-    unsigned char *dflag = mf->dead.as<unsigned char>() + c;
-    const size_t poff = (size_t) c * mf->dead_chunks;
-    if (mf->prec == 4)
-        CU(launch_dead<float>(reinterpret_cast<const float *>(row), mf->n, dflag, mf->pmin.as<float>() + poff,
-                              mf->pmax.as<float>() + poff, mf->dead_chunks, mf->stream));
+    char *row = mf->x.as<char>() + es * (size_t) c0 * mf->ldx;
+    if (nch == 1) CU(cudaMemcpyAsync(row, x, es * (size_t) n, kind, mf->stream));
     else
-        CU(launch_dead<double>(reinterpret_cast<const double *>(row), mf->n, dflag, mf->pmin.as<double>() + poff,
-                               mf->pmax.as<double>() + poff, mf->dead_chunks, mf->stream));
+        CU(cudaMemcpy2DAsync(row, es * (size_t) mf->ldx, x, es * (size_t) ld, es * (size_t) n, (size_t) nch, kind,
+                             mf->stream));
+    unsigned char *dflag = mf->dead.as<unsigned char>() + c0;
+    const size_t poff = (size_t) c0 * mf->dead_chunks;
+    if (mf->prec == 4)
+        CU(launch_dead<float>(reinterpret_cast<const float *>(row), mf->ldx, nch, mf->n, dflag,
+                              mf->pmin.as<float>() + poff, mf->pmax.as<float>() + poff, mf->dead_chunks, mf->stream));
+    else
+        CU(launch_dead<double>(reinterpret_cast<const double *>(row), mf->ldx, nch, mf->n, dflag,
+                               mf->pmin.as<double>() + poff, mf->pmax.as<double>() + poff, mf->dead_chunks,
+                               mf->stream));
     mf->launches += 2;
     // the reference copies the caller's samples before returning
     CU(cudaStreamSynchronize(mf->stream));
     return MFGPU_OK;
+}
+
+static mfgpu_status mf_store_signal(mfgpu_mf *mf, int c, int n, const void *x, cudaMemcpyKind kind)
+{
+    return mf_store_signals(mf, c, 1, n, x, n, kind);
 }
 
 mfgpu_status mfgpu_mf_set_signal(mfgpu_mf *mf, int it, int n, const void *x)
@@ -599,6 +614,16 @@ mfgpu_status mfgpu_mf_set_channel_signal(mfgpu_mf *mf, int channel, int n, const
     DeviceGuard g(mf->dev);
     if (channel < 0 || channel >= mf->nch) return fail(MFGPU_EINVAL, "channel out of range");
     return mf_store_signal(mf, channel, n, x, cudaMemcpyHostToDevice);
+}
+
+mfgpu_status mfgpu_mf_set_channel_signals(mfgpu_mf *mf, int first_channel, int n_channels, int n, const void *x,
+                                          long ld)
+{
+    MF_CHECK_INIT(mf);
+    DeviceGuard g(mf->dev);
+    if (n_channels < 1 || first_channel < 0 || first_channel + n_channels > mf->nch)
+        return fail(MFGPU_EINVAL, "channel range out of range");
+    return mf_store_signals(mf, first_channel, n_channels, n, x, ld, cudaMemcpyHostToDevice);
 }
 
 mfgpu_status mfgpu_mf_set_channel_signal_device(mfgpu_mf *mf, int channel, int n, const void *dx)

@@ -705,177 +705,281 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
 
 // ----------------------------------------------------------------------------
 // Per-channel normalisation for one template length L (normalizeSignal,
-// src/matchedFilter.cpp:94-166): den[c][k] = sqrt(L)/max(tol, sqrt(max(0,
-// L s2 - s1^2))) where s1, s2 are the sums of y and y^2 over [k, k+L) and
-// y = x - m (m = mean of the CTA's samples; both sums are shift-invariant in
-// the variance).  One CTA per (8192 lags, channel): the samples are staged
-// in shared memory with one pad word per 32 (conflict-free strided access),
-// exact prefix sums are formed at multiples of 32, and thread u slides over
-// lags [32u, 32u+32) in double-float (double for FP64 data).
+// src/matchedFilter.cpp:94-166): den[c][k] = sqrt(L)/max(tol, sqrt(max(0, V_k)))
+// with V_k = L s2 - s1^2, where s1, s2 are the sums of y and y^2 over
+// [k, k+L) and y = x - m (m = mean of the CTA's samples; V is invariant to
+// the shift).
+//
+// One CTA per (lag block, channel).  The CTA stages 32 * kThreads * R
+// samples (R = den_runs_per_thread(L)) in shared memory with one pad word per
+// 32 (conflict-free strided access) and covers den_lags_per_cta(L) =
+// 32 (kThreads R - ceil(L/32)) lags, so every thread sums exactly R runs.
+//   1. Sums of y and y^2 over each 32-sample run, and over its first L mod 32
+//      samples, to about 48 bits for FP32 data (TwoSum / TwoProd with a
+//      deferred low word) and in double for FP64 data.
+//   2. Block-wide exclusive scans of the run sums.
+//   3. Thread u owns the 32-lag runs v = u + kThreads i: the exact V at lag
+//      32v comes from the prefixes (double-float), then 32 lags of
+//      corrections in the data type,
+//        V_k = V_{32v} + L D2 - D1 (D1 + 2 s1_{32v}),
+//      D1 = sum of (y_in - y_out), D2 = sum of (y_in + y_out)(y_in - y_out)
+//      over the lags slid so far.  The corrections involve at most 64
+//      samples against the L of the window, so their rounding error stays a
+//      small multiple of the unit roundoff of V (times 1 + |window mean| /
+//      window deviation), unlike a plain running sum over the whole trace.
 constexpr int kDenRun = 32;
-constexpr int kDenLags = kThreads * kDenRun;
-constexpr int kDenMaxRunsPerLane = 16;  // supports L <= 8192
+__host__ __device__ constexpr int den_tail_runs(int L) { return (L + kDenRun - 1) / kDenRun; }
+__host__ __device__ constexpr int den_runs_per_thread(int L) { return 1 + den_tail_runs(L) / (kThreads / 2); }
+__host__ __device__ constexpr int den_lags_per_cta(int L)
+{
+    return kDenRun * (kThreads * den_runs_per_thread(L) - den_tail_runs(L));
+}
 __host__ __device__ constexpr int den_pad(int i) { return i + (i >> 5); }
 
 template <class T> struct DenLayout
 {
     using acc = typename acc_t<T>::type;
-    static constexpr int nruns(int L) { return (kDenLags + L + kDenRun - 1) / kDenRun; }
+    static constexpr int nruns(int L) { return kThreads * den_runs_per_thread(L); }
     static constexpr size_t y_bytes(int L)
     {
-        return ((sizeof(T) * (size_t) (den_pad(nruns(L) * kDenRun) + 32)) + 15) & ~size_t(15);
+        return ((sizeof(T) * (size_t) den_pad(nruns(L) * kDenRun)) + 15) & ~size_t(15);
     }
-    static constexpr size_t bytes(int L) { return y_bytes(L) + 2 * sizeof(acc) * (size_t) (nruns(L) + 1) + 32 * sizeof(T); }
+    // prefixes P1, P2 (nruns + 1 each), partial sums Q1, Q2 (nruns each),
+    // warp totals (2 x 32), block-sum scratch
+    static constexpr size_t bytes(int L)
+    {
+        return y_bytes(L) + sizeof(acc) * (4 * (size_t) nruns(L) + 2 + 64) + 32 * sizeof(T);
+    }
 };
 
-// Sliding update of the window sums by one lag, and the normalisation of a
-// window.  FP32 data: double-float with the "sloppy" addition (one TwoSum,
-// about 44 significant bits, enough within a 32-lag run that restarts from
-// exact prefixes) and a reciprocal square root; FP64 data: plain double.
-template <class T> struct DenSlide;
-template <> struct DenSlide<float>
+template <class T> struct DenOps;
+template <> struct DenOps<float>
 {
-    static __device__ __forceinline__ df add_sloppy(df a, df b)
+    using acc = df;
+    // run sums with deferred low words
+    struct Run { float h1, l1, h2, l2; };
+    static __device__ __forceinline__ Run run_zero() { return Run{0.f, 0.f, 0.f, 0.f}; }
+    static __device__ __forceinline__ df zero() { return df{0.f, 0.f}; }
+    static __device__ __forceinline__ void run_add(Run &s, float v)
+    {
+        const float t = s.h1 + v, bb = t - s.h1;
+        s.l1 += (s.h1 - (t - bb)) + (v - bb);
+        s.h1 = t;
+        const float p = v * v, pe = fmaf(v, v, -p);
+        const float u = s.h2 + p, b2 = u - s.h2;
+        s.l2 += ((s.h2 - (u - b2)) + (p - b2)) + pe;
+        s.h2 = u;
+    }
+    static __device__ __forceinline__ df s1(const Run &s) { return quick_two_sum(s.h1, s.l1); }
+    static __device__ __forceinline__ df s2(const Run &s) { return quick_two_sum(s.h2, s.l2); }
+    // addition for the scans: one TwoSum, low words added (about 44 bits)
+    static __device__ __forceinline__ df add(df a, df b)
     {
         df s = two_sum(a.hi, b.hi);
         s.lo += a.lo + b.lo;
         return quick_two_sum(s.hi, s.lo);
     }
-    static __device__ __forceinline__ void step(df &w1, df &w2, float vin, float vout)
+    static __device__ __forceinline__ df neg(df a) { return df{-a.hi, -a.lo}; }
+    static __device__ __forceinline__ df shfl_up(df a, int d)
     {
-        w1 = add_sloppy(w1, two_sum(vin, -vout));
-        df pi = two_prod(vin, vin), po = two_prod(vout, vout);
-        df d = two_sum(pi.hi, -po.hi);
-        d.lo += pi.lo - po.lo;
-        w2 = add_sloppy(w2, d);
+        return df{__shfl_up_sync(0xffffffffu, a.hi, d), __shfl_up_sync(0xffffffffu, a.lo, d)};
     }
-    // sqrt(L)/max(tol, sqrt(max(0, L w2 - w1^2)))
-    static __device__ __forceinline__ float inv(df w1, df w2, int L, float sqrtL, float tol)
+    // V = L s2 - s1^2 as (hi, lo)
+    static __device__ __forceinline__ void var0(df w1, df w2, int L, float &vh, float &vl)
     {
         df a = two_prod((float) L, w2.hi);
         a.lo = fmaf((float) L, w2.lo, a.lo);
         df b = two_prod(w1.hi, w1.hi);
         b.lo = fmaf(2.f * w1.hi, w1.lo, b.lo);
-        df v = two_sum(a.hi, -b.hi);
-        const float var = v.hi + (v.lo + (a.lo - b.lo));
+        const df v = two_sum(a.hi, -b.hi);
+        vh = v.hi;
+        vl = v.lo + (a.lo - b.lo);
+    }
+    static __device__ __forceinline__ float hi(df a) { return a.hi; }
+    static __device__ __forceinline__ float out(float var, float sqrtL, float tol)
+    {
         return var > tol * tol ? sqrtL * rsqrtf(var) : sqrtL / tol;
     }
 };
-template <> struct DenSlide<double>
+template <> struct DenOps<double>
 {
-    static __device__ __forceinline__ void step(double &w1, double &w2, double vin, double vout)
+    using acc = double;
+    struct Run { double a1, a2; };
+    static __device__ __forceinline__ Run run_zero() { return Run{0.0, 0.0}; }
+    static __device__ __forceinline__ double zero() { return 0.0; }
+    static __device__ __forceinline__ void run_add(Run &s, double v)
     {
-        w1 += vin - vout;
-        w2 = fma(vin, vin, fma(-vout, vout, w2));
+        s.a1 += v;
+        s.a2 = fma(v, v, s.a2);
     }
-    static __device__ __forceinline__ double inv(double w1, double w2, int L, double sqrtL, double tol)
+    static __device__ __forceinline__ double s1(const Run &s) { return s.a1; }
+    static __device__ __forceinline__ double s2(const Run &s) { return s.a2; }
+    static __device__ __forceinline__ double add(double a, double b) { return a + b; }
+    static __device__ __forceinline__ double neg(double a) { return -a; }
+    static __device__ __forceinline__ double shfl_up(double a, int d) { return __shfl_up_sync(0xffffffffu, a, d); }
+    static __device__ __forceinline__ void var0(double w1, double w2, int L, double &vh, double &vl)
     {
-        const double var = (double) L * w2 - w1 * w1;
+        vh = fma((double) L, w2, -w1 * w1);
+        vl = 0.0;
+    }
+    static __device__ __forceinline__ double hi(double a) { return a; }
+    static __device__ __forceinline__ double out(double var, double sqrtL, double tol)
+    {
         return sqrtL / fmax(sqrt(fmax(var, 0.0)), tol);
     }
 };
 
+// Exclusive block scan of one accumulator per thread; *total = block sum.
+// wsum: 32 entries of scratch.
+template <class T>
+__device__ __forceinline__ typename DenOps<T>::acc den_block_scan(typename DenOps<T>::acc v,
+                                                                  typename DenOps<T>::acc *wsum,
+                                                                  typename DenOps<T>::acc *total)
+{
+    using O = DenOps<T>;
+    using acc = typename O::acc;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    acc x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const acc y = O::shfl_up(x, o);
+        if (lane >= o) x = O::add(x, y);
+    }
+    acc ex = O::shfl_up(x, 1);
+    __syncthreads();  // wsum free
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    if (w == 0)
+    {
+        acc t = lane < kThreads / 32 ? wsum[lane] : O::zero();
+#pragma unroll
+        for (int o = 1; o < kThreads / 32; o <<= 1)
+        {
+            const acc y = O::shfl_up(t, o);
+            if (lane >= o) t = O::add(t, y);
+        }
+        if (lane < kThreads / 32) wsum[lane] = t;  // inclusive warp offsets
+    }
+    __syncthreads();
+    *total = wsum[kThreads / 32 - 1];
+    if (w > 0) ex = lane > 0 ? O::add(ex, wsum[w - 1]) : wsum[w - 1];
+    else if (lane == 0) ex = O::zero();
+    return ex;
+}
+
 template <class T>
 __global__ void __launch_bounds__(kThreads) den_kernel(const T *x, long ldx, int L, T *den, long ldd, T tol)
 {
-    using A = acc_t<T>;
-    using acc = typename A::type;
+    using O = DenOps<T>;
+    using acc = typename O::acc;
     extern __shared__ __align__(16) unsigned char smem_den[];
-    const int tid = threadIdx.x, lane = tid & 31;
+    const int tid = threadIdx.x;
     const int c = blockIdx.y;
-    const long k0 = (long) blockIdx.x * kDenLags;
-    const int nseg = kDenLags + L;
-    const int nruns = DenLayout<T>::nruns(L);
+    const int R = den_runs_per_thread(L);
+    const int nruns = kThreads * R;
+    const int lpc = den_lags_per_cta(L);
+    const long k0 = (long) blockIdx.x * lpc;
     T *y = reinterpret_cast<T *>(smem_den);
-    acc *r1 = reinterpret_cast<acc *>(smem_den + DenLayout<T>::y_bytes(L));
-    acc *r2 = r1 + (nruns + 1);
-    T *red = reinterpret_cast<T *>(r2 + (nruns + 1));
+    acc *P1 = reinterpret_cast<acc *>(smem_den + DenLayout<T>::y_bytes(L));
+    acc *P2 = P1 + (nruns + 1);
+    acc *Q1 = P2 + (nruns + 1);
+    acc *Q2 = Q1 + nruns;
+    acc *wsum = Q2 + nruns;
+    T *red = reinterpret_cast<T *>(wsum + 64);
+
+    // ---- stage 32 * nruns samples (16-byte loads; k0 and ldx are multiples of 32)
     const T *xr = x + (long) c * ldx + k0;
+    constexpr int VW = 16 / sizeof(T);
     T s = 0;
-    for (int i = tid; i < nruns * kDenRun; i += kThreads)
+    for (int i = tid; i < nruns * kDenRun / VW; i += kThreads)
     {
-        const T v = i < nseg ? xr[i] : (T) 0;
-        y[den_pad(i)] = v;
-        s += v;
+        T v[VW];
+        if constexpr (sizeof(T) == 4)
+        {
+            const float4 a = reinterpret_cast<const float4 *>(xr)[i];
+            v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        }
+        else
+        {
+            const double2 a = reinterpret_cast<const double2 *>(xr)[i];
+            v[0] = a.x; v[1] = a.y;
+        }
+#pragma unroll
+        for (int q = 0; q < VW; ++q)
+        {
+            y[den_pad(VW * i + q)] = v[q];
+            s += v[q];
+        }
     }
-    const T m = block_sum<T>(s, red) / (T) nseg;
-    // sums over runs of 32 samples (run j at padded offset 33 j)
-    for (int j = tid; j < nruns; j += kThreads)
+    const T m = block_sum<T>(s, red) / (T) (nruns * kDenRun);
+
+    // ---- run sums (run j = tid + kThreads r) and partial sums of the first re samples
+    const int re = L & (kDenRun - 1), Lq = L >> 5;
+    acc c1 = O::zero(), c2 = O::zero();  // running carries over the rounds
+    for (int r = 0; r < R; ++r)
     {
-        acc a1 = A::zero(), a2 = A::zero();
-#pragma unroll 8
+        const int j = tid + kThreads * r;
+        typename O::Run a = O::run_zero(), pa = O::run_zero();
+#pragma unroll
         for (int q = 0; q < kDenRun; ++q)
         {
-            const T v = y[33 * j + q] - m;
-            a1 = A::add_val(a1, v);
-            a2 = A::add_sq(a2, v);
+            if (q == re) pa = a;
+            O::run_add(a, y[33 * j + q] - m);
         }
-        r1[j + 1] = a1;
-        r2[j + 1] = a2;
+        const acc a1 = O::s1(a), a2 = O::s2(a);
+        Q1[j] = O::s1(pa);
+        Q2[j] = O::s2(pa);
+        acc t1, t2;
+        const acc e1 = den_block_scan<T>(a1, wsum, &t1);
+        const acc e2 = den_block_scan<T>(a2, wsum + 32, &t2);
+        P1[j] = O::add(c1, e1);
+        P2[j] = O::add(c2, e2);
+        c1 = O::add(c1, t1);
+        c2 = O::add(c2, t2);
     }
+    if (tid == 0) { P1[nruns] = c1; P2[nruns] = c2; }
     __syncthreads();
-    // exclusive prefix over the runs (warp 0): r[j] = sum of runs < j
-    if (tid < 32)
-    {
-        const int per = (nruns + 31) / 32;
-        acc v1[kDenMaxRunsPerLane], v2[kDenMaxRunsPerLane];
-        acc t1 = A::zero(), t2 = A::zero();
-#pragma unroll
-        for (int i = 0; i < kDenMaxRunsPerLane; ++i)
-        {
-            const int j = lane * per + i;
-            const bool ok = i < per && j < nruns;
-            v1[i] = ok ? r1[j + 1] : A::zero();
-            v2[i] = ok ? r2[j + 1] : A::zero();
-            t1 = A::add(t1, v1[i]);
-            t2 = A::add(t2, v2[i]);
-        }
-        __syncwarp();
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1)
-        {
-            acc u1 = A::shfl_up(t1, o), u2 = A::shfl_up(t2, o);
-            if (lane >= o) { t1 = A::add(t1, u1); t2 = A::add(t2, u2); }
-        }
-        acc e1 = A::shfl_up(t1, 1), e2 = A::shfl_up(t2, 1);
-        if (lane == 0) { e1 = A::zero(); e2 = A::zero(); }
-#pragma unroll
-        for (int i = 0; i < kDenMaxRunsPerLane; ++i)
-        {
-            const int j = lane * per + i;
-            if (i < per && j < nruns)
-            {
-                r1[j] = e1;
-                r2[j] = e2;
-                e1 = A::add(e1, v1[i]);
-                e2 = A::add(e2, v2[i]);
-                if (j == nruns - 1) { r1[nruns] = e1; r2[nruns] = e2; }
-            }
-        }
-    }
-    __syncthreads();
-    // thread u: lags [32u, 32u + 32); first window from the prefixes plus the
-    // L % 32 samples past the last full run
-    const int ks = kDenRun * tid;
-    const int je = tid + (L >> 5), re = L & 31;
-    acc b1 = r1[je], b2 = r2[je];
-    for (int q = 0; q < re; ++q)
-    {
-        const T v = y[33 * je + q] - m;
-        b1 = A::add_val(b1, v);
-        b2 = A::add_sq(b2, v);
-    }
-    acc w1 = A::sub(b1, r1[tid]), w2 = A::sub(b2, r2[tid]);
-    T *dr = den + (long) c * ldd + k0 + ks;
+
+    // ---- lag runs v = tid + kThreads i, 32 lags each
     const T sqrtL = sqrt((T) L);
-#pragma unroll
-    for (int q = 0; q < kDenRun; q += 2)
+    const T Lt = (T) L;
+    const int nlr = lpc / kDenRun;
+    T *drow = den + (long) c * ldd + k0;
+    for (int v = tid; v < nlr; v += kThreads)
     {
-        const T o0 = DenSlide<T>::inv(w1, w2, L, sqrtL, tol);
-        DenSlide<T>::step(w1, w2, y[den_pad(ks + q + L)] - m, y[den_pad(ks + q)] - m);
-        const T o1 = DenSlide<T>::inv(w1, w2, L, sqrtL, tol);
-        if (q + 2 < kDenRun) DenSlide<T>::step(w1, w2, y[den_pad(ks + q + 1 + L)] - m, y[den_pad(ks + q + 1)] - m);
-        store2<T>(dr + q, o0, o1);
+        // window [32v, 32v + L): prefixes at runs v and v + Lq, plus the
+        // first re samples of run v + Lq
+        const acc w1 = O::add(O::add(P1[v + Lq], Q1[v + Lq]), O::neg(P1[v]));
+        const acc w2 = O::add(O::add(P2[v + Lq], Q2[v + Lq]), O::neg(P2[v]));
+        T vh, vl;
+        O::var0(w1, w2, L, vh, vl);
+        const T c2s = (T) 2 * O::hi(w1);
+        T d1 = 0, d2 = 0;
+        T o[kDenRun];
+        const int base = 32 * v;
+#pragma unroll
+        for (int q = 0; q < kDenRun; ++q)
+        {
+            const T var = vh + (vl + fma(Lt, d2, -d1 * (d1 + c2s)));
+            o[q] = O::out(var, sqrtL, tol);
+            const T yin = y[den_pad(base + q + L)], yout = y[den_pad(base + q)];
+            const T dd = yin - yout;
+            d2 = fma(yin + yout - (T) 2 * m, dd, d2);
+            d1 += dd;
+        }
+        T *dr = drow + base;
+        if constexpr (sizeof(T) == 4)
+        {
+#pragma unroll
+            for (int q = 0; q < kDenRun; q += 4)
+                *reinterpret_cast<float4 *>(dr + q) = make_float4(o[q], o[q + 1], o[q + 2], o[q + 3]);
+        }
+        else
+        {
+#pragma unroll
+            for (int q = 0; q < kDenRun; q += 2) *reinterpret_cast<double2 *>(dr + q) = make_double2(o[q], o[q + 1]);
+        }
     }
 }
 
@@ -921,10 +1025,14 @@ __global__ void __launch_bounds__(kThreads) minmax_partial_kernel(const T *x, lo
     }
 }
 
+// one CTA per channel (blockIdx.x): partials pmin/pmax[c * nchunks + j]
 template <class T>
 __global__ void minmax_final_kernel(const T *pmin, const T *pmax, int nchunks, unsigned char *dead)
 {
     __shared__ T smin[32], smax[32];
+    pmin += (long) blockIdx.x * nchunks;
+    pmax += (long) blockIdx.x * nchunks;
+    dead += blockIdx.x;
     T mn = pmin[0], mx = pmax[0];
     for (int j = threadIdx.x; j < nchunks; j += blockDim.x)
     {

@@ -20,15 +20,15 @@ template <class T> size_t xcorr_smem_bytes(int log2p, bool shared_den, int mode,
 template <class T> cudaError_t launch_xcorr(int log2p, bool shared_den, int mode, const XcorrParams<T> &p,
                                             int nblocks, int ngroups, cudaStream_t s);
 template <class T> cudaError_t launch_spectra(int log2p, const SpecParams<T> &p, int nt, cudaStream_t s);
-// per-channel normalisation for template length L over nblocks * kDenLags lags
+// per-channel normalisation for template length L over nblocks * den_lags_per_cta(L) lags
 template <class T> cudaError_t launch_den(const T *x, long ldx, int L, T *den, long ldd, T tol, int nblocks, int nch,
                                           cudaStream_t s);
 // twiddle table of the FFT plan for P = 2^log2p (FftPlan layout)
 template <class T> void twiddle_table(int log2p, std::vector<cx<T>> &out);
-// dead-trace flag of one channel (row of n samples): two launches;
-// pmin/pmax are scratch of nchunks entries each
-template <class T> cudaError_t launch_dead(const T *x_row, long n, unsigned char *dead, T *pmin, T *pmax,
-                                           int nchunks, cudaStream_t s);
+// dead-trace flags of nch channels (rows of n samples, stride ldx): two
+// launches; pmin/pmax are scratch of nch * nchunks entries each
+template <class T> cudaError_t launch_dead(const T *x, long ldx, int nch, long n, unsigned char *dead, T *pmin,
+                                           T *pmax, int nchunks, cudaStream_t s);
 // reference debug spectrum of one prepared template at FFT length nfft
 template <class T> cudaError_t launch_ref_spectrum(const double *tmpl, int L, int nfft, T *out, cudaStream_t s);
 // shift and stack (src/matchedFilter.cpp:1319-1364)

@@ -251,6 +251,18 @@ class MatchedFilter:
         _lib.call("mfgpu_mf_set_channel_signal", self._h, int(channel), int(x.size),
                   x.ctypes.data_as(C.c_void_p))
 
+    def set_channel_signals(self, x, first_channel=0):
+        """Extension: signals of channels first_channel.. from the rows of a
+        2-D array (one copy and one dead-trace pass for all rows).  Rows may
+        be strided; pinned host memory makes the copy asynchronous DMA."""
+        x = np.asarray(x)
+        if x.ndim != 2:
+            raise ValueError("x must be 2-D (channels x samples)")
+        if x.dtype != self._dtype or x.strides[1] != x.itemsize or x.strides[0] % x.itemsize:
+            x = np.ascontiguousarray(x, dtype=self._dtype)
+        _lib.call("mfgpu_mf_set_channel_signals", self._h, int(first_channel), int(x.shape[0]), int(x.shape[1]),
+                  x.ctypes.data_as(C.c_void_p), int(x.strides[0] // x.itemsize))
+
     def zero_signal(self, it):
         _lib.call("mfgpu_mf_zero_signal", self._h, int(it))
 

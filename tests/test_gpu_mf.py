@@ -396,3 +396,66 @@ def test_repeat_apply_and_reinitialize(gpu, oracle, rng):
             f.apply()
             ref = oracle.matched_filter([tp], [sig], multi=False, fp64_from_f32=True)[0]
             assert np.max(np.abs(f.get_matched_filtered_signal(0) - ref)) < FP32_TOL
+
+
+def test_batched_channel_upload(gpu, rng):
+    """set_channel_signals (one copy, one dead-trace pass) stores the same
+    samples and dead flags as one set_channel_signal per channel, for
+    contiguous and strided rows and a channel sub-range."""
+    mf = gpu
+    n = 33_333
+    x = rng.standard_normal((5, n)).astype(np.float32)
+    x[3] = 0.0                       # dead channel
+    x[1, :] = 2.0
+    x[1, 7] = -2.0                   # |min| == |max|: dead as well
+    assign = [0, 1, 2, 3, 4, 0]
+    tps = [rng.standard_normal(64) for _ in assign]
+    p = _params(mf, tps, n)
+    f = mf.MultiChannel.MatchedFilter(dtype=np.float32)
+    f.initialize(p, template_channels=assign, n_channels=5)
+    g = mf.MultiChannel.MatchedFilter(dtype=np.float32)
+    g.initialize(p, template_channels=assign, n_channels=5)
+    wide = np.zeros((5, n + 17), dtype=np.float32)
+    wide[:, :n] = x
+    f.set_channel_signals(x[:2])
+    f.set_channel_signals(wide[2:, :n], first_channel=2)
+    for c in range(5):
+        g.set_channel_signal(c, x[c])
+    for h in (f, g):
+        h.apply()
+    for i in range(len(assign)):
+        np.testing.assert_array_equal(f.get_signal(i), x[assign[i]])
+        np.testing.assert_array_equal(f.get_matched_filtered_signal(i), g.get_matched_filtered_signal(i))
+    assert not np.any(f.get_matched_filtered_signal(3))
+    assert not np.any(f.get_matched_filtered_signal(1))
+    with pytest.raises(ValueError):
+        f.set_channel_signals(x, first_channel=1)
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+@pytest.mark.parametrize("L", [32, 33, 95, 511, 1024, 4097, 6000])
+def test_shared_length_normalisation(gpu, oracle, rng, dtype, L):
+    """Templates of one length use the per-channel normalisation kernel:
+    window lengths with L mod 32 = 0, 1, 31 and lengths that need two or
+    three 32-sample runs per thread; the signals carry an offset and a slow
+    drift of several standard deviations."""
+    mf = gpu
+    if dtype == np.float64 and L > 4065:
+        pytest.skip("the FP64 correlator's longest template is 4065 samples (N = 4096)")
+    n = 60_000 + L
+    t = np.arange(n)
+    chans = [rng.standard_normal(n) + 5.0 + 4.0 * np.sin(2 * np.pi * t / 20_000.0 + k) for k in range(2)]
+    assign = [0, 1, 1]
+    tps = [rng.standard_normal(L) for _ in assign]
+    p = _params(mf, tps, n)
+    f = mf.MultiChannel.MatchedFilter(dtype=dtype)
+    f.initialize(p, template_channels=assign, n_channels=2)
+    for c, s in enumerate(chans):
+        f.set_channel_signal(c, s.astype(dtype))
+    f.apply()
+    sig = [chans[c].astype(dtype) for c in assign]
+    ref = oracle.matched_filter(tps, sig, multi=True, fp64_from_f32=dtype == np.float32)
+    tol = FP32_TOL if dtype == np.float32 else 1e-11
+    for i in range(len(assign)):
+        a = f.get_valid_matched_filtered_signal(i)
+        assert np.max(np.abs(a - ref[i])) < tol, (i, np.max(np.abs(a - ref[i])))
