@@ -172,7 +172,7 @@ def measured_peak():
 
 def profile_traffic():
     """DRAM bytes per launch of the correlator from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "xcorr_fp32_config1_traffic.txt")
+    path = os.path.join(ROOT, "profiles", "xcorr_fp32_24ch_8.64M_traffic.txt")
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_full_launch"):
@@ -349,7 +349,8 @@ def main():
     peak, peak_kind = measured_peak()
     achieved = alg_bytes / (x_ms * 1e-3) / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": profile_traffic(), "kernel": "xcorr_kernel<float,%d,shared_den>" % (plan["fft_length"] // 2),
+            "traffic": profile_traffic() if n == N_SAMPLES else None,
+            "kernel": "xcorr_kernel<float,%d,shared_den>" % (plan["fft_length"] // 2),
             "kernel_ms": x_ms, "algorithmic_bytes": alg_bytes, "peak_source": peak_kind}
 
     value = world * lags_per_step / (el / args.steps)
@@ -360,8 +361,9 @@ def main():
             "config": {"workload": "24ch x 8.64M f32, 192 templates x 500, peaks 0.5/250, dbscan 50/3",
                        "channels": w["nch"], "samples_per_channel": n, "templates": nt,
                        "template_length": TEMPLATE_LEN, "fft_length": plan["fft_length"],
-                       "lags_per_block": plan["lags_per_block"], "l2": "inputs (830 MB) and outputs (6.6 GB) "
-                       "exceed L2; no flush needed"},
+                       "lags_per_block": plan["lags_per_block"],
+                       "l2": "inputs (%.0f MB) and outputs (%.2f GB) exceed the 129 MB L2; no flush needed"
+                             % (4e-6 * w["nch"] * n, 4e-9 * lags_per_step)},
             "e2e": {"value": world * lags_per_step / (e2e_el / args.steps), "unit": METRIC,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": roof, "gpu_launches": int(launches), "clocks": clk,
