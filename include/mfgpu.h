@@ -140,6 +140,15 @@ mfgpu_status mfgpu_mf_set_channel_signal(mfgpu_mf *mf, int channel, int n, const
  * one dead-trace pass for all rows; returns when the rows are copied. */
 mfgpu_status mfgpu_mf_set_channel_signals(mfgpu_mf *mf, int first_channel, int n_channels, int n, const void *x,
                                           long ld);
+/* Asynchronous upload of every channel's signal (row c of x, n samples,
+ * row stride ld samples) for the NEXT apply: the copy runs on a separate
+ * stream into a second device buffer, so it overlaps the work already
+ * enqueued (the current apply, peak finding), and the results of the
+ * previous apply stay readable.  The next apply -- or any call that reads
+ * or writes the signals -- makes the staged signals current.  Unlike the
+ * reference's copying setters, x must stay valid and unchanged until then
+ * (or until mfgpu_mf_synchronize); pinned host memory makes the copy DMA. */
+mfgpu_status mfgpu_mf_stage_channel_signals(mfgpu_mf *mf, int n, const void *x, long ld);
 /* Signal of channel c from device memory (same type, n samples). */
 mfgpu_status mfgpu_mf_set_channel_signal_device(mfgpu_mf *mf, int channel, int n, const void *dx);
 /* Full valid coefficient range of template it: lags 0..n-L_t (n - L_t + 1

@@ -69,6 +69,7 @@ _SIGS = {
     "mfgpu_mf_get_spectra_of_template": ([_vp, C.c_int, C.c_int, _vp, _ip], C.c_int),
     "mfgpu_mf_set_channel_signal": ([_vp, C.c_int, C.c_int, _vp], C.c_int),
     "mfgpu_mf_set_channel_signals": ([_vp, C.c_int, C.c_int, C.c_int, _vp, C.c_long], C.c_int),
+    "mfgpu_mf_stage_channel_signals": ([_vp, C.c_int, _vp, C.c_long], C.c_int),
     "mfgpu_mf_set_channel_signal_device": ([_vp, C.c_int, C.c_int, _vp], C.c_int),
     "mfgpu_mf_get_valid_signal": ([_vp, C.c_int, C.c_int, _vp, _ip], C.c_int),
     "mfgpu_mf_get_device_signal": ([_vp, C.c_int, C.POINTER(_vp), _ip], C.c_int),

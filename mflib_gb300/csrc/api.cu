@@ -120,11 +120,18 @@ struct mfgpu_mf
     int nfft = 0, log2p = 0, S = 0, nblocks = 0, ngroups = 0, maxvalid = 0;
     bool shared_den = false;
     int mode_x = 0;  // correlator organisation (launch_xcorr mode)
+    // staged upload (mfgpu_mf_stage_channel_signals): copies run on
+    // copy_stream into xstage; the next apply (or any other signal access)
+    // waits for copy_done and swaps xstage in for x.  x_ev / xstage_ev mark
+    // the end of the last apply that read each buffer.
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t copy_done = nullptr, x_ev = nullptr, xstage_ev = nullptr;
+    bool staged = false;
     long ldx = 0, ldr = 0;
     int dead_chunks = 1;
     // device buffers
     DevBuf x, rho, Bc, tw, grp_chan, grp_tb, grp_te, tids, tlen_d, nvalid_d, dead, err, tmpl_d, toff_d, pmin, pmax,
-        chan_list, stackbuf, shifts_d, weights_d, specbuf, den;
+        chan_list, stackbuf, shifts_d, weights_d, specbuf, den, xstage;
     long ldd = 0;
     int nden = 0;
     PeakWS pk;
@@ -144,13 +151,15 @@ struct mfgpu_mf
     {
         DevBuf *all[] = {&x,      &rho,      &Bc,   &tw,  &grp_chan, &grp_tb, &grp_te, &tids,      &tlen_d,
                          &nvalid_d, &dead,   &err,  &tmpl_d, &toff_d, &pmin, &pmax,  &chan_list, &stackbuf,
-                         &shifts_d, &weights_d, &specbuf, &den, &pk_cnt, &pk_idx, &pk_val};
+                         &shifts_d, &weights_d, &specbuf, &den, &pk_cnt, &pk_idx, &pk_val, &xstage};
         for (DevBuf *d : all) d->release();
         pk.release();
     }
     void reset()
     {
+        if (copy_stream) cudaStreamSynchronize(copy_stream);
         if (stream) cudaStreamSynchronize(stream);
+        staged = false;
         release_device();
         initialized = have = timed = have_peaks = pk_fused = false;
         pk_req = -1;
@@ -165,6 +174,7 @@ struct mfgpu_mf
 
 static mfgpu_status mf_sync(mfgpu_mf *mf)
 {
+    if (mf->copy_stream) CU(cudaStreamSynchronize(mf->copy_stream));
     CU(cudaStreamSynchronize(mf->stream));
     if (mf->initialized && mf->err.p)
     {
@@ -218,7 +228,11 @@ mfgpu_status mfgpu_mf_create(int precision, mfgpu_mf **out)
     mf->prec = precision;
     cudaError_t e = cudaGetDevice(&mf->dev);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&mf->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&mf->copy_stream, cudaStreamNonBlocking);
     for (int i = 0; i < 4 && e == cudaSuccess; ++i) e = cudaEventCreate(&mf->ev[i]);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&mf->copy_done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&mf->x_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&mf->xstage_ev, cudaEventDisableTiming);
     if (e != cudaSuccess)
     {
         delete mf;
@@ -236,6 +250,9 @@ mfgpu_status mfgpu_mf_destroy(mfgpu_mf *mf)
         mf->reset();
         for (auto &e : mf->ev)
             if (e) cudaEventDestroy(e);
+        for (cudaEvent_t e : {mf->copy_done, mf->x_ev, mf->xstage_ev})
+            if (e) cudaEventDestroy(e);
+        if (mf->copy_stream) cudaStreamDestroy(mf->copy_stream);
         if (mf->stream) cudaStreamDestroy(mf->stream);
     }
     delete mf;
@@ -561,6 +578,57 @@ static mfgpu_status mf_channel_of(mfgpu_mf *mf, int it, int *c)
     return MFGPU_OK;
 }
 
+// Makes staged signals current: the compute stream waits for the staged
+// copy, the buffers swap and the dead-trace flags of every channel are
+// recomputed.
+static mfgpu_status mf_resolve_stage(mfgpu_mf *mf)
+{
+    if (!mf->staged) return MFGPU_OK;
+    mf->staged = false;
+    mf->have = false;
+    mf->have_peaks = false;
+    mf->pk_fused = false;
+    CU(cudaStreamWaitEvent(mf->stream, mf->copy_done, 0));
+    std::swap(mf->x, mf->xstage);
+    std::swap(mf->x_ev, mf->xstage_ev);
+    if (mf->prec == 4)
+        CU(launch_dead<float>(mf->x.as<float>(), mf->ldx, mf->nch, mf->n, mf->dead.as<unsigned char>(),
+                              mf->pmin.as<float>(), mf->pmax.as<float>(), mf->dead_chunks, mf->stream));
+    else
+        CU(launch_dead<double>(mf->x.as<double>(), mf->ldx, mf->nch, mf->n, mf->dead.as<unsigned char>(),
+                               mf->pmin.as<double>(), mf->pmax.as<double>(), mf->dead_chunks, mf->stream));
+    mf->launches += 2;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_stage_channel_signals(mfgpu_mf *mf, int n, const void *x, long ld)
+{
+    MF_CHECK_INIT(mf);
+    DeviceGuard g(mf->dev);
+    if (n != mf->n)
+        return fail(MFGPU_EINVAL, "Number of samples = " + std::to_string(n) + " must equal" + std::to_string(mf->n));
+    if (!x) return fail(MFGPU_EINVAL, "x is NULL");
+    if (mf->nch > 1 && ld < n) return fail(MFGPU_EINVAL, "row stride is smaller than the number of samples");
+    const size_t es = mf->esz();
+    const size_t need = es * (size_t) mf->nch * mf->ldx;  // both buffers hold at least this
+    if (!mf->xstage.p || mf->xstage.bytes < need)
+    {
+        // a fresh staging buffer: no apply has read it; zero row tails like x
+        CU(cudaStreamSynchronize(mf->copy_stream));
+        CU(mf->xstage.ensure(need));
+        CU(cudaMemsetAsync(mf->xstage.p, 0, mf->xstage.bytes, mf->copy_stream));
+    }
+    // the buffer is free once the last apply that read it has finished
+    CU(cudaStreamWaitEvent(mf->copy_stream, mf->xstage_ev, 0));
+    if (mf->nch == 1) CU(cudaMemcpyAsync(mf->xstage.p, x, es * (size_t) n, cudaMemcpyHostToDevice, mf->copy_stream));
+    else
+        CU(cudaMemcpy2DAsync(mf->xstage.p, es * (size_t) mf->ldx, x, es * (size_t) ld, es * (size_t) n,
+                             (size_t) mf->nch, cudaMemcpyHostToDevice, mf->copy_stream));
+    CU(cudaEventRecord(mf->copy_done, mf->copy_stream));
+    mf->staged = true;
+    return MFGPU_OK;
+}
+
 // Copies nch channel rows (n samples each, source row stride ld samples)
 // into channels [c0, c0 + nch) and recomputes their dead-trace flags.
 static mfgpu_status mf_store_signals(mfgpu_mf *mf, int c0, int nch, int n, const void *x, long ld,
@@ -570,6 +638,8 @@ static mfgpu_status mf_store_signals(mfgpu_mf *mf, int c0, int nch, int n, const
         return fail(MFGPU_EINVAL, "Number of samples = " + std::to_string(n) + " must equal" + std::to_string(mf->n));
     if (!x) return fail(MFGPU_EINVAL, "x is NULL");
     if (nch > 1 && ld < n) return fail(MFGPU_EINVAL, "row stride is smaller than the number of samples");
+    mfgpu_status rs = mf_resolve_stage(mf);
+    if (rs != MFGPU_OK) return rs;
     mf->have = false;
     mf->have_peaks = false;
     const size_t es = mf->esz();
@@ -641,6 +711,8 @@ mfgpu_status mfgpu_mf_zero_signal(mfgpu_mf *mf, int it)
     int c;
     mfgpu_status st = mf_channel_of(mf, it, &c);
     if (st != MFGPU_OK) return st;
+    st = mf_resolve_stage(mf);
+    if (st != MFGPU_OK) return st;
     mf->have = false;
     mf->have_peaks = false;
     const size_t es = mf->esz();
@@ -659,6 +731,8 @@ mfgpu_status mfgpu_mf_get_signal(const mfgpu_mf *cmf, int it, int maxn, void *ds
     mfgpu_status st = mf_channel_of(mf, it, &c);
     if (st != MFGPU_OK) return st;
     if (!dst || maxn < mf->n) return fail(MFGPU_EINVAL, "destination too small");
+    st = mf_resolve_stage(mf);
+    if (st != MFGPU_OK) return st;
     const size_t es = mf->esz();
     CU(cudaMemcpyAsync(dst, mf->x.as<char>() + es * (size_t) c * mf->ldx, es * (size_t) mf->n,
                        cudaMemcpyDeviceToHost, mf->stream));
@@ -722,6 +796,8 @@ mfgpu_status mfgpu_mf_apply(mfgpu_mf *mf)
     if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");
     if (!mf->initialized) return fail(MFGPU_ESTATE, "Class is not initialized");
     DeviceGuard g(mf->dev);
+    mfgpu_status rs = mf_resolve_stage(mf);
+    if (rs != MFGPU_OK) return rs;
     mf->have = false;
     mf->have_peaks = false;
     CU(cudaEventRecord(mf->ev[0], mf->stream));
@@ -737,6 +813,7 @@ mfgpu_status mfgpu_mf_apply(mfgpu_mf *mf)
     }
     CU(cudaEventRecord(mf->ev[2], mf->stream));
     CU(cudaEventRecord(mf->ev[3], mf->stream));
+    CU(cudaEventRecord(mf->x_ev, mf->stream));  // the last read of x by this apply
     mf->timed = true;
     mf->have = true;
     return MFGPU_OK;

@@ -263,6 +263,21 @@ class MatchedFilter:
         _lib.call("mfgpu_mf_set_channel_signals", self._h, int(first_channel), int(x.shape[0]), int(x.shape[1]),
                   x.ctypes.data_as(C.c_void_p), int(x.strides[0] // x.itemsize))
 
+    def stage_channel_signals(self, x):
+        """Extension: asynchronous upload of every channel (rows of the 2-D
+        array x) for the next apply, overlapping the work already enqueued.
+        x must stay unchanged until the next apply's results are read (or
+        synchronize()); this object keeps references to the last two staged
+        arrays so they stay alive."""
+        x = np.asarray(x)
+        if x.ndim != 2:
+            raise ValueError("x must be 2-D (channels x samples)")
+        if x.dtype != self._dtype or x.strides[1] != x.itemsize or x.strides[0] % x.itemsize:
+            x = np.ascontiguousarray(x, dtype=self._dtype)
+        _lib.call("mfgpu_mf_stage_channel_signals", self._h, int(x.shape[1]), x.ctypes.data_as(C.c_void_p),
+                  int(x.strides[0] // x.itemsize))
+        self._staged = (x, getattr(self, "_staged", (None, None))[0])
+
     def zero_signal(self, it):
         _lib.call("mfgpu_mf_zero_signal", self._h, int(it))
 

@@ -459,3 +459,55 @@ def test_shared_length_normalisation(gpu, oracle, rng, dtype, L):
     for i in range(len(assign)):
         a = f.get_valid_matched_filtered_signal(i)
         assert np.max(np.abs(a - ref[i])) < tol, (i, np.max(np.abs(a - ref[i])))
+
+
+def test_staged_upload_pipeline(gpu, rng):
+    """stage_channel_signals: results of a pipelined loop (stage step i+1,
+    then read step i's results) equal those of synchronous uploads; staged
+    signals become current on apply, get_signal or a synchronous setter,
+    and a second stage before apply replaces the first."""
+    mf = gpu
+    n, nch = 20_000, 3
+    steps = [rng.standard_normal((nch, n)).astype(np.float32) for _ in range(4)]
+    assign = [0, 1, 2, 2]
+    tps = [rng.standard_normal(120) for _ in assign]
+    p = _params(mf, tps, n)
+    ref = mf.MultiChannel.MatchedFilter(dtype=np.float32)
+    ref.initialize(p, template_channels=assign, n_channels=nch)
+    want = []
+    for x in steps:
+        ref.set_channel_signals(x)
+        ref.apply()
+        want.append([ref.get_matched_filtered_signal(i) for i in range(len(assign))])
+    f = mf.MultiChannel.MatchedFilter(dtype=np.float32)
+    f.initialize(p, template_channels=assign, n_channels=nch)
+    f.stage_channel_signals(steps[0])
+    for k in range(len(steps)):
+        f.apply()
+        if k + 1 < len(steps):
+            f.stage_channel_signals(steps[k + 1])
+        for i in range(len(assign)):
+            np.testing.assert_array_equal(f.get_matched_filtered_signal(i), want[k][i])
+    # get_signal makes staged signals current
+    f.stage_channel_signals(steps[1])
+    np.testing.assert_array_equal(f.get_signal(0), steps[1][0])
+    # a synchronous setter after a stage: the stage lands first, then the setter
+    f.stage_channel_signals(steps[2])
+    f.set_channel_signal(1, steps[3][1])
+    mixed = steps[2].copy()
+    mixed[1] = steps[3][1]
+    for c in range(nch):
+        np.testing.assert_array_equal(f.get_signal(assign.index(c)), mixed[c])
+    # two stages before apply: the second wins
+    f.stage_channel_signals(steps[0])
+    f.stage_channel_signals(steps[3])
+    f.apply()
+    for i in range(len(assign)):
+        np.testing.assert_array_equal(f.get_matched_filtered_signal(i), want[3][i])
+    # a dead channel staged is flagged like a synchronous one
+    z = steps[0].copy()
+    z[2] = 0.0
+    f.stage_channel_signals(z)
+    f.apply()
+    assert not np.any(f.get_matched_filtered_signal(3))
+    f.synchronize()
