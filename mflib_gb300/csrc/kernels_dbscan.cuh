@@ -97,14 +97,50 @@ __device__ __forceinline__ void db_unite(int *parent, int a, int b)
     }
 }
 
+// Components of the core points.  Several features: every core pair within
+// eps is united.  One feature: ordered by (x, index), the components are the
+// runs of consecutive core points whose gaps are at most eps (any core pair
+// within eps spans only such gaps), so each core point is united with its
+// predecessor in that order alone -- O(n) unions instead of O(n k) on the
+// same few roots.
 static __global__ void __launch_bounds__(kDbThreads) db_union_kernel(DbParams p, const unsigned char *core, int *parent)
 {
     const int i = blockIdx.x * kDbWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (i >= p.n || !core[i]) return;
     const int s = p.seg_of[i];
-    const int je = p.seg_off[s + 1];
-    for (int j = i + 1 + lane; j < je; j += 32)
-        if (core[j] && db_near(p, i, j)) db_unite(parent, i, j);
+    const int jb = p.seg_off[s], je = p.seg_off[s + 1];
+    if (p.nf != 1)
+    {
+        for (int j = i + 1 + lane; j < je; j += 32)
+            if (core[j] && db_near(p, i, j)) db_unite(parent, i, j);
+        return;
+    }
+    const double xi = p.X[i];
+    double bx = 0.0;
+    int bj = -1;  // predecessor: the largest (x_j, j) below (x_i, i)
+    for (int j = jb + lane; j < je; j += 32)
+    {
+        if (j == i || !core[j]) continue;
+        const double xj = p.X[j];
+        const bool below = xj < xi || (xj == xi && j < i);
+        if (below && (bj < 0 || xj > bx || (xj == bx && j > bj)))
+        {
+            bx = xj;
+            bj = j;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        const double ox = __shfl_xor_sync(0xffffffffu, bx, o);
+        const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+        if (oj >= 0 && (bj < 0 || ox > bx || (ox == bx && oj > bj)))
+        {
+            bx = ox;
+            bj = oj;
+        }
+    }
+    if (lane == 0 && bj >= 0 && fabs(xi - bx) <= p.eps) db_unite(parent, i, bj);
 }
 
 static __global__ void db_roots_kernel(int n, const unsigned char *core, int *parent, int *is_root)

@@ -324,19 +324,22 @@ static __global__ void peak_seam_kernel(PeakTraces<T> tr, int ntr, FusedSlots<T>
 
 // Packs chunk b of a trace in index order: first lag, body (slot entries
 // ranked by index, or a re-scan of the stored trace when more than kPkCap
-// body lags passed), last lag.
+// body lags passed), last lag.  One warp per chunk (most chunks are empty).
+static_assert(kPkCap == 32, "peak_gather_fused_kernel ranks one slot entry per lane");
+
 template <class T>
 static __global__ void __launch_bounds__(kPkThreads)
     peak_gather_fused_kernel(PeakTraces<T> tr, FusedSlots<T> fs, const int *counts, const unsigned char *ht,
                              const long long *offs, int *cidx, T *cval, int *ctr, long long cap, int *overflow)
 {
-    __shared__ long long sh[32];
-    const int trace = blockIdx.y, b = blockIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int trace = blockIdx.y, b = blockIdx.x * (kPkThreads / 32) + (threadIdx.x >> 5);
+    if (b >= fs.nblk) return;
     const long slot = (long) trace * fs.nblk + b;
     const int cnt = counts[slot];
     if (cnt == 0) return;
     const long long off = offs[slot];
-    if (threadIdx.x == 0 && off + cnt > cap) *overflow = 1;
+    if (lane == 0 && off + cnt > cap) *overflow = 1;
     const int row = tr.row[trace];
     const T *x = tr.x + (long) row * tr.ldx;
     const long n = tr.len;
@@ -350,7 +353,7 @@ static __global__ void __launch_bounds__(kPkThreads)
             ctr[o] = trace;
         }
     };
-    if (threadIdx.x == 0)
+    if (lane == 0)
     {
         if (hv & 1) put(off, i0, x[i0]);
         if (hv & 2) put(off + cnt - 1, i0 + fs.S - 1, x[i0 + fs.S - 1]);
@@ -360,37 +363,45 @@ static __global__ void __launch_bounds__(kPkThreads)
     const int bc = fs.cnt[bs];
     if (bc <= kPkCap)
     {
+        // kPkCap == 32: one entry per lane, ranked by index
         const int *si = fs.idx + bs * kPkCap;
-        for (int r = threadIdx.x; r < bc; r += kPkThreads)
+        if (lane < bc)
         {
-            const int ir = si[r];
+            const int ir = si[lane];
             int rank = 0;
             for (int q = 0; q < bc; ++q) rank += si[q] < ir ? 1 : 0;
-            put(boff + rank, ir, fs.val[bs * kPkCap + r]);
+            put(boff + rank, ir, fs.val[bs * kPkCap + lane]);
         }
         return;
     }
     const long lo = i0 + 1, hi = (i0 + fs.S - 1 < n) ? i0 + fs.S - 1 : n;
     long long base = boff;
-    for (long c0 = lo; c0 < hi; c0 += kPkChunk)
+    for (long c0 = lo; c0 < hi; c0 += 32 * kPkPer)
     {
-        const long a = c0 + (long) threadIdx.x * kPkPer;
+        const long a = c0 + (long) lane * kPkPer;
         unsigned mask = 0;
 #pragma unroll 4
         for (int q = 0; q < kPkPer; ++q)
             if (a + q < hi && cand_rule<T>(x[a + q - 1], x[a + q], a + q + 1 < n ? x[a + q + 1] : (T) 0, a + q, n,
                                            tr.thr))
                 mask |= 1u << q;
-        long long tot;
-        long long r = block_excl_scan((long long) __popc(mask), sh, &tot);
+        const int c = __popc(mask);
+        int incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const int y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        long long r = base + incl - c;
         while (mask)
         {
             const int q = __ffs(mask) - 1;
             mask &= mask - 1;
-            put(base + r, a + q, x[a + q]);
+            put(r, a + q, x[a + q]);
             ++r;
         }
-        base += tot;
+        base += __shfl_sync(0xffffffffu, incl, 31);
     }
 }
 
