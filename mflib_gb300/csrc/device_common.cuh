@@ -209,13 +209,14 @@ template <> struct acc_t<float>
     {
         df r; r.hi = __shfl_up_sync(0xffffffffu, a.hi, d); r.lo = __shfl_up_sync(0xffffffffu, a.lo, d); return r;
     }
-    // sqrt(L) / max(tol, sqrt(max(0, L*s2 - s1^2)))
+    // sqrt(L) / max(tol, sqrt(L*s2 - s1^2)); 0 for a constant window
+    // (L*s2 - s1^2 <= 0), whose exact numerator is 0
     static __device__ __forceinline__ float inv_den(df s1, df s2, int L, float tol)
     {
         df v = df_sub(df_mul_f(s2, (float) L), df_sqr(s1));
         float var = df_to_f(v);
-        float den = sqrtf(fmaxf(var, 0.f));
-        return sqrtf((float) L) / fmaxf(den, tol);
+        if (!(var > 0.f)) return 0.f;
+        return sqrtf((float) L) / fmaxf(sqrtf(var), tol);
     }
 };
 template <> struct acc_t<double>
@@ -231,8 +232,8 @@ template <> struct acc_t<double>
     static __device__ __forceinline__ double inv_den(double s1, double s2, int L, double tol)
     {
         double var = (double) L * s2 - s1 * s1;
-        double den = sqrt(fmax(var, 0.0));
-        return sqrt((double) L) / fmax(den, tol);
+        if (!(var > 0.0)) return 0.0;
+        return sqrt((double) L) / fmax(sqrt(var), tol);
     }
 };
 

@@ -115,6 +115,71 @@ template <class T, int LOG2P> struct XcorrLayout
     }
 };
 
+// Compensated sum for block means: FP32 values accumulate in double-float
+// (one TwoSum per value, low words summed), FP64 in double.  A block of
+// identical samples gets exactly that sample as its mean, so the mean
+// subtraction leaves exact zeros (and, for nearly constant blocks, no
+// residual offset that would dominate the block's energy).
+template <class T> struct MeanAcc;
+template <> struct MeanAcc<float>
+{
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add(float v)
+    {
+        const df s = two_sum(hi, v);
+        hi = s.hi;
+        lo += s.lo;
+    }
+    __device__ __forceinline__ void add(const MeanAcc &o)
+    {
+        const df s = two_sum(hi, o.hi);
+        hi = s.hi;
+        lo += s.lo + o.lo;
+    }
+    __device__ __forceinline__ MeanAcc shfl_xor(int o) const
+    {
+        MeanAcc r;
+        r.hi = __shfl_xor_sync(0xffffffffu, hi, o);
+        r.lo = __shfl_xor_sync(0xffffffffu, lo, o);
+        return r;
+    }
+    __device__ __forceinline__ float mean(int n) const
+    {
+        const df q = quick_two_sum(hi, lo);
+        return q.hi / (float) n + q.lo / (float) n;
+    }
+};
+template <> struct MeanAcc<double>
+{
+    double s = 0.0;
+    __device__ __forceinline__ void add(double v) { s += v; }
+    __device__ __forceinline__ void add(const MeanAcc &o) { s += o.s; }
+    __device__ __forceinline__ MeanAcc shfl_xor(int o) const
+    {
+        MeanAcc r;
+        r.s = __shfl_xor_sync(0xffffffffu, s, o);
+        return r;
+    }
+    __device__ __forceinline__ double mean(int n) const { return s / (double) n; }
+};
+
+// block-wide mean of n values from the per-thread accumulators; red holds
+// at least 2 * kThreads / 32 values of T
+template <class T> __device__ __forceinline__ T block_mean(MeanAcc<T> a, T *red, int n)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a.add(a.shfl_xor(o));
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    MeanAcc<T> *r = reinterpret_cast<MeanAcc<T> *>(red);
+    __syncthreads();
+    if (l == 0) r[w] = a;
+    __syncthreads();
+    MeanAcc<T> t = r[0];
+#pragma unroll
+    for (int i = 1; i < kThreads / 32; ++i) t.add(r[i]);
+    return t.mean(n);
+}
+
 template <class T> __device__ __forceinline__ T block_sum(T v, T *red)
 {
 #pragma unroll
@@ -271,7 +336,8 @@ __device__ __forceinline__ void seg_chunk_prefix(SegStats<T> st, int tid)
     __syncthreads();
 }
 
-// inv_den[k] = sqrt(L)/max(tol, sqrt(max(0, L*s2 - s1^2))) for k in [0, S).
+// inv_den[k] = sqrt(L)/max(tol, sqrt(L*s2 - s1^2)) for k in [0, S), 0 where
+// L*s2 - s1^2 <= 0 (a constant window).
 // Thread u slides over an odd-length run of lags (odd stride = no bank
 // conflicts); the run's first window comes from the chunk prefixes plus a
 // skewed partial sum.
@@ -461,9 +527,9 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
 
     // ---- segment mean; sliding-window normalisation (precomputed per
     //      channel by den_kernel when every template shares one length)
-    T s = 0;
-    for (int i = tid; i < N; i += kThreads) s += xs[i];
-    const T m = block_sum<T>(s, red) / (T) N;
+    MeanAcc<T> macc;
+    for (int i = tid; i < N; i += kThreads) macc.add(xs[i]);
+    const T m = block_mean<T>(macc, red, N);
     SegStats<T> st;
     st.xs = xs; st.m = m; st.c1 = c1; st.c2 = c2;
     int Lcur = p.tlen[p.tids[t_begin]];
@@ -796,9 +862,12 @@ template <> struct DenOps<float>
         vl = v.lo + (a.lo - b.lo);
     }
     static __device__ __forceinline__ float hi(df a) { return a.hi; }
+    // a window with V <= 0 is constant (the sums are exact there) and its
+    // exact numerator against a zero-mean template is 0: rho = 0 instead of
+    // the numerator's rounding error times sqrt(L)/tol
     static __device__ __forceinline__ float out(float var, float sqrtL, float tol)
     {
-        return var > tol * tol ? sqrtL * rsqrtf(var) : sqrtL / tol;
+        return var > tol * tol ? sqrtL * rsqrtf(var) : (var > 0.f ? sqrtL / tol : 0.f);
     }
 };
 template <> struct DenOps<double>
@@ -825,7 +894,7 @@ template <> struct DenOps<double>
     static __device__ __forceinline__ double hi(double a) { return a; }
     static __device__ __forceinline__ double out(double var, double sqrtL, double tol)
     {
-        return sqrtL / fmax(sqrt(fmax(var, 0.0)), tol);
+        return var > 0.0 ? sqrtL / fmax(sqrt(var), tol) : 0.0;
     }
 };
 
@@ -891,7 +960,7 @@ __global__ void __launch_bounds__(kThreads) den_kernel(const T *x, long ldx, int
     // ---- stage 32 * nruns samples (16-byte loads; k0 and ldx are multiples of 32)
     const T *xr = x + (long) c * ldx + k0;
     constexpr int VW = 16 / sizeof(T);
-    T s = 0;
+    MeanAcc<T> macc;
     for (int i = tid; i < nruns * kDenRun / VW; i += kThreads)
     {
         T v[VW];
@@ -909,10 +978,10 @@ __global__ void __launch_bounds__(kThreads) den_kernel(const T *x, long ldx, int
         for (int q = 0; q < VW; ++q)
         {
             y[den_pad(VW * i + q)] = v[q];
-            s += v[q];
+            macc.add(v[q]);
         }
     }
-    const T m = block_sum<T>(s, red) / (T) (nruns * kDenRun);
+    const T m = block_mean<T>(macc, red, nruns * kDenRun);
 
     // ---- run sums (run j = tid + kThreads r) and partial sums of the first re samples
     const int re = L & (kDenRun - 1), Lq = L >> 5;
@@ -963,9 +1032,11 @@ __global__ void __launch_bounds__(kThreads) den_kernel(const T *x, long ldx, int
         {
             const T var = vh + (vl + fma(Lt, d2, -d1 * (d1 + c2s)));
             o[q] = O::out(var, sqrtL, tol);
-            const T yin = y[den_pad(base + q + L)], yout = y[den_pad(base + q)];
+            // the CTA mean comes off each sample first: both differences are
+            // exact for samples near a large common offset
+            const T yin = y[den_pad(base + q + L)] - m, yout = y[den_pad(base + q)] - m;
             const T dd = yin - yout;
-            d2 = fma(yin + yout - (T) 2 * m, dd, d2);
+            d2 = fma(yin + yout, dd, d2);
             d1 += dd;
         }
         T *dr = drow + base;

@@ -1,0 +1,383 @@
+// C++ API mirror (include/mfgpu.hpp) on the device, checked the way the
+// reference's own C++ tests check mflib: known-answer matched filters against
+// a two-pass Pearson correlation (testing/matchedFilter.cpp,
+// testing/singleChannel.cpp, testing/utilities.hpp), the peak finder's exact
+// index lists (testing/peakFinder.cpp), the DBSCAN golden labels
+// (testing/dbscan.cpp) and the FFT-sizing values
+// (testing/matchedFilterParameters.cpp).  Prints one line per check and
+// "ALL PASSED"; exits non-zero on the first failure.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <random>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "mfgpu.hpp"
+
+namespace {
+
+int g_checks = 0;
+
+void require(bool ok, const std::string &what)
+{
+    ++g_checks;
+    if (!ok)
+    {
+        std::printf("FAIL: %s\n", what.c_str());
+        std::exit(1);
+    }
+    std::printf("ok   %s\n", what.c_str());
+}
+
+template <class F> bool throws_invalid(F f)
+{
+    try { f(); } catch (const std::invalid_argument &) { return true; } catch (...) { return false; }
+    return false;
+}
+template <class F> bool throws_runtime(F f)
+{
+    try { f(); } catch (const std::invalid_argument &) { return false; } catch (const std::runtime_error &) { return true; }
+    catch (...) { return false; }
+    return false;
+}
+
+// two-pass Pearson correlation of template b against every window of x, in
+// long double (the reference tests' naive check)
+std::vector<double> pearson(const std::vector<double> &b, const std::vector<double> &x)
+{
+    const size_t L = b.size(), n = x.size() - L + 1;
+    long double mb = 0;
+    for (double v : b) mb += v;
+    mb /= L;
+    long double sb = 0;
+    for (double v : b) sb += (v - mb) * (v - mb);
+    std::vector<double> out(n);
+    for (size_t k = 0; k < n; ++k)
+    {
+        long double mx = 0;
+        for (size_t j = 0; j < L; ++j) mx += x[k + j];
+        mx /= L;
+        long double sxy = 0, sx = 0;
+        for (size_t j = 0; j < L; ++j)
+        {
+            const long double d = x[k + j] - mx;
+            sxy += d * (b[j] - mb);
+            sx += d * d;
+        }
+        out[k] = (sx > 0 && sb > 0) ? (double) (sxy / std::sqrt(sx * sb)) : 0.0;
+    }
+    return out;
+}
+
+template <class T> double max_err(const std::vector<T> &a, const std::vector<double> &b)
+{
+    double m = 0;
+    for (size_t i = 0; i < a.size() && i < b.size(); ++i) m = std::max(m, std::abs((double) a[i] - b[i]));
+    return a.size() == b.size() ? m : 1e30;
+}
+
+MFLib::WaveformTemplate make_template(const std::vector<double> &s, double fs)
+{
+    MFLib::WaveformTemplate wt;
+    wt.setSignal((int) s.size(), s.data());
+    wt.setSamplingRate(fs);
+    return wt;
+}
+
+// damped sine/cosine signals and 2 s templates (testing/matchedFilter.cpp:63-90)
+void damped(std::vector<double> &x, std::vector<double> &x2, std::vector<double> &b, std::vector<double> &b2)
+{
+    const int n = 1000;
+    const double tmax = 8, dt = tmax / (n - 1), f0 = 4 / tmax, pi = 3.14159265358979323846;
+    x.resize(n);
+    x2.resize(n);
+    for (int i = 0; i < n; ++i)
+    {
+        const double t = i * dt;
+        x[i] = 2 * std::exp(-0.1 * t) * std::sin(2 * pi * f0 * t);
+        x2[i] = 2 * std::exp(-0.15 * t) * std::cos(2 * pi * f0 * t);
+    }
+    const int nb = (int) (2.0 / dt + 0.5) + 1;
+    b.resize(nb);
+    b2.resize(nb);
+    for (int i = 0; i < nb; ++i)
+    {
+        b[i] = std::sin(2 * pi * f0 * i * dt);
+        b2[i] = std::cos(2 * pi * f0 * i * dt);
+    }
+}
+
+void test_fft_sizes()
+{
+    const int cases[4][4] = {{4500, 75000, 32768, 28269}, {4500, 8640000, 65536, 61037}, {101, 1024, 512, 412},
+                             {99, 1024, 512, 414}};
+    for (const auto &c : cases)
+    {
+        auto r = MFLib::computeOptimalFFTAndBlockLength(c[0], c[1]);
+        require(r.first == c[2] && r.second == c[3], "computeOptimalFFTAndBlockLength(" + std::to_string(c[0]) + ", " +
+                                                         std::to_string(c[1]) + ")");
+    }
+    require(throws_invalid([] { MFLib::computeOptimalFFTAndBlockLength(0, 10); }), "fft sizes reject nb < 1");
+}
+
+void test_multichannel_double()
+{
+    std::vector<double> x, x2, b, b2;
+    damped(x, x2, b, b2);
+    MFLib::MatchedFilterParameters p;
+    for (auto *t : {&b, &b2, &b, &b2}) p.addTemplate(make_template(*t, 1.0));
+    p.setSignalSize((int) x.size());
+    MFLib::MatchedFilter<double> mf;
+    require(throws_runtime([&] { mf.apply(); }), "apply before initialize throws runtime_error");
+    mf.initialize(p);
+    require(mf.isInitialized() && mf.getNumberOfTemplates() == 4, "initialize");
+    require(mf.getFilteredSignalLength() == (int) (x.size() - b.size() + 1), "getFilteredSignalLength");
+    const std::vector<double> *sig[4] = {&x, &x2, &x, &x2};
+    for (int i = 0; i < 4; ++i) mf.setSignal(i, (int) sig[i]->size(), sig[i]->data());
+    require(throws_invalid([&] { mf.setSignal(0, 10, x.data()); }), "setSignal with a wrong length throws");
+    require(!mf.haveMatchedFilteredSignals(), "no results before apply");
+    require(throws_runtime([&] { mf.getMatchedFilteredSignal(0); }), "results before apply throw runtime_error");
+    mf.apply();
+    require(mf.haveMatchedFilteredSignals(), "results after apply");
+    const std::vector<double> *tp[4] = {&b, &b2, &b, &b2};
+    for (int i = 0; i < 4; ++i)
+    {
+        const double e = max_err(mf.getMatchedFilteredSignal(i), pearson(*tp[i], *sig[i]));
+        require(e < 1e-13, "FP64 template " + std::to_string(i) + " vs two-pass Pearson (" + std::to_string(e) + ")");
+    }
+    const double *ptr = mf.getMatchedFilterSignalPointer(1);
+    require(ptr && std::abs(ptr[5] - mf.getMatchedFilteredSignal(1)[5]) == 0, "getMatchedFilterSignalPointer");
+    const double *sp = mf.getSignalPointer(2);
+    require(sp && sp[17] == x[17], "getSignalPointer");
+    require(throws_invalid([&] { mf.getMatchedFilteredSignal(7); }), "template index out of range throws");
+    auto spec = mf.getSpectraOfTemplate(0);
+    const int nfft = MFLib::computeOptimalFFTAndBlockLength((int) b.size(), (int) (x.size() + b.size() - 1)).first;
+    require((int) spec.size() == nfft / 2 + 1, "getSpectraOfTemplate length");
+}
+
+void test_multichannel_float()
+{
+    std::vector<double> x, x2, b, b2;
+    damped(x, x2, b, b2);
+    MFLib::MatchedFilterParameters p;
+    p.addTemplate(make_template(b, 1.0));
+    p.addTemplate(make_template(b2, 1.0));
+    p.setSignalSize((int) x.size());
+    MFLib::MatchedFilter<float> mf;
+    mf.initialize(p);
+    std::vector<float> xf(x.begin(), x.end()), x2f(x2.begin(), x2.end());
+    mf.setSignal(0, (int) xf.size(), xf.data());
+    mf.setSignal(1, (int) x2f.size(), x2f.data());
+    mf.apply();
+    std::vector<double> bd(b.size()), b2d(b2.size()), xd(xf.begin(), xf.end()), x2d(x2f.begin(), x2f.end());
+    for (size_t i = 0; i < b.size(); ++i) { bd[i] = (float) b[i]; b2d[i] = (float) b2[i]; }
+    const double e0 = max_err(mf.getMatchedFilteredSignal(0), pearson(bd, xd));
+    const double e1 = max_err(mf.getMatchedFilteredSignal(1), pearson(b2d, x2d));
+    require(e0 < 2e-6 && e1 < 2e-6, "FP32 vs two-pass Pearson (" + std::to_string(std::max(e0, e1)) + ")");
+}
+
+void test_single_channel()
+{
+    // testing/singleChannel.cpp:104-160: one signal, three templates cut from it
+    std::mt19937_64 g(7);
+    std::uniform_real_distribution<double> u(2, 3);
+    std::vector<double> wave(4000);
+    for (double &v : wave) v = u(g);
+    const int cuts[3][2] = {{25, 155}, {1124, 1264}, {3601, 3726}};
+    MFLib::SingleChannel::MatchedFilterParameters p;
+    std::vector<std::vector<double>> tps;
+    for (const auto &c : cuts)
+    {
+        tps.emplace_back(wave.begin() + c[0], wave.begin() + c[1]);
+        p.addTemplate(make_template(tps.back(), 100.0));
+    }
+    p.setSignalSize((int) wave.size());
+    require(p.getDetectionMode() == MFLib::MatchedFilterDetectionMode::SINGLE_CHANNEL, "single-channel mode");
+    MFLib::SingleChannel::MatchedFilter<double> mf;
+    mf.initialize(p);
+    mf.setSignal((int) wave.size(), wave.data());
+    mf.apply();
+    for (int i = 0; i < 3; ++i)
+    {
+        std::vector<double> r = mf.getMatchedFilteredSignal(i);
+        std::vector<double> ref = pearson(tps[i], wave);
+        ref.resize(r.size());
+        const double e = max_err(r, ref);
+        require(e < 1e-12, "single-channel template " + std::to_string(i) + " (" + std::to_string(e) + ")");
+        // the template's own position correlates perfectly
+        require(std::abs(r[cuts[i][0]] - 1.0) < 1e-12, "single-channel self match " + std::to_string(i));
+    }
+}
+
+void test_shift_and_stack()
+{
+    // three templates with onsets and travel times; the stack is the
+    // weighted sum of |rho_t| shifted by round((travel - onset) * fs)
+    std::mt19937_64 g(11);
+    std::normal_distribution<double> nd;
+    const double fs = 100;
+    const int n = 6000, L = 200;
+    std::vector<double> sig(n);
+    for (double &v : sig) v = nd(g);
+    MFLib::MatchedFilterParameters p;
+    const double travel[3] = {1.0, 2.5, 4.0}, onset[3] = {0.5, 0.25, 1.0}, w[3] = {0.5, 0.3, 0.2};
+    std::vector<std::vector<double>> tps;
+    for (int t = 0; t < 3; ++t)
+    {
+        tps.emplace_back(sig.begin() + 1000 * (t + 1), sig.begin() + 1000 * (t + 1) + L);
+        MFLib::WaveformTemplate wt = make_template(tps.back(), fs);
+        wt.setPhaseOnsetTime(onset[t]);
+        wt.setTravelTime(travel[t]);
+        wt.setShiftAndStackWeight(w[t]);
+        p.addTemplate(wt);
+    }
+    p.setSignalSize(n);
+    MFLib::MatchedFilter<double> mf;
+    mf.initialize(p);
+    for (int t = 0; t < 3; ++t) mf.setSignal(t, n, sig.data());
+    mf.apply();
+    std::vector<double> stack = mf.shiftAndStack();
+    std::vector<std::vector<double>> rho(3);
+    int smax = 0;
+    int sh[3];
+    for (int t = 0; t < 3; ++t)
+    {
+        rho[t] = mf.getMatchedFilteredSignal(t);
+        sh[t] = (int) ((travel[t] - onset[t]) * fs + 0.5);
+        smax = std::max(smax, sh[t]);
+    }
+    const int m = (int) rho[0].size() - smax;
+    double e = (int) stack.size() == m ? 0.0 : 1e30;
+    for (int k = 0; k < m && e < 1; ++k)
+    {
+        double s = 0;
+        for (int t = 0; t < 3; ++t) s += w[t] * std::abs(rho[t][k + sh[t]]);
+        e = std::max(e, std::abs(s - stack[k]));
+    }
+    require(e < 1e-12, "shiftAndStack (" + std::to_string(e) + ")");
+}
+
+// testing/peakFinder.cpp:145-170
+std::vector<double> gaussian_sine()
+{
+    const double tdur = 4, dt = 0.01, sigma = 1.2, freq = 12, pi = 3.14159265358979323846;
+    const double t0 = -tdur / 2, t1 = tdur / 2;
+    const int npts = (int) ((t1 - t0) / dt + 0.5) + 1;
+    std::vector<double> y(npts);
+    double mx = 0;
+    for (int i = 0; i < npts; ++i)
+    {
+        const double t = t0 + i * dt, a = (t / sigma) * (t / sigma);
+        y[i] = std::exp(-a * a) * std::cos(2 * pi * (t - t0) / tdur * freq);
+        mx = std::max(mx, std::abs(y[i]));
+    }
+    for (double &v : y) v /= mx;
+    y.front() = 0;
+    y.back() = 0;
+    return y;
+}
+
+void test_peak_finder()
+{
+    // testing/peakFinder.cpp:16-143
+    const int n = 4000;
+    std::vector<double> tp = gaussian_sine(), sig(n, 0.0);
+    const int ih = (int) tp.size() / 2;
+    for (int i = 0; i < (int) tp.size() - ih; ++i) sig[i] = tp[ih + i];
+    for (double frac : {0.25, 0.5, 0.75})
+    {
+        const int i1 = (int) (n * frac) - ih;
+        for (size_t i = 0; i < tp.size(); ++i) sig[i1 + i] = tp[i];
+    }
+    for (int i = 0; i < ih; ++i) sig[n - ih + i] = tp[1 + i];
+    MFLib::PeakFinder<double> pf;
+    require(throws_invalid([&] { pf.setThreshold(1.5); }), "PeakFinder threshold outside [0,1] throws");
+    std::vector<double> flat(n, 0.4);
+    pf.setThreshold(0.8);
+    pf.setMinimumPeakDistance(52);
+    pf.setSignal(n, flat.data());
+    pf.apply();
+    require(pf.getNumberOfPeaks() == 0 && pf.getPeakIndicesPointer() == nullptr, "no peaks below threshold");
+    const std::vector<int> p13 = {0, 67, 933, 1000, 1067, 1933, 2000, 2067, 2933, 3000, 3067, 3932, 3999};
+    const std::vector<int> p21 = {0,    33,   67,   933,  967,  1000, 1033, 1067, 1933, 1967, 2000,
+                                  2033, 2067, 2933, 2967, 3000, 3033, 3067, 3932, 3966, 3999};
+    pf.setMinimumPeakDistance((int) (0.5 / 0.01 + 1) + 1);
+    pf.setSignal(n, sig.data());
+    pf.apply();
+    std::vector<int> got(pf.getNumberOfPeaks());
+    int *gp = got.data();
+    if (!got.empty()) pf.getPeakIndices((int) got.size(), &gp);
+    require(got == p13, "PeakFinder 13 peaks with separation 52");
+    pf.setMinimumPeakDistance(0);
+    pf.apply();
+    got.assign(pf.getNumberOfPeaks(), 0);
+    gp = got.data();
+    if (!got.empty()) pf.getPeakIndices((int) got.size(), &gp);
+    require(got == p21, "PeakFinder 21 peaks without separation");
+}
+
+void test_dbscan()
+{
+    // testing/dbscan.cpp:8-60
+    const double X[12] = {1, 2, 2, 2, 2, 2, 8, 7, 8, 8, 25, 80};
+    MFLib::DBSCAN db;
+    require(!db.isInitialized(), "DBSCAN not initialised");
+    db.initialize(3, 2);
+    db.setData(6, 2, X);
+    db.cluster();
+    require(db.haveLabels() && db.getNumberOfClusters() == 2, "DBSCAN 2 clusters");
+    require(db.getLabels() == std::vector<int>({0, 0, 0, 1, 1, -1}), "DBSCAN labels with one noise point");
+    db.setData(5, 2, X);
+    db.cluster();
+    require(db.getLabels() == std::vector<int>({0, 0, 0, 1, 1}), "DBSCAN labels without noise");
+}
+
+void test_value_types()
+{
+    MFLib::NetworkStationPhase a, b;
+    a.setNetwork("uu ");
+    a.setStation("fo r");
+    b.setNetwork("UU");
+    b.setStation("FOR");
+    require(a == b && a.getHash() == b.getHash() && a.getStation() == "FOR", "NetworkStationPhase canonical form");
+    MFLib::WaveformTemplate wt;
+    require(throws_runtime([&] { wt.getSignalLength(); }), "WaveformTemplate without a signal throws");
+    require(throws_invalid([&] { wt.setSamplingRate(-1); }), "negative sampling rate throws");
+    require(throws_runtime([&] { wt.setTravelTime(-1); }), "negative travel time throws runtime_error");
+    MFLib::MatchedFilterParameters p;
+    require(!p.isValid(), "empty parameters invalid");
+    require(throws_invalid([&] { p.addTemplate(wt); }), "template without a signal rejected");
+}
+
+}  // namespace
+
+int main()
+{
+    std::setvbuf(stdout, nullptr, _IONBF, 0);
+    int ndev = 0;
+    if (mfgpu_device_count(&ndev) != MFGPU_OK || ndev < 1)
+    {
+        std::printf("no CUDA device\n");
+        return 2;
+    }
+    try
+    {
+        test_fft_sizes();
+        test_value_types();
+        test_multichannel_double();
+        test_multichannel_float();
+        test_single_channel();
+        test_shift_and_stack();
+        test_peak_finder();
+        test_dbscan();
+    }
+    catch (const std::exception &e)
+    {
+        std::printf("FAIL: unexpected exception after %d checks: %s\n", g_checks, e.what());
+        return 1;
+    }
+    std::printf("ALL PASSED (%d checks)\n", g_checks);
+    return 0;
+}

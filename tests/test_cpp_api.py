@@ -1,0 +1,47 @@
+"""The C++ mirror of mflib's classes (include/mfgpu.hpp) compiles against
+the C ABI, links against libmfgpu.so, and on a GPU passes the reference's
+known-answer checks (tests/cpp/test_mflib_api.cpp)."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+SRC = os.path.join(ROOT, "tests", "cpp", "test_mflib_api.cpp")
+LIBDIR = os.path.join(ROOT, "mflib_gb300")
+CXX = shutil.which("g++")
+
+
+def _compile(out, link=True):
+    cmd = [CXX, "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"), SRC]
+    if link:
+        cmd += ["-o", out, "-L", LIBDIR, "-lmfgpu", "-Wl,-rpath," + LIBDIR]
+    else:
+        cmd += ["-fsyntax-only"]
+    return subprocess.run(cmd, capture_output=True, text=True)
+
+
+@pytest.mark.skipif(CXX is None, reason="g++ not found")
+def test_header_compiles():
+    r = _compile(None, link=False)
+    assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.skipif(CXX is None, reason="g++ not found")
+def test_links_against_library(tmp_path):
+    if not os.path.exists(os.path.join(LIBDIR, "libmfgpu.so")):
+        pytest.skip("libmfgpu.so not built")
+    r = _compile(str(tmp_path / "t"))
+    assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.gpu
+def test_cpp_api_on_gpu(tmp_path):
+    assert CXX is not None
+    exe = str(tmp_path / "test_mflib_api")
+    r = _compile(exe)
+    assert r.returncode == 0, r.stderr
+    run = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert run.returncode == 0, run.stdout + run.stderr
+    assert "ALL PASSED" in run.stdout

@@ -1,0 +1,163 @@
+"""The workload recipes beyond the bench's multi-channel day, as parity cases
+on the GPU (seeded synthetic seismograms generated here, no data files):
+
+* the single-channel case (one 400-sample template against one hour at
+  100 Hz with 20 injected copies): full coefficient trace in FP64 and FP32
+  against the oracle, and the peaks (rho >= 0.6, separation 200);
+* an uneven bank (templates of 200..3,000 samples with random pass bands,
+  each on one of several channels), at reduced channel count and length;
+* the precision stress recipe (DC offsets of 1e3..1e5, a piecewise-constant
+  amplitude envelope over six decades), at reduced size: the FP64 engine
+  against the two-pass FP64 Pearson correlation, and the FP32 engine's
+  error reported and bounded where the envelope is locally constant.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+FS = 100.0
+
+
+def _bp(x, lo, hi, order=4):
+    from scipy.signal import butter, sosfilt
+    return sosfilt(butter(order, [lo, hi], btype="bandpass", fs=FS, output="sos"), x)
+
+
+def _template(seed, L, lo=2.0, hi=8.0):
+    from scipy.signal.windows import hann
+    return _bp(np.random.default_rng(seed).standard_normal(L), lo, hi) * hann(L)
+
+
+def _params(mf, tps, n, single=False):
+    p = mf.SingleChannel.MatchedFilterParameters() if single else mf.MultiChannel.MatchedFilterParameters()
+    for t in tps:
+        wt = mf.WaveformTemplate()
+        wt.set_signal(t)
+        wt.set_sampling_rate(FS)
+        p.add_template(wt)
+    p.set_signal_size(n)
+    return p
+
+
+def single_channel_case():
+    tp = _template(0, 400)
+    sig = _bp(np.random.default_rng(1).standard_normal(360_000), 1.0, 10.0)
+    rms = np.sqrt(np.mean(sig ** 2))
+    rng = np.random.default_rng(2)
+    slots = rng.choice(360_000 // 1000 - 1, 20, replace=False)
+    offs = np.sort(slots * 1000 + rng.integers(0, 500, 20))
+    amps = rng.uniform(0.3, 3.0, 20) * rms / np.sqrt(np.mean(tp ** 2))
+    for o, a in zip(offs, amps):
+        sig[o:o + tp.size] += a * tp
+    return tp, sig, offs
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_single_channel_hour(gpu, oracle, dtype):
+    mf = gpu
+    tp, sig, offs = single_channel_case()
+    f = mf.SingleChannel.MatchedFilter(dtype=dtype)
+    f.initialize(_params(mf, [tp], sig.size, single=True))
+    x = sig.astype(dtype)
+    f.set_signal(x)
+    f.apply()
+    rho = f.get_matched_filtered_signal(0).astype(np.float64)
+    ref = oracle.matched_filter([tp], [x], multi=False, fp64_from_f32=dtype == np.float32)[0]
+    tol = 1e-11 if dtype == np.float64 else 1e-5
+    assert np.max(np.abs(rho - ref)) < tol
+    # peaks: identical to the oracle's peak finder on the same trace, and
+    # every injected copy is found
+    f.find_peaks(0.6, 200)
+    pk = f.get_peaks(0)
+    np.testing.assert_array_equal(pk, oracle.peaks(rho, 0.6, 200))
+    # every copy whose correlation clears the threshold is a peak
+    for o in offs:
+        if ref[o] > 0.65:
+            assert np.min(np.abs(pk - o)) <= 1
+
+
+def test_uneven_bank(gpu, oracle):
+    """Templates of 200..3,000 samples with random 1..15 Hz pass bands, each
+    assigned to one of 6 channels (the 2,000-template bank's recipe at 60
+    templates and 120,000 samples per channel)."""
+    mf = gpu
+    rng = np.random.default_rng(200)
+    nt, nch, n = 60, 6, 120_000
+    lens = rng.integers(200, 3001, nt)
+    tps = []
+    for t, L in enumerate(lens):
+        lo = rng.uniform(1, 7)
+        hi = rng.uniform(lo + 2, 15)
+        tps.append(_template(1000 + t, int(L), lo, hi))
+    chan = rng.integers(0, nch, nt)
+    sigs = [_bp(np.random.default_rng(300 + c).standard_normal(n), 1.0, 15.0).astype(np.float32) for c in range(nch)]
+    f = mf.MultiChannel.MatchedFilter(dtype=np.float32)
+    f.initialize(_params(mf, tps, n), template_channels=chan, n_channels=nch)
+    f.set_channel_signals(np.stack(sigs))
+    f.apply()
+    ref = oracle.matched_filter(tps, [sigs[c] for c in chan], multi=True, fp64_from_f32=True)
+    worst = 0.0
+    for t in range(nt):
+        a = f.get_valid_matched_filtered_signal(t).astype(np.float64)
+        assert a.size == ref[t].size
+        worst = max(worst, float(np.max(np.abs(a - ref[t]))))
+    assert worst < 1e-5, worst
+
+
+def stress_case(n=400_000, nch=2, seed=3):
+    """DC offset U(1e3, 1e5), amplitude envelope piecewise constant over
+    segments of 20k..60k samples with levels log-uniform in [1e-3, 1e3],
+    template copies at 0.2..1 x the local RMS."""
+    rng = np.random.default_rng(seed)
+    tp = _template(500, 1000)
+    chans, bounds = [], []
+    for c in range(nch):
+        noise = _bp(rng.standard_normal(n), 1.0, 10.0)
+        env = np.empty(n)
+        edges = [0]
+        while edges[-1] < n:
+            edges.append(min(n, edges[-1] + int(rng.integers(20_000, 60_001))))
+        for a, b in zip(edges[:-1], edges[1:]):
+            env[a:b] = 10.0 ** rng.uniform(-3, 3)
+        x = env * noise
+        for o in rng.integers(0, n - tp.size, 10):
+            lvl = env[o] * np.sqrt(np.mean(noise ** 2))
+            x[o:o + tp.size] += rng.uniform(0.2, 1.0) * lvl * tp / np.sqrt(np.mean(tp ** 2))
+        chans.append(x + rng.uniform(1e3, 1e5))
+        bounds.append(np.array(edges))
+    return tp, chans, bounds
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+def test_precision_stress(gpu, oracle, dtype, capsys):
+    mf = gpu
+    tp, chans, bounds = stress_case()
+    n = chans[0].size
+    f = mf.MultiChannel.MatchedFilter(dtype=dtype)
+    f.initialize(_params(mf, [tp, tp], n), template_channels=[0, 1], n_channels=2)
+    f.set_channel_signals(np.stack([c.astype(dtype) for c in chans]))
+    f.apply()
+    rng = np.random.default_rng(9)
+    lags = np.sort(rng.choice(n - tp.size + 1, 4000, replace=False))
+    worst_all, worst_flat = 0.0, 0.0
+    for c in range(2):
+        x = chans[c].astype(dtype).astype(np.float64)
+        truth = oracle.pearson_naive(tp, x, lags)
+        got = f.get_valid_matched_filtered_signal(c).astype(np.float64)[lags]
+        err = np.abs(got - truth)
+        worst_all = max(worst_all, float(err.max()))
+        # windows whose FFT block (4096 samples either side) stays inside one
+        # envelope segment
+        e = bounds[c]
+        seg = np.searchsorted(e, lags, side="right") - 1
+        flat = (lags - 4096 >= e[seg]) & (lags + tp.size + 4096 <= e[seg + 1])
+        if flat.any():
+            worst_flat = max(worst_flat, float(err[flat].max()))
+    with capsys.disabled():
+        print("\nprecision stress %s: max|drho| all lags %.3g, lags away from envelope steps %.3g"
+              % (np.dtype(dtype).name, worst_all, worst_flat))
+    if dtype == np.float64:
+        assert worst_all < 1e-5 and worst_flat < 1e-7
+    else:
+        assert worst_flat < 1e-4
