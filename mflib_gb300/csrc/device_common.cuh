@@ -209,15 +209,6 @@ template <> struct acc_t<float>
     {
         df r; r.hi = __shfl_up_sync(0xffffffffu, a.hi, d); r.lo = __shfl_up_sync(0xffffffffu, a.lo, d); return r;
     }
-    // sqrt(L) / max(tol, sqrt(L*s2 - s1^2)); 0 for a constant window
-    // (L*s2 - s1^2 <= 0), whose exact numerator is 0
-    static __device__ __forceinline__ float inv_den(df s1, df s2, int L, float tol)
-    {
-        df v = df_sub(df_mul_f(s2, (float) L), df_sqr(s1));
-        float var = df_to_f(v);
-        if (!(var > 0.f)) return 0.f;
-        return sqrtf((float) L) / fmaxf(sqrtf(var), tol);
-    }
 };
 template <> struct acc_t<double>
 {
@@ -229,12 +220,6 @@ template <> struct acc_t<double>
     static __device__ __forceinline__ double add_val(double a, double v) { return a + v; }
     static __device__ __forceinline__ double add_sq(double a, double v) { return fma(v, v, a); }
     static __device__ __forceinline__ double shfl_up(double a, int d) { return __shfl_up_sync(0xffffffffu, a, d); }
-    static __device__ __forceinline__ double inv_den(double s1, double s2, int L, double tol)
-    {
-        double var = (double) L * s2 - s1 * s1;
-        if (!(var > 0.0)) return 0.0;
-        return sqrt((double) L) / fmax(sqrt(var), tol);
-    }
 };
 
 // ----------------------------------------------------------------------------

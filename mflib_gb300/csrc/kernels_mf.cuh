@@ -90,11 +90,16 @@ template <class T, int LOG2P> struct XcorrLayout
     static constexpr size_t up(size_t v) { return (v + 127) & ~size_t(127); }
     static constexpr size_t seg = sizeof(T) * N;
     static constexpr size_t fft = sizeof(cx<T>) * spad_size(P);
-    static constexpr size_t head(bool sd) { return up(64 + 32 * sizeof(T) + (sd ? 0 : 2 * sizeof(acc) * (NCH + 1))); }
+    static constexpr size_t head(bool sd)
+    {
+        return up(64 + 32 * sizeof(T) + (sd ? 0 : 2 * sizeof(acc) * (NCH + 1) + 2 * sizeof(T) * NCH));
+    }
     static constexpr size_t tw_bytes = sizeof(cx<T>) * FftPlan<LOG2P>::post_off();  // pass twiddles only
     static constexpr size_t uv = sizeof(cx<T>) * 2 * P;
     static constexpr size_t brow = sizeof(cx<T>) * (P + 2);
-    static constexpr size_t xs_region(bool sd) { return up(sd ? (seg > fft ? seg : fft) : seg); }
+    // without SHARED_DEN the region later holds the padded demeaned segment
+    static constexpr size_t padded = sizeof(T) * (N + N / 32);
+    static constexpr size_t xs_region(bool sd) { return up(sd ? (seg > fft ? seg : fft) : padded); }
     static constexpr size_t off_xs(bool sd) { return head(sd); }
     static constexpr size_t off_W0(bool sd) { return off_xs(sd) + (sd ? 0 : xs_region(sd)); }
     static constexpr size_t off_W1(bool sd) { return off_xs(sd) + xs_region(sd) + (sd ? 0 : up(fft)); }
@@ -260,13 +265,99 @@ __global__ void __launch_bounds__(kThreads) template_spectra_kernel(SpecParams<T
 
 // ----------------------------------------------------------------------------
 // Sliding-window statistics of the staged segment.
+// Window-sum arithmetic shared by the per-channel normalisation kernel and
+// the correlator's in-CTA normalisation (several template lengths).
+// Shared-memory sample layouts pad one word per 32 samples.
+__host__ __device__ constexpr int den_pad(int i) { return i + (i >> 5); }
+template <class T> struct DenOps;
+template <> struct DenOps<float>
+{
+    using acc = df;
+    // run sums with deferred low words
+    struct Run { float h1, l1, h2, l2; };
+    static __device__ __forceinline__ Run run_zero() { return Run{0.f, 0.f, 0.f, 0.f}; }
+    static __device__ __forceinline__ df zero() { return df{0.f, 0.f}; }
+    static __device__ __forceinline__ void run_add(Run &s, float v)
+    {
+        const float t = s.h1 + v, bb = t - s.h1;
+        s.l1 += (s.h1 - (t - bb)) + (v - bb);
+        s.h1 = t;
+        const float p = v * v, pe = fmaf(v, v, -p);
+        const float u = s.h2 + p, b2 = u - s.h2;
+        s.l2 += ((s.h2 - (u - b2)) + (p - b2)) + pe;
+        s.h2 = u;
+    }
+    static __device__ __forceinline__ df s1(const Run &s) { return quick_two_sum(s.h1, s.l1); }
+    static __device__ __forceinline__ df s2(const Run &s) { return quick_two_sum(s.h2, s.l2); }
+    // addition for the scans: one TwoSum, low words added (about 44 bits)
+    static __device__ __forceinline__ df add(df a, df b)
+    {
+        df s = two_sum(a.hi, b.hi);
+        s.lo += a.lo + b.lo;
+        return quick_two_sum(s.hi, s.lo);
+    }
+    static __device__ __forceinline__ df neg(df a) { return df{-a.hi, -a.lo}; }
+    static __device__ __forceinline__ df shfl_up(df a, int d)
+    {
+        return df{__shfl_up_sync(0xffffffffu, a.hi, d), __shfl_up_sync(0xffffffffu, a.lo, d)};
+    }
+    // V = L s2 - s1^2 as (hi, lo)
+    static __device__ __forceinline__ void var0(df w1, df w2, int L, float &vh, float &vl)
+    {
+        df a = two_prod((float) L, w2.hi);
+        a.lo = fmaf((float) L, w2.lo, a.lo);
+        df b = two_prod(w1.hi, w1.hi);
+        b.lo = fmaf(2.f * w1.hi, w1.lo, b.lo);
+        const df v = two_sum(a.hi, -b.hi);
+        vh = v.hi;
+        vl = v.lo + (a.lo - b.lo);
+    }
+    static __device__ __forceinline__ float hi(df a) { return a.hi; }
+    // a window with V <= 0 is constant (the sums are exact there) and its
+    // exact numerator against a zero-mean template is 0: rho = 0 instead of
+    // the numerator's rounding error times sqrt(L)/tol
+    static __device__ __forceinline__ float out(float var, float sqrtL, float tol)
+    {
+        return var > tol * tol ? sqrtL * rsqrtf(var) : (var > 0.f ? sqrtL / tol : 0.f);
+    }
+};
+template <> struct DenOps<double>
+{
+    using acc = double;
+    struct Run { double a1, a2; };
+    static __device__ __forceinline__ Run run_zero() { return Run{0.0, 0.0}; }
+    static __device__ __forceinline__ double zero() { return 0.0; }
+    static __device__ __forceinline__ void run_add(Run &s, double v)
+    {
+        s.a1 += v;
+        s.a2 = fma(v, v, s.a2);
+    }
+    static __device__ __forceinline__ double s1(const Run &s) { return s.a1; }
+    static __device__ __forceinline__ double s2(const Run &s) { return s.a2; }
+    static __device__ __forceinline__ double add(double a, double b) { return a + b; }
+    static __device__ __forceinline__ double neg(double a) { return -a; }
+    static __device__ __forceinline__ double shfl_up(double a, int d) { return __shfl_up_sync(0xffffffffu, a, d); }
+    static __device__ __forceinline__ void var0(double w1, double w2, int L, double &vh, double &vl)
+    {
+        vh = fma((double) L, w2, -w1 * w1);
+        vl = 0.0;
+    }
+    static __device__ __forceinline__ double hi(double a) { return a; }
+    static __device__ __forceinline__ double out(double var, double sqrtL, double tol)
+    {
+        return var > 0.0 ? sqrtL / fmax(sqrt(var), tol) : 0.0;
+    }
+};
+
 template <class T> struct SegStats
 {
     using A = acc_t<T>;
     using acc = typename A::type;
-    const T *xs;   // raw segment, N samples
+    const T *xs;   // raw segment, N samples (until the forward FFT)
+    T *yp;         // after the forward FFT: demeaned segment, one pad word per 32 (den_pad)
     T m;           // segment mean
-    acc *c1, *c2;  // chunk prefix sums (N/32 + 1 entries each)
+    acc *c1, *c2;  // chunk prefix sums of (x - m) (N/32 + 1 entries each)
+    T *p1, *p2;    // per chunk: sums of the first L mod 32 samples (N/32 entries each)
 };
 
 // Chunk sums over 32 samples with a per-lane skew (conflict-free banks),
@@ -336,44 +427,97 @@ __device__ __forceinline__ void seg_chunk_prefix(SegStats<T> st, int tid)
     __syncthreads();
 }
 
-// inv_den[k] = sqrt(L)/max(tol, sqrt(L*s2 - s1^2)) for k in [0, S), 0 where
-// L*s2 - s1^2 <= 0 (a constant window).
-// Thread u slides over an odd-length run of lags (odd stride = no bank
-// conflicts); the run's first window comes from the chunk prefixes plus a
-// skewed partial sum.
+// Rewrites the staged segment (free once the forward FFT has read it) as
+// y = x - m with one pad word per 32 samples, for conflict-free strided
+// reads by seg_inv_den.  The padded copy fits the segment's region.
+template <class T, int N>
+__device__ __forceinline__ void seg_make_padded(SegStats<T> st, int tid)
+{
+    constexpr int PER = (N + kThreads - 1) / kThreads;
+    T v[PER];
+#pragma unroll
+    for (int i = 0; i < PER; ++i)
+    {
+        const int e = tid + i * kThreads;
+        v[i] = e < N ? st.xs[e] - st.m : (T) 0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < PER; ++i)
+    {
+        const int e = tid + i * kThreads;
+        if (e < N) st.yp[den_pad(e)] = v[i];
+    }
+    __syncthreads();
+}
+
+// invd[k] = sqrt(L)/max(tol, sqrt(V_k)), V_k = L s2 - s1^2 over [k, k+L),
+// 0 where V_k <= 0 (a constant window), for k in [0, S) (S a multiple of
+// 32), from the padded demeaned segment: exact (double-float / double)
+// window sums at each 32-lag run start -- chunk prefixes plus the partial
+// sums of the first L mod 32 samples of a chunk -- then 32 lags of
+// corrections in the data type (DenOps; the same scheme as den_kernel).
+// Ends with a barrier.
 template <class T, int N>
 __device__ __forceinline__ void seg_inv_den(SegStats<T> st, int L, int S, T tol, T *invd, int tid)
 {
     using A = acc_t<T>;
+    using O = DenOps<T>;
     using acc = typename A::type;
-    const int RL = ((S + kThreads - 1) / kThreads) | 1;
-    const int k = tid * RL;
-    const int lane = tid & 31;
-    const int kend = min(S, k + RL);
-    // prefix sums at positions k and k + L
-    acc a1 = A::zero(), a2 = A::zero(), b1 = A::zero(), b2 = A::zero();
-    const int pk = k < S ? k : 0, pe = (k < S ? k : 0) + L;
-    const int ck = pk >> 5, ce = pe >> 5, rk = pk & 31, re = pe & 31;
-#pragma unroll 4
-    for (int s = 0; s < 32; ++s)
+    constexpr int NCH = N / 32;
+    const int Lq = L >> 5, re = L & 31;
+    for (int j = tid; j < NCH; j += kThreads)
     {
-        int j = (s + lane) & 31;
-        if (j < rk) { T v = st.xs[32 * ck + j] - st.m; a1 = A::add_val(a1, v); a2 = A::add_sq(a2, v); }
-        if (j < re) { T v = st.xs[32 * ce + j] - st.m; b1 = A::add_val(b1, v); b2 = A::add_sq(b2, v); }
-    }
-    if (k >= S) return;
-    acc w1 = A::sub(A::add(st.c1[ce], b1), A::add(st.c1[ck], a1));
-    acc w2 = A::sub(A::add(st.c2[ce], b2), A::add(st.c2[ck], a2));
-    for (int q = k; q < kend; ++q)
-    {
-        invd[q] = A::inv_den(w1, w2, L, tol);
-        if (q + 1 < kend)
+        T a = 0, b = 0;
+        const T *yc = st.yp + 33 * j;
+        for (int i = 0; i < re; ++i)
         {
-            T vin = st.xs[q + L] - st.m, vout = st.xs[q] - st.m;
-            w1 = A::add_val(A::add_val(w1, vin), -vout);
-            w2 = A::sub(A::add_sq(w2, vin), A::add_sq(A::zero(), vout));
+            const T v = yc[i];
+            a += v;
+            b = fma(v, v, b);
+        }
+        st.p1[j] = a;
+        st.p2[j] = b;
+    }
+    __syncthreads();
+    const T sqrtL = sqrt((T) L), Lt = (T) L;
+    for (int v = tid; v < S / 32; v += kThreads)
+    {
+        const acc w1 = A::add_val(A::sub(st.c1[v + Lq], st.c1[v]), st.p1[v + Lq]);
+        const acc w2 = A::add_val(A::sub(st.c2[v + Lq], st.c2[v]), st.p2[v + Lq]);
+        T vh, vl;
+        O::var0(w1, w2, L, vh, vl);
+        const T c2s = (T) 2 * O::hi(w1);
+        T d1 = 0, d2 = 0;
+        T o[32];
+        const int base = 32 * v;
+#pragma unroll
+        for (int q = 0; q < 32; ++q)
+        {
+            const T var = vh + (vl + fma(Lt, d2, -d1 * (d1 + c2s)));
+            o[q] = O::out(var, sqrtL, tol);
+            if (q < 31)
+            {
+                const T yin = st.yp[den_pad(base + q + L)], yout = st.yp[den_pad(base + q)];
+                const T dd = yin - yout;
+                d2 = fma(yin + yout, dd, d2);
+                d1 += dd;
+            }
+        }
+        T *dst = invd + base;
+        if constexpr (sizeof(T) == 4)
+        {
+#pragma unroll
+            for (int q = 0; q < 32; q += 4)
+                *reinterpret_cast<float4 *>(dst + q) = make_float4(o[q], o[q + 1], o[q + 2], o[q + 3]);
+        }
+        else
+        {
+#pragma unroll
+            for (int q = 0; q < 32; q += 2) *reinterpret_cast<double2 *>(dst + q) = make_double2(o[q], o[q + 1]);
         }
     }
+    __syncthreads();
 }
 
 template <class T> __device__ __forceinline__ void store2(T *dst, T a, T b);
@@ -531,13 +675,11 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
     for (int i = tid; i < N; i += kThreads) macc.add(xs[i]);
     const T m = block_mean<T>(macc, red, N);
     SegStats<T> st;
-    st.xs = xs; st.m = m; st.c1 = c1; st.c2 = c2;
+    st.xs = xs; st.yp = xs; st.m = m; st.c1 = c1; st.c2 = c2;
+    st.p1 = reinterpret_cast<T *>(c2 + NCH + 1);
+    st.p2 = st.p1 + NCH;
     int Lcur = p.tlen[p.tids[t_begin]];
-    if constexpr (!SHARED_DEN)
-    {
-        seg_chunk_prefix<T, N>(st, tid);
-        seg_inv_den<T, N>(st, Lcur, S, p.tol, invd_s, tid);
-    }
+    if constexpr (!SHARED_DEN) seg_chunk_prefix<T, N>(st, tid);
 
     // ---- forward real FFT of (x - m), read straight from the staged segment
     //      (with SHARED_DEN the work buffer overlays the segment)
@@ -584,6 +726,13 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
             }
         }
         __syncthreads();
+    }
+    if constexpr (!SHARED_DEN)
+    {
+        // the segment's region is free now: padded demeaned copy, then the
+        // first template length's normalisation
+        seg_make_padded<T, N>(st, tid);
+        seg_inv_den<T, N>(st, Lcur, S, p.tol, invd_s, tid);
     }
 
     // ---- per template: fused conj-multiply + inverse FFT + Pearson epilogue
@@ -800,7 +949,6 @@ __host__ __device__ constexpr int den_lags_per_cta(int L)
 {
     return kDenRun * (kThreads * den_runs_per_thread(L) - den_tail_runs(L));
 }
-__host__ __device__ constexpr int den_pad(int i) { return i + (i >> 5); }
 
 template <class T> struct DenLayout
 {
@@ -815,86 +963,6 @@ template <class T> struct DenLayout
     static constexpr size_t bytes(int L)
     {
         return y_bytes(L) + sizeof(acc) * (4 * (size_t) nruns(L) + 2 + 64) + 32 * sizeof(T);
-    }
-};
-
-template <class T> struct DenOps;
-template <> struct DenOps<float>
-{
-    using acc = df;
-    // run sums with deferred low words
-    struct Run { float h1, l1, h2, l2; };
-    static __device__ __forceinline__ Run run_zero() { return Run{0.f, 0.f, 0.f, 0.f}; }
-    static __device__ __forceinline__ df zero() { return df{0.f, 0.f}; }
-    static __device__ __forceinline__ void run_add(Run &s, float v)
-    {
-        const float t = s.h1 + v, bb = t - s.h1;
-        s.l1 += (s.h1 - (t - bb)) + (v - bb);
-        s.h1 = t;
-        const float p = v * v, pe = fmaf(v, v, -p);
-        const float u = s.h2 + p, b2 = u - s.h2;
-        s.l2 += ((s.h2 - (u - b2)) + (p - b2)) + pe;
-        s.h2 = u;
-    }
-    static __device__ __forceinline__ df s1(const Run &s) { return quick_two_sum(s.h1, s.l1); }
-    static __device__ __forceinline__ df s2(const Run &s) { return quick_two_sum(s.h2, s.l2); }
-    // addition for the scans: one TwoSum, low words added (about 44 bits)
-    static __device__ __forceinline__ df add(df a, df b)
-    {
-        df s = two_sum(a.hi, b.hi);
-        s.lo += a.lo + b.lo;
-        return quick_two_sum(s.hi, s.lo);
-    }
-    static __device__ __forceinline__ df neg(df a) { return df{-a.hi, -a.lo}; }
-    static __device__ __forceinline__ df shfl_up(df a, int d)
-    {
-        return df{__shfl_up_sync(0xffffffffu, a.hi, d), __shfl_up_sync(0xffffffffu, a.lo, d)};
-    }
-    // V = L s2 - s1^2 as (hi, lo)
-    static __device__ __forceinline__ void var0(df w1, df w2, int L, float &vh, float &vl)
-    {
-        df a = two_prod((float) L, w2.hi);
-        a.lo = fmaf((float) L, w2.lo, a.lo);
-        df b = two_prod(w1.hi, w1.hi);
-        b.lo = fmaf(2.f * w1.hi, w1.lo, b.lo);
-        const df v = two_sum(a.hi, -b.hi);
-        vh = v.hi;
-        vl = v.lo + (a.lo - b.lo);
-    }
-    static __device__ __forceinline__ float hi(df a) { return a.hi; }
-    // a window with V <= 0 is constant (the sums are exact there) and its
-    // exact numerator against a zero-mean template is 0: rho = 0 instead of
-    // the numerator's rounding error times sqrt(L)/tol
-    static __device__ __forceinline__ float out(float var, float sqrtL, float tol)
-    {
-        return var > tol * tol ? sqrtL * rsqrtf(var) : (var > 0.f ? sqrtL / tol : 0.f);
-    }
-};
-template <> struct DenOps<double>
-{
-    using acc = double;
-    struct Run { double a1, a2; };
-    static __device__ __forceinline__ Run run_zero() { return Run{0.0, 0.0}; }
-    static __device__ __forceinline__ double zero() { return 0.0; }
-    static __device__ __forceinline__ void run_add(Run &s, double v)
-    {
-        s.a1 += v;
-        s.a2 = fma(v, v, s.a2);
-    }
-    static __device__ __forceinline__ double s1(const Run &s) { return s.a1; }
-    static __device__ __forceinline__ double s2(const Run &s) { return s.a2; }
-    static __device__ __forceinline__ double add(double a, double b) { return a + b; }
-    static __device__ __forceinline__ double neg(double a) { return -a; }
-    static __device__ __forceinline__ double shfl_up(double a, int d) { return __shfl_up_sync(0xffffffffu, a, d); }
-    static __device__ __forceinline__ void var0(double w1, double w2, int L, double &vh, double &vl)
-    {
-        vh = fma((double) L, w2, -w1 * w1);
-        vl = 0.0;
-    }
-    static __device__ __forceinline__ double hi(double a) { return a; }
-    static __device__ __forceinline__ double out(double var, double sqrtL, double tol)
-    {
-        return var > 0.0 ? sqrtL / fmax(sqrt(var), tol) : 0.0;
     }
 };
 
