@@ -86,7 +86,9 @@ typedef struct
     int fft_length;
     /* Extension: correlator organisation; 0 = automatic, 1 = whole CTA per
        transform, 2 = whole CTA with the next spectrum prefetched by TMA,
-       3 = two 128-thread teams per CTA (templates of one length only). */
+       3 = two 128-thread teams per CTA (templates of one length only),
+       4 = split-precision (FP16 hi+lo) time-domain correlation on the tensor
+       cores (FP32 data, templates of one length). */
     int correlator_variant;
 } mfgpu_mf_params;
 

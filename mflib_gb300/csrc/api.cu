@@ -127,11 +127,16 @@ struct mfgpu_mf
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t copy_done = nullptr, x_ev = nullptr, xstage_ev = nullptr;
     bool staged = false;
+    // tensor-core correlator (correlator_variant 4): template groups of Gp
+    // slots, K padded to Kp, tiles of 1024 lags per group
+    bool tc = false;
+    int tc_Kp = 0, tc_Gp = 0, tc_groups = 0, tc_tiles = 0, tc_cols = 0, n_sm = 0;
     long ldx = 0, ldr = 0;
     int dead_chunks = 1;
     // device buffers
     DevBuf x, rho, Bc, tw, grp_chan, grp_tb, grp_te, tids, tlen_d, nvalid_d, dead, err, tmpl_d, toff_d, pmin, pmax,
-        chan_list, stackbuf, shifts_d, weights_d, specbuf, den, xstage;
+        chan_list, stackbuf, shifts_d, weights_d, specbuf, den, xstage, xrange, tc_B, tc_bscale, tc_grp_chan,
+        tc_grp_tid;
     long ldd = 0;
     int nden = 0;
     PeakWS pk;
@@ -151,7 +156,8 @@ struct mfgpu_mf
     {
         DevBuf *all[] = {&x,      &rho,      &Bc,   &tw,  &grp_chan, &grp_tb, &grp_te, &tids,      &tlen_d,
                          &nvalid_d, &dead,   &err,  &tmpl_d, &toff_d, &pmin, &pmax,  &chan_list, &stackbuf,
-                         &shifts_d, &weights_d, &specbuf, &den, &pk_cnt, &pk_idx, &pk_val, &xstage};
+                         &shifts_d, &weights_d, &specbuf, &den, &pk_cnt, &pk_idx, &pk_val, &xstage,
+                         &xrange,   &tc_B,   &tc_bscale, &tc_grp_chan, &tc_grp_tid};
         for (DevBuf *d : all) d->release();
         pk.release();
     }
@@ -377,10 +383,13 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
                              : xcorr_smem_bytes<double>(l2p, all_equal, mode, S);
     };
     const int forced_mode = p->correlator_variant >= 1 && p->correlator_variant <= 3 ? p->correlator_variant - 1 : -1;
-    if (p->correlator_variant < 0 || p->correlator_variant > 3)
-        return fail(MFGPU_EINVAL, "correlator_variant must be 0..3");
+    if (p->correlator_variant < 0 || p->correlator_variant > 4)
+        return fail(MFGPU_EINVAL, "correlator_variant must be 0..4");
     if (forced_mode == 2 && !all_equal)
         return fail(MFGPU_EINVAL, "correlator_variant 3 (teams) needs templates of one length");
+    mf->tc = p->correlator_variant == 4;
+    if (mf->tc && (mf->prec != 4 || !all_equal))
+        return fail(MFGPU_EINVAL, "correlator_variant 4 (tensor cores) needs FP32 data and templates of one length");
     int dev_smem = 0, sm_smem = 0;
     CU(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, mf->dev));
     CU(cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, mf->dev));
@@ -452,6 +461,44 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
         mf->ldd = (std::max<long>((long) mf->nblocks * best_S + 32, (long) mf->nden * lpc) + 63) / 64 * 64;
         mf->ldx = std::max<long>(mf->ldx, ((long) mf->nden * lpc + 32L * den_tail_runs(maxLen) + 63) / 64 * 64);
     }
+    std::vector<std::vector<int>> chan_t(nch);
+    for (int t = 0; t < nt; ++t) chan_t[tchan[t]].push_back(t);
+    std::vector<int> tc_gch, tc_gtid;
+    if (mf->tc)
+    {
+        // Hankel GEMM plan: K = L + 7 (8 phases) padded to 16; as many
+        // templates per group (even, MMA N = 8 per template) as fit the
+        // shared memory left beside the strips
+        const int Kp = (maxLen + 7 + 15) / 16 * 16;
+        const long room = (long) dev_smem - (long) tc_smem_bytes(Kp, 0);
+        const int gmax = (int) std::min<long>(32, room / (32L * Kp)) & ~1;
+        if (gmax < 2)
+            return fail(MFGPU_EINVAL, "template length " + std::to_string(maxLen) +
+                                          " is too long for the tensor-core correlator");
+        const int Gp = std::min(gmax, (max_tpc + 1) & ~1);
+        for (int c = 0; c < nch; ++c)
+            for (size_t i = 0; i < chan_t[c].size(); i += Gp)
+            {
+                tc_gch.push_back(c);
+                for (int k = 0; k < Gp; ++k)
+                    tc_gtid.push_back(i + k < chan_t[c].size() ? chan_t[c][i + k] : -1);
+            }
+        mf->tc_Kp = Kp;
+        mf->tc_Gp = Gp;
+        mf->tc_groups = (int) tc_gch.size();
+        mf->tc_tiles = (std::max(1, maxvalid) + kTcLags - 1) / kTcLags;
+        int cols = 32;
+        while (cols < 16 * Gp) cols *= 2;
+        mf->tc_cols = cols;
+        CU(cudaDeviceGetAttribute(&mf->n_sm, cudaDevAttrMultiProcessorCount, mf->dev));
+        // strips read tiles * 1024 + Kp samples; the normalisation row covers every tile
+        const long tl = (long) mf->tc_tiles * kTcLags;
+        const long lpc = den_lags_per_cta(maxLen);
+        mf->nden = (int) ((std::max<long>(tl, maxvalid) + lpc - 1) / lpc);
+        mf->ldd = (std::max<long>(mf->ldd, std::max<long>(tl, (long) mf->nden * lpc)) + 63) / 64 * 64;
+        mf->ldx = std::max<long>(mf->ldx, (tl + Kp + 63) / 64 * 64);
+        mf->ldx = std::max<long>(mf->ldx, ((long) mf->nden * lpc + 32L * den_tail_runs(maxLen) + 63) / 64 * 64);
+    }
     // work groups: split each channel's templates so the grid has enough CTAs
     int G = std::max(1, max_tpc);
     auto count_groups = [&](int gsz) {
@@ -461,8 +508,6 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
     };
     while (G > 1 && ((long) mf->nblocks * count_groups(G) < 4L * 152 * 2 || count_groups(G) > 65535)) G = (G + 1) / 2;
     if (count_groups(G) > 65535) return fail(MFGPU_EINVAL, "too many template groups");
-    std::vector<std::vector<int>> chan_t(nch);
-    for (int t = 0; t < nt; ++t) chan_t[tchan[t]].push_back(t);
     std::vector<int> gch, gtb, gte, tids;
     for (int c = 0; c < nch; ++c)
     {
@@ -512,8 +557,25 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
     CU(cudaMemcpyAsync(mf->nvalid_d.p, mf->nvalid.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, mf->stream));
     CU(cudaMemcpyAsync(mf->tmpl_d.p, mf->tmpl.data(), sizeof(double) * tot, cudaMemcpyHostToDevice, mf->stream));
     CU(cudaMemcpyAsync(mf->toff_d.p, mf->toff.data(), sizeof(long) * nt, cudaMemcpyHostToDevice, mf->stream));
+    CU(mf->xrange.ensure(sizeof(float) * nch));
+    CU(cudaMemsetAsync(mf->xrange.p, 0, sizeof(float) * nch, mf->stream));
     mfgpu_status s2 = mf->prec == 4 ? mf_upload_tables<float>(mf) : mf_upload_tables<double>(mf);
     if (s2 != MFGPU_OK) return s2;
+    if (mf->tc)
+    {
+        const size_t slots = (size_t) mf->tc_groups * mf->tc_Gp;
+        CU(mf->tc_grp_chan.ensure(sizeof(int) * tc_gch.size()));
+        CU(mf->tc_grp_tid.ensure(sizeof(int) * slots));
+        CU(mf->tc_bscale.ensure(sizeof(float) * slots));
+        CU(mf->tc_B.ensure(sizeof(__half) * 16 * slots * mf->tc_Kp));
+        CU(cudaMemcpyAsync(mf->tc_grp_chan.p, tc_gch.data(), sizeof(int) * tc_gch.size(), cudaMemcpyHostToDevice,
+                           mf->stream));
+        CU(cudaMemcpyAsync(mf->tc_grp_tid.p, tc_gtid.data(), sizeof(int) * slots, cudaMemcpyHostToDevice, mf->stream));
+        CU(launch_tc_bank(mf->tmpl_d.as<double>(), mf->toff_d.as<long>(), mf->tlen_d.as<int>(),
+                          mf->tc_grp_tid.as<int>(), mf->tc_groups, mf->tc_Gp, mf->tc_Kp, mf->tc_B.as<__half>(),
+                          mf->tc_bscale.as<float>(), mf->stream));
+        ++mf->launches;
+    }
     CU(cudaStreamSynchronize(mf->stream));
     CU(cudaGetLastError());
     mf->initialized = true;
@@ -593,7 +655,8 @@ static mfgpu_status mf_resolve_stage(mfgpu_mf *mf)
     std::swap(mf->x_ev, mf->xstage_ev);
     if (mf->prec == 4)
         CU(launch_dead<float>(mf->x.as<float>(), mf->ldx, mf->nch, mf->n, mf->dead.as<unsigned char>(),
-                              mf->pmin.as<float>(), mf->pmax.as<float>(), mf->dead_chunks, mf->stream));
+                              mf->pmin.as<float>(), mf->pmax.as<float>(), mf->dead_chunks, mf->stream,
+                              mf->xrange.as<float>()));
     else
         CU(launch_dead<double>(mf->x.as<double>(), mf->ldx, mf->nch, mf->n, mf->dead.as<unsigned char>(),
                                mf->pmin.as<double>(), mf->pmax.as<double>(), mf->dead_chunks, mf->stream));
@@ -652,7 +715,8 @@ static mfgpu_status mf_store_signals(mfgpu_mf *mf, int c0, int nch, int n, const
     const size_t poff = (size_t) c0 * mf->dead_chunks;
     if (mf->prec == 4)
         CU(launch_dead<float>(reinterpret_cast<const float *>(row), mf->ldx, nch, mf->n, dflag,
-                              mf->pmin.as<float>() + poff, mf->pmax.as<float>() + poff, mf->dead_chunks, mf->stream));
+                              mf->pmin.as<float>() + poff, mf->pmax.as<float>() + poff, mf->dead_chunks, mf->stream,
+                              mf->xrange.as<float>() + c0));
     else
         CU(launch_dead<double>(reinterpret_cast<const double *>(row), mf->ldx, nch, mf->n, dflag,
                                mf->pmin.as<double>() + poff, mf->pmax.as<double>() + poff, mf->dead_chunks,
@@ -765,7 +829,7 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
     // fused peak candidates
     mf->pk_fused = false;
     p.pk_on = 0;
-    if (mf->pk_req >= 0)
+    if (mf->pk_req >= 0 && !mf->tc)
     {
         const size_t nslot = (size_t) mf->nt * mf->nblocks;
         CU(mf->pk_cnt.ensure(sizeof(int) * nslot));
@@ -780,6 +844,25 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
         p.pk_val = mf->pk_val.as<T>();
     }
     CU(cudaEventRecord(mf->ev[1], mf->stream));
+    if constexpr (sizeof(T) == 4)
+    {
+        if (mf->tc)
+        {
+            TcParams q{};
+            q.x = mf->x.as<float>(); q.ldx = mf->ldx;
+            q.B = mf->tc_B.as<__half>(); q.bscale = mf->tc_bscale.as<float>();
+            q.grp_chan = mf->tc_grp_chan.as<int>(); q.grp_tid = mf->tc_grp_tid.as<int>();
+            q.xrange = mf->xrange.as<float>(); q.dead = mf->dead.as<unsigned char>();
+            q.den = mf->den.as<float>(); q.ldd = mf->ldd;
+            q.rho = mf->rho.as<float>(); q.ldr = mf->ldr;
+            q.nv = mf->maxvalid; q.Kp = mf->tc_Kp; q.Gp = mf->tc_Gp; q.tmem_cols = mf->tc_cols;
+            q.ngroups = mf->tc_groups; q.tiles = mf->tc_tiles; q.err = mf->err.as<int>();
+            const long work = (long) q.ngroups * q.tiles;
+            CU(launch_tc_xcorr(q, (int) std::min<long>(mf->n_sm, work), mf->stream));
+            ++mf->launches;
+            return MFGPU_OK;
+        }
+    }
     CU(launch_xcorr<T>(mf->log2p, mf->shared_den, mf->mode_x, p, mf->nblocks, mf->ngroups, mf->stream));
     ++mf->launches;
     if (p.pk_on)

@@ -1166,7 +1166,7 @@ __global__ void __launch_bounds__(kThreads) minmax_partial_kernel(const T *x, lo
 
 // one CTA per channel (blockIdx.x): partials pmin/pmax[c * nchunks + j]
 template <class T>
-__global__ void minmax_final_kernel(const T *pmin, const T *pmax, int nchunks, unsigned char *dead)
+__global__ void minmax_final_kernel(const T *pmin, const T *pmax, int nchunks, unsigned char *dead, float *range)
 {
     __shared__ T smin[32], smax[32];
     pmin += (long) blockIdx.x * nchunks;
@@ -1195,6 +1195,7 @@ __global__ void minmax_final_kernel(const T *pmin, const T *pmax, int nchunks, u
             mx = smax[i] > mx ? smax[i] : mx;
         }
         *dead = fabs(mn) == fabs(mx) ? 1 : 0;
+        if (range) range[blockIdx.x] = (float) (mx - mn);  // max - min (tensor-core strip scale)
     }
 }
 

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 #include "kernels_mf.cuh"
 #include "kernels_util.cuh"
+#include "tc_params.h"
 
 namespace mfgpu {
 
@@ -26,9 +27,16 @@ template <class T> cudaError_t launch_den(const T *x, long ldx, int L, T *den, l
 // twiddle table of the FFT plan for P = 2^log2p (FftPlan layout)
 template <class T> void twiddle_table(int log2p, std::vector<cx<T>> &out);
 // dead-trace flags of nch channels (rows of n samples, stride ldx): two
-// launches; pmin/pmax are scratch of nch * nchunks entries each
+// launches; pmin/pmax are scratch of nch * nchunks entries each; range
+// (optional) receives max - min per channel
 template <class T> cudaError_t launch_dead(const T *x, long ldx, int nch, long n, unsigned char *dead, T *pmin,
-                                           T *pmax, int nchunks, cudaStream_t s);
+                                           T *pmax, int nchunks, cudaStream_t s, float *range = nullptr);
+// tensor-core correlator (FP32, one template length): shared memory per CTA,
+// the template bank in MMA layout (ngroups * Gp slots), the persistent launch
+size_t tc_smem_bytes(int Kp, int Gp);
+cudaError_t launch_tc_bank(const double *tmpl, const long *toff, const int *tlen, const int *grp_tid, int ngroups,
+                           int Gp, int Kp, __half *B, float *bscale, cudaStream_t s);
+cudaError_t launch_tc_xcorr(const TcParams &p, int nctas, cudaStream_t s);
 // reference debug spectrum of one prepared template at FFT length nfft
 template <class T> cudaError_t launch_ref_spectrum(const double *tmpl, int L, int nfft, T *out, cudaStream_t s);
 // shift and stack (src/matchedFilter.cpp:1319-1364)

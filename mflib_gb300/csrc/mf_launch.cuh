@@ -101,14 +101,14 @@ template <> void twiddle_table<MFGPU_T>(int log2p, std::vector<cx<MFGPU_T>> &out
 
 template <>
 cudaError_t launch_dead<MFGPU_T>(const MFGPU_T *x, long ldx, int nch, long n, unsigned char *dead, MFGPU_T *pmin,
-                                 MFGPU_T *pmax, int nchunks, cudaStream_t s)
+                                 MFGPU_T *pmax, int nchunks, cudaStream_t s, float *range)
 {
     int chunk = (int) ((n + nchunks - 1) / nchunks);
     dim3 grid(nchunks, nch);
     minmax_partial_kernel<MFGPU_T><<<grid, kThreads, 0, s>>>(x, ldx, n, chunk, pmin, pmax, nchunks);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    minmax_final_kernel<MFGPU_T><<<nch, 256, 0, s>>>(pmin, pmax, nchunks, dead);
+    minmax_final_kernel<MFGPU_T><<<nch, 256, 0, s>>>(pmin, pmax, nchunks, dead, range);
     return cudaGetLastError();
 }
 

@@ -173,7 +173,8 @@ class MatchedFilter:
         signal; ``fft_length`` forces the overlap-save FFT length;
         ``correlator_variant`` forces the correlator organisation (0 automatic,
         1 whole CTA, 2 whole CTA with spectrum prefetch, 3 two teams per CTA,
-        templates of one length only)."""
+        templates of one length only; 4 split-precision tensor-core
+        correlation, FP32 and templates of one length)."""
         if not isinstance(params, MatchedFilterParameters) or not params.is_valid():
             raise ValueError("Parameters are invalid")
         tmpls = [params.get_template(i) for i in range(params.get_number_of_templates())]

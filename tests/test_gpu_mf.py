@@ -511,3 +511,48 @@ def test_staged_upload_pipeline(gpu, rng):
     f.apply()
     assert not np.any(f.get_matched_filtered_signal(3))
     f.synchronize()
+
+
+@pytest.mark.parametrize("L", [16, 100, 500, 1000])
+@pytest.mark.parametrize("ntpl", [1, 3, 8])
+def test_tensor_core_correlator(gpu, oracle, rng, L, ntpl, capsys):
+    """Split-precision tensor-core correlation (correlator_variant 4): the
+    FP16 hi+lo Hankel GEMM gives the oracle's FP64 coefficients within the
+    1e-4 bound stated for the split-precision form; odd template counts pad
+    a group, the last tile is partial, one channel is dead."""
+    mf = gpu
+    n = 47_111 + L
+    t = np.arange(n)
+    chans = [rng.standard_normal(n) + 40.0 + 3.0 * np.sin(2 * np.pi * t / 9_000.0 + k) for k in range(3)]
+    chans[2][:] = 7.0  # dead
+    assign = [c for c in range(3) for _ in range(ntpl)]
+    tps = [rng.standard_normal(L) for _ in assign]
+    p = _params(mf, tps, n)
+    f = mf.MultiChannel.MatchedFilter(dtype=np.float32)
+    f.initialize(p, template_channels=assign, n_channels=3, correlator_variant=4)
+    f.set_channel_signals(np.stack([c.astype(np.float32) for c in chans]))
+    f.apply()
+    sig = [chans[c].astype(np.float32) for c in assign]
+    ref = oracle.matched_filter(tps, sig, multi=True, fp64_from_f32=True)
+    worst = 0.0
+    for i, c in enumerate(assign):
+        a = f.get_valid_matched_filtered_signal(i).astype(np.float64)
+        assert a.size == ref[i].size
+        if c == 2:
+            assert not np.any(a)
+            continue
+        worst = max(worst, float(np.max(np.abs(a - ref[i]))))
+    with capsys.disabled():
+        print("\ntensor-core correlator L=%d templates/channel=%d: max|drho| %.3g" % (L, ntpl, worst))
+    assert worst < 1e-4
+
+
+def test_tensor_core_errors(gpu, rng):
+    mf = gpu
+    p = _params(mf, [rng.standard_normal(100), rng.standard_normal(120)], 5000)
+    f = mf.MultiChannel.MatchedFilter(dtype=np.float32)
+    with pytest.raises(ValueError):
+        f.initialize(p, correlator_variant=4)  # needs one template length
+    g = mf.MultiChannel.MatchedFilter(dtype=np.float64)
+    with pytest.raises(ValueError):
+        g.initialize(_params(mf, [rng.standard_normal(100)], 5000), correlator_variant=4)  # FP32 only
