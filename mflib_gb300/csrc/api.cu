@@ -390,6 +390,7 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
     mf->tc = p->correlator_variant == 4;
     if (mf->tc && (mf->prec != 4 || !all_equal))
         return fail(MFGPU_EINVAL, "correlator_variant 4 (tensor cores) needs FP32 data and templates of one length");
+    const bool tc_candidate = mf->tc || (p->correlator_variant == 0 && mf->prec == 4 && all_equal && p->fft_length == 0);
     int dev_smem = 0, sm_smem = 0;
     CU(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, mf->dev));
     CU(cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, mf->dev));
@@ -430,11 +431,19 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
         if ((int) bytes > dev_smem) continue;
         int occ = occupancy(l2p, bytes);
         if (occ < 1) continue;
-        double nb = std::ceil((double) std::max(1, maxvalid) / S);
-        double cost = nb * N * (l2p + 1) * (1.0 + 1.15 * tpc) / (occ >= 2 ? 1.4 : 1.0);
+        // seconds per (template, block), measured on GB300 at P = 2048 (N =
+        // 4096, two CTAs per SM) and scaled by the measured ratios of the
+        // neighbouring FFT lengths (0.70 at N = 2048, 2.86 at N = 8192 with one
+        // CTA per SM); shorter transforms scale as N log N
+        double rel = l2p == 11 ? 1.0 : l2p == 12 ? 2.86 : 0.70 * std::ldexp(1.0, l2p - 10) * (l2p + 1) / 11.0;
+        if (l2p <= 11 && occ < 2) rel *= 1.4;
+        const double nb = std::ceil((double) std::max(1, maxvalid) / S);
+        const double cost = nb * rel * 8.4e-9;
         if (best_l2p < 0 || cost < best_cost) { best_l2p = l2p; best_S = S; best_cost = cost; best_mode = mode; }
     }
     mf->mode_x = best_mode;
+    // seconds per template-lag of the chosen FFT plan
+    const double fft_cost_per_lag = best_l2p >= 0 ? best_cost / std::max(1, maxvalid) : 1e30;
     if (best_l2p < 0)
     {
         if (p->fft_length > 0)
@@ -464,7 +473,7 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
     std::vector<std::vector<int>> chan_t(nch);
     for (int t = 0; t < nt; ++t) chan_t[tchan[t]].push_back(t);
     std::vector<int> tc_gch, tc_gtid;
-    if (mf->tc)
+    if (tc_candidate)
     {
         // Hankel GEMM plan: K = L + 7 (8 phases) padded to 16; as many
         // templates per group (even, MMA N = 8 per template) as fit the
@@ -472,10 +481,25 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
         const int Kp = (maxLen + 7 + 15) / 16 * 16;
         const long room = (long) dev_smem - (long) tc_smem_bytes(Kp, 0);
         const int gmax = (int) std::min<long>(32, room / (32L * Kp)) & ~1;
-        if (gmax < 2)
+        if (gmax < 2 && mf->tc)
             return fail(MFGPU_EINVAL, "template length " + std::to_string(maxLen) +
                                           " is too long for the tensor-core correlator");
-        const int Gp = std::min(gmax, (max_tpc + 1) & ~1);
+        // balanced groups: the busiest channel splits into ngc equal groups
+        const int ngc = gmax >= 2 ? (max_tpc + gmax - 1) / gmax : 1;
+        const int Gp = gmax >= 2 ? std::min(gmax, ((max_tpc + ngc - 1) / ngc + 1) & ~1) : 2;
+        // automatic choice: seconds per template-lag measured on GB300, about
+        // 4.6e-15 per padded template sample plus 6.6e-12 per tile row shared
+        // by the Gp templates of a group, against the FFT plan's estimate
+        if (!mf->tc && gmax >= 2)
+            mf->tc = 4.6e-15 * Kp + 6.6e-12 / Gp < 0.9 * fft_cost_per_lag;
+    }
+    if (mf->tc)
+    {
+        const int Kp = (maxLen + 7 + 15) / 16 * 16;
+        const long room = (long) dev_smem - (long) tc_smem_bytes(Kp, 0);
+        const int gmax = (int) std::min<long>(32, room / (32L * Kp)) & ~1;
+        const int ngc = (max_tpc + gmax - 1) / gmax;
+        const int Gp = std::min(gmax, ((max_tpc + ngc - 1) / ngc + 1) & ~1);
         for (int c = 0; c < nch; ++c)
             for (size_t i = 0; i < chan_t[c].size(); i += Gp)
             {

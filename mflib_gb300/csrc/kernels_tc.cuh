@@ -18,8 +18,11 @@
 // Persistent, warp-specialised CTA (one per SM):
 //   warp 0 lane 0   issues the MMAs (K/16 steps x 3) and the commits;
 //   warps 1-3       stage strips: FP32 load, offset, scale, hi/lo split;
-//   warps 4-7       epilogue: tcgen05.ld of the accumulator rows, scales,
-//                   normalisation row, |rho| > 1.1 clamp, 32-byte stores.
+//   warps 4-11      epilogue, two warpgroups taking alternate templates:
+//                   tcgen05.ld of the accumulator rows (the buffer is
+//                   released before the stores), scales, normalisation row
+//                   (prefetched a tile ahead), |rho| > 1.1 clamp, 32-byte
+//                   stores.
 // Strips and accumulators are double-buffered (mbarriers, bounded waits);
 // the group's template operands stay resident in shared memory.
 #pragma once
@@ -147,7 +150,7 @@ static __global__ void __launch_bounds__(kTcThreads, 1) tc_xcorr_kernel(TcParams
 
     if (tid == 0)
     {
-        for (int i = 0; i < 9; ++i) mbar_init(&bar[i], (i == 6 || i == 7) ? 4 : 1);
+        for (int i = 0; i < 9; ++i) mbar_init(&bar[i], (i == 6 || i == 7) ? kTcEpiWarps : 1);
         fence_proxy_async_smem();
     }
     if (warp == 0)
@@ -241,21 +244,35 @@ static __global__ void __launch_bounds__(kTcThreads, 1) tc_xcorr_kernel(TcParams
             const float s = tc_pow2_scale(p.xrange[c], 13);
             const float off = xr[0];
             __half *ah = sA + (size_t) (2 * buf) * SA, *al = ah + SA;
+            constexpr int PR = 4;  // loads in flight per thread
             if (ok)
-                for (int e = 4 * ptid; e < SA; e += 4 * kTcProducers)
+                for (int e0 = 4 * ptid; e0 < SA; e0 += 4 * kTcProducers * PR)
                 {
-                    const float4 v = *reinterpret_cast<const float4 *>(xr + e);
-                    const float y[4] = {(v.x - off) * s, (v.y - off) * s, (v.z - off) * s, (v.w - off) * s};
-                    __align__(8) __half h[4];
-                    __align__(8) __half l[4];
+                    float4 v[PR];
 #pragma unroll
-                    for (int q = 0; q < 4; ++q)
+                    for (int r = 0; r < PR; ++r)
                     {
-                        h[q] = __float2half_rn(y[q]);
-                        l[q] = __float2half_rn(y[q] - __half2float(h[q]));
+                        const int e = e0 + r * 4 * kTcProducers;
+                        v[r] = e < SA ? *reinterpret_cast<const float4 *>(xr + e) : make_float4(0.f, 0.f, 0.f, 0.f);
                     }
-                    *reinterpret_cast<uint2 *>(ah + e) = *reinterpret_cast<const uint2 *>(h);
-                    *reinterpret_cast<uint2 *>(al + e) = *reinterpret_cast<const uint2 *>(l);
+#pragma unroll
+                    for (int r = 0; r < PR; ++r)
+                    {
+                        const int e = e0 + r * 4 * kTcProducers;
+                        if (e >= SA) break;
+                        const float y[4] = {(v[r].x - off) * s, (v[r].y - off) * s, (v[r].z - off) * s,
+                                            (v[r].w - off) * s};
+                        __align__(8) __half h[4];
+                        __align__(8) __half l[4];
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                        {
+                            h[q] = __float2half_rn(y[q]);
+                            l[q] = __float2half_rn(y[q] - __half2float(h[q]));
+                        }
+                        *reinterpret_cast<uint2 *>(ah + e) = *reinterpret_cast<const uint2 *>(h);
+                        *reinterpret_cast<uint2 *>(al + e) = *reinterpret_cast<const uint2 *>(l);
+                    }
                 }
             fence_proxy_async_smem();  // generic-proxy writes before the tensor core's reads
             asm volatile("bar.sync 1, %0;" ::"n"(kTcProducers) : "memory");
@@ -264,8 +281,20 @@ static __global__ void __launch_bounds__(kTcThreads, 1) tc_xcorr_kernel(TcParams
     }
     else
     {
-        // ---- epilogue: row i of the tile = TMEM lane i
-        const int q = warp & 3, i = 32 * q + lane;
+        // ---- epilogue: row i of the tile = TMEM lane i; warpgroup eg takes
+        //      templates eg, eg + 2, ...
+        const int q = warp & 3, i = 32 * q + lane, eg = (warp - 4) >> 2;
+        constexpr int TB = 4;  // templates per batch of TMEM loads
+        float dv[8];
+        auto load_den = [&](long w) {
+            const int c = p.grp_chan[(int) (w / p.tiles)];
+            const long lag0 = (long) (w % p.tiles) * kTcLags + 8 * i;
+            const float4 d0 = *reinterpret_cast<const float4 *>(p.den + (long) c * p.ldd + lag0);
+            const float4 d1 = *reinterpret_cast<const float4 *>(p.den + (long) c * p.ldd + lag0 + 4);
+            dv[0] = d0.x; dv[1] = d0.y; dv[2] = d0.z; dv[3] = d0.w;
+            dv[4] = d1.x; dv[5] = d1.y; dv[6] = d1.z; dv[7] = d1.w;
+        };
+        if (w0 < w1) load_den(w0);
         for (long w = w0, n = 0; w < w1; ++w, ++n)
         {
             const int g = (int) (w / p.tiles), j = (int) (w % p.tiles);
@@ -280,44 +309,72 @@ static __global__ void __launch_bounds__(kTcThreads, 1) tc_xcorr_kernel(TcParams
             const long lag0 = (long) j * kTcLags + 8 * i;
             const float s = tc_pow2_scale(p.xrange[c], 13);
             const bool dead = p.dead[c] != 0;
-            float dv[8];
-            {
-                const float4 d0 = *reinterpret_cast<const float4 *>(p.den + (long) c * p.ldd + lag0);
-                const float4 d1 = *reinterpret_cast<const float4 *>(p.den + (long) c * p.ldd + lag0 + 4);
-                dv[0] = d0.x; dv[1] = d0.y; dv[2] = d0.z; dv[3] = d0.w;
-                dv[4] = d1.x; dv[5] = d1.y; dv[6] = d1.z; dv[7] = d1.w;
-            }
-            for (int t = 0; t < Gp; ++t)
-            {
-                uint32_t r[8];
-                const uint32_t taddr = tmem + ((uint32_t) (32 * q) << 16) + (uint32_t) (buf * N + 8 * t);
-                asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                             : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                               "=r"(r[7])
-                             : "r"(taddr));
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                const int tt = p.grp_tid[g * Gp + t];
-                if (tt < 0) continue;
-                const float sc = p.bscale[g * Gp + t] / s;
-                float o[8];
+            float dcur[8];
 #pragma unroll
-                for (int f = 0; f < 8; ++f) o[f] = dead ? 0.f : clamp_rho(__uint_as_float(r[f]) * sc * dv[f]);
-                float *dst = p.rho + (long) tt * p.ldr + lag0;
-                if (lag0 + 7 < p.nv)
+            for (int f = 0; f < 8; ++f) dcur[f] = dv[f];
+            const int nmine = (Gp - eg + 1) / 2;  // templates eg, eg + 2, ... below Gp
+            bool released = false;
+            for (int b0 = 0; b0 < nmine; b0 += TB)
+            {
+                uint32_t r[TB][8];
+#pragma unroll
+                for (int u = 0; u < TB; ++u)
                 {
-                    *reinterpret_cast<float4 *>(dst) = make_float4(o[0], o[1], o[2], o[3]);
-                    *reinterpret_cast<float4 *>(dst + 4) = make_float4(o[4], o[5], o[6], o[7]);
+                    if (b0 + u < nmine)  // uniform across the warp
+                    {
+                        const int t = eg + 2 * (b0 + u);
+                        const uint32_t taddr = tmem + ((uint32_t) (32 * q) << 16) + (uint32_t) (buf * N + 8 * t);
+                        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                                     : "=r"(r[u][0]), "=r"(r[u][1]), "=r"(r[u][2]), "=r"(r[u][3]), "=r"(r[u][4]),
+                                       "=r"(r[u][5]), "=r"(r[u][6]), "=r"(r[u][7])
+                                     : "r"(taddr));
+                    }
                 }
-                else
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (b0 + TB >= nmine)
                 {
+                    // every accumulator value of this tile is in registers:
+                    // release the buffer before the stores, prefetch the
+                    // next tile's normalisation row
+                    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&acc_empty[buf]);
+                    released = true;
+                    if (w + 1 < w1) load_den(w + 1);
+                }
+#pragma unroll
+                for (int u = 0; u < TB; ++u)
+                {
+                    if (b0 + u >= nmine) break;
+                    const int t = eg + 2 * (b0 + u);
+                    const int tt = p.grp_tid[g * Gp + t];
+                    if (tt < 0) continue;
+                    const float sc = p.bscale[g * Gp + t] / s;
+                    float o[8];
 #pragma unroll
                     for (int f = 0; f < 8; ++f)
-                        if (lag0 + f < p.nv) dst[f] = o[f];
+                        o[f] = dead ? 0.f : clamp_rho(__uint_as_float(r[u][f]) * sc * dcur[f]);
+                    float *dst = p.rho + (long) tt * p.ldr + lag0;
+                    if (lag0 + 7 < p.nv)
+                    {
+                        *reinterpret_cast<float4 *>(dst) = make_float4(o[0], o[1], o[2], o[3]);
+                        *reinterpret_cast<float4 *>(dst + 4) = make_float4(o[4], o[5], o[6], o[7]);
+                    }
+                    else
+                    {
+#pragma unroll
+                        for (int f = 0; f < 8; ++f)
+                            if (lag0 + f < p.nv) dst[f] = o[f];
+                    }
                 }
             }
-            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&acc_empty[buf]);
+            if (!released)
+            {
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&acc_empty[buf]);
+                if (w + 1 < w1) load_den(w + 1);
+            }
         }
     }
 

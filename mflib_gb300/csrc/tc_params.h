@@ -8,8 +8,9 @@ namespace mfgpu {
 
 constexpr int kTcRows = 128;              // MMA M: rows of a tile
 constexpr int kTcLags = 8 * kTcRows;      // lags per tile (8 phases per row)
-constexpr int kTcThreads = 256;           // warp 0 MMA issue, warps 1-3 strips, warps 4-7 epilogue
+constexpr int kTcThreads = 384;           // warp 0 MMA issue, warps 1-3 strips, warps 4-11 epilogue
 constexpr int kTcProducers = 96;
+constexpr int kTcEpiWarps = 8;            // two warpgroups, each covering the 128 rows
 
 struct TcParams
 {
