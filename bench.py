@@ -57,7 +57,8 @@ def make_template(seed, length=TEMPLATE_LEN, lo=2.0, hi=8.0):
     return sosfilt(sos, rng.standard_normal(length)) * hann(length)
 
 
-def make_workload(n_samples=N_SAMPLES, n_stations=N_STATIONS, n_events=N_EVENTS, inj=INJ_PER_EVENT, seed=10):
+def make_workload(n_samples=N_SAMPLES, n_stations=N_STATIONS, n_events=N_EVENTS, inj=INJ_PER_EVENT, seed=10,
+                  template_length=TEMPLATE_LEN):
     """Returns dict with channel signals [C, n] float32, templates (list of
     FP64 arrays), template channel/event/shift arrays and the truth."""
     nch = n_stations * N_COMP
@@ -70,7 +71,7 @@ def make_workload(n_samples=N_SAMPLES, n_stations=N_STATIONS, n_events=N_EVENTS,
     templates, tchan, tevent, tshift = [], [], [], []
     for e in range(n_events):
         for c in range(nch):
-            templates.append(make_template(100 + e * nch + c))
+            templates.append(make_template(100 + e * nch + c, template_length))
             tchan.append(c)
             tevent.append(e)
             tshift.append(int(shifts[e, c // N_COMP]))
@@ -162,12 +163,14 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(sm)}
 
 
-def measured_peak():
+def measured_peak(key="hbm_gbs"):
+    """Measured peak of the GB300s (HBM GB/s or dense BF16 TFLOP/s),
+    else the fallback figure of an earlier GB300 measurement."""
     try:
         d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-        return float(d["hbm_gbs"]), "measured"
+        return float(d[key]), "measured"
     except (OSError, KeyError, ValueError):
-        return 6800.0, "fallback"
+        return (6800.0 if key == "hbm_gbs" else 1900.0), "fallback"
 
 
 def profile_traffic():
@@ -235,6 +238,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--samples", type=int, default=N_SAMPLES, help="samples per channel (default 24 h)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--correlator-variant", type=int, default=0,
+                    help="0 planner's choice, 1-3 FFT organisations, 4 tensor cores")
+    ap.add_argument("--template-length", type=int, default=TEMPLATE_LEN,
+                    help="samples per template (default %d)" % TEMPLATE_LEN)
+    ap.add_argument("--events", type=int, default=N_EVENTS,
+                    help="events, i.e. templates per channel (default %d)" % N_EVENTS)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -263,8 +272,9 @@ def main():
         import torch
         torch.cuda.set_device(local)
     # every rank runs the full workload on its own GPU (weak scaling)
-    w = make_workload(n_samples=args.samples, seed=10 + 97 * rank)
-    f = build_filter(mf, w)
+    w = make_workload(n_samples=args.samples, seed=10 + 97 * rank, n_events=args.events,
+                      template_length=args.template_length)
+    f = build_filter(mf, w, correlator_variant=args.correlator_variant)
     # the correlator gathers the peak candidates as it stores the traces
     f.set_peak_threshold(PEAK_THR)
     db = mf.DBSCAN()
@@ -371,22 +381,37 @@ def main():
     x_ms = float(np.mean(xcorr_ms))
     plan = f.get_plan()
     P = plan["fft_length"] // 2
-    alg_bytes = 4.0 * lags_per_step + 4.0 * w["nch"] * n + 8.0 * (P + 1) * nt
-    peak, peak_kind = measured_peak()
-    achieved = alg_bytes / (x_ms * 1e-3) / 1e9
-    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": profile_traffic() if n == N_SAMPLES else None,
-            "kernel": "xcorr_kernel<float,%d,shared_den>" % (plan["fft_length"] // 2),
-            "kernel_ms": x_ms, "algorithmic_bytes": alg_bytes, "peak_source": peak_kind}
+    if plan["correlator"] == 4:
+        # tensor-core correlator: 2 L algorithmic flops per template-lag (one
+        # multiply-add per template sample; the hi/lo split executes 3 MMAs
+        # over the padded K, reported as executed_flops)
+        alg_flops = 2.0 * args.template_length * lags_per_step
+        peak, peak_kind = measured_peak("bf16_tflops")
+        achieved = alg_flops / (x_ms * 1e-3) / 1e12
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None, "kernel": "tc_xcorr_kernel",
+                "kernel_ms": x_ms, "algorithmic_flops": alg_flops,
+                "executed_flops": 6.0 * plan["tc_k"] * lags_per_step, "peak_source": peak_kind}
+    else:
+        alg_bytes = 4.0 * lags_per_step + 4.0 * w["nch"] * n + 8.0 * (P + 1) * nt
+        peak, peak_kind = measured_peak()
+        achieved = alg_bytes / (x_ms * 1e-3) / 1e9
+        default = n == N_SAMPLES and args.template_length == TEMPLATE_LEN and args.events == N_EVENTS
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": profile_traffic() if default else None,
+                "kernel": "xcorr_kernel<float,%d,shared_den>" % P,
+                "kernel_ms": x_ms, "algorithmic_bytes": alg_bytes, "peak_source": peak_kind}
 
     value = world * lags_per_step / (el / args.steps)
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32",
             "data": "synthetic seeded seismograms (band-passed noise + injected templates)",
-            "config": {"workload": "24ch x 8.64M f32, 192 templates x 500, peaks 0.5/250, dbscan 50/3",
+            "config": {"workload": "%dch x %.2fM f32, %d templates x %d, peaks 0.5/250, dbscan 50/3"
+                                   % (w["nch"], n / 1e6, nt, args.template_length),
                        "channels": w["nch"], "samples_per_channel": n, "templates": nt,
-                       "template_length": TEMPLATE_LEN, "fft_length": plan["fft_length"],
+                       "template_length": args.template_length, "correlator": plan["correlator"],
+                       "fft_length": plan["fft_length"],
                        "lags_per_block": plan["lags_per_block"],
                        "l2": "inputs (%.0f MB) and outputs (%.2f GB) exceed the 129 MB L2; no flush needed"
                              % (4e-6 * w["nch"] * n, 4e-9 * lags_per_step)},

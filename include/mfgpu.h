@@ -161,6 +161,11 @@ mfgpu_status mfgpu_mf_get_valid_signal(mfgpu_mf *mf, int it, int maxn, void *dst
 mfgpu_status mfgpu_mf_get_device_signal(mfgpu_mf *mf, int it, const void **dptr, int *nvalid);
 /* Overlap-save plan chosen at initialize. */
 mfgpu_status mfgpu_mf_get_plan(const mfgpu_mf *mf, int *fft_length, int *lags_per_block, int *n_blocks);
+/* Correlator organisation chosen at initialize, numbered like
+ * correlator_variant (1-3 FFT organisations, 4 tensor cores); for the
+ * tensor-core path also the templates per group and the padded K, else 0.
+ * Extension: the reference has one CPU correlator and no such query. */
+mfgpu_status mfgpu_mf_get_correlator(const mfgpu_mf *mf, int *variant, int *tc_group, int *tc_k);
 /* Block until the object's stream is idle; reports device-side errors. */
 mfgpu_status mfgpu_mf_synchronize(mfgpu_mf *mf);
 /* Device time (ms) of the last apply's correlation kernel and of the whole

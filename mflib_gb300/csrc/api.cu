@@ -653,6 +653,15 @@ mfgpu_status mfgpu_mf_get_plan(const mfgpu_mf *mf, int *fft_length, int *lags_pe
     return MFGPU_OK;
 }
 
+mfgpu_status mfgpu_mf_get_correlator(const mfgpu_mf *mf, int *variant, int *tc_group, int *tc_k)
+{
+    MF_CHECK_INIT(mf);
+    if (variant) *variant = mf->tc ? 4 : mf->mode_x + 1;
+    if (tc_group) *tc_group = mf->tc ? mf->tc_Gp : 0;
+    if (tc_k) *tc_k = mf->tc ? mf->tc_Kp : 0;
+    return MFGPU_OK;
+}
+
 static mfgpu_status mf_channel_of(mfgpu_mf *mf, int it, int *c)
 {
     if (it < 0 || it >= mf->nt)

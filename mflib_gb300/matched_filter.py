@@ -342,9 +342,15 @@ class MatchedFilter:
 
     # -- extensions ---------------------------------------------------------
     def get_plan(self):
+        """The plan chosen at initialize: FFT length, lags per block, blocks,
+        and the correlator (1-3 FFT organisations, 4 tensor cores; for the
+        latter also the templates per group and the padded K)."""
         a, b, c = C.c_int(), C.c_int(), C.c_int()
         _lib.call("mfgpu_mf_get_plan", self._h, C.byref(a), C.byref(b), C.byref(c))
-        return {"fft_length": a.value, "lags_per_block": b.value, "n_blocks": c.value}
+        v, g, k = C.c_int(), C.c_int(), C.c_int()
+        _lib.call("mfgpu_mf_get_correlator", self._h, C.byref(v), C.byref(g), C.byref(k))
+        return {"fft_length": a.value, "lags_per_block": b.value, "n_blocks": c.value, "correlator": v.value,
+                "tc_group": g.value, "tc_k": k.value}
 
     def last_timings(self):
         a, b = C.c_float(), C.c_float()
