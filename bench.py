@@ -230,6 +230,103 @@ def run_reference(args, w, rank):
     print(json.dumps(line), flush=True)
 
 
+def run_serving(args):
+    """Serving loop: Poisson arrivals of detection requests (windows of
+    60-600 s on 1-64 channels with 0-5 injected events) against 4 resident
+    banks of 100 / 500 / 2,000 / 5,000 templates of 200-3,000 samples, under a
+    120 GB device-memory budget; p50/p99 latency and template-lag
+    correlations/s per arrival rate, next to the same requests served one at
+    a time."""
+    from scipy.signal import butter, sosfilt
+    from scipy.signal.windows import hann
+    from mflib_gb300.serving import DetectionRequest, GpuExecutor, Server, TemplateBank, latency_stats
+
+    rng = np.random.default_rng(400)
+    banks = []
+    for name, nt in (("bank100", 100), ("bank500", 500), ("bank2000", 2000), ("bank5000", 5000)):
+        tps = []
+        for L in rng.integers(200, 3001, nt):
+            lo = rng.uniform(1.0, 7.0)
+            hi = rng.uniform(lo + 2.0, 15.0)
+            sos = butter(4, [lo, hi], btype="bandpass", fs=FS, output="sos")
+            tps.append(sosfilt(sos, rng.standard_normal(int(L))) * hann(int(L)))
+        banks.append(TemplateBank(name, tps))
+    pool_n = 240_000
+    pool = np.stack([bandpass_noise(np.random.default_rng(4000 + c), pool_n, 1.0, 10.0) for c in range(64)])
+    rms = float(np.sqrt(np.mean(pool[:, :100_000].astype(np.float64) ** 2)))
+
+    def make_requests(count, seed):
+        r = np.random.default_rng(seed)
+        out = []
+        for _ in range(count):
+            bank = banks[int(r.integers(len(banks)))]
+            n = int(r.integers(6_000, 60_001))
+            c = int(r.integers(1, 65))
+            o = int(r.integers(0, pool_n - n))
+            ch = r.choice(64, c, replace=False)
+            x = pool[ch, o:o + n].copy()
+            for _ in range(int(r.integers(0, 6))):
+                t = int(r.integers(len(bank)))
+                tp = bank.templates[t]
+                if tp.size >= n:
+                    continue
+                at = int(r.integers(0, n - tp.size))
+                amp = r.uniform(0.5, 2.0) * rms / np.sqrt(np.mean(tp ** 2))
+                x[bank.slots[t] % c, at:at + tp.size] += (amp * tp).astype(np.float32)
+            out.append((bank.name, x))
+        return out
+
+    ex = GpuExecutor(threshold=args.serving_threshold, min_distance=250)
+    srv = Server(banks, ex, memory_budget=120e9, slots=args.serving_slots)
+    t0 = time.perf_counter()
+    srv.warm([(b.name, n) for b in banks for n in srv.buckets], per_key=args.serving_slots)
+    warm_s = time.perf_counter() - t0
+    srv.start()
+    for b, x in make_requests(4 * args.serving_slots, 1):  # untimed warm-up traffic
+        srv.submit(DetectionRequest(b, x))
+    while len(srv.served) < 4 * args.serving_slots:
+        time.sleep(0.01)
+
+    rates = []
+    for k, lam in enumerate(args.rates):
+        reqs = make_requests(args.requests, 10 + k)
+        arr = np.cumsum(np.random.default_rng(500 + k).exponential(1.0 / lam, len(reqs)))
+        objs = [DetectionRequest(b, x) for b, x in reqs]
+        base = time.perf_counter() + 0.05
+        for r, a in zip(objs, arr):
+            d = base + a - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            r.t_arrival = base + a
+            srv.submit(r)
+        for r in objs:
+            r.wait(600)
+        st = latency_stats(objs)
+        # the same requests one at a time (no overlap), back to back
+        solo = [DetectionRequest(b, x) for b, x in reqs]
+        t1 = time.perf_counter()
+        for r in solo:
+            r.t_arrival = time.perf_counter()
+            srv.run_one(r)
+        el = time.perf_counter() - t1
+        so = latency_stats(solo)
+        rates.append({"rate_req_s": lam, "requests": st["requests"], "p50_ms": 1e3 * st["p50_s"],
+                      "p99_ms": 1e3 * st["p99_s"], "mean_ms": 1e3 * st["mean_s"], "throughput": st["throughput"],
+                      "one_at_a_time": {"throughput": so["template_lags"] / el, "p50_ms": 1e3 * so["p50_s"],
+                                        "p99_ms": 1e3 * so["p99_s"]}})
+    srv.close()
+    line = {"metric": "served detection requests: p50/p99 latency and template-lag correlations/s",
+            "unit": "template-lag correlations/s; ms", "n_gpus": 1, "dtype": "f32",
+            "data": "synthetic band-passed noise windows with injected template copies",
+            "config": {"workload": "Poisson arrivals, windows 6,000-60,000 samples on 1-64 channels, banks of "
+                                   "100/500/2,000/5,000 templates of 200-3,000 samples, 120 GB budget",
+                       "slots": args.serving_slots, "buckets": list(srv.buckets),
+                       "threshold": args.serving_threshold, "min_distance": 250},
+            "rates": rates, "objects_created": srv.created, "evicted": srv.evicted,
+            "peak_device_bytes": srv.peak_held, "warm_s": warm_s}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -244,8 +341,16 @@ def main():
                     help="samples per template (default %d)" % TEMPLATE_LEN)
     ap.add_argument("--events", type=int, default=N_EVENTS,
                     help="events, i.e. templates per channel (default %d)" % N_EVENTS)
+    ap.add_argument("--serving", action="store_true", help="run the request loop instead of the day-long step")
+    ap.add_argument("--rates", type=float, nargs="+", default=[50, 100, 200, 500])
+    ap.add_argument("--requests", type=int, default=200, help="requests per arrival rate (serving)")
+    ap.add_argument("--serving-slots", type=int, default=4)
+    ap.add_argument("--serving-threshold", type=float, default=0.7)
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    if args.serving:
+        run_serving(args)
+        return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

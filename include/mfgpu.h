@@ -166,6 +166,18 @@ mfgpu_status mfgpu_mf_get_plan(const mfgpu_mf *mf, int *fft_length, int *lags_pe
  * tensor-core path also the templates per group and the padded K, else 0.
  * Extension: the reference has one CPU correlator and no such query. */
 mfgpu_status mfgpu_mf_get_correlator(const mfgpu_mf *mf, int *variant, int *tc_group, int *tc_k);
+/* Request-window upload for a serving loop.  Extension: the reference sets
+ * whole-length signals one template at a time (setSignal,
+ * src/matchedFilter.cpp:863-921) and has no serving loop.  x holds n_src
+ * channel rows (row stride ld samples) of n <= signal-length samples; every
+ * channel c of the object receives row c % n_src, zero-filled from n to the
+ * signal length; dead-trace flags are decided over the first n samples.
+ * Coefficients at lags k <= n - L_t use window samples only.  Copies before
+ * returning, like setSignal. */
+mfgpu_status mfgpu_mf_set_window(mfgpu_mf *mf, int n_src, int n, const void *x, long ld);
+/* Device bytes the object holds (its buffers and peak-finder scratch), for
+ * admission against a memory budget.  Extension: no reference counterpart. */
+mfgpu_status mfgpu_mf_get_device_bytes(const mfgpu_mf *mf, unsigned long long *bytes);
 /* Block until the object's stream is idle; reports device-side errors. */
 mfgpu_status mfgpu_mf_synchronize(mfgpu_mf *mf);
 /* Device time (ms) of the last apply's correlation kernel and of the whole

@@ -75,6 +75,8 @@ _SIGS = {
     "mfgpu_mf_get_device_signal": ([_vp, C.c_int, C.POINTER(_vp), _ip], C.c_int),
     "mfgpu_mf_get_plan": ([_vp, _ip, _ip, _ip], C.c_int),
     "mfgpu_mf_get_correlator": ([_vp, _ip, _ip, _ip], C.c_int),
+    "mfgpu_mf_set_window": ([_vp, C.c_int, C.c_int, _vp, C.c_long], C.c_int),
+    "mfgpu_mf_get_device_bytes": ([_vp, C.POINTER(C.c_ulonglong)], C.c_int),
     "mfgpu_mf_synchronize": ([_vp], C.c_int),
     "mfgpu_mf_get_last_timings": ([_vp, C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int),
     "mfgpu_mf_get_launch_count": ([_vp, C.POINTER(C.c_longlong)], C.c_int),

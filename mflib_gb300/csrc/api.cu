@@ -152,14 +152,25 @@ struct mfgpu_mf
     float last_xcorr_ms = 0, last_apply_ms = 0;
 
     size_t esz() const { return (size_t) prec; }
-    void release_device()
+    template <class F> void each_buf(F &&f)
     {
         DevBuf *all[] = {&x,      &rho,      &Bc,   &tw,  &grp_chan, &grp_tb, &grp_te, &tids,      &tlen_d,
                          &nvalid_d, &dead,   &err,  &tmpl_d, &toff_d, &pmin, &pmax,  &chan_list, &stackbuf,
                          &shifts_d, &weights_d, &specbuf, &den, &pk_cnt, &pk_idx, &pk_val, &xstage,
                          &xrange,   &tc_B,   &tc_bscale, &tc_grp_chan, &tc_grp_tid};
-        for (DevBuf *d : all) d->release();
+        for (DevBuf *d : all) f(*d);
+        pk.each_buf(f);
+    }
+    void release_device()
+    {
+        each_buf([](DevBuf &d) { d.release(); });
         pk.release();
+    }
+    size_t device_bytes()
+    {
+        size_t b = 0;
+        each_buf([&](DevBuf &d) { b += d.bytes; });
+        return b;
     }
     void reset()
     {
@@ -791,6 +802,52 @@ mfgpu_status mfgpu_mf_set_channel_signals(mfgpu_mf *mf, int first_channel, int n
     if (n_channels < 1 || first_channel < 0 || first_channel + n_channels > mf->nch)
         return fail(MFGPU_EINVAL, "channel range out of range");
     return mf_store_signals(mf, first_channel, n_channels, n, x, ld, cudaMemcpyHostToDevice);
+}
+
+mfgpu_status mfgpu_mf_set_window(mfgpu_mf *mf, int n_src, int n, const void *x, long ld)
+{
+    MF_CHECK_INIT(mf);
+    DeviceGuard g(mf->dev);
+    if (n_src < 1 || n_src > mf->nch)
+        return fail(MFGPU_EINVAL, "n_src = " + std::to_string(n_src) + " must be in [1, " + std::to_string(mf->nch) + "]");
+    if (n < 1 || n > mf->n)
+        return fail(MFGPU_EINVAL, "window length " + std::to_string(n) + " must be in [1, " + std::to_string(mf->n) + "]");
+    if (!x) return fail(MFGPU_EINVAL, "x is NULL");
+    if (n_src > 1 && ld < n) return fail(MFGPU_EINVAL, "row stride is smaller than the number of samples");
+    mfgpu_status rs = mf_resolve_stage(mf);
+    if (rs != MFGPU_OK) return rs;
+    mf->have = false;
+    mf->have_peaks = false;
+    const size_t es = mf->esz(), pitch = es * (size_t) mf->ldx;
+    char *x0 = mf->x.as<char>();
+    CU(cudaMemcpy2DAsync(x0, pitch, x, es * (size_t) (n_src > 1 ? ld : n), es * (size_t) n, (size_t) n_src,
+                         cudaMemcpyHostToDevice, mf->stream));
+    if (n < mf->n)
+        CU(cudaMemset2DAsync(x0 + es * (size_t) n, pitch, 0, es * (size_t) (mf->n - n), (size_t) n_src, mf->stream));
+    // channel c >= n_src repeats channel c % n_src
+    for (int c0 = n_src; c0 < mf->nch; c0 += n_src)
+        CU(cudaMemcpy2DAsync(x0 + pitch * (size_t) c0, pitch, x0, pitch, es * (size_t) mf->n,
+                             (size_t) std::min(n_src, mf->nch - c0), cudaMemcpyDeviceToDevice, mf->stream));
+    // dead-trace flags and ranges over the window's samples only
+    if (mf->prec == 4)
+        CU(launch_dead<float>(mf->x.as<float>(), mf->ldx, mf->nch, n, mf->dead.as<unsigned char>(),
+                              mf->pmin.as<float>(), mf->pmax.as<float>(), mf->dead_chunks, mf->stream,
+                              mf->xrange.as<float>()));
+    else
+        CU(launch_dead<double>(mf->x.as<double>(), mf->ldx, mf->nch, n, mf->dead.as<unsigned char>(),
+                               mf->pmin.as<double>(), mf->pmax.as<double>(), mf->dead_chunks, mf->stream));
+    mf->launches += 2;
+    CU(cudaStreamSynchronize(mf->stream));
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_get_device_bytes(const mfgpu_mf *cmf, unsigned long long *bytes)
+{
+    auto *mf = const_cast<mfgpu_mf *>(cmf);
+    if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");
+    if (!bytes) return fail(MFGPU_EINVAL, "bytes is NULL");
+    *bytes = mf->device_bytes();
+    return MFGPU_OK;
 }
 
 mfgpu_status mfgpu_mf_set_channel_signal_device(mfgpu_mf *mf, int channel, int n, const void *dx)

@@ -260,8 +260,14 @@ static __global__ void __launch_bounds__(kTcThreads, 1) tc_xcorr_kernel(TcParams
                     {
                         const int e = e0 + r * 4 * kTcProducers;
                         if (e >= SA) break;
-                        const float y[4] = {(v[r].x - off) * s, (v[r].y - off) * s, (v[r].z - off) * s,
-                                            (v[r].w - off) * s};
+                        // samples of the channel lie within its range, so |y| < 2^13;
+                        // the clamp only touches the zero tail past the samples (or
+                        // past a shorter uploaded window), which meets zero template
+                        // coefficients at every valid lag: finite there, never inf * 0
+                        float y[4] = {(v[r].x - off) * s, (v[r].y - off) * s, (v[r].z - off) * s,
+                                      (v[r].w - off) * s};
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) y[q] = fminf(fmaxf(y[q], -60000.f), 60000.f);
                         __align__(8) __half h[4];
                         __align__(8) __half l[4];
 #pragma unroll

@@ -3,6 +3,7 @@
 // peaks_dbscan.cu).  Used by the C ABI in api.cu.
 #pragma once
 #include <cstddef>
+#include <mutex>
 #include <string>
 #include <cuda_runtime.h>
 #include "kernels_mf.cuh"
@@ -44,6 +45,29 @@ template <class T> cudaError_t launch_stack(const T *rho, long ldr, int nt, cons
                                             int stack_abs, int outlen, T *out, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
+// Dynamic shared-memory cap of one kernel, raised on demand and never
+// lowered: objects driven from different host threads may launch the same
+// kernel with different sizes at the same time, and lowering the cap between
+// another thread's raise and its launch would fail that launch.
+struct SmemCap
+{
+    std::mutex m;
+    int cap[16] = {};
+};
+template <class K> inline cudaError_t raise_smem_cap(K kernel, size_t bytes, SmemCap &c)
+{
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(c.m);
+    int *cap = dev >= 0 && dev < 16 ? &c.cap[dev] : nullptr;
+    if (cap && (int) bytes <= *cap) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+    if (e == cudaSuccess && cap) *cap = (int) bytes;
+    return e;
+}
+
+// ---------------------------------------------------------------------------
 // grow-only device buffer
 struct DevBuf
 {
@@ -76,11 +100,15 @@ struct PeakWS
         counter, row, ht;
     long long npeaks = 0;
     long long cand_cap = 1 << 16;  // capacity of the packed candidate arrays
-    void release()
+    template <class F> void each_buf(F &&f)
     {
         DevBuf *all[] = {&counts, &offs, &slot_idx, &slot_val, &cidx, &cval, &ctr, &state, &flags,
                          &pos, &tiles, &trace_beg, &peak_off, &peaks, &counter, &row, &ht};
-        for (DevBuf *d : all) d->release();
+        for (DevBuf *d : all) f(*d);
+    }
+    void release()
+    {
+        each_buf([](DevBuf &d) { d.release(); });
         npeaks = 0;
         cand_cap = 1 << 16;
     }

@@ -13,7 +13,8 @@ template <class T, int LOG2P> struct XcorrTable
     {
         size_t bytes = smem(SD, MODE, p.S);
         auto k = xcorr_kernel<T, LOG2P, SD, MODE>;
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+        static SmemCap cap;
+        cudaError_t e = raise_smem_cap(k, bytes, cap);
         if (e != cudaSuccess) return e;
         k<<<dim3(nblocks, ngroups), kThreads, bytes, s>>>(p);
         return cudaGetLastError();
@@ -34,7 +35,8 @@ template <class T, int LOG2P> struct XcorrTable
         constexpr int P = 1 << LOG2P;
         size_t bytes = sizeof(cx<T>) * spad_size(P) + 64 * sizeof(double);
         auto k = template_spectra_kernel<T, LOG2P>;
-        cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+        static SmemCap cap;
+        cudaError_t e = raise_smem_cap(k, bytes, cap);
         if (e != cudaSuccess) return e;
         k<<<nt, kThreads, bytes, s>>>(p);
         return cudaGetLastError();
@@ -88,7 +90,8 @@ cudaError_t launch_den<MFGPU_T>(const MFGPU_T *x, long ldx, int L, MFGPU_T *den,
 {
     const size_t bytes = DenLayout<MFGPU_T>::bytes(L);
     auto k = den_kernel<MFGPU_T>;
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+    static SmemCap cap;
+    cudaError_t e = raise_smem_cap(k, bytes, cap);
     if (e != cudaSuccess) return e;
     k<<<dim3(nblocks, nch), kThreads, bytes, s>>>(x, ldx, L, den, ldd, tol);
     return cudaGetLastError();

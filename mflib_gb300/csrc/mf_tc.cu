@@ -16,7 +16,8 @@ cudaError_t launch_tc_bank(const double *tmpl, const long *toff, const int *tlen
 cudaError_t launch_tc_xcorr(const TcParams &p, int nctas, cudaStream_t s)
 {
     const size_t bytes = TcLayout::bytes(p.Kp, p.Gp);
-    cudaError_t e = cudaFuncSetAttribute(tc_xcorr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) bytes);
+    static SmemCap cap;
+    cudaError_t e = raise_smem_cap(tc_xcorr_kernel, bytes, cap);
     if (e != cudaSuccess) return e;
     tc_xcorr_kernel<<<nctas, kTcThreads, bytes, s>>>(p);
     return cudaGetLastError();

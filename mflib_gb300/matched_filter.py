@@ -279,6 +279,26 @@ class MatchedFilter:
                   int(x.strides[0] // x.itemsize))
         self._staged = (x, getattr(self, "_staged", (None, None))[0])
 
+    def set_window(self, x):
+        """Extension for a serving loop: upload a request window, the rows of
+        the 2-D array x (n_src channels x n <= signal-length samples).
+        Channel c of this object receives row c % n_src, zero-filled past n;
+        dead traces are decided over the n window samples.  Coefficients at
+        lags up to n - L_t depend on window samples only."""
+        x = np.asarray(x)
+        if x.ndim != 2:
+            raise ValueError("x must be 2-D (channels x samples)")
+        if x.dtype != self._dtype or x.strides[1] != x.itemsize or x.strides[0] % x.itemsize:
+            x = np.ascontiguousarray(x, dtype=self._dtype)
+        _lib.call("mfgpu_mf_set_window", self._h, int(x.shape[0]), int(x.shape[1]), x.ctypes.data_as(C.c_void_p),
+                  int(x.strides[0] // x.itemsize))
+
+    def device_bytes(self):
+        """Device memory held by this object (buffers and peak scratch)."""
+        v = C.c_ulonglong()
+        _lib.call("mfgpu_mf_get_device_bytes", self._h, C.byref(v))
+        return int(v.value)
+
     def zero_signal(self, it):
         _lib.call("mfgpu_mf_zero_signal", self._h, int(it))
 

@@ -129,13 +129,17 @@ def stress_case(n=400_000, nch=2, seed=3):
     return tp, chans, bounds
 
 
-@pytest.mark.parametrize("dtype", [np.float64, np.float32])
-def test_precision_stress(gpu, oracle, dtype, capsys):
+@pytest.mark.parametrize("dtype,variant", [(np.float64, 0), (np.float32, 0), (np.float32, 4)])
+def test_precision_stress(gpu, oracle, dtype, variant, capsys):
+    """Variant 0 is the planner's FFT form at these sizes; variant 4 forces
+    the split-precision tensor-core form (FP16 hi+lo operands, FP32
+    accumulation), held to the 1e-4 bound of the throughput metric."""
     mf = gpu
     tp, chans, bounds = stress_case()
     n = chans[0].size
     f = mf.MultiChannel.MatchedFilter(dtype=dtype)
-    f.initialize(_params(mf, [tp, tp], n), template_channels=[0, 1], n_channels=2)
+    f.initialize(_params(mf, [tp, tp], n), template_channels=[0, 1], n_channels=2, correlator_variant=variant)
+    assert (f.get_plan()["correlator"] == 4) == (variant == 4)
     f.set_channel_signals(np.stack([c.astype(dtype) for c in chans]))
     f.apply()
     rng = np.random.default_rng(9)
@@ -155,8 +159,8 @@ def test_precision_stress(gpu, oracle, dtype, capsys):
         if flat.any():
             worst_flat = max(worst_flat, float(err[flat].max()))
     with capsys.disabled():
-        print("\nprecision stress %s: max|drho| all lags %.3g, lags away from envelope steps %.3g"
-              % (np.dtype(dtype).name, worst_all, worst_flat))
+        print("\nprecision stress %s %s: max|drho| all lags %.3g, lags away from envelope steps %.3g"
+              % (np.dtype(dtype).name, "tensor-core" if variant == 4 else "FFT", worst_all, worst_flat))
     if dtype == np.float64:
         assert worst_all < 1e-5 and worst_flat < 1e-7
     else:
