@@ -290,7 +290,9 @@ def run_serving(args):
     rates = []
     for k, lam in enumerate(args.rates):
         reqs = make_requests(args.requests, 10 + k)
-        arr = np.cumsum(np.random.default_rng(500 + k).exponential(1.0 / lam, len(reqs)))
+        # rate 0: every request queued at once (saturation)
+        arr = (np.cumsum(np.random.default_rng(500 + k).exponential(1.0 / lam, len(reqs))) if lam > 0
+               else np.zeros(len(reqs)))
         objs = [DetectionRequest(b, x) for b, x in reqs]
         base = time.perf_counter() + 0.05
         for r, a in zip(objs, arr):
@@ -310,7 +312,7 @@ def run_serving(args):
             srv.run_one(r)
         el = time.perf_counter() - t1
         so = latency_stats(solo)
-        rates.append({"rate_req_s": lam, "requests": st["requests"], "p50_ms": 1e3 * st["p50_s"],
+        rates.append({"rate_req_s": lam if lam > 0 else "all at once", "requests": st["requests"], "p50_ms": 1e3 * st["p50_s"],
                       "p99_ms": 1e3 * st["p99_s"], "mean_ms": 1e3 * st["mean_s"], "throughput": st["throughput"],
                       "one_at_a_time": {"throughput": so["template_lags"] / el, "p50_ms": 1e3 * so["p50_s"],
                                         "p99_ms": 1e3 * so["p99_s"]}})
@@ -342,7 +344,8 @@ def main():
     ap.add_argument("--events", type=int, default=N_EVENTS,
                     help="events, i.e. templates per channel (default %d)" % N_EVENTS)
     ap.add_argument("--serving", action="store_true", help="run the request loop instead of the day-long step")
-    ap.add_argument("--rates", type=float, nargs="+", default=[50, 100, 200, 500])
+    ap.add_argument("--rates", type=float, nargs="+", default=[50, 100, 200, 500, 0],
+                    help="Poisson arrival rates in requests/s (0: all requests queued at once)")
     ap.add_argument("--requests", type=int, default=200, help="requests per arrival rate (serving)")
     ap.add_argument("--serving-slots", type=int, default=4)
     ap.add_argument("--serving-threshold", type=float, default=0.7)
