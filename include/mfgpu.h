@@ -88,7 +88,9 @@ typedef struct
        transform, 2 = whole CTA with the next spectrum prefetched by TMA,
        3 = two 128-thread teams per CTA (templates of one length only),
        4 = split-precision (FP16 hi+lo) time-domain correlation on the tensor
-       cores (FP32 data, templates of one length). */
+       cores (FP32 data, templates of one length), 5 = two teams with the
+       normalisation computed inside each CTA instead of by a separate
+       per-channel pass (templates of one length). */
     int correlator_variant;
 } mfgpu_mf_params;
 
@@ -162,7 +164,7 @@ mfgpu_status mfgpu_mf_get_device_signal(mfgpu_mf *mf, int it, const void **dptr,
 /* Overlap-save plan chosen at initialize. */
 mfgpu_status mfgpu_mf_get_plan(const mfgpu_mf *mf, int *fft_length, int *lags_per_block, int *n_blocks);
 /* Correlator organisation chosen at initialize, numbered like
- * correlator_variant (1-3 FFT organisations, 4 tensor cores); for the
+ * correlator_variant (1-3 and 5 FFT organisations, 4 tensor cores); for the
  * tensor-core path also the templates per group and the padded K, else 0.
  * Extension: the reference has one CPU correlator and no such query. */
 mfgpu_status mfgpu_mf_get_correlator(const mfgpu_mf *mf, int *variant, int *tc_group, int *tc_k);

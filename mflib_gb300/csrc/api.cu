@@ -389,15 +389,18 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
     const int hi = mf->prec == 4 ? plan_limit_hi<float>() : plan_limit_hi<double>();
     bool all_equal = minLen == maxLen;
     mf->shared_den = all_equal;
+    // mode 3 normalises inside the CTA: no per-channel rows
     auto smem_of = [&](int l2p, int mode, int S) {
-        return mf->prec == 4 ? xcorr_smem_bytes<float>(l2p, all_equal, mode, S)
-                             : xcorr_smem_bytes<double>(l2p, all_equal, mode, S);
+        const bool sd = all_equal && mode != 3;
+        return mf->prec == 4 ? xcorr_smem_bytes<float>(l2p, sd, mode, S)
+                             : xcorr_smem_bytes<double>(l2p, sd, mode, S);
     };
-    const int forced_mode = p->correlator_variant >= 1 && p->correlator_variant <= 3 ? p->correlator_variant - 1 : -1;
-    if (p->correlator_variant < 0 || p->correlator_variant > 4)
-        return fail(MFGPU_EINVAL, "correlator_variant must be 0..4");
-    if (forced_mode == 2 && !all_equal)
-        return fail(MFGPU_EINVAL, "correlator_variant 3 (teams) needs templates of one length");
+    // correlator_variant: 1..3 -> modes 0..2, 5 -> mode 3, 4 tensor cores
+    const int v = p->correlator_variant;
+    const int forced_mode = v >= 1 && v <= 3 ? v - 1 : v == 5 ? 3 : -1;
+    if (v < 0 || v > 5) return fail(MFGPU_EINVAL, "correlator_variant must be 0..5");
+    if ((forced_mode == 2 || forced_mode == 3) && !all_equal)
+        return fail(MFGPU_EINVAL, "correlator_variant " + std::to_string(v) + " (teams) needs templates of one length");
     mf->tc = p->correlator_variant == 4;
     if (mf->tc && (mf->prec != 4 || !all_equal))
         return fail(MFGPU_EINVAL, "correlator_variant 4 (tensor cores) needs FP32 data and templates of one length");
@@ -453,6 +456,7 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
         if (best_l2p < 0 || cost < best_cost) { best_l2p = l2p; best_S = S; best_cost = cost; best_mode = mode; }
     }
     mf->mode_x = best_mode;
+    if (best_mode == 3) mf->shared_den = false;
     // seconds per template-lag of the chosen FFT plan
     const double fft_cost_per_lag = best_l2p >= 0 ? best_cost / std::max(1, maxvalid) : 1e30;
     if (best_l2p < 0)
@@ -534,6 +538,7 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
         mf->ldx = std::max<long>(mf->ldx, (tl + Kp + 63) / 64 * 64);
         mf->ldx = std::max<long>(mf->ldx, ((long) mf->nden * lpc + 32L * den_tail_runs(maxLen) + 63) / 64 * 64);
     }
+    if (mf->tc) mf->shared_den = true;  // the tensor-core epilogue reads den_kernel's rows
     // work groups: split each channel's templates so the grid has enough CTAs
     int G = std::max(1, max_tpc);
     auto count_groups = [&](int gsz) {
@@ -561,7 +566,7 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
     const size_t es = mf->esz();
     const int P = 1 << mf->log2p;
     CU(mf->x.ensure(es * (size_t) nch * mf->ldx));
-    if (all_equal) CU(mf->den.ensure(es * (size_t) nch * mf->ldd));
+    if (mf->shared_den) CU(mf->den.ensure(es * (size_t) nch * mf->ldd));
     CU(cudaMemsetAsync(mf->x.p, 0, mf->x.bytes, mf->stream));
     CU(mf->rho.ensure(es * (size_t) nt * mf->ldr));
     CU(cudaMemsetAsync(mf->rho.p, 0, mf->rho.bytes, mf->stream));
@@ -667,7 +672,7 @@ mfgpu_status mfgpu_mf_get_plan(const mfgpu_mf *mf, int *fft_length, int *lags_pe
 mfgpu_status mfgpu_mf_get_correlator(const mfgpu_mf *mf, int *variant, int *tc_group, int *tc_k)
 {
     MF_CHECK_INIT(mf);
-    if (variant) *variant = mf->tc ? 4 : mf->mode_x + 1;
+    if (variant) *variant = mf->tc ? 4 : mf->mode_x == 3 ? 5 : mf->mode_x + 1;
     if (tc_group) *tc_group = mf->tc ? mf->tc_Gp : 0;
     if (tc_k) *tc_k = mf->tc ? mf->tc_Kp : 0;
     return MFGPU_OK;

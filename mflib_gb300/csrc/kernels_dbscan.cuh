@@ -71,12 +71,20 @@ static __global__ void __launch_bounds__(kDbThreads) db_core_kernel(DbParams p, 
     }
 }
 
+// Root of x with path halving: each visited node is re-pointed at its
+// grandparent.  Safe under concurrent unions: parents only ever move to an
+// ancestor (unions hook a root under a smaller root), so the write never
+// detaches a node from its component, and roots are never written here.
+// Without it the predecessor unions of the 1-D case build chains as long as
+// a component, and every find walks them.
 __device__ __forceinline__ int db_find(volatile int *parent, int x)
 {
     int p = parent[x];
     while (p != x)
     {
-        x = p;
+        const int g = parent[p];
+        if (g != p) parent[x] = g;
+        x = g;
         p = parent[x];
     }
     return x;

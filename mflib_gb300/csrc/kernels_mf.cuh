@@ -97,13 +97,26 @@ template <class T, int LOG2P> struct XcorrLayout
     static constexpr size_t tw_bytes = sizeof(cx<T>) * FftPlan<LOG2P>::post_off();  // pass twiddles only
     static constexpr size_t uv = sizeof(cx<T>) * 2 * P;
     static constexpr size_t brow = sizeof(cx<T>) * (P + 2);
-    // without SHARED_DEN the region later holds the padded demeaned segment
+    // Without SHARED_DEN (modes 0, 1) the segment's region later holds the
+    // padded demeaned segment.  With SHARED_DEN, and in mode 3, the first
+    // work buffer overlays the segment; mode 3 builds the padded copy in the
+    // second team's buffer before the forward FFT.
     static constexpr size_t padded = sizeof(T) * (N + N / 32);
-    static constexpr size_t xs_region(bool sd) { return up(sd ? (seg > fft ? seg : fft) : padded); }
+    static_assert(((sizeof(cx<T>) * spad_size(P) + 127) & ~size_t(127)) >= sizeof(T) * (N + N / 32),
+                  "a work buffer holds the padded segment");
+    static constexpr bool overlay(bool sd, int mode) { return sd || mode == 3; }
+    static constexpr bool teams(int mode) { return mode >= 2; }
+    static constexpr size_t xs_region(bool sd, int mode)
+    {
+        return up(overlay(sd, mode) ? (seg > fft ? seg : fft) : padded);
+    }
     static constexpr size_t off_xs(bool sd) { return head(sd); }
-    static constexpr size_t off_W0(bool sd) { return off_xs(sd) + (sd ? 0 : xs_region(sd)); }
-    static constexpr size_t off_W1(bool sd) { return off_xs(sd) + xs_region(sd) + (sd ? 0 : up(fft)); }
-    static constexpr size_t off_UV(bool sd, int mode) { return off_W1(sd) + (mode == 2 ? up(fft) : 0); }
+    static constexpr size_t off_W0(bool sd, int mode) { return off_xs(sd) + (overlay(sd, mode) ? 0 : xs_region(sd, mode)); }
+    static constexpr size_t off_W1(bool sd, int mode)
+    {
+        return off_xs(sd) + xs_region(sd, mode) + (overlay(sd, mode) ? 0 : up(fft));
+    }
+    static constexpr size_t off_UV(bool sd, int mode) { return off_W1(sd, mode) + (teams(mode) ? up(fft) : 0); }
     static constexpr size_t off_tw(bool sd, int mode) { return off_UV(sd, mode) + up(uv); }
     static constexpr size_t off_B(bool sd, int mode) { return off_tw(sd, mode) + up(tw_bytes); }
     static constexpr size_t off_invd(bool sd, int mode) { return off_B(sd, mode) + (mode == 1 ? 2 * up(brow) : 0); }
@@ -116,7 +129,7 @@ template <class T, int LOG2P> struct XcorrLayout
     }
     static size_t bytes(bool sd, int mode, int S)
     {
-        return off_M(sd, mode, S) + sizeof(unsigned) * 2 * (mode == 2 ? 2 : 1) * mask_words;
+        return off_M(sd, mode, S) + sizeof(unsigned) * 2 * (teams(mode) ? 2 : 1) * mask_words;
     }
 };
 
@@ -429,7 +442,8 @@ __device__ __forceinline__ void seg_chunk_prefix(SegStats<T> st, int tid)
 
 // Rewrites the staged segment (free once the forward FFT has read it) as
 // y = x - m with one pad word per 32 samples, for conflict-free strided
-// reads by seg_inv_den.  The padded copy fits the segment's region.
+// reads by seg_inv_den.  The padded copy (st.yp) fits the segment's region
+// or one FFT work buffer.
 template <class T, int N>
 __device__ __forceinline__ void seg_make_padded(SegStats<T> st, int tid)
 {
@@ -601,7 +615,11 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
     using LY = XcorrLayout<T, LOG2P>;
     using PL = FftPlan<LOG2P>;
     constexpr bool PREFETCH = MODE == 1;
-    constexpr bool TEAMS = MODE == 2;
+    constexpr bool TEAMS = MODE >= 2;
+    // mode 3: two teams, one template length, normalisation computed in the
+    // CTA (once, before the forward FFT) instead of read from den_kernel
+    constexpr bool OWN_DEN = MODE == 3;
+    static_assert(!(OWN_DEN && SHARED_DEN), "mode 3 computes its own normalisation");
     constexpr int P = LY::P, N = LY::N, NCH = LY::NCH;
     const int tid = threadIdx.x;
     const int g = blockIdx.y;
@@ -632,8 +650,8 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
     acc *c1 = reinterpret_cast<acc *>(smem_x + 64 + 32 * sizeof(T));  // only without SHARED_DEN
     acc *c2 = c1 + (NCH + 1);
     T *xs = reinterpret_cast<T *>(smem_x + LY::off_xs(SHARED_DEN));
-    cx<T> *W0 = reinterpret_cast<cx<T> *>(smem_x + LY::off_W0(SHARED_DEN));
-    cx<T> *W1 = reinterpret_cast<cx<T> *>(smem_x + LY::off_W1(SHARED_DEN));
+    cx<T> *W0 = reinterpret_cast<cx<T> *>(smem_x + LY::off_W0(SHARED_DEN, MODE));
+    cx<T> *W1 = reinterpret_cast<cx<T> *>(smem_x + LY::off_W1(SHARED_DEN, MODE));
     cx<T> *UV = reinterpret_cast<cx<T> *>(smem_x + LY::off_UV(SHARED_DEN, MODE));
     cx<T> *tws = reinterpret_cast<cx<T> *>(smem_x + LY::off_tw(SHARED_DEN, MODE));
     cx<T> *Bs0 = reinterpret_cast<cx<T> *>(smem_x + LY::off_B(SHARED_DEN, MODE));
@@ -680,6 +698,14 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
     st.p2 = st.p1 + NCH;
     int Lcur = p.tlen[p.tids[t_begin]];
     if constexpr (!SHARED_DEN) seg_chunk_prefix<T, N>(st, tid);
+    if constexpr (OWN_DEN)
+    {
+        // the second team's buffer is free until the teams start: padded
+        // demeaned copy there, then the CTA's one normalisation row
+        st.yp = reinterpret_cast<T *>(W1);
+        seg_make_padded<T, N>(st, tid);
+        seg_inv_den<T, N>(st, Lcur, S, p.tol, invd_s, tid);
+    }
 
     // ---- forward real FFT of (x - m), read straight from the staged segment
     //      (with SHARED_DEN the work buffer overlays the segment)
@@ -690,7 +716,8 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
             return cmk(v.x - m, v.y - m);
         };
         auto stb = [&](int e, cx<T> v) { W[spad(e)] = v; };
-        fft_run<T, LOG2P, kThreads, false, true, decltype(ld), decltype(stb), SHARED_DEN>(W, tws, tid, ld, stb);
+        fft_run<T, LOG2P, kThreads, false, true, decltype(ld), decltype(stb), SHARED_DEN || OWN_DEN>(W, tws, tid, ld,
+                                                                                                       stb);
         __syncthreads();
         // Real-FFT post-processing to X[k], k = 0..P, then the per-bin pairs
         //   U[e] = X[e] (1 + i wc_e),  V[e] = conj(X[P-e]) (1 - i wc_e),
@@ -727,7 +754,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
         }
         __syncthreads();
     }
-    if constexpr (!SHARED_DEN)
+    if constexpr (!SHARED_DEN && !OWN_DEN)
     {
         // the segment's region is free now: padded demeaned copy, then the
         // first template length's normalisation
@@ -1025,28 +1052,42 @@ __global__ void __launch_bounds__(kThreads) den_kernel(const T *x, long ldx, int
     acc *wsum = Q2 + nruns;
     T *red = reinterpret_cast<T *>(wsum + 64);
 
-    // ---- stage 32 * nruns samples (16-byte loads; k0 and ldx are multiples of 32)
+    // ---- stage 32 * nruns samples (16-byte loads; k0 and ldx are multiples
+    //      of 32), eight loads in flight per thread before the first use
     const T *xr = x + (long) c * ldx + k0;
-    constexpr int VW = 16 / sizeof(T);
+    constexpr int VW = 16 / sizeof(T), NB = 8;
+    const int nvec = nruns * kDenRun / VW;
     MeanAcc<T> macc;
-    for (int i = tid; i < nruns * kDenRun / VW; i += kThreads)
+    for (int i0 = tid; i0 < nvec; i0 += kThreads * NB)
     {
-        T v[VW];
-        if constexpr (sizeof(T) == 4)
+        T v[NB][VW];
+#pragma unroll
+        for (int b = 0; b < NB; ++b)
         {
-            const float4 a = reinterpret_cast<const float4 *>(xr)[i];
-            v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-        }
-        else
-        {
-            const double2 a = reinterpret_cast<const double2 *>(xr)[i];
-            v[0] = a.x; v[1] = a.y;
+            const int i = i0 + b * kThreads;
+            if (i >= nvec) break;
+            if constexpr (sizeof(T) == 4)
+            {
+                const float4 a = reinterpret_cast<const float4 *>(xr)[i];
+                v[b][0] = a.x; v[b][1] = a.y; v[b][2] = a.z; v[b][3] = a.w;
+            }
+            else
+            {
+                const double2 a = reinterpret_cast<const double2 *>(xr)[i];
+                v[b][0] = a.x; v[b][1] = a.y;
+            }
         }
 #pragma unroll
-        for (int q = 0; q < VW; ++q)
+        for (int b = 0; b < NB; ++b)
         {
-            y[den_pad(VW * i + q)] = v[q];
-            macc.add(v[q]);
+            const int i = i0 + b * kThreads;
+            if (i >= nvec) break;
+#pragma unroll
+            for (int q = 0; q < VW; ++q)
+            {
+                y[den_pad(VW * i + q)] = v[b][q];
+                macc.add(v[b][q]);
+            }
         }
     }
     const T m = block_mean<T>(macc, red, nruns * kDenRun);

@@ -324,8 +324,11 @@ static __global__ void peak_seam_kernel(PeakTraces<T> tr, int ntr, FusedSlots<T>
 
 // Packs chunk b of a trace in index order: first lag, body (slot entries
 // ranked by index, or a re-scan of the stored trace when more than kPkCap
-// body lags passed), last lag.  One warp per chunk (most chunks are empty).
+// body lags passed), last lag.  One warp per 32 consecutive chunks of a
+// trace: the lanes read the 32 counts, and the warp packs the non-empty
+// chunks one after another (most chunks are empty).
 static_assert(kPkCap == 32, "peak_gather_fused_kernel ranks one slot entry per lane");
+constexpr int kPkGatherSpan = 32;  // chunks per warp
 
 template <class T>
 static __global__ void __launch_bounds__(kPkThreads)
@@ -333,18 +336,12 @@ static __global__ void __launch_bounds__(kPkThreads)
                              const long long *offs, int *cidx, T *cval, int *ctr, long long cap, int *overflow)
 {
     const int lane = threadIdx.x & 31;
-    const int trace = blockIdx.y, b = blockIdx.x * (kPkThreads / 32) + (threadIdx.x >> 5);
-    if (b >= fs.nblk) return;
-    const long slot = (long) trace * fs.nblk + b;
-    const int cnt = counts[slot];
-    if (cnt == 0) return;
-    const long long off = offs[slot];
-    if (lane == 0 && off + cnt > cap) *overflow = 1;
+    const int trace = blockIdx.y;
+    const int b0 = (blockIdx.x * (kPkThreads / 32) + (threadIdx.x >> 5)) * kPkGatherSpan;
+    if (b0 >= fs.nblk) return;
     const int row = tr.row[trace];
     const T *x = tr.x + (long) row * tr.ldx;
     const long n = tr.len;
-    const int hv = ht[slot];
-    const long i0 = (long) b * fs.S;
     auto put = [&](long long o, long i, T v) {
         if (o < cap)
         {
@@ -353,55 +350,70 @@ static __global__ void __launch_bounds__(kPkThreads)
             ctr[o] = trace;
         }
     };
-    if (lane == 0)
+    const int bl = b0 + lane;
+    const int cnt_l = bl < fs.nblk ? counts[(long) trace * fs.nblk + bl] : 0;
+    unsigned todo = __ballot_sync(0xffffffffu, cnt_l != 0);
+    while (todo)
     {
-        if (hv & 1) put(off, i0, x[i0]);
-        if (hv & 2) put(off + cnt - 1, i0 + fs.S - 1, x[i0 + fs.S - 1]);
-    }
-    const long long boff = off + (hv & 1);
-    const long bs = (long) row * fs.nblk + b;
-    const int bc = fs.cnt[bs];
-    if (bc <= kPkCap)
-    {
-        // kPkCap == 32: one entry per lane, ranked by index
-        const int *si = fs.idx + bs * kPkCap;
-        if (lane < bc)
+        const int q = __ffs(todo) - 1;  // warp-uniform
+        todo &= todo - 1;
+        const int b = b0 + q;
+        const int cnt = __shfl_sync(0xffffffffu, cnt_l, q);
+        const long slot = (long) trace * fs.nblk + b;
+        const long long off = offs[slot];
+        if (lane == 0 && off + cnt > cap) *overflow = 1;
+        const int hv = ht[slot];
+        const long i0 = (long) b * fs.S;
+        if (lane == 0)
         {
-            const int ir = si[lane];
-            int rank = 0;
-            for (int q = 0; q < bc; ++q) rank += si[q] < ir ? 1 : 0;
-            put(boff + rank, ir, fs.val[bs * kPkCap + lane]);
+            if (hv & 1) put(off, i0, x[i0]);
+            if (hv & 2) put(off + cnt - 1, i0 + fs.S - 1, x[i0 + fs.S - 1]);
         }
-        return;
-    }
-    const long lo = i0 + 1, hi = (i0 + fs.S - 1 < n) ? i0 + fs.S - 1 : n;
-    long long base = boff;
-    for (long c0 = lo; c0 < hi; c0 += 32 * kPkPer)
-    {
-        const long a = c0 + (long) lane * kPkPer;
-        unsigned mask = 0;
+        const long long boff = off + (hv & 1);
+        const long bs = (long) row * fs.nblk + b;
+        const int bc = fs.cnt[bs];
+        if (bc <= kPkCap)
+        {
+            // kPkCap == 32: one entry per lane, ranked by index
+            const int *si = fs.idx + bs * kPkCap;
+            if (lane < bc)
+            {
+                const int ir = si[lane];
+                int rank = 0;
+                for (int r = 0; r < bc; ++r) rank += si[r] < ir ? 1 : 0;
+                put(boff + rank, ir, fs.val[bs * kPkCap + lane]);
+            }
+            continue;
+        }
+        const long lo = i0 + 1, hi = (i0 + fs.S - 1 < n) ? i0 + fs.S - 1 : n;
+        long long base = boff;
+        for (long c0 = lo; c0 < hi; c0 += 32 * kPkPer)
+        {
+            const long a = c0 + (long) lane * kPkPer;
+            unsigned mask = 0;
 #pragma unroll 4
-        for (int q = 0; q < kPkPer; ++q)
-            if (a + q < hi && cand_rule<T>(x[a + q - 1], x[a + q], a + q + 1 < n ? x[a + q + 1] : (T) 0, a + q, n,
-                                           tr.thr))
-                mask |= 1u << q;
-        const int c = __popc(mask);
-        int incl = c;
+            for (int r = 0; r < kPkPer; ++r)
+                if (a + r < hi && cand_rule<T>(x[a + r - 1], x[a + r], a + r + 1 < n ? x[a + r + 1] : (T) 0, a + r, n,
+                                               tr.thr))
+                    mask |= 1u << r;
+            const int c = __popc(mask);
+            int incl = c;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1)
-        {
-            const int y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += y;
+            for (int o = 1; o < 32; o <<= 1)
+            {
+                const int y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            long long r = base + incl - c;
+            while (mask)
+            {
+                const int qq = __ffs(mask) - 1;
+                mask &= mask - 1;
+                put(r, a + qq, x[a + qq]);
+                ++r;
+            }
+            base += __shfl_sync(0xffffffffu, incl, 31);
         }
-        long long r = base + incl - c;
-        while (mask)
-        {
-            const int q = __ffs(mask) - 1;
-            mask &= mask - 1;
-            put(r, a + q, x[a + q]);
-            ++r;
-        }
-        base += __shfl_sync(0xffffffffu, incl, 31);
     }
 }
 

@@ -17,7 +17,9 @@ template <class T> struct fft_limits;
 template <> struct fft_limits<float> { static constexpr int lo = 5, hi = 12; };   // N = 64 .. 8192
 template <> struct fft_limits<double> { static constexpr int lo = 5, hi = 11; };  // N = 64 .. 4096
 
-// mode: 0 whole CTA, 1 whole CTA + spectrum prefetch, 2 two teams (shared length only)
+// mode: 0 whole CTA, 1 whole CTA + spectrum prefetch, 2 two teams (shared
+// length, normalisation rows from den_kernel), 3 two teams (shared length,
+// normalisation computed in the CTA; shared_den false)
 template <class T> size_t xcorr_smem_bytes(int log2p, bool shared_den, int mode, int S);
 template <class T> cudaError_t launch_xcorr(int log2p, bool shared_den, int mode, const XcorrParams<T> &p,
                                             int nblocks, int ngroups, cudaStream_t s);

@@ -19,15 +19,19 @@ template <class T, int LOG2P> struct XcorrTable
         k<<<dim3(nblocks, ngroups), kThreads, bytes, s>>>(p);
         return cudaGetLastError();
     }
-    // MODE 2 (teams) exists only for a shared template length
+    // MODE 2 (teams) exists only for a shared template length with its
+    // normalisation rows precomputed, MODE 3 only for a shared length
+    // normalised inside the CTA
     static cudaError_t launch(bool sd, int mode, const XcorrParams<T> &p, int nblocks, int ngroups, cudaStream_t s)
     {
         if (sd)
         {
+            if (mode == 3) return cudaErrorInvalidValue;
             if (mode == 2) return go<true, 2>(p, nblocks, ngroups, s);
             return mode == 1 ? go<true, 1>(p, nblocks, ngroups, s) : go<true, 0>(p, nblocks, ngroups, s);
         }
         if (mode == 2) return cudaErrorInvalidValue;
+        if (mode == 3) return go<false, 3>(p, nblocks, ngroups, s);
         return mode == 1 ? go<false, 1>(p, nblocks, ngroups, s) : go<false, 0>(p, nblocks, ngroups, s);
     }
     static cudaError_t spectra(const SpecParams<T> &p, int nt, cudaStream_t s)

@@ -94,8 +94,10 @@ int run_peaks(const T *x, long ldx, const int *host_rows, int ntr, int len, doub
         peak_trace_beg_kernel<<<(ntr + 1 + 127) / 128, 128, 0, s>>>(ntr, nchunks, ws.offs.as<long long>(), cap,
                                                                     ws.trace_beg.as<long long>());
         if (fused)
-            peak_gather_fused_kernel<T><<<dim3((nchunks + kPkThreads / 32 - 1) / (kPkThreads / 32), ntr), kPkThreads,
-                                          0, s>>>(
+            peak_gather_fused_kernel<T><<<dim3((nchunks + kPkThreads / 32 * kPkGatherSpan - 1) /
+                                                   (kPkThreads / 32 * kPkGatherSpan),
+                                               ntr),
+                                          kPkThreads, 0, s>>>(
                 tr, *fused, ws.counts.as<int>(), ws.ht.as<unsigned char>(), ws.offs.as<long long>(), ws.cidx.as<int>(),
                 ws.cval.as<T>(), ws.ctr.as<int>(), cap, overflow);
         else

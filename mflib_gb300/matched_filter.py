@@ -174,7 +174,8 @@ class MatchedFilter:
         ``correlator_variant`` forces the correlator organisation (0 automatic,
         1 whole CTA, 2 whole CTA with spectrum prefetch, 3 two teams per CTA,
         templates of one length only; 4 split-precision tensor-core
-        correlation, FP32 and templates of one length)."""
+        correlation, FP32 and templates of one length; 5 two teams with the
+        normalisation computed inside each CTA, templates of one length)."""
         if not isinstance(params, MatchedFilterParameters) or not params.is_valid():
             raise ValueError("Parameters are invalid")
         tmpls = [params.get_template(i) for i in range(params.get_number_of_templates())]
@@ -363,7 +364,7 @@ class MatchedFilter:
     # -- extensions ---------------------------------------------------------
     def get_plan(self):
         """The plan chosen at initialize: FFT length, lags per block, blocks,
-        and the correlator (1-3 FFT organisations, 4 tensor cores; for the
+        and the correlator (1-3, 5 FFT organisations, 4 tensor cores; for the
         latter also the templates per group and the padded K)."""
         a, b, c = C.c_int(), C.c_int(), C.c_int()
         _lib.call("mfgpu_mf_get_plan", self._h, C.byref(a), C.byref(b), C.byref(c))

@@ -212,7 +212,7 @@ def _filter(mf, p, chans, assign, dtype, **kw):
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
-@pytest.mark.parametrize("variant", [1, 2, 3])
+@pytest.mark.parametrize("variant", [1, 2, 3, 5])
 @pytest.mark.parametrize("fft_length", [256, 1024, 4096])
 def test_fused_peak_candidates(gpu, oracle, rng, dtype, variant, fft_length):
     """Candidates gathered inside the correlator give exactly the peaks of

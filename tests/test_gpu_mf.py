@@ -222,12 +222,13 @@ def test_forced_fft_lengths(gpu, oracle, rng, fft_length):
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
-@pytest.mark.parametrize("variant", [1, 2, 3])
+@pytest.mark.parametrize("variant", [1, 2, 3, 5])
 @pytest.mark.parametrize("fft_length", [0, 256, 2048, 4096])
 @pytest.mark.parametrize("ntpl", [1, 2, 5])
 def test_correlator_variants(gpu, oracle, rng, dtype, variant, fft_length, ntpl):
     """Every correlator organisation (whole CTA, whole CTA with the next
-    spectrum prefetched, two teams of 128 threads) gives the oracle's
+    spectrum prefetched, two teams of 128 threads reading precomputed
+    normalisation rows or normalising inside the CTA) gives the oracle's
     coefficients; 5 templates on one channel leave one team a template
     short in the last round."""
     mf = gpu
@@ -243,6 +244,7 @@ def test_correlator_variants(gpu, oracle, rng, dtype, variant, fft_length, ntpl)
     f.initialize(p, template_channels=assign, n_channels=2, fft_length=fft_length, correlator_variant=variant)
     if fft_length:
         assert f.get_plan()["fft_length"] == fft_length
+    assert f.get_plan()["correlator"] == variant
     for c, s in enumerate(chans):
         f.set_channel_signal(c, s.astype(dtype))
     f.apply()
@@ -263,7 +265,11 @@ def test_correlator_variant_errors(gpu, rng):
     with pytest.raises(ValueError):
         f.initialize(p, correlator_variant=3)  # teams need one template length
     with pytest.raises(ValueError):
+        f.initialize(p, correlator_variant=5)
+    with pytest.raises(ValueError):
         f.initialize(p, correlator_variant=4)
+    with pytest.raises(ValueError):
+        f.initialize(p, correlator_variant=6)
     f.initialize(p, correlator_variant=2)
     assert f.is_initialized()
 
@@ -434,11 +440,13 @@ def test_batched_channel_upload(gpu, rng):
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 @pytest.mark.parametrize("L", [32, 33, 95, 511, 1024, 4097, 6000])
-def test_shared_length_normalisation(gpu, oracle, rng, dtype, L):
-    """Templates of one length use the per-channel normalisation kernel:
-    window lengths with L mod 32 = 0, 1, 31 and lengths that need two or
-    three 32-sample runs per thread; the signals carry an offset and a slow
-    drift of several standard deviations."""
+@pytest.mark.parametrize("variant", [0, 5])
+def test_shared_length_normalisation(gpu, oracle, rng, dtype, L, variant):
+    """Templates of one length: the planner's choice (variant 0) or the
+    in-CTA normalisation (variant 5), for window lengths
+    with L mod 32 = 0, 1, 31 and lengths that need two or three 32-sample
+    runs per thread; the signals carry an offset and a slow drift of several
+    standard deviations."""
     mf = gpu
     if dtype == np.float64 and L > 4065:
         pytest.skip("the FP64 correlator's longest template is 4065 samples (N = 4096)")
@@ -449,7 +457,7 @@ def test_shared_length_normalisation(gpu, oracle, rng, dtype, L):
     tps = [rng.standard_normal(L) for _ in assign]
     p = _params(mf, tps, n)
     f = mf.MultiChannel.MatchedFilter(dtype=dtype)
-    f.initialize(p, template_channels=assign, n_channels=2)
+    f.initialize(p, template_channels=assign, n_channels=2, correlator_variant=variant)
     for c, s in enumerate(chans):
         f.set_channel_signal(c, s.astype(dtype))
     f.apply()
