@@ -491,11 +491,11 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
     if (tc_candidate)
     {
         // Hankel GEMM plan: K = L + 7 (8 phases) padded to 16; as many
-        // templates per group (even, MMA N = 8 per template) as fit the
-        // shared memory left beside the strips
+        // templates per group (even, at most 16: the wide MMA has N = 16 per
+        // template, at most 256) as fit the shared memory beside the strips
         const int Kp = (maxLen + 7 + 15) / 16 * 16;
         const long room = (long) dev_smem - (long) tc_smem_bytes(Kp, 0);
-        const int gmax = (int) std::min<long>(32, room / (32L * Kp)) & ~1;
+        const int gmax = (int) std::min<long>(16, room / (32L * Kp)) & ~1;
         if (gmax < 2 && mf->tc)
             return fail(MFGPU_EINVAL, "template length " + std::to_string(maxLen) +
                                           " is too long for the tensor-core correlator");
@@ -512,7 +512,7 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
     {
         const int Kp = (maxLen + 7 + 15) / 16 * 16;
         const long room = (long) dev_smem - (long) tc_smem_bytes(Kp, 0);
-        const int gmax = (int) std::min<long>(32, room / (32L * Kp)) & ~1;
+        const int gmax = (int) std::min<long>(16, room / (32L * Kp)) & ~1;
         const int ngc = (max_tpc + gmax - 1) / gmax;
         const int Gp = std::min(gmax, ((max_tpc + ngc - 1) / ngc + 1) & ~1);
         for (int c = 0; c < nch; ++c)
@@ -526,8 +526,8 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
         mf->tc_Gp = Gp;
         mf->tc_groups = (int) tc_gch.size();
         mf->tc_tiles = (std::max(1, maxvalid) + kTcLags - 1) / kTcLags;
-        int cols = 32;
-        while (cols < 16 * Gp) cols *= 2;
+        int cols = 32;  // two accumulators of 16 Gp columns each
+        while (cols < 32 * Gp) cols *= 2;
         mf->tc_cols = cols;
         CU(cudaDeviceGetAttribute(&mf->n_sm, cudaDevAttrMultiProcessorCount, mf->dev));
         // strips read tiles * 1024 + Kp samples; the normalisation row covers every tile

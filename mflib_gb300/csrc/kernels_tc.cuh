@@ -2,7 +2,11 @@
 // templates of one length: the Pearson numerators as a Hankel GEMM on the
 // 5th-generation tensor cores (tcgen05.mma kind::f16, FP32 accumulators in
 // tensor memory), with FP16 hi+lo operand splits (hi*hi + hi*lo + lo*hi)
-// that restore about 22 bits of operand precision.
+// that restore about 22 bits of operand precision.  Two MMAs per 16-deep K
+// step: A_hi against [B_hi; B_lo] (N = 16 Gp: the hi*hi and hi*lo products
+// land in two column halves) and A_lo against B_hi into the first half, so
+// the A operand is fetched from shared memory twice per step, not three
+// times; the epilogue adds the two halves.
 //
 // Tile = 128 rows x 8 phases = 1024 consecutive lags of one channel against
 // a group of Gp templates.  Row i, phase f is lag k0 + 8i + f:
@@ -16,7 +20,7 @@
 // of two before the split; templates are scaled by a power of two too.
 //
 // Persistent, warp-specialised CTA (one per SM):
-//   warp 0 lane 0   issues the MMAs (K/16 steps x 3) and the commits;
+//   warp 0 lane 0   issues the MMAs (K/16 steps x 2) and the commits;
 //   warps 1-3       stage strips: FP32 load, offset, scale, hi/lo split;
 //   warps 4-11      epilogue, two warpgroups taking alternate templates:
 //                   tcgen05.ld of the accumulator rows (the buffer is
@@ -169,12 +173,15 @@ static __global__ void __launch_bounds__(kTcThreads, 1) tc_xcorr_kernel(TcParams
     {
         if (lane == 0)
         {
-            // ---- MMA issue.  Instruction descriptor: D f32, A/B f16, both
-            //      K-major, N >> 3, M >> 4
-            const uint32_t idesc = (1u << 4) | ((uint32_t) (N >> 3) << 17) | ((uint32_t) (kTcRows >> 4) << 24);
+            // ---- MMA issue.  Instruction descriptors: D f32, A/B f16, both
+            //      K-major, N >> 3, M >> 4; N = 16 Gp (hi and lo rows of B)
+            //      and N = 8 Gp (hi rows only)
+            const uint32_t idesc_w = (1u << 4) | ((uint32_t) (2 * N >> 3) << 17) | ((uint32_t) (kTcRows >> 4) << 24);
+            const uint32_t idesc_n = (1u << 4) | ((uint32_t) (N >> 3) << 17) | ((uint32_t) (kTcRows >> 4) << 24);
             const uint32_t bbytes = (uint32_t) TcLayout::b_bytes(Kp, Gp);
             const uint32_t sA0 = smem_u32(sA), sB0 = smem_u32(sB);
-            const uint32_t b_lo = (uint32_t) (16 * Gp * Kp);  // bytes from hi to lo
+            // the lo rows follow the hi rows at the same row-group stride, so
+            // one descriptor spans [B_hi; B_lo]
             const uint32_t sbo_b = (uint32_t) (Kp / 8) * 128;
             int cur = -1;
             uint32_t bph = 0;
@@ -204,16 +211,14 @@ static __global__ void __launch_bounds__(kTcThreads, 1) tc_xcorr_kernel(TcParams
                 if (ok && n >= 2) ok = mbar_wait_bounded(&acc_empty[buf], (uint32_t) (((n - 2) >> 1) & 1));
                 if (!ok) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                const uint32_t d = tmem + (uint32_t) (buf * N);
+                const uint32_t d = tmem + (uint32_t) (buf * 2 * N);
                 const uint32_t ahi = sA0 + (uint32_t) (2 * buf) * SA * 2, alo = ahi + (uint32_t) SA * 2;
                 for (int kk = 0; kk < Kp / 16; ++kk)
                 {
                     const uint64_t dAh = tc_desc(ahi + kk * 32, 16, 128), dAl = tc_desc(alo + kk * 32, 16, 128);
-                    const uint64_t dBh = tc_desc(sB0 + kk * 256, 128, sbo_b),
-                                   dBl = tc_desc(sB0 + b_lo + kk * 256, 128, sbo_b);
-                    tc_mma(d, dAh, dBh, idesc, kk > 0 ? 1u : 0u);
-                    tc_mma(d, dAh, dBl, idesc, 1u);
-                    tc_mma(d, dAl, dBh, idesc, 1u);
+                    const uint64_t dB = tc_desc(sB0 + kk * 256, 128, sbo_b);
+                    tc_mma(d, dAh, dB, idesc_w, kk > 0 ? 1u : 0u);  // [hi*hi | hi*lo]
+                    tc_mma(d, dAl, dB, idesc_n, 1u);                 // + lo*hi into the first half
                 }
                 tc_commit(&a_empty[buf]);
                 tc_commit(&acc_full[buf]);
@@ -290,7 +295,7 @@ static __global__ void __launch_bounds__(kTcThreads, 1) tc_xcorr_kernel(TcParams
         // ---- epilogue: row i of the tile = TMEM lane i; warpgroup eg takes
         //      templates eg, eg + 2, ...
         const int q = warp & 3, i = 32 * q + lane, eg = (warp - 4) >> 2;
-        constexpr int TB = 4;  // templates per batch of TMEM loads
+        constexpr int TB = 2;  // templates per batch of TMEM loads (two halves each)
         float dv[8];
         auto load_den = [&](long w) {
             const int c = p.grp_chan[(int) (w / p.tiles)];
@@ -322,18 +327,22 @@ static __global__ void __launch_bounds__(kTcThreads, 1) tc_xcorr_kernel(TcParams
             bool released = false;
             for (int b0 = 0; b0 < nmine; b0 += TB)
             {
-                uint32_t r[TB][8];
+                uint32_t r[TB][8], h[TB][8];
 #pragma unroll
                 for (int u = 0; u < TB; ++u)
                 {
                     if (b0 + u < nmine)  // uniform across the warp
                     {
                         const int t = eg + 2 * (b0 + u);
-                        const uint32_t taddr = tmem + ((uint32_t) (32 * q) << 16) + (uint32_t) (buf * N + 8 * t);
+                        const uint32_t taddr = tmem + ((uint32_t) (32 * q) << 16) + (uint32_t) (buf * 2 * N + 8 * t);
                         asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                                      : "=r"(r[u][0]), "=r"(r[u][1]), "=r"(r[u][2]), "=r"(r[u][3]), "=r"(r[u][4]),
                                        "=r"(r[u][5]), "=r"(r[u][6]), "=r"(r[u][7])
                                      : "r"(taddr));
+                        asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                                     : "=r"(h[u][0]), "=r"(h[u][1]), "=r"(h[u][2]), "=r"(h[u][3]), "=r"(h[u][4]),
+                                       "=r"(h[u][5]), "=r"(h[u][6]), "=r"(h[u][7])
+                                     : "r"(taddr + (uint32_t) N));
                     }
                 }
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
@@ -359,7 +368,8 @@ static __global__ void __launch_bounds__(kTcThreads, 1) tc_xcorr_kernel(TcParams
                     float o[8];
 #pragma unroll
                     for (int f = 0; f < 8; ++f)
-                        o[f] = dead ? 0.f : clamp_rho(__uint_as_float(r[u][f]) * sc * dcur[f]);
+                        o[f] = dead ? 0.f
+                                    : clamp_rho((__uint_as_float(r[u][f]) + __uint_as_float(h[u][f])) * sc * dcur[f]);
                     float *dst = p.rho + (long) tt * p.ldr + lag0;
                     if (lag0 + 7 < p.nv)
                     {
