@@ -148,6 +148,8 @@ struct mfgpu_mf
     double pk_fused_thr = 0;
     int pk_fused_len = 0;
     DevBuf pk_cnt, pk_idx, pk_val;
+    DevBuf pk_flags;   // tensor-core correlator: candidate flags per 64 lags
+    int pk_words = 0;
     long long launches = 0;
     float last_xcorr_ms = 0, last_apply_ms = 0;
 
@@ -157,7 +159,7 @@ struct mfgpu_mf
         DevBuf *all[] = {&x,      &rho,      &Bc,   &tw,  &grp_chan, &grp_tb, &grp_te, &tids,      &tlen_d,
                          &nvalid_d, &dead,   &err,  &tmpl_d, &toff_d, &pmin, &pmax,  &chan_list, &stackbuf,
                          &shifts_d, &weights_d, &specbuf, &den, &pk_cnt, &pk_idx, &pk_val, &xstage,
-                         &xrange,   &tc_B,   &tc_bscale, &tc_grp_chan, &tc_grp_tid};
+                         &xrange,   &tc_B,   &tc_bscale, &tc_grp_chan, &tc_grp_tid, &pk_flags};
         for (DevBuf *d : all) f(*d);
         pk.each_buf(f);
     }
@@ -502,11 +504,12 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
         // balanced groups: the busiest channel splits into ngc equal groups
         const int ngc = gmax >= 2 ? (max_tpc + gmax - 1) / gmax : 1;
         const int Gp = gmax >= 2 ? std::min(gmax, ((max_tpc + ngc - 1) / ngc + 1) & ~1) : 2;
-        // automatic choice: seconds per template-lag measured on GB300, about
-        // 4.6e-15 per padded template sample plus 6.6e-12 per tile row shared
-        // by the Gp templates of a group, against the FFT plan's estimate
+        // automatic choice: seconds per template-lag measured on GB300 (two
+        // MMAs per K step), about 3.6e-15 per padded template sample plus
+        // 5.7e-12 per tile row shared by the Gp templates of a group, against
+        // the FFT plan's estimate
         if (!mf->tc && gmax >= 2)
-            mf->tc = 4.6e-15 * Kp + 6.6e-12 / Gp < 0.9 * fft_cost_per_lag;
+            mf->tc = 3.6e-15 * Kp + 5.7e-12 / Gp < 0.9 * fft_cost_per_lag;
     }
     if (mf->tc)
     {
@@ -952,9 +955,27 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
             q.rho = mf->rho.as<float>(); q.ldr = mf->ldr;
             q.nv = mf->maxvalid; q.Kp = mf->tc_Kp; q.Gp = mf->tc_Gp; q.tmem_cols = mf->tc_cols;
             q.ngroups = mf->tc_groups; q.tiles = mf->tc_tiles; q.err = mf->err.as<int>();
+            q.pk_flags = nullptr; q.pk_words = 0; q.pk_thr = 0.f;
+            if (mf->pk_req >= 0)
+            {
+                // candidate flags: one bit per 64 lags, cleared per apply
+                q.pk_words = (mf->tc_tiles * (kTcLags / 64) + 31) / 32;
+                const size_t fb = sizeof(unsigned) * (size_t) mf->nt * q.pk_words;
+                CU(mf->pk_flags.ensure(fb));
+                CU(cudaMemsetAsync(mf->pk_flags.p, 0, fb, mf->stream));
+                q.pk_flags = mf->pk_flags.as<unsigned>();
+                q.pk_thr = (float) mf->pk_req;
+            }
             const long work = (long) q.ngroups * q.tiles;
             CU(launch_tc_xcorr(q, (int) std::min<long>(mf->n_sm, work), mf->stream));
             ++mf->launches;
+            if (q.pk_flags)
+            {
+                mf->pk_fused = true;
+                mf->pk_fused_thr = mf->pk_req;
+                mf->pk_fused_len = mf->n - mf->maxLen + 1;
+                mf->pk_words = q.pk_words;
+            }
             return MFGPU_OK;
         }
     }
@@ -1171,12 +1192,17 @@ mfgpu_status mfgpu_mf_find_peaks(mfgpu_mf *mf, double threshold, int min_distanc
     mf->pk_off.assign(mf->nt + 1, 0);
     std::string err;
     // candidates of the last apply when it gathered them for this threshold and length
-    const bool fused = mf->pk_fused && threshold == mf->pk_fused_thr && len == mf->pk_fused_len;
+    const bool match = mf->pk_fused && threshold == mf->pk_fused_thr && len <= mf->pk_fused_len;
+    // the FFT correlator gathered the candidates (same trace length); the
+    // tensor-core correlator flagged the 64-lag chunks above the threshold
+    const bool fused = match && !mf->tc && len == mf->pk_fused_len;
+    const unsigned *flags = match && mf->tc ? mf->pk_flags.as<unsigned>() : nullptr;
     FusedSlots<float> ff{mf->pk_cnt.as<int>(), mf->pk_idx.as<int>(), mf->pk_val.as<float>(), mf->nblocks, mf->S};
     FusedSlots<double> fd{mf->pk_cnt.as<int>(), mf->pk_idx.as<int>(), mf->pk_val.as<double>(), mf->nblocks, mf->S};
     int rc = mf->prec == 4
                  ? run_peaks<float>(mf->rho.as<float>(), mf->ldr, rows.data(), mf->nt, len, threshold, min_distance,
-                                    mf->pk, mf->stream, &mf->launches, mf->pk_off.data(), err, fused ? &ff : nullptr)
+                                    mf->pk, mf->stream, &mf->launches, mf->pk_off.data(), err, fused ? &ff : nullptr,
+                                    flags, mf->pk_words)
                  : run_peaks<double>(mf->rho.as<double>(), mf->ldr, rows.data(), mf->nt, len, threshold,
                                      min_distance, mf->pk, mf->stream, &mf->launches, mf->pk_off.data(), err,
                                      fused ? &fd : nullptr);

@@ -35,6 +35,11 @@ template <class T> struct PeakTraces
     const int *row;   // row of each trace
     int len;          // lags per trace
     T thr;
+    // optional: bit c of row r (word r * fwords + c / 32) set when a lag in
+    // [64c, 64c + 64) of that row exceeds thr; a warp whose 512 lags have no
+    // bit set finds no candidate and skips its reads
+    const unsigned *flags = nullptr;
+    int fwords = 0;
 };
 
 template <class T> __device__ __forceinline__ bool is_candidate(const T *x, int i, int n, T thr)
@@ -128,7 +133,15 @@ static __global__ void __launch_bounds__(kPkThreads) peak_cand_kernel(PeakTraces
     const T *x = tr.x + (long) tr.row[trace] * tr.ldx;
     const int n = tr.len;
     const int i0 = chunk * kPkChunk + threadIdx.x * kPkPer;
-    unsigned mask = cand_mask16<T>(x, i0, n, tr.thr);
+    bool scan = true;
+    if (tr.flags)
+    {
+        // the warp's 512 lags are chunks c64 .. c64 + 7 (c64 a multiple of 8)
+        const int c64 = (chunk * kPkChunk + (threadIdx.x >> 5) * 32 * kPkPer) / 64;
+        scan = c64 / 32 < tr.fwords &&
+               ((tr.flags[(long) tr.row[trace] * tr.fwords + c64 / 32] >> (c64 % 32)) & 0xFFu) != 0u;
+    }
+    unsigned mask = scan ? cand_mask16<T>(x, i0, n, tr.thr) : 0u;  // warp-uniform choice
     long long tot;
     long long r = block_excl_scan((long long) __popc(mask), sh, &tot);
     const long slot = (long) trace * nchunks + chunk;
@@ -176,7 +189,15 @@ static __global__ void __launch_bounds__(kPkThreads) peak_gather_kernel(PeakTrac
     const T *x = tr.x + (long) tr.row[trace] * tr.ldx;
     const int n = tr.len;
     const int i0 = chunk * kPkChunk + threadIdx.x * kPkPer;
-    unsigned mask = cand_mask16<T>(x, i0, n, tr.thr);
+    bool scan = true;
+    if (tr.flags)
+    {
+        // the warp's 512 lags are chunks c64 .. c64 + 7 (c64 a multiple of 8)
+        const int c64 = (chunk * kPkChunk + (threadIdx.x >> 5) * 32 * kPkPer) / 64;
+        scan = c64 / 32 < tr.fwords &&
+               ((tr.flags[(long) tr.row[trace] * tr.fwords + c64 / 32] >> (c64 % 32)) & 0xFFu) != 0u;
+    }
+    unsigned mask = scan ? cand_mask16<T>(x, i0, n, tr.thr) : 0u;  // warp-uniform choice
     long long tot;
     long long r = block_excl_scan((long long) __popc(mask), sh, &tot);
     while (mask)

@@ -370,6 +370,20 @@ static __global__ void __launch_bounds__(kTcThreads, 1) tc_xcorr_kernel(TcParams
                     for (int f = 0; f < 8; ++f)
                         o[f] = dead ? 0.f
                                     : clamp_rho((__uint_as_float(r[u][f]) + __uint_as_float(h[u][f])) * sc * dcur[f]);
+                    if (p.pk_flags)
+                    {
+                        // one bit per 64 lags (8 rows); values above the
+                        // threshold are rare, so each such row sets its bit
+                        // itself, without a warp-wide vote
+                        bool above = false;
+#pragma unroll
+                        for (int f = 0; f < 8; ++f) above |= lag0 + f < p.nv && o[f] > p.pk_thr;
+                        if (above)
+                        {
+                            const long c = lag0 >> 6;
+                            atomicOr(p.pk_flags + (long) tt * p.pk_words + (c >> 5), 1u << (c & 31));
+                        }
+                    }
                     float *dst = p.rho + (long) tt * p.ldr + lag0;
                     if (lag0 + 7 < p.nv)
                     {

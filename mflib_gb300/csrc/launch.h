@@ -119,11 +119,13 @@ struct PeakWS
 // Runs candidates + pruning + compaction; on return (stream synchronised)
 // ws.peaks / ws.peak_off hold the result and host_peak_off (ntr+1) is filled.
 // With `fused`, the candidates the correlator gathered (same threshold and
-// trace length) replace the scan over the traces.
+// trace length) replace the scan over the traces.  Otherwise `flags` (bit
+// per 64 lags of each row, fwords words per row; see PeakTraces), when given,
+// lets the scan skip the lags no value above the threshold lies in.
 template <class T>
 int run_peaks(const T *x, long ldx, const int *host_rows, int ntr, int len, double thr, int dist, PeakWS &ws,
               cudaStream_t s, long long *launches, long long *host_peak_off, std::string &err,
-              const FusedSlots<T> *fused = nullptr);
+              const FusedSlots<T> *fused = nullptr, const unsigned *flags = nullptr, int fwords = 0);
 
 // ---------------------------------------------------------------------------
 // DBSCAN over segments

@@ -35,7 +35,7 @@ cudaError_t device_excl_scan(const int *in, long n, long long *out, long long *t
 template <class T>
 int run_peaks(const T *x, long ldx, const int *host_rows, int ntr, int len, double thr, int dist, PeakWS &ws,
               cudaStream_t s, long long *launches, long long *host_peak_off, std::string &err,
-              const FusedSlots<T> *fused)
+              const FusedSlots<T> *fused, const unsigned *flags, int fwords)
 {
     ws.npeaks = 0;
     if (ntr <= 0) return 0;
@@ -66,6 +66,7 @@ int run_peaks(const T *x, long ldx, const int *host_rows, int ntr, int len, doub
 
     PeakTraces<T> tr;
     tr.x = x; tr.ldx = ldx; tr.row = ws.row.as<int>(); tr.len = len; tr.thr = (T) thr;
+    tr.flags = fused ? nullptr : flags; tr.fwords = fwords;
     const dim3 grid(nchunks, ntr);
     const bool prune = dist > 0;
     for (int attempt = 0; attempt < 4; ++attempt)
@@ -173,9 +174,11 @@ int run_peaks(const T *x, long ldx, const int *host_rows, int ntr, int len, doub
     return -1;
 }
 template int run_peaks<float>(const float *, long, const int *, int, int, double, int, PeakWS &, cudaStream_t,
-                              long long *, long long *, std::string &, const FusedSlots<float> *);
+                              long long *, long long *, std::string &, const FusedSlots<float> *,
+                              const unsigned *, int);
 template int run_peaks<double>(const double *, long, const int *, int, int, double, int, PeakWS &, cudaStream_t,
-                               long long *, long long *, std::string &, const FusedSlots<double> *);
+                               long long *, long long *, std::string &, const FusedSlots<double> *,
+                               const unsigned *, int);
 
 int run_dbscan(int n, int nf, const double *X, const double *w, double eps, int min_obs, int nseg,
                const int *seg_off_host, int *labels_host, int *nclusters_host, DbWS &ws, cudaStream_t s,

@@ -30,6 +30,11 @@ struct TcParams
     int Kp, Gp, tmem_cols;
     int ngroups, tiles;
     int *err;
+    // peak-candidate flags (null: off): bit c of word t * pk_words + c / 32
+    // set when a stored lag of [64c, 64c + 64) of template t exceeds pk_thr
+    unsigned *pk_flags;
+    int pk_words;
+    float pk_thr;
 };
 
 // barriers and the TMEM address | 2 strip buffers x (hi, lo) | template bank (hi, lo)

@@ -212,21 +212,26 @@ def _filter(mf, p, chans, assign, dtype, **kw):
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
-@pytest.mark.parametrize("variant", [1, 2, 3, 5])
+@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5])
 @pytest.mark.parametrize("fft_length", [256, 1024, 4096])
 def test_fused_peak_candidates(gpu, oracle, rng, dtype, variant, fft_length):
     """Candidates gathered inside the correlator give exactly the peaks of
     the stand-alone scan and of the oracle, including chunks with more
-    candidates than slots (threshold 0), block seams and the last lag."""
+    candidates than slots (threshold 0), block seams and the last lag.
+    Variant 4 (tensor cores, FP32) flags the 64-lag chunks above the
+    threshold instead, and the scan reads only those."""
     mf = gpu
     if dtype == np.float64 and variant == 2 and fft_length == 4096:
         pytest.skip("FP64 spectrum prefetch at N = 4096 exceeds the shared memory of a CTA")
+    if variant == 4 and (dtype == np.float64 or fft_length != 4096):
+        pytest.skip("the tensor-core correlator takes FP32 data and plans no FFT")
     lens = [150] * 6
     p, chans, assign = _fused_case(mf, rng, dtype, lens)
-    plain = _filter(mf, p, chans, assign, dtype, fft_length=fft_length, correlator_variant=variant)
+    fl = 0 if variant == 4 else fft_length
+    plain = _filter(mf, p, chans, assign, dtype, fft_length=fl, correlator_variant=variant)
     plain.apply()
     for thr, md in ((0.0, 0), (0.0, 40), (0.35, 0), (0.35, 150), (0.8, 300)):
-        f = _filter(mf, p, chans, assign, dtype, fft_length=fft_length, correlator_variant=variant)
+        f = _filter(mf, p, chans, assign, dtype, fft_length=fl, correlator_variant=variant)
         f.set_peak_threshold(thr)
         f.apply()
         assert f.get_peak_threshold() == (thr, True)
