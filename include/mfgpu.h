@@ -92,6 +92,12 @@ typedef struct
        normalisation computed inside each CTA instead of by a separate
        per-channel pass (templates of one length). */
     int correlator_variant;
+    /* Extension: templates of several lengths are split by length into at
+       most this many buckets, each with its own FFT length and block length
+       (0 = automatic: at most 3, a split must save more than a launch;
+       1 = one plan for every template; k > 1: at most k, split wherever the
+       plans get cheaper). */
+    int length_buckets;
 } mfgpu_mf_params;
 
 /* MatchedFilter<T>::MatchedFilter(); precision MFGPU_FLOAT32 | MFGPU_FLOAT64 */
@@ -168,6 +174,10 @@ mfgpu_status mfgpu_mf_get_plan(const mfgpu_mf *mf, int *fft_length, int *lags_pe
  * tensor-core path also the templates per group and the padded K, else 0.
  * Extension: the reference has one CPU correlator and no such query. */
 mfgpu_status mfgpu_mf_get_correlator(const mfgpu_mf *mf, int *variant, int *tc_group, int *tc_k);
+/* Length buckets chosen at initialize: their number, and for each (up to
+ * max, shortest templates first, the primary plan last) the FFT length and
+ * the number of templates.  Extension: the reference has one FFT length. */
+mfgpu_status mfgpu_mf_get_buckets(const mfgpu_mf *mf, int max, int *fft_lengths, int *n_templates, int *count);
 /* Request-window upload for a serving loop.  Extension: the reference sets
  * whole-length signals one template at a time (setSignal,
  * src/matchedFilter.cpp:863-921) and has no serving loop.  x holds n_src

@@ -41,6 +41,7 @@ class MfgpuParams(C.Structure):
         ("template_channel", C.POINTER(C.c_int)),
         ("fft_length", C.c_int),
         ("correlator_variant", C.c_int),
+        ("length_buckets", C.c_int),
     ]
 
 
@@ -75,6 +76,7 @@ _SIGS = {
     "mfgpu_mf_get_device_signal": ([_vp, C.c_int, C.POINTER(_vp), _ip], C.c_int),
     "mfgpu_mf_get_plan": ([_vp, _ip, _ip, _ip], C.c_int),
     "mfgpu_mf_get_correlator": ([_vp, _ip, _ip, _ip], C.c_int),
+    "mfgpu_mf_get_buckets": ([_vp, C.c_int, _ip, _ip, _ip], C.c_int),
     "mfgpu_mf_set_window": ([_vp, C.c_int, C.c_int, _vp, C.c_long], C.c_int),
     "mfgpu_mf_get_device_bytes": ([_vp, C.POINTER(C.c_ulonglong)], C.c_int),
     "mfgpu_mf_synchronize": ([_vp], C.c_int),

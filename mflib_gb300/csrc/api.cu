@@ -11,6 +11,7 @@
 #include <cstring>
 #include <limits>
 #include <string>
+#include <memory>
 #include <vector>
 #include "mfgpu.h"
 #include "launch.h"
@@ -100,6 +101,20 @@ mfgpu_status fft_sizes(int nb, int nx, int *nfft, int *L)
 void mfgpu::set_last_error(const std::string &msg) { g_err = msg; }
 
 // ============================================================================
+// Overlap-save plan of one length bucket beside the primary plan (the
+// templates of a mixed-length bank split by length, each bucket with its own
+// FFT length, block length, organisation, spectra and work groups).
+struct MfBucket
+{
+    int log2p = 0, nfft = 0, S = 0, nblocks = 0, mode = 0, ngroups = 0, ntemplates = 0;
+    DevBuf Bc, tw, grp_chan, grp_tb, grp_te, tids;
+    template <class F> void each_buf(F &&f)
+    {
+        DevBuf *all[] = {&Bc, &tw, &grp_chan, &grp_tb, &grp_te, &tids};
+        for (DevBuf *d : all) f(*d);
+    }
+};
+
 struct mfgpu_mf
 {
     int prec = 4;
@@ -150,6 +165,13 @@ struct mfgpu_mf
     DevBuf pk_cnt, pk_idx, pk_val;
     DevBuf pk_flags;   // tensor-core correlator: candidate flags per 64 lags
     int pk_words = 0;
+    // length buckets beside the primary plan (longest templates); per
+    // template its bucket's block length and block count, and the slot row
+    // stride of the gathered candidates (the largest block count)
+    std::vector<std::unique_ptr<MfBucket>> xb;
+    int ntemplates0 = 0;
+    DevBuf row_S, row_nblk;
+    int pk_stride = 0;
     long long launches = 0;
     float last_xcorr_ms = 0, last_apply_ms = 0;
 
@@ -162,6 +184,9 @@ struct mfgpu_mf
                          &xrange,   &tc_B,   &tc_bscale, &tc_grp_chan, &tc_grp_tid, &pk_flags};
         for (DevBuf *d : all) f(*d);
         pk.each_buf(f);
+        f(row_S);
+        f(row_nblk);
+        for (auto &b : xb) b->each_buf(f);
     }
     void release_device()
     {
@@ -183,6 +208,8 @@ struct mfgpu_mf
         initialized = have = timed = have_peaks = pk_fused = false;
         pk_req = -1;
         nt = n = maxLen = minLen = nch = 0;
+        xb.clear();
+        ntemplates0 = pk_stride = 0;
         lens.clear(); tchan.clear(); nvalid.clear(); tmpl.clear(); toff.clear();
         shifts.clear(); weights.clear(); pk_off.clear();
         can_stack = false;
@@ -286,20 +313,23 @@ mfgpu_status mfgpu_mf_clear(mfgpu_mf *mf)
     return MFGPU_OK;
 }
 
-template <class T> static mfgpu_status mf_upload_tables(mfgpu_mf *mf)
+// twiddles and resident template spectra of one plan (every template's
+// spectrum at the plan's FFT length; the plan reads its bucket's rows)
+template <class T> static mfgpu_status mf_upload_tables(mfgpu_mf *mf, int log2p, DevBuf &twb, DevBuf &Bc)
 {
     std::vector<cx<T>> tw;
-    twiddle_table<T>(mf->log2p, tw);
-    CU(mf->tw.ensure(sizeof(cx<T>) * tw.size()));
-    CU(cudaMemcpyAsync(mf->tw.p, tw.data(), sizeof(cx<T>) * tw.size(), cudaMemcpyHostToDevice, mf->stream));
+    twiddle_table<T>(log2p, tw);
+    CU(twb.ensure(sizeof(cx<T>) * tw.size()));
+    CU(cudaMemcpyAsync(twb.p, tw.data(), sizeof(cx<T>) * tw.size(), cudaMemcpyHostToDevice, mf->stream));
+    CU(Bc.ensure(sizeof(cx<T>) * (size_t) mf->nt * ((1L << log2p) + 2)));
     SpecParams<T> sp;
     sp.tmpl = mf->tmpl_d.as<double>();
     sp.toff = mf->toff_d.as<long>();
     sp.tlen = mf->tlen_d.as<int>();
-    sp.Bc = mf->Bc.as<cx<T>>();
-    sp.ldb = (1L << mf->log2p) + 2;
-    sp.twt = mf->tw.as<cx<T>>();
-    CU(launch_spectra<T>(mf->log2p, sp, mf->nt, mf->stream));
+    sp.Bc = Bc.as<cx<T>>();
+    sp.ldb = (1L << log2p) + 2;
+    sp.twt = twb.as<cx<T>>();
+    CU(launch_spectra<T>(log2p, sp, mf->nt, mf->stream));
     ++mf->launches;
     return MFGPU_OK;
 }
@@ -417,46 +447,133 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
         int occ = (int) (sm_smem / (bytes + 1024));
         return std::min(cap, occ);
     };
-    int best_l2p = -1, best_S = 0, best_mode = 0;
-    double best_cost = 0;
-    for (int l2p = lo; l2p <= hi; ++l2p)
+    // best plan for templates of lengths up to Lb, the longest trace mv lags:
+    // FFT length, lags per block, organisation and the cost in seconds per
+    // template of the whole trace
+    struct PlanPick
     {
-        int N = 2 << l2p;
-        if (p->fft_length > 0 && p->fft_length != N) continue;
-        int S = ((N - maxLen + 1) / 32) * 32;
-        if (S < 32) continue;
-        // organisation: forced, else two teams for a shared length when they
-        // keep the occupancy (measured 16% faster than the whole-CTA loop at
-        // N = 4096 and 5% at N = 2048, 2% slower at N = 8192), else spectrum
-        // prefetch when it keeps the occupancy
-        int mode;
-        if (forced_mode >= 0) mode = forced_mode;
-        else
+        int l2p = -1, S = 0, mode = 0;
+        double cost = 0;
+    };
+    auto plan_for = [&](int Lb, int mv, bool eq) {
+        PlanPick best;
+        for (int l2p = lo; l2p <= hi; ++l2p)
         {
-            size_t b0 = smem_of(l2p, 0, S), b1 = smem_of(l2p, 1, S);
-            int occ0 = occupancy(l2p, b0), occ1 = (int) b1 <= dev_smem ? occupancy(l2p, b1) : 0;
-            mode = (occ1 >= occ0 && occ1 > 0) ? 1 : 0;
-            if (all_equal && l2p <= 11)
+            int N = 2 << l2p;
+            if (p->fft_length > 0 && p->fft_length != N) continue;
+            int S = ((N - Lb + 1) / 32) * 32;
+            if (S < 32) continue;
+            // organisation: forced, else two teams for a shared length when
+            // they keep the occupancy (measured 16% faster than the whole-CTA
+            // loop at N = 4096 and 5% at N = 2048, 2% slower at N = 8192),
+            // else spectrum prefetch when it keeps the occupancy
+            int mode;
+            if (forced_mode >= 0) mode = forced_mode;
+            else
             {
-                size_t b2 = smem_of(l2p, 2, S);
-                int occ2 = (int) b2 <= dev_smem ? occupancy(l2p, b2) : 0;
-                if (occ2 >= std::max(occ0, occ1) && occ2 > 0) mode = 2;
+                size_t b0 = smem_of(l2p, 0, S), b1 = smem_of(l2p, 1, S);
+                int occ0 = occupancy(l2p, b0), occ1 = (int) b1 <= dev_smem ? occupancy(l2p, b1) : 0;
+                mode = (occ1 >= occ0 && occ1 > 0) ? 1 : 0;
+                if (eq && l2p <= 11)
+                {
+                    size_t b2 = smem_of(l2p, 2, S);
+                    int occ2 = (int) b2 <= dev_smem ? occupancy(l2p, b2) : 0;
+                    if (occ2 >= std::max(occ0, occ1) && occ2 > 0) mode = 2;
+                }
             }
+            size_t bytes = smem_of(l2p, mode, S);
+            if ((int) bytes > dev_smem) continue;
+            int occ = occupancy(l2p, bytes);
+            if (occ < 1) continue;
+            // seconds per (template, block), measured on GB300.  One template
+            // length (normalisation rows precomputed): 8.4 ns at P = 2048 (N =
+            // 4096, two CTAs per SM), ratios 0.70 at N = 2048 and 2.86 at N =
+            // 8192 (one CTA per SM).  Several lengths (normalisation inside the
+            // CTA for each template): 18.8 ns at N = 4096 and 35.2 ns at N =
+            // 8192 (2,000-template bank).  Shorter transforms scale as N log N.
+            double rel, base;
+            if (eq)
+            {
+                base = 8.4e-9;
+                rel = l2p == 11 ? 1.0 : l2p == 12 ? 2.86 : 0.70 * std::ldexp(1.0, l2p - 10) * (l2p + 1) / 11.0;
+                if (l2p <= 11 && occ < 2) rel *= 1.4;
+            }
+            else
+            {
+                base = 18.8e-9;
+                rel = l2p == 12 ? 1.87 : std::ldexp(1.0, l2p - 11) * (l2p + 1) / 12.0;
+            }
+            const double nb = std::ceil((double) std::max(1, mv) / S);
+            const double cost = nb * rel * base;
+            if (best.l2p < 0 || cost < best.cost) best = PlanPick{l2p, S, mode, cost};
         }
-        size_t bytes = smem_of(l2p, mode, S);
-        if ((int) bytes > dev_smem) continue;
-        int occ = occupancy(l2p, bytes);
-        if (occ < 1) continue;
-        // seconds per (template, block), measured on GB300 at P = 2048 (N =
-        // 4096, two CTAs per SM) and scaled by the measured ratios of the
-        // neighbouring FFT lengths (0.70 at N = 2048, 2.86 at N = 8192 with one
-        // CTA per SM); shorter transforms scale as N log N
-        double rel = l2p == 11 ? 1.0 : l2p == 12 ? 2.86 : 0.70 * std::ldexp(1.0, l2p - 10) * (l2p + 1) / 11.0;
-        if (l2p <= 11 && occ < 2) rel *= 1.4;
-        const double nb = std::ceil((double) std::max(1, maxvalid) / S);
-        const double cost = nb * rel * 8.4e-9;
-        if (best_l2p < 0 || cost < best_cost) { best_l2p = l2p; best_S = S; best_cost = cost; best_mode = mode; }
+        return best;
+    };
+    // Length buckets for a mixed-length bank (automatic FFT length, whole-CTA
+    // organisations): the templates sorted by length split into at most
+    // length_buckets (default 3) contiguous buckets, each with its own plan,
+    // minimising the summed plan cost plus, when the limit is automatic,
+    // 20 us per extra launch.  Cut positions are taken from 64 quantiles of
+    // the sorted lengths.
+    std::vector<int> order(nt);
+    for (int t = 0; t < nt; ++t) order[t] = t;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return mf->lens[a] < mf->lens[b]; });
+    std::vector<int> cuts{0, nt};
+    const int maxb = p->length_buckets > 0 ? p->length_buckets : 3;
+    if (p->length_buckets < 0) return fail(MFGPU_EINVAL, "length_buckets must be >= 0");
+    if (!all_equal && p->fft_length == 0 && forced_mode <= 1 && maxb > 1)
+    {
+        std::vector<int> pos{0};
+        for (int q = 1; q < 64; ++q)
+        {
+            const int i = (int) ((long) q * nt / 64);
+            if (i > pos.back() && i < nt && mf->lens[order[i]] != mf->lens[order[i - 1]]) pos.push_back(i);
+        }
+        pos.push_back(nt);
+        const int M = (int) pos.size();
+        std::vector<double> bc((size_t) M * M, 1e300);
+        for (int a = 0; a < M; ++a)
+            for (int b = a + 1; b < M; ++b)
+            {
+                const int Lb = mf->lens[order[pos[b] - 1]], mv = n - mf->lens[order[pos[a]]] + 1;
+                const PlanPick pk = plan_for(Lb, mv, false);
+                if (pk.l2p >= 0) bc[(size_t) a * M + b] = pk.cost * (pos[b] - pos[a]);
+            }
+        // an explicit bucket limit splits wherever the plans get cheaper
+        const double launch_cost = p->length_buckets == 0 ? 20e-6 : 0.0;
+        // dp[k][b]: best cost of positions [0, b) in k buckets
+        std::vector<std::vector<double>> dp(maxb + 1, std::vector<double>(M, 1e300));
+        std::vector<std::vector<int>> from(maxb + 1, std::vector<int>(M, -1));
+        dp[0][0] = 0;
+        for (int k = 1; k <= maxb; ++k)
+            for (int b = 1; b < M; ++b)
+                for (int a = 0; a < b; ++a)
+                {
+                    const double c = dp[k - 1][a] + bc[(size_t) a * M + b] + (k > 1 ? launch_cost : 0.0);
+                    if (c < dp[k][b]) { dp[k][b] = c; from[k][b] = a; }
+                }
+        int bk = 1;
+        for (int k = 2; k <= maxb; ++k)
+            if (dp[k][M - 1] < dp[bk][M - 1]) bk = k;
+        // automatic: split only for a predicted saving above 15 % (on the
+        // 2,000-template bank the model predicted 10 % for two buckets at N =
+        // 8192 and GB300 measured 1 %; for three, 10 % and -4 %)
+        if (p->length_buckets == 0 && dp[bk][M - 1] > 0.85 * dp[1][M - 1]) bk = 1;
+        if (dp[bk][M - 1] < 1e299 && bk > 1)
+        {
+            cuts.assign(1, nt);
+            for (int k = bk, b = M - 1; k > 0; b = from[k][b], --k) cuts.push_back(pos[from[k][b]]);
+            std::reverse(cuts.begin(), cuts.end());
+        }
     }
+    const int nbk = (int) cuts.size() - 1;  // bucket nbk - 1 (longest templates) is the primary plan
+    std::vector<int> bucket_of(nt, nbk - 1);
+    for (int b = 0; b < nbk; ++b)
+        for (int i = cuts[b]; i < cuts[b + 1]; ++i) bucket_of[order[i]] = b;
+    const int mv0 = n - mf->lens[order[cuts[nbk - 1]]] + 1;
+    const PlanPick best = plan_for(maxLen, nbk > 1 ? mv0 : maxvalid, all_equal);
+    const int best_l2p = best.l2p, best_S = best.S, best_mode = best.mode;
+    const double best_cost = best.cost;
     mf->mode_x = best_mode;
     if (best_mode == 3) mf->shared_den = false;
     // seconds per template-lag of the chosen FFT plan
@@ -473,8 +590,23 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
     mf->log2p = best_l2p;
     mf->nfft = 2 << best_l2p;
     mf->S = best_S;
-    mf->nblocks = (maxvalid + best_S - 1) / best_S;
+    mf->nblocks = ((nbk > 1 ? mv0 : maxvalid) + best_S - 1) / best_S;
+    for (int b = 0; b + 1 < nbk; ++b)
+    {
+        const int Lb = mf->lens[order[cuts[b + 1] - 1]], mv = n - mf->lens[order[cuts[b]]] + 1;
+        const PlanPick pk = plan_for(Lb, mv, false);
+        auto xb = std::make_unique<MfBucket>();
+        xb->log2p = pk.l2p;
+        xb->nfft = 2 << pk.l2p;
+        xb->S = pk.S;
+        xb->mode = pk.mode;
+        xb->nblocks = (mv + pk.S - 1) / pk.S;
+        xb->ntemplates = cuts[b + 1] - cuts[b];
+        mf->xb.push_back(std::move(xb));
+    }
+    mf->ntemplates0 = cuts[nbk] - cuts[nbk - 1];
     mf->ldx = ((long) mf->nblocks * best_S + mf->nfft + 63) / 64 * 64;
+    for (auto &xb : mf->xb) mf->ldx = std::max<long>(mf->ldx, ((long) xb->nblocks * xb->S + xb->nfft + 63) / 64 * 64);
     mf->ldx = std::max<long>(mf->ldx, (n + 63) / 64 * 64);
     mf->ldr = ((long) std::max(1, maxvalid) + 63) / 64 * 64;
     if (all_equal)
@@ -542,38 +674,59 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
         mf->ldx = std::max<long>(mf->ldx, ((long) mf->nden * lpc + 32L * den_tail_runs(maxLen) + 63) / 64 * 64);
     }
     if (mf->tc) mf->shared_den = true;  // the tensor-core epilogue reads den_kernel's rows
-    // work groups: split each channel's templates so the grid has enough CTAs
-    int G = std::max(1, max_tpc);
-    auto count_groups = [&](int gsz) {
-        long ng = 0;
-        for (int c = 0; c < nch; ++c) ng += (per_chan[c] + gsz - 1) / gsz;
-        return ng;
-    };
-    while (G > 1 && ((long) mf->nblocks * count_groups(G) < 4L * 152 * 2 || count_groups(G) > 65535)) G = (G + 1) / 2;
-    if (count_groups(G) > 65535) return fail(MFGPU_EINVAL, "too many template groups");
-    std::vector<int> gch, gtb, gte, tids;
-    for (int c = 0; c < nch; ++c)
+    // work groups of one plan: each channel's templates of the bucket, split
+    // so the grid has enough CTAs
+    struct Groups
     {
-        for (size_t i = 0; i < chan_t[c].size(); i += G)
+        std::vector<int> gch, gtb, gte, tids;
+    };
+    auto make_groups = [&](int bucket, int nblocks, Groups &gr) {
+        std::vector<int> pc(nch, 0);
+        int mx = 0;
+        for (int t = 0; t < nt; ++t)
+            if (bucket_of[t] == bucket) mx = std::max(mx, ++pc[tchan[t]]);
+        int G = std::max(1, mx);
+        auto count_groups = [&](int gsz) {
+            long ng = 0;
+            for (int c = 0; c < nch; ++c) ng += (pc[c] + gsz - 1) / gsz;
+            return ng;
+        };
+        while (G > 1 && ((long) nblocks * count_groups(G) < 4L * 152 * 2 || count_groups(G) > 65535)) G = (G + 1) / 2;
+        if (count_groups(G) > 65535) return false;
+        for (int c = 0; c < nch; ++c)
         {
-            gch.push_back(c);
-            gtb.push_back((int) tids.size());
-            for (size_t j = i; j < std::min(chan_t[c].size(), i + (size_t) G); ++j) tids.push_back(chan_t[c][j]);
-            gte.push_back((int) tids.size());
+            std::vector<int> mine;
+            for (int t : chan_t[c])
+                if (bucket_of[t] == bucket) mine.push_back(t);
+            for (size_t i = 0; i < mine.size(); i += G)
+            {
+                gr.gch.push_back(c);
+                gr.gtb.push_back((int) gr.tids.size());
+                for (size_t j = i; j < std::min(mine.size(), i + (size_t) G); ++j) gr.tids.push_back(mine[j]);
+                gr.gte.push_back((int) gr.tids.size());
+            }
         }
+        return true;
+    };
+    Groups g0;
+    std::vector<Groups> gx(mf->xb.size());
+    if (!make_groups(nbk - 1, mf->nblocks, g0)) return fail(MFGPU_EINVAL, "too many template groups");
+    for (size_t b = 0; b < mf->xb.size(); ++b)
+    {
+        if (!make_groups((int) b, mf->xb[b]->nblocks, gx[b])) return fail(MFGPU_EINVAL, "too many template groups");
+        mf->xb[b]->ngroups = (int) gx[b].gch.size();
     }
+    const std::vector<int> &gch = g0.gch, &gtb = g0.gtb, &gte = g0.gte, &tids = g0.tids;
     mf->ngroups = (int) gch.size();
     mf->dead_chunks = (int) std::min<long>(1024, std::max<long>(1, (n + 16383) / 16384));
 
     // ---- device memory
     const size_t es = mf->esz();
-    const int P = 1 << mf->log2p;
     CU(mf->x.ensure(es * (size_t) nch * mf->ldx));
     if (mf->shared_den) CU(mf->den.ensure(es * (size_t) nch * mf->ldd));
     CU(cudaMemsetAsync(mf->x.p, 0, mf->x.bytes, mf->stream));
     CU(mf->rho.ensure(es * (size_t) nt * mf->ldr));
     CU(cudaMemsetAsync(mf->rho.p, 0, mf->rho.bytes, mf->stream));
-    CU(mf->Bc.ensure(2 * es * (size_t) nt * (P + 2)));
     CU(mf->grp_chan.ensure(sizeof(int) * gch.size()));
     CU(mf->grp_tb.ensure(sizeof(int) * gch.size()));
     CU(mf->grp_te.ensure(sizeof(int) * gch.size()));
@@ -602,8 +755,49 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
     CU(cudaMemcpyAsync(mf->toff_d.p, mf->toff.data(), sizeof(long) * nt, cudaMemcpyHostToDevice, mf->stream));
     CU(mf->xrange.ensure(sizeof(float) * nch));
     CU(cudaMemsetAsync(mf->xrange.p, 0, sizeof(float) * nch, mf->stream));
-    mfgpu_status s2 = mf->prec == 4 ? mf_upload_tables<float>(mf) : mf_upload_tables<double>(mf);
+    mfgpu_status s2 = mf->prec == 4 ? mf_upload_tables<float>(mf, mf->log2p, mf->tw, mf->Bc)
+                                    : mf_upload_tables<double>(mf, mf->log2p, mf->tw, mf->Bc);
     if (s2 != MFGPU_OK) return s2;
+    for (size_t b = 0; b < mf->xb.size(); ++b)
+    {
+        MfBucket &xb = *mf->xb[b];
+        s2 = mf->prec == 4 ? mf_upload_tables<float>(mf, xb.log2p, xb.tw, xb.Bc)
+                           : mf_upload_tables<double>(mf, xb.log2p, xb.tw, xb.Bc);
+        if (s2 != MFGPU_OK) return s2;
+        const Groups &gr = gx[b];
+        CU(xb.grp_chan.ensure(sizeof(int) * gr.gch.size()));
+        CU(xb.grp_tb.ensure(sizeof(int) * gr.gch.size()));
+        CU(xb.grp_te.ensure(sizeof(int) * gr.gch.size()));
+        CU(xb.tids.ensure(sizeof(int) * std::max<size_t>(1, gr.tids.size())));
+        CU(cudaMemcpyAsync(xb.grp_chan.p, gr.gch.data(), sizeof(int) * gr.gch.size(), cudaMemcpyHostToDevice,
+                           mf->stream));
+        CU(cudaMemcpyAsync(xb.grp_tb.p, gr.gtb.data(), sizeof(int) * gr.gtb.size(), cudaMemcpyHostToDevice,
+                           mf->stream));
+        CU(cudaMemcpyAsync(xb.grp_te.p, gr.gte.data(), sizeof(int) * gr.gte.size(), cudaMemcpyHostToDevice,
+                           mf->stream));
+        CU(cudaMemcpyAsync(xb.tids.p, gr.tids.data(), sizeof(int) * gr.tids.size(), cudaMemcpyHostToDevice,
+                           mf->stream));
+    }
+    // block length and count of every template's plan; slot rows of the
+    // gathered peak candidates span the largest count
+    mf->pk_stride = mf->nblocks;
+    for (auto &xb : mf->xb) mf->pk_stride = std::max(mf->pk_stride, xb->nblocks);
+    if (!mf->xb.empty())
+    {
+        std::vector<int> rs(nt), rn(nt);
+        for (int t = 0; t < nt; ++t)
+        {
+            const int b = bucket_of[t];
+            rs[t] = b == nbk - 1 ? mf->S : mf->xb[b]->S;
+            rn[t] = b == nbk - 1 ? mf->nblocks : mf->xb[b]->nblocks;
+        }
+        CU(mf->row_S.ensure(sizeof(int) * nt));
+        CU(mf->row_nblk.ensure(sizeof(int) * nt));
+        CU(cudaMemcpyAsync(mf->row_S.p, rs.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, mf->stream));
+        CU(cudaMemcpyAsync(mf->row_nblk.p, rn.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, mf->stream));
+        // the host vectors above must outlive the copies
+        CU(cudaStreamSynchronize(mf->stream));
+    }
     if (mf->tc)
     {
         const size_t slots = (size_t) mf->tc_groups * mf->tc_Gp;
@@ -678,6 +872,20 @@ mfgpu_status mfgpu_mf_get_correlator(const mfgpu_mf *mf, int *variant, int *tc_g
     if (variant) *variant = mf->tc ? 4 : mf->mode_x == 3 ? 5 : mf->mode_x + 1;
     if (tc_group) *tc_group = mf->tc ? mf->tc_Gp : 0;
     if (tc_k) *tc_k = mf->tc ? mf->tc_Kp : 0;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_get_buckets(const mfgpu_mf *mf, int max, int *fft_lengths, int *n_templates, int *count)
+{
+    MF_CHECK_INIT(mf);
+    const int nb = (int) mf->xb.size() + 1;
+    if (count) *count = nb;
+    for (int b = 0; b < nb && b < max; ++b)
+    {
+        const bool prim = b == nb - 1;
+        if (fft_lengths) fft_lengths[b] = prim ? mf->nfft : mf->xb[b]->nfft;
+        if (n_templates) n_templates[b] = prim ? (mf->xb.empty() ? mf->nt : mf->ntemplates0) : mf->xb[b]->ntemplates;
+    }
     return MFGPU_OK;
 }
 
@@ -927,9 +1135,10 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
     // fused peak candidates
     mf->pk_fused = false;
     p.pk_on = 0;
+    p.pk_stride = mf->pk_stride;
     if (mf->pk_req >= 0 && !mf->tc)
     {
-        const size_t nslot = (size_t) mf->nt * mf->nblocks;
+        const size_t nslot = (size_t) mf->nt * mf->pk_stride;
         CU(mf->pk_cnt.ensure(sizeof(int) * nslot));
         CU(mf->pk_idx.ensure(sizeof(int) * nslot * kPkCap));
         CU(mf->pk_val.ensure(sizeof(T) * nslot * kPkCap));
@@ -981,6 +1190,19 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
     }
     CU(launch_xcorr<T>(mf->log2p, mf->shared_den, mf->mode_x, p, mf->nblocks, mf->ngroups, mf->stream));
     ++mf->launches;
+    // the other length buckets, one launch each
+    for (auto &xb : mf->xb)
+    {
+        if (xb->ngroups == 0) continue;
+        XcorrParams<T> q = p;
+        q.Bc = xb->Bc.as<cx<T>>(); q.ldb = (1L << xb->log2p) + 2;
+        q.grp_chan = xb->grp_chan.as<int>(); q.grp_tb = xb->grp_tb.as<int>(); q.grp_te = xb->grp_te.as<int>();
+        q.tids = xb->tids.as<int>();
+        q.twt = xb->tw.as<cx<T>>();
+        q.S = xb->S;
+        CU(launch_xcorr<T>(xb->log2p, false, xb->mode, q, xb->nblocks, xb->ngroups, mf->stream));
+        ++mf->launches;
+    }
     if (p.pk_on)
     {
         mf->pk_fused = true;
@@ -1197,8 +1419,10 @@ mfgpu_status mfgpu_mf_find_peaks(mfgpu_mf *mf, double threshold, int min_distanc
     // tensor-core correlator flagged the 64-lag chunks above the threshold
     const bool fused = match && !mf->tc && len == mf->pk_fused_len;
     const unsigned *flags = match && mf->tc ? mf->pk_flags.as<unsigned>() : nullptr;
-    FusedSlots<float> ff{mf->pk_cnt.as<int>(), mf->pk_idx.as<int>(), mf->pk_val.as<float>(), mf->nblocks, mf->S};
-    FusedSlots<double> fd{mf->pk_cnt.as<int>(), mf->pk_idx.as<int>(), mf->pk_val.as<double>(), mf->nblocks, mf->S};
+    FusedSlots<float> ff{mf->pk_cnt.as<int>(), mf->pk_idx.as<int>(), mf->pk_val.as<float>(), mf->pk_stride, mf->S,
+                         mf->row_S.as<int>(), mf->row_nblk.as<int>()};
+    FusedSlots<double> fd{mf->pk_cnt.as<int>(), mf->pk_idx.as<int>(), mf->pk_val.as<double>(), mf->pk_stride, mf->S,
+                          mf->row_S.as<int>(), mf->row_nblk.as<int>()};
     int rc = mf->prec == 4
                  ? run_peaks<float>(mf->rho.as<float>(), mf->ldr, rows.data(), mf->nt, len, threshold, min_distance,
                                     mf->pk, mf->stream, &mf->launches, mf->pk_off.data(), err, fused ? &ff : nullptr,

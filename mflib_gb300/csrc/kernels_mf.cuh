@@ -55,10 +55,11 @@ template <class T> struct XcorrParams
     int *err;
     // fused peak candidates (pk_on != 0): lags [k0+1, k0+S-2] of block b of
     // template t that pass the candidate rule on a trace of pk_len lags with
-    // threshold pk_thr go to slot (t * gridDim.x + b): count pk_cnt (zeroed
+    // threshold pk_thr go to slot (t * pk_stride + b): count pk_cnt (zeroed
     // before the launch; may exceed kPkCap), up to kPkCap (index, value)
     // pairs in pk_idx / pk_val, in no particular order.
     int pk_on;
+    int pk_stride;
     int pk_len;
     T pk_thr;
     int *pk_cnt;
@@ -798,7 +799,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
                     const T xr = l + 1 < kmax ? __ldcg(Rt + l + 1) : (T) 0;  // unused at the trace's last lag
                     if (cand_rule<T>(__ldcg(Rt + l - 1), xi, xr, k0 + l, pk_n, pk_thr))
                     {
-                        const long slot = (long) t * gridDim.x + blockIdx.x;
+                        const long slot = (long) t * p.pk_stride + blockIdx.x;
                         const int pos = atomicAdd(p.pk_cnt + slot, 1);
                         if (pos < kPkCap)
                         {

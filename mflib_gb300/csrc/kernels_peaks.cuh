@@ -334,9 +334,16 @@ static __global__ void peak_seam_kernel(PeakTraces<T> tr, int ntr, FusedSlots<T>
     if (g >= (long) ntr * fs.nblk) return;
     const int trace = (int) (g / fs.nblk), b = (int) (g % fs.nblk);
     const int row = tr.row[trace];
+    if (fs.row_nblk && b >= fs.row_nblk[row])
+    {
+        counts[g] = 0;  // past the last block of this template's plan
+        ht[g] = 0;
+        return;
+    }
+    const long S = fs.row_S ? fs.row_S[row] : fs.S;
     const T *x = tr.x + (long) row * tr.ldx;
     const long n = tr.len;
-    const long i0 = (long) b * fs.S, i1 = i0 + fs.S - 1;
+    const long i0 = (long) b * S, i1 = i0 + S - 1;
     const int h = (i0 < n && is_candidate<T>(x, (int) i0, (int) n, tr.thr)) ? 1 : 0;
     const int tl = (i1 < n && is_candidate<T>(x, (int) i1, (int) n, tr.thr)) ? 1 : 0;
     counts[g] = h + fs.cnt[(long) row * fs.nblk + b] + tl;
@@ -384,11 +391,12 @@ static __global__ void __launch_bounds__(kPkThreads)
         const long long off = offs[slot];
         if (lane == 0 && off + cnt > cap) *overflow = 1;
         const int hv = ht[slot];
-        const long i0 = (long) b * fs.S;
+        const long S = fs.row_S ? fs.row_S[row] : fs.S;
+        const long i0 = (long) b * S;
         if (lane == 0)
         {
             if (hv & 1) put(off, i0, x[i0]);
-            if (hv & 2) put(off + cnt - 1, i0 + fs.S - 1, x[i0 + fs.S - 1]);
+            if (hv & 2) put(off + cnt - 1, i0 + S - 1, x[i0 + S - 1]);
         }
         const long long boff = off + (hv & 1);
         const long bs = (long) row * fs.nblk + b;
@@ -406,7 +414,7 @@ static __global__ void __launch_bounds__(kPkThreads)
             }
             continue;
         }
-        const long lo = i0 + 1, hi = (i0 + fs.S - 1 < n) ? i0 + fs.S - 1 : n;
+        const long lo = i0 + 1, hi = (i0 + S - 1 < n) ? i0 + S - 1 : n;
         long long base = boff;
         for (long c0 = lo; c0 < hi; c0 += 32 * kPkPer)
         {

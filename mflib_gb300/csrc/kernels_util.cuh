@@ -21,8 +21,11 @@ template <class T> struct FusedSlots
     const int *cnt;
     const int *idx;
     const T *val;
-    int nblk;
+    int nblk;                   // slot row stride (the largest block count)
     int S;
+    // per row (template) when the plans differ (length buckets), else null
+    const int *row_S = nullptr;
+    const int *row_nblk = nullptr;
 };
 
 template <class T> __device__ __forceinline__ int sgn(T d) { return d > (T) 0 ? 1 : (d < (T) 0 ? -1 : 0); }

@@ -165,7 +165,8 @@ class MatchedFilter:
     def dtype(self):
         return self._dtype
 
-    def initialize(self, params, template_channels=None, n_channels=None, fft_length=0, correlator_variant=0):
+    def initialize(self, params, template_channels=None, n_channels=None, fft_length=0, correlator_variant=0,
+                   length_buckets=0):
         """MatchedFilter<T>::initialize (src/matchedFilter.cpp:507-821).
 
         Extensions: ``template_channels`` (one channel index per template,
@@ -175,7 +176,9 @@ class MatchedFilter:
         1 whole CTA, 2 whole CTA with spectrum prefetch, 3 two teams per CTA,
         templates of one length only; 4 split-precision tensor-core
         correlation, FP32 and templates of one length; 5 two teams with the
-        normalisation computed inside each CTA, templates of one length)."""
+        normalisation computed inside each CTA, templates of one length);
+        ``length_buckets`` caps the length buckets of a mixed-length bank
+        (0 automatic, 1 one plan for every template)."""
         if not isinstance(params, MatchedFilterParameters) or not params.is_valid():
             raise ValueError("Parameters are invalid")
         tmpls = [params.get_template(i) for i in range(params.get_number_of_templates())]
@@ -207,6 +210,7 @@ class MatchedFilter:
             p.template_channel = chans.ctypes.data_as(C.POINTER(C.c_int))
         p.fft_length = int(fft_length)
         p.correlator_variant = int(correlator_variant)
+        p.length_buckets = int(length_buckets)
         _lib.call("mfgpu_mf_initialize", self._h, C.byref(p))
         self._params = params
         self._nt = nt
@@ -370,8 +374,12 @@ class MatchedFilter:
         _lib.call("mfgpu_mf_get_plan", self._h, C.byref(a), C.byref(b), C.byref(c))
         v, g, k = C.c_int(), C.c_int(), C.c_int()
         _lib.call("mfgpu_mf_get_correlator", self._h, C.byref(v), C.byref(g), C.byref(k))
+        cnt = C.c_int()
+        fl, ntb = (C.c_int * 8)(), (C.c_int * 8)()
+        _lib.call("mfgpu_mf_get_buckets", self._h, 8, fl, ntb, C.byref(cnt))
         return {"fft_length": a.value, "lags_per_block": b.value, "n_blocks": c.value, "correlator": v.value,
-                "tc_group": g.value, "tc_k": k.value}
+                "tc_group": g.value, "tc_k": k.value,
+                "buckets": [(fl[i], ntb[i]) for i in range(min(8, cnt.value))]}
 
     def last_timings(self):
         a, b = C.c_float(), C.c_float()

@@ -77,10 +77,12 @@ def test_single_channel_hour(gpu, oracle, dtype):
             assert np.min(np.abs(pk - o)) <= 1
 
 
-def test_uneven_bank(gpu, oracle):
+@pytest.mark.parametrize("buckets", [0, 1, 2, 3])
+def test_uneven_bank(gpu, oracle, buckets):
     """Templates of 200..3,000 samples with random 1..15 Hz pass bands, each
     assigned to one of 6 channels (the 2,000-template bank's recipe at 60
-    templates and 120,000 samples per channel)."""
+    templates and 120,000 samples per channel), with the planner's length
+    buckets, one plan, and at most two or three buckets."""
     mf = gpu
     rng = np.random.default_rng(200)
     nt, nch, n = 60, 6, 120_000
@@ -93,7 +95,13 @@ def test_uneven_bank(gpu, oracle):
     chan = rng.integers(0, nch, nt)
     sigs = [_bp(np.random.default_rng(300 + c).standard_normal(n), 1.0, 15.0).astype(np.float32) for c in range(nch)]
     f = mf.MultiChannel.MatchedFilter(dtype=np.float32)
-    f.initialize(_params(mf, tps, n), template_channels=chan, n_channels=nch)
+    f.initialize(_params(mf, tps, n), template_channels=chan, n_channels=nch, length_buckets=buckets)
+    bk = f.get_plan()["buckets"]
+    assert sum(c for _, c in bk) == nt
+    if buckets == 1:
+        assert len(bk) == 1
+    if buckets > 1:
+        assert 1 < len(bk) <= buckets, bk
     f.set_channel_signals(np.stack(sigs))
     f.apply()
     ref = oracle.matched_filter(tps, [sigs[c] for c in chan], multi=True, fp64_from_f32=True)

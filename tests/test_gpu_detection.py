@@ -251,16 +251,21 @@ def test_fused_peak_candidates(gpu, oracle, rng, dtype, variant, fft_length):
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
-def test_fused_peak_candidates_mixed_lengths(gpu, oracle, rng, dtype):
+@pytest.mark.parametrize("plan", ["fft2048", "buckets"])
+def test_fused_peak_candidates_mixed_lengths(gpu, oracle, rng, dtype, plan):
     """Templates of several lengths: the peak trace stops at n - Lmax + 1
-    lags, inside the shorter templates' valid range."""
+    lags, inside the shorter templates' valid range; with length buckets the
+    templates' blocks differ in length and number."""
     mf = gpu
-    lens = [90, 200, 333, 120, 201]
+    lens = [90, 200, 333, 120, 201] + ([1500, 1700] if plan == "buckets" else [])
     p, chans, assign = _fused_case(mf, rng, dtype, lens, n=45_001)
-    f = _filter(mf, p, chans, assign, dtype, fft_length=2048)
+    kw = dict(fft_length=2048) if plan == "fft2048" else dict(length_buckets=3)
+    f = _filter(mf, p, chans, assign, dtype, **kw)
+    if plan == "buckets":
+        assert len(f.get_plan()["buckets"]) > 1
     f.set_peak_threshold(0.0)
     f.apply()
-    plain = _filter(mf, p, chans, assign, dtype, fft_length=2048)
+    plain = _filter(mf, p, chans, assign, dtype, **kw)
     plain.apply()
     for md in (0, 25):
         f.find_peaks(0.0, md)
