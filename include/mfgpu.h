@@ -190,6 +190,41 @@ mfgpu_status mfgpu_mf_set_window(mfgpu_mf *mf, int n_src, int n, const void *x, 
 /* Device bytes the object holds (its buffers and peak-finder scratch), for
  * admission against a memory budget.  Extension: no reference counterpart. */
 mfgpu_status mfgpu_mf_get_device_bytes(const mfgpu_mf *mf, unsigned long long *bytes);
+/* ---- single-channel detector (MFLib::SingleChannel::Detector<T>,
+ * src/singleChannel/detector.cpp:419-691) over the last apply's traces. */
+typedef struct
+{
+    double threshold;       /* DetectorParameters::setDetectionThreshold, clamped to [0, 1] */
+    int min_distance;       /* setMinimumDetectionSpacing (samples) */
+    int absolute_maximum;   /* MaximumMatchedFilterPolicy: 0 MAXIMUM, 1 ABSOLUTE_MAXIMUM */
+    int single;             /* MatchedFilteredSignalDetectorPolicy: 0 REDUCED, 1 SINGLE */
+    int interpolation;      /* DetectionTimeInterpolationType: 0 LANCZOS, 1 QUADRATIC, 2 NONE */
+    int lanczos_alpha;      /* DetectionTimeInterpolationParameters (51) */
+    int lanczos_points;     /* (100) */
+    double sampling_rate;   /* of the templates, Hz */
+    int amplitudes;         /* wantAmplitudeScalingFactor */
+} mfgpu_detect_params;
+
+typedef struct
+{
+    int template_index;
+    int sample;                   /* lag of the detection */
+    double correlation;           /* the template's coefficient there, clamped to [-1, 1] */
+    double detection_time;        /* sample / sampling_rate */
+    double interpolated_time;     /* detection_time + refinement */
+    int sign;                     /* sign of the coefficient (-1, 0, 1): polarity factor */
+    int have_amplitude;
+    double gibbons_ringdal;       /* amplitude scaling factors of the detected window */
+    double schaff_richards;
+} mfgpu_detection;
+
+/* Detector::detect: reduce (REDUCED) or keep (SINGLE) the traces, PeakFinder,
+ * then per detection the refined time, polarity factor and amplitudes; the
+ * detections stay in the object (REDUCED: lag order; SINGLE: by time, then
+ * template). */
+mfgpu_status mfgpu_mf_detect(mfgpu_mf *mf, const mfgpu_detect_params *params, int *n_detections);
+/* Copies up to max detections of the last mfgpu_mf_detect. */
+mfgpu_status mfgpu_mf_get_detections(mfgpu_mf *mf, int max, mfgpu_detection *out, int *n);
 /* Block until the object's stream is idle; reports device-side errors. */
 mfgpu_status mfgpu_mf_synchronize(mfgpu_mf *mf);
 /* Device time (ms) of the last apply's correlation kernel and of the whole

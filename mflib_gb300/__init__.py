@@ -13,6 +13,11 @@ from .matched_filter import (MatchedFilter, MatchedFilterParameters, MultiChanne
                              compute_optimal_fft_and_block_length)
 from .detection import DBSCAN, PeakFinder
 from ._lib import MfgpuError, MfgpuTimeout
+from .detector import (DetectionTimeInterpolationType, MatchedFilteredSignalDetectorPolicy,
+                       MaximumMatchedFilterPolicy, RelativeMagnitudeType)
+from .matched_filter import _attach_detector
+
+_attach_detector()
 
 __version__ = "1.0.0"
 
@@ -20,4 +25,6 @@ __all__ = [
     "DBSCAN", "MatchedFilter", "MatchedFilterDetectionMode", "MatchedFilterImplementation",
     "MatchedFilterParameters", "MfgpuError", "MfgpuTimeout", "MultiChannel", "NetworkStationPhase",
     "PeakFinder", "Polarity", "SingleChannel", "WaveformTemplate", "compute_optimal_fft_and_block_length",
+    "DetectionTimeInterpolationType", "MatchedFilteredSignalDetectorPolicy", "MaximumMatchedFilterPolicy",
+    "RelativeMagnitudeType",
 ]

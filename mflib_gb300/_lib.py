@@ -27,6 +27,34 @@ class MfgpuTimeout(MfgpuError):
     """A bounded device-side wait gave up (MFGPU_ETIMEOUT)."""
 
 
+class MfgpuDetectParams(C.Structure):
+    _fields_ = [
+        ("threshold", C.c_double),
+        ("min_distance", C.c_int),
+        ("absolute_maximum", C.c_int),
+        ("single", C.c_int),
+        ("interpolation", C.c_int),
+        ("lanczos_alpha", C.c_int),
+        ("lanczos_points", C.c_int),
+        ("sampling_rate", C.c_double),
+        ("amplitudes", C.c_int),
+    ]
+
+
+class MfgpuDetection(C.Structure):
+    _fields_ = [
+        ("template_index", C.c_int),
+        ("sample", C.c_int),
+        ("correlation", C.c_double),
+        ("detection_time", C.c_double),
+        ("interpolated_time", C.c_double),
+        ("sign", C.c_int),
+        ("have_amplitude", C.c_int),
+        ("gibbons_ringdal", C.c_double),
+        ("schaff_richards", C.c_double),
+    ]
+
+
 class MfgpuParams(C.Structure):
     _fields_ = [
         ("detection_mode", C.c_int),
@@ -77,6 +105,8 @@ _SIGS = {
     "mfgpu_mf_get_plan": ([_vp, _ip, _ip, _ip], C.c_int),
     "mfgpu_mf_get_correlator": ([_vp, _ip, _ip, _ip], C.c_int),
     "mfgpu_mf_get_buckets": ([_vp, C.c_int, _ip, _ip, _ip], C.c_int),
+    "mfgpu_mf_detect": ([_vp, C.POINTER(MfgpuDetectParams), _ip], C.c_int),
+    "mfgpu_mf_get_detections": ([_vp, C.c_int, C.POINTER(MfgpuDetection), _ip], C.c_int),
     "mfgpu_mf_set_window": ([_vp, C.c_int, C.c_int, _vp, C.c_long], C.c_int),
     "mfgpu_mf_get_device_bytes": ([_vp, C.POINTER(C.c_ulonglong)], C.c_int),
     "mfgpu_mf_synchronize": ([_vp], C.c_int),

@@ -15,6 +15,7 @@
 #include <vector>
 #include "mfgpu.h"
 #include "launch.h"
+#include "kernels_detect.cuh"
 
 using namespace mfgpu;
 
@@ -169,6 +170,10 @@ struct mfgpu_mf
     // template its bucket's block length and block count, and the slot row
     // stride of the gathered candidates (the largest block count)
     std::vector<std::unique_ptr<MfBucket>> xb;
+    // single-channel detector: reduced trace and argmax (or transformed
+    // traces), detection rows and results
+    DevBuf det_buf, det_id, det_rows, det_out, tchan_d;
+    std::vector<mfgpu_detection> dets;
     int ntemplates0 = 0;
     DevBuf row_S, row_nblk;
     int pk_stride = 0;
@@ -186,6 +191,11 @@ struct mfgpu_mf
         pk.each_buf(f);
         f(row_S);
         f(row_nblk);
+        f(det_buf);
+        f(det_id);
+        f(det_rows);
+        f(det_out);
+        f(tchan_d);
         for (auto &b : xb) b->each_buf(f);
     }
     void release_device()
@@ -209,6 +219,7 @@ struct mfgpu_mf
         pk_req = -1;
         nt = n = maxLen = minLen = nch = 0;
         xb.clear();
+        dets.clear();
         ntemplates0 = pk_stride = 0;
         lens.clear(); tchan.clear(); nvalid.clear(); tmpl.clear(); toff.clear();
         shifts.clear(); weights.clear(); pk_off.clear();
@@ -753,6 +764,8 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
     CU(cudaMemcpyAsync(mf->nvalid_d.p, mf->nvalid.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, mf->stream));
     CU(cudaMemcpyAsync(mf->tmpl_d.p, mf->tmpl.data(), sizeof(double) * tot, cudaMemcpyHostToDevice, mf->stream));
     CU(cudaMemcpyAsync(mf->toff_d.p, mf->toff.data(), sizeof(long) * nt, cudaMemcpyHostToDevice, mf->stream));
+    CU(mf->tchan_d.ensure(sizeof(int) * nt));
+    CU(cudaMemcpyAsync(mf->tchan_d.p, mf->tchan.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, mf->stream));
     CU(mf->xrange.ensure(sizeof(float) * nch));
     CU(cudaMemsetAsync(mf->xrange.p, 0, sizeof(float) * nch, mf->stream));
     mfgpu_status s2 = mf->prec == 4 ? mf_upload_tables<float>(mf, mf->log2p, mf->tw, mf->Bc)
@@ -1432,6 +1445,127 @@ mfgpu_status mfgpu_mf_find_peaks(mfgpu_mf *mf, double threshold, int min_distanc
                                      fused ? &fd : nullptr);
     if (rc != 0) return fail(MFGPU_ECUDA, err);
     mf->have_peaks = true;
+    return MFGPU_OK;
+}
+
+template <class T> static mfgpu_status mf_detect(mfgpu_mf *mf, const mfgpu_detect_params *dp, long len)
+{
+    const double thr = std::min(1.0, std::max(0.0, dp->threshold));
+    const int nt = mf->nt;
+    const T *rho = mf->rho.as<T>();
+    std::vector<int> rows_host;
+    std::vector<long long> off(nt + 1, 0);
+    std::string err;
+    int ndet = 0;
+    mf->have_peaks = false;  // the peak workspace is reused below
+    if (!dp->single)
+    {
+        CU(mf->det_buf.ensure(sizeof(T) * (size_t) len));
+        CU(mf->det_id.ensure(sizeof(int) * (size_t) len));
+        CU(launch_det_reduce<T>(rho, mf->ldr, nt, len, dp->absolute_maximum, mf->det_buf.as<T>(),
+                                mf->det_id.as<int>(), mf->stream));
+        ++mf->launches;
+        const int row0 = 0;
+        if (run_peaks<T>(mf->det_buf.as<T>(), 0, &row0, 1, (int) len, thr, dp->min_distance, mf->pk, mf->stream,
+                         &mf->launches, off.data(), err) != 0)
+            return fail(MFGPU_ECUDA, err);
+        ndet = (int) off[1];
+        rows_host.assign(ndet, -1);
+    }
+    else
+    {
+        CU(mf->det_buf.ensure(sizeof(T) * (size_t) nt * mf->ldr));
+        CU(launch_det_single<T>(rho, mf->ldr, nt, len, dp->absolute_maximum, mf->det_buf.as<T>(), mf->stream));
+        ++mf->launches;
+        std::vector<int> rows(nt);
+        for (int t = 0; t < nt; ++t) rows[t] = t;
+        if (run_peaks<T>(mf->det_buf.as<T>(), mf->ldr, rows.data(), nt, (int) len, thr, dp->min_distance, mf->pk,
+                         mf->stream, &mf->launches, off.data(), err) != 0)
+            return fail(MFGPU_ECUDA, err);
+        ndet = (int) off[nt];
+        rows_host.resize(ndet);
+        for (int t = 0; t < nt; ++t)
+            for (long long i = off[t]; i < off[t + 1]; ++i) rows_host[i] = t;
+    }
+    mf->dets.clear();
+    if (ndet == 0) return MFGPU_OK;
+    CU(mf->det_rows.ensure(sizeof(int) * (size_t) ndet));
+    CU(mf->det_out.ensure(sizeof(DetectOut) * (size_t) ndet));
+    CU(mf->det_id.ensure(sizeof(int)));
+    CU(cudaMemcpyAsync(mf->det_rows.p, rows_host.data(), sizeof(int) * ndet, cudaMemcpyHostToDevice, mf->stream));
+    DetectParams q{};
+    q.peak = mf->pk.peaks.as<int>();
+    q.row = mf->det_rows.as<int>();
+    q.id = mf->det_id.as<int>();
+    q.ndet = ndet;
+    q.len = len;
+    q.use_abs = dp->absolute_maximum;
+    q.interp = dp->interpolation;
+    q.alpha = dp->lanczos_alpha;
+    q.nrefine = dp->lanczos_points;
+    q.dt = 1.0 / dp->sampling_rate;
+    q.amplitudes = dp->amplitudes;
+    q.tmpl = mf->tmpl_d.as<double>();
+    q.toff = mf->toff_d.as<long>();
+    q.tlen = mf->tlen_d.as<int>();
+    q.tchan = mf->tchan_d.as<int>();
+    q.n = mf->n;
+    q.out = mf->det_out.as<DetectOut>();
+    CU(launch_det_refine<T>(rho, mf->ldr, mf->x.as<T>(), mf->ldx, q, mf->stream));
+    ++mf->launches;
+    std::vector<DetectOut> out(ndet);
+    CU(cudaMemcpyAsync(out.data(), mf->det_out.p, sizeof(DetectOut) * ndet, cudaMemcpyDeviceToHost, mf->stream));
+    CU(cudaStreamSynchronize(mf->stream));
+    const double dt = 1.0 / dp->sampling_rate;
+    mf->dets.resize(ndet);
+    for (int i = 0; i < ndet; ++i)
+    {
+        const DetectOut &o = out[i];
+        mfgpu_detection &d = mf->dets[i];
+        d.template_index = o.tmpl;
+        d.sample = o.sample;
+        d.correlation = o.xc;
+        d.detection_time = o.sample * dt;
+        d.interpolated_time = d.detection_time + o.shift;
+        d.sign = o.sign;
+        d.have_amplitude = o.have_amp;
+        d.gibbons_ringdal = o.gr;
+        d.schaff_richards = o.sr;
+    }
+    if (dp->single)
+        std::stable_sort(mf->dets.begin(), mf->dets.end(), [](const mfgpu_detection &a, const mfgpu_detection &b) {
+            return a.detection_time < b.detection_time;
+        });
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_detect(mfgpu_mf *mf, const mfgpu_detect_params *dp, int *n_detections)
+{
+    MF_CHECK_INIT(mf);
+    DeviceGuard g(mf->dev);
+    if (!dp) return fail(MFGPU_EINVAL, "params is NULL");
+    if (!mf->have) return fail(MFGPU_EINVAL, "Matched filtered signals not computed");
+    if (dp->interpolation < 0 || dp->interpolation > 2) return fail(MFGPU_EINVAL, "invalid interpolation type");
+    if (dp->interpolation == 0 && (dp->lanczos_alpha < 1 || dp->lanczos_points < 1))
+        return fail(MFGPU_EINVAL, "Lanczos alpha and points must be positive");
+    if (!(dp->sampling_rate > 0)) return fail(MFGPU_EINVAL, "sampling rate must be positive");
+    const long len = (long) mf->n - mf->maxLen + 1;  // getFilteredSignalLength
+    if (len < 1) return fail(MFGPU_EINVAL, "Matched filtered signal length is 0");
+    mfgpu_status st = mf_sync(mf);
+    if (st != MFGPU_OK) return st;
+    st = mf->prec == 4 ? mf_detect<float>(mf, dp, len) : mf_detect<double>(mf, dp, len);
+    if (st != MFGPU_OK) return st;
+    if (n_detections) *n_detections = (int) mf->dets.size();
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_get_detections(mfgpu_mf *mf, int max, mfgpu_detection *out, int *n)
+{
+    MF_CHECK_INIT(mf);
+    const int nd = (int) mf->dets.size();
+    if (n) *n = nd;
+    if (max > 0 && !out) return fail(MFGPU_EINVAL, "out is NULL");
+    for (int i = 0; i < nd && i < max; ++i) out[i] = mf->dets[i];
     return MFGPU_OK;
 }
 

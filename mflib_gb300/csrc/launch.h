@@ -40,6 +40,15 @@ size_t tc_smem_bytes(int Kp, int Gp);
 cudaError_t launch_tc_bank(const double *tmpl, const long *toff, const int *tlen, const int *grp_tid, int ngroups,
                            int Gp, int Kp, __half *B, float *bscale, cudaStream_t s);
 cudaError_t launch_tc_xcorr(const TcParams &p, int nctas, cudaStream_t s);
+// single-channel detector (kernels_detect.cuh): reduction across templates,
+// per-template transformed traces, per-detection refinement and amplitudes
+template <class T>
+cudaError_t launch_det_reduce(const T *rho, long ldr, int nt, long len, int use_abs, T *det, int *id, cudaStream_t s);
+template <class T>
+cudaError_t launch_det_single(const T *rho, long ldr, int nt, long len, int use_abs, T *out, cudaStream_t s);
+template <class T>
+cudaError_t launch_det_refine(const T *rho, long ldr, const T *x, long ldx, const struct DetectParams &q,
+                              cudaStream_t s);
 // reference debug spectrum of one prepared template at FFT length nfft
 template <class T> cudaError_t launch_ref_spectrum(const double *tmpl, int L, int nfft, T *out, cudaStream_t s);
 // shift and stack (src/matchedFilter.cpp:1319-1364)

@@ -485,3 +485,10 @@ class _SingleChannel:
 
 MultiChannel = _MultiChannel
 SingleChannel = _SingleChannel
+
+
+def _attach_detector():
+    # pymflib.SingleChannel.{Detector, DetectorParameters, Detection, ...}
+    from . import detector as d
+    for name in ("Detector", "DetectorParameters", "DetectionTimeInterpolationParameters", "Detection"):
+        setattr(_SingleChannel, name, getattr(d, name))

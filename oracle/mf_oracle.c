@@ -14,6 +14,8 @@
  *   orc_shift_and_stack  src/matchedFilter.cpp:577-592, :1319-1364
  *   orc_pearson_naive    testing/utilities.hpp:33-69 (two-pass FP64 Pearson)
  *   orc_peaks            src/peakFinder.cpp:329-446
+ *   orc_detect_f / _d    src/singleChannel/detector.cpp:38-284, :419-691
+ *                        and src/singleChannel/relativeMagnitude.cpp:35-130
  *   orc_dbscan           src/dbscan.cpp:187-214 -> Intel DAAL dbscan::Batch
  *                        (third-party, not vendored; restated from DAAL's
  *                        published algorithm, see the function comment)
@@ -334,3 +336,154 @@ ORC_API int orc_dbscan(int nobs, int nf, const double *X, const double *w,
     free(core);
     return ncl;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Single-channel detector: Detector<T>::detect (src/singleChannel/
+ * detector.cpp:419-691) for one matched-filter object, T = float or double:
+ *   reduceAllCorrelations / setCorrelations + cleanReducedTemplate
+ *   (:191-284), PeakFinder (orc_peaks), then per detection the clamped
+ *   coefficient of the chosen template, the sign of its coefficient, the
+ *   refinement quadraticRefinement (:38-91, double, returned as T) or
+ *   lanczosRefinement (:93-152, in T), and the relative amplitudes of
+ *   RelativeMagnitude (src/singleChannel/relativeMagnitude.cpp:35-130) in
+ *   double with the window mean (the double overload's semantics).
+ * SINGLE-policy detections are ordered by time, ties in template order. */
+static double orc_quadratic(long n, const double *ys, long p, double dt, int use_abs)
+{
+    if (!(p > 0 && p < n - 1)) { return 0.0; }
+    double y1 = ys[0], y2 = ys[1], y3 = ys[2];
+    if (use_abs) { y1 = fabs(y1); y2 = fabs(y2); y3 = fabs(y3); }
+    if (y2 < y1 || y2 < y3)
+    {
+        if (y2 < y1 && y2 < y3) { y1 = -y1; y2 = -y2; y3 = -y3; }
+        else { return 0.0; }
+    }
+    y1 = fmin(y2 - 100 * DBL_EPSILON, y1);
+    y3 = fmin(y2 - 100 * DBL_EPSILON, y3);
+    return (dt * (y1 - y3)) / (2 * (y1 - 2 * y2 + y3));
+}
+
+typedef struct { int t; int p; } orc_det_pair;
+
+static int orc_det_cmp(const void *a, const void *b)
+{
+    const orc_det_pair *x = (const orc_det_pair *) a, *y = (const orc_det_pair *) b;
+    if (x->p != y->p) { return x->p < y->p ? -1 : 1; }
+    return x->t < y->t ? -1 : (x->t > y->t);
+}
+
+#define ORC_DETECT(NAME, T, SINF, TEPS, TMAX)                                                            \
+static T NAME##_sinc(T x)                                                                                   \
+{                                                                                                           \
+    const T tol = TEPS * (T) 100;                                                                           \
+    if (fabs((double) x) > tol) { T pix = (T) (3.14159265358979323846 * (double) x); return SINF(pix) / pix; } \
+    return (T) 1;                                                                                           \
+}                                                                                                           \
+static T NAME##_lanczos(T x, int a)                                                                         \
+{                                                                                                           \
+    if ((int) fabs((double) x) <= a) { return NAME##_sinc(x) * NAME##_sinc(x / (T) a); }                   \
+    return (T) 0;                                                                                           \
+}                                                                                                           \
+ORC_API int NAME(int nt, long len, const T *rho, long ldr, int use_abs, int single, double thr,            \
+                 int min_dist, int interp, int alpha, int nrefine, double fs, int amplitudes,              \
+                 const int *tlen, const double *const *templates, const T *const *signals, long n,         \
+                 int maxdet, int *o_tmpl, int *o_sample, double *o_xc, double *o_shift, int *o_sign,       \
+                 int *o_have, double *o_gr, double *o_sr)                                                   \
+{                                                                                                           \
+    double *det = (double *) malloc(sizeof(double) * (size_t) (len > 0 ? len : 1));                        \
+    int *pk = (int *) malloc(sizeof(int) * (size_t) (len > 0 ? len : 1));                                  \
+    int *id = (int *) calloc((size_t) (len > 0 ? len : 1), sizeof(int));                                   \
+    orc_det_pair *pairs = NULL;                                                                             \
+    int np = 0, cap = 0;                                                                                    \
+    for (int pass = 0; pass < (single ? nt : 1); ++pass)                                                    \
+    {                                                                                                       \
+        for (long k = 0; k < len; ++k)                                                                      \
+        {                                                                                                   \
+            T best = rho[(long) (single ? pass : 0) * ldr + k];                                             \
+            if (use_abs) { best = (T) fabs((double) best); }                                                \
+            int bi = single ? pass : 0;                                                                     \
+            if (!single)                                                                                    \
+                for (int t = 1; t < nt; ++t)                                                                \
+                {                                                                                           \
+                    T v = rho[(long) t * ldr + k];                                                          \
+                    if (use_abs) { v = (T) fabs((double) v); }                                              \
+                    if (v > best) { best = v; bi = t; }                                                     \
+                }                                                                                           \
+            if (best > (T) 1) { best = (T) 1; }                                                             \
+            if (best < (T) -1) { best = (T) -1; }                                                           \
+            det[k] = (double) best;                                                                         \
+            id[k] = bi;                                                                                     \
+        }                                                                                                   \
+        int m = orc_peaks((int) len, det, thr, min_dist, pk);                                              \
+        if (np + m > cap)                                                                                   \
+        {                                                                                                   \
+            cap = 2 * (np + m) + 16;                                                                        \
+            pairs = (orc_det_pair *) realloc(pairs, sizeof(orc_det_pair) * (size_t) cap);                   \
+        }                                                                                                   \
+        for (int i = 0; i < m; ++i) { pairs[np].t = id[pk[i]]; pairs[np].p = pk[i]; ++np; }                 \
+    }                                                                                                       \
+    if (single && np > 1) { qsort(pairs, (size_t) np, sizeof(orc_det_pair), orc_det_cmp); }               \
+    const double dt = 1.0 / fs;                                                                             \
+    for (int d = 0; d < np && d < maxdet; ++d)                                                              \
+    {                                                                                                       \
+        const int it = pairs[d].t;                                                                          \
+        const long p = pairs[d].p;                                                                          \
+        const T *xc = rho + (long) it * ldr;                                                                \
+        const T v = xc[p];                                                                                  \
+        T c = v > (T) 1 ? (T) 1 : (v < (T) -1 ? (T) -1 : v);                                                \
+        o_tmpl[d] = it; o_sample[d] = (int) p; o_xc[d] = (double) c;                                        \
+        o_sign[d] = v < (T) 0 ? -1 : (v == (T) 0 ? 0 : 1);                                                  \
+        double shift = 0.0;                                                                                 \
+        if (interp == 1)                                                                                    \
+        {                                                                                                   \
+            double ys[3] = {0.0, 0.0, 0.0};                                                                 \
+            if (p > 0 && p < len - 1) { ys[0] = xc[p - 1]; ys[1] = xc[p]; ys[2] = xc[p + 1]; }              \
+            shift = (double) (T) orc_quadratic(len, ys, p, dt, use_abs);                                    \
+        }                                                                                                   \
+        else if (interp == 0)                                                                               \
+        {                                                                                                   \
+            const T dtw = (T) (1.0 / (double) nrefine);                                                     \
+            T opt = 0, ymax = -TMAX;                                                                        \
+            for (int idx = 1; idx < nrefine; ++idx)                                                         \
+            {                                                                                               \
+                const T sh = (T) (-0.5 + (double) (dtw * (T) idx));                                         \
+                const T x = (T) p + sh;                                                                     \
+                T y = 0;                                                                                    \
+                const int fl = (int) floor((double) x);                                                     \
+                for (int a = -alpha; a <= alpha; ++a)                                                       \
+                {                                                                                           \
+                    const int i = fl - a + 1;                                                               \
+                    const T xi = x - (T) i;                                                                 \
+                    const T xv = (i >= 0 && i < len) ? xc[i] : (T) 0;                                       \
+                    y = y + xv * NAME##_lanczos(xi, alpha);                                                 \
+                }                                                                                           \
+                if (use_abs) { y = (T) fabs((double) y); }                                                  \
+                if (y > ymax) { opt = (T) (dt * (double) sh); ymax = y; }                                   \
+            }                                                                                               \
+            shift = (double) opt;                                                                           \
+        }                                                                                                   \
+        o_shift[d] = shift;                                                                                 \
+        o_have[d] = 0; o_gr[d] = 0; o_sr[d] = 0;                                                            \
+        const int L = tlen[it];                                                                             \
+        if (amplitudes && p + L <= n)                                                                       \
+        {                                                                                                   \
+            const double *b = templates[it];                                                                \
+            const T *y = signals[it] + p;                                                                   \
+            double sb = 0, sy = 0;                                                                          \
+            for (int j = 0; j < L; ++j) { sb += b[j]; sy += (double) y[j]; }                                \
+            const double mb = sb / L, my = sy / L;                                                          \
+            double bb = 0, yy = 0, by = 0;                                                                  \
+            for (int j = 0; j < L; ++j)                                                                     \
+            {                                                                                               \
+                const double db = b[j] - mb, dy = (double) y[j] - my;                                       \
+                bb += db * db; yy += dy * dy; by += db * dy;                                                \
+            }                                                                                               \
+            if (bb > 0 && yy > 0) { o_have[d] = 1; o_gr[d] = fabs(by) / bb; o_sr[d] = sqrt(yy / bb); }      \
+        }                                                                                                   \
+    }                                                                                                       \
+    free(det); free(pk); free(id); free(pairs);                                                             \
+    return np;                                                                                              \
+}
+
+ORC_DETECT(orc_detect_f, float, sinf, FLT_EPSILON, FLT_MAX)
+ORC_DETECT(orc_detect_d, double, sin, DBL_EPSILON, DBL_MAX)

@@ -49,6 +49,11 @@ class Oracle:
         L.orc_peaks.restype = C.c_int
         L.orc_dbscan.argtypes = [C.c_int, C.c_int, _dp, _dp, C.c_double, C.c_int, _ip]
         L.orc_dbscan.restype = C.c_int
+        for nm in ("orc_detect_f", "orc_detect_d"):
+            getattr(L, nm).argtypes = [C.c_int, C.c_long, C.c_void_p, C.c_long, C.c_int, C.c_int, C.c_double,
+                                       C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, _ip, C.c_void_p,
+                                       C.c_void_p, C.c_long, C.c_int, _ip, _ip, _dp, _dp, _ip, _ip, _dp, _dp]
+            getattr(L, nm).restype = C.c_int
 
     def fft_sizes(self, nb, nx):
         a, b = C.c_int(), C.c_int()
@@ -143,6 +148,37 @@ class Oracle:
         return ncl, labels
 
 
+    def detect(self, rho, templates, signals, fs, threshold=0.7, min_distance=0, absolute_maximum=False,
+               single=False, interpolation=1, alpha=51, npts=100, amplitudes=True):
+        """Detector<T>::detect restated (orc_detect_f/_d) on given traces:
+        rho [nt, len] (float32 or float64), templates (FP64), one signal per
+        template (same dtype as rho).  interpolation: 0 Lanczos, 1 quadratic,
+        2 none.  Returns a dict of per-detection arrays."""
+        rho = np.ascontiguousarray(rho)
+        dt = rho.dtype
+        ct = C.c_float if dt == np.float32 else C.c_double
+        nt, ln = rho.shape
+        tps = [np.ascontiguousarray(t, dtype=np.float64) for t in templates]
+        sig = [np.ascontiguousarray(x, dtype=dt) for x in signals]
+        lens = np.array([t.size for t in tps], dtype=np.int32)
+        maxdet = nt * ln + 1
+        o = {k: np.zeros(maxdet, np.int32) for k in ("template", "sample", "sign", "have_amplitude")}
+        o.update({k: np.zeros(maxdet, np.float64) for k in ("correlation", "shift", "gibbons_ringdal",
+                                                             "schaff_richards")})
+        fn = self.lib.orc_detect_f if dt == np.float32 else self.lib.orc_detect_d
+        nd = fn(nt, ln, rho.ctypes.data_as(C.c_void_p), ln, int(absolute_maximum), int(single), float(threshold),
+                int(min_distance), int(interpolation), int(alpha), int(npts), float(fs), int(amplitudes),
+                lens.ctypes.data_as(_ip), _ptr_array(tps, C.c_double), _ptr_array(sig, ct), sig[0].size, maxdet,
+                o["template"].ctypes.data_as(_ip), o["sample"].ctypes.data_as(_ip),
+                o["correlation"].ctypes.data_as(_dp), o["shift"].ctypes.data_as(_dp),
+                o["sign"].ctypes.data_as(_ip), o["have_amplitude"].ctypes.data_as(_ip),
+                o["gibbons_ringdal"].ctypes.data_as(_dp), o["schaff_richards"].ctypes.data_as(_dp))
+        out = {k: v[:nd].copy() for k, v in o.items()}
+        out["time"] = out["sample"] * (1.0 / fs)
+        out["interpolated_time"] = out["time"] + out["shift"]
+        return out
+
+
 class Reference:
     """The reference's own classes (compiled against the FFTW/MKL shim)."""
 
@@ -161,6 +197,33 @@ class Reference:
                                      C.c_long, C.c_double, _dp, _dp, _dp, C.c_int, _dp, _ip]
         L.ref_peaks_d.argtypes = [C.c_int, _dp, C.c_double, C.c_int, _ip]
         L.ref_peaks_f.argtypes = [C.c_int, _fp, C.c_float, C.c_int, _ip]
+        for nm in ("ref_detect_d", "ref_detect_f"):
+            getattr(L, nm).argtypes = [C.c_int, _ip, C.c_void_p, C.c_int, C.c_void_p, C.c_double, C.c_double,
+                                       C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                       _ip, _dp, _dp, _dp, _ip, _ip, _dp, _dp]
+            getattr(L, nm).restype = C.c_int
+
+    def detect(self, templates, signal, fs, threshold=0.7, min_distance=0, absolute_maximum=False, single=False,
+               interpolation=1, alpha=51, npts=100, amplitudes=True, dtype=np.float64, maxdet=100000):
+        """SingleChannel::MatchedFilter<T> + SingleChannel::Detector<T> of the
+        reference on one signal; templates carry COMPRESSION polarity."""
+        tps = [np.ascontiguousarray(t, dtype=np.float64) for t in templates]
+        x = np.ascontiguousarray(signal, dtype=dtype)
+        lens = np.array([t.size for t in tps], dtype=np.int32)
+        o = {k: np.zeros(maxdet, np.int32) for k in ("template", "polarity", "have_amplitude")}
+        o.update({k: np.zeros(maxdet, np.float64) for k in ("correlation", "time", "interpolated_time",
+                                                             "gibbons_ringdal", "schaff_richards")})
+        fn = self.lib.ref_detect_f if x.dtype == np.float32 else self.lib.ref_detect_d
+        nd = fn(len(tps), lens.ctypes.data_as(_ip), _ptr_array(tps, C.c_double), x.size,
+                x.ctypes.data_as(C.c_void_p), float(fs), float(threshold), int(min_distance), int(absolute_maximum),
+                int(single), int(interpolation), int(alpha), int(npts), int(amplitudes), maxdet,
+                o["template"].ctypes.data_as(_ip), o["correlation"].ctypes.data_as(_dp),
+                o["time"].ctypes.data_as(_dp), o["interpolated_time"].ctypes.data_as(_dp),
+                o["polarity"].ctypes.data_as(_ip), o["have_amplitude"].ctypes.data_as(_ip),
+                o["gibbons_ringdal"].ctypes.data_as(_dp), o["schaff_richards"].ctypes.data_as(_dp))
+        if nd < 0:
+            raise RuntimeError("reference detector failed")
+        return {k: v[:min(nd, maxdet)].copy() for k, v in o.items()}
 
     @staticmethod
     def available():

@@ -8,7 +8,9 @@
  * Calls: MFLib::computeOptimalFFTAndBlockLength
  *        (include/mflib/matchedFilterParameters.hpp:208),
  *        MFLib::MatchedFilter<T> (include/mflib/matchedFilter.hpp:28-178),
- *        MFLib::PeakFinder<T> (include/private/peakFinder.hpp:12-138).
+ *        MFLib::PeakFinder<T> (include/private/peakFinder.hpp:12-138),
+ *        MFLib::SingleChannel::{MatchedFilter, Detector}<T>
+ *        (include/mflib/singleChannel/matchedFilter.hpp, detector.hpp).
  */
 #include <cstdio>
 #include <cstring>
@@ -19,6 +21,13 @@
 #include "mflib/matchedFilter.hpp"
 #include "mflib/enums.hpp"
 #include "private/peakFinder.hpp"
+#include "mflib/networkStationPhase.hpp"
+#include "mflib/singleChannel/matchedFilterParameters.hpp"
+#include "mflib/singleChannel/matchedFilter.hpp"
+#include "mflib/singleChannel/detector.hpp"
+#include "mflib/singleChannel/detectorParameters.hpp"
+#include "mflib/singleChannel/detectionTimeInterpolationParameters.hpp"
+#include "mflib/singleChannel/detection.hpp"
 
 using namespace MFLib;
 
@@ -163,4 +172,93 @@ REF_API int ref_peaks_f(int n, const float *x, float thr, int minDist, int *peak
         return np;
     }
     catch (const std::exception &) { return -1; }
+}
+
+/* SingleChannel::MatchedFilter<T> on one signal, then SingleChannel::
+ * Detector<T>::detect; templates carry COMPRESSION polarity and no
+ * identifier (so a detection's identifier is the template index).  Up to
+ * maxdet detections are returned; the result is the number found or -1.
+ * The float matched filter object is not destroyed: the reference's float
+ * clear() frees one buffer twice. */
+template<class T>
+static int run_detect(int nt, const int *lens, const double *const *templates, int n, const T *signal,
+                      double fs, double thr, int minDist, int absMax, int single, int interp, int alpha,
+                      int npts, int amplitudes, int maxdet, int *o_tmpl, double *o_xc, double *o_time,
+                      double *o_itime, int *o_pol, int *o_have, double *o_gr, double *o_sr)
+{
+    try
+    {
+        SingleChannel::MatchedFilterParameters parms;
+        for (int t = 0; t < nt; ++t)
+        {
+            WaveformTemplate wt;
+            wt.setSignal(lens[t], templates[t]);
+            wt.setSamplingRate(fs);
+            wt.setPolarity(Polarity::COMPRESSION);
+            parms.addTemplate(wt);
+        }
+        parms.setSignalSize(n);
+        auto *mf = new SingleChannel::MatchedFilter<T>();
+        mf->initialize(parms);
+        mf->setSignal(n, signal);
+        mf->apply();
+        SingleChannel::DetectorParameters dp;
+        dp.setDetectionThreshold(thr);
+        dp.setMinimumDetectionSpacing(minDist);
+        dp.setMaximaPolicy(absMax ? MaximumMatchedFilterPolicy::ABSOLUTE_MAXIMUM
+                                  : MaximumMatchedFilterPolicy::MAXIMUM);
+        dp.setMatchedFilteredSignalDetectorPolicy(single ? MatchedFilteredSignalDetectorPolicy::SINGLE
+                                                         : MatchedFilteredSignalDetectorPolicy::REDUCED);
+        SingleChannel::DetectionTimeInterpolationParameters ip;
+        if (interp == 0) { ip.enableLanczos(); }
+        else if (interp == 1) { ip.enableQuadratic(); }
+        else { ip.disable(); }
+        ip.setLanczosAlpha(alpha);
+        ip.setLanczosNumberOfInterpolationPoints(npts);
+        dp.setDetectionTimeInterpolationParameters(ip);
+        if (amplitudes) { dp.enableSaveAmplitudeScalingFactor(); }
+        else { dp.disableSaveAmplitudeScalingFactor(); }
+        SingleChannel::Detector<T> det;
+        det.initialize(dp);
+        det.detect(*mf);
+        const int nd = det.getNumberOfDetections();
+        for (int i = 0; i < nd && i < maxdet; ++i)
+        {
+            auto d = det.getDetection(i);
+            o_tmpl[i] = (int) d.getTemplateIdentifier().second;
+            o_xc[i] = d.getCorrelationCoefficient();
+            o_time[i] = d.getDetectionTime();
+            o_itime[i] = d.getInterpolatedDetectionTime();
+            o_pol[i] = (int) d.getPolarity();
+            const bool h = d.haveAmplitudeScalingFactor(RelativeMagnitudeType::GIBBONS_RINGDAL_2006);
+            o_have[i] = h ? 1 : 0;
+            o_gr[i] = h ? (double) d.getAmplitudeScalingFactor(RelativeMagnitudeType::GIBBONS_RINGDAL_2006) : 0.0;
+            o_sr[i] = h ? (double) d.getAmplitudeScalingFactor(RelativeMagnitudeType::SCHAFF_RICHARDS_2014) : 0.0;
+        }
+        if (sizeof(T) == 8) { delete mf; }
+        return nd;
+    }
+    catch (const std::exception &e)
+    {
+        fprintf(stderr, "ref_detect: %s\n", e.what());
+        return -1;
+    }
+}
+
+REF_API int ref_detect_d(int nt, const int *lens, const double *const *templates, int n, const double *signal,
+                         double fs, double thr, int minDist, int absMax, int single, int interp, int alpha,
+                         int npts, int amplitudes, int maxdet, int *o_tmpl, double *o_xc, double *o_time,
+                         double *o_itime, int *o_pol, int *o_have, double *o_gr, double *o_sr)
+{
+    return run_detect<double>(nt, lens, templates, n, signal, fs, thr, minDist, absMax, single, interp, alpha, npts,
+                              amplitudes, maxdet, o_tmpl, o_xc, o_time, o_itime, o_pol, o_have, o_gr, o_sr);
+}
+
+REF_API int ref_detect_f(int nt, const int *lens, const double *const *templates, int n, const float *signal,
+                         double fs, double thr, int minDist, int absMax, int single, int interp, int alpha,
+                         int npts, int amplitudes, int maxdet, int *o_tmpl, double *o_xc, double *o_time,
+                         double *o_itime, int *o_pol, int *o_have, double *o_gr, double *o_sr)
+{
+    return run_detect<float>(nt, lens, templates, n, signal, fs, thr, minDist, absMax, single, interp, alpha, npts,
+                             amplitudes, maxdet, o_tmpl, o_xc, o_time, o_itime, o_pol, o_have, o_gr, o_sr);
 }

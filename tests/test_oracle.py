@@ -161,3 +161,65 @@ def test_dbscan_vs_sklearn(oracle, rng):
                 ref = sk.DBSCAN(eps=eps, min_samples=mo).fit(X, sample_weight=weights).labels_
                 assert ncl == (ref.max() + 1 if ref.size else 0)
                 np.testing.assert_array_equal(lab, ref)
+
+
+def _golden_detector():
+    import os
+    return dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "detector_golden.npz")))
+
+
+@pytest.mark.parametrize("single", [0, 1])
+@pytest.mark.parametrize("interp", [0, 1, 2])
+@pytest.mark.parametrize("absm", [0, 1])
+def test_detector_oracle_vs_golden(oracle, single, interp, absm):
+    """The detector restatement (orc_detect_d) on the oracle's FP64 traces
+    reproduces the reference's own SingleChannel::Detector<double> output
+    stored in tests/golden/detector_golden.npz (generated by
+    make_detector_golden.py from the reference compiled unchanged): the
+    same detections in the same order, times and coefficients to 1e-12,
+    polarity, amplitude scaling factors to 1e-12 relative."""
+    g = _golden_detector()
+    tps = list(g["templates"])
+    x = g["signal"]
+    fs = float(g["fs"])
+    rho = np.stack(oracle.matched_filter(tps, [x] * len(tps), multi=False, dtype=np.float64))
+    o = oracle.detect(rho, tps, [x] * len(tps), fs, threshold=float(g["threshold"]),
+                      min_distance=int(g["min_distance"]), single=single, interpolation=interp,
+                      absolute_maximum=absm)
+    key = "s%d_i%d_a%d_" % (single, interp, absm)
+    assert g[key + "template"].size > 5
+    np.testing.assert_array_equal(o["template"], g[key + "template"])
+    np.testing.assert_allclose(o["time"], g[key + "time"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(o["interpolated_time"], g[key + "interpolated_time"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(o["correlation"], g[key + "correlation"], rtol=0, atol=1e-12)
+    np.testing.assert_array_equal(o["sign"], g[key + "polarity"])  # templates carry COMPRESSION (+1)
+    np.testing.assert_array_equal(o["have_amplitude"], g[key + "have_amplitude"])
+    np.testing.assert_allclose(o["gibbons_ringdal"], g[key + "gibbons_ringdal"], rtol=1e-12)
+    np.testing.assert_allclose(o["schaff_richards"], g[key + "schaff_richards"], rtol=1e-12)
+
+
+def test_detector_oracle_vs_reference(oracle, reference, rng):
+    """Random cases against the compiled reference detector (FP64), every
+    option combination; where the checkout exists."""
+    from scipy.signal.windows import hann
+    for trial in range(3):
+        nt = int(rng.integers(1, 5))
+        L = int(rng.integers(50, 400))
+        tps = [rng.standard_normal(L) * hann(L) for _ in range(nt)]
+        n = int(rng.integers(3_000, 12_000))
+        x = rng.standard_normal(n)
+        for t in range(nt):
+            for o in rng.integers(0, n - L, 3):
+                x[o:o + L] += rng.choice([-1.5, 1.5]) * tps[t]
+        rho = np.stack(oracle.matched_filter(tps, [x] * nt, multi=False, dtype=np.float64))
+        for single in (0, 1):
+            for interp in (0, 1, 2):
+                for absm in (0, 1):
+                    kw = dict(threshold=0.4, min_distance=int(rng.integers(0, 200)), single=single,
+                              interpolation=interp, absolute_maximum=absm, alpha=int(rng.integers(3, 60)),
+                              npts=int(rng.integers(5, 120)))
+                    r = reference.detect(tps, x, 50.0, dtype=np.float64, **kw)
+                    o = oracle.detect(rho, tps, [x] * nt, 50.0, **kw)
+                    np.testing.assert_array_equal(o["template"], r["template"])
+                    np.testing.assert_allclose(o["interpolated_time"], r["interpolated_time"], rtol=0, atol=1e-12)
+                    np.testing.assert_allclose(o["gibbons_ringdal"], r["gibbons_ringdal"], rtol=1e-11)
