@@ -22,7 +22,7 @@ import numpy as np
 
 from . import _lib
 from .matched_filter import MatchedFilter
-from .waveform import NetworkStationPhase, Polarity
+from .waveform import MatchedFilterDetectionMode, NetworkStationPhase, Polarity
 
 
 class MaximumMatchedFilterPolicy(enum.IntEnum):
@@ -352,10 +352,12 @@ class Detector:
                 d.set_amplitude_scaling_factor(r.schaff_richards, RelativeMagnitudeType.schaff_richards_2014)
             if want_wave:
                 it = r.template_index
-                if it not in signals:
-                    signals[it] = MatchedFilter.get_signal(mf, it)
+                # single-channel objects hold one signal (slot 0)
+                slot = 0 if mf._params.get_detection_mode() == MatchedFilterDetectionMode.single_channel else it
+                if slot not in signals:
+                    signals[slot] = MatchedFilter.get_signal(mf, slot)
                 L = wt.get_signal_length()
-                d.set_detected_signal(signals[it][r.sample:r.sample + L])
+                d.set_detected_signal(signals[slot][r.sample:r.sample + L])
             self._dets.append(d)
         return self
 
