@@ -329,6 +329,75 @@ def run_serving(args):
     print(json.dumps(line), flush=True)
 
 
+def run_detector(args):
+    """Single-channel detector timing: one 24 h channel (8.64 M samples of
+    band-passed noise with injected copies) against 192 templates of 500
+    samples; a step is Detector.detect (reduction of the 192 traces to their
+    per-lag maximum and argmax, PeakFinder at rho > 0.5 with separation 250,
+    quadratic refinement, amplitudes) on the traces of one apply, timed with
+    CUDA events on the library's stream."""
+    import torch
+    import mflib_gb300 as mf
+    w = make_workload(n_samples=args.samples, n_stations=1, n_events=64)
+    x = w["signals"][0]
+    p = mf.SingleChannel.MatchedFilterParameters()
+    for tp in w["templates"][:192]:
+        wt = mf.WaveformTemplate()
+        wt.set_signal(tp)
+        wt.set_sampling_rate(FS)
+        p.add_template(wt)
+    p.set_signal_size(x.size)
+    f = mf.SingleChannel.MatchedFilter(dtype=np.float32)
+    f.initialize(p)
+    f.set_signal(x)
+    f.apply()
+    prm = mf.SingleChannel.DetectorParameters()
+    prm.set_detection_threshold(0.5)
+    prm.set_minimum_detection_spacing(250)
+    prm.set_matched_filtered_signal_detector_policy(mf.MatchedFilteredSignalDetectorPolicy.reduce)
+    det = mf.SingleChannel.Detector()
+    det.initialize(prm)
+    import ctypes as C
+    from mflib_gb300 import _lib
+    dp = _lib.MfgpuDetectParams()
+    dp.threshold, dp.min_distance, dp.absolute_maximum, dp.single = 0.5, 250, 0, 0
+    dp.interpolation, dp.lanczos_alpha, dp.lanczos_points, dp.sampling_rate, dp.amplitudes = 1, 51, 100, FS, 1
+    nd = C.c_int()
+
+    def abi_detect():
+        _lib.call("mfgpu_mf_detect", f._h, C.byref(dp), C.byref(nd))
+
+    stream = torch.cuda.ExternalStream(f.stream_handle())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        f.synchronize()
+        ev0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        ev1.record(stream)
+        f.synchronize()
+        torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / args.steps
+
+    ms = timed(abi_detect)  # the C ABI call: device work, detections copied to host structs
+    py_ms = timed(lambda: det.detect(f))  # plus the Python Detection objects
+    nt = len(w["templates"][:192])
+    ln = f.get_filtered_signal_length()
+    alg = 4.0 * nt * ln + 8.0 * ln  # traces read, reduced trace and argmax written
+    peak, kind = measured_peak()
+    line = {"metric": "detector step through the C ABI (reduce + peaks + refinement + amplitudes)", "value": ms,
+            "unit": "ms",
+            "higher_is_better": False, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "dtype": "f32",
+            "config": {"workload": "1 channel x %d samples, %d templates x 500, REDUCED, quadratic" % (x.size, nt)},
+            "detections": det.get_number_of_detections(), "python_api_ms": py_ms,
+            "roofline_bound_ms": alg / (peak * 1e9) * 1e3, "algorithmic_bytes": alg, "peak_gbs": peak,
+            "peak_source": kind}
+    print(json.dumps(line), flush=True)
+
+
 def run_uneven(args):
     """The uneven bank: 2,000 templates of 200-3,000 samples (uniform) with
     random 1-15 Hz pass bands, each on one of 96 channels (uniform), against
@@ -424,6 +493,7 @@ def main():
     ap.add_argument("--serving", action="store_true", help="run the request loop instead of the day-long step")
     ap.add_argument("--uneven", action="store_true",
                     help="the 2,000-template uneven bank on 96 channels instead of the 24-channel day")
+    ap.add_argument("--detector", action="store_true", help="time the single-channel detector")
     ap.add_argument("--length-buckets", type=int, default=0,
                     help="length buckets of a mixed-length bank (0 planner's choice, 1 one plan)")
     ap.add_argument("--rates", type=float, nargs="+", default=[50, 100, 200, 500, 0],
@@ -438,6 +508,9 @@ def main():
         return
     if args.uneven:
         run_uneven(args)
+        return
+    if args.detector:
+        run_detector(args)
         return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -160,6 +160,8 @@ class Detection:
     """src/singleChannel/detection.cpp: a detection's value fields, each with
     get / set / have."""
 
+    __slots__ = ("_id", "_xc", "_sig", "_t", "_ti", "_tt", "_po", "_poi", "_amp", "_pol")
+
     def __init__(self):
         self.clear()
 
@@ -312,7 +314,7 @@ class Detector:
             raise ValueError("No templates on matched filter class")
         prm = self._params
         ip = prm.get_detection_time_interpolation_parameters()
-        templates = [mf.get_waveform_template(i) for i in range(nt)]
+        templates = mf._templates  # read only: metadata of the detected templates
         fs = templates[0].get_sampling_rate()
         dp = _lib.MfgpuDetectParams()
         dp.threshold = min(1.0, max(0.0, prm.get_detection_threshold()))
@@ -330,33 +332,37 @@ class Detector:
         _lib.call("mfgpu_mf_get_detections", mf._h, n.value, raw, C.byref(n))
         want_wave = prm.want_detected_waveform()
         signals = {}
+        meta = {}
+        pols = {v: Polarity(v) for v in (-1, 0, 1)}
         for r in raw[: n.value]:
-            wt = templates[r.template_index]
+            it = r.template_index
+            if it not in meta:
+                wt = templates[it]
+                meta[it] = (wt.get_identifier() if wt.have_identifier() else (NetworkStationPhase(), it),
+                            wt.get_phase_onset_time_in_signal() if wt.have_phase_onset_time() else None,
+                            int(wt.get_polarity()),
+                            wt.get_phase_travel_time() if wt.have_travel_time() else None,
+                            wt.get_signal_length())
+            ident, onset, pol, travel, L = meta[it]
             d = Detection()
-            if wt.have_identifier():
-                d.set_template_identifier(wt.get_identifier())
-            else:
-                d.set_template_identifier((NetworkStationPhase(), r.template_index))
-            d.set_correlation_coefficient(r.correlation)
-            d.set_detection_time(r.detection_time)
-            d.set_interpolated_detection_time(r.interpolated_time)
-            if wt.have_phase_onset_time():
-                onset = wt.get_phase_onset_time_in_signal()
-                d.set_phase_onset_time(r.detection_time + onset)
-                d.set_interpolated_phase_onset_time(r.interpolated_time + onset)
-            d.set_polarity(r.sign * int(wt.get_polarity()))
-            if wt.have_travel_time():
-                d.set_travel_time(wt.get_phase_travel_time())
+            d._id = (ident[0], int(ident[1]))
+            d._xc = r.correlation  # clamped to [-1, 1] on the device
+            d._t = r.detection_time
+            d._ti = r.interpolated_time
+            if onset is not None:
+                d._po = r.detection_time + onset
+                d._poi = r.interpolated_time + onset
+            d._pol = pols[r.sign * pol]
+            if travel is not None:
+                d._tt = travel
             if r.have_amplitude:
-                d.set_amplitude_scaling_factor(r.gibbons_ringdal, RelativeMagnitudeType.gibbons_ringdal_2006)
-                d.set_amplitude_scaling_factor(r.schaff_richards, RelativeMagnitudeType.schaff_richards_2014)
+                d._amp = {RelativeMagnitudeType.gibbons_ringdal_2006: r.gibbons_ringdal,
+                          RelativeMagnitudeType.schaff_richards_2014: r.schaff_richards}
             if want_wave:
-                it = r.template_index
                 # single-channel objects hold one signal (slot 0)
                 slot = 0 if mf._params.get_detection_mode() == MatchedFilterDetectionMode.single_channel else it
                 if slot not in signals:
                     signals[slot] = MatchedFilter.get_signal(mf, slot)
-                L = wt.get_signal_length()
                 d.set_detected_signal(signals[slot][r.sample:r.sample + L])
             self._dets.append(d)
         return self
