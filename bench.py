@@ -640,6 +640,7 @@ def main():
 
     serial_el, _ = timed(serial)
     e2e_el, (counts, idx, labels, ncl) = timed(pipelined)
+    last_pipelined = f.last_timings()  # correlator and apply of the last pipelined step
     h2d = w["nch"] * n * 4
     d2h = int(4 * (counts.size + idx.size + labels.size + ncl.size))
 
@@ -685,6 +686,7 @@ def main():
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "ms_per_step": 1e3 * e2e_el / args.steps,
                     "serial_value": world * lags_per_step / (serial_el / args.steps),
+                    "last_step_xcorr_ms": last_pipelined["xcorr_ms"], "last_step_apply_ms": last_pipelined["apply_ms"],
                     "api": "stage_channel_signals (async H2D of step i+1 under step i), apply, find_peaks, "
                            "get_all_peaks, DBSCAN association; serial_value: set_channel_signals then the step"},
             "roofline": roof, "gpu_launches": int(launches), "clocks": clk,

@@ -156,8 +156,10 @@ mfgpu_status mfgpu_mf_set_channel_signals(mfgpu_mf *mf, int first_channel, int n
  * enqueued (the current apply, peak finding), and the results of the
  * previous apply stay readable.  The next apply -- or any call that reads
  * or writes the signals -- makes the staged signals current.  Unlike the
- * reference's copying setters, x must stay valid and unchanged until then
- * (or until mfgpu_mf_synchronize); pinned host memory makes the copy DMA. */
+ * reference's copying setters, x must stay valid and unchanged until the
+ * copy has finished: until a result of that next apply has been read (a
+ * getter or find_peaks after it), or until mfgpu_mf_synchronize; pinned host
+ * memory makes the copy DMA. */
 mfgpu_status mfgpu_mf_stage_channel_signals(mfgpu_mf *mf, int n, const void *x, long ld);
 /* Signal of channel c from device memory (same type, n samples). */
 mfgpu_status mfgpu_mf_set_channel_signal_device(mfgpu_mf *mf, int channel, int n, const void *dx);
@@ -225,7 +227,9 @@ typedef struct
 mfgpu_status mfgpu_mf_detect(mfgpu_mf *mf, const mfgpu_detect_params *params, int *n_detections);
 /* Copies up to max detections of the last mfgpu_mf_detect. */
 mfgpu_status mfgpu_mf_get_detections(mfgpu_mf *mf, int max, mfgpu_detection *out, int *n);
-/* Block until the object's stream is idle; reports device-side errors. */
+/* Block until the object's streams are idle (work and staged uploads);
+ * reports device-side errors.  Result getters and find_peaks wait for the
+ * work only: a staged upload in flight feeds the next apply. */
 mfgpu_status mfgpu_mf_synchronize(mfgpu_mf *mf);
 /* Device time (ms) of the last apply's correlation kernel and of the whole
  * apply (correlation + dead-trace checks), measured with CUDA events on

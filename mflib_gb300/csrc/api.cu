@@ -229,9 +229,13 @@ struct mfgpu_mf
     }
 };
 
-static mfgpu_status mf_sync(mfgpu_mf *mf)
+// Waits for the object's compute stream (and, with `copies`, for a staged
+// upload in flight).  Results on the device never depend on the staged
+// copy, which only feeds the next apply (that apply waits for it on the
+// device), so reading results does not wait for the next step's upload.
+static mfgpu_status mf_sync(mfgpu_mf *mf, bool copies = false)
 {
-    if (mf->copy_stream) CU(cudaStreamSynchronize(mf->copy_stream));
+    if (copies && mf->copy_stream) CU(cudaStreamSynchronize(mf->copy_stream));
     CU(cudaStreamSynchronize(mf->stream));
     if (mf->initialized && mf->err.p)
     {
@@ -1257,7 +1261,7 @@ mfgpu_status mfgpu_mf_synchronize(mfgpu_mf *mf)
 {
     if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");
     DeviceGuard g(mf->dev);
-    return mf_sync(mf);
+    return mf_sync(mf, true);
 }
 
 mfgpu_status mfgpu_mf_have_matched_filtered_signals(const mfgpu_mf *mf, int *flag)

@@ -151,12 +151,26 @@ static __global__ void __launch_bounds__(kDbThreads) db_union_kernel(DbParams p,
     if (lane == 0 && bj >= 0 && fabs(xi - bx) <= p.eps) db_unite(parent, i, bj);
 }
 
+// Root without writes: in the roots pass a halving write from one thread
+// could land after another thread stored its node's final root and replace
+// it with an intermediate ancestor.
+__device__ __forceinline__ int db_find_ro(const volatile int *parent, int x)
+{
+    int p = parent[x];
+    while (p != x)
+    {
+        x = p;
+        p = parent[x];
+    }
+    return x;
+}
+
 static __global__ void db_roots_kernel(int n, const unsigned char *core, int *parent, int *is_root)
 {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (!core[i]) { is_root[i] = 0; return; }
-    int r = db_find(parent, i);
+    int r = db_find_ro(parent, i);
     parent[i] = r;
     is_root[i] = r == i ? 1 : 0;
 }

@@ -5,6 +5,7 @@
 #include <cstddef>
 #include <mutex>
 #include <string>
+#include <vector>
 #include <cuda_runtime.h>
 #include "kernels_mf.cuh"
 #include "kernels_util.cuh"
@@ -111,6 +112,7 @@ struct PeakWS
         counter, row, ht;
     long long npeaks = 0;
     long long cand_cap = 1 << 16;  // capacity of the packed candidate arrays
+    std::vector<int> rows_on_device;  // the trace rows last uploaded to `row`
     template <class F> void each_buf(F &&f)
     {
         DevBuf *all[] = {&counts, &offs, &slot_idx, &slot_val, &cidx, &cval, &ctr, &state, &flags,
@@ -122,6 +124,7 @@ struct PeakWS
         each_buf([](DevBuf &d) { d.release(); });
         npeaks = 0;
         cand_cap = 1 << 16;
+        rows_on_device.clear();
     }
 };
 

@@ -48,7 +48,11 @@ int run_peaks(const T *x, long ldx, const int *host_rows, int ntr, int len, doub
     // (fused.S lags) when the correlator gathered the candidates
     const int nchunks = fused ? fused->nblk : (len + kPkChunk - 1) / kPkChunk;
     const size_t nslots = (size_t) ntr * nchunks;
-    MF_TRY(ws.row.ensure(sizeof(int) * ntr));
+    {
+        void *old = ws.row.p;
+        MF_TRY(ws.row.ensure(sizeof(int) * ntr));
+        if (ws.row.p != old) ws.rows_on_device.clear();  // a new buffer holds no rows
+    }
     MF_TRY(ws.trace_beg.ensure(sizeof(long long) * (ntr + 1)));
     MF_TRY(ws.peak_off.ensure(sizeof(long long) * (ntr + 1)));
     MF_TRY(ws.counts.ensure(sizeof(int) * nslots));
@@ -60,7 +64,15 @@ int run_peaks(const T *x, long ldx, const int *host_rows, int ntr, int len, doub
         MF_TRY(ws.slot_val.ensure(sizeof(T) * nslots * kPkCap));
     }
     MF_TRY(ws.counter.ensure(4 * sizeof(int)));  // [0] undecided after the last round, [1] overflow
-    MF_TRY(cudaMemcpyAsync(ws.row.p, host_rows, sizeof(int) * ntr, cudaMemcpyHostToDevice, s));
+    // the rows rarely change between calls: upload only when they do (an
+    // upload queues behind any large host-to-device copy in flight)
+    if (ws.rows_on_device.size() != (size_t) ntr ||
+        !std::equal(host_rows, host_rows + ntr, ws.rows_on_device.begin()))
+    {
+        MF_TRY(cudaMemcpyAsync(ws.row.p, host_rows, sizeof(int) * ntr, cudaMemcpyHostToDevice, s));
+        MF_TRY(cudaStreamSynchronize(s));  // host_rows may be a temporary
+        ws.rows_on_device.assign(host_rows, host_rows + ntr);
+    }
     int *undecided = ws.counter.as<int>(), *overflow = ws.counter.as<int>() + 1;
     const long long *ncand_dev = ws.offs.as<long long>() + nslots;
 
