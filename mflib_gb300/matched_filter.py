@@ -489,6 +489,9 @@ SingleChannel = _SingleChannel
 
 def _attach_detector():
     # pymflib.SingleChannel.{Detector, DetectorParameters, Detection, ...}
+    from . import associator as a
     from . import detector as d
     for name in ("Detector", "DetectorParameters", "DetectionTimeInterpolationParameters", "Detection"):
         setattr(_SingleChannel, name, getattr(d, name))
+    for name in ("Associator", "AssociatorParameters"):
+        setattr(_SingleChannel, name, getattr(a, name))

@@ -179,6 +179,33 @@ class Oracle:
         return out
 
 
+    def associate(self, evid, onset, travel, xc, tol, min_picks, weighted=False):
+        """Associator<T>::associate (src/singleChannel/associator.cpp:
+        156-267) restated: detections sorted by event id then onset time
+        (stable), DBSCAN (orc_dbscan) of each event's origin times (onset -
+        travel), eps = tol, minPts = min_picks, optionally weighted by xc.
+        Returns the sort order and the events as (event id, [positions in
+        the sorted order]), ordered by event id then cluster."""
+        evid = np.asarray(evid, dtype=np.uint64)
+        onset = np.asarray(onset, dtype=np.float64)
+        travel = np.asarray(travel, dtype=np.float64)
+        xc = np.asarray(xc, dtype=np.float64)
+        order = np.lexsort((onset, evid))
+        events = []
+        ev, on, tr, w = evid[order], onset[order], travel[order], xc[order]
+        i = 0
+        while i < ev.size:
+            j = i
+            while j < ev.size and ev[j] == ev[i]:
+                j += 1
+            ot = (on[i:j] - tr[i:j]).reshape(-1, 1)
+            ncl, lab = self.dbscan(ot, tol, min_picks, w[i:j] if weighted else None)
+            for c in range(ncl):
+                events.append((int(ev[i]), [i + k for k in range(j - i) if lab[k] == c]))
+            i = j
+        return order, events
+
+
 class Reference:
     """The reference's own classes (compiled against the FFTW/MKL shim)."""
 

@@ -223,3 +223,19 @@ def test_detector_oracle_vs_reference(oracle, reference, rng):
                     np.testing.assert_array_equal(o["template"], r["template"])
                     np.testing.assert_allclose(o["interpolated_time"], r["interpolated_time"], rtol=0, atol=1e-12)
                     np.testing.assert_allclose(o["gibbons_ringdal"], r["gibbons_ringdal"], rtol=1e-11)
+
+
+def test_associate_known_answer(oracle):
+    """Associator<T>::associate restatement on a hand-made case: event 7 has
+    picks whose origin times form two groups of 3 (0.0..0.2 s and 10.0..10.4
+    s) and one straggler at 30 s; event 3 has 2 picks (below min_picks 3)."""
+    evid = [7, 7, 3, 7, 7, 7, 3, 7, 7]
+    travel = [1.0, 2.0, 5.0, 3.0, 1.0, 2.0, 5.0, 4.0, 1.0]
+    origin = [0.0, 0.1, 50.0, 0.2, 10.0, 10.2, 50.5, 10.4, 30.0]
+    onset = [o + t for o, t in zip(origin, travel)]
+    order, events = oracle.associate(evid, onset, travel, [1.0] * 9, tol=0.5, min_picks=3)
+    # sorted by event id, then onset: event 3 first
+    assert [evid[i] for i in order] == [3, 3, 7, 7, 7, 7, 7, 7, 7]
+    assert len(events) == 2
+    got = [(e, sorted(origin[order[k]] for k in m)) for e, m in events]
+    assert got == [(7, [0.0, 0.1, 0.2]), (7, [10.0, 10.2, 10.4])]
