@@ -227,6 +227,17 @@ typedef struct
 mfgpu_status mfgpu_mf_detect(mfgpu_mf *mf, const mfgpu_detect_params *params, int *n_detections);
 /* Copies up to max detections of the last mfgpu_mf_detect. */
 mfgpu_status mfgpu_mf_get_detections(mfgpu_mf *mf, int max, mfgpu_detection *out, int *n);
+/* Relative amplitudes of detected windows against one template:
+ * RelativeMagnitude<T>::computeAmplitudeScalingFactor
+ * (src/singleChannel/relativeMagnitude.cpp:35-130, :334-372) for a batch of
+ * n_windows host windows of L samples (row stride ld, precision
+ * MFGPU_FLOAT32 | MFGPU_FLOAT64): gr = GIBBONS_RINGDAL_2006 = |<b, y>| /
+ * <b, b>, sr = SCHAFF_RICHARDS_2014 = sqrt(<y, y> / <b, b>) of the demeaned
+ * template b (FP64) and window y, in double; valid[w] = 0 for a constant
+ * window (the reference throws there).  Extension: the reference takes one
+ * window per call. */
+mfgpu_status mfgpu_relative_amplitudes(int precision, int L, const double *templ, int n_windows, const void *windows,
+                                       long ld, double *gr, double *sr, int *valid);
 /* Block until the object's streams are idle (work and staged uploads);
  * reports device-side errors.  Result getters and find_peaks wait for the
  * work only: a staged upload in flight feeds the next apply. */

@@ -106,6 +106,7 @@ _SIGS = {
     "mfgpu_mf_get_correlator": ([_vp, _ip, _ip, _ip], C.c_int),
     "mfgpu_mf_get_buckets": ([_vp, C.c_int, _ip, _ip, _ip], C.c_int),
     "mfgpu_mf_detect": ([_vp, C.POINTER(MfgpuDetectParams), _ip], C.c_int),
+    "mfgpu_relative_amplitudes": ([C.c_int, C.c_int, _vp, C.c_int, _vp, C.c_long, _vp, _vp, _ip], C.c_int),
     "mfgpu_mf_get_detections": ([_vp, C.c_int, C.POINTER(MfgpuDetection), _ip], C.c_int),
     "mfgpu_mf_set_window": ([_vp, C.c_int, C.c_int, _vp, C.c_long], C.c_int),
     "mfgpu_mf_get_device_bytes": ([_vp, C.POINTER(C.c_ulonglong)], C.c_int),

@@ -1573,6 +1573,47 @@ mfgpu_status mfgpu_mf_get_detections(mfgpu_mf *mf, int max, mfgpu_detection *out
     return MFGPU_OK;
 }
 
+mfgpu_status mfgpu_relative_amplitudes(int precision, int L, const double *templ, int n_windows, const void *windows,
+                                       long ld, double *gr, double *sr, int *valid)
+{
+    if (precision != MFGPU_FLOAT32 && precision != MFGPU_FLOAT64)
+        return fail(MFGPU_EINVAL, "precision must be MFGPU_FLOAT32 or MFGPU_FLOAT64");
+    if (L < 1 || n_windows < 0) return fail(MFGPU_EINVAL, "L must be positive and n_windows non-negative");
+    if (!templ || (n_windows > 0 && (!windows || !gr || !sr || !valid))) return fail(MFGPU_EINVAL, "NULL argument");
+    if (n_windows > 1 && ld < L) return fail(MFGPU_EINVAL, "row stride is smaller than the window length");
+    if (n_windows == 0) return MFGPU_OK;
+    const size_t es = (size_t) precision, rows = (size_t) n_windows;
+    const long ldd = n_windows > 1 ? ld : L;
+    struct Scratch  // released on every return
+    {
+        DevBuf b[5];
+        ~Scratch()
+        {
+            for (DevBuf &d : b) d.release();
+        }
+    } tmp;
+    DevBuf &db = tmp.b[0], &dy = tmp.b[1], &dg = tmp.b[2], &ds = tmp.b[3], &dv = tmp.b[4];
+    cudaStream_t s = cudaStreamPerThread;
+    CU(db.ensure(sizeof(double) * L));
+    CU(dy.ensure(es * (size_t) ldd * rows));
+    CU(dg.ensure(sizeof(double) * rows));
+    CU(ds.ensure(sizeof(double) * rows));
+    CU(dv.ensure(sizeof(int) * rows));
+    CU(cudaMemcpyAsync(db.p, templ, sizeof(double) * L, cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(dy.p, windows, es * (size_t) ldd * (rows - 1) + es * L, cudaMemcpyHostToDevice, s));
+    if (precision == MFGPU_FLOAT32)
+        CU(launch_amp<float>(db.as<double>(), L, dy.as<float>(), ldd, n_windows, dg.as<double>(), ds.as<double>(),
+                             dv.as<int>(), s));
+    else
+        CU(launch_amp<double>(db.as<double>(), L, dy.as<double>(), ldd, n_windows, dg.as<double>(),
+                              ds.as<double>(), dv.as<int>(), s));
+    CU(cudaMemcpyAsync(gr, dg.p, sizeof(double) * rows, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(sr, ds.p, sizeof(double) * rows, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(valid, dv.p, sizeof(int) * rows, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    return MFGPU_OK;
+}
+
 mfgpu_status mfgpu_mf_set_peak_threshold(mfgpu_mf *mf, double threshold)
 {
     if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");

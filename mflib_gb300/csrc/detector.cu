@@ -29,6 +29,20 @@ cudaError_t launch_det_refine(const T *rho, long ldr, const T *x, long ldx, cons
     return cudaGetLastError();
 }
 
+template <class T>
+cudaError_t launch_amp(const double *b, int L, const T *y, long ld, int nw, double *gr, double *sr, int *valid,
+                       cudaStream_t s)
+{
+    if (nw <= 0) return cudaSuccess;
+    const long threads = 32L * nw;
+    amp_kernel<T><<<(unsigned) ((threads + 255) / 256), 256, 0, s>>>(b, L, y, ld, nw, gr, sr, valid);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_amp<float>(const double *, int, const float *, long, int, double *, double *, int *,
+                                       cudaStream_t);
+template cudaError_t launch_amp<double>(const double *, int, const double *, long, int, double *, double *, int *,
+                                        cudaStream_t);
 template cudaError_t launch_det_reduce<float>(const float *, long, int, long, int, float *, int *, cudaStream_t);
 template cudaError_t launch_det_reduce<double>(const double *, long, int, long, int, double *, int *, cudaStream_t);
 template cudaError_t launch_det_single<float>(const float *, long, int, long, int, float *, cudaStream_t);

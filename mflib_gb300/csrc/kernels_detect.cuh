@@ -223,4 +223,45 @@ __global__ void det_refine_kernel(const T *rho, long ldr, const T *x, long ldx, 
     if (lane == 0) q.out[w] = o;
 }
 
+// RelativeMagnitude (src/singleChannel/relativeMagnitude.cpp:35-130) for a
+// batch of detected windows against one template, one warp per window:
+// gr = |<b, y>| / <b, b>, sr = sqrt(<y, y> / <b, b>) of the demeaned
+// template b and window y, in double; valid = <y, y> > 0
+template <class T>
+__global__ void amp_kernel(const double *b, int L, const T *y, long ld, int nw, double *gr, double *sr, int *valid)
+{
+    const int w = (int) ((blockIdx.x * (long) blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (w >= nw) return;
+    const T *yw = y + (long) w * ld;
+    double sb = 0, sy = 0;
+    for (int j = lane; j < L; j += 32) { sb += b[j]; sy += (double) yw[j]; }
+    for (int off = 16; off > 0; off >>= 1)
+    {
+        sb += __shfl_xor_sync(0xffffffffu, sb, off);
+        sy += __shfl_xor_sync(0xffffffffu, sy, off);
+    }
+    const double mb = sb / L, my = sy / L;
+    double bb = 0, yy = 0, by = 0;
+    for (int j = lane; j < L; j += 32)
+    {
+        const double db = b[j] - mb, dy = (double) yw[j] - my;
+        bb += db * db;
+        yy += dy * dy;
+        by += db * dy;
+    }
+    for (int off = 16; off > 0; off >>= 1)
+    {
+        bb += __shfl_xor_sync(0xffffffffu, bb, off);
+        yy += __shfl_xor_sync(0xffffffffu, yy, off);
+        by += __shfl_xor_sync(0xffffffffu, by, off);
+    }
+    if (lane == 0)
+    {
+        const bool ok = bb > 0 && yy > 0;
+        valid[w] = ok ? 1 : 0;
+        gr[w] = ok ? fabs(by) / bb : 0.0;
+        sr[w] = ok ? sqrt(yy / bb) : 0.0;
+    }
+}
+
 }  // namespace mfgpu

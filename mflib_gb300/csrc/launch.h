@@ -50,6 +50,9 @@ cudaError_t launch_det_single(const T *rho, long ldr, int nt, long len, int use_
 template <class T>
 cudaError_t launch_det_refine(const T *rho, long ldr, const T *x, long ldx, const struct DetectParams &q,
                               cudaStream_t s);
+template <class T>
+cudaError_t launch_amp(const double *b, int L, const T *y, long ld, int nw, double *gr, double *sr, int *valid,
+                       cudaStream_t s);
 // reference debug spectrum of one prepared template at FFT length nfft
 template <class T> cudaError_t launch_ref_spectrum(const double *tmpl, int L, int nfft, T *out, cudaStream_t s);
 // shift and stack (src/matchedFilter.cpp:1319-1364)

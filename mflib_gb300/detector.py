@@ -277,6 +277,25 @@ class Detection:
     def get_polarity(self):
         return self._pol
 
+    # pickling (python/singleChannel/detection.cpp:498-585 keeps the same fields)
+    def __getstate__(self):
+        ident = None if self._id is None else (self._id[0].__getstate__(), self._id[1])
+        return {"id": ident, "xc": self._xc, "sig": None if self._sig is None else self._sig.tolist(),
+                "t": self._t, "ti": self._ti, "tt": self._tt, "po": self._po, "poi": self._poi,
+                "amp": {int(k): v for k, v in self._amp.items()}, "pol": int(self._pol)}
+
+    def __setstate__(self, st):
+        self.clear()
+        if st["id"] is not None:
+            nsp = NetworkStationPhase()
+            nsp.__setstate__(st["id"][0])
+            self._id = (nsp, int(st["id"][1]))
+        self._xc = st["xc"]
+        self._sig = None if st["sig"] is None else np.array(st["sig"], dtype=np.float64)
+        self._t, self._ti, self._tt, self._po, self._poi = st["t"], st["ti"], st["tt"], st["po"], st["poi"]
+        self._amp = {RelativeMagnitudeType(k): v for k, v in st["amp"].items()}
+        self._pol = Polarity(st["pol"])
+
 
 class Detector:
     """Detector<T> (src/singleChannel/detector.cpp): initialize(parameters),
@@ -379,3 +398,78 @@ class Detector:
 
     def get_detections(self):
         return list(self._dets)
+
+
+class RelativeMagnitude:
+    """RelativeMagnitude<T> (src/singleChannel/relativeMagnitude.cpp):
+    initialize(template), set_detected_signal(y),
+    compute_amplitude_scaling_factor(type), compute_magnitude_perturbation
+    (type).  The sums run on the GPU (mfgpu_relative_amplitudes, which also
+    takes many windows at once: amplitude_scaling_factors)."""
+
+    def __init__(self, dtype=np.float64):
+        self._dtype = np.dtype(dtype)
+        if self._dtype not in (np.float32, np.float64):
+            raise ValueError("dtype must be float32 or float64")
+        self.clear()
+
+    def clear(self):
+        self._b = None
+        self._alpha = None
+
+    def initialize(self, wt):
+        self.clear()
+        b = np.ascontiguousarray(wt.get_signal(), dtype=np.float64)
+        if b.size < 1:
+            raise ValueError("Template signal length = %d must be positive" % b.size)
+        if np.all(b == b[0]):
+            raise ValueError("Template signal cannot be constant")
+        self._b = b
+
+    def is_initialized(self):
+        return self._b is not None
+
+    def get_detected_signal_length(self):
+        if self._b is None:
+            raise RuntimeError("Class not initialized")
+        return self._b.size
+
+    def amplitude_scaling_factors(self, windows):
+        """Extension: (gibbons_ringdal, schaff_richards, valid) for every row
+        of the 2-D array windows (n x template length)."""
+        if self._b is None:
+            raise RuntimeError("Class not initialized")
+        y = np.ascontiguousarray(np.atleast_2d(windows), dtype=self._dtype)
+        if y.shape[1] != self._b.size:
+            raise ValueError("Signal length = %d must = %d" % (y.shape[1], self._b.size))
+        nw = y.shape[0]
+        gr, sr = np.zeros(max(1, nw)), np.zeros(max(1, nw))
+        ok = np.zeros(max(1, nw), dtype=np.int32)
+        _lib.call("mfgpu_relative_amplitudes", int(self._dtype.itemsize), int(self._b.size),
+                  self._b.ctypes.data_as(C.c_void_p), nw, y.ctypes.data_as(C.c_void_p), int(y.shape[1]),
+                  gr.ctypes.data_as(C.c_void_p), sr.ctypes.data_as(C.c_void_p), ok.ctypes.data_as(C.POINTER(C.c_int)))
+        return gr[:nw], sr[:nw], ok[:nw].astype(bool)
+
+    def set_detected_signal(self, y):
+        self._alpha = None
+        gr, sr, ok = self.amplitude_scaling_factors(np.asarray(y).reshape(1, -1))
+        if not ok[0]:
+            raise ValueError("Detected signal cannot be constant")
+        self._alpha = {RelativeMagnitudeType.gibbons_ringdal_2006: float(gr[0]),
+                       RelativeMagnitudeType.schaff_richards_2014: float(sr[0])}
+
+    def have_detected_signal(self):
+        return self._alpha is not None
+
+    def compute_amplitude_scaling_factor(self, mag_type):
+        if self._b is None:
+            raise RuntimeError("Class is not initialized")
+        if self._alpha is None:
+            raise RuntimeError("Detected waveform not set")
+        return self._alpha[RelativeMagnitudeType(int(mag_type))]
+
+    def compute_magnitude_perturbation(self, mag_type):
+        a = self.compute_amplitude_scaling_factor(mag_type)
+        if a <= 0:
+            raise ValueError("Scaling factor = %g must be positive" % a)
+        return math.log10(a)

@@ -491,7 +491,8 @@ def _attach_detector():
     # pymflib.SingleChannel.{Detector, DetectorParameters, Detection, ...}
     from . import associator as a
     from . import detector as d
-    for name in ("Detector", "DetectorParameters", "DetectionTimeInterpolationParameters", "Detection"):
+    for name in ("Detector", "DetectorParameters", "DetectionTimeInterpolationParameters", "Detection",
+                 "RelativeMagnitude"):
         setattr(_SingleChannel, name, getattr(d, name))
     for name in ("Associator", "AssociatorParameters"):
         setattr(_SingleChannel, name, getattr(a, name))

@@ -206,6 +206,23 @@ class Oracle:
         return order, events
 
 
+    @staticmethod
+    def relative_amplitudes(b, windows):
+        """RelativeMagnitude<double> (src/singleChannel/relativeMagnitude.cpp:
+        35-130): per window y, |<b, y>| / <b, b> and sqrt(<y, y> / <b, b>) of
+        the demeaned template and window, sequential double sums."""
+        b = np.asarray(b, dtype=np.float64)
+        bd = b - np.sum(b) / b.size
+        bb = float(np.dot(bd, bd))
+        out = []
+        for y in np.atleast_2d(np.asarray(windows, dtype=np.float64)):
+            yd = y - np.sum(y) / y.size
+            yy = float(np.dot(yd, yd))
+            out.append((abs(float(np.dot(bd, yd))) / bb, np.sqrt(yy / bb), yy > 0))
+        gr, sr, ok = (np.array(v) for v in zip(*out))
+        return gr, sr, ok
+
+
 class Reference:
     """The reference's own classes (compiled against the FFTW/MKL shim)."""
 
@@ -224,11 +241,20 @@ class Reference:
                                      C.c_long, C.c_double, _dp, _dp, _dp, C.c_int, _dp, _ip]
         L.ref_peaks_d.argtypes = [C.c_int, _dp, C.c_double, C.c_int, _ip]
         L.ref_peaks_f.argtypes = [C.c_int, _fp, C.c_float, C.c_int, _ip]
+        L.ref_relmag_d.argtypes = [C.c_int, _dp, _dp, _dp, _dp]
         for nm in ("ref_detect_d", "ref_detect_f"):
             getattr(L, nm).argtypes = [C.c_int, _ip, C.c_void_p, C.c_int, C.c_void_p, C.c_double, C.c_double,
                                        C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                        _ip, _dp, _dp, _dp, _ip, _ip, _dp, _dp]
             getattr(L, nm).restype = C.c_int
+
+    def relative_amplitudes(self, b, y):
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        y = np.ascontiguousarray(y, dtype=np.float64)
+        gr, sr = C.c_double(), C.c_double()
+        if self.lib.ref_relmag_d(b.size, b.ctypes.data_as(_dp), y.ctypes.data_as(_dp), C.byref(gr), C.byref(sr)):
+            raise ValueError("reference RelativeMagnitude rejected the input")
+        return gr.value, sr.value
 
     def detect(self, templates, signal, fs, threshold=0.7, min_distance=0, absolute_maximum=False, single=False,
                interpolation=1, alpha=51, npts=100, amplitudes=True, dtype=np.float64, maxdet=100000):

@@ -28,6 +28,7 @@
 #include "mflib/singleChannel/detectorParameters.hpp"
 #include "mflib/singleChannel/detectionTimeInterpolationParameters.hpp"
 #include "mflib/singleChannel/detection.hpp"
+#include "mflib/singleChannel/relativeMagnitude.hpp"
 
 using namespace MFLib;
 
@@ -261,4 +262,23 @@ REF_API int ref_detect_f(int nt, const int *lens, const double *const *templates
 {
     return run_detect<float>(nt, lens, templates, n, signal, fs, thr, minDist, absMax, single, interp, alpha, npts,
                              amplitudes, maxdet, o_tmpl, o_xc, o_time, o_itime, o_pol, o_have, o_gr, o_sr);
+}
+
+/* RelativeMagnitude<double> of one window y against template b (both L
+ * samples): the two amplitude scaling factors; -1 if the reference throws. */
+REF_API int ref_relmag_d(int L, const double *b, const double *y, double *gr, double *sr)
+{
+    try
+    {
+        WaveformTemplate wt;
+        wt.setSignal(L, b);
+        wt.setSamplingRate(100.0);
+        SingleChannel::RelativeMagnitude<double> rm;
+        rm.initialize(wt);
+        rm.setDetectedSignal(L, y);
+        *gr = rm.computeAmplitudeScalingFactor(RelativeMagnitudeType::GIBBONS_RINGDAL_2006);
+        *sr = rm.computeAmplitudeScalingFactor(RelativeMagnitudeType::SCHAFF_RICHARDS_2014);
+        return 0;
+    }
+    catch (const std::exception &) { return -1; }
 }

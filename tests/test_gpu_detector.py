@@ -153,3 +153,33 @@ def test_detector_errors_and_waveforms(gpu, rng):
     np.testing.assert_array_equal(d.get_detected_signal(), x[t:t + 120])
     with pytest.raises(ValueError):
         det.get_detection(det.get_number_of_detections())
+
+
+@pytest.mark.parametrize("dtype", [np.float32, np.float64])
+def test_relative_magnitude(gpu, oracle, rng, dtype):
+    """RelativeMagnitude on the GPU against the restatement (pinned to the
+    reference's RelativeMagnitude<double>), one window and a batch."""
+    mf = gpu
+    L = 333
+    b = rng.standard_normal(L)
+    wt = mf.WaveformTemplate()
+    wt.set_signal(b)
+    wt.set_sampling_rate(100.0)
+    rm = mf.SingleChannel.RelativeMagnitude(dtype=dtype)
+    with pytest.raises(RuntimeError):
+        rm.compute_amplitude_scaling_factor(0)
+    rm.initialize(wt)
+    ys = (rng.uniform(0.1, 5, (50, 1)) * (b + 0.2 * rng.standard_normal((50, L))) + 7.0).astype(dtype)
+    gr, sr, ok = rm.amplitude_scaling_factors(ys)
+    g0, s0, ok0 = oracle.relative_amplitudes(b, ys.astype(np.float64))
+    assert ok.all() and ok0.all()
+    np.testing.assert_allclose(gr, g0, rtol=1e-10)
+    np.testing.assert_allclose(sr, s0, rtol=1e-10)
+    rm.set_detected_signal(ys[3])
+    assert abs(rm.compute_amplitude_scaling_factor(mf.RelativeMagnitudeType.gibbons_ringdal_2006) - g0[3]) <= 1e-10 * g0[3]
+    assert abs(rm.compute_magnitude_perturbation(mf.RelativeMagnitudeType.schaff_richards_2014)
+               - np.log10(s0[3])) < 1e-9
+    with pytest.raises(ValueError):
+        rm.set_detected_signal(np.full(L, 3.0, dtype=dtype))  # constant window
+    with pytest.raises(ValueError):
+        rm.set_detected_signal(ys[0, :10])

@@ -239,3 +239,41 @@ def test_associate_known_answer(oracle):
     assert len(events) == 2
     got = [(e, sorted(origin[order[k]] for k in m)) for e, m in events]
     assert got == [(7, [0.0, 0.1, 0.2]), (7, [10.0, 10.2, 10.4])]
+
+
+def test_relative_amplitudes_vs_reference(oracle, reference, rng):
+    """The amplitude restatement against RelativeMagnitude<double> compiled
+    unchanged (where the checkout exists)."""
+    for _ in range(20):
+        L = int(rng.integers(2, 600))
+        b = rng.standard_normal(L) + rng.uniform(-3, 3)
+        y = rng.uniform(0.1, 10) * (b + 0.3 * rng.standard_normal(L)) + rng.uniform(-50, 50)
+        g0, s0 = reference.relative_amplitudes(b, y)
+        gr, sr, ok = oracle.relative_amplitudes(b, y[None, :])
+        assert ok[0]
+        np.testing.assert_allclose([gr[0], sr[0]], [g0, s0], rtol=1e-12)
+
+
+def test_detection_pickling():
+    import pickle
+    import mflib_gb300 as mf
+    from mflib_gb300.detector import Detection, RelativeMagnitudeType
+    d = Detection()
+    nsp = mf.NetworkStationPhase()
+    nsp.set_network("UU")
+    d.set_template_identifier((nsp, 12))
+    d.set_correlation_coefficient(-0.75)
+    d.set_detection_time(10.5)
+    d.set_interpolated_detection_time(10.52)
+    d.set_travel_time(3.0)
+    d.set_polarity(mf.Polarity.dilatation)
+    d.set_amplitude_scaling_factor(2.5, RelativeMagnitudeType.gibbons_ringdal_2006)
+    d.set_detected_signal(np.arange(5.0))
+    e = pickle.loads(pickle.dumps(d))
+    assert e.get_template_identifier()[0].get_network() == "UU" and e.get_template_identifier()[1] == 12
+    assert e.get_correlation_coefficient() == -0.75 and e.get_interpolated_detection_time() == 10.52
+    assert e.get_polarity() == mf.Polarity.dilatation and e.get_travel_time() == 3.0
+    assert e.get_amplitude_scaling_factor(RelativeMagnitudeType.gibbons_ringdal_2006) == 2.5
+    assert not e.have_amplitude_scaling_factor(RelativeMagnitudeType.schaff_richards_2014)
+    np.testing.assert_array_equal(e.get_detected_signal(), np.arange(5.0))
+    assert not e.have_phase_onset_time()
