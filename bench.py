@@ -398,6 +398,98 @@ def run_detector(args):
     print(json.dumps(line), flush=True)
 
 
+def run_stress(args):
+    """Precision stress: 512 templates of 1,000 samples against 16 channels of
+    4.32 M samples (all pairs: each channel against every template, one
+    single-channel object reused per channel).  Signals: a DC offset
+    U(1e3, 1e5) plus band-passed noise under a piecewise-constant envelope
+    (segments of 10-60 min, levels log-uniform in [1e-3, 1e3]) with injected
+    template copies at 0.2-1 x the local RMS.  For the FP32 FFT correlator
+    and the split-precision tensor-core correlator: template-lags/s of the
+    applies (CUDA events) and max |drho| against the FP64 oracle on sampled
+    lags of 8 templates per channel, over all sampled lags and over lags
+    whose window and FFT blocks stay inside one envelope segment."""
+    import torch
+    import mflib_gb300 as mf
+    from scipy.signal import butter, sosfilt
+    from scipy.signal.windows import hann
+    from oracle.orc import Oracle
+    rng = np.random.default_rng(300)
+    nt, nch, L, n = 512, 16, 1000, args.samples if args.samples != N_SAMPLES else 4_320_000
+    tps = []
+    for _ in range(nt):
+        lo = rng.uniform(1.0, 7.0)
+        hi = rng.uniform(lo + 2.0, 15.0)
+        tps.append(sosfilt(butter(4, [lo, hi], btype="bandpass", fs=FS, output="sos"), rng.standard_normal(L))
+                   * hann(L))
+    sos = butter(4, [1.0, 10.0], btype="bandpass", fs=FS, output="sos")
+    chans, edges_all = [], []
+    for c in range(nch):
+        r = np.random.default_rng(3000 + c)
+        noise = sosfilt(sos, r.standard_normal(n))
+        env = np.empty(n)
+        edges = [0]
+        while edges[-1] < n:
+            edges.append(min(n, edges[-1] + int(r.integers(60_000, 360_001))))
+        for a, b in zip(edges[:-1], edges[1:]):
+            env[a:b] = 10.0 ** r.uniform(-3, 3)
+        x = env * noise
+        for o in r.integers(0, n - L, 40):
+            t = int(r.integers(nt))
+            lvl = env[o] * np.std(noise[o:o + L])
+            x[o:o + L] += r.uniform(0.2, 1.0) * lvl * tps[t] / np.std(tps[t])
+        chans.append((x + r.uniform(1e3, 1e5)).astype(np.float32))
+        edges_all.append(np.array(edges))
+    o = Oracle()
+    out = {}
+    for name, variant in (("fft", 3), ("tensor", 4)):
+        p = mf.SingleChannel.MatchedFilterParameters()
+        for tp in tps:
+            wt = mf.WaveformTemplate()
+            wt.set_signal(tp)
+            wt.set_sampling_rate(FS)
+            p.add_template(wt)
+        p.set_signal_size(n)
+        f = mf.SingleChannel.MatchedFilter(dtype=np.float32)
+        f.initialize(p, correlator_variant=variant)
+        stream = torch.cuda.ExternalStream(f.stream_handle())
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        total_ms, worst_all, worst_flat = 0.0, 0.0, 0.0
+        for c in range(nch):
+            f.set_signal(chans[c])
+            f.apply()  # warm
+            f.synchronize()
+            ev0.record(stream)
+            f.apply()
+            ev1.record(stream)
+            f.synchronize()
+            torch.cuda.synchronize()
+            total_ms += ev0.elapsed_time(ev1)
+            lr = np.random.default_rng(7 + c)
+            xs = chans[c].astype(np.float64)
+            e = edges_all[c]
+            for t in lr.choice(nt, 8, replace=False):
+                lags = np.sort(lr.choice(n - L + 1, 500, replace=False))
+                truth = o.pearson_naive(tps[t], xs, lags)
+                got = f.get_matched_filtered_signal(int(t)).astype(np.float64)[lags]
+                err = np.abs(got - truth)
+                worst_all = max(worst_all, float(err.max()))
+                seg = np.searchsorted(e, lags, side="right") - 1
+                flat = (lags - 8192 >= e[seg]) & (lags + L + 8192 <= e[seg + 1])
+                if flat.any():
+                    worst_flat = max(worst_flat, float(err[flat].max()))
+        lags_total = float(nch) * nt * (n - L + 1)
+        out[name] = {"template_lags_per_s": lags_total / (total_ms * 1e-3), "apply_ms_per_channel": total_ms / nch,
+                     "max_abs_drho_all": worst_all, "max_abs_drho_away_from_envelope_steps": worst_flat,
+                     "correlator": f.get_plan()["correlator"]}
+        f.clear()
+    line = {"metric": "precision stress: template-lag correlations/s and max |drho| vs FP64 oracle", "n_gpus": 1,
+            "dtype": "f32", "config": {"workload": "512 templates x 1,000 against 16 channels x %d samples, all pairs,"
+                                                   " DC 1e3..1e5, envelope 1e-3..1e3" % n},
+            "paths": out}
+    print(json.dumps(line), flush=True)
+
+
 def run_uneven(args):
     """The uneven bank: 2,000 templates of 200-3,000 samples (uniform) with
     random 1-15 Hz pass bands, each on one of 96 channels (uniform), against
@@ -494,6 +586,7 @@ def main():
     ap.add_argument("--uneven", action="store_true",
                     help="the 2,000-template uneven bank on 96 channels instead of the 24-channel day")
     ap.add_argument("--detector", action="store_true", help="time the single-channel detector")
+    ap.add_argument("--stress", action="store_true", help="precision stress: FFT and tensor-core paths")
     ap.add_argument("--length-buckets", type=int, default=0,
                     help="length buckets of a mixed-length bank (0 planner's choice, 1 one plan)")
     ap.add_argument("--rates", type=float, nargs="+", default=[50, 100, 200, 500, 0],
@@ -511,6 +604,9 @@ def main():
         return
     if args.detector:
         run_detector(args)
+        return
+    if args.stress:
+        run_stress(args)
         return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
