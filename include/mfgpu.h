@@ -227,6 +227,15 @@ typedef struct
 mfgpu_status mfgpu_mf_detect(mfgpu_mf *mf, const mfgpu_detect_params *params, int *n_detections);
 /* Copies up to max detections of the last mfgpu_mf_detect. */
 mfgpu_status mfgpu_mf_get_detections(mfgpu_mf *mf, int max, mfgpu_detection *out, int *n);
+/* Replay apply as a CUDA graph (extension, no reference counterpart):
+ * with enable != 0, the second apply with the same input buffer and
+ * peak-gathering setup captures the stream work (events, normalisation,
+ * correlators) into a graph, and later applies with that setup launch it;
+ * staged uploads alternate between two captured graphs.  Results are those
+ * of the direct launches.  Call it outside any stream capture. */
+mfgpu_status mfgpu_mf_set_graph(mfgpu_mf *mf, int enable);
+/* Number of applies launched as graphs so far. */
+mfgpu_status mfgpu_mf_get_graph_launches(const mfgpu_mf *mf, long long *count);
 /* Relative amplitudes of detected windows against one template:
  * RelativeMagnitude<T>::computeAmplitudeScalingFactor
  * (src/singleChannel/relativeMagnitude.cpp:35-130, :334-372) for a batch of

@@ -106,6 +106,8 @@ _SIGS = {
     "mfgpu_mf_get_correlator": ([_vp, _ip, _ip, _ip], C.c_int),
     "mfgpu_mf_get_buckets": ([_vp, C.c_int, _ip, _ip, _ip], C.c_int),
     "mfgpu_mf_detect": ([_vp, C.POINTER(MfgpuDetectParams), _ip], C.c_int),
+    "mfgpu_mf_set_graph": ([_vp, C.c_int], C.c_int),
+    "mfgpu_mf_get_graph_launches": ([_vp, C.POINTER(C.c_longlong)], C.c_int),
     "mfgpu_relative_amplitudes": ([C.c_int, C.c_int, _vp, C.c_int, _vp, C.c_long, _vp, _vp, _ip], C.c_int),
     "mfgpu_mf_get_detections": ([_vp, C.c_int, C.POINTER(MfgpuDetection), _ip], C.c_int),
     "mfgpu_mf_set_window": ([_vp, C.c_int, C.c_int, _vp, C.c_long], C.c_int),

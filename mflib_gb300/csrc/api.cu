@@ -174,6 +174,38 @@ struct mfgpu_mf
     // traces), detection rows and results
     DevBuf det_buf, det_id, det_rows, det_out, tchan_d;
     std::vector<mfgpu_detection> dets;
+    // apply replayed as a CUDA graph (mfgpu_mf_set_graph): one executable
+    // per input buffer and peak-gathering setup; captured on the second
+    // apply with the same setup (the first sizes every buffer)
+    struct ApplyGraph
+    {
+        cudaGraphExec_t exec = nullptr;
+        const void *x = nullptr, *pk_cnt = nullptr, *pk_flags = nullptr;
+        double pk_req = -2;
+        bool pk_fused = false;
+        double pk_fused_thr = 0;
+        int pk_fused_len = 0, pk_words = 0;
+        long long launches = 0;
+        bool same(const ApplyGraph &o) const
+        {
+            return x == o.x && pk_cnt == o.pk_cnt && pk_flags == o.pk_flags && pk_req == o.pk_req;
+        }
+    };
+    bool use_graph = false;
+    ApplyGraph graphs[2];
+    int graph_next = 0;
+    ApplyGraph last_direct[2];  // setups of the last direct applies (one per input buffer)
+    int direct_next = 0;
+    long long graph_launches = 0;  // replays of captured applies
+    void drop_graphs()
+    {
+        for (ApplyGraph &g : graphs)
+        {
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+            g = ApplyGraph();
+        }
+        last_direct[0] = last_direct[1] = ApplyGraph();
+    }
     int ntemplates0 = 0;
     DevBuf row_S, row_nblk;
     int pk_stride = 0;
@@ -211,6 +243,7 @@ struct mfgpu_mf
     }
     void reset()
     {
+        drop_graphs();
         if (copy_stream) cudaStreamSynchronize(copy_stream);
         if (stream) cudaStreamSynchronize(stream);
         staged = false;
@@ -251,8 +284,12 @@ static mfgpu_status mf_sync(mfgpu_mf *mf, bool copies = false)
     }
     if (mf->timed)
     {
-        cudaEventElapsedTime(&mf->last_xcorr_ms, mf->ev[1], mf->ev[2]);
-        cudaEventElapsedTime(&mf->last_apply_ms, mf->ev[0], mf->ev[3]);
+        if (cudaEventElapsedTime(&mf->last_xcorr_ms, mf->ev[1], mf->ev[2]) != cudaSuccess ||
+            cudaEventElapsedTime(&mf->last_apply_ms, mf->ev[0], mf->ev[3]) != cudaSuccess)
+        {
+            (void) cudaGetLastError();  // timings unavailable: not an error of the work
+            mf->last_xcorr_ms = mf->last_apply_ms = 0.f;
+        }
         mf->timed = false;
     }
     return MFGPU_OK;
@@ -1127,6 +1164,18 @@ mfgpu_status mfgpu_mf_get_signal(const mfgpu_mf *cmf, int it, int maxn, void *ds
     return MFGPU_OK;
 }
 
+// Records ev on the object's stream.  While apply is being captured into a
+// graph the record must be external, or the replays would not record it
+// (the staging buffers' reuse and the timings depend on these events).
+static cudaError_t mf_record(mfgpu_mf *mf, cudaEvent_t ev)
+{
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(mf->stream, &cs);
+    if (e != cudaSuccess) return e;
+    return cudaEventRecordWithFlags(ev, mf->stream,
+                                    cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault);
+}
+
 template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
 {
     XcorrParams<T> p{};
@@ -1167,7 +1216,7 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
         p.pk_idx = mf->pk_idx.as<int>();
         p.pk_val = mf->pk_val.as<T>();
     }
-    CU(cudaEventRecord(mf->ev[1], mf->stream));
+    CU(mf_record(mf, mf->ev[1]));
     if constexpr (sizeof(T) == 4)
     {
         if (mf->tc)
@@ -1229,6 +1278,26 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
     return MFGPU_OK;
 }
 
+// the stream work of one apply (events, normalisation, correlators)
+static mfgpu_status mf_apply_body(mfgpu_mf *mf)
+{
+    CU(mf_record(mf, mf->ev[0]));
+    if (mf->nblocks > 0)
+    {
+        // records ev[1] between the normalisation and the correlator
+        mfgpu_status st = mf->prec == 4 ? mf_launch_xcorr<float>(mf) : mf_launch_xcorr<double>(mf);
+        if (st != MFGPU_OK) return st;
+    }
+    else
+    {
+        CU(mf_record(mf, mf->ev[1]));
+    }
+    CU(mf_record(mf, mf->ev[2]));
+    CU(mf_record(mf, mf->ev[3]));
+    CU(mf_record(mf, mf->x_ev));  // the last read of x by this apply
+    return MFGPU_OK;
+}
+
 mfgpu_status mfgpu_mf_apply(mfgpu_mf *mf)
 {
     if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");
@@ -1238,22 +1307,95 @@ mfgpu_status mfgpu_mf_apply(mfgpu_mf *mf)
     if (rs != MFGPU_OK) return rs;
     mf->have = false;
     mf->have_peaks = false;
-    CU(cudaEventRecord(mf->ev[0], mf->stream));
-    if (mf->nblocks > 0)
+    if (mf->use_graph)
     {
-        // records ev[1] between the normalisation and the correlator
-        mfgpu_status st = mf->prec == 4 ? mf_launch_xcorr<float>(mf) : mf_launch_xcorr<double>(mf);
-        if (st != MFGPU_OK) return st;
+        mfgpu_mf::ApplyGraph key;
+        key.x = mf->x.p;
+        key.pk_cnt = mf->pk_cnt.p;
+        key.pk_flags = mf->pk_flags.p;
+        key.pk_req = mf->pk_req;
+        for (mfgpu_mf::ApplyGraph &gr : mf->graphs)
+            if (gr.exec && gr.same(key))
+            {
+                CU(cudaGraphLaunch(gr.exec, mf->stream));
+                mf->pk_fused = gr.pk_fused;
+                mf->pk_fused_thr = gr.pk_fused_thr;
+                mf->pk_fused_len = gr.pk_fused_len;
+                mf->pk_words = gr.pk_words;
+                mf->launches += gr.launches;
+                ++mf->graph_launches;
+                mf->timed = true;
+                mf->have = true;
+                return MFGPU_OK;
+            }
+        if (mf->last_direct[0].same(key) || mf->last_direct[1].same(key))
+        {
+            // every buffer of this setup is sized: capture the stream work
+            const long long l0 = mf->launches;
+            CU(cudaStreamBeginCapture(mf->stream, cudaStreamCaptureModeThreadLocal));
+            mfgpu_status st = mf_apply_body(mf);
+            cudaGraph_t graph = nullptr;
+            cudaError_t e = cudaStreamEndCapture(mf->stream, &graph);
+            if (st != MFGPU_OK)
+            {
+                if (graph) cudaGraphDestroy(graph);
+                return st;
+            }
+            if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+            cudaGraphExec_t exec = nullptr;
+            e = cudaGraphInstantiate(&exec, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+            mfgpu_mf::ApplyGraph &slot = mf->graphs[mf->graph_next];
+            mf->graph_next ^= 1;
+            if (slot.exec) cudaGraphExecDestroy(slot.exec);
+            slot = key;
+            slot.exec = exec;
+            slot.pk_fused = mf->pk_fused;
+            slot.pk_fused_thr = mf->pk_fused_thr;
+            slot.pk_fused_len = mf->pk_fused_len;
+            slot.pk_words = mf->pk_words;
+            slot.launches = mf->launches - l0;
+            CU(cudaGraphLaunch(exec, mf->stream));
+            ++mf->graph_launches;
+            mf->timed = true;
+            mf->have = true;
+            return MFGPU_OK;
+        }
     }
-    else
+    mfgpu_status st = mf_apply_body(mf);
+    if (st != MFGPU_OK) return st;
+    if (mf->use_graph)
     {
-        CU(cudaEventRecord(mf->ev[1], mf->stream));
+        // the direct run may have resized buffers: the setup is taken after it
+        mfgpu_mf::ApplyGraph &d = mf->last_direct[mf->direct_next];
+        mf->direct_next ^= 1;
+        d = mfgpu_mf::ApplyGraph();
+        d.x = mf->x.p;
+        d.pk_cnt = mf->pk_cnt.p;
+        d.pk_flags = mf->pk_flags.p;
+        d.pk_req = mf->pk_req;
     }
-    CU(cudaEventRecord(mf->ev[2], mf->stream));
-    CU(cudaEventRecord(mf->ev[3], mf->stream));
-    CU(cudaEventRecord(mf->x_ev, mf->stream));  // the last read of x by this apply
     mf->timed = true;
     mf->have = true;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_set_graph(mfgpu_mf *mf, int enable)
+{
+    if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");
+    DeviceGuard g(mf->dev);
+    if (mf->copy_stream) CU(cudaStreamSynchronize(mf->copy_stream));
+    CU(cudaStreamSynchronize(mf->stream));
+    mf->drop_graphs();
+    mf->use_graph = enable != 0;
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_get_graph_launches(const mfgpu_mf *mf, long long *count)
+{
+    if (!mf || !count) return fail(MFGPU_EINVAL, "NULL argument");
+    *count = mf->graph_launches;
     return MFGPU_OK;
 }
 

@@ -298,6 +298,16 @@ class MatchedFilter:
         _lib.call("mfgpu_mf_set_window", self._h, int(x.shape[0]), int(x.shape[1]), x.ctypes.data_as(C.c_void_p),
                   int(x.strides[0] // x.itemsize))
 
+    def set_graph(self, enable=True):
+        """Extension: replay apply as a CUDA graph (captured on the second
+        apply with the same input buffer and peak-gathering setup)."""
+        _lib.call("mfgpu_mf_set_graph", self._h, 1 if enable else 0)
+
+    def graph_launches(self):
+        v = C.c_longlong()
+        _lib.call("mfgpu_mf_get_graph_launches", self._h, C.byref(v))
+        return v.value
+
     def device_bytes(self):
         """Device memory held by this object (buffers and peak scratch)."""
         v = C.c_ulonglong()

@@ -152,6 +152,7 @@ class GpuExecutor:
             p.set_signal_size(int(n))
             f.initialize(p, template_channels=[int(s) for s in bank.slots], n_channels=N_SLOTS,
                          correlator_variant=self.correlator_variant)
+        f.set_graph(True)  # a pooled object's applies replay one CUDA graph
         return f
 
     def device_bytes(self, f):

@@ -564,3 +564,38 @@ def test_tensor_core_errors(gpu, rng):
     g = mf.MultiChannel.MatchedFilter(dtype=np.float64)
     with pytest.raises(ValueError):
         g.initialize(_params(mf, [rng.standard_normal(100)], 5000), correlator_variant=4)  # FP32 only
+
+
+@pytest.mark.parametrize("variant", [0, 4, 1])
+def test_apply_graph_replay(gpu, rng, variant):
+    """apply replayed as a CUDA graph gives the direct launches' results
+    bit for bit, through staged uploads that alternate the input buffers and
+    with candidate gathering on; FFT organisations and tensor cores."""
+    mf = gpu
+    n, L = 50_000, 200
+    assign = [0, 0, 1, 1, 2, 2]
+    tps = [rng.standard_normal(L) for _ in assign]
+    p = _params(mf, tps, n)
+    objs = []
+    for graph in (False, True):
+        f = mf.MultiChannel.MatchedFilter(dtype=np.float32)
+        f.initialize(p, template_channels=assign, n_channels=3, correlator_variant=variant)
+        f.set_peak_threshold(0.3)
+        f.set_graph(graph)
+        objs.append(f)
+    plain, graphed = objs
+    for step in range(6):
+        x = rng.standard_normal((3, n)).astype(np.float32)
+        for f in objs:
+            f.stage_channel_signals(x)
+            f.apply()
+            f.find_peaks(0.3, 50)
+        for t in range(len(assign)):
+            np.testing.assert_array_equal(graphed.get_matched_filtered_signal(t), plain.get_matched_filtered_signal(t))
+        for a, b in zip(graphed.get_all_peaks(), plain.get_all_peaks()):
+            np.testing.assert_array_equal(a, b)
+    assert graphed.graph_launches() >= 2 and plain.graph_launches() == 0
+    # same input again: replayed too
+    k = graphed.graph_launches()
+    graphed.apply()
+    assert graphed.graph_launches() == k + 1
