@@ -87,7 +87,7 @@ class DetectionRequest:
         self.keep = tuple(int(t) for t in keep)
         self.t_arrival = arrival
         self.t_start = self.t_done = None
-        self.peaks = None  # list of int32 index arrays, one per template
+        self.peaks = None  # per template its int32 peak indices (peaks[t])
         self.rho = {}
         self.error = None
         self.lags = 0
@@ -112,6 +112,33 @@ class DetectionRequest:
         if self.error is not None:
             raise self.error
         return self
+
+
+class _Peaks:
+    """Peak indices of every template of a request, kept as one flat array
+    with offsets; template t's indices are sliced out when asked for."""
+
+    __slots__ = ("_off", "_idx")
+
+    def __init__(self, counts, idx):
+        self._off = np.concatenate([[0], np.cumsum(counts)])
+        self._idx = idx
+
+    def __len__(self):
+        return self._off.size - 1
+
+    def __getitem__(self, t):
+        if t < 0:
+            t += len(self)
+        if not 0 <= t < len(self):
+            raise IndexError(t)
+        return self._idx[self._off[t]:self._off[t + 1]]
+
+    def __iter__(self):
+        return (self[t] for t in range(len(self)))
+
+    def counts(self):
+        return np.diff(self._off)
 
 
 class GpuExecutor:
@@ -164,11 +191,9 @@ class GpuExecutor:
         nv = bank.valid_lags(req.n)
         if nv > 0:
             f.find_peaks(self.threshold, self.min_distance, nv)
-            counts, idx = f.get_all_peaks()
-            offs = np.concatenate([[0], np.cumsum(counts)])
-            req.peaks = [idx[offs[t]:offs[t + 1]] for t in range(len(bank))]
+            req.peaks = _Peaks(*f.get_all_peaks())
         else:
-            req.peaks = [np.zeros(0, np.int32) for _ in range(len(bank))]
+            req.peaks = _Peaks(np.zeros(len(bank), np.int64), np.zeros(0, np.int32))
         for t in req.keep:
             req.rho[t] = f.get_matched_filtered_signal(t)[:nv].copy()
         req.lags = len(bank) * nv
