@@ -364,24 +364,31 @@ static __global__ void __launch_bounds__(kTcThreads, 1) tc_xcorr_kernel(TcParams
                     const int t = eg + 2 * (b0 + u);
                     const int tt = p.grp_tid[g * Gp + t];
                     if (tt < 0) continue;
-                    const float sc = p.bscale[g * Gp + t] / s;
+                    // a dead channel's tiles store zeros (sc = 0, no flags)
+                    const float sc = dead ? 0.f : p.bscale[g * Gp + t] / s;
                     float o[8];
 #pragma unroll
                     for (int f = 0; f < 8; ++f)
-                        o[f] = dead ? 0.f
-                                    : clamp_rho((__uint_as_float(r[u][f]) + __uint_as_float(h[u][f])) * sc * dcur[f]);
+                        o[f] = clamp_rho((__uint_as_float(r[u][f]) + __uint_as_float(h[u][f])) * sc * dcur[f]);
                     if (p.pk_flags)
                     {
                         // one bit per 64 lags (8 rows); values above the
                         // threshold are rare, so each such row sets its bit
-                        // itself, without a warp-wide vote
-                        bool above = false;
+                        // itself, without a warp-wide vote; the lag bound
+                        // matters only in the last tile
+                        float mx = o[0];
 #pragma unroll
-                        for (int f = 0; f < 8; ++f) above |= lag0 + f < p.nv && o[f] > p.pk_thr;
-                        if (above)
+                        for (int f = 1; f < 8; ++f) mx = fmaxf(mx, o[f]);
+                        if (mx > p.pk_thr)
                         {
-                            const long c = lag0 >> 6;
-                            atomicOr(p.pk_flags + (long) tt * p.pk_words + (c >> 5), 1u << (c & 31));
+                            bool above = false;
+#pragma unroll
+                            for (int f = 0; f < 8; ++f) above |= lag0 + f < p.nv && o[f] > p.pk_thr;
+                            if (above)
+                            {
+                                const long c = lag0 >> 6;
+                                atomicOr(p.pk_flags + (long) tt * p.pk_words + (c >> 5), 1u << (c & 31));
+                            }
                         }
                     }
                     float *dst = p.rho + (long) tt * p.ldr + lag0;
