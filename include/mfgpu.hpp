@@ -42,6 +42,10 @@ namespace MFLib
 enum class MatchedFilterImplementation { DIRECT, OVERLAP_ADD, AUTO };
 enum class MatchedFilterDetectionMode { SINGLE_CHANNEL, MULTI_CHANNEL };
 enum class Polarity : int { UNKNOWN = 0, COMPRESSION = 1, DILATATION = -1 };
+enum class RelativeMagnitudeType { GIBBONS_RINGDAL_2006 = 0, SCHAFF_RICHARDS_2014 };
+enum class MaximumMatchedFilterPolicy { MAXIMUM = 0, ABSOLUTE_MAXIMUM };
+enum class MatchedFilteredSignalDetectorPolicy { REDUCED = 0, SINGLE };
+enum class DetectionTimeInterpolationType { LANCZOS = 0, QUADRATIC, NONE };
 
 namespace detail
 {
@@ -542,6 +546,237 @@ template <class T = double> class MatchedFilter
 
   private:
     MFLib::MatchedFilter<T> mF;
+};
+
+/* MFLib::SingleChannel::DetectionTimeInterpolationParameters
+   (src/singleChannel/detectionTimeInterpolationParameters.cpp) */
+class DetectionTimeInterpolationParameters
+{
+  public:
+    void clear() noexcept { *this = DetectionTimeInterpolationParameters(); }
+    void enableLanczos() noexcept { mType = DetectionTimeInterpolationType::LANCZOS; }
+    void enableQuadratic() noexcept { mType = DetectionTimeInterpolationType::QUADRATIC; }
+    void disable() noexcept { mType = DetectionTimeInterpolationType::NONE; }
+    DetectionTimeInterpolationType getType() const noexcept { return mType; }
+    void setLanczosAlpha(int alpha)
+    {
+        if (alpha < 1) throw std::invalid_argument("alpha must be positive");
+        mAlpha = alpha;
+    }
+    int getLanczosAlpha() const noexcept { return mAlpha; }
+    void setLanczosNumberOfInterpolationPoints(int npts)
+    {
+        if (npts < 1) throw std::invalid_argument("Number of interpolation points must be positive");
+        mPoints = npts;
+    }
+    int getLanczosNumberOfInterpolationPoints() const noexcept { return mPoints; }
+
+  private:
+    int mAlpha = 51, mPoints = 100;
+    DetectionTimeInterpolationType mType = DetectionTimeInterpolationType::QUADRATIC;
+};
+
+/* MFLib::SingleChannel::DetectorParameters (src/singleChannel/detectorParameters.cpp:9-26) */
+class DetectorParameters
+{
+  public:
+    void clear() noexcept { *this = DetectorParameters(); }
+    void setDetectionThreshold(double tol)
+    {
+        if (tol <= 0 || tol > 1) throw std::invalid_argument("Threshold must be in range (0,1]");
+        mThreshold = tol;
+    }
+    double getDetectionThreshold() const noexcept { return mThreshold; }
+    void setMinimumDetectionSpacing(int n) noexcept { mMinSpacing = n; }
+    int getMinimumDetectionSpacing() const noexcept { return mMinSpacing; }
+    void setMatchedFilteredSignalDetectorPolicy(MatchedFilteredSignalDetectorPolicy p) noexcept { mPolicy = p; }
+    MatchedFilteredSignalDetectorPolicy getMatchedFilteredSignalDetectorPolicy() const noexcept { return mPolicy; }
+    void setMaximaPolicy(MaximumMatchedFilterPolicy p) noexcept { mMax = p; }
+    MaximumMatchedFilterPolicy getMaximaPolicy() const noexcept { return mMax; }
+    void enableSaveDetectedWaveform() noexcept { mWave = true; }
+    void disableSaveDetectedWaveform() noexcept { mWave = false; }
+    bool wantDetectedWaveform() const noexcept { return mWave; }
+    void enableSaveAmplitudeScalingFactor() noexcept { mAmp = true; }
+    void disableSaveAmplitudeScalingFactor() noexcept { mAmp = false; }
+    bool wantAmplitudeScalingFactor() const noexcept { return mAmp; }
+    void setDetectionTimeInterpolationParameters(const DetectionTimeInterpolationParameters &p) noexcept
+    {
+        mInterp = p;
+    }
+    const DetectionTimeInterpolationParameters &getDetectionTimeInterpolationParameters() const noexcept
+    {
+        return mInterp;
+    }
+
+  private:
+    double mThreshold = 0.7;
+    int mMinSpacing = 0;
+    MaximumMatchedFilterPolicy mMax = MaximumMatchedFilterPolicy::MAXIMUM;
+    MatchedFilteredSignalDetectorPolicy mPolicy = MatchedFilteredSignalDetectorPolicy::SINGLE;
+    bool mWave = false, mAmp = true;
+    DetectionTimeInterpolationParameters mInterp;
+};
+
+/* MFLib::SingleChannel::Detection<T> (src/singleChannel/detection.cpp): the
+   value fields the detector fills, each with get / set / have */
+template <class T = double> class Detection
+{
+  public:
+    void setTemplateIdentifier(const std::pair<NetworkStationPhase, uint64_t> &id) { mId = id; mHaveId = true; }
+    std::pair<NetworkStationPhase, uint64_t> getTemplateIdentifier() const
+    {
+        if (!mHaveId) throw std::runtime_error("Template identifier not set");
+        return mId;
+    }
+    bool haveTemplateIdentifier() const noexcept { return mHaveId; }
+    void setCorrelationCoefficient(double v)
+    {
+        if (v < -1 || v > 1) throw std::invalid_argument("Correlation coefficient must be in range [-1,1]");
+        mXc = v;
+        mHaveXc = true;
+    }
+    double getCorrelationCoefficient() const { return get(mXc, mHaveXc, "Correlation coefficient"); }
+    bool haveCorrelationCoefficient() const noexcept { return mHaveXc; }
+    void setDetectedSignal(int n, const T x[]) { mSignal.assign(x, x + n); }
+    const T *getDetectedSignalPointer() const
+    {
+        if (mSignal.empty()) throw std::runtime_error("Detected signal not set");
+        return mSignal.data();
+    }
+    int getDetectedSignalLength() const { return (int) mSignal.size(); }
+    bool haveDetectedSignal() const noexcept { return !mSignal.empty(); }
+    void setDetectionTime(double t) { mT = t; mHaveT = true; }
+    double getDetectionTime() const { return get(mT, mHaveT, "Detection time"); }
+    bool haveDetectionTime() const noexcept { return mHaveT; }
+    void setInterpolatedDetectionTime(double t) { mTi = t; mHaveTi = true; }
+    double getInterpolatedDetectionTime() const { return get(mTi, mHaveTi, "Interpolated detection time"); }
+    bool haveInterpolatedDetectionTime() const noexcept { return mHaveTi; }
+    void setTravelTime(double t) { mTt = t; mHaveTt = true; }
+    double getTravelTime() const { return get(mTt, mHaveTt, "Travel time"); }
+    bool haveTravelTime() const noexcept { return mHaveTt; }
+    void setPhaseOnsetTime(double t) { mPo = t; mHavePo = true; }
+    double getPhaseOnsetTime() const { return get(mPo, mHavePo, "Phase onset time"); }
+    bool havePhaseOnsetTime() const noexcept { return mHavePo; }
+    void setInterpolatedPhaseOnsetTime(double t) { mPoi = t; mHavePoi = true; }
+    double getInterpolatedPhaseOnsetTime() const { return get(mPoi, mHavePoi, "Interpolated phase onset time"); }
+    bool haveInterpolatedPhaseOnsetTime() const noexcept { return mHavePoi; }
+    void setAmplitudeScalingFactor(T value, RelativeMagnitudeType type)
+    {
+        mAmp[(int) type] = value;
+        mHaveAmp[(int) type] = true;
+    }
+    T getAmplitudeScalingFactor(RelativeMagnitudeType type) const
+    {
+        if (!mHaveAmp[(int) type]) throw std::runtime_error("Amplitude scaling factor not set");
+        return mAmp[(int) type];
+    }
+    bool haveAmplitudeScalingFactor(RelativeMagnitudeType type) const noexcept { return mHaveAmp[(int) type]; }
+    T getMagnitudePerturbation(RelativeMagnitudeType type) const
+    {
+        const T a = getAmplitudeScalingFactor(type);
+        if (a <= 0) throw std::invalid_argument("Scaling factor must be positive");
+        return std::log10(a);
+    }
+    void setPolarity(Polarity p) noexcept { mPol = p; }
+    Polarity getPolarity() const noexcept { return mPol; }
+
+  private:
+    static double get(double v, bool have, const char *what)
+    {
+        if (!have) throw std::runtime_error(std::string(what) + " not set");
+        return v;
+    }
+    std::pair<NetworkStationPhase, uint64_t> mId;
+    double mXc = 0, mT = 0, mTi = 0, mTt = 0, mPo = 0, mPoi = 0;
+    bool mHaveId = false, mHaveXc = false, mHaveT = false, mHaveTi = false, mHaveTt = false, mHavePo = false,
+         mHavePoi = false;
+    T mAmp[2] = {0, 0};
+    bool mHaveAmp[2] = {false, false};
+    std::vector<T> mSignal;
+    Polarity mPol = Polarity::UNKNOWN;
+};
+
+/* MFLib::SingleChannel::Detector<T> (src/singleChannel/detector.cpp:385-691):
+   the data-parallel work in one mfgpu_mf_detect call, the Detection objects
+   filled from the templates' metadata */
+template <class T = double> class Detector
+{
+  public:
+    void clear() noexcept
+    {
+        mInit = false;
+        mDets.clear();
+    }
+    void initialize(const DetectorParameters &parameters)
+    {
+        clear();
+        mP = parameters;
+        mInit = true;
+    }
+    bool isInitialized() const noexcept { return mInit; }
+    void detect(const MFLib::SingleChannel::MatchedFilter<T> &mf)
+    {
+        mDets.clear();
+        if (!mInit) throw std::invalid_argument("Detector class not initialized");
+        if (!mf.haveMatchedFilteredSignals()) throw std::invalid_argument("Matched filtered signals not computed");
+        const int nt = mf.getNumberOfTemplates();
+        std::vector<WaveformTemplate> tps;
+        for (int t = 0; t < nt; ++t) tps.push_back(mf.getWaveformTemplate(t));
+        const DetectionTimeInterpolationParameters &ip = mP.getDetectionTimeInterpolationParameters();
+        mfgpu_detect_params dp{};
+        dp.threshold = std::min(1.0, std::max(0.0, mP.getDetectionThreshold()));
+        dp.min_distance = mP.getMinimumDetectionSpacing();
+        dp.absolute_maximum = mP.getMaximaPolicy() == MaximumMatchedFilterPolicy::ABSOLUTE_MAXIMUM;
+        dp.single = mP.getMatchedFilteredSignalDetectorPolicy() == MatchedFilteredSignalDetectorPolicy::SINGLE;
+        dp.interpolation = (int) ip.getType();
+        dp.lanczos_alpha = ip.getLanczosAlpha();
+        dp.lanczos_points = ip.getLanczosNumberOfInterpolationPoints();
+        dp.sampling_rate = tps.at(0).getSamplingRate();
+        dp.amplitudes = mP.wantAmplitudeScalingFactor();
+        int n = 0;
+        detail::check(mfgpu_mf_detect(mf.handle(), &dp, &n));
+        std::vector<mfgpu_detection> raw(std::max(1, n));
+        detail::check(mfgpu_mf_get_detections(mf.handle(), n, raw.data(), &n));
+        const T *signal = mP.wantDetectedWaveform() ? mf.getSignalPointer() : nullptr;
+        const int ns = mf.getSignalLength();
+        for (int i = 0; i < n; ++i)
+        {
+            const mfgpu_detection &r = raw[i];
+            const WaveformTemplate &wt = tps[r.template_index];
+            Detection<T> d;
+            if (wt.haveIdentifier()) d.setTemplateIdentifier(wt.getIdentifier());
+            else d.setTemplateIdentifier({NetworkStationPhase(), (uint64_t) r.template_index});
+            d.setCorrelationCoefficient(r.correlation);
+            d.setDetectionTime(r.detection_time);
+            d.setInterpolatedDetectionTime(r.interpolated_time);
+            if (wt.havePhaseOnsetTime())
+            {
+                d.setPhaseOnsetTime(r.detection_time + wt.getPhaseOnsetTime());
+                d.setInterpolatedPhaseOnsetTime(r.interpolated_time + wt.getPhaseOnsetTime());
+            }
+            d.setPolarity((Polarity) (r.sign * (int) wt.getPolarity()));
+            if (wt.haveTravelTime()) d.setTravelTime(wt.getTravelTime());
+            if (r.have_amplitude)
+            {
+                d.setAmplitudeScalingFactor((T) r.gibbons_ringdal, RelativeMagnitudeType::GIBBONS_RINGDAL_2006);
+                d.setAmplitudeScalingFactor((T) r.schaff_richards, RelativeMagnitudeType::SCHAFF_RICHARDS_2014);
+            }
+            if (signal)
+                d.setDetectedSignal(std::min(wt.getSignalLength(), ns - r.sample), signal + r.sample);
+            mDets.push_back(std::move(d));
+        }
+    }
+    int getNumberOfDetections() const noexcept { return (int) mDets.size(); }
+    Detection<T> getDetection(int id) const
+    {
+        if (id < 0 || id >= (int) mDets.size()) throw std::invalid_argument("detection index out of range");
+        return mDets[id];
+    }
+
+  private:
+    DetectorParameters mP;
+    std::vector<Detection<T>> mDets;
+    bool mInit = false;
 };
 }  // namespace SingleChannel
 

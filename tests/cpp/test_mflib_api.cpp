@@ -351,6 +351,78 @@ void test_value_types()
     require(throws_invalid([&] { p.addTemplate(wt); }), "template without a signal rejected");
 }
 
+// The detector on a signal holding exact copies of two templates at known
+// samples: REDUCED and SINGLE policies find each copy with coefficient 1 at
+// its sample, the quadratic refinement of a self match stays within a sample,
+// the polarity follows the template's, the amplitude of a copy scaled by 3 is
+// 3 (Gibbons-Ringdal and Schaff-Richards).
+void test_detector()
+{
+    const int n = 6000, L = 150;
+    std::vector<double> x(n), t0(L), t1(L);
+    unsigned s = 7;
+    auto rnd = [&] {
+        s = s * 1664525u + 1013904223u;
+        return ((s >> 8) & 0xFFFF) / 65536.0 - 0.5;
+    };
+    for (double &v : x) v = 0.1 * rnd();
+    for (int i = 0; i < L; ++i)
+    {
+        t0[i] = std::sin(0.21 * i) * std::exp(-0.01 * i) + 0.05 * rnd();
+        t1[i] = std::cos(0.37 * i) * std::exp(-0.02 * i) + 0.05 * rnd();
+    }
+    const int at0 = 1000, at1 = 3500;
+    for (int i = 0; i < L; ++i)
+    {
+        x[at0 + i] = 3.0 * t0[i];
+        x[at1 + i] = -2.0 * t1[i];
+    }
+    MFLib::SingleChannel::MatchedFilterParameters p;
+    for (const auto *t : {&t0, &t1})
+    {
+        MFLib::WaveformTemplate wt;
+        wt.setSignal(L, t->data());
+        wt.setSamplingRate(100.0);
+        wt.setPolarity(MFLib::Polarity::COMPRESSION);
+        wt.setPhaseOnsetTime(0.0);
+        p.addTemplate(wt);
+    }
+    p.setSignalSize(n);
+    MFLib::SingleChannel::MatchedFilter<double> mf;
+    mf.initialize(p);
+    mf.setSignal(n, x.data());
+    mf.apply();
+    for (auto policy : {MFLib::MatchedFilteredSignalDetectorPolicy::REDUCED,
+                        MFLib::MatchedFilteredSignalDetectorPolicy::SINGLE})
+    {
+        MFLib::SingleChannel::DetectorParameters dp;
+        dp.setDetectionThreshold(0.95);
+        dp.setMinimumDetectionSpacing(100);
+        dp.setMaximaPolicy(MFLib::MaximumMatchedFilterPolicy::ABSOLUTE_MAXIMUM);
+        dp.setMatchedFilteredSignalDetectorPolicy(policy);
+        MFLib::SingleChannel::Detector<double> det;
+        det.initialize(dp);
+        det.detect(mf);
+        require(det.getNumberOfDetections() == 2, "detector: two detections");
+        auto a = det.getDetection(0), b = det.getDetection(1);
+        require(std::abs(a.getDetectionTime() - at0 / 100.0) < 1e-12 && a.getTemplateIdentifier().second == 0,
+                "detector: first copy at its sample, template 0");
+        require(std::abs(b.getDetectionTime() - at1 / 100.0) < 1e-12 && b.getTemplateIdentifier().second == 1,
+                "detector: second copy at its sample, template 1");
+        require(std::abs(a.getCorrelationCoefficient() - 1.0) < 1e-9 &&
+                    std::abs(b.getCorrelationCoefficient() + 1.0) < 1e-9,
+                "detector: coefficients +1 and -1");
+        require(std::abs(a.getInterpolatedDetectionTime() - a.getDetectionTime()) <= 0.01,
+                "detector: refinement within a sample");
+        require(a.getPolarity() == MFLib::Polarity::COMPRESSION && b.getPolarity() == MFLib::Polarity::DILATATION,
+                "detector: polarity from the coefficient's sign");
+        require(std::abs(a.getAmplitudeScalingFactor(MFLib::RelativeMagnitudeType::GIBBONS_RINGDAL_2006) - 3.0) < 1e-9 &&
+                    std::abs(a.getAmplitudeScalingFactor(MFLib::RelativeMagnitudeType::SCHAFF_RICHARDS_2014) - 3.0) < 1e-9,
+                "detector: amplitude scaling factors of a copy scaled by 3");
+        require(std::abs(a.getPhaseOnsetTime() - a.getDetectionTime()) < 1e-12, "detector: phase onset time");
+    }
+}
+
 }  // namespace
 
 int main()
@@ -372,6 +444,7 @@ int main()
         test_shift_and_stack();
         test_peak_finder();
         test_dbscan();
+        test_detector();
     }
     catch (const std::exception &e)
     {
