@@ -93,3 +93,26 @@ def test_serving_alone_equals_mix(gpu):
             worst = max(worst, float(np.max(np.abs(a.rho[t].astype(np.float64) - m.rho[t]))))
     print("\nserving: max|drho| alone vs mix %.3g" % worst)
     assert worst <= 1e-6
+
+
+def test_serving_under_tight_budget(gpu):
+    """A device-memory budget that holds only about one object forces the
+    loop to evict idle objects between keys; every result still equals the
+    same request served alone with room to spare."""
+    banks = _banks()
+    reqs = _requests(banks, np.random.default_rng(9))
+    ex = GpuExecutor(threshold=0.5, min_distance=100)
+    big = max(ex.estimate_bytes(b, 15000) for b in banks)
+    tight = Server(banks, ex, memory_budget=1.2 * big, slots=3, buckets=(5000, 10000, 15000)).start()
+    rs = [tight.submit(DetectionRequest(b, x, keep=k)) for b, x, k in reqs]
+    for r in rs:
+        r.wait(120)
+    tight.close()
+    assert tight.evicted > 0
+    assert tight.peak_held <= 1.2 * big + max(ex.estimate_bytes(b, 15000) for b in banks)
+    alone = _serve(banks, reqs, slots=1)
+    for a, m in zip(alone, rs):
+        for pa, pm in zip(a.peaks, m.peaks):
+            np.testing.assert_array_equal(pa, pm)
+        for t in a.rho:
+            np.testing.assert_array_equal(a.rho[t], m.rho[t])
