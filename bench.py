@@ -78,7 +78,7 @@ def make_workload(n_samples=N_SAMPLES, n_stations=N_STATIONS, n_events=N_EVENTS,
     # origin times on a coarse grid: copies never overlap
     slot = 1000
     nslots = (n_samples - 2 * slot) // slot
-    picks = rng.choice(nslots, size=min(n_events * inj, nslots), replace=False)
+    picks = rng.choice(nslots, size=min(n_events * inj, (nslots // n_events) * n_events), replace=False)
     origins = (picks.reshape(n_events, -1) + 1) * slot + rng.integers(0, 100, (n_events, picks.size // n_events))
     for t, tp in enumerate(templates):
         c, e, s = tchan[t], tevent[t], tshift[t]
@@ -161,6 +161,17 @@ class ClockSampler:
                           if r[i].lower() == "active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(sm)}
+
+
+def max_over_ranks(value, dist, device="cpu"):
+    """The largest value over the ranks of the process group (the job's
+    time is its slowest rank's); the value itself without a group."""
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
 
 
 def measured_peak(key="hbm_gbs"):
@@ -694,10 +705,7 @@ def main():
     el = 1e-3 * ev0.elapsed_time(ev1)
     clk = clocks.stop()
     launches = f.launch_count() + db.launch_count() - launches0
-    if dist is not None:
-        t = torch.tensor([el], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        el = float(t.item())
+    el = max_over_ranks(el, dist, "cuda")
     counts, idx, labels, ncl = out
     ms_step = 1e3 * el / args.steps
 
@@ -711,11 +719,7 @@ def main():
         t0 = time.perf_counter()
         r = fn()
         el = time.perf_counter() - t0
-        if dist is not None:
-            t = torch.tensor([el], dtype=torch.float64, device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            el = float(t.item())
-        return el, r
+        return max_over_ranks(el, dist, "cuda"), r
 
     def serial():
         r = None
