@@ -88,10 +88,17 @@ template <int BAR, int NT> __device__ __forceinline__ void team_sync()
     if constexpr (BAR == 0) __syncthreads();
     else asm volatile("bar.sync %0, %1;" ::"n"(BAR), "n"(NT) : "memory");
 }
+// BAR < 0: the barrier id is a run-time value (one code path serves every
+// team of a CTA, so the instruction cache holds one copy)
+template <int BAR, int NT> __device__ __forceinline__ void team_sync(int bar_id)
+{
+    if constexpr (BAR < 0) asm volatile("bar.sync %0, %1;" ::"r"(bar_id), "n"(NT) : "memory");
+    else team_sync<BAR, NT>();
+}
 
 template <class T, int LOG2P, int NT, bool INV, bool ST_BUF, int PASS, class LD, class ST, bool LD_ALIAS = false,
           int BAR = 0>
-__device__ __forceinline__ void fft_pass_io(cx<T> *s, const cx<T> *tws, int tid, LD &ld, ST &st)
+__device__ __forceinline__ void fft_pass_io(cx<T> *s, const cx<T> *tws, int tid, LD &ld, ST &st, int bar_id = 0)
 {
     using PL = FftPlan<LOG2P>;
     constexpr int P = PL::P, NP = PL::npass();
@@ -113,7 +120,7 @@ __device__ __forceinline__ void fft_pass_io(cx<T> *s, const cx<T> *tws, int tid,
             }
         }
     }
-    if constexpr ((!FIRST && (!LAST || ST_BUF)) || (FIRST && LD_ALIAS)) team_sync<BAR, NT>();
+    if constexpr ((!FIRST && (!LAST || ST_BUF)) || (FIRST && LD_ALIAS)) team_sync<BAR, NT>(bar_id);
 #pragma unroll
     for (int b = 0; b < BPT; ++b)
     {
@@ -142,7 +149,7 @@ __device__ __forceinline__ void fft_pass_io(cx<T> *s, const cx<T> *tws, int tid,
             }
         }
     }
-    if constexpr (!LAST) team_sync<BAR, NT>();
+    if constexpr (!LAST) team_sync<BAR, NT>(bar_id);
 }
 
 // Runs every pass.  The first pass reads its inputs through ld(e) (e in
@@ -154,12 +161,12 @@ __device__ __forceinline__ void fft_pass_io(cx<T> *s, const cx<T> *tws, int tid,
 // synchronises before reading s.
 template <class T, int LOG2P, int NT, bool INV, bool ST_BUF, class LD, class ST, bool LD_ALIAS = false, int BAR = 0,
           int PASS = 0>
-__device__ __forceinline__ void fft_run(cx<T> *s, const cx<T> *tws, int tid, LD &ld, ST &st)
+__device__ __forceinline__ void fft_run(cx<T> *s, const cx<T> *tws, int tid, LD &ld, ST &st, int bar_id = 0)
 {
     if constexpr (PASS < FftPlan<LOG2P>::npass())
     {
-        fft_pass_io<T, LOG2P, NT, INV, ST_BUF, PASS, LD, ST, LD_ALIAS, BAR>(s, tws, tid, ld, st);
-        fft_run<T, LOG2P, NT, INV, ST_BUF, LD, ST, LD_ALIAS, BAR, PASS + 1>(s, tws, tid, ld, st);
+        fft_pass_io<T, LOG2P, NT, INV, ST_BUF, PASS, LD, ST, LD_ALIAS, BAR>(s, tws, tid, ld, st, bar_id);
+        fft_run<T, LOG2P, NT, INV, ST_BUF, LD, ST, LD_ALIAS, BAR, PASS + 1>(s, tws, tid, ld, st, bar_id);
     }
 }
 

@@ -811,7 +811,8 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
             }
         }
     };
-    auto template_body = [&](auto bar_tag, auto nt_tag, int j, const cx<T> *B, cx<T> *Wt, unsigned *mk, int ttid) {
+    auto template_body = [&](auto bar_tag, auto nt_tag, int j, const cx<T> *B, cx<T> *Wt, unsigned *mk, int ttid,
+                             int bar_id) {
         constexpr int BAR = decltype(bar_tag)::value;
         constexpr int NTT = decltype(nt_tag)::value;
         const int t = p.tids[t_begin + j];
@@ -838,53 +839,39 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
             else dst[k] = r0;
             if (pk && (r0 > pk_thr || r1 > pk_thr)) atomicOr(mk + (e >> 10), 1u << ((e >> 5) & 31));
         };
-        fft_run<T, LOG2P, NTT, true, false, decltype(pre), decltype(epi), false, BAR>(Wt, tws, ttid, pre, epi);
+        fft_run<T, LOG2P, NTT, true, false, decltype(pre), decltype(epi), false, BAR>(Wt, tws, ttid, pre, epi,
+                                                                                     bar_id);
     };
 
     if constexpr (TEAMS)
     {
         // two teams of 128 threads; each keeps its own work buffer, chunk
         // masks and barrier
-        const int team = tid >> 7, ttid = tid & 127;
+        // one code path for both teams: named barrier 1 + team, chosen at
+        // run time
+        const int team = tid >> 7, ttid = tid & 127, bar_id = 1 + team;
         unsigned *mkt = Mk + team * 2 * MW;
+        cx<T> *Wt = team ? W1 : W0;
         int t_prev = -1, it = 0;
         for (int j = team; j < ntl; j += 2, ++it)
         {
             const cx<T> *B = p.Bc + (long) p.tids[t_begin + j] * p.ldb;
-            if (team == 0)
+            if (it > 0)
             {
-                if (it > 0)
+                team_sync<-1, 128>(bar_id);
+                if (pk)
                 {
-                    team_sync<1, 128>();
-                    if (pk)
-                    {
-                        pk_scan(std::integral_constant<int, 128>(), mkt + ((it - 1) & 1) * MW, t_prev, ttid);
-                        if (ttid < MW) mkt[(it & 1) * MW + ttid] = 0u;
-                    }
+                    pk_scan(std::integral_constant<int, 128>(), mkt + ((it - 1) & 1) * MW, t_prev, ttid);
+                    if (ttid < MW) mkt[(it & 1) * MW + ttid] = 0u;
                 }
-                template_body(std::integral_constant<int, 1>(), std::integral_constant<int, 128>(), j, B, W0,
-                              mkt + (it & 1) * MW, ttid);
             }
-            else
-            {
-                if (it > 0)
-                {
-                    team_sync<2, 128>();
-                    if (pk)
-                    {
-                        pk_scan(std::integral_constant<int, 128>(), mkt + ((it - 1) & 1) * MW, t_prev, ttid);
-                        if (ttid < MW) mkt[(it & 1) * MW + ttid] = 0u;
-                    }
-                }
-                template_body(std::integral_constant<int, 2>(), std::integral_constant<int, 128>(), j, B, W1,
-                              mkt + (it & 1) * MW, ttid);
-            }
+            template_body(std::integral_constant<int, -1>(), std::integral_constant<int, 128>(), j, B, Wt,
+                          mkt + (it & 1) * MW, ttid, bar_id);
             t_prev = p.tids[t_begin + j];
         }
         if (pk && it > 0)
         {
-            if (team == 0) team_sync<1, 128>();
-            else team_sync<2, 128>();
+            team_sync<-1, 128>(bar_id);
             pk_scan(std::integral_constant<int, 128>(), mkt + ((it - 1) & 1) * MW, t_prev, ttid);
         }
     }
@@ -936,7 +923,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
                 }
             }
             template_body(std::integral_constant<int, 0>(), std::integral_constant<int, kThreads>(), j, B, W,
-                          Mk + (j & 1) * MW, tid);
+                          Mk + (j & 1) * MW, tid, 0);
         }
         if (pk)
         {
