@@ -536,6 +536,16 @@ def run_uneven(args):
                  correlator_variant=args.correlator_variant, length_buckets=args.length_buckets)
     f.set_channel_signals(sig)
     f.set_peak_threshold(0.7)
+    tune = None
+    if args.autotune:
+        # measured per-bucket plan choice (1-3 buckets, FFT length and
+        # organisation per bucket) before anything is timed
+        t0 = time.perf_counter()
+        res = f.autotune(sig, repeats=1, max_buckets=3)
+        ok = [t for t in res["trials"] if t["apply_ms"] is not None]
+        tune = {"seconds": time.perf_counter() - t0, "trials": len(ok),
+                "model_apply_ms": ok[0]["apply_ms"], "tuned_apply_ms": res["apply_ms"],
+                "chosen": res["plan"]["bucket_plans"]}
     f.set_graph(True)  # the day-long apply replayed as a CUDA graph after its first run
     lags = float(sum(n - int(L) + 1 for L in lens))
 
@@ -578,6 +588,8 @@ def run_uneven(args):
                          "peak_source": kind},
             "gpu_launches": int(f.launch_count() - launches0), "detections": int(idx.size),
             "graph_replays": f.graph_launches()}
+    if tune is not None:
+        line["config"]["autotune"] = tune
     print(json.dumps(line), flush=True)
 
 
@@ -596,6 +608,8 @@ def main():
     ap.add_argument("--events", type=int, default=N_EVENTS,
                     help="events, i.e. templates per channel (default %d)" % N_EVENTS)
     ap.add_argument("--serving", action="store_true", help="run the request loop instead of the day-long step")
+    ap.add_argument("--autotune", action="store_true",
+                    help="with --uneven: measured per-bucket plan choice before timing")
     ap.add_argument("--uneven", action="store_true",
                     help="the 2,000-template uneven bank on 96 channels instead of the 24-channel day")
     ap.add_argument("--detector", action="store_true", help="time the single-channel detector")

@@ -98,6 +98,20 @@ typedef struct
        1 = one plan for every template; k > 1: at most k, split wherever the
        plans get cheaper). */
     int length_buckets;
+    /* Extension: per-bucket plan overrides, e.g. from a measured autotune.
+       Entry b applies to length bucket b (shortest templates first, as
+       mfgpu_mf_get_buckets reports them); entries past the bucket count are
+       ignored.  bucket_fft_lengths[b]: the bucket's FFT length (0 =
+       automatic); bucket_variants[b]: its correlator organisation numbered
+       like correlator_variant (0 = automatic; 1 or 2 when the templates have
+       several lengths, 1, 2, 3 or 5 for one length).  Either array may be
+       NULL when n_bucket_plans is 0.  An override whose plan does not fit
+       (block too short, shared memory, unsupported length) fails with
+       MFGPU_EINVAL.  Any non-zero entry turns off the automatic choice of
+       the tensor-core correlator. */
+    int n_bucket_plans;
+    const int *bucket_fft_lengths;
+    const int *bucket_variants;
 } mfgpu_mf_params;
 
 /* MatchedFilter<T>::MatchedFilter(); precision MFGPU_FLOAT32 | MFGPU_FLOAT64 */
@@ -180,6 +194,10 @@ mfgpu_status mfgpu_mf_get_correlator(const mfgpu_mf *mf, int *variant, int *tc_g
  * max, shortest templates first, the primary plan last) the FFT length and
  * the number of templates.  Extension: the reference has one FFT length. */
 mfgpu_status mfgpu_mf_get_buckets(const mfgpu_mf *mf, int max, int *fft_lengths, int *n_templates, int *count);
+/* Per length bucket (same order, up to max): lags per block and the FFT
+ * organisation numbered like correlator_variant (4 for the tensor-core
+ * correlator, which has one bucket).  Extension. */
+mfgpu_status mfgpu_mf_get_bucket_plans(const mfgpu_mf *mf, int max, int *lags_per_block, int *variants, int *count);
 /* Request-window upload for a serving loop.  Extension: the reference sets
  * whole-length signals one template at a time (setSignal,
  * src/matchedFilter.cpp:863-921) and has no serving loop.  x holds n_src

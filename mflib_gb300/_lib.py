@@ -70,6 +70,9 @@ class MfgpuParams(C.Structure):
         ("fft_length", C.c_int),
         ("correlator_variant", C.c_int),
         ("length_buckets", C.c_int),
+        ("n_bucket_plans", C.c_int),
+        ("bucket_fft_lengths", C.POINTER(C.c_int)),
+        ("bucket_variants", C.POINTER(C.c_int)),
     ]
 
 
@@ -105,6 +108,7 @@ _SIGS = {
     "mfgpu_mf_get_plan": ([_vp, _ip, _ip, _ip], C.c_int),
     "mfgpu_mf_get_correlator": ([_vp, _ip, _ip, _ip], C.c_int),
     "mfgpu_mf_get_buckets": ([_vp, C.c_int, _ip, _ip, _ip], C.c_int),
+    "mfgpu_mf_get_bucket_plans": ([_vp, C.c_int, _ip, _ip, _ip], C.c_int),
     "mfgpu_mf_detect": ([_vp, C.POINTER(MfgpuDetectParams), _ip], C.c_int),
     "mfgpu_mf_set_graph": ([_vp, C.c_int], C.c_int),
     "mfgpu_mf_get_graph_launches": ([_vp, C.POINTER(C.c_longlong)], C.c_int),

@@ -488,7 +488,30 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
     mf->tc = p->correlator_variant == 4;
     if (mf->tc && (mf->prec != 4 || !all_equal))
         return fail(MFGPU_EINVAL, "correlator_variant 4 (tensor cores) needs FP32 data and templates of one length");
-    const bool tc_candidate = mf->tc || (p->correlator_variant == 0 && mf->prec == 4 && all_equal && p->fft_length == 0);
+    // per-bucket overrides: FFT length and organisation (mode) of bucket b
+    if (p->n_bucket_plans < 0) return fail(MFGPU_EINVAL, "n_bucket_plans must be >= 0");
+    bool bucket_forced = false;
+    for (int b = 0; b < p->n_bucket_plans; ++b)
+    {
+        const int F = p->bucket_fft_lengths ? p->bucket_fft_lengths[b] : 0;
+        const int bv = p->bucket_variants ? p->bucket_variants[b] : 0;
+        if (F < 0 || (F > 0 && (F & (F - 1)) != 0))
+            return fail(MFGPU_EINVAL, "bucket_fft_lengths[" + std::to_string(b) + "] = " + std::to_string(F) +
+                                          " is not 0 or a power of two");
+        if (!(bv == 0 || bv == 1 || bv == 2 || ((bv == 3 || bv == 5) && all_equal)))
+            return fail(MFGPU_EINVAL, "bucket_variants[" + std::to_string(b) + "] = " + std::to_string(bv) +
+                                          (all_equal ? " must be 0, 1, 2, 3 or 5" : " must be 0, 1 or 2 (several template lengths)"));
+        bucket_forced = bucket_forced || F > 0 || bv > 0;
+    }
+    auto bucket_nfft = [&](int b) {
+        return b < p->n_bucket_plans && p->bucket_fft_lengths ? p->bucket_fft_lengths[b] : 0;
+    };
+    auto bucket_mode = [&](int b) {
+        const int bv = b < p->n_bucket_plans && p->bucket_variants ? p->bucket_variants[b] : 0;
+        return bv == 0 ? -1 : bv == 5 ? 3 : bv - 1;
+    };
+    const bool tc_candidate =
+        mf->tc || (p->correlator_variant == 0 && mf->prec == 4 && all_equal && p->fft_length == 0 && !bucket_forced);
     int dev_smem = 0, sm_smem = 0;
     CU(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, mf->dev));
     CU(cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, mf->dev));
@@ -507,12 +530,14 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
         int l2p = -1, S = 0, mode = 0;
         double cost = 0;
     };
-    auto plan_for = [&](int Lb, int mv, bool eq) {
+    // f_nfft / f_mode: a bucket's plan override (0 / -1: automatic)
+    auto plan_for = [&](int Lb, int mv, bool eq, int f_nfft = 0, int f_mode = -1) {
         PlanPick best;
         for (int l2p = lo; l2p <= hi; ++l2p)
         {
             int N = 2 << l2p;
             if (p->fft_length > 0 && p->fft_length != N) continue;
+            if (f_nfft > 0 && f_nfft != N) continue;
             int S = ((N - Lb + 1) / 32) * 32;
             if (S < 32) continue;
             // organisation: forced, else two teams for a shared length when
@@ -520,7 +545,8 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
             // loop at N = 4096 and 5% at N = 2048, 2% slower at N = 8192),
             // else spectrum prefetch when it keeps the occupancy
             int mode;
-            if (forced_mode >= 0) mode = forced_mode;
+            if (f_mode >= 0) mode = f_mode;
+            else if (forced_mode >= 0) mode = forced_mode;
             else
             {
                 size_t b0 = smem_of(l2p, 0, S), b1 = smem_of(l2p, 1, S);
@@ -623,7 +649,10 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
     for (int b = 0; b < nbk; ++b)
         for (int i = cuts[b]; i < cuts[b + 1]; ++i) bucket_of[order[i]] = b;
     const int mv0 = n - mf->lens[order[cuts[nbk - 1]]] + 1;
-    const PlanPick best = plan_for(maxLen, nbk > 1 ? mv0 : maxvalid, all_equal);
+    const PlanPick best =
+        plan_for(maxLen, nbk > 1 ? mv0 : maxvalid, all_equal, bucket_nfft(nbk - 1), bucket_mode(nbk - 1));
+    if (best.l2p < 0 && (bucket_nfft(nbk - 1) > 0 || bucket_mode(nbk - 1) >= 0))
+        return fail(MFGPU_EINVAL, "the plan override of bucket " + std::to_string(nbk - 1) + " does not fit");
     const int best_l2p = best.l2p, best_S = best.S, best_mode = best.mode;
     const double best_cost = best.cost;
     mf->mode_x = best_mode;
@@ -646,7 +675,8 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
     for (int b = 0; b + 1 < nbk; ++b)
     {
         const int Lb = mf->lens[order[cuts[b + 1] - 1]], mv = n - mf->lens[order[cuts[b]]] + 1;
-        const PlanPick pk = plan_for(Lb, mv, false);
+        const PlanPick pk = plan_for(Lb, mv, false, bucket_nfft(b), bucket_mode(b));
+        if (pk.l2p < 0) return fail(MFGPU_EINVAL, "the plan override of bucket " + std::to_string(b) + " does not fit");
         auto xb = std::make_unique<MfBucket>();
         xb->log2p = pk.l2p;
         xb->nfft = 2 << pk.l2p;
@@ -939,6 +969,21 @@ mfgpu_status mfgpu_mf_get_buckets(const mfgpu_mf *mf, int max, int *fft_lengths,
         const bool prim = b == nb - 1;
         if (fft_lengths) fft_lengths[b] = prim ? mf->nfft : mf->xb[b]->nfft;
         if (n_templates) n_templates[b] = prim ? (mf->xb.empty() ? mf->nt : mf->ntemplates0) : mf->xb[b]->ntemplates;
+    }
+    return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_get_bucket_plans(const mfgpu_mf *mf, int max, int *lags_per_block, int *variants, int *count)
+{
+    MF_CHECK_INIT(mf);
+    const int nb = (int) mf->xb.size() + 1;
+    if (count) *count = nb;
+    auto variant_of = [](int mode) { return mode == 3 ? 5 : mode + 1; };
+    for (int b = 0; b < nb && b < max; ++b)
+    {
+        const bool prim = b == nb - 1;
+        if (lags_per_block) lags_per_block[b] = prim ? mf->S : mf->xb[b]->S;
+        if (variants) variants[b] = prim ? (mf->tc ? 4 : variant_of(mf->mode_x)) : variant_of(mf->xb[b]->mode);
     }
     return MFGPU_OK;
 }

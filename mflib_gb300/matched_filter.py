@@ -166,7 +166,7 @@ class MatchedFilter:
         return self._dtype
 
     def initialize(self, params, template_channels=None, n_channels=None, fft_length=0, correlator_variant=0,
-                   length_buckets=0):
+                   length_buckets=0, bucket_plans=None):
         """MatchedFilter<T>::initialize (src/matchedFilter.cpp:507-821).
 
         Extensions: ``template_channels`` (one channel index per template,
@@ -178,7 +178,10 @@ class MatchedFilter:
         correlation, FP32 and templates of one length; 5 two teams with the
         normalisation computed inside each CTA, templates of one length);
         ``length_buckets`` caps the length buckets of a mixed-length bank
-        (0 automatic, 1 one plan for every template)."""
+        (0 automatic, 1 one plan for every template); ``bucket_plans``
+        overrides the plan of each length bucket (shortest templates first):
+        a list of (fft_length, correlator_variant) pairs, 0 keeping the
+        automatic choice (see ``autotune``)."""
         if not isinstance(params, MatchedFilterParameters) or not params.is_valid():
             raise ValueError("Parameters are invalid")
         tmpls = [params.get_template(i) for i in range(params.get_number_of_templates())]
@@ -211,7 +214,17 @@ class MatchedFilter:
         p.fft_length = int(fft_length)
         p.correlator_variant = int(correlator_variant)
         p.length_buckets = int(length_buckets)
+        if bucket_plans:
+            nbp = len(bucket_plans)
+            bfl = (C.c_int * nbp)(*[int(fv[0]) for fv in bucket_plans])
+            bva = (C.c_int * nbp)(*[int(fv[1]) for fv in bucket_plans])
+            p.n_bucket_plans = nbp
+            p.bucket_fft_lengths = bfl
+            p.bucket_variants = bva
         _lib.call("mfgpu_mf_initialize", self._h, C.byref(p))
+        self._init_kw = dict(template_channels=template_channels, n_channels=n_channels, fft_length=fft_length,
+                             correlator_variant=correlator_variant, length_buckets=length_buckets,
+                             bucket_plans=list(bucket_plans) if bucket_plans else None)
         self._params = params
         self._nt = nt
         self._templates = tmpls
@@ -387,9 +400,116 @@ class MatchedFilter:
         cnt = C.c_int()
         fl, ntb = (C.c_int * 8)(), (C.c_int * 8)()
         _lib.call("mfgpu_mf_get_buckets", self._h, 8, fl, ntb, C.byref(cnt))
+        lpb, bv = (C.c_int * 8)(), (C.c_int * 8)()
+        _lib.call("mfgpu_mf_get_bucket_plans", self._h, 8, lpb, bv, C.byref(cnt))
+        nb = min(8, cnt.value)
         return {"fft_length": a.value, "lags_per_block": b.value, "n_blocks": c.value, "correlator": v.value,
                 "tc_group": g.value, "tc_k": k.value,
-                "buckets": [(fl[i], ntb[i]) for i in range(min(8, cnt.value))]}
+                "buckets": [(fl[i], ntb[i]) for i in range(nb)],
+                "bucket_plans": [{"fft_length": fl[i], "templates": ntb[i], "lags_per_block": lpb[i],
+                                  "correlator": bv[i]} for i in range(nb)]}
+
+    def autotune(self, x, repeats=3, max_buckets=3, fft_lengths=None, variants=None):
+        """Extension: measured plan choice on this object's templates and the
+        signals ``x`` (a 2-D array: channel rows when the object was
+        initialised with shared channels, else one row per signal slot).
+
+        The planner's choice comes from a cost model calibrated on GB300;
+        this times the real thing instead.  For 1 .. ``max_buckets`` length
+        buckets (a mixed-length bank; one bucket for one length) it re-plans
+        every bucket in turn (coordinate descent, shortest bucket first) over
+        the FFT lengths half, equal to and twice the current one and every
+        organisation allowed for the bucket, timing ``repeats`` applies of
+        each candidate after one untimed apply; for one template length in
+        FP32 it also times the tensor-core correlator.  The object is left
+        initialised with the fastest configuration (its signals loaded) and
+        the method returns it with its apply time and every trial.
+        ``fft_lengths`` / ``variants`` restrict the candidates.  User-forced
+        fft_length and correlator_variant are replaced by the tuned plans."""
+        if self._params is None:
+            raise RuntimeError("Class not initialized")
+        x = np.asarray(x)
+        if x.ndim != 2:
+            raise ValueError("x must be 2-D")
+        base = dict(self._init_kw)
+        params = self._params
+        peak_thr = getattr(self, "_peak_thr", None)
+        lens = [t.get_signal_length() for t in self._templates]
+        one_length = min(lens) == max(lens)
+
+        def load():
+            if base["template_channels"] is not None:
+                self.set_channel_signals(x)
+            else:
+                for i in range(x.shape[0]):
+                    MatchedFilter.set_signal(self, i, x[i])  # slot i (SingleChannel: slot 0 only)
+            if peak_thr is not None:
+                self.set_peak_threshold(peak_thr)
+
+        trials = []
+
+        def run(kw):
+            try:
+                self.initialize(params, **kw)
+            except (ValueError, RuntimeError) as e:
+                trials.append({"config": kw, "apply_ms": None, "error": str(e)})
+                return None
+            load()
+            self.apply()
+            self.synchronize()
+            ts = []
+            for _ in range(max(1, int(repeats))):
+                self.apply()
+                self.synchronize()
+                ts.append(self.last_timings()["apply_ms"])
+            ms = float(np.median(ts))
+            trials.append({"config": kw, "apply_ms": ms, "plan": self.get_plan()})
+            return ms
+
+        def common(**over):
+            kw = dict(base, fft_length=0, correlator_variant=0)
+            kw.update(over)
+            return kw
+
+        best_ms, best_kw = None, None
+        allowed_v = [1, 2, 3, 5] if one_length else [1, 2]
+        if variants is not None:
+            allowed_v = [v for v in allowed_v if v in variants]
+        for nb in range(1, (1 if one_length else max(1, int(max_buckets))) + 1):
+            kw = common(length_buckets=nb, bucket_plans=None)
+            ms = run(kw)
+            if ms is None:
+                continue
+            plans = [(bp["fft_length"], bp["correlator"]) for bp in self.get_plan()["bucket_plans"]]
+            if any(v == 4 for _, v in plans):
+                plans = [(0, 0)] * len(plans)  # the automatic choice took the tensor cores: tune the FFT plans
+            cur_ms, cur = ms, plans
+            for b in range(len(plans)):
+                f0 = plans[b][0] if plans[b][0] > 0 else self.get_plan()["fft_length"]
+                fmax = 8192 if self._dtype == np.float32 else 4096  # longest transforms built
+                cands_f = [f for f in (f0 // 2, f0, 2 * f0) if 64 <= f <= fmax]
+                if fft_lengths is not None:
+                    cands_f = [f for f in cands_f if f in fft_lengths]
+                for f in cands_f:
+                    for v in allowed_v:
+                        if (f, v) == cur[b]:
+                            continue
+                        trial = list(cur)
+                        trial[b] = (f, v)
+                        ms = run(common(length_buckets=nb, bucket_plans=trial))
+                        if ms is not None and ms < cur_ms:
+                            cur_ms, cur = ms, trial
+            if best_ms is None or cur_ms < best_ms:
+                best_ms, best_kw = cur_ms, common(length_buckets=nb, bucket_plans=cur)
+        if one_length and self._dtype == np.float32 and (variants is None or 4 in variants):
+            ms = run(common(correlator_variant=4, length_buckets=1, bucket_plans=None))
+            if ms is not None and (best_ms is None or ms < best_ms):
+                best_ms, best_kw = ms, common(correlator_variant=4, length_buckets=1, bucket_plans=None)
+        if best_kw is None:
+            raise RuntimeError("no candidate plan could be initialised")
+        self.initialize(params, **best_kw)
+        load()
+        return {"config": best_kw, "apply_ms": best_ms, "plan": self.get_plan(), "trials": trials}
 
     def last_timings(self):
         a, b = C.c_float(), C.c_float()
@@ -417,6 +537,7 @@ class MatchedFilter:
         ``threshold`` inside the correlator (None or a negative value: off);
         find_peaks with that threshold then skips its scan of the traces."""
         _lib.call("mfgpu_mf_set_peak_threshold", self._h, -1.0 if threshold is None else float(threshold))
+        self._peak_thr = None if threshold is None or threshold < 0 else float(threshold)
 
     def get_peak_threshold(self):
         """(requested gathering threshold or None, whether the last apply gathered)."""
