@@ -2025,7 +2025,12 @@ mfgpu_status mfgpu_dbscan_create(mfgpu_dbscan **out)
     if (!out) return fail(MFGPU_EINVAL, "db is NULL");
     auto *db = new mfgpu_dbscan();
     cudaError_t e = cudaGetDevice(&db->dev);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&db->stream, cudaStreamNonBlocking);
+    // the highest stream priority: clustering is small latency-bound work
+    // that typically runs beside a matched filter's long correlator launch,
+    // whose waiting CTAs should not hold it back
+    int least = 0, greatest = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&db->stream, cudaStreamNonBlocking, greatest);
     if (e != cudaSuccess)
     {
         delete db;
