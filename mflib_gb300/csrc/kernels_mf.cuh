@@ -519,20 +519,35 @@ __device__ __forceinline__ void seg_inv_den(SegStats<T> st, int L, int S, T tol,
                 d1 += dd;
             }
         }
+        // the row's 16-byte chunks are stored XOR-swizzled by the run index
+        // (chunk c at c ^ (v & 7)): the eight threads of a wavefront then
+        // hit eight different bank groups instead of one; inv_den_pair()
+        // undoes it
         T *dst = invd + base;
+        const int sw = v & 7;
         if constexpr (sizeof(T) == 4)
         {
 #pragma unroll
             for (int q = 0; q < 32; q += 4)
-                *reinterpret_cast<float4 *>(dst + q) = make_float4(o[q], o[q + 1], o[q + 2], o[q + 3]);
+                *reinterpret_cast<float4 *>(dst + (((q >> 2) ^ sw) << 2)) =
+                    make_float4(o[q], o[q + 1], o[q + 2], o[q + 3]);
         }
         else
         {
 #pragma unroll
-            for (int q = 0; q < 32; q += 2) *reinterpret_cast<double2 *>(dst + q) = make_double2(o[q], o[q + 1]);
+            for (int q = 0; q < 32; q += 2)
+                *reinterpret_cast<double2 *>(dst + (((q >> 1) ^ sw) << 1)) = make_double2(o[q], o[q + 1]);
         }
     }
     __syncthreads();
+}
+
+// Index of the pair (lags 2e, 2e + 1) in a normalisation row written by
+// seg_inv_den (rows of 32 lags, 16-byte chunks swizzled by the row index)
+template <class T> __device__ __forceinline__ int inv_den_pair(int e)
+{
+    if constexpr (sizeof(T) == 4) return e ^ ((e >> 3) & 14);  // 2 pairs per chunk, 8 chunks per row
+    else return e ^ ((e >> 4) & 7);                             // 1 pair per chunk, 16 chunks per row
 }
 
 template <class T> __device__ __forceinline__ void store2(T *dst, T a, T b);
@@ -832,7 +847,8 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
         auto epi = [&](int e, cx<T> z) {
             const int k = 2 * e;
             if (k >= kmax) return;
-            const cx<T> d = invd2[e];
+            // rows from den_kernel (TMA) are plain, rows from seg_inv_den swizzled
+            const cx<T> d = invd2[SHARED_DEN ? e : inv_den_pair<T>(e)];
             const T r0 = clamp_rho(z.x * d.x);
             const T r1 = clamp_rho(z.y * d.y);
             if (k + 1 < kmax) store2<T>(dst + k, r0, r1);
