@@ -1128,42 +1128,72 @@ __global__ void __launch_bounds__(kThreads) den_kernel(const T *x, long ldx, int
     const T Lt = (T) L;
     const int nlr = lpc / kDenRun;
     T *drow = den + (long) c * ldd + k0;
-    for (int v = tid; v < nlr; v += kThreads)
+    // Each thread's 32 results go to shared memory first (rows of 32 lags
+    // over the samples' buffer, 16-byte chunks swizzled by the row index so
+    // the stores are conflict-free), then the CTA's row is written to global
+    // memory in coalesced 16-byte stores.  Round r's rows lie below every
+    // sample that a later round reads, so one barrier per round suffices.
+    constexpr int CPR = kDenRun / VW;  // 16-byte chunks per row of 32 lags
+    T *ob = y;
+    const int rounds = (nlr + kThreads - 1) / kThreads;
+    for (int r = 0; r < rounds; ++r)
     {
-        // window [32v, 32v + L): prefixes at runs v and v + Lq, plus the
-        // first re samples of run v + Lq
-        const acc w1 = O::add(O::add(P1[v + Lq], Q1[v + Lq]), O::neg(P1[v]));
-        const acc w2 = O::add(O::add(P2[v + Lq], Q2[v + Lq]), O::neg(P2[v]));
-        T vh, vl;
-        O::var0(w1, w2, L, vh, vl);
-        const T c2s = (T) 2 * O::hi(w1);
-        T d1 = 0, d2 = 0;
+        const int v = tid + kThreads * r;
+        const bool act = v < nlr;
         T o[kDenRun];
-        const int base = 32 * v;
-#pragma unroll
-        for (int q = 0; q < kDenRun; ++q)
+        if (act)
         {
-            const T var = vh + (vl + fma(Lt, d2, -d1 * (d1 + c2s)));
-            o[q] = O::out(var, sqrtL, tol);
-            // the CTA mean comes off each sample first: both differences are
-            // exact for samples near a large common offset
-            const T yin = y[den_pad(base + q + L)] - m, yout = y[den_pad(base + q)] - m;
-            const T dd = yin - yout;
-            d2 = fma(yin + yout, dd, d2);
-            d1 += dd;
+            // window [32v, 32v + L): prefixes at runs v and v + Lq, plus the
+            // first re samples of run v + Lq
+            const acc w1 = O::add(O::add(P1[v + Lq], Q1[v + Lq]), O::neg(P1[v]));
+            const acc w2 = O::add(O::add(P2[v + Lq], Q2[v + Lq]), O::neg(P2[v]));
+            T vh, vl;
+            O::var0(w1, w2, L, vh, vl);
+            const T c2s = (T) 2 * O::hi(w1);
+            T d1 = 0, d2 = 0;
+            const int base = 32 * v;
+#pragma unroll
+            for (int q = 0; q < kDenRun; ++q)
+            {
+                const T var = vh + (vl + fma(Lt, d2, -d1 * (d1 + c2s)));
+                o[q] = O::out(var, sqrtL, tol);
+                // the CTA mean comes off each sample first: both differences
+                // are exact for samples near a large common offset
+                const T yin = y[den_pad(base + q + L)] - m, yout = y[den_pad(base + q)] - m;
+                const T dd = yin - yout;
+                d2 = fma(yin + yout, dd, d2);
+                d1 += dd;
+            }
         }
-        T *dr = drow + base;
+        __syncthreads();  // this round's samples read
+        if (act)
+        {
+            T *row = ob + 32 * v;
+            const int sw = v & 7;
+            if constexpr (sizeof(T) == 4)
+            {
+#pragma unroll
+                for (int q = 0; q < kDenRun; q += 4)
+                    *reinterpret_cast<float4 *>(row + (((q >> 2) ^ sw) << 2)) =
+                        make_float4(o[q], o[q + 1], o[q + 2], o[q + 3]);
+            }
+            else
+            {
+#pragma unroll
+                for (int q = 0; q < kDenRun; q += 2)
+                    *reinterpret_cast<double2 *>(row + (((q >> 1) ^ sw) << 1)) = make_double2(o[q], o[q + 1]);
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < nlr * CPR; i += kThreads)
+    {
+        const int v = i / CPR, ch = i % CPR;
+        const T *src = ob + 32 * v + ((ch ^ (v & 7)) * VW);
         if constexpr (sizeof(T) == 4)
-        {
-#pragma unroll
-            for (int q = 0; q < kDenRun; q += 4)
-                *reinterpret_cast<float4 *>(dr + q) = make_float4(o[q], o[q + 1], o[q + 2], o[q + 3]);
-        }
+            reinterpret_cast<float4 *>(drow)[i] = *reinterpret_cast<const float4 *>(src);
         else
-        {
-#pragma unroll
-            for (int q = 0; q < kDenRun; q += 2) *reinterpret_cast<double2 *>(dr + q) = make_double2(o[q], o[q + 1]);
-        }
+            reinterpret_cast<double2 *>(drow)[i] = *reinterpret_cast<const double2 *>(src);
     }
 }
 
