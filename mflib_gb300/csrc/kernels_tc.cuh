@@ -394,8 +394,12 @@ static __global__ void __launch_bounds__(kTcThreads, 1) tc_xcorr_kernel(TcParams
                     float *dst = p.rho + (long) tt * p.ldr + lag0;
                     if (lag0 + 7 < p.nv)
                     {
-                        *reinterpret_cast<float4 *>(dst) = make_float4(o[0], o[1], o[2], o[3]);
-                        *reinterpret_cast<float4 *>(dst + 4) = make_float4(o[4], o[5], o[6], o[7]);
+                        // the row's 8 lags in one 32-byte store (rows of rho
+                        // are 256-byte aligned, lag0 a multiple of 8): whole
+                        // sectors per store instead of two half-sector halves
+                        asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(dst), "f"(o[0]),
+                                     "f"(o[1]), "f"(o[2]), "f"(o[3]), "f"(o[4]), "f"(o[5]), "f"(o[6]), "f"(o[7])
+                                     : "memory");
                     }
                     else
                     {
