@@ -425,7 +425,10 @@ class MatchedFilter:
         initialised with the fastest configuration (its signals loaded) and
         the method returns it with its apply time and every trial.
         ``fft_lengths`` / ``variants`` restrict the candidates.  User-forced
-        fft_length and correlator_variant are replaced by the tuned plans."""
+        fft_length and correlator_variant are replaced by the tuned plans.
+        Candidates that do not fit (invalid argument, no device memory) are
+        recorded with their error and skipped; any other failure puts the
+        object back on the configuration it had, then propagates."""
         if self._params is None:
             raise RuntimeError("Class not initialized")
         x = np.asarray(x)
@@ -451,7 +454,7 @@ class MatchedFilter:
         def run(kw):
             try:
                 self.initialize(params, **kw)
-            except (ValueError, RuntimeError) as e:
+            except (ValueError, RuntimeError, MemoryError) as e:  # infeasible, or no room for this plan
                 trials.append({"config": kw, "apply_ms": None, "error": str(e)})
                 return None
             load()
@@ -471,44 +474,53 @@ class MatchedFilter:
             kw.update(over)
             return kw
 
-        best_ms, best_kw = None, None
-        allowed_v = [1, 2, 3, 5] if one_length else [1, 2]
-        if variants is not None:
-            allowed_v = [v for v in allowed_v if v in variants]
-        for nb in range(1, (1 if one_length else max(1, int(max_buckets))) + 1):
-            kw = common(length_buckets=nb, bucket_plans=None)
-            ms = run(kw)
-            if ms is None:
-                continue
-            plans = [(bp["fft_length"], bp["correlator"]) for bp in self.get_plan()["bucket_plans"]]
-            if any(v == 4 for _, v in plans):
-                plans = [(0, 0)] * len(plans)  # the automatic choice took the tensor cores: tune the FFT plans
-            cur_ms, cur = ms, plans
-            for b in range(len(plans)):
-                f0 = plans[b][0] if plans[b][0] > 0 else self.get_plan()["fft_length"]
-                fmax = 8192 if self._dtype == np.float32 else 4096  # longest transforms built
-                cands_f = [f for f in (f0 // 2, f0, 2 * f0) if 64 <= f <= fmax]
-                if fft_lengths is not None:
-                    cands_f = [f for f in cands_f if f in fft_lengths]
-                for f in cands_f:
-                    for v in allowed_v:
-                        if (f, v) == cur[b]:
-                            continue
-                        trial = list(cur)
-                        trial[b] = (f, v)
-                        ms = run(common(length_buckets=nb, bucket_plans=trial))
-                        if ms is not None and ms < cur_ms:
-                            cur_ms, cur = ms, trial
-            if best_ms is None or cur_ms < best_ms:
-                best_ms, best_kw = cur_ms, common(length_buckets=nb, bucket_plans=cur)
-        if one_length and self._dtype == np.float32 and (variants is None or 4 in variants):
-            ms = run(common(correlator_variant=4, length_buckets=1, bucket_plans=None))
-            if ms is not None and (best_ms is None or ms < best_ms):
-                best_ms, best_kw = ms, common(correlator_variant=4, length_buckets=1, bucket_plans=None)
-        if best_kw is None:
-            raise RuntimeError("no candidate plan could be initialised")
-        self.initialize(params, **best_kw)
-        load()
+        try:
+            best_ms, best_kw = None, None
+            allowed_v = [1, 2, 3, 5] if one_length else [1, 2]
+            if variants is not None:
+                allowed_v = [v for v in allowed_v if v in variants]
+            for nb in range(1, (1 if one_length else max(1, int(max_buckets))) + 1):
+                kw = common(length_buckets=nb, bucket_plans=None)
+                ms = run(kw)
+                if ms is None:
+                    continue
+                plans = [(bp["fft_length"], bp["correlator"]) for bp in self.get_plan()["bucket_plans"]]
+                if any(v == 4 for _, v in plans):
+                    plans = [(0, 0)] * len(plans)  # the automatic choice took the tensor cores: tune the FFT plans
+                cur_ms, cur = ms, plans
+                for b in range(len(plans)):
+                    f0 = plans[b][0] if plans[b][0] > 0 else self.get_plan()["fft_length"]
+                    fmax = 8192 if self._dtype == np.float32 else 4096  # longest transforms built
+                    cands_f = [f for f in (f0 // 2, f0, 2 * f0) if 64 <= f <= fmax]
+                    if fft_lengths is not None:
+                        cands_f = [f for f in cands_f if f in fft_lengths]
+                    for f in cands_f:
+                        for v in allowed_v:
+                            if (f, v) == cur[b]:
+                                continue
+                            trial = list(cur)
+                            trial[b] = (f, v)
+                            ms = run(common(length_buckets=nb, bucket_plans=trial))
+                            if ms is not None and ms < cur_ms:
+                                cur_ms, cur = ms, trial
+                if best_ms is None or cur_ms < best_ms:
+                    best_ms, best_kw = cur_ms, common(length_buckets=nb, bucket_plans=cur)
+            if one_length and self._dtype == np.float32 and (variants is None or 4 in variants):
+                ms = run(common(correlator_variant=4, length_buckets=1, bucket_plans=None))
+                if ms is not None and (best_ms is None or ms < best_ms):
+                    best_ms, best_kw = ms, common(correlator_variant=4, length_buckets=1, bucket_plans=None)
+            if best_kw is None:
+                raise RuntimeError("no candidate plan could be initialised")
+            self.initialize(params, **best_kw)
+            load()
+        except BaseException:
+            # leave the object as it was found (best effort), then re-raise
+            try:
+                self.initialize(params, **base)
+                load()
+            except Exception:
+                pass
+            raise
         return {"config": best_kw, "apply_ms": best_ms, "plan": self.get_plan(), "trials": trials}
 
     def last_timings(self):

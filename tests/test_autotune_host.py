@@ -30,6 +30,9 @@ class FakeFilter(MatchedFilter):
         self._init_kw = dict(template_channels=[0] * len(lens), n_channels=1, fft_length=0, correlator_variant=0,
                              length_buckets=0, bucket_plans=None)
         self.cost = cost
+        self.oom = None        # a plan whose initialize runs out of memory
+        self.fail_at = None    # the initialize call that fails hard
+        self.calls = 0
         self.loads = 0
         self.thresholds = []
         self.inits = []
@@ -44,6 +47,11 @@ class FakeFilter(MatchedFilter):
             plans = [(4096, 4)]
         if any(p == (2048, 2) for p in plans):
             raise ValueError("the plan override does not fit")
+        if any(p == self.oom for p in plans):
+            raise MemoryError("out of device memory")
+        self.calls += 1
+        if self.fail_at is not None and self.calls == self.fail_at:
+            raise OSError("device lost")
         self.inits.append(kw)
         self.kw = kw
         self.plans = plans
@@ -129,3 +137,21 @@ def test_autotune_restrictions_and_errors():
     f._params = None
     with pytest.raises(RuntimeError):
         f.autotune(np.zeros((1, 10), np.float32))
+
+
+def test_autotune_skips_out_of_memory_and_restores_on_failure():
+    cost = lambda k, b, fl, v: 2.0 if (fl, v) == (8192, 1) else 3.0
+    f = FakeFilter([200, 900], cost=cost)
+    f.oom = (8192, 1)
+    res = f.autotune(np.zeros((1, 10), np.float32), repeats=1, max_buckets=1)
+    assert any("out of device memory" in t.get("error", "") for t in res["trials"])
+    assert res["apply_ms"] == 3.0
+    # a hard failure mid-search: the object goes back to the plan it had
+    g = FakeFilter([200, 900], cost=cost)
+    g.initialize(None, **dict(g._init_kw, length_buckets=2))
+    start = dict(g._init_kw)
+    g.fail_at = 4
+    with pytest.raises(OSError):
+        g.autotune(np.zeros((1, 10), np.float32), repeats=1, max_buckets=2)
+    assert g.kw == start and g.plans == [(4096, 1), (4096, 1)]
+
