@@ -222,6 +222,7 @@ class Server:
         self.peak_held = 0
         self.created = 0
         self.evicted = 0
+        self.discarded = 0  # objects dropped after a failed request
         self._threads = []
         self._stop = False
         self.served = []
@@ -263,9 +264,10 @@ class Server:
                     self._reserved += est
                     break
                 self._cv.wait()
-        for v in victims:
-            self.executor.destroy(v)
         try:
+            # inside the try: a failing destroy must not keep the reservation
+            for v in victims:
+                self.executor.destroy(v)
             obj = self.executor.create(bank, key[1])
             b = self.executor.device_bytes(obj)
         except BaseException:
@@ -280,6 +282,18 @@ class Server:
             self.peak_held = max(self.peak_held, self._held)
             self.created += 1
         return obj
+
+    def _discard(self, obj):
+        """Drop an object whose request failed: it leaves the pool instead of
+        serving the next request in an unknown state."""
+        with self._cv:
+            self._held -= self._bytes.pop(id(obj), 0)
+            self.discarded += 1
+            self._cv.notify_all()
+        try:
+            self.executor.destroy(obj)
+        except Exception:  # noqa: BLE001 -- the request already carries the first error
+            pass
 
     def _release(self, key, obj):
         b = self.executor.device_bytes(obj)  # peak scratch may have grown
@@ -326,7 +340,8 @@ class Server:
             self.executor.run(obj, self.banks[req.bank], req)
         except BaseException as e:  # noqa: BLE001
             req.error = e
-        finally:
+            self._discard(obj)
+        else:
             self._release(key, obj)
 
     def _worker(self):

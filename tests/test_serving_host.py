@@ -131,3 +131,53 @@ def test_latency_stats():
     assert 0 < st["p50_s"] <= st["p99_s"]
     assert st["template_lags"] == 6 * (1200 - 200 + 1)
     assert st["throughput"] > 0
+
+
+class FailingExecutor(FakeExecutor):
+    """run() fails for requests whose signals hold a NaN; destroy() can be
+    made to fail."""
+
+    def __init__(self, **kw):
+        super().__init__(**kw)
+        self.destroy_fails = False
+
+    def run(self, obj, bank, req):
+        if np.isnan(req.signals).any():
+            raise RuntimeError("device error")
+        super().run(obj, bank, req)
+
+    def destroy(self, obj):
+        super().destroy(obj)
+        if self.destroy_fails:
+            raise OSError("destroy failed")
+
+
+def test_failed_request_discards_its_object():
+    ex = FailingExecutor(size=100, delay=0.0)
+    srv = Server(banks(), ex, memory_budget=1000, slots=1).start()
+    bad = req("a")
+    bad.signals[0, 0] = np.nan
+    rb = srv.submit(bad)
+    with pytest.raises(RuntimeError):
+        rb.wait(10)
+    good = srv.submit(req("a")).wait(10)
+    srv.close()
+    assert good.error is None
+    assert srv.discarded == 1 and srv.created == 2  # the failed object was not reused
+    assert not ex.alive
+
+
+def test_failing_destroy_keeps_no_reservation():
+    ex = FailingExecutor(size=100, delay=0.0)
+    srv = Server(banks(), ex, memory_budget=150, slots=1).start()
+    assert srv.submit(req("a")).wait(10).error is None
+    ex.destroy_fails = True  # evicting bank a's idle object for bank b fails
+    rb = srv.submit(req("b"))
+    with pytest.raises(OSError):
+        rb.wait(10)
+    ex.destroy_fails = False
+    # the budget is whole again: another request is admitted and served
+    assert srv.submit(req("c")).wait(10).error is None
+    srv.close()
+    assert srv._reserved == 0
+
