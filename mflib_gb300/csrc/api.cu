@@ -12,6 +12,8 @@
 #include <limits>
 #include <string>
 #include <memory>
+#include <new>
+#include <stdexcept>
 #include <vector>
 #include "mfgpu.h"
 #include "launch.h"
@@ -100,6 +102,47 @@ mfgpu_status fft_sizes(int nb, int nx, int *nfft, int *L)
 }  // namespace
 
 void mfgpu::set_last_error(const std::string &msg) { g_err = msg; }
+
+mfgpu_status mfgpu::status_of_exception() noexcept
+{
+    mfgpu_status st = MFGPU_ESTATE;
+    const char *what = "unknown exception";
+    try
+    {
+        throw;
+    }
+    catch (const std::bad_alloc &e)
+    {
+        st = MFGPU_ENOMEM;
+        what = e.what();
+    }
+    catch (const std::invalid_argument &e)
+    {
+        st = MFGPU_EINVAL;
+        what = e.what();
+    }
+    catch (const std::out_of_range &e)
+    {
+        st = MFGPU_EINVAL;
+        what = e.what();
+    }
+    catch (const std::exception &e)
+    {
+        what = e.what();
+    }
+    catch (...)
+    {
+    }
+    try
+    {
+        g_err = std::string("host exception: ") + what;
+    }
+    catch (...)
+    {
+        // no memory for the message either: keep the status
+    }
+    return st;
+}
 
 // ============================================================================
 // Overlap-save plan of one length bucket beside the primary plan (the
@@ -301,6 +344,7 @@ const char *mfgpu_last_error(void) { return g_err.c_str(); }
 int mfgpu_version(void) { return 100; }
 
 mfgpu_status mfgpu_device_count(int *count)
+try
 {
     if (!count) return fail(MFGPU_EINVAL, "count is NULL");
     int n = 0;
@@ -309,15 +353,25 @@ mfgpu_status mfgpu_device_count(int *count)
     *count = n;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_fft_sizes(int nb, int nx, int *fft_length, int *block_length)
+try
 {
     if (!fft_length || !block_length) return fail(MFGPU_EINVAL, "output is NULL");
     return fft_sizes(nb, nx, fft_length, block_length);
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 // ---------------------------------------------------------------------------
 mfgpu_status mfgpu_mf_create(int precision, mfgpu_mf **out)
+try
 {
     if (!out) return fail(MFGPU_EINVAL, "mf is NULL");
     if (precision != MFGPU_FLOAT32 && precision != MFGPU_FLOAT64)
@@ -339,8 +393,13 @@ mfgpu_status mfgpu_mf_create(int precision, mfgpu_mf **out)
     *out = mf;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_destroy(mfgpu_mf *mf)
+try
 {
     if (!mf) return MFGPU_OK;
     {
@@ -356,13 +415,22 @@ mfgpu_status mfgpu_mf_destroy(mfgpu_mf *mf)
     delete mf;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_clear(mfgpu_mf *mf)
+try
 {
     if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");
     DeviceGuard g(mf->dev);
     mf->reset();
     return MFGPU_OK;
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
 }
 
 // twiddles and resident template spectra of one plan (every template's
@@ -390,6 +458,7 @@ template <class T> static int plan_limit_lo() { return fft_limits<T>::lo; }
 template <class T> static int plan_limit_hi() { return fft_limits<T>::hi; }
 
 mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
+try
 {
     if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");
     DeviceGuard g(mf->dev);
@@ -902,6 +971,10 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
     mf->initialized = true;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 #define MF_CHECK_INIT(mf)                                                                                          \
     do                                                                                                             \
@@ -911,37 +984,58 @@ mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *p)
     } while (0)
 
 mfgpu_status mfgpu_mf_is_initialized(const mfgpu_mf *mf, int *flag)
+try
 {
     if (!mf || !flag) return fail(MFGPU_EINVAL, "NULL argument");
     *flag = mf->initialized ? 1 : 0;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_get_number_of_templates(const mfgpu_mf *mf, int *n)
+try
 {
     MF_CHECK_INIT(mf);
     if (!n) return fail(MFGPU_EINVAL, "n is NULL");
     *n = mf->nt;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_get_signal_length(const mfgpu_mf *mf, int *n)
+try
 {
     MF_CHECK_INIT(mf);
     if (!n) return fail(MFGPU_EINVAL, "n is NULL");
     *n = mf->n;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_get_filtered_signal_length(const mfgpu_mf *mf, int *n)
+try
 {
     MF_CHECK_INIT(mf);
     if (!n) return fail(MFGPU_EINVAL, "n is NULL");
     *n = mf->n - mf->maxLen + 1;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_get_plan(const mfgpu_mf *mf, int *fft_length, int *lags_per_block, int *n_blocks)
+try
 {
     MF_CHECK_INIT(mf);
     if (fft_length) *fft_length = mf->nfft;
@@ -949,8 +1043,13 @@ mfgpu_status mfgpu_mf_get_plan(const mfgpu_mf *mf, int *fft_length, int *lags_pe
     if (n_blocks) *n_blocks = mf->nblocks;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_get_correlator(const mfgpu_mf *mf, int *variant, int *tc_group, int *tc_k)
+try
 {
     MF_CHECK_INIT(mf);
     if (variant) *variant = mf->tc ? 4 : mf->mode_x == 3 ? 5 : mf->mode_x + 1;
@@ -958,8 +1057,13 @@ mfgpu_status mfgpu_mf_get_correlator(const mfgpu_mf *mf, int *variant, int *tc_g
     if (tc_k) *tc_k = mf->tc ? mf->tc_Kp : 0;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_get_buckets(const mfgpu_mf *mf, int max, int *fft_lengths, int *n_templates, int *count)
+try
 {
     MF_CHECK_INIT(mf);
     const int nb = (int) mf->xb.size() + 1;
@@ -972,8 +1076,13 @@ mfgpu_status mfgpu_mf_get_buckets(const mfgpu_mf *mf, int max, int *fft_lengths,
     }
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_get_bucket_plans(const mfgpu_mf *mf, int max, int *lags_per_block, int *variants, int *count)
+try
 {
     MF_CHECK_INIT(mf);
     const int nb = (int) mf->xb.size() + 1;
@@ -986,6 +1095,10 @@ mfgpu_status mfgpu_mf_get_bucket_plans(const mfgpu_mf *mf, int max, int *lags_pe
         if (variants) variants[b] = prim ? (mf->tc ? 4 : variant_of(mf->mode_x)) : variant_of(mf->xb[b]->mode);
     }
     return MFGPU_OK;
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
 }
 
 static mfgpu_status mf_channel_of(mfgpu_mf *mf, int it, int *c)
@@ -1024,6 +1137,7 @@ static mfgpu_status mf_resolve_stage(mfgpu_mf *mf)
 }
 
 mfgpu_status mfgpu_mf_stage_channel_signals(mfgpu_mf *mf, int n, const void *x, long ld)
+try
 {
     MF_CHECK_INIT(mf);
     DeviceGuard g(mf->dev);
@@ -1049,6 +1163,10 @@ mfgpu_status mfgpu_mf_stage_channel_signals(mfgpu_mf *mf, int n, const void *x, 
     CU(cudaEventRecord(mf->copy_done, mf->copy_stream));
     mf->staged = true;
     return MFGPU_OK;
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
 }
 
 // Copies nch channel rows (n samples each, source row stride ld samples)
@@ -1092,6 +1210,7 @@ static mfgpu_status mf_store_signal(mfgpu_mf *mf, int c, int n, const void *x, c
 }
 
 mfgpu_status mfgpu_mf_set_signal(mfgpu_mf *mf, int it, int n, const void *x)
+try
 {
     MF_CHECK_INIT(mf);
     DeviceGuard g(mf->dev);
@@ -1100,17 +1219,27 @@ mfgpu_status mfgpu_mf_set_signal(mfgpu_mf *mf, int it, int n, const void *x)
     if (st != MFGPU_OK) return st;
     return mf_store_signal(mf, c, n, x, cudaMemcpyHostToDevice);
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_set_channel_signal(mfgpu_mf *mf, int channel, int n, const void *x)
+try
 {
     MF_CHECK_INIT(mf);
     DeviceGuard g(mf->dev);
     if (channel < 0 || channel >= mf->nch) return fail(MFGPU_EINVAL, "channel out of range");
     return mf_store_signal(mf, channel, n, x, cudaMemcpyHostToDevice);
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_set_channel_signals(mfgpu_mf *mf, int first_channel, int n_channels, int n, const void *x,
                                           long ld)
+try
 {
     MF_CHECK_INIT(mf);
     DeviceGuard g(mf->dev);
@@ -1118,8 +1247,13 @@ mfgpu_status mfgpu_mf_set_channel_signals(mfgpu_mf *mf, int first_channel, int n
         return fail(MFGPU_EINVAL, "channel range out of range");
     return mf_store_signals(mf, first_channel, n_channels, n, x, ld, cudaMemcpyHostToDevice);
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_set_window(mfgpu_mf *mf, int n_src, int n, const void *x, long ld)
+try
 {
     MF_CHECK_INIT(mf);
     DeviceGuard g(mf->dev);
@@ -1155,8 +1289,13 @@ mfgpu_status mfgpu_mf_set_window(mfgpu_mf *mf, int n_src, int n, const void *x, 
     CU(cudaStreamSynchronize(mf->stream));
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_get_device_bytes(const mfgpu_mf *cmf, unsigned long long *bytes)
+try
 {
     auto *mf = const_cast<mfgpu_mf *>(cmf);
     if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");
@@ -1164,16 +1303,26 @@ mfgpu_status mfgpu_mf_get_device_bytes(const mfgpu_mf *cmf, unsigned long long *
     *bytes = mf->device_bytes();
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_set_channel_signal_device(mfgpu_mf *mf, int channel, int n, const void *dx)
+try
 {
     MF_CHECK_INIT(mf);
     DeviceGuard g(mf->dev);
     if (channel < 0 || channel >= mf->nch) return fail(MFGPU_EINVAL, "channel out of range");
     return mf_store_signal(mf, channel, n, dx, cudaMemcpyDeviceToDevice);
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_zero_signal(mfgpu_mf *mf, int it)
+try
 {
     MF_CHECK_INIT(mf);
     DeviceGuard g(mf->dev);
@@ -1190,8 +1339,13 @@ mfgpu_status mfgpu_mf_zero_signal(mfgpu_mf *mf, int it)
     CU(cudaStreamSynchronize(mf->stream));
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_get_signal(const mfgpu_mf *cmf, int it, int maxn, void *dst)
+try
 {
     auto *mf = const_cast<mfgpu_mf *>(cmf);
     MF_CHECK_INIT(mf);
@@ -1207,6 +1361,10 @@ mfgpu_status mfgpu_mf_get_signal(const mfgpu_mf *cmf, int it, int maxn, void *ds
                        cudaMemcpyDeviceToHost, mf->stream));
     CU(cudaStreamSynchronize(mf->stream));
     return MFGPU_OK;
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
 }
 
 // Records ev on the object's stream.  While apply is being captured into a
@@ -1344,6 +1502,7 @@ static mfgpu_status mf_apply_body(mfgpu_mf *mf)
 }
 
 mfgpu_status mfgpu_mf_apply(mfgpu_mf *mf)
+try
 {
     if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");
     if (!mf->initialized) return fail(MFGPU_ESTATE, "Class is not initialized");
@@ -1425,8 +1584,13 @@ mfgpu_status mfgpu_mf_apply(mfgpu_mf *mf)
     mf->have = true;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_set_graph(mfgpu_mf *mf, int enable)
+try
 {
     if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");
     DeviceGuard g(mf->dev);
@@ -1436,29 +1600,49 @@ mfgpu_status mfgpu_mf_set_graph(mfgpu_mf *mf, int enable)
     mf->use_graph = enable != 0;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_get_graph_launches(const mfgpu_mf *mf, long long *count)
+try
 {
     if (!mf || !count) return fail(MFGPU_EINVAL, "NULL argument");
     *count = mf->graph_launches;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_synchronize(mfgpu_mf *mf)
+try
 {
     if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");
     DeviceGuard g(mf->dev);
     return mf_sync(mf, true);
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_have_matched_filtered_signals(const mfgpu_mf *mf, int *flag)
+try
 {
     if (!mf || !flag) return fail(MFGPU_EINVAL, "NULL argument");
     *flag = mf->have ? 1 : 0;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_get_last_timings(mfgpu_mf *mf, float *xcorr_ms, float *apply_ms)
+try
 {
     if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");
     DeviceGuard g(mf->dev);
@@ -1468,19 +1652,33 @@ mfgpu_status mfgpu_mf_get_last_timings(mfgpu_mf *mf, float *xcorr_ms, float *app
     if (apply_ms) *apply_ms = mf->last_apply_ms;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_get_launch_count(const mfgpu_mf *mf, long long *count)
+try
 {
     if (!mf || !count) return fail(MFGPU_EINVAL, "NULL argument");
     *count = mf->launches;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_get_stream(const mfgpu_mf *mf, void **stream)
+try
 {
     if (!mf || !stream) return fail(MFGPU_EINVAL, "NULL argument");
     *stream = (void *) mf->stream;
     return MFGPU_OK;
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
 }
 
 static mfgpu_status mf_check_template(mfgpu_mf *mf, int it)
@@ -1510,13 +1708,19 @@ static mfgpu_status mf_copy_rho(mfgpu_mf *mf, int it, int count, int maxn, void 
 }
 
 mfgpu_status mfgpu_mf_get_matched_filtered_signal(mfgpu_mf *mf, int it, int maxn, void *dst, int *nout)
+try
 {
     MF_CHECK_INIT(mf);
     DeviceGuard g(mf->dev);
     return mf_copy_rho(mf, it, mf->n - mf->maxLen + 1, maxn, dst, nout);
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_get_valid_signal(mfgpu_mf *mf, int it, int maxn, void *dst, int *nout)
+try
 {
     MF_CHECK_INIT(mf);
     DeviceGuard g(mf->dev);
@@ -1524,8 +1728,13 @@ mfgpu_status mfgpu_mf_get_valid_signal(mfgpu_mf *mf, int it, int maxn, void *dst
     if (st != MFGPU_OK) return st;
     return mf_copy_rho(mf, it, mf->nvalid[it], maxn, dst, nout);
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_get_device_signal(mfgpu_mf *mf, int it, const void **dptr, int *nvalid)
+try
 {
     MF_CHECK_INIT(mf);
     mfgpu_status st = mf_check_template(mf, it);
@@ -1534,6 +1743,10 @@ mfgpu_status mfgpu_mf_get_device_signal(mfgpu_mf *mf, int it, const void **dptr,
     *dptr = mf->rho.as<char>() + mf->esz() * (size_t) it * mf->ldr;
     if (nvalid) *nvalid = mf->nvalid[it];
     return MFGPU_OK;
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
 }
 
 template <class T> static mfgpu_status mf_stack(mfgpu_mf *mf, int maxn, void *dst, int *nout)
@@ -1568,6 +1781,7 @@ template <class T> static mfgpu_status mf_stack(mfgpu_mf *mf, int maxn, void *ds
 }
 
 mfgpu_status mfgpu_mf_shift_and_stack(mfgpu_mf *mf, int maxn, void *dst, int *nout)
+try
 {
     MF_CHECK_INIT(mf);
     DeviceGuard g(mf->dev);
@@ -1577,8 +1791,13 @@ mfgpu_status mfgpu_mf_shift_and_stack(mfgpu_mf *mf, int maxn, void *dst, int *no
     if (st != MFGPU_OK) return st;
     return mf->prec == 4 ? mf_stack<float>(mf, maxn, dst, nout) : mf_stack<double>(mf, maxn, dst, nout);
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_get_spectra_of_template(mfgpu_mf *mf, int it, int maxn, void *dst, int *nout)
+try
 {
     MF_CHECK_INIT(mf);
     DeviceGuard g(mf->dev);
@@ -1600,8 +1819,13 @@ mfgpu_status mfgpu_mf_get_spectra_of_template(mfgpu_mf *mf, int it, int maxn, vo
     if (nout) *nout = 2 * ns;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_find_peaks(mfgpu_mf *mf, double threshold, int min_distance, int trace_length)
+try
 {
     MF_CHECK_INIT(mf);
     DeviceGuard g(mf->dev);
@@ -1637,6 +1861,10 @@ mfgpu_status mfgpu_mf_find_peaks(mfgpu_mf *mf, double threshold, int min_distanc
     if (rc != 0) return fail(MFGPU_ECUDA, err);
     mf->have_peaks = true;
     return MFGPU_OK;
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
 }
 
 template <class T> static mfgpu_status mf_detect(mfgpu_mf *mf, const mfgpu_detect_params *dp, long len)
@@ -1731,6 +1959,7 @@ template <class T> static mfgpu_status mf_detect(mfgpu_mf *mf, const mfgpu_detec
 }
 
 mfgpu_status mfgpu_mf_detect(mfgpu_mf *mf, const mfgpu_detect_params *dp, int *n_detections)
+try
 {
     MF_CHECK_INIT(mf);
     DeviceGuard g(mf->dev);
@@ -1749,8 +1978,13 @@ mfgpu_status mfgpu_mf_detect(mfgpu_mf *mf, const mfgpu_detect_params *dp, int *n
     if (n_detections) *n_detections = (int) mf->dets.size();
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_get_detections(mfgpu_mf *mf, int max, mfgpu_detection *out, int *n)
+try
 {
     MF_CHECK_INIT(mf);
     const int nd = (int) mf->dets.size();
@@ -1759,9 +1993,14 @@ mfgpu_status mfgpu_mf_get_detections(mfgpu_mf *mf, int max, mfgpu_detection *out
     for (int i = 0; i < nd && i < max; ++i) out[i] = mf->dets[i];
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_relative_amplitudes(int precision, int L, const double *templ, int n_windows, const void *windows,
                                        long ld, double *gr, double *sr, int *valid)
+try
 {
     if (precision != MFGPU_FLOAT32 && precision != MFGPU_FLOAT64)
         return fail(MFGPU_EINVAL, "precision must be MFGPU_FLOAT32 or MFGPU_FLOAT64");
@@ -1800,24 +2039,39 @@ mfgpu_status mfgpu_relative_amplitudes(int precision, int L, const double *templ
     CU(cudaStreamSynchronize(s));
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_set_peak_threshold(mfgpu_mf *mf, double threshold)
+try
 {
     if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");
     if (threshold > 1) return fail(MFGPU_EINVAL, "Threshold = " + std::to_string(threshold) + " must be at most 1");
     mf->pk_req = threshold < 0 ? -1.0 : threshold;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_get_peak_threshold(const mfgpu_mf *mf, double *threshold, int *active)
+try
 {
     if (!mf || !threshold) return fail(MFGPU_EINVAL, "NULL argument");
     *threshold = mf->pk_req;
     if (active) *active = mf->pk_fused ? 1 : 0;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_get_peaks(mfgpu_mf *mf, int it, int maxn, int *dst, int *nout)
+try
 {
     MF_CHECK_INIT(mf);
     DeviceGuard g(mf->dev);
@@ -1832,8 +2086,13 @@ mfgpu_status mfgpu_mf_get_peaks(mfgpu_mf *mf, int it, int maxn, int *dst, int *n
     if (nout) *nout = (int) cnt;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_mf_get_all_peaks(mfgpu_mf *mf, int nt, int *counts, int max_total, int *indices, int *total)
+try
 {
     MF_CHECK_INIT(mf);
     DeviceGuard g(mf->dev);
@@ -1849,6 +2108,10 @@ mfgpu_status mfgpu_mf_get_all_peaks(mfgpu_mf *mf, int nt, int *counts, int max_t
         CU(cudaMemcpy(indices, mf->pk.peaks.p, sizeof(int) * (size_t) tot, cudaMemcpyDeviceToHost));
     }
     return MFGPU_OK;
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
 }
 
 
@@ -1870,6 +2133,7 @@ struct mfgpu_peaks
 
 
 mfgpu_status mfgpu_peaks_create(int precision, mfgpu_peaks **out)
+try
 {
     if (!out) return fail(MFGPU_EINVAL, "pf is NULL");
     if (precision != MFGPU_FLOAT32 && precision != MFGPU_FLOAT64)
@@ -1886,8 +2150,13 @@ mfgpu_status mfgpu_peaks_create(int precision, mfgpu_peaks **out)
     *out = pf;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_peaks_destroy(mfgpu_peaks *pf)
+try
 {
     if (!pf) return MFGPU_OK;
     {
@@ -1900,8 +2169,13 @@ mfgpu_status mfgpu_peaks_destroy(mfgpu_peaks *pf)
     delete pf;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_peaks_clear(mfgpu_peaks *pf)
+try
 {
     if (!pf) return fail(MFGPU_EINVAL, "pf is NULL");
     DeviceGuard g(pf->dev);
@@ -1915,8 +2189,13 @@ mfgpu_status mfgpu_peaks_clear(mfgpu_peaks *pf)
     pf->peaks.clear();
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_peaks_set_threshold(mfgpu_peaks *pf, double threshold)
+try
 {
     if (!pf) return fail(MFGPU_EINVAL, "pf is NULL");
     pf->npeaks = 0;
@@ -1925,30 +2204,50 @@ mfgpu_status mfgpu_peaks_set_threshold(mfgpu_peaks *pf, double threshold)
     pf->thr = threshold;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_peaks_get_threshold(const mfgpu_peaks *pf, double *threshold)
+try
 {
     if (!pf || !threshold) return fail(MFGPU_EINVAL, "NULL argument");
     *threshold = pf->thr;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_peaks_set_minimum_peak_distance(mfgpu_peaks *pf, int min_distance)
+try
 {
     if (!pf) return fail(MFGPU_EINVAL, "pf is NULL");
     pf->npeaks = 0;
     pf->dist = min_distance;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_peaks_get_minimum_peak_distance(const mfgpu_peaks *pf, int *min_distance)
+try
 {
     if (!pf || !min_distance) return fail(MFGPU_EINVAL, "NULL argument");
     *min_distance = pf->dist;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_peaks_set_signal(mfgpu_peaks *pf, int n, const void *x)
+try
 {
     if (!pf) return fail(MFGPU_EINVAL, "pf is NULL");
     pf->npeaks = 0;
@@ -1962,8 +2261,13 @@ mfgpu_status mfgpu_peaks_set_signal(mfgpu_peaks *pf, int n, const void *x)
     pf->n = n;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_peaks_apply(mfgpu_peaks *pf)
+try
 {
     if (!pf) return fail(MFGPU_EINVAL, "pf is NULL");
     DeviceGuard g(pf->dev);
@@ -1984,15 +2288,25 @@ mfgpu_status mfgpu_peaks_apply(mfgpu_peaks *pf)
         CU(cudaMemcpy(pf->peaks.data(), pf->ws.peaks.p, sizeof(int) * pf->npeaks, cudaMemcpyDeviceToHost));
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_peaks_get_number_of_peaks(const mfgpu_peaks *pf, int *n)
+try
 {
     if (!pf || !n) return fail(MFGPU_EINVAL, "NULL argument");
     *n = pf->npeaks;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_peaks_get_peak_indices(const mfgpu_peaks *pf, int maxn, int *dst)
+try
 {
     if (!pf) return fail(MFGPU_EINVAL, "pf is NULL");
     if (maxn < pf->npeaks)
@@ -2001,6 +2315,10 @@ mfgpu_status mfgpu_peaks_get_peak_indices(const mfgpu_peaks *pf, int maxn, int *
     if (!dst) return fail(MFGPU_EINVAL, "peaks is NULL");
     if (pf->npeaks > 0) std::memcpy(dst, pf->peaks.data(), sizeof(int) * pf->npeaks);
     return MFGPU_OK;
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
 }
 
 
@@ -2021,6 +2339,7 @@ struct mfgpu_dbscan
 
 
 mfgpu_status mfgpu_dbscan_create(mfgpu_dbscan **out)
+try
 {
     if (!out) return fail(MFGPU_EINVAL, "db is NULL");
     auto *db = new mfgpu_dbscan();
@@ -2039,8 +2358,13 @@ mfgpu_status mfgpu_dbscan_create(mfgpu_dbscan **out)
     *out = db;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_dbscan_destroy(mfgpu_dbscan *db)
+try
 {
     if (!db) return MFGPU_OK;
     {
@@ -2052,8 +2376,13 @@ mfgpu_status mfgpu_dbscan_destroy(mfgpu_dbscan *db)
     delete db;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_dbscan_clear(mfgpu_dbscan *db)
+try
 {
     if (!db) return fail(MFGPU_EINVAL, "db is NULL");
     db->eps = 3;
@@ -2063,8 +2392,13 @@ mfgpu_status mfgpu_dbscan_clear(mfgpu_dbscan *db)
     db->X.clear(); db->w.clear(); db->labels.clear();
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_dbscan_initialize(mfgpu_dbscan *db, double epsilon, int min_observations)
+try
 {
     if (!db) return fail(MFGPU_EINVAL, "db is NULL");
     mfgpu_dbscan_clear(db);
@@ -2075,6 +2409,10 @@ mfgpu_status mfgpu_dbscan_initialize(mfgpu_dbscan *db, double epsilon, int min_o
     db->min_obs = min_observations;
     db->init = true;
     return MFGPU_OK;
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
 }
 
 static mfgpu_status db_set(mfgpu_dbscan *db, int n_obs, int n_features, const double *X, const double *w)
@@ -2101,17 +2439,28 @@ static mfgpu_status db_set(mfgpu_dbscan *db, int n_obs, int n_features, const do
 }
 
 mfgpu_status mfgpu_dbscan_set_data(mfgpu_dbscan *db, int n_obs, int n_features, const double *X)
+try
 {
     return db_set(db, n_obs, n_features, X, nullptr);
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
 }
 
 mfgpu_status mfgpu_dbscan_set_weighted_data(mfgpu_dbscan *db, int n_obs, int n_features, const double *X,
                                             const double *weights)
+try
 {
     return db_set(db, n_obs, n_features, X, weights);
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_dbscan_cluster(mfgpu_dbscan *db)
+try
 {
     if (!db) return fail(MFGPU_EINVAL, "db is NULL");
     db->have_labels = false;
@@ -2128,15 +2477,25 @@ mfgpu_status mfgpu_dbscan_cluster(mfgpu_dbscan *db)
     db->have_labels = true;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_dbscan_get_number_of_clusters(const mfgpu_dbscan *db, int *n)
+try
 {
     if (!db || !n) return fail(MFGPU_EINVAL, "NULL argument");
     *n = db->ncl;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_dbscan_get_labels(const mfgpu_dbscan *db, int maxn, int *labels)
+try
 {
     if (!db) return fail(MFGPU_EINVAL, "db is NULL");
     if (!db->have_labels) return fail(MFGPU_ESTATE, "clustering not yet done");
@@ -2144,37 +2503,62 @@ mfgpu_status mfgpu_dbscan_get_labels(const mfgpu_dbscan *db, int maxn, int *labe
     std::memcpy(labels, db->labels.data(), sizeof(int) * db->labels.size());
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_dbscan_get_launch_count(const mfgpu_dbscan *db, long long *count)
+try
 {
     if (!db || !count) return fail(MFGPU_EINVAL, "NULL argument");
     *count = db->launches;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_dbscan_is_initialized(const mfgpu_dbscan *db, int *flag)
+try
 {
     if (!db || !flag) return fail(MFGPU_EINVAL, "NULL argument");
     *flag = db->init;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_dbscan_have_data(const mfgpu_dbscan *db, int *flag)
+try
 {
     if (!db || !flag) return fail(MFGPU_EINVAL, "NULL argument");
     *flag = db->have_data;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_dbscan_have_labels(const mfgpu_dbscan *db, int *flag)
+try
 {
     if (!db || !flag) return fail(MFGPU_EINVAL, "NULL argument");
     *flag = db->have_labels;
     return MFGPU_OK;
 }
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
 
 mfgpu_status mfgpu_dbscan_segmented(mfgpu_dbscan *db, int n_segments, const int *seg_offsets, int n_features,
                                     const double *X, const double *weights, int *labels, int *n_clusters)
+try
 {
     if (!db) return fail(MFGPU_EINVAL, "db is NULL");
     if (!db->init) return fail(MFGPU_ESTATE, "Class not initialized");
@@ -2196,5 +2580,9 @@ mfgpu_status mfgpu_dbscan_segmented(mfgpu_dbscan *db, int n_segments, const int 
                         n_clusters, db->ws, db->stream, &db->launches, err);
     if (rc != 0) return fail(MFGPU_ECUDA, err);
     return MFGPU_OK;
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
 }
 

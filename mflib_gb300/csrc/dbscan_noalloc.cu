@@ -108,6 +108,7 @@ mfgpu_status fail(mfgpu_status s, const std::string &m)
 mfgpu_status mfgpu_dbscan_segmented_noalloc(int n_segments, const int *d_seg_offsets, int n_obs, int n_features,
                                             const double *d_X, const double *d_weights, double epsilon,
                                             int min_observations, int *d_labels, int *d_n_clusters, void *stream)
+try
 {
     if (n_segments < 1 || n_segments > kMaxSegments)
         return fail(MFGPU_EINVAL, "n_segments = " + std::to_string(n_segments) + " must be in [1, " +
@@ -158,4 +159,8 @@ mfgpu_status mfgpu_dbscan_segmented_noalloc(int n_segments, const int *d_seg_off
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(MFGPU_ECUDA, cudaGetErrorString(e));
     return MFGPU_OK;
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
 }

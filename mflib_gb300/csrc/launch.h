@@ -10,6 +10,7 @@
 #include "kernels_mf.cuh"
 #include "kernels_util.cuh"
 #include "tc_params.h"
+#include "mfgpu.h"
 
 namespace mfgpu {
 
@@ -160,6 +161,11 @@ int run_dbscan(int n, int nf, const double *X, const double *w, double eps, int 
 
 // message returned by mfgpu_last_error() on the calling thread
 void set_last_error(const std::string &msg);
+// Status for an exception caught at the C ABI (called inside a catch
+// handler): std::bad_alloc -> MFGPU_ENOMEM, std::invalid_argument and
+// std::out_of_range -> MFGPU_EINVAL, anything else -> MFGPU_ESTATE, with
+// the exception's text as the last error.  Exceptions never cross the ABI.
+mfgpu_status status_of_exception() noexcept;
 
 // device scan helper: out[0..n] = exclusive scan of in[0..n) (+ total)
 cudaError_t device_excl_scan(const int *in, long n, long long *out, long long *tiles, cudaStream_t s,
