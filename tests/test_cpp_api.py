@@ -1,6 +1,8 @@
 """The C++ mirror of mflib's classes (include/mfgpu.hpp) compiles against
 the C ABI, links against libmfgpu.so, and on a GPU passes the reference's
-known-answer checks (tests/cpp/test_mflib_api.cpp)."""
+known-answer checks (tests/cpp/test_mflib_api.cpp); the ABI's exception
+handler maps host exceptions to status codes (tests/cpp/test_abi_exceptions.cpp,
+no GPU)."""
 import os
 import shutil
 import subprocess
@@ -45,3 +47,19 @@ def test_cpp_api_on_gpu(tmp_path):
     run = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert run.returncode == 0, run.stdout + run.stderr
     assert "ALL PASSED" in run.stdout
+
+
+@pytest.mark.skipif(CXX is None, reason="g++ not found")
+def test_abi_exception_mapping(tmp_path):
+    if not os.path.exists(os.path.join(LIBDIR, "libmfgpu.so")):
+        pytest.skip("libmfgpu.so not built")
+    exe = str(tmp_path / "test_abi_exceptions")
+    src = os.path.join(ROOT, "tests", "cpp", "test_abi_exceptions.cpp")
+    r = subprocess.run([CXX, "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        src, "-o", exe, "-L", LIBDIR, "-lmfgpu", "-Wl,-rpath," + LIBDIR],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    run = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert run.returncode == 0, run.stdout + run.stderr
+    assert "ALL PASSED" in run.stdout
+
