@@ -275,6 +275,12 @@ mfgpu_status mfgpu_mf_synchronize(mfgpu_mf *mf);
 mfgpu_status mfgpu_mf_get_last_timings(mfgpu_mf *mf, float *xcorr_ms, float *apply_ms);
 /* Number of kernel launches issued by the object since it was created. */
 mfgpu_status mfgpu_mf_get_launch_count(const mfgpu_mf *mf, long long *count);
+/* No reference counterpart.  FP32 objects: the number of 32-lag runs (per
+ * channel row) that the last apply recomputed by direct correlation because
+ * the chosen correlator's rounding-error bound exceeded 2e-5 of the run's
+ * quietest window (windows or FFT blocks that straddle amplitude changes of
+ * several decades); 0 for FP64 objects.  Waits for the apply. */
+mfgpu_status mfgpu_mf_get_fixup_runs(mfgpu_mf *mf, long long *runs);
 /* The object's CUDA stream (a cudaStream_t), on which every launch and
  * copy of the object is issued; for event timing by the caller. */
 mfgpu_status mfgpu_mf_get_stream(const mfgpu_mf *mf, void **stream);

@@ -16,7 +16,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libmfgpu.so")
-SOURCES = ["api.cu", "mf_f32.cu", "mf_f64.cu", "mf_tc.cu", "peaks_dbscan.cu", "dbscan_noalloc.cu", "detector.cu"]
+SOURCES = ["api.cu", "mf_f32.cu", "mf_f64.cu", "mf_tc.cu", "peaks_dbscan.cu", "dbscan_noalloc.cu", "detector.cu", "fixup.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -209,6 +209,15 @@ struct mfgpu_mf
     DevBuf pk_cnt, pk_idx, pk_val;
     DevBuf pk_flags;   // tensor-core correlator: candidate flags per 64 lags
     int pk_words = 0;
+    // FP32 accuracy safeguards (kernels_fix.cuh): per-run window statistics
+    // (rstat, row stride ldrs), per-chunk statistics (cst, row stride ldc,
+    // nchunks valid), run flags, the tensor-core strips' operand offsets, the
+    // fix-up batches (channel, templates, coefficient offsets and lengths,
+    // coefficients, coefficient sums) and the candidate slots to recount
+    bool fx_on = false;
+    int fx_L = 0, fx_nden = 0, fx_nruns = 0, fx_nbatch = 0;
+    long ldrs = 0, ldc = 0, fx_nchunks = 0;
+    DevBuf rstat, cst, fxflags, tc_off, fx_bch, fx_btid, fx_boff, fx_bL, fx_bco, fx_bsum, pk_dirty;
     // length buckets beside the primary plan (longest templates); per
     // template its bucket's block length and block count, and the slot row
     // stride of the gathered candidates (the largest block count)
@@ -261,7 +270,9 @@ struct mfgpu_mf
         DevBuf *all[] = {&x,      &rho,      &Bc,   &tw,  &grp_chan, &grp_tb, &grp_te, &tids,      &tlen_d,
                          &nvalid_d, &dead,   &err,  &tmpl_d, &toff_d, &pmin, &pmax,  &chan_list, &stackbuf,
                          &shifts_d, &weights_d, &specbuf, &den, &pk_cnt, &pk_idx, &pk_val, &xstage,
-                         &xrange,   &tc_B,   &tc_bscale, &tc_grp_chan, &tc_grp_tid, &pk_flags};
+                         &xrange,   &tc_B,   &tc_bscale, &tc_grp_chan, &tc_grp_tid, &pk_flags,
+                         &rstat,    &cst,    &fxflags, &tc_off, &fx_bch, &fx_btid, &fx_boff, &fx_bL,
+                         &fx_bco,   &fx_bsum, &pk_dirty};
         for (DevBuf *d : all) f(*d);
         pk.each_buf(f);
         f(row_S);
@@ -302,6 +313,9 @@ struct mfgpu_mf
         can_stack = false;
         nfft = log2p = S = nblocks = ngroups = maxvalid = 0;
         ldx = ldr = 0;
+        fx_on = false;
+        fx_L = fx_nden = fx_nruns = fx_nbatch = 0;
+        ldrs = ldc = fx_nchunks = 0;
     }
 };
 
@@ -825,6 +839,33 @@ try
         mf->ldx = std::max<long>(mf->ldx, ((long) mf->nden * lpc + 32L * den_tail_runs(maxLen) + 63) / 64 * 64);
     }
     if (mf->tc) mf->shared_den = true;  // the tensor-core epilogue reads den_kernel's rows
+    if (mf->prec == 4)
+    {
+        // accuracy safeguards: window statistics of the shared length (the
+        // normalisation rows come from the same launch) or, for several
+        // lengths, of the shortest one (a longer window starting at the same
+        // lag contains it, so its variance is no smaller: the bound stays
+        // conservative for every template)
+        mf->fx_on = true;
+        mf->fx_L = mf->shared_den ? maxLen : minLen;
+        const long lpc = den_lags_per_cta(mf->fx_L);
+        mf->fx_nruns = (std::max(1, maxvalid) + 31) / 32;
+        long cover = (long) mf->fx_nruns * 32;
+        if (mf->tc) cover = std::max<long>(cover, (long) mf->tc_tiles * kTcLags);
+        mf->fx_nden = mf->shared_den ? mf->nden : (int) ((cover + lpc - 1) / lpc);
+        if (mf->shared_den) mf->fx_nden = std::max<int>(mf->nden, (int) ((cover + lpc - 1) / lpc));
+        mf->ldrs = ((long) mf->fx_nden * lpc / 32 + 63) / 64 * 64;
+        mf->fx_nchunks = (long) mf->fx_nden * lpc / 32 + den_tail_runs(mf->fx_L) + 1;
+        mf->ldc = (mf->fx_nchunks + 63) / 64 * 64;
+        mf->ldx = std::max<long>(mf->ldx, ((long) mf->fx_nden * lpc + 32L * den_tail_runs(mf->fx_L) + 63) / 64 * 64);
+        // the fix-up stages L + 31 samples from the start of every run
+        mf->ldx = std::max<long>(mf->ldx, ((long) mf->fx_nruns * 32 + maxLen + 32 + 63) / 64 * 64);
+        if (mf->shared_den)
+        {
+            mf->nden = mf->fx_nden;
+            mf->ldd = std::max<long>(mf->ldd, ((long) mf->nden * lpc + 63) / 64 * 64);
+        }
+    }
     // work groups of one plan: each channel's templates of the bucket, split
     // so the grid has enough CTAs
     struct Groups
@@ -965,6 +1006,55 @@ try
                           mf->tc_grp_tid.as<int>(), mf->tc_groups, mf->tc_Gp, mf->tc_Kp, mf->tc_B.as<__half>(),
                           mf->tc_bscale.as<float>(), mf->stream));
         ++mf->launches;
+    }
+    if (mf->fx_on)
+    {
+        // fix-up batches: each channel's templates sorted by length, kFixBatch
+        // per batch, coefficients interleaved [i][kFixBatch]
+        std::vector<int> bch, btid, bL;
+        std::vector<long> boff;
+        long tot_co = 0;
+        for (int c = 0; c < nch; ++c)
+        {
+            std::vector<int> ts = chan_t[c];
+            std::stable_sort(ts.begin(), ts.end(), [&](int a, int b) { return mf->lens[a] < mf->lens[b]; });
+            for (size_t i = 0; i < ts.size(); i += kFixBatch)
+            {
+                int lb = 0;
+                bch.push_back(c);
+                for (int k = 0; k < kFixBatch; ++k)
+                {
+                    const int t = i + k < ts.size() ? ts[i + k] : -1;
+                    btid.push_back(t);
+                    if (t >= 0) lb = std::max(lb, mf->lens[t]);
+                }
+                bL.push_back(lb);
+                boff.push_back(tot_co);
+                tot_co += (long) kFixBatch * lb;
+            }
+        }
+        mf->fx_nbatch = (int) bch.size();
+        CU(mf->rstat.ensure(sizeof(float4) * (size_t) nch * mf->ldrs));
+        CU(mf->cst.ensure(sizeof(float2) * (size_t) nch * mf->ldc));
+        CU(mf->fxflags.ensure((size_t) nch * mf->ldrs));
+        if (mf->tc) CU(mf->tc_off.ensure(sizeof(float) * (size_t) nch * mf->tc_tiles));
+        CU(mf->fx_bch.ensure(sizeof(int) * bch.size()));
+        CU(mf->fx_btid.ensure(sizeof(int) * btid.size()));
+        CU(mf->fx_boff.ensure(sizeof(long) * boff.size()));
+        CU(mf->fx_bL.ensure(sizeof(int) * bL.size()));
+        CU(mf->fx_bco.ensure(sizeof(float) * (size_t) std::max<long>(1, tot_co)));
+        CU(mf->fx_bsum.ensure(sizeof(float) * nt));
+        CU(cudaMemcpyAsync(mf->fx_bch.p, bch.data(), sizeof(int) * bch.size(), cudaMemcpyHostToDevice, mf->stream));
+        CU(cudaMemcpyAsync(mf->fx_btid.p, btid.data(), sizeof(int) * btid.size(), cudaMemcpyHostToDevice, mf->stream));
+        CU(cudaMemcpyAsync(mf->fx_boff.p, boff.data(), sizeof(long) * boff.size(), cudaMemcpyHostToDevice, mf->stream));
+        CU(cudaMemcpyAsync(mf->fx_bL.p, bL.data(), sizeof(int) * bL.size(), cudaMemcpyHostToDevice, mf->stream));
+        CU(launch_fix_prep(mf->tmpl_d.as<double>(), mf->toff_d.as<long>(), mf->tlen_d.as<int>(), mf->fx_btid.as<int>(),
+                           mf->fx_boff.as<long>(), mf->fx_bL.as<int>(), mf->fx_nbatch, mf->fx_bco.as<float>(),
+                           mf->fx_bsum.as<float>(), mf->stream));
+        ++mf->launches;
+        if (!mf->n_sm) CU(cudaDeviceGetAttribute(&mf->n_sm, cudaDevAttrMultiProcessorCount, mf->dev));
+        // the host vectors above must outlive the copies
+        CU(cudaStreamSynchronize(mf->stream));
     }
     CU(cudaStreamSynchronize(mf->stream));
     CU(cudaGetLastError());
@@ -1395,7 +1485,46 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
     p.err = mf->err.as<int>();
     p.den = mf->den.as<T>();
     p.ldd = mf->ldd;
-    if (mf->shared_den)
+    if constexpr (sizeof(T) == 4)
+    {
+        if (mf->fx_on)
+        {
+            // normalisation rows (one length) and window statistics, then the
+            // per-run error bounds of the chosen correlator
+            CU(launch_den_robust(mf->x.as<float>(), mf->ldx, mf->fx_L, mf->shared_den ? mf->den.as<float>() : nullptr,
+                                 mf->ldd, (float) p.tol, mf->rstat.as<float4>(), mf->ldrs, mf->cst.as<float2>(),
+                                 mf->ldc, mf->fx_nden, mf->nch, mf->stream));
+            CU(cudaMemsetAsync(mf->fxflags.p, 0, (size_t) mf->nch * mf->ldrs, mf->stream));
+            ++mf->launches;
+            if (mf->tc)
+            {
+                CU(launch_fix_flag_tc(mf->x.as<float>(), mf->ldx, mf->maxLen, mf->rstat.as<float4>(), mf->ldrs,
+                                      mf->fx_nruns, mf->tc_tiles, mf->nch, mf->dead.as<unsigned char>(),
+                                      mf->xrange.as<float>(), mf->tc_off.as<float>(),
+                                      mf->fxflags.as<unsigned char>(), kFixTcC1, kFixTcC2, kFixTol, mf->stream));
+                ++mf->launches;
+            }
+            else
+            {
+                const float coef = kFixFftK * 0x1p-24f / kFixTol;
+                CU(launch_fix_flag_fft(mf->cst.as<float2>(), mf->ldc, mf->fx_nchunks, mf->S, mf->nfft, mf->nblocks,
+                                       mf->nch, mf->rstat.as<float4>(), mf->ldrs, mf->fx_nruns,
+                                       mf->dead.as<unsigned char>(), mf->fxflags.as<unsigned char>(), coef * coef,
+                                       mf->stream));
+                ++mf->launches;
+                for (auto &xb : mf->xb)
+                {
+                    if (xb->ngroups == 0) continue;
+                    CU(launch_fix_flag_fft(mf->cst.as<float2>(), mf->ldc, mf->fx_nchunks, xb->S, xb->nfft, xb->nblocks,
+                                           mf->nch, mf->rstat.as<float4>(), mf->ldrs, mf->fx_nruns,
+                                           mf->dead.as<unsigned char>(), mf->fxflags.as<unsigned char>(),
+                                           coef * coef, mf->stream));
+                    ++mf->launches;
+                }
+            }
+        }
+    }
+    if (mf->shared_den && !(sizeof(T) == 4 && mf->fx_on))
     {
         CU(launch_den<T>(mf->x.as<T>(), mf->ldx, mf->maxLen, mf->den.as<T>(), mf->ldd, p.tol, mf->nden, mf->nch,
                          mf->stream));
@@ -1429,6 +1558,7 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
             q.B = mf->tc_B.as<__half>(); q.bscale = mf->tc_bscale.as<float>();
             q.grp_chan = mf->tc_grp_chan.as<int>(); q.grp_tid = mf->tc_grp_tid.as<int>();
             q.xrange = mf->xrange.as<float>(); q.dead = mf->dead.as<unsigned char>();
+            q.off = mf->tc_off.as<float>();
             q.den = mf->den.as<float>(); q.ldd = mf->ldd;
             q.rho = mf->rho.as<float>(); q.ldr = mf->ldr;
             q.nv = mf->maxvalid; q.Kp = mf->tc_Kp; q.Gp = mf->tc_Gp; q.tmem_cols = mf->tc_cols;
@@ -1481,6 +1611,55 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
     return MFGPU_OK;
 }
 
+// FP32: recomputes the runs the error bounds flagged (every template of the
+// run's channel), then recounts the fused peak candidates of the blocks it
+// touched.  Both kernels scan the flag bytes themselves, so the host never
+// waits for the flags; with no flagged run they only read the flags.
+static mfgpu_status mf_launch_fixup(mfgpu_mf *mf)
+{
+    FixParams f{};
+    f.x = mf->x.as<float>(); f.ldx = mf->ldx;
+    f.rho = mf->rho.as<float>(); f.ldr = mf->ldr;
+    f.flags = mf->fxflags.as<unsigned char>(); f.ldf = mf->ldrs;
+    f.nruns = mf->fx_nruns; f.nspans = (mf->fx_nruns + 31) / 32;
+    f.nbatch = mf->fx_nbatch;
+    f.bch = mf->fx_bch.as<int>(); f.btid = mf->fx_btid.as<int>(); f.boff = mf->fx_boff.as<long>();
+    f.bL = mf->fx_bL.as<int>(); f.bco = mf->fx_bco.as<float>(); f.bsum = mf->fx_bsum.as<float>();
+    f.tlen = mf->tlen_d.as<int>(); f.nvalid = mf->nvalid_d.as<int>();
+    f.tol = 1.e-6f;  // src/matchedFilter.cpp:1287
+    f.Lmax = mf->maxLen;
+    const bool fused = mf->pk_fused && !mf->tc;
+    if (mf->pk_fused && mf->tc)
+    {
+        f.pk_flags = mf->pk_flags.as<unsigned>();
+        f.pk_words = mf->pk_words;
+        f.pk_thr = (float) mf->pk_fused_thr;
+        f.pk_len = mf->pk_fused_len;
+    }
+    if (fused)
+    {
+        const size_t ns = (size_t) mf->nt * mf->pk_stride;
+        CU(mf->pk_dirty.ensure(ns));
+        CU(cudaMemsetAsync(mf->pk_dirty.p, 0, ns, mf->stream));
+        f.pk_dirty = mf->pk_dirty.as<unsigned char>();
+        f.pk_stride = mf->pk_stride;
+        f.row_S = mf->xb.empty() ? nullptr : mf->row_S.as<int>();
+        f.S0 = mf->S;
+    }
+    CU(launch_fixup(f, 4 * std::max(1, mf->n_sm), mf->stream));
+    ++mf->launches;
+    if (fused)
+    {
+        CU(launch_fix_rescan(mf->rho.as<float>(), mf->ldr, mf->nt, mf->pk_stride, mf->pk_dirty.as<unsigned char>(),
+                             mf->xb.empty() ? nullptr : mf->row_S.as<int>(),
+                             mf->xb.empty() ? nullptr : mf->row_nblk.as<int>(), mf->S, mf->nblocks,
+                             mf->nvalid_d.as<int>(), mf->pk_fused_len, (float) mf->pk_fused_thr,
+                             mf->pk_cnt.as<int>(), mf->pk_idx.as<int>(), mf->pk_val.as<float>(), mf->stream));
+        ++mf->launches;
+    }
+    return MFGPU_OK;
+}
+
 // the stream work of one apply (events, normalisation, correlators)
 static mfgpu_status mf_apply_body(mfgpu_mf *mf)
 {
@@ -1496,6 +1675,11 @@ static mfgpu_status mf_apply_body(mfgpu_mf *mf)
         CU(mf_record(mf, mf->ev[1]));
     }
     CU(mf_record(mf, mf->ev[2]));
+    if (mf->nblocks > 0 && mf->fx_on)
+    {
+        mfgpu_status st = mf_launch_fixup(mf);
+        if (st != MFGPU_OK) return st;
+    }
     CU(mf_record(mf, mf->ev[3]));
     CU(mf_record(mf, mf->x_ev));  // the last read of x by this apply
     return MFGPU_OK;
@@ -1662,6 +1846,28 @@ try
 {
     if (!mf || !count) return fail(MFGPU_EINVAL, "NULL argument");
     *count = mf->launches;
+    return MFGPU_OK;
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
+
+mfgpu_status mfgpu_mf_get_fixup_runs(mfgpu_mf *mf, long long *runs)
+try
+{
+    if (!mf || !runs) return fail(MFGPU_EINVAL, "NULL argument");
+    if (!mf->initialized) return fail(MFGPU_ESTATE, "Class is not initialized");
+    DeviceGuard g(mf->dev);
+    *runs = 0;
+    mfgpu_status st = mf_sync(mf);
+    if (st != MFGPU_OK) return st;
+    if (!mf->fx_on || !mf->have) return MFGPU_OK;
+    std::vector<unsigned char> h((size_t) mf->nch * mf->ldrs);
+    CU(cudaMemcpy(h.data(), mf->fxflags.p, h.size(), cudaMemcpyDeviceToHost));
+    long long k = 0;
+    for (unsigned char b : h) k += b != 0;
+    *runs = k;
     return MFGPU_OK;
 }
 catch (...)

@@ -1,0 +1,66 @@
+// fixup.cu -- launchers of the FP32 accuracy safeguards (kernels_fix.cuh).
+#include "launch.h"
+#include "kernels_fix.cuh"
+
+namespace mfgpu {
+
+cudaError_t launch_den_robust(const float *x, long ldx, int L, float *den, long ldd, float tol, float4 *rstat,
+                              long ldrs, float2 *cst, long ldc, int nblocks, int nch, cudaStream_t s)
+{
+    const size_t bytes = DenRobustLayout::bytes(L);
+    static SmemCap cap;
+    cudaError_t e = raise_smem_cap(den_robust_kernel, bytes, cap);
+    if (e != cudaSuccess) return e;
+    den_robust_kernel<<<dim3(nblocks, nch), kThreads, bytes, s>>>(x, ldx, L, den, ldd, tol, rstat, ldrs, cst, ldc);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fix_flag_fft(const float2 *cst, long ldc, long nchunks, int S, int N, int nblocks, int nch,
+                                const float4 *rstat, long ldrs, int nruns, const unsigned char *dead,
+                                unsigned char *flags, float coef2, cudaStream_t s)
+{
+    fix_flag_fft_kernel<<<dim3((nblocks + 7) / 8, nch), 256, 0, s>>>(cst, ldc, nchunks, S, N, nblocks, rstat, ldrs,
+                                                                      nruns, dead, flags, coef2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fix_flag_tc(const float *x, long ldx, int L, const float4 *rstat, long ldrs, int nruns, int tiles,
+                               int nch, const unsigned char *dead, const float *xrange, float *off,
+                               unsigned char *flags, float c1, float c2, float tau, cudaStream_t s)
+{
+    fix_flag_tc_kernel<<<dim3((tiles + 7) / 8, nch), 256, 0, s>>>(x, ldx, L, rstat, ldrs, nruns, tiles, dead, xrange,
+                                                                   off, flags, c1, c2, tau);
+    return cudaGetLastError();
+}
+
+size_t fixup_smem_bytes(int Lmax) { return sizeof(float) * (size_t) kFixWarps * (Lmax + 64); }
+
+cudaError_t launch_fix_prep(const double *tmpl, const long *toff, const int *tlen, const int *btid, const long *boff,
+                            const int *bL, int nbatch, float *bco, float *bsum, cudaStream_t s)
+{
+    fix_prep_kernel<<<nbatch * kFixBatch, 256, 0, s>>>(tmpl, toff, tlen, btid, boff, bL, bco, bsum);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fixup(const FixParams &p, int nctas, cudaStream_t s)
+{
+    const size_t bytes = fixup_smem_bytes(p.Lmax);
+    static SmemCap cap;
+    cudaError_t e = raise_smem_cap(fixup_kernel, bytes, cap);
+    if (e != cudaSuccess) return e;
+    fixup_kernel<<<nctas, 32 * kFixWarps, bytes, s>>>(p);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fix_rescan(const float *rho, long ldr, int nt, int pk_stride, const unsigned char *dirty,
+                              const int *row_S, const int *row_nblk, int S0, int nblk0, const int *nvalid, int pk_len,
+                              float thr, int *cnt, int *idx, float *val, cudaStream_t s)
+{
+    const long ns = (long) nt * pk_stride;
+    const long warps = (ns + 31) / 32;
+    fix_rescan_kernel<<<(unsigned) ((warps + 7) / 8), 256, 0, s>>>(rho, ldr, nt, pk_stride, dirty, row_S, row_nblk, S0,
+                                                                    nblk0, nvalid, pk_len, thr, cnt, idx, val);
+    return cudaGetLastError();
+}
+
+}  // namespace mfgpu

@@ -32,6 +32,15 @@ namespace mfgpu {
 
 constexpr int kThreads = 256;
 
+// power-of-two scale that maps |v| <= range onto |v * s| < 2^e
+__device__ __forceinline__ float tc_pow2_scale(float range, int e)
+{
+    if (!(range > 0.f) || !isfinite(range)) return 1.f;
+    int ex;
+    frexpf(range, &ex);  // range < 2^ex
+    return ldexpf(1.f, e - ex);
+}
+
 template <class T> struct XcorrParams
 {
     const T *x;               // channel signals, row stride ldx (zero padded tail)

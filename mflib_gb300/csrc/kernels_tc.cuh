@@ -16,8 +16,10 @@
 // the signal strip itself (leading-dimension offset 16 B, stride offset
 // 128 B), and B holds each template at its 8 phase shifts.  The numerator is
 // invariant to a constant added to the window (templates are zero-mean), so
-// each strip is offset by its first sample and scaled by a per-channel power
-// of two before the split; templates are scaled by a power of two too.
+// each strip is offset by the level of its quietest 32-lag run (chosen by
+// fix_flag_tc_kernel from the window statistics; the split's error is
+// relative to |x - offset|) and scaled by a per-channel power of two before
+// the split; templates are scaled by a power of two too.
 //
 // Persistent, warp-specialised CTA (one per SM):
 //   warp 0 lane 0   issues the MMAs (K/16 steps x 2) and the commits;
@@ -35,15 +37,6 @@
 #include "tc_params.h"
 
 namespace mfgpu {
-
-// power-of-two scale that maps |v| <= range onto |v * s| < 2^e
-__device__ __forceinline__ float tc_pow2_scale(float range, int e)
-{
-    if (!(range > 0.f) || !isfinite(range)) return 1.f;
-    int ex;
-    frexpf(range, &ex);  // range < 2^ex
-    return ldexpf(1.f, e - ex);
-}
 
 // shared-memory matrix descriptor: start address, leading and stride byte
 // offsets (16-byte units), descriptor version 1, no swizzle
@@ -232,7 +225,7 @@ static __global__ void __launch_bounds__(kTcThreads, 1) tc_xcorr_kernel(TcParams
     }
     else if (warp < 4)
     {
-        // ---- strips: x[k0, k0 + 1024 + Kp) -> (x - x[k0]) * s -> FP16 hi, lo
+        // ---- strips: x[k0, k0 + 1024 + Kp) -> (x - off) * s -> FP16 hi, lo
         const int ptid = tid - 32;
         bool ok = true;
         for (long w = w0, n = 0; w < w1; ++w, ++n)
@@ -247,7 +240,7 @@ static __global__ void __launch_bounds__(kTcThreads, 1) tc_xcorr_kernel(TcParams
             const int c = p.grp_chan[g];
             const float *xr = p.x + (long) c * p.ldx + (long) j * kTcLags;
             const float s = tc_pow2_scale(p.xrange[c], 13);
-            const float off = xr[0];
+            const float off = p.off[(long) c * p.tiles + j];
             __half *ah = sA + (size_t) (2 * buf) * SA, *al = ah + SA;
             constexpr int PR = 4;  // loads in flight per thread
             if (ok)

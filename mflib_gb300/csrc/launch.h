@@ -10,6 +10,7 @@
 #include "kernels_mf.cuh"
 #include "kernels_util.cuh"
 #include "tc_params.h"
+#include "fix_params.h"
 #include "mfgpu.h"
 
 namespace mfgpu {
@@ -42,6 +43,27 @@ size_t tc_smem_bytes(int Kp, int Gp);
 cudaError_t launch_tc_bank(const double *tmpl, const long *toff, const int *tlen, const int *grp_tid, int ngroups,
                            int Gp, int Kp, __half *B, float *bscale, cudaStream_t s);
 cudaError_t launch_tc_xcorr(const TcParams &p, int nctas, cudaStream_t s);
+// FP32 accuracy safeguards (kernels_fix.cuh): cancellation-free window
+// variances with per-run statistics (float4 per 32 lags, row stride ldrs;
+// den optional) and per-chunk statistics (float2 per 32 samples, row stride
+// ldc), the per-run error bounds of the FFT and tensor-core
+// correlators (flags: one byte per run, row stride ldrs), and the fix-up of
+// the flagged runs.
+cudaError_t launch_den_robust(const float *x, long ldx, int L, float *den, long ldd, float tol, float4 *rstat,
+                              long ldrs, float2 *cst, long ldc, int nblocks, int nch, cudaStream_t s);
+cudaError_t launch_fix_flag_fft(const float2 *cst, long ldc, long nchunks, int S, int N, int nblocks, int nch,
+                                const float4 *rstat, long ldrs, int nruns, const unsigned char *dead,
+                                unsigned char *flags, float coef2, cudaStream_t s);
+cudaError_t launch_fix_flag_tc(const float *x, long ldx, int L, const float4 *rstat, long ldrs, int nruns, int tiles,
+                               int nch, const unsigned char *dead, const float *xrange, float *off,
+                               unsigned char *flags, float c1, float c2, float tau, cudaStream_t s);
+size_t fixup_smem_bytes(int Lmax);
+cudaError_t launch_fix_prep(const double *tmpl, const long *toff, const int *tlen, const int *btid, const long *boff,
+                            const int *bL, int nbatch, float *bco, float *bsum, cudaStream_t s);
+cudaError_t launch_fixup(const FixParams &p, int nctas, cudaStream_t s);
+cudaError_t launch_fix_rescan(const float *rho, long ldr, int nt, int pk_stride, const unsigned char *dirty,
+                              const int *row_S, const int *row_nblk, int S0, int nblk0, const int *nvalid, int pk_len,
+                              float thr, int *cnt, int *idx, float *val, cudaStream_t s);
 // single-channel detector (kernels_detect.cuh): reduction across templates,
 // per-template transformed traces, per-detection refinement and amplitudes
 template <class T>

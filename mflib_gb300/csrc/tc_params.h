@@ -21,6 +21,7 @@ struct TcParams
     const int *grp_chan;       // channel of each group
     const int *grp_tid;        // [ngroups * Gp] template id or -1
     const float *xrange;       // per channel: max - min of the samples
+    const float *off;          // per (channel, tile): operand offset of the strip, row stride tiles
     const unsigned char *dead; // per channel dead-trace flag
     const float *den;          // per channel normalisation row, stride ldd
     long ldd;

@@ -533,6 +533,14 @@ class MatchedFilter:
         _lib.call("mfgpu_mf_get_launch_count", self._h, C.byref(v))
         return v.value
 
+    def get_fixup_runs(self):
+        """FP32: 32-lag runs the last apply recomputed by direct correlation
+        (the correlator's rounding-error bound exceeded 2e-5 of the run's
+        quietest window); waits for the apply."""
+        v = C.c_longlong()
+        _lib.call("mfgpu_mf_get_fixup_runs", self._h, C.byref(v))
+        return v.value
+
     def stream_handle(self):
         """The object's cudaStream_t as an integer (every launch and copy of
         the object is issued on it)."""
