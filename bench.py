@@ -1,22 +1,25 @@
-"""Benchmark: multi-channel FP32 matched filtering + peaks + DBSCAN association.
+"""Benchmark of the matched-filtering hot path on one GB300.
 
-Workload (one step): 24 channels (8 stations x 3 components) x 8,640,000
-float32 samples (24 h at 100 Hz) of 1-10 Hz band-passed N(0,1) noise; 8
-events x 24 per-channel templates of 500 samples (192 templates, 8 per
-channel); each event injected 50 times per channel at its station-shifted
-onsets with amplitude 0.5-2 x RMS.  A step computes every template's
-Pearson trace (192 x 8,639,501 template-lags), the peaks (rho >= 0.5,
-separation 250 samples) and a DBSCAN association of the detections' origin
-times per event (eps 50 samples, minPts 3).  Steps are software-pipelined:
-step i's association runs on the clustering object's stream while step
-i + 1's apply runs; K timed steps still contain K of everything.  Data are
+Default workload (the headline line): the uneven bank.  2,000 templates of
+200-3,000 samples (uniform) with random 1-15 Hz pass bands, each assigned
+to one of 96 channels of 8,640,000 float32 samples (24 h at 100 Hz) of
+1-10 Hz band-passed noise.  A step is one apply over the whole day (every
+template's Pearson trace, 1.728e10 template-lags; CUDA-graph replay, the
+planner's length buckets) plus the batched peak finder (rho > 0.7,
+separation 250) with candidates gathered inside the correlator.  Data are
 seeded synthetic seismograms (no dataset is used by the reference).
 
 Prints ONE JSON line (rank 0).  `value` is template-lag correlations/s with
-inputs resident in HBM; `e2e` is the same metric through the C-ABI with the
-channel samples copied from pinned host buffers and the detections copied
-back inside the timed region.  `--impl reference` times the reference's
-algorithm (the CPU restatement in oracle/) on the host cores instead.
+inputs resident in HBM; `e2e` is the same metric through the C ABI with
+every channel's samples copied from pinned host buffers (staged under the
+previous step) and the peaks copied back inside the timed region.  Extra
+keys hold the other workloads measured in the same run: the 24-channel
+day with peaks and DBSCAN association (`multichannel_day`), the
+precision-stress bank on the FFT and split-precision tensor-core paths
+(`precision_stress`) and the serving loop at one arrival rate
+(`serving`).  `--impl reference` times the reference's algorithm (the CPU
+restatement in oracle/) on the host cores instead.  Other modes:
+--day24, --stress, --serving, --detector.
 """
 import argparse
 import ctypes
@@ -51,6 +54,20 @@ def bandpass_noise(rng, n, lo, hi, fs=FS, order=4):
     return sosfilt(sos, rng.standard_normal(n)).astype(np.float32)
 
 
+def gen_channels(seeds, n, lo=1.0, hi=10.0):
+    """Band-passed N(0,1) noise, one float32 row per seed (threads: the
+    filter runs in compiled code)."""
+    from concurrent.futures import ThreadPoolExecutor
+    out = np.empty((len(seeds), n), dtype=np.float32)
+
+    def one(i):
+        out[i] = bandpass_noise(np.random.default_rng(seeds[i]), n, lo, hi)
+
+    with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 1)) as ex:
+        list(ex.map(one, range(len(seeds))))
+    return out
+
+
 def make_template(seed, length=TEMPLATE_LEN, lo=2.0, hi=8.0):
     from scipy.signal import butter, sosfilt
     from scipy.signal.windows import hann
@@ -64,9 +81,7 @@ def make_workload(n_samples=N_SAMPLES, n_stations=N_STATIONS, n_events=N_EVENTS,
     """Returns dict with channel signals [C, n] float32, templates (list of
     FP64 arrays), template channel/event/shift arrays and the truth."""
     nch = n_stations * N_COMP
-    sig = np.empty((nch, n_samples), dtype=np.float32)
-    for c in range(nch):
-        sig[c] = bandpass_noise(np.random.default_rng(seed + c), n_samples, 1.0, 10.0)
+    sig = gen_channels([seed + c for c in range(nch)], n_samples)
     rms = float(np.sqrt(np.mean(sig[:, : min(n_samples, 1_000_000)].astype(np.float64) ** 2)))
     rng = np.random.default_rng(1000 + seed)
     shifts = rng.integers(0, 301, (n_events, n_stations))
@@ -89,6 +104,29 @@ def make_workload(n_samples=N_SAMPLES, n_stations=N_STATIONS, n_events=N_EVENTS,
             sig[c, o + s: o + s + tp.size] += (a * tp).astype(np.float32)
     return dict(signals=sig, templates=templates, tchan=np.array(tchan), tevent=np.array(tevent),
                 tshift=np.array(tshift), origins=origins, n=n_samples, nch=nch)
+
+
+UNEVEN_NT, UNEVEN_NCH, UNEVEN_THR, UNEVEN_SEP = 2000, 96, 0.7, 250
+
+
+def make_uneven_workload(n_samples=N_SAMPLES, nt=UNEVEN_NT, nch=UNEVEN_NCH, rows=None):
+    """The uneven bank: nt templates of 200-3,000 samples (uniform) with
+    random 1-15 Hz pass bands (Hann-tapered band-passed noise), each on one
+    of nch channels (uniform), against nch channels of band-passed noise
+    (only the first `rows` channels' samples are generated when given)."""
+    from scipy.signal import butter, sosfilt
+    from scipy.signal.windows import hann
+    rng = np.random.default_rng(200)
+    lens = rng.integers(200, 3001, nt)
+    tps = []
+    for L in lens:
+        lo = rng.uniform(1.0, 7.0)
+        hi = rng.uniform(lo + 2.0, 15.0)
+        tps.append(sosfilt(butter(4, [lo, hi], btype="bandpass", fs=FS, output="sos"),
+                           rng.standard_normal(int(L))) * hann(int(L)))
+    chan = rng.integers(0, nch, nt)
+    sig = gen_channels([300 + c for c in range(nch if rows is None else rows)], n_samples)
+    return dict(signals=sig, templates=tps, tchan=np.array(chan), lens=lens, n=n_samples, nch=nch)
 
 
 # ---------------------------------------------------------------------------
@@ -186,9 +224,9 @@ def measured_peak(key="hbm_gbs"):
         return (6800.0 if key == "hbm_gbs" else 1900.0), "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per launch of the correlator from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "xcorr_fp32_24ch_8.64M_traffic.txt")
+def profile_traffic(name="xcorr_fp32_24ch_8.64M_traffic.txt"):
+    """DRAM bytes per launch of the correlator from a committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", name)
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_full_launch"):
@@ -220,30 +258,74 @@ def cpu_baseline(w, minutes=None, threads=None):
             "seconds": dt}
 
 
-def run_reference(args, w, rank):
+def cpu_baseline_uneven(w, channels=8, minutes=None, threads=None):
+    """The reference algorithm (oracle restatement, FP32) on a bounded sample
+    of the uneven bank: for each of the first `channels` channels, its
+    templates against its first `minutes` of samples in SINGLE_CHANNEL mode
+    (a MULTI_CHANNEL instance of the whole bank would hold one signal copy
+    per template, 3 x 2,000 x 8.64 M floats, beyond the host's memory)."""
+    from oracle.orc import Oracle
+    o = Oracle()
+    threads = threads or os.cpu_count() or 1
+    minutes = minutes if minutes is not None else float(os.environ.get("MFGPU_CPU_MINUTES", "180"))
+    # at least four times the longest template (the reference sizes its
+    # transforms from the signal length and rejects shorter signals)
+    n = min(max(int(minutes * 60 * FS), 4 * int(max(w["lens"]))), w["n"])
+    minutes = n / (60 * FS)
+    lags, dt, nt = 0, 0.0, 0
+    for c in range(channels):
+        tps = [w["templates"][t] for t in np.nonzero(w["tchan"] == c)[0]]
+        if not tps:
+            continue
+        x = w["signals"][c, :n]
+        t0 = time.perf_counter()
+        o.matched_filter(tps, [x], multi=False, dtype=np.float32, threads=threads)
+        dt += time.perf_counter() - t0
+        lags += sum(n - tp.size + 1 for tp in tps)
+        nt += len(tps)
+    return {"value": lags / dt, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": "channels 0-%d (%d templates of the bank) x first %.0f min, SINGLE_CHANNEL mode per channel "
+                      "(%d template-lags); reference overlap-add algorithm restated in C, FFT by the oracle's "
+                      "radix-2 transform" % (channels - 1, nt, minutes, lags),
+            "seconds": dt}
+
+
+def run_reference(args, rank):
+    """The reference arm: the reference's algorithm (the oracle's C
+    restatement) on the host cores, each step a bounded sample of the same
+    workload as the default line (or of the 24-channel day with --day24)."""
     if rank != 0:
         return
     cores = os.cpu_count() or 1
+    if args.day24:
+        w = make_workload(n_samples=min(args.samples, int(180 * 60 * FS)))
+        base = lambda quick: cpu_baseline(w, minutes=1.0 if quick else None, threads=cores)
+        workload = "24ch x 8.64M f32, 192 templates x 500, peaks 0.5/250, dbscan 50/3"
+    else:
+        w = make_uneven_workload(n_samples=min(args.samples, int(180 * 60 * FS)), rows=8)
+        base = lambda quick: cpu_baseline_uneven(w, channels=1 if quick else 8, minutes=10.0 if quick else None,
+                                                 threads=cores)
+        workload = ("uneven bank: 2,000 templates of 200-3,000 samples on 96 channels x %d samples, peaks %.1f/%d"
+                    % (args.samples, UNEVEN_THR, UNEVEN_SEP))
     for _ in range(args.warmup):
-        cpu_baseline(w, minutes=1.0, threads=cores)
+        base(True)
     vals = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        vals.append(cpu_baseline(w, threads=cores))
+        vals.append(base(False))
     el = time.perf_counter() - t0
     v = float(np.mean([x["value"] for x in vals]))
     line = {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "impl": "reference",
             "data": "synthetic seeded seismograms (band-passed noise + injected templates)",
-            "config": {"workload": "24ch x 8.64M f32, 192 templates x 500, peaks 0.5/250, dbscan 50/3",
-                       "sample_per_step": vals[0]["sample"]},
+            "config": {"workload": workload, "sample_per_step": vals[0]["sample"]},
             "cpu_baseline": {k: vals[0][k] for k in ("kind", "cores", "sample")} | {"value": v, "unit": METRIC},
             "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def run_serving(args):
+def run_serving(args, rates=None, requests=None):
     """Serving loop: Poisson arrivals of detection requests (windows of
     60-600 s on 1-64 channels with 0-5 injected events) against 4 resident
     banks of 100 / 500 / 2,000 / 5,000 templates of 200-3,000 samples, under a
@@ -300,9 +382,9 @@ def run_serving(args):
     while len(srv.served) < 4 * args.serving_slots:
         time.sleep(0.01)
 
-    rates = []
-    for k, lam in enumerate(args.rates):
-        reqs = make_requests(args.requests, 10 + k)
+    out_rates = []
+    for k, lam in enumerate(rates if rates is not None else args.rates):
+        reqs = make_requests(requests if requests is not None else args.requests, 10 + k)
         # rate 0: every request queued at once (saturation)
         arr = (np.cumsum(np.random.default_rng(500 + k).exponential(1.0 / lam, len(reqs))) if lam > 0
                else np.zeros(len(reqs)))
@@ -325,7 +407,7 @@ def run_serving(args):
             srv.run_one(r)
         el = time.perf_counter() - t1
         so = latency_stats(solo)
-        rates.append({"rate_req_s": lam if lam > 0 else "all at once", "requests": st["requests"], "p50_ms": 1e3 * st["p50_s"],
+        out_rates.append({"rate_req_s": lam if lam > 0 else "all at once", "requests": st["requests"], "p50_ms": 1e3 * st["p50_s"],
                       "p99_ms": 1e3 * st["p99_s"], "mean_ms": 1e3 * st["mean_s"], "throughput": st["throughput"],
                       "one_at_a_time": {"throughput": so["template_lags"] / el, "p50_ms": 1e3 * so["p50_s"],
                                         "p99_ms": 1e3 * so["p99_s"]}})
@@ -337,9 +419,9 @@ def run_serving(args):
                                    "100/500/2,000/5,000 templates of 200-3,000 samples, 120 GB budget",
                        "slots": args.serving_slots, "buckets": list(srv.buckets),
                        "threshold": args.serving_threshold, "min_distance": 250},
-            "rates": rates, "objects_created": srv.created, "evicted": srv.evicted,
+            "rates": out_rates, "objects_created": srv.created, "evicted": srv.evicted,
             "peak_device_bytes": srv.peak_held, "warm_s": warm_s}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def run_detector(args):
@@ -467,7 +549,7 @@ def run_stress(args):
         f.initialize(p, correlator_variant=variant)
         stream = torch.cuda.ExternalStream(f.stream_handle())
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        total_ms, worst_all, worst_flat = 0.0, 0.0, 0.0
+        total_ms, worst_all, worst_flat, fixups = 0.0, 0.0, 0.0, 0
         for c in range(nch):
             f.set_signal(chans[c])
             f.apply()  # warm
@@ -478,6 +560,7 @@ def run_stress(args):
             f.synchronize()
             torch.cuda.synchronize()
             total_ms += ev0.elapsed_time(ev1)
+            fixups += f.get_fixup_runs()
             lr = np.random.default_rng(7 + c)
             xs = chans[c].astype(np.float64)
             e = edges_all[c]
@@ -494,176 +577,158 @@ def run_stress(args):
         lags_total = float(nch) * nt * (n - L + 1)
         out[name] = {"template_lags_per_s": lags_total / (total_ms * 1e-3), "apply_ms_per_channel": total_ms / nch,
                      "max_abs_drho_all": worst_all, "max_abs_drho_away_from_envelope_steps": worst_flat,
+                     "fixup_runs": fixups, "runs": nch * ((n - L + 1 + 31) // 32),
                      "correlator": f.get_plan()["correlator"]}
         f.clear()
     line = {"metric": "precision stress: template-lag correlations/s and max |drho| vs FP64 oracle", "n_gpus": 1,
             "dtype": "f32", "config": {"workload": "512 templates x 1,000 against 16 channels x %d samples, all pairs,"
                                                    " DC 1e3..1e5, envelope 1e-3..1e3" % n},
-            "paths": out}
-    print(json.dumps(line), flush=True)
+            "paths": out, "tensor_over_fft": out["tensor"]["template_lags_per_s"] / out["fft"]["template_lags_per_s"]}
+    return line
 
 
-def run_uneven(args):
-    """The uneven bank: 2,000 templates of 200-3,000 samples (uniform) with
-    random 1-15 Hz pass bands, each on one of 96 channels (uniform), against
-    96 channels of band-passed noise (24 h at 100 Hz unless --samples).  A
-    step is apply (normalisation inside the correlator for every template's
-    own length) plus the batched peak finder with candidates gathered in
-    the correlator (rho > 0.7, separation 250), timed with CUDA events on
-    the library's stream."""
+class Ctx:
+    """Ranks of the job (torchrun: one per GPU) and the job-wide helpers."""
+
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.dist = None
+
+    def barrier(self):
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def max(self, v):
+        return max_over_ranks(v, self.dist, "cuda")
+
+
+def run_uneven_day(args, ctx):
+    """The headline: the uneven bank over a whole day.  A step is apply
+    (CUDA-graph replay after the first) plus the batched peak finder with
+    candidates gathered in the correlator (rho > 0.7, separation 250) and the
+    peaks copied to the host.  value: K steps with the channels resident,
+    CUDA events on the library's stream; e2e: the same K steps with every
+    step's channels staged from pinned host memory under the previous step."""
     import torch
     import mflib_gb300 as mf
-    from scipy.signal import butter, sosfilt
-    from scipy.signal.windows import hann
-    rng = np.random.default_rng(200)
-    nt, nch, n = 2000, 96, args.samples
-    lens = rng.integers(200, 3001, nt)
-    tps = []
-    for L in lens:
-        lo = rng.uniform(1.0, 7.0)
-        hi = rng.uniform(lo + 2.0, 15.0)
-        tps.append(sosfilt(butter(4, [lo, hi], btype="bandpass", fs=FS, output="sos"),
-                           rng.standard_normal(int(L))) * hann(int(L)))
-    chan = rng.integers(0, nch, nt)
-    sig = np.stack([bandpass_noise(np.random.default_rng(300 + c), n, 1.0, 10.0) for c in range(nch)])
+    w = make_uneven_workload(n_samples=args.samples)
+    n, nch, lens = w["n"], w["nch"], w["lens"]
+    nt = len(w["templates"])
     p = mf.MultiChannel.MatchedFilterParameters()
-    for tp in tps:
+    for tp in w["templates"]:
         wt = mf.WaveformTemplate()
         wt.set_signal(tp)
         wt.set_sampling_rate(FS)
         p.add_template(wt)
     p.set_signal_size(n)
     f = mf.MultiChannel.MatchedFilter(dtype=np.float32)
-    f.initialize(p, template_channels=[int(c) for c in chan], n_channels=nch,
+    f.initialize(p, template_channels=[int(c) for c in w["tchan"]], n_channels=nch,
                  correlator_variant=args.correlator_variant, length_buckets=args.length_buckets)
-    f.set_channel_signals(sig)
-    f.set_peak_threshold(0.7)
+    pinned = torch.empty((nch, n), dtype=torch.float32, pin_memory=True)
+    pinned.numpy()[:] = w["signals"]
+    host = pinned.numpy()
+    f.set_channel_signals(host)
+    f.set_peak_threshold(UNEVEN_THR)
     tune = None
     if args.autotune:
         # measured per-bucket plan choice (1-3 buckets, FFT length and
         # organisation per bucket) before anything is timed
         t0 = time.perf_counter()
-        res = f.autotune(sig, repeats=1, max_buckets=3)
+        res = f.autotune(w["signals"], repeats=1, max_buckets=3)
         ok = [t for t in res["trials"] if t["apply_ms"] is not None]
         tune = {"seconds": time.perf_counter() - t0, "trials": len(ok),
                 "model_apply_ms": ok[0]["apply_ms"], "tuned_apply_ms": res["apply_ms"],
                 "chosen": res["plan"]["bucket_plans"]}
+        f.set_channel_signals(host)
     f.set_graph(True)  # the day-long apply replayed as a CUDA graph after its first run
     lags = float(sum(n - int(L) + 1 for L in lens))
 
-    def step():
-        f.apply()
-        f.find_peaks(0.7, 250)
-        return f.get_all_peaks()
+    def run_steps(k, stage=False):
+        xms, out = [], None
+        if stage:
+            f.stage_channel_signals(host)
+        for i in range(k):
+            f.apply()
+            if stage and i + 1 < k:
+                f.stage_channel_signals(host)
+            f.find_peaks(UNEVEN_THR, UNEVEN_SEP)
+            out = f.get_all_peaks()
+            xms.append(f.last_timings()["xcorr_ms"])
+        return out, xms
 
-    for _ in range(args.warmup):
-        step()
+    run_steps(args.warmup)
     f.synchronize()
     stream = torch.cuda.ExternalStream(f.stream_handle())
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     launches0 = f.launch_count()
-    xms = []
+    clocks = ClockSampler(ctx.local)
+    clocks.start()
+    ctx.barrier()
+    torch.cuda.synchronize()
     ev0.record(stream)
-    for _ in range(args.steps):
-        counts, idx = step()
-        xms.append(f.last_timings()["xcorr_ms"])
+    (counts, idx), xms = run_steps(args.steps)
     ev1.record(stream)
     f.synchronize()
     torch.cuda.synchronize()
-    el = 1e-3 * ev0.elapsed_time(ev1)
+    ctx.barrier()
+    el = ctx.max(1e-3 * ev0.elapsed_time(ev1))
+    clk = clocks.stop()
+    launches = f.launch_count() - launches0
+
+    # end to end through the C ABI: every step's channels copied from pinned
+    # host memory (staged under the previous step), peaks copied back
+    ctx.barrier()
+    t0 = time.perf_counter()
+    (c2, i2), _ = run_steps(args.steps, stage=True)
+    e2e_el = ctx.max(time.perf_counter() - t0)
+    h2d = nch * n * 4
+    d2h = int(4 * (c2.size + i2.size))
+
     plan = f.get_plan()
     P = plan["fft_length"] // 2
     x_ms = float(np.mean(xms))
     alg = 4.0 * lags + 4.0 * nch * n + 8.0 * (P + 1) * nt
     peak, kind = measured_peak()
-    line = {"metric": METRIC, "value": lags / (el / args.steps), "unit": METRIC, "n_gpus": 1,
+    traffic = profile_traffic("xcorr_fp32_uneven_traffic.txt")
+    default = n == N_SAMPLES and args.correlator_variant == 0 and args.length_buckets == 0 and not args.autotune
+    roof = {"bound": "hbm", "achieved": alg / (x_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+            "frac": alg / (x_ms * 1e-3) / 1e9 / peak, "traffic": traffic if default else None,
+            "kernel": "xcorr_kernel<float,%d,per-template normalisation>" % P, "kernel_ms": x_ms,
+            "algorithmic_bytes": alg, "peak_source": kind}
+    line = {"metric": METRIC, "value": ctx.world * lags / (el / args.steps), "unit": METRIC, "n_gpus": ctx.world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
-            "higher_is_better": True, "dtype": "f32", "data": "synthetic band-passed noise, seeded templates",
-            "config": {"workload": "uneven bank: 2,000 templates of 200-3,000 samples on 96 channels x %d samples"
-                                   % n, "template_lags": lags, "fft_length": plan["fft_length"],
-                       "buckets": plan["buckets"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic seeded seismograms (band-passed noise, Hann-tapered band-passed templates)",
+            "config": {"workload": "uneven bank: 2,000 templates of 200-3,000 samples on 96 channels x %d samples, "
+                                   "peaks %.1f/%d" % (n, UNEVEN_THR, UNEVEN_SEP),
+                       "template_lags": lags, "fft_length": plan["fft_length"], "buckets": plan["buckets"],
                        "lags_per_block": plan["lags_per_block"], "correlator": plan["correlator"],
-                       "l2": "inputs and outputs exceed the 129 MB L2"},
-            "roofline": {"bound": "hbm", "kernel": "xcorr_kernel<float,%d,per-template normalisation>" % P,
-                         "kernel_ms": x_ms, "algorithmic_bytes": alg, "achieved": alg / (x_ms * 1e-3) / 1e9,
-                         "peak": peak, "unit": "GB/s", "frac": alg / (x_ms * 1e-3) / 1e9 / peak,
-                         "peak_source": kind},
-            "gpu_launches": int(f.launch_count() - launches0), "detections": int(idx.size),
+                       "graph": True,
+                       "l2": "inputs (%.2f GB) and outputs (%.0f GB) exceed the 129 MB L2; no flush needed"
+                             % (4e-9 * nch * n, 4e-9 * lags)},
+            "e2e": {"value": ctx.world * lags / (e2e_el / args.steps), "unit": METRIC, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_el / args.steps,
+                    "api": "stage_channel_signals (async H2D of step i+1 under step i), apply, find_peaks, "
+                           "get_all_peaks"},
+            "roofline": roof, "gpu_launches": int(launches), "clocks": clk, "detections": int(idx.size),
             "graph_replays": f.graph_launches()}
     if tune is not None:
         line["config"]["autotune"] = tune
-    print(json.dumps(line), flush=True)
+    f.clear()
+    return line, w
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--samples", type=int, default=N_SAMPLES, help="samples per channel (default 24 h)")
-    ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--correlator-variant", type=int, default=0,
-                    help="0 planner's choice, 1-3 FFT organisations, 4 tensor cores")
-    ap.add_argument("--template-length", type=int, default=TEMPLATE_LEN,
-                    help="samples per template (default %d)" % TEMPLATE_LEN)
-    ap.add_argument("--events", type=int, default=N_EVENTS,
-                    help="events, i.e. templates per channel (default %d)" % N_EVENTS)
-    ap.add_argument("--serving", action="store_true", help="run the request loop instead of the day-long step")
-    ap.add_argument("--autotune", action="store_true",
-                    help="with --uneven: measured per-bucket plan choice before timing")
-    ap.add_argument("--uneven", action="store_true",
-                    help="the 2,000-template uneven bank on 96 channels instead of the 24-channel day")
-    ap.add_argument("--detector", action="store_true", help="time the single-channel detector")
-    ap.add_argument("--stress", action="store_true", help="precision stress: FFT and tensor-core paths")
-    ap.add_argument("--length-buckets", type=int, default=0,
-                    help="length buckets of a mixed-length bank (0 planner's choice, 1 one plan)")
-    ap.add_argument("--rates", type=float, nargs="+", default=[50, 100, 200, 500, 0],
-                    help="Poisson arrival rates in requests/s (0: all requests queued at once)")
-    ap.add_argument("--requests", type=int, default=200, help="requests per arrival rate (serving)")
-    ap.add_argument("--serving-slots", type=int, default=4)
-    ap.add_argument("--serving-threshold", type=float, default=0.7)
-    args = ap.parse_args()
-    args.warmup = max(3, args.warmup)
-    if args.serving:
-        run_serving(args)
-        return
-    if args.uneven:
-        run_uneven(args)
-        return
-    if args.detector:
-        run_detector(args)
-        return
-    if args.stress:
-        run_stress(args)
-        return
-
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    dist = None
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-        if args.impl == "ours":
-            torch.cuda.set_device(local)
-        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
-
-    if args.impl == "reference":
-        if rank == 0:
-            w = make_workload(n_samples=min(args.samples, int(180 * 60 * FS)))
-            run_reference(args, w, rank)
-        if dist is not None:
-            dist.destroy_process_group()
-        return
-
+def run_day24(args, ctx, steps=None, warmup=None, cpu=True):
+    """The 24-channel day: apply + peaks + DBSCAN association per step
+    (software-pipelined: step i's association beside step i + 1's apply)."""
+    import torch
     import mflib_gb300 as mf
-    if world > 1:
-        import torch
-        torch.cuda.set_device(local)
-    # every rank runs the full workload on its own GPU (weak scaling)
-    w = make_workload(n_samples=args.samples, seed=10 + 97 * rank, n_events=args.events,
+    steps = steps or args.steps
+    warmup = warmup or args.warmup
+    samples = args.samples if args.day24 else N_SAMPLES
+    w = make_workload(n_samples=samples, seed=10 + 97 * ctx.rank, n_events=args.events,
                       template_length=args.template_length)
     f = build_filter(mf, w, correlator_variant=args.correlator_variant)
     # the correlator gathers the peak candidates as it stores the traces
@@ -675,7 +740,6 @@ def main():
     lags_per_step = sum(n - tp.size + 1 for tp in w["templates"])
 
     # pinned host copies of the channel samples for the end-to-end leg
-    import torch
     pinned = torch.empty((w["nch"], n), dtype=torch.float32, pin_memory=True)
     pinned.numpy()[:] = w["signals"]
     host = pinned.numpy()
@@ -696,7 +760,7 @@ def main():
         step i + 1's apply runs on the matched filter's stream; every step's
         association has finished when this returns.  stage: each step's
         channels are uploaded asynchronously under the previous step."""
-        pending, out, xms = None, None, []
+        pending, xms = None, []
         if stage:
             f.stage_channel_signals(host)
         for i in range(k):
@@ -704,19 +768,15 @@ def main():
             if stage and i + 1 < k:
                 f.stage_channel_signals(host)
             if pending is not None:
-                out = pending + tuple(associate(db, *pending, w))
+                associate(db, *pending, w)
             f.find_peaks(PEAK_THR, PEAK_SEP)
             pending = f.get_all_peaks()
             xms.append(f.last_timings()["xcorr_ms"])
         return pending + tuple(associate(db, *pending, w)), xms
 
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
     load_all()
-    for _ in range(args.warmup):
-        out = step()
+    for _ in range(warmup):
+        step()
     f.synchronize()
 
     # ---- device-resident timing (value): CUDA events on the library's
@@ -726,24 +786,23 @@ def main():
     stream = torch.cuda.ExternalStream(f.stream_handle())
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     launches0 = f.launch_count() + db.launch_count()
-    xcorr_ms = []
-    clocks = ClockSampler(local)
+    clocks = ClockSampler(ctx.local)
     clocks.start()
-    barrier()
+    ctx.barrier()
     torch.cuda.synchronize()
     f.synchronize()
     ev0.record(stream)
-    out, xcorr_ms = run_steps(args.steps)
+    out, xcorr_ms = run_steps(steps)
     ev1.record(stream)
     f.synchronize()
     torch.cuda.synchronize()
-    barrier()
+    ctx.barrier()
     el = 1e-3 * ev0.elapsed_time(ev1)
     clk = clocks.stop()
     launches = f.launch_count() + db.launch_count() - launches0
-    el = max_over_ranks(el, dist, "cuda")
+    el = ctx.max(el)
     counts, idx, labels, ncl = out
-    ms_step = 1e3 * el / args.steps
+    ms_step = 1e3 * el / steps
 
     # ---- end to end through the C ABI with host buffers.  Serial: copy all
     #      channels (one batched call, returns when copied), then the step.
@@ -751,24 +810,20 @@ def main():
     #      asynchronously while the previous step's correlation and peak
     #      finding run; every step still copies its 830 MB from pinned memory.
     def timed(fn):
-        barrier()
+        ctx.barrier()
         t0 = time.perf_counter()
         r = fn()
-        el = time.perf_counter() - t0
-        return max_over_ranks(el, dist, "cuda"), r
+        return ctx.max(time.perf_counter() - t0), r
 
     def serial():
         r = None
-        for _ in range(args.steps):
+        for _ in range(steps):
             load_all()
             r = step()
         return r
 
-    def pipelined():
-        return run_steps(args.steps, stage=True)[0]
-
     serial_el, _ = timed(serial)
-    e2e_el, (counts, idx, labels, ncl) = timed(pipelined)
+    e2e_el, (counts, idx, labels, ncl) = timed(lambda: run_steps(steps, stage=True)[0])
     last_pipelined = f.last_timings()  # correlator and apply of the last pipelined step
     h2d = w["nch"] * n * 4
     d2h = int(4 * (counts.size + idx.size + labels.size + ncl.size))
@@ -779,8 +834,8 @@ def main():
     P = plan["fft_length"] // 2
     if plan["correlator"] == 4:
         # tensor-core correlator: 2 L algorithmic flops per template-lag (one
-        # multiply-add per template sample; the hi/lo split executes 3 MMAs
-        # over the padded K, reported as executed_flops)
+        # multiply-add per template sample; the hi/lo split executes 3
+        # products over the padded K, reported as executed_flops)
         alg_flops = 2.0 * args.template_length * lags_per_step
         peak, peak_kind = measured_peak("bf16_tflops")
         achieved = alg_flops / (x_ms * 1e-3) / 1e12
@@ -798,10 +853,9 @@ def main():
                 "kernel": "xcorr_kernel<float,%d,shared_den>" % P,
                 "kernel_ms": x_ms, "algorithmic_bytes": alg_bytes, "peak_source": peak_kind}
 
-    value = world * lags_per_step / (el / args.steps)
-    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32",
+    line = {"metric": METRIC, "value": ctx.world * lags_per_step / (el / steps), "unit": METRIC,
+            "n_gpus": ctx.world, "steps": steps, "warmup": warmup, "ms_per_step": ms_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic seeded seismograms (band-passed noise + injected templates)",
             "config": {"workload": "%dch x %.2fM f32, %d templates x %d, peaks 0.5/250, dbscan 50/3"
                                    % (w["nch"], n / 1e6, nt, args.template_length),
@@ -811,10 +865,10 @@ def main():
                        "lags_per_block": plan["lags_per_block"],
                        "l2": "inputs (%.0f MB) and outputs (%.2f GB) exceed the 129 MB L2; no flush needed"
                              % (4e-6 * w["nch"] * n, 4e-9 * lags_per_step)},
-            "e2e": {"value": world * lags_per_step / (e2e_el / args.steps), "unit": METRIC,
+            "e2e": {"value": ctx.world * lags_per_step / (e2e_el / steps), "unit": METRIC,
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "ms_per_step": 1e3 * e2e_el / args.steps,
-                    "serial_value": world * lags_per_step / (serial_el / args.steps),
+                    "ms_per_step": 1e3 * e2e_el / steps,
+                    "serial_value": ctx.world * lags_per_step / (serial_el / steps),
                     "last_step_xcorr_ms": last_pipelined["xcorr_ms"], "last_step_apply_ms": last_pipelined["apply_ms"],
                     "api": "stage_channel_signals (async H2D of step i+1 under step i), apply, find_peaks, "
                            "get_all_peaks, DBSCAN association (step i's beside step i+1's apply); "
@@ -822,12 +876,106 @@ def main():
             "roofline": roof, "gpu_launches": int(launches), "clocks": clk,
             "detections": int(idx.size), "events_found": int(np.sum(ncl)),
             "events_injected": int(w["origins"].size)}
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if cpu and ctx.rank == 0 and ctx.world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(w).items() if k != "seconds"}
-    if rank == 0:
+    f.clear()
+    return line
+
+
+def _extra(fn):
+    """An extra workload of the default run; its failure is recorded, not raised."""
+    try:
+        return fn()
+    except Exception as e:  # noqa: BLE001 -- the headline line must still print
+        return {"error": "%s: %s" % (type(e).__name__, e)}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--samples", type=int, default=N_SAMPLES, help="samples per channel (default 24 h)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default run: skip the 24-channel day, precision stress and serving extras")
+    ap.add_argument("--day24", action="store_true",
+                    help="the 24-channel day (peaks + DBSCAN association) as the headline line")
+    ap.add_argument("--correlator-variant", type=int, default=0,
+                    help="0 planner's choice, 1-3 FFT organisations, 4 tensor cores")
+    ap.add_argument("--template-length", type=int, default=TEMPLATE_LEN,
+                    help="24-channel day: samples per template (default %d)" % TEMPLATE_LEN)
+    ap.add_argument("--events", type=int, default=N_EVENTS,
+                    help="24-channel day: events, i.e. templates per channel (default %d)" % N_EVENTS)
+    ap.add_argument("--serving", action="store_true", help="run the request loop instead of the day-long step")
+    ap.add_argument("--autotune", action="store_true",
+                    help="uneven bank: measured per-bucket plan choice before timing")
+    ap.add_argument("--uneven", action="store_true", help="the uneven bank alone (the default headline, no extras)")
+    ap.add_argument("--detector", action="store_true", help="time the single-channel detector")
+    ap.add_argument("--stress", action="store_true", help="precision stress: FFT and tensor-core paths")
+    ap.add_argument("--length-buckets", type=int, default=0,
+                    help="length buckets of a mixed-length bank (0 planner's choice, 1 one plan)")
+    ap.add_argument("--rates", type=float, nargs="+", default=[50, 100, 200, 500, 0],
+                    help="Poisson arrival rates in requests/s (0: all requests queued at once)")
+    ap.add_argument("--requests", type=int, default=200, help="requests per arrival rate (serving)")
+    ap.add_argument("--serving-slots", type=int, default=4)
+    ap.add_argument("--serving-threshold", type=float, default=0.7)
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.serving:
+        print(json.dumps(run_serving(args)), flush=True)
+        return
+    if args.detector:
+        run_detector(args)
+        return
+    if args.stress:
+        print(json.dumps(run_stress(args)), flush=True)
+        return
+
+    ctx = Ctx()
+    if ctx.world > 1:
+        import torch
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        if args.impl == "ours":
+            torch.cuda.set_device(ctx.local)
+        dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
+        ctx.dist = dist
+
+    if args.impl == "reference":
+        run_reference(args, ctx.rank)
+        if ctx.dist is not None:
+            ctx.dist.destroy_process_group()
+        return
+
+    import mflib_gb300  # noqa: F401
+    if ctx.world > 1:
+        import torch
+        torch.cuda.set_device(ctx.local)
+    if args.day24:
+        line = run_day24(args, ctx)
+    else:
+        # every rank runs the whole uneven day on its own GPU (weak scaling)
+        line, w = run_uneven_day(args, ctx)
+        if ctx.rank == 0 and ctx.world == 1 and not args.no_cpu_baseline:
+            # a short warm-up, then the mean of three timed samples (a single
+            # cold sample had read well below the reference arm's steady mean)
+            cpu_baseline_uneven(w, channels=1, minutes=10.0)
+            reps = [cpu_baseline_uneven(w) for _ in range(3)]
+            cb = {k: v for k, v in reps[0].items() if k != "seconds"}
+            cb["value"] = float(np.mean([r["value"] for r in reps]))
+            cb["repeats"] = 3
+            line["cpu_baseline"] = cb
+        del w
+        if ctx.rank == 0 and ctx.world == 1 and not args.no_extras and not args.uneven:
+            line["multichannel_day"] = _extra(lambda: run_day24(args, ctx, steps=20, warmup=3, cpu=False))
+            line["precision_stress"] = _extra(lambda: run_stress(args))
+            line["serving"] = _extra(lambda: run_serving(args, rates=[100], requests=100))
+    if ctx.rank == 0:
         print(json.dumps(line), flush=True)
-    if dist is not None:
-        dist.destroy_process_group()
+    if ctx.dist is not None:
+        ctx.dist.destroy_process_group()
 
 
 if __name__ == "__main__":

@@ -281,6 +281,13 @@ mfgpu_status mfgpu_mf_get_launch_count(const mfgpu_mf *mf, long long *count);
  * quietest window (windows or FFT blocks that straddle amplitude changes of
  * several decades); 0 for FP64 objects.  Waits for the apply. */
 mfgpu_status mfgpu_mf_get_fixup_runs(mfgpu_mf *mf, long long *runs);
+/* No reference counterpart; for tests of the bounded device waits.  The
+ * next apply's FFT correlator expects its segment copy without issuing it
+ * (no copy is in flight) and gives up after a short bounded wait: that apply
+ * fails with MFGPU_ETIMEOUT at the next synchronising call, which also clears
+ * the device status word, and later applies run normally.  The apply is not
+ * captured into a CUDA graph.  MFGPU_EINVAL for the tensor-core correlator. */
+mfgpu_status mfgpu_mf_test_wait_timeout(mfgpu_mf *mf);
 /* The object's CUDA stream (a cudaStream_t), on which every launch and
  * copy of the object is issued; for event timing by the caller. */
 mfgpu_status mfgpu_mf_get_stream(const mfgpu_mf *mf, void **stream);
@@ -379,10 +386,16 @@ mfgpu_status mfgpu_dbscan_segmented(mfgpu_dbscan *db, int n_segments, const int 
  * MFGPU_DBSCAN_NOALLOC_MAX_OBS observations and
  * MFGPU_DBSCAN_NOALLOC_MAX_SEGMENTS segments (about 1.4 MB, held on every
  * device that loads the library until the process exits); larger requests
- * fail with MFGPU_EINVAL.  The first call on each device looks up the
- * array's device address; make that first call before any stream capture.
- * All calls share the array: calls that overlap on the GPU race, so the
- * caller must serialise them. */
+ * fail with MFGPU_EINVAL.  Every call looks up the array's device address
+ * in the current context (no allocation); the first call in a context also
+ * loads the module that places the array, so make that first call before
+ * any stream capture.  All calls share the array: calls that overlap on the
+ * GPU race, so the caller must serialise them.
+ * Unchecked on the device (the call does not wait for the GPU): weights
+ * must be > 0 as the reference requires (src/dbscan.cpp:152-158), and
+ * malformed seg_offsets (first not 0, decreasing, last not n_obs) are
+ * clamped into a valid partition of [0, n_obs) instead of rejected.
+ * n_obs = 0 writes zero clusters for every segment. */
 #define MFGPU_DBSCAN_NOALLOC_MAX_OBS 65536
 #define MFGPU_DBSCAN_NOALLOC_MAX_SEGMENTS 4096
 mfgpu_status mfgpu_dbscan_segmented_noalloc(int n_segments, const int *seg_offsets, int n_obs, int n_features,

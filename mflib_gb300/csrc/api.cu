@@ -263,6 +263,7 @@ struct mfgpu_mf
     int pk_stride = 0;
     long long launches = 0;
     float last_xcorr_ms = 0, last_apply_ms = 0;
+    bool test_wait_timeout = false;  // mfgpu_mf_test_wait_timeout: the next apply only
 
     size_t esz() const { return (size_t) prec; }
     template <class F> void each_buf(F &&f)
@@ -1485,6 +1486,8 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
     p.err = mf->err.as<int>();
     p.den = mf->den.as<T>();
     p.ldd = mf->ldd;
+    p.test_skip_copy = mf->test_wait_timeout && !mf->tc ? 1 : 0;
+    mf->test_wait_timeout = false;
     if constexpr (sizeof(T) == 4)
     {
         if (mf->fx_on)
@@ -1695,7 +1698,7 @@ try
     if (rs != MFGPU_OK) return rs;
     mf->have = false;
     mf->have_peaks = false;
-    if (mf->use_graph)
+    if (mf->use_graph && !mf->test_wait_timeout)
     {
         mfgpu_mf::ApplyGraph key;
         key.x = mf->x.p;
@@ -1751,9 +1754,10 @@ try
             return MFGPU_OK;
         }
     }
+    const bool testing = mf->test_wait_timeout;
     mfgpu_status st = mf_apply_body(mf);
     if (st != MFGPU_OK) return st;
-    if (mf->use_graph)
+    if (mf->use_graph && !testing)
     {
         // the direct run may have resized buffers: the setup is taken after it
         mfgpu_mf::ApplyGraph &d = mf->last_direct[mf->direct_next];
@@ -1846,6 +1850,20 @@ try
 {
     if (!mf || !count) return fail(MFGPU_EINVAL, "NULL argument");
     *count = mf->launches;
+    return MFGPU_OK;
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
+
+mfgpu_status mfgpu_mf_test_wait_timeout(mfgpu_mf *mf)
+try
+{
+    if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");
+    if (!mf->initialized) return fail(MFGPU_ESTATE, "Class is not initialized");
+    if (mf->tc) return fail(MFGPU_EINVAL, "the wait test runs on the FFT correlator");
+    mf->test_wait_timeout = true;
     return MFGPU_OK;
 }
 catch (...)

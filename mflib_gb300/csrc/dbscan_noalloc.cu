@@ -15,7 +15,6 @@
 // must serialise them.  Every kernel writes each scratch word it later reads,
 // so no clearing between calls is needed.
 #include <cstdint>
-#include <mutex>
 #include <string>
 #include "mfgpu.h"
 #include "launch.h"
@@ -42,32 +41,24 @@ constexpr size_t kScratchBytes = kOffSegOff + align256(sizeof(int) * (kMaxSegmen
 
 __device__ __align__(256) unsigned char g_dbscan_scratch[kScratchBytes];
 
-std::mutex g_mutex;
-void *g_scratch_addr[64] = {};
-
-// Device address of the scratch array on the current device, looked up
-// once per device (the host-side symbol is not a device address).
+// Device address of the scratch array in the current context.  The host-side
+// symbol is not a device address; the address belongs to the context that
+// loaded the module, so it is looked up on every call (a lookup, no
+// allocation) rather than cached: a cached pointer would go stale after
+// cudaDeviceReset or under another context on the same device.  The first
+// lookup in a context loads the module, which places the array.
 cudaError_t scratch_address(void **out)
 {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-    std::lock_guard<std::mutex> lock(g_mutex);
-    if (!g_scratch_addr[dev])
-    {
-        void *p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_dbscan_scratch);
-        if (e != cudaSuccess) return e;
-        g_scratch_addr[dev] = p;
-    }
-    *out = g_scratch_addr[dev];
-    return cudaSuccess;
+    *out = nullptr;
+    return cudaGetSymbolAddress(out, g_dbscan_scratch);
 }
 
 // Copy of the caller's offsets forced into a valid partition of [0, n):
 // first 0, last n, non-decreasing and clamped to [0, n], so no later kernel
-// can index outside the caller's arrays whatever the offsets hold.
+// can index outside the caller's arrays whatever the offsets hold.  The
+// offsets live in device memory and the call does not wait for the GPU, so
+// malformed offsets are clamped rather than rejected (the allocating entry
+// point, which reads them on the host, rejects them).
 __global__ void sanitize_offsets_kernel(int n, int nseg, const int *seg_off, int *safe)
 {
     int prev = 0;
@@ -117,7 +108,7 @@ try
         return fail(MFGPU_EINVAL, "n_obs = " + std::to_string(n_obs) + " exceeds the fixed scratch capacity of " +
                                       std::to_string(kMaxPoints) + " observations");
     if (n_features < 1) return fail(MFGPU_EINVAL, "No features");
-    if (epsilon < 0) return fail(MFGPU_EINVAL, "epsilon must be non-negative");
+    if (!(epsilon >= 0)) return fail(MFGPU_EINVAL, "epsilon must be non-negative");
     if (min_observations < 1) return fail(MFGPU_EINVAL, "minObservations must be positive");
     if (!d_seg_offsets || !d_n_clusters || (n_obs > 0 && (!d_X || !d_labels)))
         return fail(MFGPU_EINVAL, "NULL argument");

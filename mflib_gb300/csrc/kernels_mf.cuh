@@ -74,6 +74,10 @@ template <class T> struct XcorrParams
     int *pk_cnt;
     int *pk_idx;
     T *pk_val;
+    // test of the bounded-wait error path: expect the segment copy's bytes
+    // without issuing the copy (nothing in flight) and give up after a short
+    // wait, reporting KERR_TMA_TIMEOUT
+    int test_skip_copy;
 };
 
 template <class T> struct SpecParams
@@ -615,9 +619,9 @@ template <> __device__ __forceinline__ void load_pair<double>(const cx<double> *
 
 // Bounded wait on a TMA phase; on timeout record the error and let every
 // thread return (the caller returns when this yields false).
-__device__ __forceinline__ bool xcorr_wait(uint64_t *bar, uint32_t parity, int *err)
+__device__ __forceinline__ bool xcorr_wait(uint64_t *bar, uint32_t parity, int *err, uint32_t limit = (1u << 24))
 {
-    bool ok = mbar_wait_bounded(bar, parity);
+    bool ok = mbar_wait_bounded(bar, parity, limit);
     if (!__syncthreads_and(ok))
     {
         if (threadIdx.x == 0) atomicExch(err, KERR_TMA_TIMEOUT);
@@ -696,9 +700,12 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
         fence_proxy_async_smem();
         const uint32_t den_bytes = SHARED_DEN ? (uint32_t) (sizeof(T) * S) : 0u;
         mbar_arrive_expect_tx(&bar[0], (uint32_t) LY::seg + kTwBytes + den_bytes);
-        tma_load_1d(xs, p.x + (long) c * p.ldx + k0, (uint32_t) LY::seg, &bar[0]);
-        tma_load_1d(tws, p.twt, kTwBytes, &bar[0]);
-        if (SHARED_DEN) tma_load_1d(invd_s, p.den + (long) c * p.ldd + k0, den_bytes, &bar[0]);
+        if (!p.test_skip_copy)
+        {
+            tma_load_1d(xs, p.x + (long) c * p.ldx + k0, (uint32_t) LY::seg, &bar[0]);
+            tma_load_1d(tws, p.twt, kTwBytes, &bar[0]);
+            if (SHARED_DEN) tma_load_1d(invd_s, p.den + (long) c * p.ldd + k0, den_bytes, &bar[0]);
+        }
         if (PREFETCH)
         {
             mbar_arrive_expect_tx(&bar[1], (uint32_t) LY::brow);
@@ -706,7 +713,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
         }
     }
     __syncthreads();
-    if (!xcorr_wait(&bar[0], 0, p.err))
+    if (!xcorr_wait(&bar[0], 0, p.err, p.test_skip_copy ? (1u << 12) : (1u << 24)))
     {
         if (PREFETCH) mbar_wait_bounded(&bar[1], 0);  // let the spectrum copy land before exiting
         return;

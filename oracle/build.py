@@ -16,7 +16,12 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_ROOT = os.environ.get("MFLIB_REFERENCE_ROOT", "/root/reference")
+# Where this recipe reads the reference checkout: $MFLIB_REFERENCE_ROOT when
+# set, else the development host's read-only checkout below.  Only this
+# recipe names it; on a host without the checkout build_ref() is skipped and
+# the tests that need the compiled reference skip with it.
+DEV_HOST_REFERENCE = "/root/reference"
+REF_ROOT = os.environ.get("MFLIB_REFERENCE_ROOT") or DEV_HOST_REFERENCE
 REF_SOURCES = [
     "src/matchedFilter.cpp",
     "src/matchedFilterParameters.cpp",

@@ -74,6 +74,9 @@ class Oracle:
         else:
             sg = [np.ascontiguousarray(s, dtype=np.float64) for s in signals]
         n = len(sg[0])
+        if any(len(x) != n for x in sg) or int(lens.max()) > n:
+            # MatchedFilter::initialize rejects signals shorter than a template
+            raise ValueError("signals must share one length of at least the longest template")
         tarr = _ptr_array(tp, C.c_double)
         if dtype == np.float32 and not fp64_from_f32:
             out = np.zeros((nt, n), dtype=np.float32)

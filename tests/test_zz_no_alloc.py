@@ -7,7 +7,10 @@ caller passes device buffers and a stream; the library's working memory is
 a fixed static device array.  This test drives it through the C ABI and
 checks it against the allocating entry point, mfgpu_dbscan_segmented, on
 two calls in a row (the second call reuses the array the first one left
-behind).  Labels are integers and must match exactly.
+behind).  Labels are integers and must match exactly.  Once the module is
+loaded, further calls leave the device's free memory unchanged; an empty
+problem and malformed (clamped) segment offsets stay inside the caller's
+buffers.
 """
 import ctypes
 
@@ -69,4 +72,56 @@ def test_noalloc_rejects_oversize(gpu):
     assert st == _lib.MFGPU_EINVAL
     assert "65536" in lib.mfgpu_last_error().decode()
     st = lib.mfgpu_dbscan_segmented_noalloc(4097, None, 10, 1, None, None, 1.0, 2, None, None, None)
+    assert st == _lib.MFGPU_EINVAL
+
+
+def test_noalloc_allocates_nothing(gpu):
+    """After a first call (which loads the module holding the scratch array),
+    repeated calls change neither the device's free memory nor anything the
+    caller did not pass."""
+    torch = pytest.importorskip("torch")
+    from mflib_gb300 import _lib
+    lib = _lib.lib()
+    rng = np.random.default_rng(11)
+    X, off = _case(rng, [400, 900], 1)
+    dev = torch.device("cuda", 0)
+    Xd = torch.tensor(X, device=dev)
+    so = torch.tensor(off, device=dev)
+    labels = torch.empty(X.shape[0], dtype=torch.int32, device=dev)
+    ncl = torch.empty(2, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def call():
+        st = lib.mfgpu_dbscan_segmented_noalloc(
+            2, ctypes.c_void_p(so.data_ptr()), X.shape[0], 1, ctypes.c_void_p(Xd.data_ptr()), None, 3.0, 3,
+            ctypes.c_void_p(labels.data_ptr()), ctypes.c_void_p(ncl.data_ptr()), ctypes.c_void_p(stream.cuda_stream))
+        _lib.check(st)
+        torch.cuda.synchronize(dev)
+
+    call()
+    free0, _ = torch.cuda.mem_get_info(dev)
+    for _ in range(5):
+        call()
+    free1, _ = torch.cuda.mem_get_info(dev)
+    assert free1 == free0
+
+
+def test_noalloc_empty_and_malformed_offsets(gpu):
+    from mflib_gb300 import _lib
+    lib = _lib.lib()
+    rng = np.random.default_rng(13)
+    # no observations: every segment gets zero clusters
+    labels, ncl = _noalloc(lib, np.zeros((0, 1)), np.array([0, 0, 0], np.int32), 1.0, 2)
+    np.testing.assert_array_equal(ncl, [0, 0])
+    # decreasing / out-of-range offsets are clamped: labels stay in range and
+    # the clusters of the clamped partition are counted
+    X, _ = _case(rng, [500], 1)
+    bad = np.array([5, 300, 100, 10_000], np.int32)   # first not 0, decreasing, last past n
+    labels, ncl = _noalloc(lib, X, bad, 2.0, 3)
+    assert labels.shape == (500,)
+    assert labels.min() >= -1
+    assert np.all(ncl >= 0) and int(ncl.sum()) <= 500
+    assert labels.max() < max(1, int(ncl.max()))
+    # NaN epsilon is rejected before any work is enqueued
+    st = lib.mfgpu_dbscan_segmented_noalloc(1, None, 10, 1, None, None, float("nan"), 2, None, None, None)
     assert st == _lib.MFGPU_EINVAL
