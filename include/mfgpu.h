@@ -90,7 +90,9 @@ typedef struct
        4 = split-precision (FP16 hi+lo) time-domain correlation on the tensor
        cores (FP32 data, templates of one length), 5 = two teams with the
        normalisation computed inside each CTA instead of by a separate
-       per-channel pass (templates of one length). */
+       per-channel pass (templates of one length), 6 = two 256-thread teams
+       in a 512-thread CTA, each normalising its own templates (FP32 data,
+       templates of several lengths). */
     int correlator_variant;
     /* Extension: templates of several lengths are split by length into at
        most this many buckets, each with its own FFT length and block length
@@ -103,8 +105,8 @@ typedef struct
        mfgpu_mf_get_buckets reports them); entries past the bucket count are
        ignored.  bucket_fft_lengths[b]: the bucket's FFT length (0 =
        automatic); bucket_variants[b]: its correlator organisation numbered
-       like correlator_variant (0 = automatic; 1 or 2 when the templates have
-       several lengths, 1, 2, 3 or 5 for one length).  Either array may be
+       like correlator_variant (0 = automatic; 1, 2 or (FP32) 6 when the
+       templates have several lengths, 1, 2, 3 or 5 for one length).  Either array may be
        NULL when n_bucket_plans is 0.  An override whose plan does not fit
        (block too short, shared memory, unsupported length) fails with
        MFGPU_EINVAL.  Any non-zero entry turns off the automatic choice of
@@ -186,7 +188,7 @@ mfgpu_status mfgpu_mf_get_device_signal(mfgpu_mf *mf, int it, const void **dptr,
 /* Overlap-save plan chosen at initialize. */
 mfgpu_status mfgpu_mf_get_plan(const mfgpu_mf *mf, int *fft_length, int *lags_per_block, int *n_blocks);
 /* Correlator organisation chosen at initialize, numbered like
- * correlator_variant (1-3 and 5 FFT organisations, 4 tensor cores); for the
+ * correlator_variant (1-3, 5 and 6 FFT organisations, 4 tensor cores); for the
  * tensor-core path also the templates per group and the padded K, else 0.
  * Extension: the reference has one CPU correlator and no such query. */
 mfgpu_status mfgpu_mf_get_correlator(const mfgpu_mf *mf, int *variant, int *tc_group, int *tc_k);

@@ -151,10 +151,10 @@ mfgpu_status mfgpu::status_of_exception() noexcept
 struct MfBucket
 {
     int log2p = 0, nfft = 0, S = 0, nblocks = 0, mode = 0, ngroups = 0, ntemplates = 0;
-    DevBuf Bc, tw, grp_chan, grp_tb, grp_te, tids;
+    DevBuf Bc, tw, tws, grp_chan, grp_tb, grp_te, tids;
     template <class F> void each_buf(F &&f)
     {
-        DevBuf *all[] = {&Bc, &tw, &grp_chan, &grp_tb, &grp_te, &tids};
+        DevBuf *all[] = {&Bc, &tw, &tws, &grp_chan, &grp_tb, &grp_te, &tids};
         for (DevBuf *d : all) f(*d);
     }
 };
@@ -217,7 +217,10 @@ struct mfgpu_mf
     bool fx_on = false;
     int fx_L = 0, fx_nden = 0, fx_nruns = 0, fx_nbatch = 0;
     long ldrs = 0, ldc = 0, fx_nchunks = 0;
-    DevBuf rstat, cst, fxflags, tc_off, fx_bch, fx_btid, fx_boff, fx_bL, fx_bco, fx_bsum, pk_dirty;
+    DevBuf rstat, cst, fxbits, fxlist, fxcount, tc_off, fx_btid, fx_boff, fx_bL, fx_bco, fx_bsum, pk_dirty,
+        fx_cb0, fx_cnb;
+    int fx_nbmax = 0;
+    DevBuf tws;  // pass twiddles in the split layout (correlator mode 4)
     // length buckets beside the primary plan (longest templates); per
     // template its bucket's block length and block count, and the slot row
     // stride of the gathered candidates (the largest block count)
@@ -272,8 +275,9 @@ struct mfgpu_mf
                          &nvalid_d, &dead,   &err,  &tmpl_d, &toff_d, &pmin, &pmax,  &chan_list, &stackbuf,
                          &shifts_d, &weights_d, &specbuf, &den, &pk_cnt, &pk_idx, &pk_val, &xstage,
                          &xrange,   &tc_B,   &tc_bscale, &tc_grp_chan, &tc_grp_tid, &pk_flags,
-                         &rstat,    &cst,    &fxflags, &tc_off, &fx_bch, &fx_btid, &fx_boff, &fx_bL,
-                         &fx_bco,   &fx_bsum, &pk_dirty};
+                         &rstat,    &cst,    &fxbits, &fxlist, &fxcount, &tc_off, &fx_btid, &fx_boff,
+                         &fx_bL,    &fx_cb0, &fx_cnb,
+                         &fx_bco,   &fx_bsum, &pk_dirty, &tws};
         for (DevBuf *d : all) f(*d);
         pk.each_buf(f);
         f(row_S);
@@ -450,12 +454,21 @@ catch (...)
 
 // twiddles and resident template spectra of one plan (every template's
 // spectrum at the plan's FFT length; the plan reads its bucket's rows)
-template <class T> static mfgpu_status mf_upload_tables(mfgpu_mf *mf, int log2p, DevBuf &twb, DevBuf &Bc)
+template <class T>
+static mfgpu_status mf_upload_tables(mfgpu_mf *mf, int log2p, DevBuf &twb, DevBuf &Bc, DevBuf *tws = nullptr)
 {
     std::vector<cx<T>> tw;
     twiddle_table<T>(log2p, tw);
     CU(twb.ensure(sizeof(cx<T>) * tw.size()));
     CU(cudaMemcpyAsync(twb.p, tw.data(), sizeof(cx<T>) * tw.size(), cudaMemcpyHostToDevice, mf->stream));
+    if (tws)
+    {
+        // mode 4 copies the pass twiddles in the split layout
+        std::vector<cx<T>> ts;
+        twiddle_split<T>(log2p, ts);
+        CU(tws->ensure(sizeof(cx<T>) * ts.size()));
+        CU(cudaMemcpyAsync(tws->p, ts.data(), sizeof(cx<T>) * ts.size(), cudaMemcpyHostToDevice, mf->stream));
+    }
     CU(Bc.ensure(sizeof(cx<T>) * (size_t) mf->nt * ((1L << log2p) + 2)));
     SpecParams<T> sp;
     sp.tmpl = mf->tmpl_d.as<double>();
@@ -559,14 +572,17 @@ try
     mf->shared_den = all_equal;
     // mode 3 normalises inside the CTA: no per-channel rows
     auto smem_of = [&](int l2p, int mode, int S) {
-        const bool sd = all_equal && mode != 3;
+        const bool sd = all_equal && mode != 3 && mode != 4;
         return mf->prec == 4 ? xcorr_smem_bytes<float>(l2p, sd, mode, S)
                              : xcorr_smem_bytes<double>(l2p, sd, mode, S);
     };
     // correlator_variant: 1..3 -> modes 0..2, 5 -> mode 3, 4 tensor cores
     const int v = p->correlator_variant;
-    const int forced_mode = v >= 1 && v <= 3 ? v - 1 : v == 5 ? 3 : -1;
-    if (v < 0 || v > 5) return fail(MFGPU_EINVAL, "correlator_variant must be 0..5");
+    const int forced_mode = v >= 1 && v <= 3 ? v - 1 : v == 5 ? 3 : v == 6 ? 4 : -1;
+    if (v < 0 || v > 6) return fail(MFGPU_EINVAL, "correlator_variant must be 0..6");
+    if (v == 6 && (mf->prec != 4 || all_equal))
+        return fail(MFGPU_EINVAL, "correlator_variant 6 (two 256-thread teams) needs FP32 data and templates of "
+                                  "several lengths");
     if ((forced_mode == 2 || forced_mode == 3) && !all_equal)
         return fail(MFGPU_EINVAL, "correlator_variant " + std::to_string(v) + " (teams) needs templates of one length");
     mf->tc = p->correlator_variant == 4;
@@ -582,7 +598,8 @@ try
         if (F < 0 || (F > 0 && (F & (F - 1)) != 0))
             return fail(MFGPU_EINVAL, "bucket_fft_lengths[" + std::to_string(b) + "] = " + std::to_string(F) +
                                           " is not 0 or a power of two");
-        if (!(bv == 0 || bv == 1 || bv == 2 || ((bv == 3 || bv == 5) && all_equal)))
+        if (!(bv == 0 || bv == 1 || bv == 2 || ((bv == 3 || bv == 5) && all_equal) ||
+              (bv == 6 && !all_equal && mf->prec == 4)))
             return fail(MFGPU_EINVAL, "bucket_variants[" + std::to_string(b) + "] = " + std::to_string(bv) +
                                           (all_equal ? " must be 0, 1, 2, 3 or 5" : " must be 0, 1 or 2 (several template lengths)"));
         bucket_forced = bucket_forced || F > 0 || bv > 0;
@@ -592,7 +609,7 @@ try
     };
     auto bucket_mode = [&](int b) {
         const int bv = b < p->n_bucket_plans && p->bucket_variants ? p->bucket_variants[b] : 0;
-        return bv == 0 ? -1 : bv == 5 ? 3 : bv - 1;
+        return bv == 0 ? -1 : bv == 5 ? 3 : bv == 6 ? 4 : bv - 1;
     };
     const bool tc_candidate =
         mf->tc || (p->correlator_variant == 0 && mf->prec == 4 && all_equal && p->fft_length == 0 && !bucket_forced);
@@ -642,10 +659,23 @@ try
                     int occ2 = (int) b2 <= dev_smem ? occupancy(l2p, b2) : 0;
                     if (occ2 >= std::max(occ0, occ1) && occ2 > 0) mode = 2;
                 }
+                // several lengths at N = 8192 (FP32): two 256-thread teams
+                // when the block's two normalisation rows fit (measured 12 %
+                // faster than the whole-CTA organisation on the 2,000-template
+                // bank)
+                if (!eq && mf->prec == 4 && l2p == 12 && (int) smem_of(l2p, 4, S) <= dev_smem) mode = 4;
+            }
+            if (mode == 4)
+            {
+                // two normalisation rows: the block may have to be shorter
+                // than the longest that the FFT length allows
+                if (l2p < 11) continue;
+                while (S > 32 && (int) smem_of(l2p, 4, S) > dev_smem) S -= 32;
             }
             size_t bytes = smem_of(l2p, mode, S);
             if ((int) bytes > dev_smem) continue;
-            int occ = occupancy(l2p, bytes);
+            // a 512-thread mode-4 CTA holds as many warps as two others
+            int occ = mode == 4 ? 2 : occupancy(l2p, bytes);
             if (occ < 1) continue;
             // seconds per (template, block), measured on GB300.  One template
             // length (normalisation rows precomputed): 8.4 ns at P = 2048 (N =
@@ -664,6 +694,7 @@ try
             {
                 base = 18.8e-9;
                 rel = l2p == 12 ? 1.87 : std::ldexp(1.0, l2p - 11) * (l2p + 1) / 12.0;
+                if (mode == 4) rel *= 0.88;
             }
             const double nb = std::ceil((double) std::max(1, mv) / S);
             const double cost = nb * rel * base;
@@ -683,7 +714,7 @@ try
     std::vector<int> cuts{0, nt};
     const int maxb = p->length_buckets > 0 ? p->length_buckets : 3;
     if (p->length_buckets < 0) return fail(MFGPU_EINVAL, "length_buckets must be >= 0");
-    if (!all_equal && p->fft_length == 0 && forced_mode <= 1 && maxb > 1)
+    if (!all_equal && p->fft_length == 0 && (forced_mode <= 1 || forced_mode == 4) && maxb > 1)
     {
         std::vector<int> pos{0};
         for (int q = 1; q < 64; ++q)
@@ -950,13 +981,14 @@ try
     CU(cudaMemcpyAsync(mf->tchan_d.p, mf->tchan.data(), sizeof(int) * nt, cudaMemcpyHostToDevice, mf->stream));
     CU(mf->xrange.ensure(sizeof(float) * nch));
     CU(cudaMemsetAsync(mf->xrange.p, 0, sizeof(float) * nch, mf->stream));
-    mfgpu_status s2 = mf->prec == 4 ? mf_upload_tables<float>(mf, mf->log2p, mf->tw, mf->Bc)
+    mfgpu_status s2 = mf->prec == 4 ? mf_upload_tables<float>(mf, mf->log2p, mf->tw, mf->Bc,
+                                                              mf->mode_x == 4 ? &mf->tws : nullptr)
                                     : mf_upload_tables<double>(mf, mf->log2p, mf->tw, mf->Bc);
     if (s2 != MFGPU_OK) return s2;
     for (size_t b = 0; b < mf->xb.size(); ++b)
     {
         MfBucket &xb = *mf->xb[b];
-        s2 = mf->prec == 4 ? mf_upload_tables<float>(mf, xb.log2p, xb.tw, xb.Bc)
+        s2 = mf->prec == 4 ? mf_upload_tables<float>(mf, xb.log2p, xb.tw, xb.Bc, xb.mode == 4 ? &xb.tws : nullptr)
                            : mf_upload_tables<double>(mf, xb.log2p, xb.tw, xb.Bc);
         if (s2 != MFGPU_OK) return s2;
         const Groups &gr = gx[b];
@@ -1012,17 +1044,20 @@ try
     {
         // fix-up batches: each channel's templates sorted by length, kFixBatch
         // per batch, coefficients interleaved [i][kFixBatch]
-        std::vector<int> bch, btid, bL;
+        std::vector<int> btid, bL, cb0(nch), cnb(nch);
         std::vector<long> boff;
         long tot_co = 0;
+        mf->fx_nbmax = 0;
         for (int c = 0; c < nch; ++c)
         {
+            cb0[c] = (int) bL.size();
+            cnb[c] = (int) ((chan_t[c].size() + kFixBatch - 1) / kFixBatch);
+            mf->fx_nbmax = std::max(mf->fx_nbmax, cnb[c]);
             std::vector<int> ts = chan_t[c];
             std::stable_sort(ts.begin(), ts.end(), [&](int a, int b) { return mf->lens[a] < mf->lens[b]; });
             for (size_t i = 0; i < ts.size(); i += kFixBatch)
             {
                 int lb = 0;
-                bch.push_back(c);
                 for (int k = 0; k < kFixBatch; ++k)
                 {
                     const int t = i + k < ts.size() ? ts[i + k] : -1;
@@ -1034,18 +1069,23 @@ try
                 tot_co += (long) kFixBatch * lb;
             }
         }
-        mf->fx_nbatch = (int) bch.size();
+        mf->fx_nbatch = (int) bL.size();
         CU(mf->rstat.ensure(sizeof(float4) * (size_t) nch * mf->ldrs));
         CU(mf->cst.ensure(sizeof(float2) * (size_t) nch * mf->ldc));
-        CU(mf->fxflags.ensure((size_t) nch * mf->ldrs));
+        CU(mf->fxbits.ensure(sizeof(unsigned) * (size_t) nch * (mf->ldrs / 32)));
+        CU(mf->fxlist.ensure(sizeof(int) * (size_t) nch * mf->ldrs));
+        CU(mf->fxcount.ensure(sizeof(int)));
+        CU(cudaMemsetAsync(mf->fxcount.p, 0, sizeof(int), mf->stream));
         if (mf->tc) CU(mf->tc_off.ensure(sizeof(float) * (size_t) nch * mf->tc_tiles));
-        CU(mf->fx_bch.ensure(sizeof(int) * bch.size()));
         CU(mf->fx_btid.ensure(sizeof(int) * btid.size()));
         CU(mf->fx_boff.ensure(sizeof(long) * boff.size()));
         CU(mf->fx_bL.ensure(sizeof(int) * bL.size()));
         CU(mf->fx_bco.ensure(sizeof(float) * (size_t) std::max<long>(1, tot_co)));
         CU(mf->fx_bsum.ensure(sizeof(float) * nt));
-        CU(cudaMemcpyAsync(mf->fx_bch.p, bch.data(), sizeof(int) * bch.size(), cudaMemcpyHostToDevice, mf->stream));
+        CU(mf->fx_cb0.ensure(sizeof(int) * nch));
+        CU(mf->fx_cnb.ensure(sizeof(int) * nch));
+        CU(cudaMemcpyAsync(mf->fx_cb0.p, cb0.data(), sizeof(int) * nch, cudaMemcpyHostToDevice, mf->stream));
+        CU(cudaMemcpyAsync(mf->fx_cnb.p, cnb.data(), sizeof(int) * nch, cudaMemcpyHostToDevice, mf->stream));
         CU(cudaMemcpyAsync(mf->fx_btid.p, btid.data(), sizeof(int) * btid.size(), cudaMemcpyHostToDevice, mf->stream));
         CU(cudaMemcpyAsync(mf->fx_boff.p, boff.data(), sizeof(long) * boff.size(), cudaMemcpyHostToDevice, mf->stream));
         CU(cudaMemcpyAsync(mf->fx_bL.p, bL.data(), sizeof(int) * bL.size(), cudaMemcpyHostToDevice, mf->stream));
@@ -1143,7 +1183,7 @@ mfgpu_status mfgpu_mf_get_correlator(const mfgpu_mf *mf, int *variant, int *tc_g
 try
 {
     MF_CHECK_INIT(mf);
-    if (variant) *variant = mf->tc ? 4 : mf->mode_x == 3 ? 5 : mf->mode_x + 1;
+    if (variant) *variant = mf->tc ? 4 : mf->mode_x == 3 ? 5 : mf->mode_x == 4 ? 6 : mf->mode_x + 1;
     if (tc_group) *tc_group = mf->tc ? mf->tc_Gp : 0;
     if (tc_k) *tc_k = mf->tc ? mf->tc_Kp : 0;
     return MFGPU_OK;
@@ -1178,7 +1218,7 @@ try
     MF_CHECK_INIT(mf);
     const int nb = (int) mf->xb.size() + 1;
     if (count) *count = nb;
-    auto variant_of = [](int mode) { return mode == 3 ? 5 : mode + 1; };
+    auto variant_of = [](int mode) { return mode == 3 ? 5 : mode == 4 ? 6 : mode + 1; };
     for (int b = 0; b < nb && b < max; ++b)
     {
         const bool prim = b == nb - 1;
@@ -1481,6 +1521,7 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
     p.tlen = mf->tlen_d.as<int>(); p.nvalid = mf->nvalid_d.as<int>();
     p.dead = mf->dead.as<unsigned char>();
     p.twt = mf->tw.as<cx<T>>();
+    p.twt_split = mf->tws.as<cx<T>>();
     p.S = mf->S;
     p.tol = sizeof(T) == 4 ? (T) 1.e-6 : (T) 1.e-12;  // src/matchedFilter.cpp:1287 / :1115
     p.err = mf->err.as<int>();
@@ -1497,14 +1538,16 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
             CU(launch_den_robust(mf->x.as<float>(), mf->ldx, mf->fx_L, mf->shared_den ? mf->den.as<float>() : nullptr,
                                  mf->ldd, (float) p.tol, mf->rstat.as<float4>(), mf->ldrs, mf->cst.as<float2>(),
                                  mf->ldc, mf->fx_nden, mf->nch, mf->stream));
-            CU(cudaMemsetAsync(mf->fxflags.p, 0, (size_t) mf->nch * mf->ldrs, mf->stream));
+            CU(cudaMemsetAsync(mf->fxbits.p, 0, sizeof(unsigned) * (size_t) mf->nch * (mf->ldrs / 32), mf->stream));
+            CU(cudaMemsetAsync(mf->fxcount.p, 0, sizeof(int), mf->stream));
             ++mf->launches;
             if (mf->tc)
             {
                 CU(launch_fix_flag_tc(mf->x.as<float>(), mf->ldx, mf->maxLen, mf->rstat.as<float4>(), mf->ldrs,
                                       mf->fx_nruns, mf->tc_tiles, mf->nch, mf->dead.as<unsigned char>(),
                                       mf->xrange.as<float>(), mf->tc_off.as<float>(),
-                                      mf->fxflags.as<unsigned char>(), kFixTcC1, kFixTcC2, kFixTol, mf->stream));
+                                      mf->fxbits.as<unsigned>(), mf->fxlist.as<int>(), mf->fxcount.as<int>(), kFixTcC1,
+                                      kFixTcC2, kFixTol, mf->stream));
                 ++mf->launches;
             }
             else
@@ -1512,7 +1555,8 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
                 const float coef = kFixFftK * 0x1p-24f / kFixTol;
                 CU(launch_fix_flag_fft(mf->cst.as<float2>(), mf->ldc, mf->fx_nchunks, mf->S, mf->nfft, mf->nblocks,
                                        mf->nch, mf->rstat.as<float4>(), mf->ldrs, mf->fx_nruns,
-                                       mf->dead.as<unsigned char>(), mf->fxflags.as<unsigned char>(), coef * coef,
+                                       mf->dead.as<unsigned char>(), mf->fxbits.as<unsigned>(), mf->fxlist.as<int>(),
+                                       mf->fxcount.as<int>(), coef * coef,
                                        mf->stream));
                 ++mf->launches;
                 for (auto &xb : mf->xb)
@@ -1520,7 +1564,8 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
                     if (xb->ngroups == 0) continue;
                     CU(launch_fix_flag_fft(mf->cst.as<float2>(), mf->ldc, mf->fx_nchunks, xb->S, xb->nfft, xb->nblocks,
                                            mf->nch, mf->rstat.as<float4>(), mf->ldrs, mf->fx_nruns,
-                                           mf->dead.as<unsigned char>(), mf->fxflags.as<unsigned char>(),
+                                           mf->dead.as<unsigned char>(), mf->fxbits.as<unsigned>(),
+                                           mf->fxlist.as<int>(), mf->fxcount.as<int>(),
                                            coef * coef, mf->stream));
                     ++mf->launches;
                 }
@@ -1601,6 +1646,7 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
         q.grp_chan = xb->grp_chan.as<int>(); q.grp_tb = xb->grp_tb.as<int>(); q.grp_te = xb->grp_te.as<int>();
         q.tids = xb->tids.as<int>();
         q.twt = xb->tw.as<cx<T>>();
+        q.twt_split = xb->tws.as<cx<T>>();
         q.S = xb->S;
         CU(launch_xcorr<T>(xb->log2p, false, xb->mode, q, xb->nblocks, xb->ngroups, mf->stream));
         ++mf->launches;
@@ -1623,10 +1669,10 @@ static mfgpu_status mf_launch_fixup(mfgpu_mf *mf)
     FixParams f{};
     f.x = mf->x.as<float>(); f.ldx = mf->ldx;
     f.rho = mf->rho.as<float>(); f.ldr = mf->ldr;
-    f.flags = mf->fxflags.as<unsigned char>(); f.ldf = mf->ldrs;
-    f.nruns = mf->fx_nruns; f.nspans = (mf->fx_nruns + 31) / 32;
-    f.nbatch = mf->fx_nbatch;
-    f.bch = mf->fx_bch.as<int>(); f.btid = mf->fx_btid.as<int>(); f.boff = mf->fx_boff.as<long>();
+    f.flist = mf->fxlist.as<int>(); f.fcount = mf->fxcount.as<int>(); f.ldf = mf->ldrs;
+    f.nruns = mf->fx_nruns; f.nbmax = mf->fx_nbmax;
+    f.chan_b0 = mf->fx_cb0.as<int>(); f.chan_nb = mf->fx_cnb.as<int>();
+    f.btid = mf->fx_btid.as<int>(); f.boff = mf->fx_boff.as<long>();
     f.bL = mf->fx_bL.as<int>(); f.bco = mf->fx_bco.as<float>(); f.bsum = mf->fx_bsum.as<float>();
     f.tlen = mf->tlen_d.as<int>(); f.nvalid = mf->nvalid_d.as<int>();
     f.tol = 1.e-6f;  // src/matchedFilter.cpp:1287
@@ -1881,10 +1927,8 @@ try
     mfgpu_status st = mf_sync(mf);
     if (st != MFGPU_OK) return st;
     if (!mf->fx_on || !mf->have) return MFGPU_OK;
-    std::vector<unsigned char> h((size_t) mf->nch * mf->ldrs);
-    CU(cudaMemcpy(h.data(), mf->fxflags.p, h.size(), cudaMemcpyDeviceToHost));
-    long long k = 0;
-    for (unsigned char b : h) k += b != 0;
+    int k = 0;
+    CU(cudaMemcpy(&k, mf->fxcount.p, sizeof(int), cudaMemcpyDeviceToHost));
     *runs = k;
     return MFGPU_OK;
 }

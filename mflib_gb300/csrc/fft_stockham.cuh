@@ -48,6 +48,24 @@ template <int LOG2P> struct FftPlan
     static constexpr int post_off() { return tw_off(npass()); }
     // padded to a multiple of 4 entries (16-byte multiple for TMA copies)
     static constexpr int tw_total() { return (post_off() + P / 2 + 1 + 3) & ~3; }
+    // Split layout (pass twiddles only): a pass with NS <= 16 keeps its
+    // (R-1) NS entries; a pass with NS > 16 stores, for k = 16 a + b,
+    // A[r-1][a] = exp(-2 pi i r a / (R NS / 16)) ((R-1) NS/16 entries) and
+    // Bt[r-1][b] = exp(-2 pi i r b / (R NS)) ((R-1) 16 entries); the twiddle
+    // is A[r-1][a] Bt[r-1][b].  At P = 4096 that is 720 entries instead of
+    // 4080, for a CTA whose shared memory cannot hold the full table.
+    static constexpr int tws_size(int pass)
+    {
+        return ((1 << radix_log(pass)) - 1) * ((1 << ns_log(pass)) <= 16 ? (1 << ns_log(pass))
+                                                                            : (1 << ns_log(pass)) / 16 + 16);
+    }
+    static constexpr int tws_off(int pass)
+    {
+        int off = 0;
+        for (int p = 1; p < pass; ++p) off += tws_size(p);
+        return off;
+    }
+    static constexpr int tws_total() { return (tws_off(npass()) + 1) & ~1; }  // 16-byte multiple
 };
 
 // Host-side construction of the same table (double precision, rounded once).
@@ -75,6 +93,42 @@ template <int LOG2P, class T> void build_twiddle_table_fixed(std::vector<cx<T>> 
     }
 }
 
+// The split layout of FftPlan::tws_off (double precision, each factor rounded once).
+template <int LOG2P, class T> void build_twiddle_split_fixed(std::vector<cx<T>> &out)
+{
+    using PL = FftPlan<LOG2P>;
+    const double two_pi = 6.283185307179586476925286766559;
+    out.assign(PL::tws_total(), cx<T>{(T) 0, (T) 0});
+    auto ph = [&](long long num, long long den) {
+        const double a = -two_pi * (double) (num % den) / (double) den;
+        return cx<T>{(T) std::cos(a), (T) std::sin(a)};
+    };
+    for (int p = 1; p < PL::npass(); ++p)
+    {
+        const int R = 1 << PL::radix_log(p), NS = 1 << PL::ns_log(p), o = PL::tws_off(p);
+        for (int r = 1; r < R; ++r)
+        {
+            if (NS <= 16)
+            {
+                for (int k = 0; k < NS; ++k) out[o + (r - 1) * NS + k] = ph((long long) r * k, (long long) NS * R);
+            }
+            else
+            {
+                const int NA = NS / 16;
+                for (int a = 0; a < NA; ++a) out[o + (r - 1) * NA + a] = ph((long long) r * a, (long long) NA * R);
+                for (int b = 0; b < 16; ++b)
+                    out[o + (R - 1) * NA + (r - 1) * 16 + b] = ph((long long) r * b, (long long) NS * R);
+            }
+        }
+    }
+}
+
+template <class T, int LO = 1, int HI = 13> void build_twiddle_split(int log2p, std::vector<cx<T>> &out)
+{
+    if (log2p == LO) build_twiddle_split_fixed<LO, T>(out);
+    else if constexpr (LO < HI) build_twiddle_split<T, LO + 1, HI>(log2p, out);
+}
+
 template <class T, int LO = 1, int HI = 13> void build_twiddle_table(int log2p, std::vector<cx<T>> &out)
 {
     if (log2p == LO) build_twiddle_table_fixed<LO, T>(out);
@@ -97,7 +151,7 @@ template <int BAR, int NT> __device__ __forceinline__ void team_sync(int bar_id)
 }
 
 template <class T, int LOG2P, int NT, bool INV, bool ST_BUF, int PASS, class LD, class ST, bool LD_ALIAS = false,
-          int BAR = 0>
+          int BAR = 0, bool TWSPLIT = false>
 __device__ __forceinline__ void fft_pass_io(cx<T> *s, const cx<T> *tws, int tid, LD &ld, ST &st, int bar_id = 0)
 {
     using PL = FftPlan<LOG2P>;
@@ -128,13 +182,26 @@ __device__ __forceinline__ void fft_pass_io(cx<T> *s, const cx<T> *tws, int tid,
         if (NB % NT == 0 || q < NB)
         {
             const int k = q & (NS - 1);
-            if constexpr (NS > 1)
+            if constexpr (NS > 1 && (!TWSPLIT || NS <= 16))
             {
-                const cx<T> *tp = tws + PL::tw_off(PASS) + k;
+                const cx<T> *tp = tws + (TWSPLIT ? PL::tws_off(PASS) : PL::tw_off(PASS)) + k;
 #pragma unroll
                 for (int r = 1; r < R; ++r)
                 {
                     cx<T> w = tp[(r - 1) * NS];
+                    if (INV) w.y = -w.y;
+                    a[b][r] = cmul(a[b][r], w);
+                }
+            }
+            else if constexpr (NS > 1)
+            {
+                constexpr int NA = NS / 16;
+                const cx<T> *ta = tws + PL::tws_off(PASS) + (k >> 4);
+                const cx<T> *tb = tws + PL::tws_off(PASS) + (R - 1) * NA + (k & 15);
+#pragma unroll
+                for (int r = 1; r < R; ++r)
+                {
+                    cx<T> w = cmul(ta[(r - 1) * NA], tb[(r - 1) * 16]);
                     if (INV) w.y = -w.y;
                     a[b][r] = cmul(a[b][r], w);
                 }
@@ -160,13 +227,13 @@ __device__ __forceinline__ void fft_pass_io(cx<T> *s, const cx<T> *tws, int tid,
 // sure s is free on entry; after return (with ST_BUF) the caller
 // synchronises before reading s.
 template <class T, int LOG2P, int NT, bool INV, bool ST_BUF, class LD, class ST, bool LD_ALIAS = false, int BAR = 0,
-          int PASS = 0>
+          bool TWSPLIT = false, int PASS = 0>
 __device__ __forceinline__ void fft_run(cx<T> *s, const cx<T> *tws, int tid, LD &ld, ST &st, int bar_id = 0)
 {
     if constexpr (PASS < FftPlan<LOG2P>::npass())
     {
-        fft_pass_io<T, LOG2P, NT, INV, ST_BUF, PASS, LD, ST, LD_ALIAS, BAR>(s, tws, tid, ld, st, bar_id);
-        fft_run<T, LOG2P, NT, INV, ST_BUF, LD, ST, LD_ALIAS, BAR, PASS + 1>(s, tws, tid, ld, st, bar_id);
+        fft_pass_io<T, LOG2P, NT, INV, ST_BUF, PASS, LD, ST, LD_ALIAS, BAR, TWSPLIT>(s, tws, tid, ld, st, bar_id);
+        fft_run<T, LOG2P, NT, INV, ST_BUF, LD, ST, LD_ALIAS, BAR, TWSPLIT, PASS + 1>(s, tws, tid, ld, st, bar_id);
     }
 }
 

@@ -11,12 +11,15 @@ constexpr int kFixBatch = 16;
 // (a single-precision FFT's error grows as sqrt(log N) times the unit
 // roundoff; K = 8 covers N up to 8192 several times over); tensor-core form
 // C1 ||x - off|| (FP16 hi+lo keeps 2^-22 of each operand, FP32 accumulation
-// over K/16 steps) plus C2 sqrt(L) / s for the split's subnormal floor (FP16
-// subnormal spacing 2^-24, half of it per operand, in units of the strip scale s).
+// over K/16 steps) plus C2 / s for the split's subnormal floor: a low part
+// below FP16's normal range is rounded to its 2^-24 spacing, an error of at
+// most 2^-25 / s per sample in signal units; summed against a unit-norm
+// template, independent roundings give a standard deviation of
+// 2^-25 / (s sqrt 3), and C2 = 2^-23 is six of those.
 constexpr float kFixTol = 2.0e-5f;
 constexpr float kFixFftK = 8.0f;
 constexpr float kFixTcC1 = 2.0e-6f;
-constexpr float kFixTcC2 = 0x1p-24f;
+constexpr float kFixTcC2 = 0x1p-23f;
 
 // Fix-up batches: the templates of a channel sorted by length, kFixBatch per
 // batch; coefficients (demeaned, unit norm, FP32) interleaved as
@@ -27,12 +30,13 @@ struct FixParams
     long ldx;
     float *rho;
     long ldr;
-    const unsigned char *flags;  // per channel and run, row stride ldf
+    const int *flist;            // listed runs: c * ldf + r
+    const int *fcount;           // number of listed runs
     long ldf;
-    int nruns;                   // runs per channel row that may be flagged
-    int nspans;                  // (nruns + 31) / 32
-    int nbatch;
-    const int *bch;              // channel of each batch
+    int nruns;                   // runs per channel row that may be listed
+    int nbmax;                   // most batches of one channel
+    const int *chan_b0;          // first batch of each channel
+    const int *chan_nb;          // batches of each channel
     const int *btid;             // [nbatch][kFixBatch] template ids, -1 empty
     const long *boff;            // first coefficient of each batch in bco
     const int *bL;               // longest template of each batch

@@ -43,6 +43,18 @@ namespace mfgpu {
 constexpr float kRunConst = 3.0e38f;
 // warps per fix-up CTA
 constexpr int kFixWarps = 4;
+// coefficients per fix-up chunk staged in shared memory (per template)
+constexpr int kFixChunk = 64;
+
+// Marks run r of channel c for the fix-up: one bit per run (row stride
+// ldrs / 32 words) makes every run enter the list once, however many bounds
+// flag it; the list holds c * ldrs + r (capacity: every run of every channel).
+__device__ __forceinline__ void fix_mark(unsigned *fbits, int *flist, int *fcount, int c, int r, long ldrs)
+{
+    const unsigned bit = 1u << (r & 31);
+    const unsigned old = atomicOr(fbits + (long) c * (ldrs >> 5) + (r >> 5), bit);
+    if (!(old & bit)) flist[atomicAdd(fcount, 1)] = (int) ((long) c * ldrs + r);
+}
 
 // Shared memory of den_robust_kernel: staged samples (padded as den_kernel),
 // chunk statistics, reduction scratch.
@@ -263,8 +275,8 @@ __global__ void __launch_bounds__(kThreads) den_robust_kernel(const float *x, lo
 // tol_rho)^2) or the run is unreliable.  One warp per block, 8 per CTA.
 __global__ void __launch_bounds__(256) fix_flag_fft_kernel(const float2 *cst, long ldc, long nchunks, int S, int N,
                                                           int nblocks, const float4 *rstat, long ldrs, int nruns,
-                                                          const unsigned char *dead, unsigned char *flags,
-                                                          float coef2)
+                                                          const unsigned char *dead, unsigned *fbits, int *flist,
+                                                          int *fcount, float coef2)
 {
     const int lane = threadIdx.x & 31;
     const int b = blockIdx.x * 8 + (threadIdx.x >> 5), c = blockIdx.y;
@@ -300,20 +312,20 @@ __global__ void __launch_bounds__(256) fix_flag_fft_kernel(const float2 *cst, lo
     for (int r = (int) j0 + lane; r < r1; r += 32)
     {
         const float mm = rstat[(long) c * ldrs + r].x;
-        if (mm < 0.f || (mm < kRunConst && lim > mm)) flags[(long) c * ldrs + r] = 1;
+        if (mm < 0.f || (mm < kRunConst && lim > mm)) fix_mark(fbits, flist, fcount, c, r, ldrs);
     }
 }
 
 // Tensor-core form: one warp per strip j of 1024 lags (32 runs) of channel
 // c.  The strip's operand offset is the reference level R of its quietest
 // run (the strip's first sample when no run has a positive variance); run r
-// is flagged when c1 ||x - off|| + c2 sqrt(L) / s > tau sqrt(M2min_r), with
+// is flagged when c1 ||x - off|| + c2 / s > tau sqrt(M2min_r), with
 // ||x - off||^2 <= M2min + L (|R_r - off| + spread_r)^2 and s the strip's
 // power-of-two operand scale.  256 threads (8 strips).
 __global__ void __launch_bounds__(256) fix_flag_tc_kernel(const float *x, long ldx, int L, const float4 *rstat,
                                                          long ldrs, int nruns, int tiles, const unsigned char *dead,
-                                                         const float *xrange, float *off_out, unsigned char *flags,
-                                                         float c1, float c2, float tau)
+                                                         const float *xrange, float *off_out, unsigned *fbits,
+                                                         int *flist, int *fcount, float c1, float c2, float tau)
 {
     const int lane = threadIdx.x & 31;
     const int j = blockIdx.x * 8 + (threadIdx.x >> 5), c = blockIdx.y;
@@ -338,10 +350,10 @@ __global__ void __launch_bounds__(256) fix_flag_tc_kernel(const float *x, long l
     {
         const float s = tc_pow2_scale(xrange[c], 13);
         const float d = fabsf(st.y - off) + st.z;
-        const float bound = c1 * sqrtf(fmaf((float) L * d, d, st.x)) + c2 * sqrtf((float) L) / s;
+        const float bound = c1 * sqrtf(fmaf((float) L * d, d, st.x)) + c2 / s;
         f = bound > tau * sqrtf(st.x);
     }
-    if (f) flags[(long) c * ldrs + r] = 1;
+    if (f) fix_mark(fbits, flist, fcount, c, r, ldrs);
 }
 
 
@@ -398,99 +410,104 @@ __device__ __forceinline__ float fix_rho(float num, float M2, int L, float tol)
     return clamp_rho(r);
 }
 
-// One warp per (batch, span of 32 runs), grid-strided; for every flagged run
-// of the span, the 32 lags of each template of the batch: dot products
-// against the window's samples about a local reference, window mean and M2
-// two-pass per distinct template length.
+// Work item j of the fix-up: listed run i = j / nbmax, the k-th batch of
+// that run's channel (k = j % nbmax, items past the channel's batches are
+// skipped), one warp per item, grid-strided, so the runs of one step (which
+// cluster) spread over every warp.  Per item, the 32 lags of each template of
+// the batch: dot products against the window's samples about a local
+// reference (coefficients staged kFixChunk at a time in shared memory),
+// window mean and M2 two-pass per distinct template length.
 __global__ void __launch_bounds__(32 * kFixWarps, 4) fixup_kernel(FixParams p)
 {
     extern __shared__ __align__(16) float smem_fx[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    float *ys = smem_fx + (size_t) wid * (p.Lmax + 64);
+    const int yrow = (p.Lmax + 64 + 3) & ~3;  // samples row, a multiple of 16 bytes
+    float *ys = smem_fx + (size_t) wid * (yrow + kFixBatch * kFixChunk);
+    float4 *cs4 = reinterpret_cast<float4 *>(ys + yrow);
     const long W = (long) gridDim.x * kFixWarps;
-    const long U = (long) p.nbatch * p.nspans;
-    for (long u = (long) blockIdx.x * kFixWarps + wid; u < U; u += W)
+    const long U = (long) *p.fcount * p.nbmax;
+    for (long j = (long) blockIdx.x * kFixWarps + wid; j < U; j += W)
     {
-        const int B = (int) (u % p.nbatch), span = (int) (u / p.nbatch);
-        const int c = p.bch[B];
-        const int r0 = 32 * span;
-        const bool fl = r0 + lane < p.nruns && p.flags[(long) c * p.ldf + r0 + lane] != 0;
-        unsigned m = __ballot_sync(0xffffffffu, fl);
-        if (!m) continue;
+        const int e = p.flist[j / p.nbmax], k = (int) (j % p.nbmax);
+        const int c = (int) (e / p.ldf), r = (int) (e % p.ldf);
+        if (k >= p.chan_nb[c] || r >= p.nruns) continue;
+        const int B = p.chan_b0[c] + k;
         const int Lb = p.bL[B];
         const int mytid = lane < kFixBatch ? p.btid[B * kFixBatch + lane] : -1;
         const int L0 = __shfl_sync(0xffffffffu, mytid >= 0 ? p.tlen[mytid] : 0, 0);
         const float *xc = p.x + (long) c * p.ldx;
         const float4 *co = reinterpret_cast<const float4 *>(p.bco + p.boff[B]);
-        while (m)
+        const long lag0 = 32L * r;
+        const float Rref = xc[lag0 + 16 + L0 / 2];
+        for (int i = lane; i < Lb + 31; i += 32) ys[i] = xc[lag0 + i] - Rref;
+        float acc[kFixBatch];
+#pragma unroll
+        for (int q = 0; q < kFixBatch; ++q) acc[q] = 0.f;
+        constexpr int V4 = kFixBatch / 4;  // float4 per coefficient index
+        for (int i0 = 0; i0 < Lb; i0 += kFixChunk)
         {
-            const int r = r0 + __ffs(m) - 1;
-            m &= m - 1;
-            const long lag0 = 32L * r;
-            const float Rref = xc[lag0 + 16 + L0 / 2];
-            for (int i = lane; i < Lb + 31; i += 32) ys[i] = xc[lag0 + i] - Rref;
+            const int ni = min(kFixChunk, Lb - i0);
+            __syncwarp();  // the previous chunk (and, first, the samples) fully read / written
+            for (int v = lane; v < ni * V4; v += 32) cs4[v] = co[(long) i0 * V4 + v];
             __syncwarp();
-            float acc[kFixBatch];
-#pragma unroll
-            for (int k = 0; k < kFixBatch; ++k) acc[k] = 0.f;
-#pragma unroll 2
-            for (int i = 0; i < Lb; ++i)
+#pragma unroll 4
+            for (int i = 0; i < ni; ++i)
             {
-                const float yv = ys[lane + i];
+                const float yv = ys[lane + i0 + i];
 #pragma unroll
-                for (int q = 0; q < kFixBatch / 4; ++q)
+                for (int q = 0; q < V4; ++q)
                 {
-                    const float4 cf = co[(long) i * (kFixBatch / 4) + q];
+                    const float4 cf = cs4[i * V4 + q];
                     acc[4 * q] = fmaf(cf.x, yv, acc[4 * q]);
                     acc[4 * q + 1] = fmaf(cf.y, yv, acc[4 * q + 1]);
                     acc[4 * q + 2] = fmaf(cf.z, yv, acc[4 * q + 2]);
                     acc[4 * q + 3] = fmaf(cf.w, yv, acc[4 * q + 3]);
                 }
             }
-            const long lag = lag0 + lane;
-            int prevL = -1;
-            float mu = 0.f, M2 = 0.f;
+        }
+        const long lag = lag0 + lane;
+        int prevL = -1;
+        float mu = 0.f, M2 = 0.f;
 #pragma unroll
-            for (int k = 0; k < kFixBatch; ++k)
+        for (int q = 0; q < kFixBatch; ++q)
+        {
+            const int t = __shfl_sync(0xffffffffu, mytid, q);
+            if (t < 0) continue;  // empty slots (the batch's last ones)
+            const int Lt = p.tlen[t];
+            if (Lt != prevL)
             {
-                const int t = __shfl_sync(0xffffffffu, mytid, k);
-                if (t < 0) continue;  // empty slots (the batch's last ones)
-                const int Lt = p.tlen[t];
-                if (Lt != prevL)
+                float s = 0.f;
+                for (int i = 0; i < Lt; ++i) s += ys[lane + i];
+                mu = s / (float) Lt;
+                float a = 0.f, b = 0.f;
+                for (int i = 0; i < Lt; ++i)
                 {
-                    float s = 0.f;
-                    for (int i = 0; i < Lt; ++i) s += ys[lane + i];
-                    mu = s / (float) Lt;
-                    float a = 0.f, b = 0.f;
-                    for (int i = 0; i < Lt; ++i)
-                    {
-                        const float d = ys[lane + i] - mu;
-                        a += d;
-                        b = fmaf(d, d, b);
-                    }
-                    M2 = fmaf(-a, a / (float) Lt, b);
-                    prevL = Lt;
+                    const float d = ys[lane + i] - mu;
+                    a += d;
+                    b = fmaf(d, d, b);
                 }
-                const float rho = fix_rho(fmaf(-mu, p.bsum[t], acc[k]), M2, Lt, p.tol);
-                if (lag < p.nvalid[t])
+                M2 = fmaf(-a, a / (float) Lt, b);
+                prevL = Lt;
+            }
+            const float rho = fix_rho(fmaf(-mu, p.bsum[t], acc[q]), M2, Lt, p.tol);
+            if (lag < p.nvalid[t])
+            {
+                p.rho[(long) t * p.ldr + lag] = rho;
+                if (p.pk_flags && lag < p.pk_len && rho > p.pk_thr)
                 {
-                    p.rho[(long) t * p.ldr + lag] = rho;
-                    if (p.pk_flags && lag < p.pk_len && rho > p.pk_thr)
-                    {
-                        const long cc = lag >> 6;
-                        atomicOr(p.pk_flags + (long) t * p.pk_words + (cc >> 5), 1u << (cc & 31));
-                    }
-                }
-                if (p.pk_dirty && lane == 0)
-                {
-                    // candidates at lags lag0 - 1 .. lag0 + 32 depend on these values
-                    const long S = p.row_S ? p.row_S[t] : p.S0;
-                    const long bl = (lag0 > 0 ? lag0 - 1 : 0) / S, bh = (lag0 + 32) / S;
-                    for (long bb = bl; bb <= bh && bb < p.pk_stride; ++bb) p.pk_dirty[(long) t * p.pk_stride + bb] = 1;
+                    const long cc = lag >> 6;
+                    atomicOr(p.pk_flags + (long) t * p.pk_words + (cc >> 5), 1u << (cc & 31));
                 }
             }
-            __syncwarp();  // ys reused by the next run
+            if (p.pk_dirty && lane == 0)
+            {
+                // candidates at lags lag0 - 1 .. lag0 + 32 depend on these values
+                const long S = p.row_S ? p.row_S[t] : p.S0;
+                const long bl = (lag0 > 0 ? lag0 - 1 : 0) / S, bh = (lag0 + 32) / S;
+                for (long bb = bl; bb <= bh && bb < p.pk_stride; ++bb) p.pk_dirty[(long) t * p.pk_stride + bb] = 1;
+            }
         }
+        __syncwarp();  // ys reused by the next item
     }
 }
 

@@ -57,6 +57,7 @@ template <class T> struct XcorrParams
     const int *nvalid;        // valid lags per template (n - L_t + 1)
     const unsigned char *dead;// dead-trace flag per channel
     const cx<T> *twt;         // twiddle table of the plan (FftPlan layout)
+    const cx<T> *twt_split;   // mode 4: pass twiddles in the split layout (FftPlan::tws_off)
     const T *den;             // SHARED_DEN: sqrt(L)/max(tol, den) per channel and lag, row stride ldd
     long ldd;
     int S;                    // lags per block (multiple of 32)
@@ -92,11 +93,13 @@ template <class T> struct SpecParams
 
 // Shared-memory carve-up of the correlator (used by host and device).
 //   head | xs (staged segment; with SD also the first FFT work buffer W0) |
-//   [W0] | [W1 (MODE 2)] | UV (per-bin U, V pairs of the block spectrum) |
-//   pass twiddles | [2 spectrum buffers (MODE 1)] | invd
+//   [W0] | [W1 (MODE 2, 3, 4)] | UV (per-bin U, V pairs of the block spectrum) |
+//   pass twiddles | [2 spectrum buffers (MODE 1)] | invd (two rows in MODE 4)
 // MODE 0: whole CTA per transform, spectra read from L2;  MODE 1: whole CTA,
 // spectra TMA-prefetched;  MODE 2: two 128-thread teams transform different
-// templates with their own named barriers, spectra read from L2.
+// templates with their own named barriers, spectra read from L2;  MODE 4:
+// 512 threads, two 256-thread teams, each normalising its own templates
+// (several lengths), pass twiddles in the split layout.
 template <class T, int LOG2P> struct XcorrLayout
 {
     using acc = typename acc_t<T>::type;
@@ -104,11 +107,18 @@ template <class T, int LOG2P> struct XcorrLayout
     static constexpr size_t up(size_t v) { return (v + 127) & ~size_t(127); }
     static constexpr size_t seg = sizeof(T) * N;
     static constexpr size_t fft = sizeof(cx<T>) * spad_size(P);
-    static constexpr size_t head(bool sd)
+    // mode 4 keeps a second pair of partial-sum rows (p1, p2) for the second team
+    static constexpr size_t head(bool sd, int mode = 0)
     {
-        return up(64 + 32 * sizeof(T) + (sd ? 0 : 2 * sizeof(acc) * (NCH + 1) + 2 * sizeof(T) * NCH));
+        return up(64 + 32 * sizeof(T) +
+                  (sd ? 0 : 2 * sizeof(acc) * (NCH + 1) + (mode == 4 ? 4 : 2) * sizeof(T) * NCH));
     }
-    static constexpr size_t tw_bytes = sizeof(cx<T>) * FftPlan<LOG2P>::post_off();  // pass twiddles only
+    // pass twiddles only; mode 4 holds them in the split layout (FftPlan::tws_off)
+    static constexpr size_t tw_bytes_of(int mode)
+    {
+        return sizeof(cx<T>) * (mode == 4 ? FftPlan<LOG2P>::tws_total() : FftPlan<LOG2P>::post_off());
+    }
+    static constexpr size_t tw_bytes = tw_bytes_of(0);
     static constexpr size_t uv = sizeof(cx<T>) * 2 * P;
     static constexpr size_t brow = sizeof(cx<T>) * (P + 2);
     // Without SHARED_DEN (modes 0, 1) the segment's region later holds the
@@ -124,22 +134,27 @@ template <class T, int LOG2P> struct XcorrLayout
     {
         return up(overlay(sd, mode) ? (seg > fft ? seg : fft) : padded);
     }
-    static constexpr size_t off_xs(bool sd) { return head(sd); }
-    static constexpr size_t off_W0(bool sd, int mode) { return off_xs(sd) + (overlay(sd, mode) ? 0 : xs_region(sd, mode)); }
+    static constexpr size_t off_xs(bool sd, int mode = 0) { return head(sd, mode); }
+    static constexpr size_t off_W0(bool sd, int mode)
+    {
+        return off_xs(sd, mode) + (overlay(sd, mode) ? 0 : xs_region(sd, mode));
+    }
     static constexpr size_t off_W1(bool sd, int mode)
     {
-        return off_xs(sd) + xs_region(sd, mode) + (overlay(sd, mode) ? 0 : up(fft));
+        return off_xs(sd, mode) + xs_region(sd, mode) + (overlay(sd, mode) ? 0 : up(fft));
     }
     static constexpr size_t off_UV(bool sd, int mode) { return off_W1(sd, mode) + (teams(mode) ? up(fft) : 0); }
     static constexpr size_t off_tw(bool sd, int mode) { return off_UV(sd, mode) + up(uv); }
-    static constexpr size_t off_B(bool sd, int mode) { return off_tw(sd, mode) + up(tw_bytes); }
+    static constexpr size_t off_B(bool sd, int mode) { return off_tw(sd, mode) + up(tw_bytes_of(mode)); }
     static constexpr size_t off_invd(bool sd, int mode) { return off_B(sd, mode) + (mode == 1 ? 2 * up(brow) : 0); }
+    // mode 4: one normalisation row per team
+    static constexpr int invd_rows(int mode) { return mode == 4 ? 2 : 1; }
     // fused peak candidates: per team two chunk masks (one bit per 64 lags,
     // P/32 chunks)
     static constexpr int mask_words = (P / 32 + 31) / 32;
     static __host__ __device__ size_t off_M(bool sd, int mode, int S)
     {
-        return off_invd(sd, mode) + up(sizeof(T) * (size_t) S);
+        return off_invd(sd, mode) + invd_rows(mode) * up(sizeof(T) * (size_t) S);
     }
     static size_t bytes(bool sd, int mode, int S)
     {
@@ -197,7 +212,8 @@ template <> struct MeanAcc<double>
 
 // block-wide mean of n values from the per-thread accumulators; red holds
 // at least 2 * kThreads / 32 values of T
-template <class T> __device__ __forceinline__ T block_mean(MeanAcc<T> a, T *red, int n)
+// (NTH threads in the CTA; red holds at least 2 * NTH / 32 values of T)
+template <class T, int NTH = kThreads> __device__ __forceinline__ T block_mean(MeanAcc<T> a, T *red, int n)
 {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) a.add(a.shfl_xor(o));
@@ -208,7 +224,7 @@ template <class T> __device__ __forceinline__ T block_mean(MeanAcc<T> a, T *red,
     __syncthreads();
     MeanAcc<T> t = r[0];
 #pragma unroll
-    for (int i = 1; i < kThreads / 32; ++i) t.add(r[i]);
+    for (int i = 1; i < NTH / 32; ++i) t.add(r[i]);
     return t.mean(n);
 }
 
@@ -389,14 +405,14 @@ template <class T> struct SegStats
 
 // Chunk sums over 32 samples with a per-lane skew (conflict-free banks),
 // then an exclusive scan by warp 0.
-template <class T, int N>
+template <class T, int N, int NTH = kThreads>
 __device__ __forceinline__ void seg_chunk_prefix(SegStats<T> st, int tid)
 {
     using A = acc_t<T>;
     using acc = typename A::type;
     constexpr int NCH = N / 32;
     const int lane = tid & 31;
-    for (int j = tid; j < NCH; j += kThreads)
+    for (int j = tid; j < NCH; j += NTH)
     {
         acc s1 = A::zero(), s2 = A::zero();
         const T *xp = st.xs + 32 * j;
@@ -458,22 +474,22 @@ __device__ __forceinline__ void seg_chunk_prefix(SegStats<T> st, int tid)
 // y = x - m with one pad word per 32 samples, for conflict-free strided
 // reads by seg_inv_den.  The padded copy (st.yp) fits the segment's region
 // or one FFT work buffer.
-template <class T, int N>
+template <class T, int N, int NTH = kThreads>
 __device__ __forceinline__ void seg_make_padded(SegStats<T> st, int tid)
 {
-    constexpr int PER = (N + kThreads - 1) / kThreads;
+    constexpr int PER = (N + NTH - 1) / NTH;
     T v[PER];
 #pragma unroll
     for (int i = 0; i < PER; ++i)
     {
-        const int e = tid + i * kThreads;
+        const int e = tid + i * NTH;
         v[i] = e < N ? st.xs[e] - st.m : (T) 0;
     }
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < PER; ++i)
     {
-        const int e = tid + i * kThreads;
+        const int e = tid + i * NTH;
         if (e < N) st.yp[den_pad(e)] = v[i];
     }
     __syncthreads();
@@ -486,15 +502,15 @@ __device__ __forceinline__ void seg_make_padded(SegStats<T> st, int tid)
 // sums of the first L mod 32 samples of a chunk -- then 32 lags of
 // corrections in the data type (DenOps; the same scheme as den_kernel).
 // Ends with a barrier.
-template <class T, int N>
-__device__ __forceinline__ void seg_inv_den(SegStats<T> st, int L, int S, T tol, T *invd, int tid)
+template <class T, int N, int NT = kThreads, int BAR = 0>
+__device__ __forceinline__ void seg_inv_den(SegStats<T> st, int L, int S, T tol, T *invd, int tid, int bar_id = 0)
 {
     using A = acc_t<T>;
     using O = DenOps<T>;
     using acc = typename A::type;
     constexpr int NCH = N / 32;
     const int Lq = L >> 5, re = L & 31;
-    for (int j = tid; j < NCH; j += kThreads)
+    for (int j = tid; j < NCH; j += NT)
     {
         T a = 0, b = 0;
         const T *yc = st.yp + 33 * j;
@@ -507,9 +523,9 @@ __device__ __forceinline__ void seg_inv_den(SegStats<T> st, int L, int S, T tol,
         st.p1[j] = a;
         st.p2[j] = b;
     }
-    __syncthreads();
+    team_sync<BAR, NT>(bar_id);
     const T sqrtL = sqrt((T) L), Lt = (T) L;
-    for (int v = tid; v < S / 32; v += kThreads)
+    for (int v = tid; v < S / 32; v += NT)
     {
         const acc w1 = A::add_val(A::sub(st.c1[v + Lq], st.c1[v]), st.p1[v + Lq]);
         const acc w2 = A::add_val(A::sub(st.c2[v + Lq], st.c2[v]), st.p2[v + Lq]);
@@ -552,7 +568,7 @@ __device__ __forceinline__ void seg_inv_den(SegStats<T> st, int L, int S, T tol,
                 *reinterpret_cast<double2 *>(dst + (((q >> 1) ^ sw) << 1)) = make_double2(o[q], o[q + 1]);
         }
     }
-    __syncthreads();
+    team_sync<BAR, NT>(bar_id);
 }
 
 // Index of the pair (lags 2e, 2e + 1) in a normalisation row written by
@@ -636,7 +652,8 @@ __device__ __forceinline__ bool xcorr_wait(uint64_t *bar, uint32_t parity, int *
 // precomputed per channel (den_kernel) and the first FFT work buffer
 // overlays the staged segment.  MODE: see XcorrLayout.
 template <class T, int LOG2P, bool SHARED_DEN, int MODE>
-__global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 : 1)
+__global__ void __launch_bounds__(MODE == 4 ? 2 * kThreads : kThreads,
+                                  (sizeof(T) == 4 && LOG2P <= 11 && MODE != 4) ? 2 : 1)
     xcorr_kernel(XcorrParams<T> p)
 {
     using Acc = acc_t<T>;
@@ -645,6 +662,11 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
     using PL = FftPlan<LOG2P>;
     constexpr bool PREFETCH = MODE == 1;
     constexpr bool TEAMS = MODE >= 2;
+    // mode 4: 512 threads in two 256-thread teams, each normalising its own
+    // templates (several lengths) into its own row; split twiddle table
+    constexpr bool WIDE = MODE == 4;
+    constexpr int NTH = WIDE ? 2 * kThreads : kThreads;  // threads of the CTA
+    static_assert(!(WIDE && SHARED_DEN), "mode 4 normalises each template inside the CTA");
     // mode 3: two teams, one template length, normalisation computed in the
     // CTA (once, before the forward FFT) instead of read from den_kernel
     constexpr bool OWN_DEN = MODE == 3;
@@ -667,7 +689,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
             const int t = p.tids[ti];
             const long nv = p.nvalid[t];
             T *dst = p.rho + (long) t * p.ldr;
-            for (int k = tid; k < S; k += kThreads)
+            for (int k = tid; k < S; k += NTH)
                 if (k0 + k < nv) dst[k0 + k] = (T) 0;
         }
         return;
@@ -678,7 +700,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
     T *red = reinterpret_cast<T *>(smem_x + 64);
     acc *c1 = reinterpret_cast<acc *>(smem_x + 64 + 32 * sizeof(T));  // only without SHARED_DEN
     acc *c2 = c1 + (NCH + 1);
-    T *xs = reinterpret_cast<T *>(smem_x + LY::off_xs(SHARED_DEN));
+    T *xs = reinterpret_cast<T *>(smem_x + LY::off_xs(SHARED_DEN, MODE));
     cx<T> *W0 = reinterpret_cast<cx<T> *>(smem_x + LY::off_W0(SHARED_DEN, MODE));
     cx<T> *W1 = reinterpret_cast<cx<T> *>(smem_x + LY::off_W1(SHARED_DEN, MODE));
     cx<T> *UV = reinterpret_cast<cx<T> *>(smem_x + LY::off_UV(SHARED_DEN, MODE));
@@ -689,7 +711,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
     unsigned *Mk = reinterpret_cast<unsigned *>(smem_x + LY::off_M(SHARED_DEN, MODE, S));
     cx<T> *W = W0;
     const cx<T> *post = p.twt + PL::post_off();  // real-FFT twiddles, read once per CTA from L2
-    constexpr uint32_t kTwBytes = (uint32_t) LY::tw_bytes;
+    constexpr uint32_t kTwBytes = (uint32_t) LY::tw_bytes_of(MODE);
 
     // ---- stage segment, pass twiddles and the first spectrum with bulk async copies
     if (tid < 2 * (TEAMS ? 2 : 1) * LY::mask_words) Mk[tid] = 0u;  // chunk masks of the fused peak candidates
@@ -703,7 +725,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
         if (!p.test_skip_copy)
         {
             tma_load_1d(xs, p.x + (long) c * p.ldx + k0, (uint32_t) LY::seg, &bar[0]);
-            tma_load_1d(tws, p.twt, kTwBytes, &bar[0]);
+            tma_load_1d(tws, WIDE ? p.twt_split : p.twt, kTwBytes, &bar[0]);
             if (SHARED_DEN) tma_load_1d(invd_s, p.den + (long) c * p.ldd + k0, den_bytes, &bar[0]);
         }
         if (PREFETCH)
@@ -722,14 +744,14 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
     // ---- segment mean; sliding-window normalisation (precomputed per
     //      channel by den_kernel when every template shares one length)
     MeanAcc<T> macc;
-    for (int i = tid; i < N; i += kThreads) macc.add(xs[i]);
-    const T m = block_mean<T>(macc, red, N);
+    for (int i = tid; i < N; i += NTH) macc.add(xs[i]);
+    const T m = block_mean<T, NTH>(macc, red, N);
     SegStats<T> st;
     st.xs = xs; st.yp = xs; st.m = m; st.c1 = c1; st.c2 = c2;
     st.p1 = reinterpret_cast<T *>(c2 + NCH + 1);
     st.p2 = st.p1 + NCH;
     int Lcur = p.tlen[p.tids[t_begin]];
-    if constexpr (!SHARED_DEN) seg_chunk_prefix<T, N>(st, tid);
+    if constexpr (!SHARED_DEN) seg_chunk_prefix<T, N, NTH>(st, tid);
     if constexpr (OWN_DEN)
     {
         // the second team's buffer is free until the teams start: padded
@@ -748,14 +770,14 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
             return cmk(v.x - m, v.y - m);
         };
         auto stb = [&](int e, cx<T> v) { W[spad(e)] = v; };
-        fft_run<T, LOG2P, kThreads, false, true, decltype(ld), decltype(stb), SHARED_DEN || OWN_DEN>(W, tws, tid, ld,
-                                                                                                       stb);
+        fft_run<T, LOG2P, NTH, false, true, decltype(ld), decltype(stb), SHARED_DEN || OWN_DEN, 0, WIDE>(W, tws, tid,
+                                                                                                        ld, stb);
         __syncthreads();
         // Real-FFT post-processing to X[k], k = 0..P, then the per-bin pairs
         //   U[e] = X[e] (1 + i wc_e),  V[e] = conj(X[P-e]) (1 - i wc_e),
         // wc_e = exp(+2 pi i e/N), so that the inverse pre-processing of
         // Y = B X becomes Z'[e] = B[e] U[e] + conj(B[P-e]) V[e].
-        for (int k = tid; k <= P / 2; k += kThreads)
+        for (int k = tid; k <= P / 2; k += NTH)
         {
             cx<T> xk, xp;  // X[k], X[P-k]
             if (k == 0)
@@ -786,7 +808,13 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
         }
         __syncthreads();
     }
-    if constexpr (!SHARED_DEN && !OWN_DEN)
+    if constexpr (WIDE)
+    {
+        // the segment's region is free now: padded demeaned copy; each team
+        // normalises its templates in the loop below
+        seg_make_padded<T, N, NTH>(st, tid);
+    }
+    else if constexpr (!SHARED_DEN && !OWN_DEN)
     {
         // the segment's region is free now: padded demeaned copy, then the
         // first template length's normalisation
@@ -843,7 +871,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
         }
     };
     auto template_body = [&](auto bar_tag, auto nt_tag, int j, const cx<T> *B, cx<T> *Wt, unsigned *mk, int ttid,
-                             int bar_id) {
+                             int bar_id, const T *invd_row) {
         constexpr int BAR = decltype(bar_tag)::value;
         constexpr int NTT = decltype(nt_tag)::value;
         const int t = p.tids[t_begin + j];
@@ -859,7 +887,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
         };
         // lags [k0, k0 + kmax) of this block are stored (kmax <= S, even S)
         const int kmax = (int) (nv - k0 < (long) S ? nv - k0 : (long) S);
-        const cx<T> *invd2 = reinterpret_cast<const cx<T> *>(invd_s);
+        const cx<T> *invd2 = reinterpret_cast<const cx<T> *>(invd_row);
         auto epi = [&](int e, cx<T> z) {
             const int k = 2 * e;
             if (k >= kmax) return;
@@ -871,11 +899,57 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
             else dst[k] = r0;
             if (pk && (r0 > pk_thr || r1 > pk_thr)) atomicOr(mk + (e >> 10), 1u << ((e >> 5) & 31));
         };
-        fft_run<T, LOG2P, NTT, true, false, decltype(pre), decltype(epi), false, BAR>(Wt, tws, ttid, pre, epi,
-                                                                                     bar_id);
+        fft_run<T, LOG2P, NTT, true, false, decltype(pre), decltype(epi), false, BAR, WIDE>(Wt, tws, ttid, pre, epi,
+                                                                                           bar_id);
     };
 
-    if constexpr (TEAMS)
+    if constexpr (WIDE)
+    {
+        // two teams of 256 threads; each keeps its own work buffer, chunk
+        // masks, normalisation row (its templates' own lengths), partial-sum
+        // rows and barrier
+        const int team = tid >> 8, ttid = tid & 255, bar_id = 1 + team;
+        unsigned *mkt = Mk + team * 2 * MW;
+        cx<T> *Wt = team ? W1 : W0;
+        T *invd_t = invd_s + team * (LY::up(sizeof(T) * (size_t) S) / sizeof(T));
+        SegStats<T> stt = st;
+        if (team)
+        {
+            stt.p1 = st.p2 + NCH;
+            stt.p2 = stt.p1 + NCH;
+        }
+        int t_prev = -1, it = 0, Lt = -1;
+        for (int j = team; j < ntl; j += 2, ++it)
+        {
+            const int t = p.tids[t_begin + j];
+            const cx<T> *B = p.Bc + (long) t * p.ldb;
+            if (it > 0)
+            {
+                team_sync<-1, kThreads>(bar_id);
+                if (pk)
+                {
+                    pk_scan(std::integral_constant<int, kThreads>(), mkt + ((it - 1) & 1) * MW, t_prev, ttid);
+                    if (ttid < MW) mkt[(it & 1) * MW + ttid] = 0u;
+                }
+            }
+            const int L = p.tlen[t];
+            if (L != Lt)
+            {
+                // ends with the team's barrier: the row is complete before the epilogue reads it
+                seg_inv_den<T, N, kThreads, -1>(stt, L, S, p.tol, invd_t, ttid, bar_id);
+                Lt = L;
+            }
+            template_body(std::integral_constant<int, -1>(), std::integral_constant<int, kThreads>(), j, B, Wt,
+                          mkt + (it & 1) * MW, ttid, bar_id, invd_t);
+            t_prev = t;
+        }
+        if (pk && it > 0)
+        {
+            team_sync<-1, kThreads>(bar_id);
+            pk_scan(std::integral_constant<int, kThreads>(), mkt + ((it - 1) & 1) * MW, t_prev, ttid);
+        }
+    }
+    else if constexpr (TEAMS)
     {
         // two teams of 128 threads; each keeps its own work buffer, chunk
         // masks and barrier
@@ -898,7 +972,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
                 }
             }
             template_body(std::integral_constant<int, -1>(), std::integral_constant<int, 128>(), j, B, Wt,
-                          mkt + (it & 1) * MW, ttid, bar_id);
+                          mkt + (it & 1) * MW, ttid, bar_id, invd_s);
             t_prev = p.tids[t_begin + j];
         }
         if (pk && it > 0)
@@ -955,7 +1029,7 @@ __global__ void __launch_bounds__(kThreads, (sizeof(T) == 4 && LOG2P <= 11) ? 2 
                 }
             }
             template_body(std::integral_constant<int, 0>(), std::integral_constant<int, kThreads>(), j, B, W,
-                          Mk + (j & 1) * MW, tid, 0);
+                          Mk + (j & 1) * MW, tid, 0, invd_s);
         }
         if (pk)
         {

@@ -22,7 +22,9 @@ template <> struct fft_limits<double> { static constexpr int lo = 5, hi = 11; };
 
 // mode: 0 whole CTA, 1 whole CTA + spectrum prefetch, 2 two teams (shared
 // length, normalisation rows from den_kernel), 3 two teams (shared length,
-// normalisation computed in the CTA; shared_den false)
+// normalisation computed in the CTA; shared_den false), 4 two 256-thread
+// teams in a 512-thread CTA (several lengths, each team normalising its own
+// templates; FP32, P >= 2048; shared_den false)
 template <class T> size_t xcorr_smem_bytes(int log2p, bool shared_den, int mode, int S);
 template <class T> cudaError_t launch_xcorr(int log2p, bool shared_den, int mode, const XcorrParams<T> &p,
                                             int nblocks, int ngroups, cudaStream_t s);
@@ -32,6 +34,8 @@ template <class T> cudaError_t launch_den(const T *x, long ldx, int L, T *den, l
                                           cudaStream_t s);
 // twiddle table of the FFT plan for P = 2^log2p (FftPlan layout)
 template <class T> void twiddle_table(int log2p, std::vector<cx<T>> &out);
+// the pass twiddles in the split layout (FftPlan::tws_off; correlator mode 4)
+template <class T> void twiddle_split(int log2p, std::vector<cx<T>> &out);
 // dead-trace flags of nch channels (rows of n samples, stride ldx): two
 // launches; pmin/pmax are scratch of nch * nchunks entries each; range
 // (optional) receives max - min per channel
@@ -47,16 +51,16 @@ cudaError_t launch_tc_xcorr(const TcParams &p, int nctas, cudaStream_t s);
 // variances with per-run statistics (float4 per 32 lags, row stride ldrs;
 // den optional) and per-chunk statistics (float2 per 32 samples, row stride
 // ldc), the per-run error bounds of the FFT and tensor-core
-// correlators (flags: one byte per run, row stride ldrs), and the fix-up of
-// the flagged runs.
+// correlators (flagged runs listed once each: a bit per run, the list and its
+// count), and the fix-up of the listed runs.
 cudaError_t launch_den_robust(const float *x, long ldx, int L, float *den, long ldd, float tol, float4 *rstat,
                               long ldrs, float2 *cst, long ldc, int nblocks, int nch, cudaStream_t s);
 cudaError_t launch_fix_flag_fft(const float2 *cst, long ldc, long nchunks, int S, int N, int nblocks, int nch,
-                                const float4 *rstat, long ldrs, int nruns, const unsigned char *dead,
-                                unsigned char *flags, float coef2, cudaStream_t s);
+                                const float4 *rstat, long ldrs, int nruns, const unsigned char *dead, unsigned *fbits,
+                                int *flist, int *fcount, float coef2, cudaStream_t s);
 cudaError_t launch_fix_flag_tc(const float *x, long ldx, int L, const float4 *rstat, long ldrs, int nruns, int tiles,
-                               int nch, const unsigned char *dead, const float *xrange, float *off,
-                               unsigned char *flags, float c1, float c2, float tau, cudaStream_t s);
+                               int nch, const unsigned char *dead, const float *xrange, float *off, unsigned *fbits,
+                               int *flist, int *fcount, float c1, float c2, float tau, cudaStream_t s);
 size_t fixup_smem_bytes(int Lmax);
 cudaError_t launch_fix_prep(const double *tmpl, const long *toff, const int *tlen, const int *btid, const long *boff,
                             const int *bL, int nbatch, float *bco, float *bsum, cudaStream_t s);

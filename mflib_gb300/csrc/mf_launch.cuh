@@ -2,6 +2,7 @@
 // type; included once by mf_f32.cu and once by mf_f64.cu so the two
 // precisions compile in parallel.
 #pragma once
+#include <type_traits>
 #include "launch.h"
 
 namespace mfgpu {
@@ -16,9 +17,11 @@ template <class T, int LOG2P> struct XcorrTable
         static SmemCap cap;
         cudaError_t e = raise_smem_cap(k, bytes, cap);
         if (e != cudaSuccess) return e;
-        k<<<dim3(nblocks, ngroups), kThreads, bytes, s>>>(p);
+        k<<<dim3(nblocks, ngroups), MODE == 4 ? 2 * kThreads : kThreads, bytes, s>>>(p);
         return cudaGetLastError();
     }
+    // mode 4 (two 256-thread teams, several template lengths): FP32, P >= 2048
+    static constexpr bool wide_ok = std::is_same<T, float>::value && LOG2P >= 11;
     // MODE 2 (teams) exists only for a shared template length with its
     // normalisation rows precomputed, MODE 3 only for a shared length
     // normalised inside the CTA
@@ -32,6 +35,11 @@ template <class T, int LOG2P> struct XcorrTable
         }
         if (mode == 2) return cudaErrorInvalidValue;
         if (mode == 3) return go<false, 3>(p, nblocks, ngroups, s);
+        if (mode == 4)
+        {
+            if constexpr (wide_ok) return go<false, 4>(p, nblocks, ngroups, s);
+            else return cudaErrorInvalidValue;
+        }
         return mode == 1 ? go<false, 1>(p, nblocks, ngroups, s) : go<false, 0>(p, nblocks, ngroups, s);
     }
     static cudaError_t spectra(const SpecParams<T> &p, int nt, cudaStream_t s)
@@ -104,6 +112,11 @@ cudaError_t launch_den<MFGPU_T>(const MFGPU_T *x, long ldx, int L, MFGPU_T *den,
 template <> void twiddle_table<MFGPU_T>(int log2p, std::vector<cx<MFGPU_T>> &out)
 {
     build_twiddle_table<MFGPU_T>(log2p, out);
+}
+
+template <> void twiddle_split<MFGPU_T>(int log2p, std::vector<cx<MFGPU_T>> &out)
+{
+    build_twiddle_split<MFGPU_T>(log2p, out);
 }
 
 template <>

@@ -176,7 +176,9 @@ class MatchedFilter:
         1 whole CTA, 2 whole CTA with spectrum prefetch, 3 two teams per CTA,
         templates of one length only; 4 split-precision tensor-core
         correlation, FP32 and templates of one length; 5 two teams with the
-        normalisation computed inside each CTA, templates of one length);
+        normalisation computed inside each CTA, templates of one length;
+        6 two 256-thread teams per 512-thread CTA, FP32 and templates of
+        several lengths);
         ``length_buckets`` caps the length buckets of a mixed-length bank
         (0 automatic, 1 one plan for every template); ``bucket_plans``
         overrides the plan of each length bucket (shortest templates first):

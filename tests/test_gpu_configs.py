@@ -78,12 +78,13 @@ def test_single_channel_hour(gpu, oracle, dtype):
             assert np.min(np.abs(pk - o)) <= 1
 
 
-@pytest.mark.parametrize("buckets", [0, 1, 2, 3])
-def test_uneven_bank(gpu, oracle, buckets):
+@pytest.mark.parametrize("buckets,variant", [(0, 0), (1, 0), (2, 0), (3, 0), (1, 6), (2, 6)])
+def test_uneven_bank(gpu, oracle, buckets, variant):
     """Templates of 200..3,000 samples with random 1..15 Hz pass bands, each
     assigned to one of 6 channels (the 2,000-template bank's recipe at 60
     templates and 120,000 samples per channel), with the planner's length
-    buckets, one plan, and at most two or three buckets."""
+    buckets, one plan, and at most two or three buckets; variant 6 runs every
+    bucket on two 256-thread teams per CTA."""
     mf = gpu
     rng = np.random.default_rng(200)
     nt, nch, n = 60, 6, 120_000
@@ -96,7 +97,10 @@ def test_uneven_bank(gpu, oracle, buckets):
     chan = rng.integers(0, nch, nt)
     sigs = [_bp(np.random.default_rng(300 + c).standard_normal(n), 1.0, 15.0).astype(np.float32) for c in range(nch)]
     f = mf.MultiChannel.MatchedFilter(dtype=np.float32)
-    f.initialize(_params(mf, tps, n), template_channels=chan, n_channels=nch, length_buckets=buckets)
+    f.initialize(_params(mf, tps, n), template_channels=chan, n_channels=nch, length_buckets=buckets,
+                 correlator_variant=variant)
+    if variant:
+        assert f.get_plan()["correlator"] == variant
     bk = f.get_plan()["buckets"]
     assert sum(c for _, c in bk) == nt
     if buckets == 1:

@@ -251,7 +251,7 @@ def test_fused_peak_candidates(gpu, oracle, rng, dtype, variant, fft_length):
 
 
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
-@pytest.mark.parametrize("plan", ["fft2048", "buckets"])
+@pytest.mark.parametrize("plan", ["fft2048", "buckets", "wide"])
 def test_fused_peak_candidates_mixed_lengths(gpu, oracle, rng, dtype, plan):
     """Templates of several lengths: the peak trace stops at n - Lmax + 1
     lags, inside the shorter templates' valid range; with length buckets the
@@ -259,7 +259,10 @@ def test_fused_peak_candidates_mixed_lengths(gpu, oracle, rng, dtype, plan):
     mf = gpu
     lens = [90, 200, 333, 120, 201] + ([1500, 1700] if plan == "buckets" else [])
     p, chans, assign = _fused_case(mf, rng, dtype, lens, n=45_001)
-    kw = dict(fft_length=2048) if plan == "fft2048" else dict(length_buckets=3)
+    if plan == "wide" and dtype == np.float64:
+        pytest.skip("two 256-thread teams (variant 6) take FP32 data")
+    kw = (dict(fft_length=2048) if plan == "fft2048" else
+          dict(length_buckets=3) if plan == "buckets" else dict(fft_length=4096, correlator_variant=6))
     f = _filter(mf, p, chans, assign, dtype, **kw)
     if plan == "buckets":
         assert len(f.get_plan()["buckets"]) > 1

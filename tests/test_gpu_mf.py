@@ -269,9 +269,16 @@ def test_correlator_variant_errors(gpu, rng):
     with pytest.raises(ValueError):
         f.initialize(p, correlator_variant=4)
     with pytest.raises(ValueError):
-        f.initialize(p, correlator_variant=6)
+        f.initialize(p, correlator_variant=7)
     f.initialize(p, correlator_variant=2)
     assert f.is_initialized()
+    # two 256-thread teams: FP32 and templates of several lengths only
+    f.initialize(p, correlator_variant=6)
+    assert f.get_plan()["correlator"] == 6
+    with pytest.raises(ValueError):
+        mf.MultiChannel.MatchedFilter(dtype=np.float64).initialize(p, correlator_variant=6)
+    with pytest.raises(ValueError):
+        f.initialize(_params(mf, [rng.standard_normal(100)] * 2, n), correlator_variant=6)
 
 
 def test_shared_channels_extension(gpu, oracle, rng):
