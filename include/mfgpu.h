@@ -120,7 +120,15 @@ typedef struct
 mfgpu_status mfgpu_mf_create(int precision, mfgpu_mf **mf);
 /* ~MatchedFilter() */
 mfgpu_status mfgpu_mf_destroy(mfgpu_mf *mf);
-/* MatchedFilter<T>::initialize, src/matchedFilter.cpp:507-821 */
+/* MatchedFilter<T>::initialize, src/matchedFilter.cpp:507-821.  Like the
+ * reference (which sizes its FFT up to 2^21, src/matchedFilterParameters.cpp:54-64)
+ * any template length is accepted: templates longer than the largest
+ * overlap-save plan takes (FP32: 8,161 samples, FP64: 4,065) are correlated
+ * directly in the time domain (two-pass Pearson per lag, cost proportional to
+ * the template length per lag), beside the FFT plan of the others.  The direct
+ * correlator keeps L + 31 samples per warp in shared memory, which bounds L
+ * at about 57,000 samples (FP32) or 27,900 (FP64); longer templates fail
+ * with MFGPU_EINVAL. */
 mfgpu_status mfgpu_mf_initialize(mfgpu_mf *mf, const mfgpu_mf_params *params);
 /* MatchedFilter<T>::clear, src/matchedFilter.cpp:501-504 */
 mfgpu_status mfgpu_mf_clear(mfgpu_mf *mf);
@@ -194,7 +202,8 @@ mfgpu_status mfgpu_mf_get_plan(const mfgpu_mf *mf, int *fft_length, int *lags_pe
 mfgpu_status mfgpu_mf_get_correlator(const mfgpu_mf *mf, int *variant, int *tc_group, int *tc_k);
 /* Length buckets chosen at initialize: their number, and for each (up to
  * max, shortest templates first, the primary plan last) the FFT length and
- * the number of templates.  Extension: the reference has one FFT length. */
+ * the number of templates (templates correlated directly in the time domain
+ * belong to no bucket).  Extension: the reference has one FFT length. */
 mfgpu_status mfgpu_mf_get_buckets(const mfgpu_mf *mf, int max, int *fft_lengths, int *n_templates, int *count);
 /* Per length bucket (same order, up to max): lags per block and the FFT
  * organisation numbered like correlator_variant (4 for the tensor-core

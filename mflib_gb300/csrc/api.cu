@@ -219,7 +219,12 @@ struct mfgpu_mf
     long ldrs = 0, ldc = 0, fx_nchunks = 0;
     DevBuf rstat, cst, fxbits, fxlist, fxcount, tc_off, fx_btid, fx_boff, fx_bL, fx_bco, fx_bsum, pk_dirty,
         fx_cb0, fx_cnb;
-    int fx_nbmax = 0;
+    int fx_nbmax = 0, fx_lmax = 0;
+    // templates longer than any FFT plan takes: correlated directly (batches
+    // dir_b0 .. dir_b0 + dir_nb - 1 of the fix-up tables)
+    int n_direct = 0, dir_b0 = 0, dir_nb = 0, dir_lmax = 0;
+    int fLen = 0;  // longest template of the FFT plans (their shared length when all are equal)
+    DevBuf fx_bch;
     DevBuf tws;  // pass twiddles in the split layout (correlator mode 4)
     // length buckets beside the primary plan (longest templates); per
     // template its bucket's block length and block count, and the slot row
@@ -267,6 +272,7 @@ struct mfgpu_mf
     long long launches = 0;
     float last_xcorr_ms = 0, last_apply_ms = 0;
     bool test_wait_timeout = false;  // mfgpu_mf_test_wait_timeout: the next apply only
+    int dev_smem = 0;                // opt-in shared memory per block of the device
 
     size_t esz() const { return (size_t) prec; }
     template <class F> void each_buf(F &&f)
@@ -276,7 +282,7 @@ struct mfgpu_mf
                          &shifts_d, &weights_d, &specbuf, &den, &pk_cnt, &pk_idx, &pk_val, &xstage,
                          &xrange,   &tc_B,   &tc_bscale, &tc_grp_chan, &tc_grp_tid, &pk_flags,
                          &rstat,    &cst,    &fxbits, &fxlist, &fxcount, &tc_off, &fx_btid, &fx_boff,
-                         &fx_bL,    &fx_cb0, &fx_cnb,
+                         &fx_bL,    &fx_cb0, &fx_cnb, &fx_bch,
                          &fx_bco,   &fx_bsum, &pk_dirty, &tws};
         for (DevBuf *d : all) f(*d);
         pk.each_buf(f);
@@ -320,6 +326,7 @@ struct mfgpu_mf
         ldx = ldr = 0;
         fx_on = false;
         fx_L = fx_nden = fx_nruns = fx_nbatch = 0;
+        fx_nbmax = fx_lmax = n_direct = dir_b0 = dir_nb = dir_lmax = fLen = 0;
         ldrs = ldc = fx_nchunks = 0;
     }
 };
@@ -560,15 +567,54 @@ try
         mf->weights.assign(p->stack_weights, p->stack_weights + nt);
     }
 
+    // Templates longer than the longest FFT plan takes (S >= 32 lags per
+    // block: N - 31 samples) are correlated directly in the time domain
+    // (fixup_kernel in direct mode); the FFT plan below covers the others.
+    const int lcap = (2 << (mf->prec == 4 ? plan_limit_hi<float>() : plan_limit_hi<double>())) - 31;
+    std::vector<char> is_direct(nt, 0);
+    int ndirect = 0, fMax = 0, fMin = std::numeric_limits<int>::max();
+    for (int t = 0; t < nt; ++t)
+    {
+        if (mf->lens[t] > lcap)
+        {
+            is_direct[t] = 1;
+            ++ndirect;
+        }
+        else
+        {
+            fMax = std::max(fMax, mf->lens[t]);
+            fMin = std::min(fMin, mf->lens[t]);
+        }
+    }
+    const int ntf = nt - ndirect;
+    mf->n_direct = ndirect;
+    mf->fLen = ntf > 0 ? fMax : 0;
+    if (ndirect > 0)
+    {
+        if (p->correlator_variant == 4)
+            return fail(MFGPU_EINVAL, "correlator_variant 4 (tensor cores) takes templates of at most " +
+                                          std::to_string(lcap) + " samples");
+        int dev_smem0 = 0;
+        CU(cudaDeviceGetAttribute(&dev_smem0, cudaDevAttrMaxSharedMemoryPerBlockOptin, mf->dev));
+        if ((mf->prec == 4 ? fixup_warps<float>(maxLen, dev_smem0) : fixup_warps<double>(maxLen, dev_smem0)) < 1)
+            return fail(MFGPU_EINVAL, "template length " + std::to_string(maxLen) +
+                                          " exceeds the supported maximum of the direct correlator");
+    }
+    // the FFT plan sees its own templates only
+    maxLen = ntf > 0 ? fMax : 0;
+    minLen = ntf > 0 ? fMin : 0;
+    const int maxvalid_f = ntf > 0 ? n - fMin + 1 : 0;
+
     // ---- plan: FFT length (autotuned unless given), lags per block, groups
     std::vector<int> per_chan(nch, 0);
-    for (int t = 0; t < nt; ++t) per_chan[tchan[t]]++;
+    for (int t = 0; t < nt; ++t)
+        if (!is_direct[t]) per_chan[tchan[t]]++;
     int used_ch = 0, max_tpc = 0;
     for (int c = 0; c < nch; ++c) if (per_chan[c]) { ++used_ch; max_tpc = std::max(max_tpc, per_chan[c]); }
     const double tpc = (double) nt / std::max(1, used_ch);
     const int lo = mf->prec == 4 ? plan_limit_lo<float>() : plan_limit_lo<double>();
     const int hi = mf->prec == 4 ? plan_limit_hi<float>() : plan_limit_hi<double>();
-    bool all_equal = minLen == maxLen;
+    bool all_equal = ntf > 0 && minLen == maxLen;
     mf->shared_den = all_equal;
     // mode 3 normalises inside the CTA: no per-channel rows
     auto smem_of = [&](int l2p, int mode, int S) {
@@ -611,11 +657,12 @@ try
         const int bv = b < p->n_bucket_plans && p->bucket_variants ? p->bucket_variants[b] : 0;
         return bv == 0 ? -1 : bv == 5 ? 3 : bv == 6 ? 4 : bv - 1;
     };
-    const bool tc_candidate =
-        mf->tc || (p->correlator_variant == 0 && mf->prec == 4 && all_equal && p->fft_length == 0 && !bucket_forced);
+    const bool tc_candidate = mf->tc || (p->correlator_variant == 0 && mf->prec == 4 && all_equal &&
+                                         p->fft_length == 0 && !bucket_forced && ndirect == 0);
     int dev_smem = 0, sm_smem = 0;
     CU(cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, mf->dev));
     CU(cudaDeviceGetAttribute(&sm_smem, cudaDevAttrMaxSharedMemoryPerMultiprocessor, mf->dev));
+    mf->dev_smem = dev_smem;
     // CTAs per SM for a given shared-memory size (the register budget caps
     // the FP32 kernels at 2 per SM for P <= 2048 and 1 above, FP64 at 1)
     auto occupancy = [&](int l2p, size_t bytes) {
@@ -711,7 +758,7 @@ try
     std::vector<int> order(nt);
     for (int t = 0; t < nt; ++t) order[t] = t;
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return mf->lens[a] < mf->lens[b]; });
-    std::vector<int> cuts{0, nt};
+    std::vector<int> cuts{0, ntf};
     const int maxb = p->length_buckets > 0 ? p->length_buckets : 3;
     if (p->length_buckets < 0) return fail(MFGPU_EINVAL, "length_buckets must be >= 0");
     if (!all_equal && p->fft_length == 0 && (forced_mode <= 1 || forced_mode == 4) && maxb > 1)
@@ -719,10 +766,10 @@ try
         std::vector<int> pos{0};
         for (int q = 1; q < 64; ++q)
         {
-            const int i = (int) ((long) q * nt / 64);
-            if (i > pos.back() && i < nt && mf->lens[order[i]] != mf->lens[order[i - 1]]) pos.push_back(i);
+            const int i = (int) ((long) q * ntf / 64);
+            if (i > pos.back() && i < ntf && mf->lens[order[i]] != mf->lens[order[i - 1]]) pos.push_back(i);
         }
-        pos.push_back(nt);
+        pos.push_back(ntf);
         const int M = (int) pos.size();
         std::vector<double> bc((size_t) M * M, 1e300);
         for (int a = 0; a < M; ++a)
@@ -754,7 +801,7 @@ try
         if (p->length_buckets == 0 && dp[bk][M - 1] > 0.85 * dp[1][M - 1]) bk = 1;
         if (dp[bk][M - 1] < 1e299 && bk > 1)
         {
-            cuts.assign(1, nt);
+            cuts.assign(1, ntf);
             for (int k = bk, b = M - 1; k > 0; b = from[k][b], --k) cuts.push_back(pos[from[k][b]]);
             std::reverse(cuts.begin(), cuts.end());
         }
@@ -763,9 +810,11 @@ try
     std::vector<int> bucket_of(nt, nbk - 1);
     for (int b = 0; b < nbk; ++b)
         for (int i = cuts[b]; i < cuts[b + 1]; ++i) bucket_of[order[i]] = b;
-    const int mv0 = n - mf->lens[order[cuts[nbk - 1]]] + 1;
+    for (int t = 0; t < nt; ++t)
+        if (is_direct[t]) bucket_of[t] = -1;  // in no FFT plan
+    const int mv0 = ntf > 0 ? n - mf->lens[order[cuts[nbk - 1]]] + 1 : 0;
     const PlanPick best =
-        plan_for(maxLen, nbk > 1 ? mv0 : maxvalid, all_equal, bucket_nfft(nbk - 1), bucket_mode(nbk - 1));
+        plan_for(maxLen, nbk > 1 ? mv0 : maxvalid_f, all_equal, bucket_nfft(nbk - 1), bucket_mode(nbk - 1));
     if (best.l2p < 0 && (bucket_nfft(nbk - 1) > 0 || bucket_mode(nbk - 1) >= 0))
         return fail(MFGPU_EINVAL, "the plan override of bucket " + std::to_string(nbk - 1) + " does not fit");
     const int best_l2p = best.l2p, best_S = best.S, best_mode = best.mode;
@@ -773,7 +822,7 @@ try
     mf->mode_x = best_mode;
     if (best_mode == 3) mf->shared_den = false;
     // seconds per template-lag of the chosen FFT plan
-    const double fft_cost_per_lag = best_l2p >= 0 ? best_cost / std::max(1, maxvalid) : 1e30;
+    const double fft_cost_per_lag = best_l2p >= 0 ? best_cost / std::max(1, maxvalid_f) : 1e30;
     if (best_l2p < 0)
     {
         if (p->fft_length > 0)
@@ -786,7 +835,7 @@ try
     mf->log2p = best_l2p;
     mf->nfft = 2 << best_l2p;
     mf->S = best_S;
-    mf->nblocks = ((nbk > 1 ? mv0 : maxvalid) + best_S - 1) / best_S;
+    mf->nblocks = ((nbk > 1 ? mv0 : maxvalid_f) + best_S - 1) / best_S;
     for (int b = 0; b + 1 < nbk; ++b)
     {
         const int Lb = mf->lens[order[cuts[b + 1] - 1]], mv = n - mf->lens[order[cuts[b]]] + 1;
@@ -871,7 +920,13 @@ try
         mf->ldx = std::max<long>(mf->ldx, ((long) mf->nden * lpc + 32L * den_tail_runs(maxLen) + 63) / 64 * 64);
     }
     if (mf->tc) mf->shared_den = true;  // the tensor-core epilogue reads den_kernel's rows
-    if (mf->prec == 4)
+    if (ndirect > 0)
+    {
+        // the direct correlator stages L + 31 samples from the start of every run
+        mf->fx_nruns = (std::max(1, maxvalid) + 31) / 32;
+        mf->ldx = std::max<long>(mf->ldx, ((long) mf->fx_nruns * 32 + mf->maxLen + 32 + 63) / 64 * 64);
+    }
+    if (mf->prec == 4 && ntf > 0)
     {
         // accuracy safeguards: window statistics of the shared length (the
         // normalisation rows come from the same launch) or, for several
@@ -1014,9 +1069,9 @@ try
         std::vector<int> rs(nt), rn(nt);
         for (int t = 0; t < nt; ++t)
         {
-            const int b = bucket_of[t];
-            rs[t] = b == nbk - 1 ? mf->S : mf->xb[b]->S;
-            rn[t] = b == nbk - 1 ? mf->nblocks : mf->xb[b]->nblocks;
+            const int b = bucket_of[t];  // -1: a direct template, slots laid out like the primary plan's
+            rs[t] = b < 0 || b == nbk - 1 ? mf->S : mf->xb[b]->S;
+            rn[t] = b < 0 || b == nbk - 1 ? mf->nblocks : mf->xb[b]->nblocks;
         }
         CU(mf->row_S.ensure(sizeof(int) * nt));
         CU(mf->row_nblk.ensure(sizeof(int) * nt));
@@ -1040,20 +1095,22 @@ try
                           mf->tc_bscale.as<float>(), mf->stream));
         ++mf->launches;
     }
-    if (mf->fx_on)
+    if (mf->fx_on || ndirect > 0)
     {
-        // fix-up batches: each channel's templates sorted by length, kFixBatch
-        // per batch, coefficients interleaved [i][kFixBatch]
-        std::vector<int> btid, bL, cb0(nch), cnb(nch);
+        // Template batches, kFixBatch templates of one channel each,
+        // coefficients interleaved [i][kFixBatch]: first every channel's FFT
+        // templates sorted by length (the FP32 fix-up), then every channel's
+        // direct templates (the time-domain correlator)
+        std::vector<int> btid, bL, bch, cb0(nch, 0), cnb(nch, 0);
         std::vector<long> boff;
         long tot_co = 0;
         mf->fx_nbmax = 0;
-        for (int c = 0; c < nch; ++c)
-        {
-            cb0[c] = (int) bL.size();
-            cnb[c] = (int) ((chan_t[c].size() + kFixBatch - 1) / kFixBatch);
-            mf->fx_nbmax = std::max(mf->fx_nbmax, cnb[c]);
-            std::vector<int> ts = chan_t[c];
+        mf->fx_lmax = 0;
+        mf->dir_lmax = 0;
+        auto add_batches = [&](int c, bool direct) {
+            std::vector<int> ts;
+            for (int t : chan_t[c])
+                if ((bool) is_direct[t] == direct) ts.push_back(t);
             std::stable_sort(ts.begin(), ts.end(), [&](int a, int b) { return mf->lens[a] < mf->lens[b]; });
             for (size_t i = 0; i < ts.size(); i += kFixBatch)
             {
@@ -1065,23 +1122,41 @@ try
                     if (t >= 0) lb = std::max(lb, mf->lens[t]);
                 }
                 bL.push_back(lb);
+                bch.push_back(c);
                 boff.push_back(tot_co);
                 tot_co += (long) kFixBatch * lb;
+                if (direct) mf->dir_lmax = std::max(mf->dir_lmax, lb);
+                else mf->fx_lmax = std::max(mf->fx_lmax, lb);
             }
-        }
+            return (int) ((ts.size() + kFixBatch - 1) / kFixBatch);
+        };
+        if (mf->fx_on)
+            for (int c = 0; c < nch; ++c)
+            {
+                cb0[c] = (int) bL.size();
+                cnb[c] = add_batches(c, false);
+                mf->fx_nbmax = std::max(mf->fx_nbmax, cnb[c]);
+            }
+        mf->dir_b0 = (int) bL.size();
+        for (int c = 0; c < nch && ndirect > 0; ++c) add_batches(c, true);
+        mf->dir_nb = (int) bL.size() - mf->dir_b0;
         mf->fx_nbatch = (int) bL.size();
-        CU(mf->rstat.ensure(sizeof(float4) * (size_t) nch * mf->ldrs));
-        CU(mf->cst.ensure(sizeof(float2) * (size_t) nch * mf->ldc));
-        CU(mf->fxbits.ensure(sizeof(unsigned) * (size_t) nch * (mf->ldrs / 32)));
-        CU(mf->fxlist.ensure(sizeof(int) * (size_t) nch * mf->ldrs));
-        CU(mf->fxcount.ensure(sizeof(int)));
-        CU(cudaMemsetAsync(mf->fxcount.p, 0, sizeof(int), mf->stream));
-        if (mf->tc) CU(mf->tc_off.ensure(sizeof(float) * (size_t) nch * mf->tc_tiles));
+        if (mf->fx_on)
+        {
+            CU(mf->rstat.ensure(sizeof(float4) * (size_t) nch * mf->ldrs));
+            CU(mf->cst.ensure(sizeof(float2) * (size_t) nch * mf->ldc));
+            CU(mf->fxbits.ensure(sizeof(unsigned) * (size_t) nch * (mf->ldrs / 32)));
+            CU(mf->fxlist.ensure(sizeof(int) * (size_t) nch * mf->ldrs));
+            CU(mf->fxcount.ensure(sizeof(int)));
+            CU(cudaMemsetAsync(mf->fxcount.p, 0, sizeof(int), mf->stream));
+            if (mf->tc) CU(mf->tc_off.ensure(sizeof(float) * (size_t) nch * mf->tc_tiles));
+        }
         CU(mf->fx_btid.ensure(sizeof(int) * btid.size()));
         CU(mf->fx_boff.ensure(sizeof(long) * boff.size()));
         CU(mf->fx_bL.ensure(sizeof(int) * bL.size()));
-        CU(mf->fx_bco.ensure(sizeof(float) * (size_t) std::max<long>(1, tot_co)));
-        CU(mf->fx_bsum.ensure(sizeof(float) * nt));
+        CU(mf->fx_bch.ensure(sizeof(int) * bch.size()));
+        CU(mf->fx_bco.ensure(es * (size_t) std::max<long>(1, tot_co)));
+        CU(mf->fx_bsum.ensure(es * nt));
         CU(mf->fx_cb0.ensure(sizeof(int) * nch));
         CU(mf->fx_cnb.ensure(sizeof(int) * nch));
         CU(cudaMemcpyAsync(mf->fx_cb0.p, cb0.data(), sizeof(int) * nch, cudaMemcpyHostToDevice, mf->stream));
@@ -1089,9 +1164,15 @@ try
         CU(cudaMemcpyAsync(mf->fx_btid.p, btid.data(), sizeof(int) * btid.size(), cudaMemcpyHostToDevice, mf->stream));
         CU(cudaMemcpyAsync(mf->fx_boff.p, boff.data(), sizeof(long) * boff.size(), cudaMemcpyHostToDevice, mf->stream));
         CU(cudaMemcpyAsync(mf->fx_bL.p, bL.data(), sizeof(int) * bL.size(), cudaMemcpyHostToDevice, mf->stream));
-        CU(launch_fix_prep(mf->tmpl_d.as<double>(), mf->toff_d.as<long>(), mf->tlen_d.as<int>(), mf->fx_btid.as<int>(),
-                           mf->fx_boff.as<long>(), mf->fx_bL.as<int>(), mf->fx_nbatch, mf->fx_bco.as<float>(),
-                           mf->fx_bsum.as<float>(), mf->stream));
+        CU(cudaMemcpyAsync(mf->fx_bch.p, bch.data(), sizeof(int) * bch.size(), cudaMemcpyHostToDevice, mf->stream));
+        if (mf->prec == 4)
+            CU(launch_fix_prep<float>(mf->tmpl_d.as<double>(), mf->toff_d.as<long>(), mf->tlen_d.as<int>(),
+                                      mf->fx_btid.as<int>(), mf->fx_boff.as<long>(), mf->fx_bL.as<int>(), mf->fx_nbatch,
+                                      mf->fx_bco.as<float>(), mf->fx_bsum.as<float>(), mf->stream));
+        else
+            CU(launch_fix_prep<double>(mf->tmpl_d.as<double>(), mf->toff_d.as<long>(), mf->tlen_d.as<int>(),
+                                       mf->fx_btid.as<int>(), mf->fx_boff.as<long>(), mf->fx_bL.as<int>(),
+                                       mf->fx_nbatch, mf->fx_bco.as<double>(), mf->fx_bsum.as<double>(), mf->stream));
         ++mf->launches;
         if (!mf->n_sm) CU(cudaDeviceGetAttribute(&mf->n_sm, cudaDevAttrMultiProcessorCount, mf->dev));
         // the host vectors above must outlive the copies
@@ -1203,7 +1284,7 @@ try
     {
         const bool prim = b == nb - 1;
         if (fft_lengths) fft_lengths[b] = prim ? mf->nfft : mf->xb[b]->nfft;
-        if (n_templates) n_templates[b] = prim ? (mf->xb.empty() ? mf->nt : mf->ntemplates0) : mf->xb[b]->ntemplates;
+        if (n_templates) n_templates[b] = prim ? mf->ntemplates0 : mf->xb[b]->ntemplates;
     }
     return MFGPU_OK;
 }
@@ -1543,7 +1624,7 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
             ++mf->launches;
             if (mf->tc)
             {
-                CU(launch_fix_flag_tc(mf->x.as<float>(), mf->ldx, mf->maxLen, mf->rstat.as<float4>(), mf->ldrs,
+                CU(launch_fix_flag_tc(mf->x.as<float>(), mf->ldx, mf->fLen, mf->rstat.as<float4>(), mf->ldrs,
                                       mf->fx_nruns, mf->tc_tiles, mf->nch, mf->dead.as<unsigned char>(),
                                       mf->xrange.as<float>(), mf->tc_off.as<float>(),
                                       mf->fxbits.as<unsigned>(), mf->fxlist.as<int>(), mf->fxcount.as<int>(), kFixTcC1,
@@ -1574,7 +1655,7 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
     }
     if (mf->shared_den && !(sizeof(T) == 4 && mf->fx_on))
     {
-        CU(launch_den<T>(mf->x.as<T>(), mf->ldx, mf->maxLen, mf->den.as<T>(), mf->ldd, p.tol, mf->nden, mf->nch,
+        CU(launch_den<T>(mf->x.as<T>(), mf->ldx, mf->fLen, mf->den.as<T>(), mf->ldd, p.tol, mf->nden, mf->nch,
                          mf->stream));
         ++mf->launches;
     }
@@ -1660,29 +1741,29 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
     return MFGPU_OK;
 }
 
-// FP32: recomputes the runs the error bounds flagged (every template of the
-// run's channel), then recounts the fused peak candidates of the blocks it
-// touched.  Both kernels scan the flag bytes themselves, so the host never
-// waits for the flags; with no flagged run they only read the flags.
-static mfgpu_status mf_launch_fixup(mfgpu_mf *mf)
+// After the correlator: the FP32 fix-up of the runs the error bounds listed
+// (every template of the run's channel), and the direct time-domain
+// correlation of templates longer than any FFT plan takes (every run); then
+// the fused peak candidates of the blocks either touched are recounted.  The
+// fix-up reads the list's length from device memory, so the host never
+// waits for the bounds; with no listed run it returns at once.
+template <class T> static mfgpu_status mf_launch_fixup(mfgpu_mf *mf)
 {
-    FixParams f{};
-    f.x = mf->x.as<float>(); f.ldx = mf->ldx;
-    f.rho = mf->rho.as<float>(); f.ldr = mf->ldr;
-    f.flist = mf->fxlist.as<int>(); f.fcount = mf->fxcount.as<int>(); f.ldf = mf->ldrs;
-    f.nruns = mf->fx_nruns; f.nbmax = mf->fx_nbmax;
-    f.chan_b0 = mf->fx_cb0.as<int>(); f.chan_nb = mf->fx_cnb.as<int>();
+    FixParams<T> f{};
+    f.x = mf->x.as<T>(); f.ldx = mf->ldx;
+    f.rho = mf->rho.as<T>(); f.ldr = mf->ldr;
+    f.ldf = mf->ldrs; f.nruns = mf->fx_nruns;
+    f.bch = mf->fx_bch.as<int>(); f.dead = mf->dead.as<unsigned char>();
     f.btid = mf->fx_btid.as<int>(); f.boff = mf->fx_boff.as<long>();
-    f.bL = mf->fx_bL.as<int>(); f.bco = mf->fx_bco.as<float>(); f.bsum = mf->fx_bsum.as<float>();
+    f.bL = mf->fx_bL.as<int>(); f.bco = mf->fx_bco.as<T>(); f.bsum = mf->fx_bsum.as<T>();
     f.tlen = mf->tlen_d.as<int>(); f.nvalid = mf->nvalid_d.as<int>();
-    f.tol = 1.e-6f;  // src/matchedFilter.cpp:1287
-    f.Lmax = mf->maxLen;
+    f.tol = sizeof(T) == 4 ? (T) 1.e-6 : (T) 1.e-12;  // src/matchedFilter.cpp:1287 / :1115
     const bool fused = mf->pk_fused && !mf->tc;
     if (mf->pk_fused && mf->tc)
     {
         f.pk_flags = mf->pk_flags.as<unsigned>();
         f.pk_words = mf->pk_words;
-        f.pk_thr = (float) mf->pk_fused_thr;
+        f.pk_thr = (T) mf->pk_fused_thr;
         f.pk_len = mf->pk_fused_len;
     }
     if (fused)
@@ -1695,15 +1776,33 @@ static mfgpu_status mf_launch_fixup(mfgpu_mf *mf)
         f.row_S = mf->xb.empty() ? nullptr : mf->row_S.as<int>();
         f.S0 = mf->S;
     }
-    CU(launch_fixup(f, 4 * std::max(1, mf->n_sm), mf->stream));
-    ++mf->launches;
+    const int nctas = 4 * std::max(1, mf->n_sm);
+    if (mf->fx_on && mf->nblocks > 0)
+    {
+        FixParams<T> g = f;
+        g.flist = mf->fxlist.as<int>(); g.fcount = mf->fxcount.as<int>();
+        g.nbmax = mf->fx_nbmax;
+        g.chan_b0 = mf->fx_cb0.as<int>(); g.chan_nb = mf->fx_cnb.as<int>();
+        g.Lmax = mf->fx_lmax;
+        CU(launch_fixup<T>(g, nctas, fixup_warps<T>(g.Lmax, mf->dev_smem), mf->stream));
+        ++mf->launches;
+    }
+    if (mf->n_direct > 0)
+    {
+        FixParams<T> g = f;
+        g.flist = nullptr;
+        g.dir_b0 = mf->dir_b0; g.ndir = mf->dir_nb;
+        g.Lmax = mf->dir_lmax;
+        CU(launch_fixup<T>(g, nctas, fixup_warps<T>(g.Lmax, mf->dev_smem), mf->stream));
+        ++mf->launches;
+    }
     if (fused)
     {
-        CU(launch_fix_rescan(mf->rho.as<float>(), mf->ldr, mf->nt, mf->pk_stride, mf->pk_dirty.as<unsigned char>(),
-                             mf->xb.empty() ? nullptr : mf->row_S.as<int>(),
-                             mf->xb.empty() ? nullptr : mf->row_nblk.as<int>(), mf->S, mf->nblocks,
-                             mf->nvalid_d.as<int>(), mf->pk_fused_len, (float) mf->pk_fused_thr,
-                             mf->pk_cnt.as<int>(), mf->pk_idx.as<int>(), mf->pk_val.as<float>(), mf->stream));
+        CU(launch_fix_rescan<T>(mf->rho.as<T>(), mf->ldr, mf->nt, mf->pk_stride, mf->pk_dirty.as<unsigned char>(),
+                                mf->xb.empty() ? nullptr : mf->row_S.as<int>(),
+                                mf->xb.empty() ? nullptr : mf->row_nblk.as<int>(), mf->S, mf->nblocks,
+                                mf->nvalid_d.as<int>(), mf->pk_fused_len, (T) mf->pk_fused_thr, mf->pk_cnt.as<int>(),
+                                mf->pk_idx.as<int>(), mf->pk_val.as<T>(), mf->stream));
         ++mf->launches;
     }
     return MFGPU_OK;
@@ -1724,9 +1823,9 @@ static mfgpu_status mf_apply_body(mfgpu_mf *mf)
         CU(mf_record(mf, mf->ev[1]));
     }
     CU(mf_record(mf, mf->ev[2]));
-    if (mf->nblocks > 0 && mf->fx_on)
+    if ((mf->nblocks > 0 && mf->fx_on) || mf->n_direct > 0)
     {
-        mfgpu_status st = mf_launch_fixup(mf);
+        mfgpu_status st = mf->prec == 4 ? mf_launch_fixup<float>(mf) : mf_launch_fixup<double>(mf);
         if (st != MFGPU_OK) return st;
     }
     CU(mf_record(mf, mf->ev[3]));

@@ -1,4 +1,4 @@
-// fix_params.h -- parameters of the FP32 fix-up kernel (kernels_fix.cuh),
+// fix_params.h -- parameters of the fix-up kernel (kernels_fix.cuh),
 // shared by the host code that fills them.
 #pragma once
 
@@ -22,34 +22,40 @@ constexpr float kFixTcC1 = 2.0e-6f;
 constexpr float kFixTcC2 = 0x1p-23f;
 
 // Fix-up batches: the templates of a channel sorted by length, kFixBatch per
-// batch; coefficients (demeaned, unit norm, FP32) interleaved as
-// [i][kFixBatch] and zero past each template's length.
-struct FixParams
+// batch; coefficients (demeaned, unit norm, in the sample type) interleaved
+// as [i][kFixBatch] and zero past each template's length.  Two uses of the
+// same kernel: the FP32 fix-up of listed runs (flist), and the direct
+// time-domain correlation of templates too long for any FFT plan (every run
+// of batches dir_b0 .. dir_b0 + ndir - 1, both sample types).
+template <class T> struct FixParams
 {
-    const float *x;
+    const T *x;
     long ldx;
-    float *rho;
+    T *rho;
     long ldr;
-    const int *flist;            // listed runs: c * ldf + r
+    const int *flist;            // listed runs: c * ldf + r (null: direct mode)
     const int *fcount;           // number of listed runs
     long ldf;
-    int nruns;                   // runs per channel row that may be listed
-    int nbmax;                   // most batches of one channel
-    const int *chan_b0;          // first batch of each channel
-    const int *chan_nb;          // batches of each channel
+    int nruns;                   // runs per channel row
+    int nbmax;                   // most batches of one channel (list mode)
+    const int *chan_b0;          // first batch of each channel (list mode)
+    const int *chan_nb;          // batches of each channel (list mode)
+    int dir_b0, ndir;            // direct mode: the batches to correlate
+    const int *bch;              // channel of each batch
+    const unsigned char *dead;   // per channel dead-trace flag (direct mode writes zeros)
     const int *btid;             // [nbatch][kFixBatch] template ids, -1 empty
     const long *boff;            // first coefficient of each batch in bco
     const int *bL;               // longest template of each batch
-    const float *bco;
-    const float *bsum;           // per template: sum of its FP32 coefficients
+    const T *bco;
+    const T *bsum;               // per template: sum of its rounded coefficients
     const int *tlen;
     const int *nvalid;
-    float tol;
-    int Lmax;                    // longest template (shared-memory rows)
+    T tol;
+    int Lmax;                    // longest template of the batches (shared-memory rows)
     // tensor-core candidate flags (one bit per 64 lags of each row), or null
     unsigned *pk_flags;
     int pk_words;
-    float pk_thr;
+    T pk_thr;
     int pk_len;
     // fused FFT candidates: a byte per (template, block) slot to recount, or null
     unsigned char *pk_dirty;

@@ -1,4 +1,4 @@
-// fixup.cu -- launchers of the FP32 accuracy safeguards (kernels_fix.cuh).
+// fixup.cu -- launchers of the accuracy safeguards and the direct correlator (kernels_fix.cuh).
 #include "launch.h"
 #include "kernels_fix.cuh"
 
@@ -33,37 +33,55 @@ cudaError_t launch_fix_flag_tc(const float *x, long ldx, int L, const float4 *rs
     return cudaGetLastError();
 }
 
-size_t fixup_smem_bytes(int Lmax)
+template <class T> int fixup_warps(int Lmax, int dev_smem)
 {
-    return sizeof(float) * (size_t) kFixWarps * (((Lmax + 64 + 3) & ~3) + kFixBatch * kFixChunk);
+    const size_t w = fix_warp_bytes<T>(Lmax);
+    const int k = (int) ((size_t) dev_smem / w);
+    return k < 1 ? 0 : (k < kFixWarps ? k : kFixWarps);
 }
+template int fixup_warps<float>(int, int);
+template int fixup_warps<double>(int, int);
 
+template <class T>
 cudaError_t launch_fix_prep(const double *tmpl, const long *toff, const int *tlen, const int *btid, const long *boff,
-                            const int *bL, int nbatch, float *bco, float *bsum, cudaStream_t s)
+                            const int *bL, int nbatch, T *bco, T *bsum, cudaStream_t s)
 {
-    fix_prep_kernel<<<nbatch * kFixBatch, 256, 0, s>>>(tmpl, toff, tlen, btid, boff, bL, bco, bsum);
+    fix_prep_kernel<T><<<nbatch * kFixBatch, 256, 0, s>>>(tmpl, toff, tlen, btid, boff, bL, bco, bsum);
     return cudaGetLastError();
 }
+template cudaError_t launch_fix_prep<float>(const double *, const long *, const int *, const int *, const long *,
+                                            const int *, int, float *, float *, cudaStream_t);
+template cudaError_t launch_fix_prep<double>(const double *, const long *, const int *, const int *, const long *,
+                                             const int *, int, double *, double *, cudaStream_t);
 
-cudaError_t launch_fixup(const FixParams &p, int nctas, cudaStream_t s)
+template <class T> cudaError_t launch_fixup(const FixParams<T> &p, int nctas, int warps, cudaStream_t s)
 {
-    const size_t bytes = fixup_smem_bytes(p.Lmax);
+    const size_t bytes = (size_t) warps * fix_warp_bytes<T>(p.Lmax);
     static SmemCap cap;
-    cudaError_t e = raise_smem_cap(fixup_kernel, bytes, cap);
+    cudaError_t e = raise_smem_cap(fixup_kernel<T>, bytes, cap);
     if (e != cudaSuccess) return e;
-    fixup_kernel<<<nctas, 32 * kFixWarps, bytes, s>>>(p);
+    fixup_kernel<T><<<nctas, 32 * warps, bytes, s>>>(p);
     return cudaGetLastError();
 }
+template cudaError_t launch_fixup<float>(const FixParams<float> &, int, int, cudaStream_t);
+template cudaError_t launch_fixup<double>(const FixParams<double> &, int, int, cudaStream_t);
 
-cudaError_t launch_fix_rescan(const float *rho, long ldr, int nt, int pk_stride, const unsigned char *dirty,
+template <class T>
+cudaError_t launch_fix_rescan(const T *rho, long ldr, int nt, int pk_stride, const unsigned char *dirty,
                               const int *row_S, const int *row_nblk, int S0, int nblk0, const int *nvalid, int pk_len,
-                              float thr, int *cnt, int *idx, float *val, cudaStream_t s)
+                              T thr, int *cnt, int *idx, T *val, cudaStream_t s)
 {
     const long ns = (long) nt * pk_stride;
     const long warps = (ns + 31) / 32;
-    fix_rescan_kernel<<<(unsigned) ((warps + 7) / 8), 256, 0, s>>>(rho, ldr, nt, pk_stride, dirty, row_S, row_nblk, S0,
-                                                                    nblk0, nvalid, pk_len, thr, cnt, idx, val);
+    fix_rescan_kernel<T><<<(unsigned) ((warps + 7) / 8), 256, 0, s>>>(rho, ldr, nt, pk_stride, dirty, row_S, row_nblk,
+                                                                       S0, nblk0, nvalid, pk_len, thr, cnt, idx, val);
     return cudaGetLastError();
 }
+template cudaError_t launch_fix_rescan<float>(const float *, long, int, int, const unsigned char *, const int *,
+                                              const int *, int, int, const int *, int, float, int *, int *, float *,
+                                              cudaStream_t);
+template cudaError_t launch_fix_rescan<double>(const double *, long, int, int, const unsigned char *, const int *,
+                                               const int *, int, int, const int *, int, double, int *, int *,
+                                               double *, cudaStream_t);
 
 }  // namespace mfgpu

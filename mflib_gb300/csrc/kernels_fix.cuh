@@ -32,7 +32,9 @@
 //     channel by a direct two-pass FP32 Pearson correlation about a local
 //     reference, whose error is relative to each window's own variance.  The
 //     fused peak candidates of the touched blocks are recounted
-//     (fix_rescan_kernel) and the tensor-core candidate flags updated.
+//     (fix_rescan_kernel) and the tensor-core candidate flags updated.  The
+//     same kernel, in direct mode and in either sample type, correlates the
+//     templates too long for any FFT plan over every lag.
 #pragma once
 #include "kernels_mf.cuh"
 #include "fix_params.h"
@@ -359,16 +361,17 @@ __global__ void __launch_bounds__(256) fix_flag_tc_kernel(const float *x, long l
 
 // Coefficient table of the fix-up batches: one CTA per (batch, slot).  The
 // template is demeaned and unit-normed in FP64 (as for the spectra), rounded
-// to FP32; bsum receives the sum of the rounded coefficients.
+// to T; bsum receives the sum of the rounded coefficients.
+template <class T>
 __global__ void __launch_bounds__(256) fix_prep_kernel(const double *tmpl, const long *toff, const int *tlen,
-                                                      const int *btid, const long *boff, const int *bL, float *bco,
-                                                      float *bsum)
+                                                      const int *btid, const long *boff, const int *bL, T *bco,
+                                                      T *bsum)
 {
     __shared__ double red[8];
     const int B = blockIdx.x / kFixBatch, k = blockIdx.x % kFixBatch;
     const int t = btid[B * kFixBatch + k];
     const int Lb = bL[B];
-    float *dst = bco + boff[B] + k;
+    T *dst = bco + boff[B] + k;
     auto bsum_d = [&](double v) {
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         __syncthreads();
@@ -380,7 +383,7 @@ __global__ void __launch_bounds__(256) fix_prep_kernel(const double *tmpl, const
     };
     if (t < 0)
     {
-        for (int i = threadIdx.x; i < Lb; i += 256) dst[(long) i * kFixBatch] = 0.f;
+        for (int i = threadIdx.x; i < Lb; i += 256) dst[(long) i * kFixBatch] = (T) 0;
         return;
     }
     const int L = tlen[t];
@@ -395,101 +398,123 @@ __global__ void __launch_bounds__(256) fix_prep_kernel(const double *tmpl, const
     double cs = 0;
     for (int i = threadIdx.x; i < Lb; i += 256)
     {
-        const float v = i < L ? (float) ((b[i] - mean) * inv) : 0.f;
+        const T v = i < L ? (T) ((b[i] - mean) * inv) : (T) 0;
         dst[(long) i * kFixBatch] = v;
         cs += (double) v;
     }
     cs = bsum_d(cs);
-    if (threadIdx.x == 0) bsum[t] = (float) cs;
+    if (threadIdx.x == 0) bsum[t] = (T) cs;
 }
 
-__device__ __forceinline__ float fix_rho(float num, float M2, int L, float tol)
+template <class T> __device__ __forceinline__ T fix_rho(T num, T M2, int L, T tol)
 {
-    if (!(M2 > 0.f)) return 0.f;
-    const float r = num * DenOps<float>::out((float) L * M2, sqrtf((float) L), tol);
+    if (!(M2 > (T) 0)) return (T) 0;
+    const T r = num * DenOps<T>::out((T) L * M2, sqrt((T) L), tol);
     return clamp_rho(r);
 }
 
-// Work item j of the fix-up: listed run i = j / nbmax, the k-th batch of
-// that run's channel (k = j % nbmax, items past the channel's batches are
-// skipped), one warp per item, grid-strided, so the runs of one step (which
-// cluster) spread over every warp.  Per item, the 32 lags of each template of
-// the batch: dot products against the window's samples about a local
-// reference (coefficients staged kFixChunk at a time in shared memory),
-// window mean and M2 two-pass per distinct template length.
-__global__ void __launch_bounds__(32 * kFixWarps, 4) fixup_kernel(FixParams p)
+// Shared-memory row of samples per warp (a multiple of 16 bytes) and the
+// warp's share: the row plus one staged chunk of coefficients.
+template <class T> __host__ __device__ constexpr int fix_yrow(int Lmax) { return (Lmax + 64 + 3) & ~3; }
+template <class T> __host__ __device__ constexpr size_t fix_warp_bytes(int Lmax)
 {
-    extern __shared__ __align__(16) float smem_fx[];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int yrow = (p.Lmax + 64 + 3) & ~3;  // samples row, a multiple of 16 bytes
-    float *ys = smem_fx + (size_t) wid * (yrow + kFixBatch * kFixChunk);
-    float4 *cs4 = reinterpret_cast<float4 *>(ys + yrow);
-    const long W = (long) gridDim.x * kFixWarps;
-    const long U = (long) *p.fcount * p.nbmax;
-    for (long j = (long) blockIdx.x * kFixWarps + wid; j < U; j += W)
+    return sizeof(T) * ((size_t) fix_yrow<T>(Lmax) + kFixBatch * kFixChunk);
+}
+
+// One warp per work item, grid-strided (blockDim.x / 32 warps per CTA).
+// List mode: item j is listed run i = j / nbmax with the k-th batch of its
+// channel (k = j % nbmax; items past the channel's batches are skipped), so
+// the runs of one amplitude step (which cluster) spread over every warp.
+// Direct mode: item j is run j / ndir of direct batch j % ndir.  Per item,
+// the 32 lags of each template of the batch: dot products against the
+// window's samples about a local reference (coefficients staged kFixChunk at
+// a time in shared memory), window mean and M2 two-pass per distinct
+// template length.
+template <class T> __global__ void __launch_bounds__(32 * kFixWarps) fixup_kernel(FixParams<T> p)
+{
+    extern __shared__ __align__(16) unsigned char smem_fx_raw[];
+    T *smem_fx = reinterpret_cast<T *>(smem_fx_raw);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int yrow = fix_yrow<T>(p.Lmax);
+    T *ys = smem_fx + (size_t) wid * (yrow + kFixBatch * kFixChunk);
+    T *csh = ys + yrow;
+    const long W = (long) gridDim.x * nw;
+    const bool direct = p.flist == nullptr;
+    const long U = direct ? (long) p.nruns * p.ndir : (long) *p.fcount * p.nbmax;
+    for (long j = (long) blockIdx.x * nw + wid; j < U; j += W)
     {
-        const int e = p.flist[j / p.nbmax], k = (int) (j % p.nbmax);
-        const int c = (int) (e / p.ldf), r = (int) (e % p.ldf);
-        if (k >= p.chan_nb[c] || r >= p.nruns) continue;
-        const int B = p.chan_b0[c] + k;
+        int B, c, r;
+        if (direct)
+        {
+            B = p.dir_b0 + (int) (j % p.ndir);
+            r = (int) (j / p.ndir);
+            c = p.bch[B];
+        }
+        else
+        {
+            const int e = p.flist[j / p.nbmax], k = (int) (j % p.nbmax);
+            c = (int) (e / p.ldf);
+            r = (int) (e % p.ldf);
+            if (k >= p.chan_nb[c] || r >= p.nruns) continue;
+            B = p.chan_b0[c] + k;
+        }
         const int Lb = p.bL[B];
         const int mytid = lane < kFixBatch ? p.btid[B * kFixBatch + lane] : -1;
         const int L0 = __shfl_sync(0xffffffffu, mytid >= 0 ? p.tlen[mytid] : 0, 0);
-        const float *xc = p.x + (long) c * p.ldx;
-        const float4 *co = reinterpret_cast<const float4 *>(p.bco + p.boff[B]);
+        const T *xc = p.x + (long) c * p.ldx;
         const long lag0 = 32L * r;
-        const float Rref = xc[lag0 + 16 + L0 / 2];
-        for (int i = lane; i < Lb + 31; i += 32) ys[i] = xc[lag0 + i] - Rref;
-        float acc[kFixBatch];
+        const bool dead = direct && p.dead[c];
+        T acc[kFixBatch];
 #pragma unroll
-        for (int q = 0; q < kFixBatch; ++q) acc[q] = 0.f;
-        constexpr int V4 = kFixBatch / 4;  // float4 per coefficient index
-        for (int i0 = 0; i0 < Lb; i0 += kFixChunk)
+        for (int q = 0; q < kFixBatch; ++q) acc[q] = (T) 0;
+        if (!dead)
         {
-            const int ni = min(kFixChunk, Lb - i0);
-            __syncwarp();  // the previous chunk (and, first, the samples) fully read / written
-            for (int v = lane; v < ni * V4; v += 32) cs4[v] = co[(long) i0 * V4 + v];
-            __syncwarp();
-#pragma unroll 4
-            for (int i = 0; i < ni; ++i)
+            const uint4 *co = reinterpret_cast<const uint4 *>(p.bco + p.boff[B]);
+            uint4 *cs4 = reinterpret_cast<uint4 *>(csh);
+            constexpr int V4 = kFixBatch * (int) sizeof(T) / 16;  // 16-byte pieces per coefficient index
+            const T Rref = xc[lag0 + 16 + L0 / 2];
+            for (int i = lane; i < Lb + 31; i += 32) ys[i] = xc[lag0 + i] - Rref;
+            for (int i0 = 0; i0 < Lb; i0 += kFixChunk)
             {
-                const float yv = ys[lane + i0 + i];
-#pragma unroll
-                for (int q = 0; q < V4; ++q)
+                const int ni = min(kFixChunk, Lb - i0);
+                __syncwarp();  // the previous chunk (and, first, the samples) fully read / written
+                for (int v = lane; v < ni * V4; v += 32) cs4[v] = co[(long) i0 * V4 + v];
+                __syncwarp();
+#pragma unroll 4
+                for (int i = 0; i < ni; ++i)
                 {
-                    const float4 cf = cs4[i * V4 + q];
-                    acc[4 * q] = fmaf(cf.x, yv, acc[4 * q]);
-                    acc[4 * q + 1] = fmaf(cf.y, yv, acc[4 * q + 1]);
-                    acc[4 * q + 2] = fmaf(cf.z, yv, acc[4 * q + 2]);
-                    acc[4 * q + 3] = fmaf(cf.w, yv, acc[4 * q + 3]);
+                    const T yv = ys[lane + i0 + i];
+                    const T *cf = csh + i * kFixBatch;
+#pragma unroll
+                    for (int q = 0; q < kFixBatch; ++q) acc[q] = fma(cf[q], yv, acc[q]);
                 }
             }
         }
         const long lag = lag0 + lane;
         int prevL = -1;
-        float mu = 0.f, M2 = 0.f;
+        T mu = 0, M2 = 0;
 #pragma unroll
         for (int q = 0; q < kFixBatch; ++q)
         {
             const int t = __shfl_sync(0xffffffffu, mytid, q);
             if (t < 0) continue;  // empty slots (the batch's last ones)
             const int Lt = p.tlen[t];
-            if (Lt != prevL)
+            if (!dead && Lt != prevL)
             {
-                float s = 0.f;
+                T s = 0;
                 for (int i = 0; i < Lt; ++i) s += ys[lane + i];
-                mu = s / (float) Lt;
-                float a = 0.f, b = 0.f;
+                mu = s / (T) Lt;
+                T a = 0, b = 0;
                 for (int i = 0; i < Lt; ++i)
                 {
-                    const float d = ys[lane + i] - mu;
+                    const T d = ys[lane + i] - mu;
                     a += d;
-                    b = fmaf(d, d, b);
+                    b = fma(d, d, b);
                 }
-                M2 = fmaf(-a, a / (float) Lt, b);
+                M2 = fma(-a, a / (T) Lt, b);
                 prevL = Lt;
             }
-            const float rho = fix_rho(fmaf(-mu, p.bsum[t], acc[q]), M2, Lt, p.tol);
+            const T rho = dead ? (T) 0 : fix_rho<T>(fma(-mu, p.bsum[t], acc[q]), M2, Lt, p.tol);
             if (lag < p.nvalid[t])
             {
                 p.rho[(long) t * p.ldr + lag] = rho;
@@ -514,10 +539,11 @@ __global__ void __launch_bounds__(32 * kFixWarps, 4) fixup_kernel(FixParams p)
 // Recounts the fused candidates of every (template, block) slot marked by the
 // fix-up: body lags [bS + 1, bS + S - 2] of the trace under the correlator's
 // rule.  One warp per 32 slots.
-__global__ void __launch_bounds__(256) fix_rescan_kernel(const float *rho, long ldr, int nt, int pk_stride,
+template <class T>
+__global__ void __launch_bounds__(256) fix_rescan_kernel(const T *rho, long ldr, int nt, int pk_stride,
                                                         const unsigned char *dirty, const int *row_S,
                                                         const int *row_nblk, int S0, int nblk0, const int *nvalid,
-                                                        int pk_len, float thr, int *cnt, int *idx, float *val)
+                                                        int pk_len, T thr, int *cnt, int *idx, T *val)
 {
     const int lane = threadIdx.x & 31;
     const long s0 = ((long) blockIdx.x * 8 + (threadIdx.x >> 5)) * 32;
@@ -533,21 +559,21 @@ __global__ void __launch_bounds__(256) fix_rescan_kernel(const float *rho, long 
         const long S = row_S ? row_S[t] : S0;
         const int nb = row_nblk ? row_nblk[t] : nblk0;
         if (b >= nb) continue;
-        const float *R = rho + (long) t * ldr;
+        const T *R = rho + (long) t * ldr;
         const long k0 = (long) b * S, nv = nvalid[t];
         int total = 0;
         for (long l0 = 1; l0 <= S - 2; l0 += 32)
         {
             const long l = l0 + lane;
             bool cnd = false;
-            float xi = 0.f;
+            T xi = 0;
             if (l <= S - 2 && k0 + l < pk_len)
             {
                 xi = R[k0 + l];
                 if (xi > thr)
                 {
-                    const float xr = k0 + l + 1 < nv ? R[k0 + l + 1] : 0.f;
-                    cnd = cand_rule<float>(R[k0 + l - 1], xi, xr, k0 + l, pk_len, thr);
+                    const T xr = k0 + l + 1 < nv ? R[k0 + l + 1] : (T) 0;
+                    cnd = cand_rule<T>(R[k0 + l - 1], xi, xr, k0 + l, pk_len, thr);
                 }
             }
             const unsigned bm = __ballot_sync(0xffffffffu, cnd);

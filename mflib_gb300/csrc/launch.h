@@ -61,13 +61,17 @@ cudaError_t launch_fix_flag_fft(const float2 *cst, long ldc, long nchunks, int S
 cudaError_t launch_fix_flag_tc(const float *x, long ldx, int L, const float4 *rstat, long ldrs, int nruns, int tiles,
                                int nch, const unsigned char *dead, const float *xrange, float *off, unsigned *fbits,
                                int *flist, int *fcount, float c1, float c2, float tau, cudaStream_t s);
-size_t fixup_smem_bytes(int Lmax);
+// warps per fix-up CTA whose sample rows (templates up to Lmax) fit dev_smem
+// bytes (0: none fits)
+template <class T> int fixup_warps(int Lmax, int dev_smem);
+template <class T>
 cudaError_t launch_fix_prep(const double *tmpl, const long *toff, const int *tlen, const int *btid, const long *boff,
-                            const int *bL, int nbatch, float *bco, float *bsum, cudaStream_t s);
-cudaError_t launch_fixup(const FixParams &p, int nctas, cudaStream_t s);
-cudaError_t launch_fix_rescan(const float *rho, long ldr, int nt, int pk_stride, const unsigned char *dirty,
+                            const int *bL, int nbatch, T *bco, T *bsum, cudaStream_t s);
+template <class T> cudaError_t launch_fixup(const FixParams<T> &p, int nctas, int warps, cudaStream_t s);
+template <class T>
+cudaError_t launch_fix_rescan(const T *rho, long ldr, int nt, int pk_stride, const unsigned char *dirty,
                               const int *row_S, const int *row_nblk, int S0, int nblk0, const int *nvalid, int pk_len,
-                              float thr, int *cnt, int *idx, float *val, cudaStream_t s);
+                              T thr, int *cnt, int *idx, T *val, cudaStream_t s);
 // single-channel detector (kernels_detect.cuh): reduction across templates,
 // per-template transformed traces, per-detection refinement and amplitudes
 template <class T>
