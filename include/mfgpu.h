@@ -114,6 +114,12 @@ typedef struct
     int n_bucket_plans;
     const int *bucket_fft_lengths;
     const int *bucket_variants;
+    /* Extension: 1 = run the FFT correlator as one persistent launch whose
+       CTAs take (template group, signal block) tiles from a device ticket
+       instead of a static grid (FP32, two-team organisations 3 and 6, FFT
+       length >= 4096; ignored otherwise).  0 = the static grid, which
+       measured faster on GB300. */
+    int persistent;
 } mfgpu_mf_params;
 
 /* MatchedFilter<T>::MatchedFilter(); precision MFGPU_FLOAT32 | MFGPU_FLOAT64 */

@@ -73,6 +73,7 @@ class MfgpuParams(C.Structure):
         ("n_bucket_plans", C.c_int),
         ("bucket_fft_lengths", C.POINTER(C.c_int)),
         ("bucket_variants", C.POINTER(C.c_int)),
+        ("persistent", C.c_int),
     ]
 
 

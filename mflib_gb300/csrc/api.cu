@@ -226,6 +226,7 @@ struct mfgpu_mf
     int fLen = 0;  // longest template of the FFT plans (their shared length when all are equal)
     DevBuf fx_bch;
     DevBuf tws;  // pass twiddles in the split layout (correlator mode 4)
+    DevBuf tickets;  // one persistent-launch ticket per correlator launch of an apply
     // length buckets beside the primary plan (longest templates); per
     // template its bucket's block length and block count, and the slot row
     // stride of the gathered candidates (the largest block count)
@@ -273,6 +274,7 @@ struct mfgpu_mf
     float last_xcorr_ms = 0, last_apply_ms = 0;
     bool test_wait_timeout = false;  // mfgpu_mf_test_wait_timeout: the next apply only
     int dev_smem = 0;                // opt-in shared memory per block of the device
+    bool persistent = false;         // FFT correlator as a persistent work-queue launch (option)
 
     size_t esz() const { return (size_t) prec; }
     template <class F> void each_buf(F &&f)
@@ -283,7 +285,7 @@ struct mfgpu_mf
                          &xrange,   &tc_B,   &tc_bscale, &tc_grp_chan, &tc_grp_tid, &pk_flags,
                          &rstat,    &cst,    &fxbits, &fxlist, &fxcount, &tc_off, &fx_btid, &fx_boff,
                          &fx_bL,    &fx_cb0, &fx_cnb, &fx_bch,
-                         &fx_bco,   &fx_bsum, &pk_dirty, &tws};
+                         &fx_bco,   &fx_bsum, &pk_dirty, &tws, &tickets};
         for (DevBuf *d : all) f(*d);
         pk.each_buf(f);
         f(row_S);
@@ -589,6 +591,7 @@ try
     const int ntf = nt - ndirect;
     mf->n_direct = ndirect;
     mf->fLen = ntf > 0 ? fMax : 0;
+    mf->persistent = p->persistent != 0;
     if (ndirect > 0)
     {
         if (p->correlator_variant == 4)
@@ -1716,6 +1719,19 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
             return MFGPU_OK;
         }
     }
+    // persistent launches (an option): one ticket per correlator launch,
+    // zeroed per apply; the FP32 two-team organisations at P >= 2048 only
+    auto persist = [&](int mode, int log2p) {
+        return mf->persistent && sizeof(T) == 4 && log2p >= 11 && (mode == 4 || (mode == 2 && mf->shared_den));
+    };
+    if (mf->persistent)
+    {
+        CU(mf->tickets.ensure(sizeof(int) * (1 + mf->xb.size())));
+        CU(cudaMemsetAsync(mf->tickets.p, 0, sizeof(int) * (1 + mf->xb.size()), mf->stream));
+    }
+    p.ticket = persist(mf->mode_x, mf->log2p) ? mf->tickets.as<int>() : nullptr;
+    p.nblk = mf->nblocks;
+    p.ntiles = mf->nblocks * mf->ngroups;
     CU(launch_xcorr<T>(mf->log2p, mf->shared_den, mf->mode_x, p, mf->nblocks, mf->ngroups, mf->stream));
     ++mf->launches;
     // the other length buckets, one launch each
@@ -1729,6 +1745,9 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
         q.twt = xb->tw.as<cx<T>>();
         q.twt_split = xb->tws.as<cx<T>>();
         q.S = xb->S;
+        q.ticket = persist(xb->mode, xb->log2p) ? mf->tickets.as<int>() + 1 + (&xb - &mf->xb[0]) : nullptr;
+        q.nblk = xb->nblocks;
+        q.ntiles = xb->nblocks * xb->ngroups;
         CU(launch_xcorr<T>(xb->log2p, false, xb->mode, q, xb->nblocks, xb->ngroups, mf->stream));
         ++mf->launches;
     }

@@ -2,6 +2,7 @@
 // type; included once by mf_f32.cu and once by mf_f64.cu so the two
 // precisions compile in parallel.
 #pragma once
+#include <algorithm>
 #include <type_traits>
 #include "launch.h"
 
@@ -10,16 +11,33 @@ namespace mfgpu {
 template <class T, int LOG2P> struct XcorrTable
 {
     static size_t smem(bool shared_den, int mode, int S) { return XcorrLayout<T, LOG2P>::bytes(shared_den, mode, S); }
-    template <bool SD, int MODE> static cudaError_t go(const XcorrParams<T> &p, int nblocks, int ngroups, cudaStream_t s)
+    template <bool SD, int MODE, bool PERSIST = false>
+    static cudaError_t go(const XcorrParams<T> &p, int nblocks, int ngroups, cudaStream_t s)
     {
         size_t bytes = smem(SD, MODE, p.S);
-        auto k = xcorr_kernel<T, LOG2P, SD, MODE>;
+        auto k = xcorr_kernel<T, LOG2P, SD, MODE, PERSIST>;
         static SmemCap cap;
         cudaError_t e = raise_smem_cap(k, bytes, cap);
         if (e != cudaSuccess) return e;
-        k<<<dim3(nblocks, ngroups), MODE == 4 ? 2 * kThreads : kThreads, bytes, s>>>(p);
+        const int threads = MODE == 4 ? 2 * kThreads : kThreads;
+        if constexpr (PERSIST)
+        {
+            // as many CTAs as fit on the device at once
+            int dev = 0, nsm = 0, occ = 0;
+            if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+            if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, threads, bytes)) != cudaSuccess) return e;
+            const long want = (long) std::max(1, occ) * nsm;
+            const int grid = (int) std::max<long>(1, std::min<long>(want, (long) p.ntiles));
+            k<<<grid, threads, bytes, s>>>(p);
+        }
+        else
+            k<<<dim3(nblocks, ngroups), threads, bytes, s>>>(p);
         return cudaGetLastError();
     }
+    // the persistent work-queue form is compiled for the FP32 team
+    // organisations (modes 2 and 4) only
+    static constexpr bool persist_ok = std::is_same<T, float>::value && LOG2P >= 11;
     // mode 4 (two 256-thread teams, several template lengths): FP32, P >= 2048
     static constexpr bool wide_ok = std::is_same<T, float>::value && LOG2P >= 11;
     // MODE 2 (teams) exists only for a shared template length with its
@@ -27,6 +45,15 @@ template <class T, int LOG2P> struct XcorrTable
     // normalised inside the CTA
     static cudaError_t launch(bool sd, int mode, const XcorrParams<T> &p, int nblocks, int ngroups, cudaStream_t s)
     {
+        if (p.ticket)
+        {
+            if constexpr (persist_ok)
+            {
+                if (sd && mode == 2) return go<true, 2, true>(p, nblocks, ngroups, s);
+                if (!sd && mode == 4) return go<false, 4, true>(p, nblocks, ngroups, s);
+            }
+            return cudaErrorInvalidValue;
+        }
         if (sd)
         {
             if (mode == 3) return cudaErrorInvalidValue;

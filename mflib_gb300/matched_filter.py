@@ -166,7 +166,7 @@ class MatchedFilter:
         return self._dtype
 
     def initialize(self, params, template_channels=None, n_channels=None, fft_length=0, correlator_variant=0,
-                   length_buckets=0, bucket_plans=None):
+                   length_buckets=0, bucket_plans=None, persistent=False):
         """MatchedFilter<T>::initialize (src/matchedFilter.cpp:507-821).
 
         Extensions: ``template_channels`` (one channel index per template,
@@ -183,7 +183,9 @@ class MatchedFilter:
         (0 automatic, 1 one plan for every template); ``bucket_plans``
         overrides the plan of each length bucket (shortest templates first):
         a list of (fft_length, correlator_variant) pairs, 0 keeping the
-        automatic choice (see ``autotune``)."""
+        automatic choice (see ``autotune``); ``persistent`` runs the FFT
+        correlator as one persistent launch fed by a device work ticket
+        (FP32, variants 3 and 6; the static grid is the default)."""
         if not isinstance(params, MatchedFilterParameters) or not params.is_valid():
             raise ValueError("Parameters are invalid")
         tmpls = [params.get_template(i) for i in range(params.get_number_of_templates())]
@@ -223,10 +225,11 @@ class MatchedFilter:
             p.n_bucket_plans = nbp
             p.bucket_fft_lengths = bfl
             p.bucket_variants = bva
+        p.persistent = 1 if persistent else 0
         _lib.call("mfgpu_mf_initialize", self._h, C.byref(p))
         self._init_kw = dict(template_channels=template_channels, n_channels=n_channels, fft_length=fft_length,
                              correlator_variant=correlator_variant, length_buckets=length_buckets,
-                             bucket_plans=list(bucket_plans) if bucket_plans else None)
+                             bucket_plans=list(bucket_plans) if bucket_plans else None, persistent=persistent)
         self._params = params
         self._nt = nt
         self._templates = tmpls

@@ -230,3 +230,38 @@ def test_precision_stress_mixed_lengths(gpu, oracle):
         truth = oracle.pearson_naive(tps[t], xs[c].astype(np.float64))
         worst = max(worst, float(np.max(np.abs(got - truth[: got.size]))))
     assert worst < 1e-4, worst
+
+
+@pytest.mark.parametrize("variant", [3, 6])
+def test_persistent_correlator(gpu, oracle, variant):
+    """The persistent work-queue launch (CTAs taking tiles from a device
+    ticket) gives bit-identical coefficients and peaks to the static grid:
+    two teams of one template length at N = 4096 (variant 3) and two
+    256-thread teams of several lengths at N = 8192 (variant 6)."""
+    mf = gpu
+    rng = np.random.default_rng(77)
+    nch, n = 3, 90_000
+    lens = [500] * 9 if variant == 3 else list(rng.integers(200, 3001, 9))
+    tps = [_template(600 + i, int(L), 1.0 + i % 5, 9.0) for i, L in enumerate(lens)]
+    chan = [i % nch for i in range(len(tps))]
+    sigs = np.stack([_bp(np.random.default_rng(700 + c).standard_normal(n), 1.0, 10.0) for c in range(nch)])
+    sigs = sigs.astype(np.float32)
+    out = []
+    for persistent in (False, True):
+        f = mf.MultiChannel.MatchedFilter(dtype=np.float32)
+        kw = dict(fft_length=4096) if variant == 3 else {}
+        f.initialize(_params(mf, tps, n), template_channels=chan, n_channels=nch, correlator_variant=variant,
+                     persistent=persistent, **kw)
+        assert f.get_plan()["correlator"] == variant
+        f.set_peak_threshold(0.3)
+        f.set_channel_signals(sigs)
+        f.apply()
+        f.find_peaks(0.3, 100)
+        out.append(([f.get_matched_filtered_signal(t) for t in range(len(tps))], f.get_all_peaks()))
+    for a, b in zip(out[0][0], out[1][0]):
+        np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(out[0][1][0], out[1][1][0])
+    np.testing.assert_array_equal(out[0][1][1], out[1][1][1])
+    ref = oracle.matched_filter(tps, [sigs[c] for c in chan], multi=True, fp64_from_f32=True)
+    for t in range(len(tps)):
+        assert np.max(np.abs(out[1][0][t].astype(np.float64) - ref[t][: out[1][0][t].size])) < 1e-5
