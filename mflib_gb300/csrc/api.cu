@@ -224,6 +224,12 @@ struct mfgpu_mf
     // dir_b0 .. dir_b0 + dir_nb - 1 of the fix-up tables)
     int n_direct = 0, dir_b0 = 0, dir_nb = 0, dir_lmax = 0;
     int fLen = 0;  // longest template of the FFT plans (their shared length when all are equal)
+    int fMin = 0;  // shortest template of the FFT plans
+    // lags backed by data for the FFT plans' shortest template (device int
+    // read by the error-bound kernels), smaller while a request window
+    // shorter than the signal is loaded (win_active)
+    DevBuf dlags;
+    bool win_active = false;
     DevBuf fx_bch;
     DevBuf tws;  // pass twiddles in the split layout (correlator mode 4)
     DevBuf tickets;  // one persistent-launch ticket per correlator launch of an apply
@@ -284,7 +290,7 @@ struct mfgpu_mf
                          &shifts_d, &weights_d, &specbuf, &den, &pk_cnt, &pk_idx, &pk_val, &xstage,
                          &xrange,   &tc_B,   &tc_bscale, &tc_grp_chan, &tc_grp_tid, &pk_flags,
                          &rstat,    &cst,    &fxbits, &fxlist, &fxcount, &tc_off, &fx_btid, &fx_boff,
-                         &fx_bL,    &fx_cb0, &fx_cnb, &fx_bch,
+                         &fx_bL,    &fx_cb0, &fx_cnb, &fx_bch, &dlags,
                          &fx_bco,   &fx_bsum, &pk_dirty, &tws, &tickets};
         for (DevBuf *d : all) f(*d);
         pk.each_buf(f);
@@ -328,7 +334,8 @@ struct mfgpu_mf
         ldx = ldr = 0;
         fx_on = false;
         fx_L = fx_nden = fx_nruns = fx_nbatch = 0;
-        fx_nbmax = fx_lmax = n_direct = dir_b0 = dir_nb = dir_lmax = fLen = 0;
+        fx_nbmax = fx_lmax = n_direct = dir_b0 = dir_nb = dir_lmax = fLen = fMin = 0;
+        win_active = false;
         ldrs = ldc = fx_nchunks = 0;
     }
 };
@@ -591,6 +598,7 @@ try
     const int ntf = nt - ndirect;
     mf->n_direct = ndirect;
     mf->fLen = ntf > 0 ? fMax : 0;
+    mf->fMin = ntf > 0 ? fMin : 0;
     mf->persistent = p->persistent != 0;
     if (ndirect > 0)
     {
@@ -1152,6 +1160,8 @@ try
             CU(mf->fxlist.ensure(sizeof(int) * (size_t) nch * mf->ldrs));
             CU(mf->fxcount.ensure(sizeof(int)));
             CU(cudaMemsetAsync(mf->fxcount.p, 0, sizeof(int), mf->stream));
+            CU(mf->dlags.ensure(sizeof(int)));
+            CU(launch_set_int(mf->dlags.as<int>(), std::max(0, n - mf->fMin + 1), mf->stream));
             if (mf->tc) CU(mf->tc_off.ensure(sizeof(float) * (size_t) nch * mf->tc_tiles));
         }
         CU(mf->fx_btid.ensure(sizeof(int) * btid.size()));
@@ -1316,6 +1326,19 @@ catch (...)
     return mfgpu::status_of_exception();
 }
 
+// Records, in stream order, how many samples of every row carry data
+// (ndata; the rest is zero tail): the error bounds list no run past the lags
+// those samples back.  Cheap, and skipped while nothing changes.
+static mfgpu_status mf_set_data_length(mfgpu_mf *mf, int ndata)
+{
+    if (!mf->fx_on) return MFGPU_OK;
+    const bool window = ndata < mf->n;
+    if (!window && !mf->win_active) return MFGPU_OK;
+    CU(launch_set_int(mf->dlags.as<int>(), std::max(0, ndata - mf->fMin + 1), mf->stream));
+    mf->win_active = window;
+    return MFGPU_OK;
+}
+
 static mfgpu_status mf_channel_of(mfgpu_mf *mf, int it, int *c)
 {
     if (it < 0 || it >= mf->nt)
@@ -1369,6 +1392,9 @@ try
         CU(mf->xstage.ensure(need));
         CU(cudaMemsetAsync(mf->xstage.p, 0, mf->xstage.bytes, mf->copy_stream));
     }
+    // full rows from the next apply on (after a shorter request window)
+    mfgpu_status ds = mf_set_data_length(mf, mf->n);
+    if (ds != MFGPU_OK) return ds;
     // the buffer is free once the last apply that read it has finished
     CU(cudaStreamWaitEvent(mf->copy_stream, mf->xstage_ev, 0));
     if (mf->nch == 1) CU(cudaMemcpyAsync(mf->xstage.p, x, es * (size_t) n, cudaMemcpyHostToDevice, mf->copy_stream));
@@ -1394,6 +1420,8 @@ static mfgpu_status mf_store_signals(mfgpu_mf *mf, int c0, int nch, int n, const
     if (!x) return fail(MFGPU_EINVAL, "x is NULL");
     if (nch > 1 && ld < n) return fail(MFGPU_EINVAL, "row stride is smaller than the number of samples");
     mfgpu_status rs = mf_resolve_stage(mf);
+    if (rs != MFGPU_OK) return rs;
+    rs = mf_set_data_length(mf, mf->n);
     if (rs != MFGPU_OK) return rs;
     mf->have = false;
     mf->have_peaks = false;
@@ -1479,6 +1507,8 @@ try
     if (!x) return fail(MFGPU_EINVAL, "x is NULL");
     if (n_src > 1 && ld < n) return fail(MFGPU_EINVAL, "row stride is smaller than the number of samples");
     mfgpu_status rs = mf_resolve_stage(mf);
+    if (rs != MFGPU_OK) return rs;
+    rs = mf_set_data_length(mf, n);
     if (rs != MFGPU_OK) return rs;
     mf->have = false;
     mf->have_peaks = false;
@@ -1628,7 +1658,8 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
             if (mf->tc)
             {
                 CU(launch_fix_flag_tc(mf->x.as<float>(), mf->ldx, mf->fLen, mf->rstat.as<float4>(), mf->ldrs,
-                                      mf->fx_nruns, mf->tc_tiles, mf->nch, mf->dead.as<unsigned char>(),
+                                      mf->fx_nruns, mf->dlags.as<int>(), mf->tc_tiles, mf->nch,
+                                      mf->dead.as<unsigned char>(),
                                       mf->xrange.as<float>(), mf->tc_off.as<float>(),
                                       mf->fxbits.as<unsigned>(), mf->fxlist.as<int>(), mf->fxcount.as<int>(), kFixTcC1,
                                       kFixTcC2, kFixTol, mf->stream));
@@ -1638,7 +1669,7 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
             {
                 const float coef = kFixFftK * 0x1p-24f / kFixTol;
                 CU(launch_fix_flag_fft(mf->cst.as<float2>(), mf->ldc, mf->fx_nchunks, mf->S, mf->nfft, mf->nblocks,
-                                       mf->nch, mf->rstat.as<float4>(), mf->ldrs, mf->fx_nruns,
+                                       mf->nch, mf->rstat.as<float4>(), mf->ldrs, mf->fx_nruns, mf->dlags.as<int>(),
                                        mf->dead.as<unsigned char>(), mf->fxbits.as<unsigned>(), mf->fxlist.as<int>(),
                                        mf->fxcount.as<int>(), coef * coef,
                                        mf->stream));
@@ -1648,7 +1679,7 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
                     if (xb->ngroups == 0) continue;
                     CU(launch_fix_flag_fft(mf->cst.as<float2>(), mf->ldc, mf->fx_nchunks, xb->S, xb->nfft, xb->nblocks,
                                            mf->nch, mf->rstat.as<float4>(), mf->ldrs, mf->fx_nruns,
-                                           mf->dead.as<unsigned char>(), mf->fxbits.as<unsigned>(),
+                                           mf->dlags.as<int>(), mf->dead.as<unsigned char>(), mf->fxbits.as<unsigned>(),
                                            mf->fxlist.as<int>(), mf->fxcount.as<int>(),
                                            coef * coef, mf->stream));
                     ++mf->launches;

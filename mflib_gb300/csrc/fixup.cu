@@ -16,20 +16,27 @@ cudaError_t launch_den_robust(const float *x, long ldx, int L, float *den, long 
 }
 
 cudaError_t launch_fix_flag_fft(const float2 *cst, long ldc, long nchunks, int S, int N, int nblocks, int nch,
-                                const float4 *rstat, long ldrs, int nruns, const unsigned char *dead, unsigned *fbits,
-                                int *flist, int *fcount, float coef2, cudaStream_t s)
+                                const float4 *rstat, long ldrs, int nruns, const int *dlags, const unsigned char *dead,
+                                unsigned *fbits, int *flist, int *fcount, float coef2, cudaStream_t s)
 {
     fix_flag_fft_kernel<<<dim3((nblocks + 7) / 8, nch), 256, 0, s>>>(cst, ldc, nchunks, S, N, nblocks, rstat, ldrs,
-                                                                      nruns, dead, fbits, flist, fcount, coef2);
+                                                                      nruns, dlags, dead, fbits, flist, fcount, coef2);
     return cudaGetLastError();
 }
 
-cudaError_t launch_fix_flag_tc(const float *x, long ldx, int L, const float4 *rstat, long ldrs, int nruns, int tiles,
-                               int nch, const unsigned char *dead, const float *xrange, float *off, unsigned *fbits,
-                               int *flist, int *fcount, float c1, float c2, float tau, cudaStream_t s)
+cudaError_t launch_fix_flag_tc(const float *x, long ldx, int L, const float4 *rstat, long ldrs, int nruns,
+                               const int *dlags, int tiles, int nch, const unsigned char *dead, const float *xrange,
+                               float *off, unsigned *fbits, int *flist, int *fcount, float c1, float c2, float tau,
+                               cudaStream_t s)
 {
-    fix_flag_tc_kernel<<<dim3((tiles + 7) / 8, nch), 256, 0, s>>>(x, ldx, L, rstat, ldrs, nruns, tiles, dead, xrange,
-                                                                   off, fbits, flist, fcount, c1, c2, tau);
+    fix_flag_tc_kernel<<<dim3((tiles + 7) / 8, nch), 256, 0, s>>>(x, ldx, L, rstat, ldrs, nruns, dlags, tiles, dead,
+                                                                   xrange, off, fbits, flist, fcount, c1, c2, tau);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_set_int(int *p, int v, cudaStream_t s)
+{
+    fix_set_int_kernel<<<1, 1, 0, s>>>(p, v);
     return cudaGetLastError();
 }
 

@@ -277,8 +277,8 @@ __global__ void __launch_bounds__(kThreads) den_robust_kernel(const float *x, lo
 // tol_rho)^2) or the run is unreliable.  One warp per block, 8 per CTA.
 __global__ void __launch_bounds__(256) fix_flag_fft_kernel(const float2 *cst, long ldc, long nchunks, int S, int N,
                                                           int nblocks, const float4 *rstat, long ldrs, int nruns,
-                                                          const unsigned char *dead, unsigned *fbits, int *flist,
-                                                          int *fcount, float coef2)
+                                                          const int *dlags, const unsigned char *dead, unsigned *fbits,
+                                                          int *flist, int *fcount, float coef2)
 {
     const int lane = threadIdx.x & 31;
     const int b = blockIdx.x * 8 + (threadIdx.x >> 5), c = blockIdx.y;
@@ -310,7 +310,9 @@ __global__ void __launch_bounds__(256) fix_flag_fft_kernel(const float2 *cst, lo
         merge(nb, mb, qb);
     }
     const float lim = M2 * coef2;
-    const int r1 = min((int) (((long) b * S + S) / kDenRun), nruns);
+    // runs past the lags backed by data (a request window shorter than the
+    // object's signal) are never used: none is listed
+    const int r1 = min(min((int) (((long) b * S + S) / kDenRun), nruns), (*dlags + kDenRun - 1) / kDenRun);
     for (int r = (int) j0 + lane; r < r1; r += 32)
     {
         const float mm = rstat[(long) c * ldrs + r].x;
@@ -325,7 +327,8 @@ __global__ void __launch_bounds__(256) fix_flag_fft_kernel(const float2 *cst, lo
 // ||x - off||^2 <= M2min + L (|R_r - off| + spread_r)^2 and s the strip's
 // power-of-two operand scale.  256 threads (8 strips).
 __global__ void __launch_bounds__(256) fix_flag_tc_kernel(const float *x, long ldx, int L, const float4 *rstat,
-                                                         long ldrs, int nruns, int tiles, const unsigned char *dead,
+                                                         long ldrs, int nruns, const int *dlags, int tiles,
+                                                         const unsigned char *dead,
                                                          const float *xrange, float *off_out, unsigned *fbits,
                                                          int *flist, int *fcount, float c1, float c2, float tau)
 {
@@ -346,7 +349,7 @@ __global__ void __launch_bounds__(256) fix_flag_tc_kernel(const float *x, long l
     float off = __shfl_sync(0xffffffffu, st.y, src);
     if (!(key < INFINITY)) off = x[(long) c * ldx + (long) j * 1024];
     if (lane == 0) off_out[(long) c * tiles + j] = off;
-    if (dead[c] || r >= nruns) return;
+    if (dead[c] || r >= nruns || 32L * r >= *dlags) return;
     bool f = st.x < 0.f;
     if (!f && st.x < kRunConst)
     {
@@ -412,6 +415,9 @@ template <class T> __device__ __forceinline__ T fix_rho(T num, T M2, int L, T to
     const T r = num * DenOps<T>::out((T) L * M2, sqrt((T) L), tol);
     return clamp_rho(r);
 }
+
+// Sets *p = v in stream order (a CUDA-graph replay reads the current value).
+__global__ void fix_set_int_kernel(int *p, int v) { *p = v; }
 
 // Shared-memory row of samples per warp (a multiple of 16 bytes) and the
 // warp's share: the row plus one staged chunk of coefficients.

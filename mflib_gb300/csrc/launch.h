@@ -56,11 +56,14 @@ cudaError_t launch_tc_xcorr(const TcParams &p, int nctas, cudaStream_t s);
 cudaError_t launch_den_robust(const float *x, long ldx, int L, float *den, long ldd, float tol, float4 *rstat,
                               long ldrs, float2 *cst, long ldc, int nblocks, int nch, cudaStream_t s);
 cudaError_t launch_fix_flag_fft(const float2 *cst, long ldc, long nchunks, int S, int N, int nblocks, int nch,
-                                const float4 *rstat, long ldrs, int nruns, const unsigned char *dead, unsigned *fbits,
-                                int *flist, int *fcount, float coef2, cudaStream_t s);
-cudaError_t launch_fix_flag_tc(const float *x, long ldx, int L, const float4 *rstat, long ldrs, int nruns, int tiles,
-                               int nch, const unsigned char *dead, const float *xrange, float *off, unsigned *fbits,
-                               int *flist, int *fcount, float c1, float c2, float tau, cudaStream_t s);
+                                const float4 *rstat, long ldrs, int nruns, const int *dlags, const unsigned char *dead,
+                                unsigned *fbits, int *flist, int *fcount, float coef2, cudaStream_t s);
+cudaError_t launch_fix_flag_tc(const float *x, long ldx, int L, const float4 *rstat, long ldrs, int nruns,
+                               const int *dlags, int tiles, int nch, const unsigned char *dead, const float *xrange,
+                               float *off, unsigned *fbits, int *flist, int *fcount, float c1, float c2, float tau,
+                               cudaStream_t s);
+// *p = v in stream order
+cudaError_t launch_set_int(int *p, int v, cudaStream_t s);
 // warps per fix-up CTA whose sample rows (templates up to Lmax) fit dev_smem
 // bytes (0: none fits)
 template <class T> int fixup_warps(int Lmax, int dev_smem);

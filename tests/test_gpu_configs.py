@@ -265,3 +265,33 @@ def test_persistent_correlator(gpu, oracle, variant):
     ref = oracle.matched_filter(tps, [sigs[c] for c in chan], multi=True, fp64_from_f32=True)
     for t in range(len(tps)):
         assert np.max(np.abs(out[1][0][t].astype(np.float64) - ref[t][: out[1][0][t].size])) < 1e-5
+
+
+def test_window_tail_not_fixed_up(gpu, oracle):
+    """A request window shorter than the object's signal (zero tail): the
+    error bounds list no run past the lags the window's samples back (none
+    of those lags is used), the window's own lags match the oracle, and a
+    full-length upload afterwards restores the full range."""
+    mf = gpu
+    rng = np.random.default_rng(31)
+    n, nw, nch = 40_000, 29_000, 2
+    tps = [_template(900 + i, L) for i, L in enumerate((300, 700, 1200, 450))]
+    chan = [0, 1, 0, 1]
+    f = mf.MultiChannel.MatchedFilter(dtype=np.float32)
+    f.initialize(_params(mf, tps, n), template_channels=chan, n_channels=nch)
+    full = np.stack([_bp(rng.standard_normal(n), 1.0, 10.0) for _ in range(nch)]).astype(np.float32)
+    f.set_window(full[:, :nw])
+    f.apply()
+    assert f.get_fixup_runs() == 0
+    for t, c in enumerate(chan):
+        nv = nw - tps[t].size + 1
+        got = f.get_valid_matched_filtered_signal(t).astype(np.float64)[:nv]
+        ref = oracle.pearson_naive(tps[t], full[c, :nw].astype(np.float64))
+        assert np.max(np.abs(got - ref)) < 1e-5
+    f.set_channel_signals(full)
+    f.apply()
+    assert f.get_fixup_runs() == 0
+    for t, c in enumerate(chan):
+        got = f.get_valid_matched_filtered_signal(t).astype(np.float64)
+        ref = oracle.pearson_naive(tps[t], full[c].astype(np.float64))
+        assert np.max(np.abs(got - ref)) < 1e-5
