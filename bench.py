@@ -714,6 +714,18 @@ def run_uneven_day(args, ctx):
                            "get_all_peaks"},
             "roofline": roof, "gpu_launches": int(launches), "clocks": clk, "detections": int(idx.size),
             "graph_replays": f.graph_launches()}
+    # The split-precision tensor-core form on this bank, by arithmetic: per
+    # template-lag it executes 3 products (hi*hi, hi*lo, lo*hi) over the
+    # template's K padded to 16 (K = L + 7 for the 8 phases of a row), 2 flops
+    # each; even at the measured dense BF16/FP16 peak that takes longer than
+    # the FFT form's measured step.
+    kp = ((lens.astype(np.int64) + 7 + 15) // 16) * 16
+    tc_flops = float(np.sum(3.0 * 2.0 * kp * (n - lens + 1)))
+    bf16, bf16_kind = measured_peak("bf16_tflops")
+    tc_ms = tc_flops / (bf16 * 1e12) * 1e3
+    line["split_precision_ceiling"] = {
+        "executed_flops": tc_flops, "ms_at_tensor_peak": tc_ms, "peak_tflops": bf16, "peak_source": bf16_kind,
+        "fft_ms_per_step": 1e3 * el / args.steps, "best_possible_ratio_over_fft": (1e3 * el / args.steps) / tc_ms}
     if tune is not None:
         line["config"]["autotune"] = tune
     f.clear()
