@@ -205,6 +205,127 @@ static __global__ void __launch_bounds__(kDbThreads) db_label_kernel(DbParams p,
     if (lane == 0) labels[i] = best == 0x7fffffffffffffffLL ? -1 : (int) best;
 }
 
+// ----------------------------------------------------------------------------
+// One feature with the points of every segment sorted by (x, index) on the
+// host: xs[r] is the r-th smallest value of its segment (positions keep the
+// segment offsets), perm[r] its point, rank[i] the position of point i.  The
+// eps-neighbourhood of a point is then the contiguous range of positions
+// [lo, hi) found by binary search with the same predicate |x_i - x_j| <= eps
+// (a rounded difference is monotone in x_j), so every pass visits the
+// neighbours only: O(n log n + sum of neighbourhood sizes) instead of a scan
+// of the whole segment per point.
+struct Db1Sorted
+{
+    const double *xs;
+    const int *perm;
+    const int *rank;
+};
+
+// [lo, hi): positions of the segment [jb, je) within eps of the value xi
+__device__ __forceinline__ void db1_range(const double *xs, int jb, int je, double xi, double eps, int &lo, int &hi)
+{
+    int a = jb, b = je;  // first position with xi - xs <= eps
+    while (a < b)
+    {
+        const int m = (a + b) >> 1;
+        if (xi - xs[m] <= eps) b = m;
+        else a = m + 1;
+    }
+    lo = a;
+    b = je;              // first position with xs - xi > eps
+    while (a < b)
+    {
+        const int m = (a + b) >> 1;
+        if (xs[m] - xi <= eps) a = m + 1;
+        else b = m;
+    }
+    hi = a;
+}
+
+static __global__ void __launch_bounds__(kDbThreads) db1_core_kernel(DbParams p, Db1Sorted q, unsigned char *core,
+                                                                     int *parent)
+{
+    const int i = blockIdx.x * kDbWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (i >= p.n) return;
+    const int s = p.seg_of[i];
+    int lo = 0, hi = 0;
+    if (lane == 0) db1_range(q.xs, p.seg_off[s], p.seg_off[s + 1], p.X[i], p.eps, lo, hi);
+    lo = __shfl_sync(0xffffffffu, lo, 0);
+    hi = __shfl_sync(0xffffffffu, hi, 0);
+    double acc = 0;
+    for (int r = lo + lane; r < hi; r += 32) acc += p.w ? p.w[q.perm[r]] : 1.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0)
+    {
+        core[i] = acc >= p.min_obs ? 1 : 0;
+        parent[i] = i;
+    }
+}
+
+// each core point united with the nearest core point before it in the sorted
+// order when that one lies within eps (the runs of consecutive core points
+// with gaps <= eps are the components, as in db_union_kernel's 1-D case)
+static __global__ void __launch_bounds__(kDbThreads) db1_union_kernel(DbParams p, Db1Sorted q, const unsigned char *core,
+                                                                      int *parent)
+{
+    const int i = blockIdx.x * kDbWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (i >= p.n || !core[i]) return;
+    const int s = p.seg_of[i];
+    const int jb = p.seg_off[s];
+    const double xi = p.X[i];
+    for (int r0 = q.rank[i] - 1; r0 >= jb; r0 -= 32)
+    {
+        const int r = r0 - lane;
+        const bool in = r >= jb && xi - q.xs[r] <= p.eps;
+        const bool hit = in && core[q.perm[r]];
+        const unsigned hm = __ballot_sync(0xffffffffu, hit), im = __ballot_sync(0xffffffffu, in);
+        if (hm)
+        {
+            const int l = __ffs(hm) - 1;  // the nearest position (lowest lane)
+            if (lane == l) db_unite(parent, i, q.perm[r]);
+            return;
+        }
+        if (im != 0xffffffffu) return;  // left the neighbourhood before finding a core point
+    }
+}
+
+// border points: the smallest cluster id among their core neighbours
+static __global__ void __launch_bounds__(kDbThreads) db1_label_kernel(DbParams p, Db1Sorted q, const unsigned char *core,
+                                                                      const int *root, const long long *root_pos,
+                                                                      int *labels)
+{
+    const int i = blockIdx.x * kDbWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+    if (i >= p.n) return;
+    const int s = p.seg_of[i];
+    const int jb = p.seg_off[s], je = p.seg_off[s + 1];
+    const long long base = root_pos[jb];
+    if (core[i])
+    {
+        if (lane == 0) labels[i] = (int) (root_pos[root[i]] - base);
+        return;
+    }
+    int lo = 0, hi = 0;
+    if (lane == 0) db1_range(q.xs, jb, je, p.X[i], p.eps, lo, hi);
+    lo = __shfl_sync(0xffffffffu, lo, 0);
+    hi = __shfl_sync(0xffffffffu, hi, 0);
+    long long best = 0x7fffffffffffffffLL;
+    for (int r = lo + lane; r < hi; r += 32)
+    {
+        const int j = q.perm[r];
+        if (!core[j]) continue;
+        const long long id = root_pos[root[j]] - base;
+        best = id < best ? id : best;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+        const long long v = __shfl_xor_sync(0xffffffffu, best, o);
+        best = v < best ? v : best;
+    }
+    if (lane == 0) labels[i] = best == 0x7fffffffffffffffLL ? -1 : (int) best;
+}
+
 static __global__ void db_count_kernel(int nseg, const int *seg_off, const long long *root_pos, int *n_clusters)
 {
     int s = blockIdx.x * blockDim.x + threadIdx.x;

@@ -180,10 +180,11 @@ int run_peaks(const T *x, long ldx, const int *host_rows, int ntr, int len, doub
 // DBSCAN over segments
 struct DbWS
 {
-    DevBuf X, w, seg_of, seg_off, parent, is_root, labels, nclusters, core, pos, tiles;
+    DevBuf X, w, seg_of, seg_off, parent, is_root, labels, nclusters, core, pos, tiles, xs, perm, rank;
     void release()
     {
-        DevBuf *all[] = {&X, &w, &seg_of, &seg_off, &parent, &is_root, &labels, &nclusters, &core, &pos, &tiles};
+        DevBuf *all[] = {&X, &w, &seg_of, &seg_off, &parent, &is_root, &labels, &nclusters, &core, &pos, &tiles,
+                         &xs, &perm, &rank};
         for (DevBuf *d : all) d->release();
     }
 };

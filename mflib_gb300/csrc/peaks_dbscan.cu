@@ -1,6 +1,7 @@
 // peaks_dbscan.cu -- host drivers of the peak-finder and DBSCAN pipelines
 // (kernels in kernels_peaks.cuh / kernels_dbscan.cuh) and the device scan.
 #include <algorithm>
+#include <cmath>
 #include <string>
 #include <vector>
 #include "launch.h"
@@ -216,6 +217,34 @@ int run_dbscan(int n, int nf, const double *X, const double *w, double eps, int 
     std::vector<int> seg_of(n);
     for (int sg = 0; sg < nseg; ++sg)
         for (int i = seg_off_host[sg]; i < seg_off_host[sg + 1]; ++i) seg_of[i] = sg;
+    // one feature: every segment's points sorted by (x, index), so each point
+    // visits its neighbourhood only (Db1Sorted).  A NaN has no order and no
+    // neighbour; data holding one keeps the full scans.
+    bool sorted1 = nf == 1;
+    for (int i = 0; sorted1 && i < n; ++i) sorted1 = !std::isnan(X[i]);
+    std::vector<double> xs;
+    std::vector<int> perm, rank;
+    if (sorted1)
+    {
+        xs.resize(n);
+        perm.resize(n);
+        rank.resize(n);
+        for (int i = 0; i < n; ++i) perm[i] = i;
+        for (int sg = 0; sg < nseg; ++sg)
+            std::sort(perm.begin() + seg_off_host[sg], perm.begin() + seg_off_host[sg + 1],
+                      [&](int a, int b) { return X[a] < X[b] || (X[a] == X[b] && a < b); });
+        for (int r = 0; r < n; ++r)
+        {
+            xs[r] = X[perm[r]];
+            rank[perm[r]] = r;
+        }
+        MF_TRY(ws.xs.ensure(sizeof(double) * (size_t) n));
+        MF_TRY(ws.perm.ensure(sizeof(int) * (size_t) n));
+        MF_TRY(ws.rank.ensure(sizeof(int) * (size_t) n));
+        MF_TRY(cudaMemcpyAsync(ws.xs.p, xs.data(), sizeof(double) * (size_t) n, cudaMemcpyHostToDevice, s));
+        MF_TRY(cudaMemcpyAsync(ws.perm.p, perm.data(), sizeof(int) * (size_t) n, cudaMemcpyHostToDevice, s));
+        MF_TRY(cudaMemcpyAsync(ws.rank.p, rank.data(), sizeof(int) * (size_t) n, cudaMemcpyHostToDevice, s));
+    }
     MF_TRY(cudaMemcpyAsync(ws.X.p, X, sizeof(double) * (size_t) n * nf, cudaMemcpyHostToDevice, s));
     if (w) MF_TRY(cudaMemcpyAsync(ws.w.p, w, sizeof(double) * (size_t) n, cudaMemcpyHostToDevice, s));
     MF_TRY(cudaMemcpyAsync(ws.seg_of.p, seg_of.data(), sizeof(int) * (size_t) n, cudaMemcpyHostToDevice, s));
@@ -227,22 +256,36 @@ int run_dbscan(int n, int nf, const double *X, const double *w, double eps, int 
     p.min_obs = (double) min_obs; p.seg_of = ws.seg_of.as<int>(); p.seg_off = ws.seg_off.as<int>(); p.n = n;
     const unsigned blocks = (unsigned) ((n + kDbThreads - 1) / kDbThreads);   // one thread per point
     const unsigned wblocks = (unsigned) ((n + kDbWarps - 1) / kDbWarps);      // one warp per point
-    db_core_kernel<<<wblocks, kDbThreads, 0, s>>>(p, ws.core.as<unsigned char>(), ws.parent.as<int>());
-    db_union_kernel<<<wblocks, kDbThreads, 0, s>>>(p, ws.core.as<unsigned char>(), ws.parent.as<int>());
+    Db1Sorted q{ws.xs.as<double>(), ws.perm.as<int>(), ws.rank.as<int>()};
+    if (sorted1)
+    {
+        db1_core_kernel<<<wblocks, kDbThreads, 0, s>>>(p, q, ws.core.as<unsigned char>(), ws.parent.as<int>());
+        db1_union_kernel<<<wblocks, kDbThreads, 0, s>>>(p, q, ws.core.as<unsigned char>(), ws.parent.as<int>());
+    }
+    else
+    {
+        db_core_kernel<<<wblocks, kDbThreads, 0, s>>>(p, ws.core.as<unsigned char>(), ws.parent.as<int>());
+        db_union_kernel<<<wblocks, kDbThreads, 0, s>>>(p, ws.core.as<unsigned char>(), ws.parent.as<int>());
+    }
     db_roots_kernel<<<blocks, kDbThreads, 0, s>>>(n, ws.core.as<unsigned char>(), ws.parent.as<int>(),
                                                   ws.is_root.as<int>());
     *launches += 3;
     MF_TRY(cudaGetLastError());
     MF_TRY(device_excl_scan(ws.is_root.as<int>(), n, ws.pos.as<long long>(), ws.tiles.as<long long>(), s,
                             launches));
-    db_label_kernel<<<wblocks, kDbThreads, 0, s>>>(p, ws.core.as<unsigned char>(), ws.parent.as<int>(),
-                                                  ws.pos.as<long long>(), ws.labels.as<int>());
+    if (sorted1)
+        db1_label_kernel<<<wblocks, kDbThreads, 0, s>>>(p, q, ws.core.as<unsigned char>(), ws.parent.as<int>(),
+                                                       ws.pos.as<long long>(), ws.labels.as<int>());
+    else
+        db_label_kernel<<<wblocks, kDbThreads, 0, s>>>(p, ws.core.as<unsigned char>(), ws.parent.as<int>(),
+                                                      ws.pos.as<long long>(), ws.labels.as<int>());
     db_count_kernel<<<(nseg + 127) / 128, 128, 0, s>>>(nseg, ws.seg_off.as<int>(), ws.pos.as<long long>(),
                                                        ws.nclusters.as<int>());
     *launches += 2;
     MF_TRY(cudaGetLastError());
     MF_TRY(cudaMemcpyAsync(labels_host, ws.labels.p, sizeof(int) * (size_t) n, cudaMemcpyDeviceToHost, s));
     MF_TRY(cudaMemcpyAsync(nclusters_host, ws.nclusters.p, sizeof(int) * (size_t) nseg, cudaMemcpyDeviceToHost, s));
+    // the host vectors above must outlive the copies
     MF_TRY(cudaStreamSynchronize(s));
     return 0;
 }

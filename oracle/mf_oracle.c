@@ -322,7 +322,8 @@ ORC_API int orc_dbscan(int nobs, int nf, const double *X, const double *w,
             if (!core[p]) { continue; }
             for (int j = 0; j < nobs; ++j)
             {
-                if (orc_dist(&X[(size_t) p*nf], &X[(size_t) j*nf], nf) > eps) { continue; }
+                /* the same predicate as the core count: a NaN distance is no neighbour */
+                if (!(orc_dist(&X[(size_t) p*nf], &X[(size_t) j*nf], nf) <= eps)) { continue; }
                 if (labels[j] == UNDEF || labels[j] == NOISE)
                 {
                     int was_undef = labels[j] == UNDEF;

@@ -3,7 +3,7 @@ golden vectors.  Indices and labels are compared exactly."""
 import numpy as np
 import pytest
 
-from test_oracle import DBSCAN_X, PEAKS_13, PEAKS_21, peak_signal
+from test_oracle import DBSCAN_X, PEAKS_13, PEAKS_21, dbscan_1d, peak_signal
 
 pytestmark = pytest.mark.gpu
 
@@ -178,6 +178,56 @@ def test_dbscan_segmented(gpu, oracle, rng):
         n_ref, lab_ref = oracle.dbscan(seg, 50.0, 3)
         assert ncl[s] == n_ref
         np.testing.assert_array_equal(labels[off[s]:off[s + 1]], lab_ref)
+
+
+def test_dbscan_1d_sorted_vs_oracle(gpu, oracle, rng):
+    # one feature runs on the per-segment sort; values on a quarter grid put
+    # exact ties at eps, and +-inf have no neighbour
+    db = gpu.DBSCAN()
+    x = np.round(rng.uniform(0, 3000, 20_000) * 4) / 4
+    x[rng.integers(0, x.size, 40)] = np.inf
+    x[rng.integers(0, x.size, 40)] = -np.inf
+    w = rng.integers(1, 7, x.size) / 2.0
+    for eps, mo in ((0.25, 2), (0.75, 5), (2.0, 12)):
+        for weights in (None, w):
+            db.initialize(eps, mo)
+            db.set_weighted_data(x, weights)
+            db.cluster()
+            ncl, lab = oracle.dbscan(x, eps, mo, weights)
+            assert db.get_number_of_clusters() == ncl
+            np.testing.assert_array_equal(db.get_labels(), lab)
+
+
+def test_dbscan_1d_nan_keeps_full_scans(gpu, oracle, rng):
+    # a NaN has no order: such data keeps the all-pairs scans
+    db = gpu.DBSCAN()
+    x = np.round(rng.uniform(0, 100, 3000) * 4) / 4
+    x[::97] = np.nan
+    db.initialize(0.5, 3)
+    db.set_data(x)
+    db.cluster()
+    ncl, lab = oracle.dbscan(x, 0.5, 3)
+    assert db.get_number_of_clusters() == ncl
+    np.testing.assert_array_equal(db.get_labels(), lab)
+
+
+def test_dbscan_1d_segmented_large(gpu, rng):
+    # 400,000 observations in 700 segments of ragged sizes against the
+    # sort-based restatement (pinned against the oracle on the CPU)
+    db = gpu.DBSCAN()
+    sizes = rng.integers(0, 1150, 700)
+    sizes[:3] = (0, 1, 60_000)
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int32)
+    x = np.round(rng.uniform(0, 1000, off[-1]) * 8) / 8
+    w = rng.integers(1, 5, x.size) / 2.0
+    for eps, mo, weights in ((0.125, 3, None), (0.5, 4, w)):
+        db.initialize(eps, mo)
+        labels, ncl = db.cluster_segments(x, off, weights)
+        for s in range(sizes.size):
+            a, b = off[s], off[s + 1]
+            n_ref, lab_ref = dbscan_1d(x[a:b], eps, mo, None if weights is None else weights[a:b])
+            assert ncl[s] == n_ref
+            np.testing.assert_array_equal(labels[a:b], lab_ref)
 
 
 def _fused_case(mf, rng, dtype, lens, n=60_000, nch=2):

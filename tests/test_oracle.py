@@ -163,6 +163,60 @@ def test_dbscan_vs_sklearn(oracle, rng):
                 np.testing.assert_array_equal(lab, ref)
 
 
+def dbscan_1d(x, eps, min_obs, weights=None):
+    """DBSCAN over one feature by sorting, for sizes where the oracle's
+    all-pairs scans take too long.  Exact where |x_i - x_j| and the weight
+    sums are exact (values on a binary grid): the eps-neighbourhood of a
+    point is a contiguous range of the sorted values; the clusters are the
+    runs of sorted core points with gaps <= eps, numbered by their smallest
+    index; a border point takes the smallest cluster number among the core
+    points in its range (the oracle's index-order expansion gives the same).
+    Pinned against the oracle in test_dbscan_1d_checker."""
+    x = np.asarray(x, dtype=np.float64)
+    n = x.size
+    if n == 0:
+        return 0, np.zeros(0, np.int32)
+    order = np.argsort(x, kind="stable")
+    xs = x[order]
+    lo = np.searchsorted(xs, xs - eps, side="left")
+    hi = np.searchsorted(xs, xs + eps, side="right")
+    w = np.ones(n) if weights is None else np.asarray(weights, np.float64)[order]
+    cw = np.concatenate([[0.0], np.cumsum(w)])
+    core = (cw[hi] - cw[lo]) >= min_obs
+    cpos = np.flatnonzero(core)
+    labels_s = np.full(n, -1, np.int64)
+    if cpos.size:
+        new = np.concatenate([[True], np.diff(xs[cpos]) > eps])
+        comp = np.cumsum(new) - 1
+        first = np.full(comp[-1] + 1, n, np.int64)
+        np.minimum.at(first, comp, order[cpos])
+        ids = np.argsort(np.argsort(first, kind="stable"), kind="stable")
+        cid = np.full(n + 1, np.iinfo(np.int64).max, np.int64)
+        cid[cpos] = ids[comp]
+        idx = np.empty(2 * n, np.int64)
+        idx[0::2], idx[1::2] = lo, hi
+        best = np.minimum.reduceat(cid, idx)[0::2]
+        labels_s = np.where(best == np.iinfo(np.int64).max, -1, best)
+        ncl = int(comp[-1] + 1)
+    else:
+        ncl = 0
+    labels = np.empty(n, np.int32)
+    labels[order] = labels_s
+    return ncl, labels
+
+
+def test_dbscan_1d_checker(oracle, rng):
+    for _ in range(12):
+        n = int(rng.integers(1, 1500))
+        x = np.round(rng.uniform(0, 200, n) * 4) / 4
+        eps = float(rng.integers(1, 12)) / 4
+        mo = int(rng.integers(1, 9))
+        w = rng.integers(1, 7, n) / 2.0
+        for weights in (None, w):
+            assert dbscan_1d(x, eps, mo, weights)[0] == oracle.dbscan(x, eps, mo, weights)[0]
+            np.testing.assert_array_equal(dbscan_1d(x, eps, mo, weights)[1], oracle.dbscan(x, eps, mo, weights)[1])
+
+
 def _golden_detector():
     import os
     return dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "detector_golden.npz")))
