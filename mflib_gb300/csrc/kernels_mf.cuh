@@ -112,11 +112,11 @@ template <class T, int LOG2P> struct XcorrLayout
     static constexpr size_t up(size_t v) { return (v + 127) & ~size_t(127); }
     static constexpr size_t seg = sizeof(T) * N;
     static constexpr size_t fft = sizeof(cx<T>) * spad_size(P);
-    // mode 4 keeps a second pair of partial-sum rows (p1, p2) for the second team
+    // after the chunk prefixes: two rows of NCH values (per-chunk partial
+    // sums, or in mode 4 the chunk totals of y and y^2)
     static constexpr size_t head(bool sd, int mode = 0)
     {
-        return up(64 + 32 * sizeof(T) +
-                  (sd ? 0 : 2 * sizeof(acc) * (NCH + 1) + (mode == 4 ? 4 : 2) * sizeof(T) * NCH));
+        return up(64 + 32 * sizeof(T) + (sd ? 0 : 2 * sizeof(acc) * (NCH + 1) + 2 * sizeof(T) * NCH));
     }
     // pass twiddles only; mode 4 holds them in the split layout (FftPlan::tws_off)
     static constexpr size_t tw_bytes_of(int mode)
@@ -131,13 +131,19 @@ template <class T, int LOG2P> struct XcorrLayout
     // work buffer overlays the segment; mode 3 builds the padded copy in the
     // second team's buffer before the forward FFT.
     static constexpr size_t padded = sizeof(T) * (N + N / 32);
+    // mode 4: after the forward FFT the segment's region holds the in-chunk
+    // prefix sums of y and y^2, interleaved (2 N values, and a zero pair at
+    // position N: the prefix where the last lag's window ends), and each team
+    // keeps 8 values per 32-lag run of its template's window statistics
+    static constexpr size_t q12 = sizeof(T) * 2 * (N + 2);
+    static __host__ __device__ size_t rd_bytes(int S) { return up(8 * sizeof(T) * (size_t) (S / 32)); }
     static_assert(((sizeof(cx<T>) * spad_size(P) + 127) & ~size_t(127)) >= sizeof(T) * (N + N / 32),
                   "a work buffer holds the padded segment");
     static constexpr bool overlay(bool sd, int mode) { return sd || mode == 3; }
     static constexpr bool teams(int mode) { return mode >= 2; }
     static constexpr size_t xs_region(bool sd, int mode)
     {
-        return up(overlay(sd, mode) ? (seg > fft ? seg : fft) : padded);
+        return up(overlay(sd, mode) ? (seg > fft ? seg : fft) : mode == 4 ? q12 : padded);
     }
     static constexpr size_t off_xs(bool sd, int mode = 0) { return head(sd, mode); }
     static constexpr size_t off_W0(bool sd, int mode)
@@ -152,14 +158,17 @@ template <class T, int LOG2P> struct XcorrLayout
     static constexpr size_t off_tw(bool sd, int mode) { return off_UV(sd, mode) + up(uv); }
     static constexpr size_t off_B(bool sd, int mode) { return off_tw(sd, mode) + up(tw_bytes_of(mode)); }
     static constexpr size_t off_invd(bool sd, int mode) { return off_B(sd, mode) + (mode == 1 ? 2 * up(brow) : 0); }
-    // mode 4: one normalisation row per team
-    static constexpr int invd_rows(int mode) { return mode == 4 ? 2 : 1; }
+    // one normalisation row (mode 4: a run-statistics row per team)
+    static __host__ __device__ size_t invd_bytes(int mode, int S)
+    {
+        return mode == 4 ? 2 * rd_bytes(S) : up(sizeof(T) * (size_t) S);
+    }
     // fused peak candidates: per team two chunk masks (one bit per 64 lags,
     // P/32 chunks)
     static constexpr int mask_words = (P / 32 + 31) / 32;
     static __host__ __device__ size_t off_M(bool sd, int mode, int S)
     {
-        return off_invd(sd, mode) + invd_rows(mode) * up(sizeof(T) * (size_t) S);
+        return off_invd(sd, mode) + invd_bytes(mode, S);
     }
     static size_t bytes(bool sd, int mode, int S)
     {
@@ -638,6 +647,107 @@ template <> __device__ __forceinline__ void load_pair<double>(const cx<double> *
     b = p[1];
 }
 
+// Mode 4 (each template normalised for its own length) keeps no
+// normalisation rows.  Once per CTA, after the forward FFT has read the
+// staged segment, its region is rewritten as the in-chunk exclusive prefix
+// sums of y = x - m and y^2, interleaved: q12[k] = (sum, sum of squares of
+// y[32 (k/32) .. k)), one warp scan per 32-sample chunk, q12[N] = q12[N + 1]
+// = 0 (a window ending at the segment's end reads q12[N]), and the chunk
+// totals go to tot1 / tot2.  Ends with a barrier.
+template <class T, int N, int NTH>
+__device__ __forceinline__ void seg_prefix_q12(SegStats<T> st, cx<T> *q12, T *tot1, T *tot2, int tid)
+{
+    constexpr int NCH = N / 32, NW = NTH / 32, CPW = (NCH + NW - 1) / NW;
+    const int w = tid >> 5, lane = tid & 31;
+    T v[CPW];
+#pragma unroll
+    for (int i = 0; i < CPW; ++i)
+    {
+        const int j = w + i * NW;
+        v[i] = j < NCH ? st.xs[32 * j + lane] - st.m : (T) 0;
+    }
+    __syncthreads();  // q12 overlays the segment
+    if (tid < 2) q12[N + tid] = cmk((T) 0, (T) 0);
+#pragma unroll
+    for (int i = 0; i < CPW; ++i)
+    {
+        const int j = w + i * NW;
+        if (j >= NCH) break;
+        T a = v[i], b = v[i] * v[i];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const T ua = __shfl_up_sync(0xffffffffu, a, o), ub = __shfl_up_sync(0xffffffffu, b, o);
+            if (lane >= o) { a += ua; b += ub; }
+        }
+        const T ea = __shfl_up_sync(0xffffffffu, a, 1), eb = __shfl_up_sync(0xffffffffu, b, 1);
+        q12[32 * j + lane] = lane ? cmk(ea, eb) : cmk((T) 0, (T) 0);
+        if (lane == 31)
+        {
+            tot1[j] = a;
+            tot2[j] = b;
+        }
+    }
+    __syncthreads();
+}
+
+// Per 32-lag run v of a template of length L = 32 Lq + re (mode 4): the
+// exact (double-float) window statistics at the run's first lag 32 v, as in
+// seg_inv_den -- chunk prefixes of chunks [v, j), j = v + Lq, plus the first
+// re samples of chunk j -- stored as rd[4v..4v+3] = (V0 hi, V0 lo), (2 W1
+// hi, 0), (-a1, t1 - a1), (-a2, t2 - a2): a = the partial sums of chunk j
+// up to re, t = its totals.  Lag 32 v + q of the run then needs only the
+// prefix sums at its head and tail (inv_den_wide).
+template <class T, int NTT>
+__device__ __forceinline__ void seg_run_stats(SegStats<T> st, const cx<T> *q12, const T *tot1, const T *tot2, int L,
+                                              int S, cx<T> *rd, int ttid)
+{
+    using A = acc_t<T>;
+    using O = DenOps<T>;
+    const int Lq = L >> 5, re = L & 31;
+    for (int v = ttid; v < S / 32; v += NTT)
+    {
+        const int j = v + Lq;
+        const cx<T> a = q12[32 * j + re];
+        const auto w1 = A::add_val(A::sub(st.c1[j], st.c1[v]), a.x);
+        const auto w2 = A::add_val(A::sub(st.c2[j], st.c2[v]), a.y);
+        T vh, vl;
+        O::var0(w1, w2, L, vh, vl);
+        rd[4 * v] = cmk(vh, vl);
+        rd[4 * v + 1] = cmk((T) 2 * O::hi(w1), (T) 0);
+        rd[4 * v + 2] = cmk(-a.x, tot1[j] - a.x);
+        rd[4 * v + 3] = cmk(-a.y, tot2[j] - a.y);
+    }
+}
+
+// sqrt(L)/max(tol, sqrt(V)) for the lags k and k + 1 (k even) of a template
+// of length L = 32 Lq + re, from its run statistics (seg_run_stats) and the
+// prefix sums: the window moved by q = k mod 32 lags from the run start
+// gained sum y over [32 v + L, k + L) and lost it over [32 v, k), so
+//   V(k) = V0 + L d2 - d1 (d1 + 2 W1),  d = (tail prefix - a (+ t when k + L
+// passed into chunk j + 1)) - head prefix,
+// the same correction the sliding form accumulates, here without a serial
+// chain.
+template <class T>
+__device__ __forceinline__ cx<T> inv_den_wide(const cx<T> *q12, const cx<T> *rd, int k, int L, int re, T Lt,
+                                              T sqrtL, T tol)
+{
+    using O = DenOps<T>;
+    const int v = k >> 5, q = k & 31;
+    cx<T> r0, r1, ra, rb, h0, h1, t0, t1;
+    load_pair<T>(rd + 4 * v, r0, r1);
+    load_pair<T>(rd + 4 * v + 2, ra, rb);
+    load_pair<T>(q12 + k, h0, h1);
+    if ((L & 1) == 0) load_pair<T>(q12 + k + L, t0, t1);
+    else { t0 = q12[k + L]; t1 = q12[k + L + 1]; }
+    const bool c0 = q + re >= 32, c1 = q + 1 + re >= 32;
+    const T d10 = (t0.x + (c0 ? ra.y : ra.x)) - h0.x, d20 = (t0.y + (c0 ? rb.y : rb.x)) - h0.y;
+    const T d11 = (t1.x + (c1 ? ra.y : ra.x)) - h1.x, d21 = (t1.y + (c1 ? rb.y : rb.x)) - h1.y;
+    const T v0 = r0.x + (r0.y + fma(Lt, d20, -d10 * (d10 + r1.x)));
+    const T v1 = r0.x + (r0.y + fma(Lt, d21, -d11 * (d11 + r1.x)));
+    return cmk(O::out(v0, sqrtL, tol), O::out(v1, sqrtL, tol));
+}
+
 // Bounded wait on a TMA phase; on timeout record the error and let every
 // thread return (the caller returns when this yields false).
 __device__ __forceinline__ bool xcorr_wait(uint64_t *bar, uint32_t parity, int *err, uint32_t limit = (1u << 24))
@@ -810,11 +920,13 @@ __device__ __forceinline__ int xcorr_tile(const XcorrParams<T> &p, const int bx,
         }
         __syncthreads();
     }
+    cx<T> *q12 = reinterpret_cast<cx<T> *>(xs);
     if constexpr (WIDE)
     {
-        // the segment's region is free now: padded demeaned copy; each team
-        // normalises its templates in the loop below
-        seg_make_padded<T, N, NTH>(st, tid);
+        // the segment's region is free now: in-chunk prefix sums of y and
+        // y^2; each team derives its templates' normalisation from them in
+        // the epilogue (inv_den_wide)
+        seg_prefix_q12<T, N, NTH>(st, q12, st.p1, st.p2, tid);
     }
     else if constexpr (!SHARED_DEN && !OWN_DEN)
     {
@@ -890,11 +1002,16 @@ __device__ __forceinline__ int xcorr_tile(const XcorrParams<T> &p, const int bx,
         // lags [k0, k0 + kmax) of this block are stored (kmax <= S, even S)
         const int kmax = (int) (nv - k0 < (long) S ? nv - k0 : (long) S);
         const cx<T> *invd2 = reinterpret_cast<const cx<T> *>(invd_row);
+        const int L = p.tlen[t], re = L & 31;
+        const T Lt = (T) L, sqrtL = sqrt(Lt);
         auto epi = [&](int e, cx<T> z) {
             const int k = 2 * e;
             if (k >= kmax) return;
-            // rows from den_kernel (TMA) are plain, rows from seg_inv_den swizzled
-            const cx<T> d = invd2[SHARED_DEN ? e : inv_den_pair<T>(e)];
+            // rows from den_kernel (TMA) are plain, rows from seg_inv_den
+            // swizzled; mode 4 derives the pair from its run statistics
+            cx<T> d;
+            if constexpr (WIDE) d = inv_den_wide<T>(q12, invd2, k, L, re, Lt, sqrtL, p.tol);
+            else d = invd2[SHARED_DEN ? e : inv_den_pair<T>(e)];
             const T r0 = clamp_rho(z.x * d.x);
             const T r1 = clamp_rho(z.y * d.y);
             if (k + 1 < kmax) store2<T>(dst + k, r0, r1);
@@ -908,18 +1025,12 @@ __device__ __forceinline__ int xcorr_tile(const XcorrParams<T> &p, const int bx,
     if constexpr (WIDE)
     {
         // two teams of 256 threads; each keeps its own work buffer, chunk
-        // masks, normalisation row (its templates' own lengths), partial-sum
-        // rows and barrier
+        // masks, run statistics (its templates' own lengths) and barrier
         const int team = tid >> 8, ttid = tid & 255, bar_id = 1 + team;
         unsigned *mkt = Mk + team * 2 * MW;
         cx<T> *Wt = team ? W1 : W0;
-        T *invd_t = invd_s + team * (LY::up(sizeof(T) * (size_t) S) / sizeof(T));
-        SegStats<T> stt = st;
-        if (team)
-        {
-            stt.p1 = st.p2 + NCH;
-            stt.p2 = stt.p1 + NCH;
-        }
+        // the team's run statistics (seg_run_stats), passed as the epilogue's row
+        cx<T> *rd_t = reinterpret_cast<cx<T> *>(reinterpret_cast<unsigned char *>(invd_s) + team * LY::rd_bytes(S));
         int t_prev = -1, it = 0, Lt = -1;
         for (int j = team; j < ntl; j += 2, ++it)
         {
@@ -937,12 +1048,13 @@ __device__ __forceinline__ int xcorr_tile(const XcorrParams<T> &p, const int bx,
             const int L = p.tlen[t];
             if (L != Lt)
             {
-                // ends with the team's barrier: the row is complete before the epilogue reads it
-                seg_inv_den<T, N, kThreads, -1>(stt, L, S, p.tol, invd_t, ttid, bar_id);
+                // read in the last inverse pass, after the passes' barriers;
+                // the previous template's epilogue finished at the barrier above
+                seg_run_stats<T, kThreads>(st, q12, st.p1, st.p2, L, S, rd_t, ttid);
                 Lt = L;
             }
             template_body(std::integral_constant<int, -1>(), std::integral_constant<int, kThreads>(), j, B, Wt,
-                          mkt + (it & 1) * MW, ttid, bar_id, invd_t);
+                          mkt + (it & 1) * MW, ttid, bar_id, reinterpret_cast<const T *>(rd_t));
             t_prev = t;
         }
         if (pk && it > 0)
