@@ -500,10 +500,13 @@ def run_stress(args):
     U(1e3, 1e5) plus band-passed noise under a piecewise-constant envelope
     (segments of 10-60 min, levels log-uniform in [1e-3, 1e3]) with injected
     template copies at 0.2-1 x the local RMS.  For the FP32 FFT correlator
-    and the split-precision tensor-core correlator: template-lags/s of the
-    applies (CUDA events) and max |drho| against the FP64 oracle on sampled
-    lags of 8 templates per channel, over all sampled lags and over lags
-    whose window and FFT blocks stay inside one envelope segment."""
+    and the split-precision tensor-core correlator (FP16 hi+lo operands):
+    template-lags/s of the applies (CUDA events) and max |drho| against the
+    FP64 oracle on sampled lags of 8 templates per channel, over all sampled
+    lags and over lags whose window and FFT blocks stay inside one envelope
+    segment; for the tensor-core correlator also the raw error (the accuracy
+    fix-up skipped), and the same raw figures with BF16 hi+lo operands, whose
+    error bound sends every run to the fix-up."""
     import torch
     import mflib_gb300 as mf
     from scipy.signal import butter, sosfilt
@@ -537,7 +540,22 @@ def run_stress(args):
         edges_all.append(np.array(edges))
     o = Oracle()
     out = {}
-    for name, variant in (("fft", 3), ("tensor", 4)):
+    def errors(f, c, xs, e):
+        lr = np.random.default_rng(7 + c)
+        wa, wf = 0.0, 0.0
+        for t in lr.choice(nt, 8, replace=False):
+            lags = np.sort(lr.choice(n - L + 1, 500, replace=False))
+            truth = o.pearson_naive(tps[t], xs, lags)
+            got = f.get_matched_filtered_signal(int(t)).astype(np.float64)[lags]
+            err = np.abs(got - truth)
+            wa = max(wa, float(err.max()))
+            seg = np.searchsorted(e, lags, side="right") - 1
+            flat = (lags - 8192 >= e[seg]) & (lags + L + 8192 <= e[seg + 1])
+            if flat.any():
+                wf = max(wf, float(err[flat].max()))
+        return wa, wf
+
+    for name, variant, bf16 in (("fft", 3, False), ("tensor", 4, False), ("tensor_bf16", 4, True)):
         p = mf.SingleChannel.MatchedFilterParameters()
         for tp in tps:
             wt = mf.WaveformTemplate()
@@ -546,10 +564,13 @@ def run_stress(args):
             p.add_template(wt)
         p.set_signal_size(n)
         f = mf.SingleChannel.MatchedFilter(dtype=np.float32)
-        f.initialize(p, correlator_variant=variant)
+        f.initialize(p, correlator_variant=variant, tc_bf16=bf16)
+        # BF16: every run's bound is over the tolerance; time and check the
+        # raw correlator (flagged runs counted, not recomputed)
+        f.test_skip_fixup(bf16)
         stream = torch.cuda.ExternalStream(f.stream_handle())
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        total_ms, worst_all, worst_flat, fixups = 0.0, 0.0, 0.0, 0
+        total_ms, worst_all, worst_flat, fixups, raw_all, raw_flat = 0.0, 0.0, 0.0, 0, 0.0, 0.0
         for c in range(nch):
             f.set_signal(chans[c])
             f.apply()  # warm
@@ -561,24 +582,27 @@ def run_stress(args):
             torch.cuda.synchronize()
             total_ms += ev0.elapsed_time(ev1)
             fixups += f.get_fixup_runs()
-            lr = np.random.default_rng(7 + c)
             xs = chans[c].astype(np.float64)
-            e = edges_all[c]
-            for t in lr.choice(nt, 8, replace=False):
-                lags = np.sort(lr.choice(n - L + 1, 500, replace=False))
-                truth = o.pearson_naive(tps[t], xs, lags)
-                got = f.get_matched_filtered_signal(int(t)).astype(np.float64)[lags]
-                err = np.abs(got - truth)
-                worst_all = max(worst_all, float(err.max()))
-                seg = np.searchsorted(e, lags, side="right") - 1
-                flat = (lags - 8192 >= e[seg]) & (lags + L + 8192 <= e[seg + 1])
-                if flat.any():
-                    worst_flat = max(worst_flat, float(err[flat].max()))
+            wa, wf = errors(f, c, xs, edges_all[c])
+            worst_all, worst_flat = max(worst_all, wa), max(worst_flat, wf)
+            if variant == 4 and not bf16:
+                f.test_skip_fixup(True)
+                f.apply()
+                wa, wf = errors(f, c, xs, edges_all[c])
+                raw_all, raw_flat = max(raw_all, wa), max(raw_flat, wf)
+                f.test_skip_fixup(False)
         lags_total = float(nch) * nt * (n - L + 1)
-        out[name] = {"template_lags_per_s": lags_total / (total_ms * 1e-3), "apply_ms_per_channel": total_ms / nch,
-                     "max_abs_drho_all": worst_all, "max_abs_drho_away_from_envelope_steps": worst_flat,
-                     "fixup_runs": fixups, "runs": nch * ((n - L + 1 + 31) // 32),
-                     "correlator": f.get_plan()["correlator"]}
+        res = {"template_lags_per_s": lags_total / (total_ms * 1e-3), "apply_ms_per_channel": total_ms / nch,
+               "max_abs_drho_all": worst_all, "max_abs_drho_away_from_envelope_steps": worst_flat,
+               "fixup_runs": fixups, "runs": nch * ((n - L + 1 + 31) // 32),
+               "correlator": f.get_plan()["correlator"], "operands": "bf16 hi+lo" if bf16 else
+               ("fp16 hi+lo" if variant == 4 else "fp32")}
+        if bf16:
+            res["fixup"] = "skipped: figures are the raw correlator's; fixup_runs counts the flagged runs"
+        elif variant == 4:
+            res["raw_max_abs_drho_all"] = raw_all
+            res["raw_max_abs_drho_away_from_envelope_steps"] = raw_flat
+        out[name] = res
         f.clear()
     line = {"metric": "precision stress: template-lag correlations/s and max |drho| vs FP64 oracle", "n_gpus": 1,
             "dtype": "f32", "config": {"workload": "512 templates x 1,000 against 16 channels x %d samples, all pairs,"

@@ -120,6 +120,13 @@ typedef struct
        length >= 4096; ignored otherwise).  0 = the static grid, which
        measured faster on GB300. */
     int persistent;
+    /* Extension, for precision comparison: 1 = the tensor-core correlator
+       splits its operands into BF16 hi + lo (about 16 bits of each FP32
+       value kept) instead of FP16 hi + lo (22 bits).  Its error bound then
+       exceeds the 2e-5 tolerance everywhere, so the accuracy fix-up
+       recomputes every run by direct correlation: correct but slow.
+       0 = FP16. */
+    int tc_bf16;
 } mfgpu_mf_params;
 
 /* MatchedFilter<T>::MatchedFilter(); precision MFGPU_FLOAT32 | MFGPU_FLOAT64 */
@@ -305,6 +312,13 @@ mfgpu_status mfgpu_mf_get_fixup_runs(mfgpu_mf *mf, long long *runs);
  * the device status word, and later applies run normally.  The apply is not
  * captured into a CUDA graph.  MFGPU_EINVAL for the tensor-core correlator. */
 mfgpu_status mfgpu_mf_test_wait_timeout(mfgpu_mf *mf);
+/* No reference counterpart; for measuring a correlator's raw rounding
+ * error.  skip = 1: later applies of an FP32 object still flag the runs
+ * whose error bound exceeds the tolerance (mfgpu_mf_get_fixup_runs counts
+ * them) but do not recompute them, so the coefficients carry the chosen
+ * correlator's own error; skip = 0 restores the fix-up.  Waits for the
+ * object's work and drops its captured CUDA graphs. */
+mfgpu_status mfgpu_mf_test_skip_fixup(mfgpu_mf *mf, int skip);
 /* The object's CUDA stream (a cudaStream_t), on which every launch and
  * copy of the object is issued; for event timing by the caller. */
 mfgpu_status mfgpu_mf_get_stream(const mfgpu_mf *mf, void **stream);

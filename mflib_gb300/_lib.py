@@ -74,6 +74,7 @@ class MfgpuParams(C.Structure):
         ("bucket_fft_lengths", C.POINTER(C.c_int)),
         ("bucket_variants", C.POINTER(C.c_int)),
         ("persistent", C.c_int),
+        ("tc_bf16", C.c_int),
     ]
 
 
@@ -122,6 +123,7 @@ _SIGS = {
     "mfgpu_mf_get_launch_count": ([_vp, C.POINTER(C.c_longlong)], C.c_int),
     "mfgpu_mf_get_fixup_runs": ([_vp, C.POINTER(C.c_longlong)], C.c_int),
     "mfgpu_mf_test_wait_timeout": ([_vp], C.c_int),
+    "mfgpu_mf_test_skip_fixup": ([_vp, C.c_int], C.c_int),
     "mfgpu_mf_get_stream": ([_vp, C.POINTER(_vp)], C.c_int),
     "mfgpu_mf_find_peaks": ([_vp, C.c_double, C.c_int, C.c_int], C.c_int),
     "mfgpu_mf_set_peak_threshold": ([_vp, C.c_double], C.c_int),

@@ -281,6 +281,8 @@ struct mfgpu_mf
     bool test_wait_timeout = false;  // mfgpu_mf_test_wait_timeout: the next apply only
     int dev_smem = 0;                // opt-in shared memory per block of the device
     bool persistent = false;         // FFT correlator as a persistent work-queue launch (option)
+    bool tc_bf16 = false;            // tensor-core operands split into BF16 instead of FP16 (option)
+    bool test_skip_fixup = false;    // mfgpu_mf_test_skip_fixup: flag runs but do not recompute them
 
     size_t esz() const { return (size_t) prec; }
     template <class F> void each_buf(F &&f)
@@ -600,6 +602,7 @@ try
     mf->fLen = ntf > 0 ? fMax : 0;
     mf->fMin = ntf > 0 ? fMin : 0;
     mf->persistent = p->persistent != 0;
+    mf->tc_bf16 = p->tc_bf16 != 0;
     if (ndirect > 0)
     {
         if (p->correlator_variant == 4)
@@ -1103,7 +1106,7 @@ try
         CU(cudaMemcpyAsync(mf->tc_grp_tid.p, tc_gtid.data(), sizeof(int) * slots, cudaMemcpyHostToDevice, mf->stream));
         CU(launch_tc_bank(mf->tmpl_d.as<double>(), mf->toff_d.as<long>(), mf->tlen_d.as<int>(),
                           mf->tc_grp_tid.as<int>(), mf->tc_groups, mf->tc_Gp, mf->tc_Kp, mf->tc_B.as<__half>(),
-                          mf->tc_bscale.as<float>(), mf->stream));
+                          mf->tc_bscale.as<float>(), mf->tc_bf16, mf->stream));
         ++mf->launches;
     }
     if (mf->fx_on || ndirect > 0)
@@ -1661,8 +1664,9 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
                                       mf->fx_nruns, mf->dlags.as<int>(), mf->tc_tiles, mf->nch,
                                       mf->dead.as<unsigned char>(),
                                       mf->xrange.as<float>(), mf->tc_off.as<float>(),
-                                      mf->fxbits.as<unsigned>(), mf->fxlist.as<int>(), mf->fxcount.as<int>(), kFixTcC1,
-                                      kFixTcC2, kFixTol, mf->stream));
+                                      mf->fxbits.as<unsigned>(), mf->fxlist.as<int>(), mf->fxcount.as<int>(),
+                                      mf->tc_bf16 ? kFixTcC1Bf16 : kFixTcC1, mf->tc_bf16 ? kFixTcC2Bf16 : kFixTcC2,
+                                      kFixTol, mf->stream));
                 ++mf->launches;
             }
             else
@@ -1738,7 +1742,7 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
                 q.pk_thr = (float) mf->pk_req;
             }
             const long work = (long) q.ngroups * q.tiles;
-            CU(launch_tc_xcorr(q, (int) std::min<long>(mf->n_sm, work), mf->stream));
+            CU(launch_tc_xcorr(q, (int) std::min<long>(mf->n_sm, work), mf->tc_bf16, mf->stream));
             ++mf->launches;
             if (q.pk_flags)
             {
@@ -1827,7 +1831,7 @@ template <class T> static mfgpu_status mf_launch_fixup(mfgpu_mf *mf)
         f.S0 = mf->S;
     }
     const int nctas = 4 * std::max(1, mf->n_sm);
-    if (mf->fx_on && mf->nblocks > 0)
+    if (mf->fx_on && mf->nblocks > 0 && !mf->test_skip_fixup)
     {
         FixParams<T> g = f;
         g.flist = mf->fxlist.as<int>(); g.fcount = mf->fxcount.as<int>();
@@ -2045,6 +2049,22 @@ try
 {
     if (!mf || !count) return fail(MFGPU_EINVAL, "NULL argument");
     *count = mf->launches;
+    return MFGPU_OK;
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
+
+mfgpu_status mfgpu_mf_test_skip_fixup(mfgpu_mf *mf, int skip)
+try
+{
+    if (!mf) return fail(MFGPU_EINVAL, "mf is NULL");
+    DeviceGuard g(mf->dev);
+    if (mf->copy_stream) CU(cudaStreamSynchronize(mf->copy_stream));
+    CU(cudaStreamSynchronize(mf->stream));
+    mf->drop_graphs();  // captured applies hold the old setting
+    mf->test_skip_fixup = skip != 0;
     return MFGPU_OK;
 }
 catch (...)

@@ -20,6 +20,11 @@ constexpr float kFixTol = 2.0e-5f;
 constexpr float kFixFftK = 8.0f;
 constexpr float kFixTcC1 = 2.0e-6f;
 constexpr float kFixTcC2 = 0x1p-23f;
+// BF16 hi+lo keeps 2^-18 of each operand instead of 2^-22: C1 sixteen times
+// larger (above the tolerance itself, so every run is recomputed), and no
+// subnormal floor in BF16's exponent range
+constexpr float kFixTcC1Bf16 = 16 * kFixTcC1;
+constexpr float kFixTcC2Bf16 = 0.f;
 
 // Fix-up batches: the templates of a channel sorted by length, kFixBatch per
 // batch; coefficients (demeaned, unit norm, in the sample type) interleaved

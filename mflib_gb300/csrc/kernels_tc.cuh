@@ -31,12 +31,43 @@
 //                   stores.
 // Strips and accumulators are double-buffered (mbarriers, bounded waits);
 // the group's template operands stay resident in shared memory.
+//
+// BF16 operands (template flag BF, an option for precision comparison): the
+// same kernel with BF16 hi and lo (about 16 of the 24 bits kept, against 22
+// for FP16; BF16's exponent range needs no scaling but the powers of two
+// are kept), and the instruction descriptor's A and B format fields set to
+// BF16.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include "kernels_mf.cuh"
 #include "tc_params.h"
 
 namespace mfgpu {
+
+// hi + lo split of an FP32 value into two 16-bit operands (bit patterns
+// stored as __half either way) and the matching kind::f16 A / B format bits
+template <bool BF> struct TcSplit;
+template <> struct TcSplit<false>
+{
+    static constexpr uint32_t ab_format = 0u;
+    static __device__ __forceinline__ void split(float y, __half &h, __half &l)
+    {
+        h = __float2half_rn(y);
+        l = __float2half_rn(y - __half2float(h));
+    }
+};
+template <> struct TcSplit<true>
+{
+    static constexpr uint32_t ab_format = (1u << 7) | (1u << 10);
+    static __device__ __forceinline__ void split(float y, __half &h, __half &l)
+    {
+        const __nv_bfloat16 bh = __float2bfloat16_rn(y);
+        const __nv_bfloat16 bl = __float2bfloat16_rn(y - __bfloat162float(bh));
+        h = __ushort_as_half(__bfloat16_as_ushort(bh));
+        l = __ushort_as_half(__bfloat16_as_ushort(bl));
+    }
+};
 
 // shared-memory matrix descriptor: start address, leading and stride byte
 // offsets (16-byte units), descriptor version 1, no swizzle
@@ -70,11 +101,11 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
 // Template bank in MMA layout: one CTA per (group, slot).  Row 8*slot + f of
 // the group's B holds the demeaned unit-norm template (FP64 preparation as
 // in the FFT path) shifted right by f, scaled by a power of two, split into
-// FP16 hi and lo; element (row n, k) sits in core matrix (n/8, k/8) at
+// FP16 (or BF16) hi and lo; element (row n, k) sits in core matrix (n/8, k/8) at
 // ((n/8) * Kp/8 + k/8) * 64 + (n%8) * 8 + k%8.
-static __global__ void __launch_bounds__(256) tc_bank_kernel(const double *tmpl, const long *toff, const int *tlen,
-                                                              const int *grp_tid, int Gp, int Kp, __half *B,
-                                                              float *bscale)
+template <bool BF>
+__global__ void __launch_bounds__(256) tc_bank_kernel(const double *tmpl, const long *toff, const int *tlen,
+                                                      const int *grp_tid, int Gp, int Kp, __half *B, float *bscale)
 {
     __shared__ double red[32];
     const int g = blockIdx.x / Gp, slot = blockIdx.x % Gp;
@@ -123,15 +154,16 @@ static __global__ void __launch_bounds__(256) tc_bank_kernel(const double *tmpl,
         const int f = idx / Kp, k = idx % Kp;
         const int j = k - f;
         const float v = (t >= 0 && j >= 0 && j < L) ? (float) ((b[j] - mean) * inv) : 0.f;
-        const __half h = __float2half_rn(v);
-        const __half l = __float2half_rn(v - __half2float(h));
+        __half h, l;
+        TcSplit<BF>::split(v, h, l);
         const size_t o = ((size_t) slot * KG + k / 8) * 64 + f * 8 + (k & 7);
         bh[o] = h;
         bl[o] = l;
     }
 }
 
-static __global__ void __launch_bounds__(kTcThreads, 1) tc_xcorr_kernel(TcParams p)
+template <bool BF>
+__global__ void __launch_bounds__(kTcThreads, 1) tc_xcorr_kernel(TcParams p)
 {
     extern __shared__ __align__(128) unsigned char smem_tc[];
     uint64_t *bar = reinterpret_cast<uint64_t *>(smem_tc);  // a_full[2] a_empty[2] acc_full[2] acc_empty[2] b_full
@@ -169,8 +201,9 @@ static __global__ void __launch_bounds__(kTcThreads, 1) tc_xcorr_kernel(TcParams
             // ---- MMA issue.  Instruction descriptors: D f32, A/B f16, both
             //      K-major, N >> 3, M >> 4; N = 16 Gp (hi and lo rows of B)
             //      and N = 8 Gp (hi rows only)
-            const uint32_t idesc_w = (1u << 4) | ((uint32_t) (2 * N >> 3) << 17) | ((uint32_t) (kTcRows >> 4) << 24);
-            const uint32_t idesc_n = (1u << 4) | ((uint32_t) (N >> 3) << 17) | ((uint32_t) (kTcRows >> 4) << 24);
+            constexpr uint32_t fmt = (1u << 4) | TcSplit<BF>::ab_format;
+            const uint32_t idesc_w = fmt | ((uint32_t) (2 * N >> 3) << 17) | ((uint32_t) (kTcRows >> 4) << 24);
+            const uint32_t idesc_n = fmt | ((uint32_t) (N >> 3) << 17) | ((uint32_t) (kTcRows >> 4) << 24);
             const uint32_t bbytes = (uint32_t) TcLayout::b_bytes(Kp, Gp);
             const uint32_t sA0 = smem_u32(sA), sB0 = smem_u32(sB);
             // the lo rows follow the hi rows at the same row-group stride, so
@@ -269,11 +302,7 @@ static __global__ void __launch_bounds__(kTcThreads, 1) tc_xcorr_kernel(TcParams
                         __align__(8) __half h[4];
                         __align__(8) __half l[4];
 #pragma unroll
-                        for (int q = 0; q < 4; ++q)
-                        {
-                            h[q] = __float2half_rn(y[q]);
-                            l[q] = __float2half_rn(y[q] - __half2float(h[q]));
-                        }
+                        for (int q = 0; q < 4; ++q) TcSplit<BF>::split(y[q], h[q], l[q]);
                         *reinterpret_cast<uint2 *>(ah + e) = *reinterpret_cast<const uint2 *>(h);
                         *reinterpret_cast<uint2 *>(al + e) = *reinterpret_cast<const uint2 *>(l);
                     }

@@ -44,9 +44,10 @@ template <class T> cudaError_t launch_dead(const T *x, long ldx, int nch, long n
 // tensor-core correlator (FP32, one template length): shared memory per CTA,
 // the template bank in MMA layout (ngroups * Gp slots), the persistent launch
 size_t tc_smem_bytes(int Kp, int Gp);
+// bf16: operands split into BF16 hi + lo instead of FP16 (precision comparison)
 cudaError_t launch_tc_bank(const double *tmpl, const long *toff, const int *tlen, const int *grp_tid, int ngroups,
-                           int Gp, int Kp, __half *B, float *bscale, cudaStream_t s);
-cudaError_t launch_tc_xcorr(const TcParams &p, int nctas, cudaStream_t s);
+                           int Gp, int Kp, __half *B, float *bscale, bool bf16, cudaStream_t s);
+cudaError_t launch_tc_xcorr(const TcParams &p, int nctas, bool bf16, cudaStream_t s);
 // FP32 accuracy safeguards (kernels_fix.cuh): cancellation-free window
 // variances with per-run statistics (float4 per 32 lags, row stride ldrs;
 // den optional) and per-chunk statistics (float2 per 32 samples, row stride

@@ -166,7 +166,7 @@ class MatchedFilter:
         return self._dtype
 
     def initialize(self, params, template_channels=None, n_channels=None, fft_length=0, correlator_variant=0,
-                   length_buckets=0, bucket_plans=None, persistent=False):
+                   length_buckets=0, bucket_plans=None, persistent=False, tc_bf16=False):
         """MatchedFilter<T>::initialize (src/matchedFilter.cpp:507-821).
 
         Extensions: ``template_channels`` (one channel index per template,
@@ -185,7 +185,10 @@ class MatchedFilter:
         a list of (fft_length, correlator_variant) pairs, 0 keeping the
         automatic choice (see ``autotune``); ``persistent`` runs the FFT
         correlator as one persistent launch fed by a device work ticket
-        (FP32, variants 3 and 6; the static grid is the default)."""
+        (FP32, variants 3 and 6; the static grid is the default);
+        ``tc_bf16`` splits the tensor-core correlator's operands into BF16
+        hi + lo instead of FP16 (precision comparison: every run is then
+        recomputed by the accuracy fix-up)."""
         if not isinstance(params, MatchedFilterParameters) or not params.is_valid():
             raise ValueError("Parameters are invalid")
         tmpls = [params.get_template(i) for i in range(params.get_number_of_templates())]
@@ -226,10 +229,12 @@ class MatchedFilter:
             p.bucket_fft_lengths = bfl
             p.bucket_variants = bva
         p.persistent = 1 if persistent else 0
+        p.tc_bf16 = 1 if tc_bf16 else 0
         _lib.call("mfgpu_mf_initialize", self._h, C.byref(p))
         self._init_kw = dict(template_channels=template_channels, n_channels=n_channels, fft_length=fft_length,
                              correlator_variant=correlator_variant, length_buckets=length_buckets,
-                             bucket_plans=list(bucket_plans) if bucket_plans else None, persistent=persistent)
+                             bucket_plans=list(bucket_plans) if bucket_plans else None, persistent=persistent,
+                             tc_bf16=tc_bf16)
         self._params = params
         self._nt = nt
         self._templates = tmpls
@@ -545,6 +550,12 @@ class MatchedFilter:
         v = C.c_longlong()
         _lib.call("mfgpu_mf_get_fixup_runs", self._h, C.byref(v))
         return v.value
+
+    def test_skip_fixup(self, skip=True):
+        """Test support: later applies flag the runs over the error bound
+        (``get_fixup_runs`` counts them) without recomputing them, so the
+        coefficients carry the correlator's raw rounding error."""
+        _lib.call("mfgpu_mf_test_skip_fixup", self._h, 1 if skip else 0)
 
     def stream_handle(self):
         """The object's cudaStream_t as an integer (every launch and copy of

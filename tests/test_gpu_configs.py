@@ -185,6 +185,51 @@ def test_precision_stress(gpu, oracle, dtype, variant, capsys):
         assert f.get_fixup_runs() > 0
 
 
+def test_tc_operand_splits_raw_error(gpu, oracle, capsys):
+    """The tensor-core correlator's raw error (the fix-up skipped) with FP16
+    and with BF16 hi+lo operands on the stress channels, at lags whose FFT
+    block and window stay inside one envelope segment.  BF16 keeps about 16
+    bits of each operand against FP16's 22, but the representation errors
+    average out over the window: both raw errors sit at the FP32
+    accumulation's level, within the tolerance.  The BF16 worst-case bound
+    still flags every run, and with the fix-up on the object is
+    oracle-equal."""
+    mf = gpu
+    tp, chans, bounds = stress_case()
+    n = chans[0].size
+    rng = np.random.default_rng(9)
+    lags = np.sort(rng.choice(n - tp.size + 1, 4000, replace=False))
+    raw = {}
+    for bf16 in (False, True):
+        f = mf.MultiChannel.MatchedFilter(dtype=np.float32)
+        f.initialize(_params(mf, [tp, tp], n), template_channels=[0, 1], n_channels=2, correlator_variant=4,
+                     tc_bf16=bf16)
+        f.set_channel_signals(np.stack([c.astype(np.float32) for c in chans]))
+        worst = {}
+        for skip in (True, False):
+            f.test_skip_fixup(skip)
+            f.apply()
+            w_all, w_flat = 0.0, 0.0
+            for c in range(2):
+                x = chans[c].astype(np.float32).astype(np.float64)
+                err = np.abs(f.get_valid_matched_filtered_signal(c).astype(np.float64)[lags]
+                             - oracle.pearson_naive(tp, x, lags))
+                e = bounds[c]
+                seg = np.searchsorted(e, lags, side="right") - 1
+                flat = (lags - 4096 >= e[seg]) & (lags + tp.size + 4096 <= e[seg + 1])
+                w_all = max(w_all, float(err.max()))
+                w_flat = max(w_flat, float(err[flat].max()))
+            worst[skip] = (w_all, w_flat)
+            if bf16:
+                assert f.get_fixup_runs() >= 0.99 * 2 * ((n - tp.size + 1 + 31) // 32)
+        raw[bf16] = worst[True][1]
+        assert worst[False][0] < 1e-4, (bf16, worst)
+    with capsys.disabled():
+        print("\ntensor-core raw max|drho| away from envelope steps: fp16 hi+lo %.3g, bf16 hi+lo %.3g"
+              % (raw[False], raw[True]))
+    assert raw[False] < 2e-5 and raw[True] < 2e-5, raw
+
+
 @pytest.mark.parametrize("variant", [0, 4])
 def test_precision_stress_all_lags_and_peaks(gpu, oracle, variant):
     """One stress channel, every lag of the trace against the FP64 two-pass
