@@ -231,6 +231,31 @@ mfgpu_status mfgpu_mf_get_bucket_plans(const mfgpu_mf *mf, int max, int *lags_pe
  * Coefficients at lags k <= n - L_t use window samples only.  Copies before
  * returning, like setSignal. */
 mfgpu_status mfgpu_mf_set_window(mfgpu_mf *mf, int n_src, int n, const void *x, long ld);
+/* ---- Device ring of recent samples per channel.  No reference
+ * counterpart: a serving loop keeps each station channel's latest samples
+ * on the device, appends only the new samples, and sets a request's window
+ * from the ring by a device gather instead of uploading the window from the
+ * host.  Sample s (counted from the first append) of channel c lives at
+ * c * capacity + s mod capacity; the last `capacity` samples are kept.
+ * Appends and window reads of one ring are serialised by the ring. */
+typedef struct mfgpu_ring mfgpu_ring;
+/* precision MFGPU_FLOAT32 | MFGPU_FLOAT64 (that of the objects it feeds);
+ * n_channels rows of capacity samples, zeroed, on the current device */
+mfgpu_status mfgpu_ring_create(int precision, int n_channels, long capacity, mfgpu_ring **ring);
+mfgpu_status mfgpu_ring_destroy(mfgpu_ring *ring);
+/* Appends n samples to every channel from host rows with stride ld (ld is
+ * ignored for one channel); copies before returning.  Of a chunk longer
+ * than the capacity only its last capacity samples are kept. */
+mfgpu_status mfgpu_ring_append(mfgpu_ring *ring, int n, const void *x, long ld);
+/* Samples appended per channel so far (the end of the newest window). */
+mfgpu_status mfgpu_ring_get_head(mfgpu_ring *ring, long long *appended);
+/* mfgpu_mf_set_window with the window read from a ring: samples
+ * [end - n, end) of ring channels channels[0 .. n_src) (NULL: 0 .. n_src-1)
+ * become the object's source rows; the window must still be in the ring
+ * (end <= head, end - n >= head - capacity) and n_src <= 256.  Same
+ * precision and device as the object; waits for the gather. */
+mfgpu_status mfgpu_mf_set_window_ring(mfgpu_mf *mf, mfgpu_ring *ring, int n_src, const int *channels,
+                                      long long end, int n);
 /* Device bytes the object holds (its buffers and peak-finder scratch), for
  * admission against a memory budget.  Extension: no reference counterpart. */
 mfgpu_status mfgpu_mf_get_device_bytes(const mfgpu_mf *mf, unsigned long long *bytes);

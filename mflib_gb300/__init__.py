@@ -9,7 +9,7 @@ behind the C ABI in include/mfgpu.h).
 """
 from .waveform import (MatchedFilterDetectionMode, MatchedFilterImplementation, NetworkStationPhase,
                        Polarity, WaveformTemplate)
-from .matched_filter import (MatchedFilter, MatchedFilterParameters, MultiChannel, SingleChannel,
+from .matched_filter import (MatchedFilter, MatchedFilterParameters, MultiChannel, SignalRing, SingleChannel,
                              compute_optimal_fft_and_block_length)
 from .detection import DBSCAN, PeakFinder
 from ._lib import MfgpuError, MfgpuTimeout
@@ -24,7 +24,8 @@ __version__ = "1.0.0"
 __all__ = [
     "DBSCAN", "MatchedFilter", "MatchedFilterDetectionMode", "MatchedFilterImplementation",
     "MatchedFilterParameters", "MfgpuError", "MfgpuTimeout", "MultiChannel", "NetworkStationPhase",
-    "PeakFinder", "Polarity", "SingleChannel", "WaveformTemplate", "compute_optimal_fft_and_block_length",
+    "PeakFinder", "Polarity", "SignalRing", "SingleChannel", "WaveformTemplate",
+    "compute_optimal_fft_and_block_length",
     "DetectionTimeInterpolationType", "MatchedFilteredSignalDetectorPolicy", "MaximumMatchedFilterPolicy",
     "RelativeMagnitudeType",
 ]

@@ -117,6 +117,11 @@ _SIGS = {
     "mfgpu_relative_amplitudes": ([C.c_int, C.c_int, _vp, C.c_int, _vp, C.c_long, _vp, _vp, _ip], C.c_int),
     "mfgpu_mf_get_detections": ([_vp, C.c_int, C.POINTER(MfgpuDetection), _ip], C.c_int),
     "mfgpu_mf_set_window": ([_vp, C.c_int, C.c_int, _vp, C.c_long], C.c_int),
+    "mfgpu_ring_create": ([C.c_int, C.c_int, C.c_long, C.POINTER(_vp)], C.c_int),
+    "mfgpu_ring_destroy": ([_vp], C.c_int),
+    "mfgpu_ring_append": ([_vp, C.c_int, _vp, C.c_long], C.c_int),
+    "mfgpu_ring_get_head": ([_vp, C.POINTER(C.c_longlong)], C.c_int),
+    "mfgpu_mf_set_window_ring": ([_vp, _vp, C.c_int, _ip, C.c_longlong, C.c_int], C.c_int),
     "mfgpu_mf_get_device_bytes": ([_vp, C.POINTER(C.c_ulonglong)], C.c_int),
     "mfgpu_mf_synchronize": ([_vp], C.c_int),
     "mfgpu_mf_get_last_timings": ([_vp, C.POINTER(C.c_float), C.POINTER(C.c_float)], C.c_int),

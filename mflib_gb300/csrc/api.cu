@@ -12,12 +12,14 @@
 #include <limits>
 #include <string>
 #include <memory>
+#include <mutex>
 #include <new>
 #include <stdexcept>
 #include <vector>
 #include "mfgpu.h"
 #include "launch.h"
 #include "kernels_detect.cuh"
+#include "kernels_ring.cuh"
 
 using namespace mfgpu;
 
@@ -1498,34 +1500,34 @@ catch (...)
     return mfgpu::status_of_exception();
 }
 
-mfgpu_status mfgpu_mf_set_window(mfgpu_mf *mf, int n_src, int n, const void *x, long ld)
-try
+// Checks and state shared by the window setters: n_src source rows, n
+// samples; the caller then fills rows [0, n_src) of x with the window.
+static mfgpu_status mf_window_begin(mfgpu_mf *mf, int n_src, int n)
 {
-    MF_CHECK_INIT(mf);
-    DeviceGuard g(mf->dev);
     if (n_src < 1 || n_src > mf->nch)
         return fail(MFGPU_EINVAL, "n_src = " + std::to_string(n_src) + " must be in [1, " + std::to_string(mf->nch) + "]");
     if (n < 1 || n > mf->n)
         return fail(MFGPU_EINVAL, "window length " + std::to_string(n) + " must be in [1, " + std::to_string(mf->n) + "]");
-    if (!x) return fail(MFGPU_EINVAL, "x is NULL");
-    if (n_src > 1 && ld < n) return fail(MFGPU_EINVAL, "row stride is smaller than the number of samples");
     mfgpu_status rs = mf_resolve_stage(mf);
     if (rs != MFGPU_OK) return rs;
     rs = mf_set_data_length(mf, n);
     if (rs != MFGPU_OK) return rs;
     mf->have = false;
     mf->have_peaks = false;
+    return MFGPU_OK;
+}
+
+// After the window's rows are in place: zero tail, channels c >= n_src
+// repeating channel c % n_src, dead-trace flags over the window; waits.
+static mfgpu_status mf_window_end(mfgpu_mf *mf, int n_src, int n)
+{
     const size_t es = mf->esz(), pitch = es * (size_t) mf->ldx;
     char *x0 = mf->x.as<char>();
-    CU(cudaMemcpy2DAsync(x0, pitch, x, es * (size_t) (n_src > 1 ? ld : n), es * (size_t) n, (size_t) n_src,
-                         cudaMemcpyHostToDevice, mf->stream));
     if (n < mf->n)
         CU(cudaMemset2DAsync(x0 + es * (size_t) n, pitch, 0, es * (size_t) (mf->n - n), (size_t) n_src, mf->stream));
-    // channel c >= n_src repeats channel c % n_src
     for (int c0 = n_src; c0 < mf->nch; c0 += n_src)
         CU(cudaMemcpy2DAsync(x0 + pitch * (size_t) c0, pitch, x0, pitch, es * (size_t) mf->n,
                              (size_t) std::min(n_src, mf->nch - c0), cudaMemcpyDeviceToDevice, mf->stream));
-    // dead-trace flags and ranges over the window's samples only
     if (mf->prec == 4)
         CU(launch_dead<float>(mf->x.as<float>(), mf->ldx, mf->nch, n, mf->dead.as<unsigned char>(),
                               mf->pmin.as<float>(), mf->pmax.as<float>(), mf->dead_chunks, mf->stream,
@@ -1536,6 +1538,173 @@ try
     mf->launches += 2;
     CU(cudaStreamSynchronize(mf->stream));
     return MFGPU_OK;
+}
+
+mfgpu_status mfgpu_mf_set_window(mfgpu_mf *mf, int n_src, int n, const void *x, long ld)
+try
+{
+    MF_CHECK_INIT(mf);
+    DeviceGuard g(mf->dev);
+    if (!x) return fail(MFGPU_EINVAL, "x is NULL");
+    if (n_src > 1 && ld < n) return fail(MFGPU_EINVAL, "row stride is smaller than the number of samples");
+    mfgpu_status rs = mf_window_begin(mf, n_src, n);
+    if (rs != MFGPU_OK) return rs;
+    const size_t es = mf->esz(), pitch = es * (size_t) mf->ldx;
+    CU(cudaMemcpy2DAsync(mf->x.as<char>(), pitch, x, es * (size_t) (n_src > 1 ? ld : n), es * (size_t) n,
+                         (size_t) n_src, cudaMemcpyHostToDevice, mf->stream));
+    return mf_window_end(mf, n_src, n);
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
+
+// ---- device ring of recent samples per channel (no reference counterpart)
+struct mfgpu_ring
+{
+    int dev = 0, prec = 4, nch = 0;
+    long cap = 0;          // samples kept per channel
+    long long head = 0;    // samples appended so far: sample s of channel c at c * cap + s mod cap
+    DevBuf buf;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;         // appends and window reads
+    size_t esz() const { return (size_t) prec; }
+};
+
+mfgpu_status mfgpu_ring_create(int precision, int n_channels, long capacity, mfgpu_ring **out)
+try
+{
+    if (!out) return fail(MFGPU_EINVAL, "ring is NULL");
+    if (precision != MFGPU_FLOAT32 && precision != MFGPU_FLOAT64)
+        return fail(MFGPU_EINVAL, "precision must be MFGPU_FLOAT32 or MFGPU_FLOAT64");
+    if (n_channels < 1) return fail(MFGPU_EINVAL, "n_channels must be positive");
+    if (capacity < 1) return fail(MFGPU_EINVAL, "capacity must be positive");
+    auto *r = new mfgpu_ring();
+    r->prec = precision;
+    r->nch = n_channels;
+    r->cap = capacity;
+    const size_t bytes = r->esz() * (size_t) n_channels * (size_t) capacity;
+    cudaError_t e = cudaGetDevice(&r->dev);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&r->buf.p, bytes);  // exact size: no growth margin for a ring
+    if (e == cudaSuccess) r->buf.bytes = bytes;
+    if (e == cudaSuccess) e = cudaMemsetAsync(r->buf.p, 0, bytes, r->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(r->stream);
+    if (e != cudaSuccess)
+    {
+        mfgpu_ring_destroy(r);
+        return cuda_fail(e, "mfgpu_ring_create");
+    }
+    *out = r;
+    return MFGPU_OK;
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
+
+mfgpu_status mfgpu_ring_destroy(mfgpu_ring *r)
+try
+{
+    if (!r) return MFGPU_OK;
+    {
+        DeviceGuard g(r->dev);
+        if (r->stream) cudaStreamSynchronize(r->stream);
+        r->buf.release();
+        if (r->stream) cudaStreamDestroy(r->stream);
+    }
+    delete r;
+    return MFGPU_OK;
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
+
+mfgpu_status mfgpu_ring_append(mfgpu_ring *r, int n, const void *x, long ld)
+try
+{
+    if (!r) return fail(MFGPU_EINVAL, "ring is NULL");
+    if (n < 1) return fail(MFGPU_EINVAL, "n must be positive");
+    if (!x) return fail(MFGPU_EINVAL, "x is NULL");
+    if (r->nch > 1 && ld < n) return fail(MFGPU_EINVAL, "row stride is smaller than the number of samples");
+    DeviceGuard g(r->dev);
+    std::lock_guard<std::mutex> lk(r->mu);
+    const size_t es = r->esz();
+    const long keep = std::min<long>(n, r->cap);  // older samples of the chunk would be overwritten at once
+    const long skip = n - keep;
+    long long s = r->head + skip;
+    long done = 0;
+    while (done < keep)
+    {
+        const long pos = (long) (s % r->cap);
+        const long len = std::min<long>(keep - done, r->cap - pos);
+        CU(cudaMemcpy2DAsync(r->buf.as<char>() + es * (size_t) pos, es * (size_t) r->cap,
+                             static_cast<const char *>(x) + es * (size_t) (skip + done), es * (size_t) (r->nch > 1 ? ld : n),
+                             es * (size_t) len, (size_t) r->nch, cudaMemcpyHostToDevice, r->stream));
+        done += len;
+        s += len;
+    }
+    CU(cudaStreamSynchronize(r->stream));
+    r->head += n;
+    return MFGPU_OK;
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
+
+mfgpu_status mfgpu_ring_get_head(mfgpu_ring *r, long long *appended)
+try
+{
+    if (!r || !appended) return fail(MFGPU_EINVAL, "ring or appended is NULL");
+    std::lock_guard<std::mutex> lk(r->mu);
+    *appended = r->head;
+    return MFGPU_OK;
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
+
+mfgpu_status mfgpu_mf_set_window_ring(mfgpu_mf *mf, mfgpu_ring *r, int n_src, const int *channels, long long end,
+                                      int n)
+try
+{
+    MF_CHECK_INIT(mf);
+    if (!r) return fail(MFGPU_EINVAL, "ring is NULL");
+    if (r->dev != mf->dev) return fail(MFGPU_EINVAL, "the ring and the object are on different devices");
+    if (r->prec != mf->prec) return fail(MFGPU_EINVAL, "the ring and the object have different precisions");
+    if (n_src < 1 || n_src > kRingMaxRows)
+        return fail(MFGPU_EINVAL, "n_src must be in [1, " + std::to_string(kRingMaxRows) + "]");
+    RingRows rr;
+    for (int i = 0; i < n_src; ++i)
+    {
+        const int c = channels ? channels[i] : i;
+        if (c < 0 || c >= r->nch)
+            return fail(MFGPU_EINVAL, "ring channel " + std::to_string(c) + " must be in [0, " + std::to_string(r->nch) + ")");
+        rr.src[i] = c;
+    }
+    if (n < 1 || n > r->cap)
+        return fail(MFGPU_EINVAL, "window length " + std::to_string(n) + " must be in [1, " + std::to_string(r->cap) + "]");
+    DeviceGuard g(mf->dev);
+    std::lock_guard<std::mutex> lk(r->mu);  // no append overwrites the window while it is read
+    if (end > r->head || end - n < 0 || end - n < r->head - r->cap)
+        return fail(MFGPU_EINVAL, "window [" + std::to_string(end - n) + ", " + std::to_string(end) +
+                                      ") is not in the ring (samples [" + std::to_string(std::max<long long>(0, r->head - r->cap)) +
+                                      ", " + std::to_string(r->head) + "))");
+    mfgpu_status rs = mf_window_begin(mf, n_src, n);
+    if (rs != MFGPU_OK) return rs;
+    const dim3 grid((unsigned) std::min<long>(64, (n + 255) / 256), (unsigned) n_src);
+    if (mf->prec == 4)
+        ring_gather_kernel<float><<<grid, 256, 0, mf->stream>>>(r->buf.as<float>(), r->cap, rr, end - n, n,
+                                                                mf->x.as<float>(), mf->ldx);
+    else
+        ring_gather_kernel<double><<<grid, 256, 0, mf->stream>>>(r->buf.as<double>(), r->cap, rr, end - n, n,
+                                                                 mf->x.as<double>(), mf->ldx);
+    CU(cudaGetLastError());
+    ++mf->launches;
+    return mf_window_end(mf, n_src, n);  // waits: the window has been read before the lock is released
 }
 catch (...)
 {

@@ -135,6 +135,55 @@ class MatchedFilterParameters:
         return self.get_max_template_length() >= 1
 
 
+class SignalRing:
+    """Extension (no reference counterpart): the latest ``capacity`` samples
+    of ``n_channels`` station channels kept on the device.  ``append`` sends
+    only new samples; ``MatchedFilter.set_window_ring`` sets a request
+    window from the ring by a device gather.  Samples are counted from the
+    first append; ``head`` is the count so far."""
+
+    def __init__(self, n_channels, capacity, dtype=np.float32):
+        self.dtype = np.dtype(dtype)
+        if self.dtype not in (np.dtype(np.float32), np.dtype(np.float64)):
+            raise ValueError("dtype must be float32 or float64")
+        prec = _lib.MFGPU_FLOAT32 if self.dtype == np.float32 else _lib.MFGPU_FLOAT64
+        h = C.c_void_p()
+        _lib.call("mfgpu_ring_create", prec, int(n_channels), int(capacity), C.byref(h))
+        self._h = h
+        self.n_channels = int(n_channels)
+        self.capacity = int(capacity)
+
+    def __del__(self):
+        self.close()
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h:
+            try:
+                _lib.lib().mfgpu_ring_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def append(self, x):
+        """Append the columns of x (n_channels x n samples) to every channel."""
+        x = np.asarray(x)
+        if x.ndim == 1:
+            x = x[None, :]
+        if x.ndim != 2 or x.shape[0] != self.n_channels or x.shape[1] < 1:
+            raise ValueError("x must be %d x n samples" % self.n_channels)
+        if x.dtype != self.dtype or x.strides[1] != x.itemsize or x.strides[0] % x.itemsize:
+            x = np.ascontiguousarray(x, dtype=self.dtype)
+        _lib.call("mfgpu_ring_append", self._h, int(x.shape[1]), x.ctypes.data_as(C.c_void_p),
+                  int(x.strides[0] // x.itemsize))
+
+    @property
+    def head(self):
+        v = C.c_longlong()
+        _lib.call("mfgpu_ring_get_head", self._h, C.byref(v))
+        return v.value
+
+
 class MatchedFilter:
     """MFLib::MatchedFilter<T> (include/mflib/matchedFilter.hpp:28-178) on the GPU.
 
@@ -320,6 +369,20 @@ class MatchedFilter:
             x = np.ascontiguousarray(x, dtype=self._dtype)
         _lib.call("mfgpu_mf_set_window", self._h, int(x.shape[0]), int(x.shape[1]), x.ctypes.data_as(C.c_void_p),
                   int(x.strides[0] // x.itemsize))
+
+    def set_window_ring(self, ring, end, n, channels):
+        """Extension for a serving loop: the request window is samples
+        [end - n, end) of the ring's channels ``channels`` (a SignalRing of
+        this object's dtype), gathered on the device; otherwise as
+        ``set_window`` with one source row per listed channel."""
+        ch = np.ascontiguousarray(channels, dtype=np.int32)
+        if ch.ndim != 1 or ch.size < 1:
+            raise ValueError("channels must list at least one ring channel")
+        if np.dtype(ring.dtype) != np.dtype(self._dtype):
+            raise ValueError("the ring holds %s samples, the object %s" % (np.dtype(ring.dtype).name,
+                                                                         np.dtype(self._dtype).name))
+        _lib.call("mfgpu_mf_set_window_ring", self._h, ring._h, int(ch.size), ch.ctypes.data_as(C.POINTER(C.c_int)),
+                  int(end), int(n))
 
     def set_graph(self, enable=True):
         """Extension: replay apply as a CUDA graph (captured on the second

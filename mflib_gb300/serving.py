@@ -8,7 +8,10 @@ device and serves detection requests as they arrive.
 * A ``TemplateBank`` is a named list of templates, each assigned to one of
   64 channel slots.
 * A ``DetectionRequest`` is a window of continuous data on C = 1..64
-  channels (C x n samples) against one bank.  Template t of the bank
+  channels (C x n samples) against one bank, given as a host array or as
+  a window of a ``SignalRing`` (the stations' latest samples kept on the
+  device: producers append only new samples, and the request's window is
+  gathered from the ring on the device instead of uploaded).  Template t of the bank
   correlates with request channel ``slot_t % C``.  The result is, for every
   template, the PeakFinder indices (threshold and minimum separation of the
   server) over the window's valid lags n - L_max + 1, the reference's
@@ -70,17 +73,34 @@ class TemplateBank:
 
 
 class DetectionRequest:
-    """A window (C x n samples) against a named bank.  ``keep`` lists
-    templates whose Pearson traces are returned besides the peaks."""
+    """A window (C x n samples) against a named bank: host ``signals``, or
+    samples [end - n, end) of the ring channels ``channels`` of ``ring``
+    (``end`` defaults to the ring's head when the request is made).
+    ``keep`` lists templates whose Pearson traces are returned besides the
+    peaks."""
 
     _ids = iter(range(1 << 62))
 
-    def __init__(self, bank, signals, keep=(), arrival=None):
-        x = np.asarray(signals)
-        if x.ndim == 1:
-            x = x[None, :]
-        if x.ndim != 2 or not 1 <= x.shape[0] <= N_SLOTS or x.shape[1] < 1:
-            raise ValueError("signals must be C x n with 1 <= C <= %d" % N_SLOTS)
+    def __init__(self, bank, signals=None, keep=(), arrival=None, ring=None, channels=None, n=None, end=None):
+        self.ring = ring
+        if ring is not None:
+            if signals is not None:
+                raise ValueError("give signals or a ring window, not both")
+            ch = np.asarray(channels if channels is not None else np.arange(ring.n_channels), dtype=np.int64)
+            if ch.ndim != 1 or not 1 <= ch.size <= N_SLOTS or ch.min() < 0 or ch.max() >= ring.n_channels:
+                raise ValueError("channels must list 1..%d ring channels" % N_SLOTS)
+            if n is None or int(n) < 1:
+                raise ValueError("a ring window needs its length n")
+            self.ring_channels = ch
+            self._n = int(n)
+            self.end = int(ring.head if end is None else end)
+            x = None
+        else:
+            x = np.asarray(signals)
+            if x.ndim == 1:
+                x = x[None, :]
+            if x.ndim != 2 or not 1 <= x.shape[0] <= N_SLOTS or x.shape[1] < 1:
+                raise ValueError("signals must be C x n with 1 <= C <= %d" % N_SLOTS)
         self.id = next(DetectionRequest._ids)
         self.bank = str(bank)
         self.signals = x
@@ -95,11 +115,11 @@ class DetectionRequest:
 
     @property
     def channels(self):
-        return self.signals.shape[0]
+        return self.ring_channels.size if self.ring is not None else self.signals.shape[0]
 
     @property
     def n(self):
-        return self.signals.shape[1]
+        return self._n if self.ring is not None else self.signals.shape[1]
 
     @property
     def latency(self):
@@ -186,7 +206,10 @@ class GpuExecutor:
         return f.device_bytes()
 
     def run(self, f, bank, req):
-        f.set_window(req.signals.astype(np.float32, copy=False))
+        if req.ring is not None:
+            f.set_window_ring(req.ring, req.end, req.n, req.ring_channels)
+        else:
+            f.set_window(req.signals.astype(np.float32, copy=False))
         f.apply()
         nv = bank.valid_lags(req.n)
         if nv > 0:

@@ -119,6 +119,35 @@ def test_validation_and_buckets():
         TemplateBank("x", [np.ones(10)], channel_slots=[64])
 
 
+class FakeRing:
+    """Stands in for a SignalRing (channel count and head only)."""
+
+    def __init__(self, n_channels=8, head=5000):
+        self.n_channels, self.head = n_channels, head
+
+
+def test_ring_window_requests():
+    ring = FakeRing()
+    r = DetectionRequest("a", ring=ring, channels=[2, 5, 7], n=1200)
+    assert r.channels == 3 and r.n == 1200 and r.end == 5000 and r.signals is None
+    r = DetectionRequest("a", ring=ring, n=300, end=4000)
+    assert r.channels == 8 and r.end == 4000
+    with pytest.raises(ValueError):
+        DetectionRequest("a", np.zeros((2, 10)), ring=ring, n=10)
+    with pytest.raises(ValueError):
+        DetectionRequest("a", ring=ring, channels=[8], n=10)
+    with pytest.raises(ValueError):
+        DetectionRequest("a", ring=ring, channels=[0])
+    with pytest.raises(ValueError):
+        DetectionRequest("a", ring=FakeRing(n_channels=100), n=10)
+    # the server buckets and admits a ring request like any other
+    ex = FakeExecutor()
+    srv = Server(banks(), ex, slots=1).start()
+    done = srv.submit(DetectionRequest("a", ring=ring, channels=[1], n=1200)).wait(10)
+    srv.close()
+    assert done.error is None
+
+
 def test_latency_stats():
     ex = FakeExecutor(delay=0.01)
     srv = Server(banks(), ex, slots=2).start()
