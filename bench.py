@@ -331,9 +331,11 @@ def run_serving(args, rates=None, requests=None):
     banks of 100 / 500 / 2,000 / 5,000 templates of 200-3,000 samples, under a
     120 GB device-memory budget; p50/p99 latency and template-lag
     correlations/s per arrival rate, next to the same requests served one at
-    a time."""
+    a time; then, at the first rate, windows of the stations' data read from
+    a device ring (SignalRing) against the same windows uploaded."""
     from scipy.signal import butter, sosfilt
     from scipy.signal.windows import hann
+    from mflib_gb300 import SignalRing
     from mflib_gb300.serving import DetectionRequest, GpuExecutor, Server, TemplateBank, latency_stats
 
     rng = np.random.default_rng(400)
@@ -411,6 +413,38 @@ def run_serving(args, rates=None, requests=None):
                       "p99_ms": 1e3 * st["p99_s"], "mean_ms": 1e3 * st["mean_s"], "throughput": st["throughput"],
                       "one_at_a_time": {"throughput": so["template_lags"] / el, "p50_ms": 1e3 * so["p50_s"],
                                         "p99_ms": 1e3 * so["p99_s"]}})
+    # ring arm: the pool as the stations' recent samples in a device ring
+    # (appended in chunks), requests naming windows of it, against the same
+    # windows (no injected events) uploaded from the host
+    ring = SignalRing(64, pool_n)
+    for a in range(0, pool_n, 20_000):
+        ring.append(pool[:, a:a + 20_000])
+    lam = (rates if rates is not None else args.rates)[0] or 100.0
+    rr = np.random.default_rng(900)
+    specs = []
+    for _ in range(requests if requests is not None else args.requests):
+        n = int(rr.integers(6_000, 60_001))
+        specs.append((banks[int(rr.integers(len(banks)))].name, rr.choice(64, int(rr.integers(1, 65)), replace=False),
+                      int(rr.integers(0, pool_n - n)), n))
+    ring_arm = {"rate_req_s": lam}
+    for mode in ("ring", "upload"):
+        objs = [DetectionRequest(b, ring=ring, channels=ch, n=n, end=o + n) if mode == "ring"
+                else DetectionRequest(b, pool[ch, o:o + n]) for b, ch, o, n in specs]
+        arr = np.cumsum(np.random.default_rng(901).exponential(1.0 / lam, len(objs)))
+        base = time.perf_counter() + 0.05
+        for r, a in zip(objs, arr):
+            d = base + a - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            r.t_arrival = base + a
+            srv.submit(r)
+        for r in objs:
+            r.wait(600)
+        st = latency_stats(objs)
+        ring_arm[mode] = {"p50_ms": 1e3 * st["p50_s"], "p99_ms": 1e3 * st["p99_s"], "mean_ms": 1e3 * st["mean_s"],
+                          "h2d_bytes_per_request": 0 if mode == "ring" else
+                          float(np.mean([4 * len(ch) * n for _, ch, _, n in specs]))}
+    ring.close()
     srv.close()
     line = {"metric": "served detection requests: p50/p99 latency and template-lag correlations/s",
             "unit": "template-lag correlations/s; ms", "n_gpus": 1, "dtype": "f32",
@@ -419,7 +453,7 @@ def run_serving(args, rates=None, requests=None):
                                    "100/500/2,000/5,000 templates of 200-3,000 samples, 120 GB budget",
                        "slots": args.serving_slots, "buckets": list(srv.buckets),
                        "threshold": args.serving_threshold, "min_distance": 250},
-            "rates": out_rates, "objects_created": srv.created, "evicted": srv.evicted,
+            "rates": out_rates, "ring_windows": ring_arm, "objects_created": srv.created, "evicted": srv.evicted,
             "peak_device_bytes": srv.peak_held, "warm_s": warm_s}
     return line
 
