@@ -127,6 +127,12 @@ typedef struct
        recomputes every run by direct correlation: correct but slow.
        0 = FP16. */
     int tc_bf16;
+    /* Extension: the tensor-core correlator's tile shape, as templates per
+       group Gp (the MMA's N = 16 Gp: the hi and lo columns of each): an even
+       number in [2, 16] that fits the shared memory beside the strips for
+       the templates' padded length (MFGPU_EINVAL otherwise); 0 = automatic
+       (the most that fit, balanced over the busiest channel). */
+    int tc_group;
 } mfgpu_mf_params;
 
 /* MatchedFilter<T>::MatchedFilter(); precision MFGPU_FLOAT32 | MFGPU_FLOAT64 */

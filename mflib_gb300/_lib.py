@@ -75,6 +75,7 @@ class MfgpuParams(C.Structure):
         ("bucket_variants", C.POINTER(C.c_int)),
         ("persistent", C.c_int),
         ("tc_bf16", C.c_int),
+        ("tc_group", C.c_int),
     ]
 
 

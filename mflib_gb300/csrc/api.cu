@@ -895,9 +895,14 @@ try
         if (gmax < 2 && mf->tc)
             return fail(MFGPU_EINVAL, "template length " + std::to_string(maxLen) +
                                           " is too long for the tensor-core correlator");
+        if (p->tc_group != 0 && (p->tc_group < 2 || p->tc_group > gmax || (p->tc_group & 1)))
+            return fail(MFGPU_EINVAL, "tc_group = " + std::to_string(p->tc_group) +
+                                          " must be even and in [2, " + std::to_string(std::max(2, gmax)) +
+                                          "] for templates of " + std::to_string(maxLen) + " samples");
         // balanced groups: the busiest channel splits into ngc equal groups
         const int ngc = gmax >= 2 ? (max_tpc + gmax - 1) / gmax : 1;
-        const int Gp = gmax >= 2 ? std::min(gmax, ((max_tpc + ngc - 1) / ngc + 1) & ~1) : 2;
+        const int Gp = p->tc_group ? p->tc_group
+                                   : gmax >= 2 ? std::min(gmax, ((max_tpc + ngc - 1) / ngc + 1) & ~1) : 2;
         // automatic choice: seconds per template-lag measured on GB300 (two
         // MMAs per K step), about 3.6e-15 per padded template sample plus
         // 5.7e-12 per tile row shared by the Gp templates of a group, against
@@ -911,7 +916,7 @@ try
         const long room = (long) dev_smem - (long) tc_smem_bytes(Kp, 0);
         const int gmax = (int) std::min<long>(16, room / (32L * Kp)) & ~1;
         const int ngc = (max_tpc + gmax - 1) / gmax;
-        const int Gp = std::min(gmax, ((max_tpc + ngc - 1) / ngc + 1) & ~1);
+        const int Gp = p->tc_group ? p->tc_group : std::min(gmax, ((max_tpc + ngc - 1) / ngc + 1) & ~1);
         for (int c = 0; c < nch; ++c)
             for (size_t i = 0; i < chan_t[c].size(); i += Gp)
             {

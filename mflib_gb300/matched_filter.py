@@ -215,7 +215,7 @@ class MatchedFilter:
         return self._dtype
 
     def initialize(self, params, template_channels=None, n_channels=None, fft_length=0, correlator_variant=0,
-                   length_buckets=0, bucket_plans=None, persistent=False, tc_bf16=False):
+                   length_buckets=0, bucket_plans=None, persistent=False, tc_bf16=False, tc_group=0):
         """MatchedFilter<T>::initialize (src/matchedFilter.cpp:507-821).
 
         Extensions: ``template_channels`` (one channel index per template,
@@ -237,7 +237,9 @@ class MatchedFilter:
         (FP32, variants 3 and 6; the static grid is the default);
         ``tc_bf16`` splits the tensor-core correlator's operands into BF16
         hi + lo instead of FP16 (precision comparison: every run is then
-        recomputed by the accuracy fix-up)."""
+        recomputed by the accuracy fix-up); ``tc_group`` sets the
+        tensor-core tile shape as templates per group (even, 2..16, MMA N =
+        16 per template; 0 automatic)."""
         if not isinstance(params, MatchedFilterParameters) or not params.is_valid():
             raise ValueError("Parameters are invalid")
         tmpls = [params.get_template(i) for i in range(params.get_number_of_templates())]
@@ -279,11 +281,12 @@ class MatchedFilter:
             p.bucket_variants = bva
         p.persistent = 1 if persistent else 0
         p.tc_bf16 = 1 if tc_bf16 else 0
+        p.tc_group = int(tc_group)
         _lib.call("mfgpu_mf_initialize", self._h, C.byref(p))
         self._init_kw = dict(template_channels=template_channels, n_channels=n_channels, fft_length=fft_length,
                              correlator_variant=correlator_variant, length_buckets=length_buckets,
                              bucket_plans=list(bucket_plans) if bucket_plans else None, persistent=persistent,
-                             tc_bf16=tc_bf16)
+                             tc_bf16=tc_bf16, tc_group=tc_group)
         self._params = params
         self._nt = nt
         self._templates = tmpls
@@ -482,7 +485,7 @@ class MatchedFilter:
                 "bucket_plans": [{"fft_length": fl[i], "templates": ntb[i], "lags_per_block": lpb[i],
                                   "correlator": bv[i]} for i in range(nb)]}
 
-    def autotune(self, x, repeats=3, max_buckets=3, fft_lengths=None, variants=None):
+    def autotune(self, x, repeats=3, max_buckets=3, fft_lengths=None, variants=None, tc_groups=(2, 4, 6, 8, 12, 16)):
         """Extension: measured plan choice on this object's templates and the
         signals ``x`` (a 2-D array: channel rows when the object was
         initialised with shared channels, else one row per signal slot).
@@ -494,7 +497,8 @@ class MatchedFilter:
         the FFT lengths half, equal to and twice the current one and every
         organisation allowed for the bucket, timing ``repeats`` applies of
         each candidate after one untimed apply; for one template length in
-        FP32 it also times the tensor-core correlator.  The object is left
+        FP32 it also times the tensor-core correlator at its automatic tile
+        shape and at each of ``tc_groups`` templates per group (the MMA's N).  The object is left
         initialised with the fastest configuration (its signals loaded) and
         the method returns it with its apply time and every trial.
         ``fft_lengths`` / ``variants`` restrict the candidates.  User-forced
@@ -543,7 +547,7 @@ class MatchedFilter:
             return ms
 
         def common(**over):
-            kw = dict(base, fft_length=0, correlator_variant=0)
+            kw = dict(base, fft_length=0, correlator_variant=0, tc_group=0)
             kw.update(over)
             return kw
 
@@ -579,9 +583,18 @@ class MatchedFilter:
                 if best_ms is None or cur_ms < best_ms:
                     best_ms, best_kw = cur_ms, common(length_buckets=nb, bucket_plans=cur)
             if one_length and self._dtype == np.float32 and (variants is None or 4 in variants):
-                ms = run(common(correlator_variant=4, length_buckets=1, bucket_plans=None))
-                if ms is not None and (best_ms is None or ms < best_ms):
-                    best_ms, best_kw = ms, common(correlator_variant=4, length_buckets=1, bucket_plans=None)
+                seen = set()
+                for g in (0,) + tuple(tc_groups or ()):
+                    kw = common(correlator_variant=4, length_buckets=1, bucket_plans=None, tc_group=int(g))
+                    ms = run(kw)
+                    if ms is None:
+                        continue  # this tile shape does not fit the templates' length
+                    shape = self.get_plan()["tc_group"]
+                    if shape in seen:
+                        continue
+                    seen.add(shape)
+                    if best_ms is None or ms < best_ms:
+                        best_ms, best_kw = ms, kw
             if best_kw is None:
                 raise RuntimeError("no candidate plan could be initialised")
             self.initialize(params, **best_kw)

@@ -21,7 +21,9 @@ class _Tpl:
 class FakeFilter(MatchedFilter):
     """Bucket b of a k-bucket plan has automatic FFT length 4096 and
     organisation 1; apply time = sum over buckets of cost(k, b, fft,
-    variant).  Plans with fft 2048 and organisation 2 do not fit."""
+    variant), plus tc_cost(templates per group) for the tensor-core plan
+    (automatic group 8; groups above 12 do not fit).  Plans with fft 2048
+    and organisation 2 do not fit."""
 
     def __init__(self, lens, dtype=np.float32, cost=None):  # no device object
         self._dtype = dtype
@@ -30,6 +32,8 @@ class FakeFilter(MatchedFilter):
         self._init_kw = dict(template_channels=[0] * len(lens), n_channels=1, fft_length=0, correlator_variant=0,
                              length_buckets=0, bucket_plans=None)
         self.cost = cost
+        self.tc_cost = lambda g: 0.0
+        self.tcg = 0
         self.oom = None        # a plan whose initialize runs out of memory
         self.fail_at = None    # the initialize call that fails hard
         self.calls = 0
@@ -43,8 +47,12 @@ class FakeFilter(MatchedFilter):
         plans = [(4096, 1)] * k
         for b, (f, v) in enumerate((kw.get("bucket_plans") or [])[:k]):
             plans[b] = (f or plans[b][0], v or plans[b][1])
+        tcg = 0
         if kw.get("correlator_variant") == 4:
             plans = [(4096, 4)]
+            tcg = kw.get("tc_group") or 8
+            if tcg > 12:
+                raise ValueError("tc_group does not fit")
         if any(p == (2048, 2) for p in plans):
             raise ValueError("the plan override does not fit")
         if any(p == self.oom for p in plans):
@@ -55,6 +63,7 @@ class FakeFilter(MatchedFilter):
         self.inits.append(kw)
         self.kw = kw
         self.plans = plans
+        self.tcg = tcg
         self._init_kw = dict(kw)
 
     def set_channel_signals(self, x, first_channel=0):
@@ -72,10 +81,11 @@ class FakeFilter(MatchedFilter):
 
     def last_timings(self):
         k = len(self.plans)
-        return {"xcorr_ms": 0.0, "apply_ms": float(sum(self.cost(k, b, f, v) for b, (f, v) in enumerate(self.plans)))}
+        ms = float(sum(self.cost(k, b, f, v) for b, (f, v) in enumerate(self.plans)))
+        return {"xcorr_ms": 0.0, "apply_ms": ms + (self.tc_cost(self.tcg) if self.tcg else 0.0)}
 
     def get_plan(self):
-        return {"fft_length": self.plans[-1][0], "correlator": self.plans[-1][1],
+        return {"fft_length": self.plans[-1][0], "correlator": self.plans[-1][1], "tc_group": self.tcg,
                 "bucket_plans": [{"fft_length": f, "correlator": v, "templates": 1, "lags_per_block": f // 2}
                                  for f, v in self.plans]}
 
@@ -126,6 +136,22 @@ def test_autotune_one_length_includes_tensor_cores():
     res = g.autotune(np.zeros((1, 10), np.float64), repeats=1)
     assert all(t["config"]["correlator_variant"] != 4 for t in res["trials"])
     assert res["config"]["bucket_plans"] == [(4096, 3)]
+
+
+def test_autotune_searches_tensor_core_tile_shape():
+    def cost(k, b, f, v):
+        return {4: 1.0, 3: 2.0}.get(v, 5.0) + (f != 4096)
+
+    f = FakeFilter([300] * 8, cost=cost)
+    f.tc_cost = lambda g: abs(g - 4) * 0.1  # four templates per group is best
+    res = f.autotune(np.zeros((1, 10), np.float32), repeats=1)
+    assert res["config"]["correlator_variant"] == 4 and res["config"]["tc_group"] == 4
+    assert res["plan"]["tc_group"] == 4 and res["apply_ms"] == 1.0
+    tc = [t for t in res["trials"] if t["config"]["correlator_variant"] == 4]
+    assert [t["config"]["tc_group"] for t in tc] == [0, 2, 4, 6, 8, 12, 16]
+    assert tc[-1]["apply_ms"] is None and "does not fit" in tc[-1]["error"]
+    # the FFT candidates never carry a tile shape
+    assert all(t["config"]["tc_group"] == 0 for t in res["trials"] if t["config"]["correlator_variant"] != 4)
 
 
 def test_autotune_restrictions_and_errors():

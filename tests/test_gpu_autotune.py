@@ -110,3 +110,35 @@ def test_autotune_one_length(gpu, oracle):
     worst = max(float(np.max(np.abs(f.get_valid_matched_filtered_signal(t).astype(np.float64) - ref[t])))
                 for t in range(len(tps)))
     assert worst < 2e-5, worst
+    # the tensor-core tile shapes were timed, each trial at the shape asked for
+    tc = [t for t in ok if t["config"]["correlator_variant"] == 4 and t["config"]["tc_group"]]
+    assert len({t["plan"]["tc_group"] for t in tc}) >= 3
+    assert all(t["plan"]["tc_group"] == t["config"]["tc_group"] for t in tc)
+
+
+@pytest.mark.parametrize("g", [2, 4, 8, 16])
+def test_tensor_core_tile_shape(gpu, oracle, g):
+    """tc_group sets the tensor-core correlator's templates per group (MMA
+    N = 16 per template); every shape gives oracle-equal coefficients."""
+    mf = gpu
+    rng = np.random.default_rng(6)
+    tps = [_template(70 + t, 240) for t in range(10)]
+    nch, n = 2, 40_000
+    chan = np.arange(10) % nch
+    sigs = np.stack([_bp(rng.standard_normal(n), 1.0, 10.0) for _ in range(nch)]).astype(np.float32)
+    f = _filter(mf, tps, chan, n, nch, correlator_variant=4, tc_group=g)
+    assert f.get_plan()["correlator"] == 4 and f.get_plan()["tc_group"] == g
+    f.set_channel_signals(sigs)
+    f.apply()
+    ref = oracle.matched_filter(tps, [sigs[c] for c in chan], multi=True, fp64_from_f32=True)
+    worst = max(float(np.max(np.abs(f.get_valid_matched_filtered_signal(t).astype(np.float64) - ref[t])))
+                for t in range(len(tps)))
+    assert worst < 2e-5, worst
+
+
+@pytest.mark.parametrize("g", [1, 3, 18, -2])
+def test_bad_tensor_core_tile_shape(gpu, g):
+    mf = gpu
+    tps = [_template(90 + t, 240) for t in range(4)]
+    with pytest.raises(ValueError):
+        _filter(mf, tps, np.arange(4) % 2, 20_000, 2, correlator_variant=4, tc_group=g)
