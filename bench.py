@@ -963,7 +963,8 @@ def _extra(fn):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    # 12 steps of the default uneven day time about 1.1 s (the clock sampler sees the load)
+    ap.add_argument("--steps", type=int, default=12)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--samples", type=int, default=N_SAMPLES, help="samples per channel (default 24 h)")
