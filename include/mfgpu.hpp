@@ -315,6 +315,36 @@ class MatchedFilterParameters
 };
 
 /* ------------------------------------------------------------------------ */
+/* Extension, no reference counterpart: the stations' latest samples kept on
+   the device (mfgpu_ring_*).  append() sends only new samples; a
+   MatchedFilter<T> sets a request window from the ring on the device
+   (setWindowFromRing). */
+template <class T = double> class SignalRing
+{
+  public:
+    SignalRing(int nChannels, long capacity)
+    {
+        detail::check(mfgpu_ring_create(detail::precision<T>::value, nChannels, capacity, &mH));
+    }
+    ~SignalRing() { mfgpu_ring_destroy(mH); }
+    SignalRing(const SignalRing &) = delete;
+    SignalRing &operator=(const SignalRing &) = delete;
+    /* n new samples of every channel, rows of stride ld */
+    void append(int n, const T *x, long ld) { detail::check(mfgpu_ring_append(mH, n, x, ld)); }
+    /* samples appended per channel so far */
+    long long getHead() const
+    {
+        long long h = 0;
+        detail::check(mfgpu_ring_get_head(mH, &h));
+        return h;
+    }
+    mfgpu_ring *handle() const noexcept { return mH; }
+
+  private:
+    mfgpu_ring *mH = nullptr;
+};
+
+/* ------------------------------------------------------------------------ */
 /* MFLib::MatchedFilter<T> (include/mflib/matchedFilter.hpp:28-178) */
 template <class T = double> class MatchedFilter
 {
@@ -457,6 +487,15 @@ template <class T = double> class MatchedFilter
         std::vector<std::complex<T>> out((size_t) nout / 2);
         for (size_t k = 0; k < out.size(); ++k) out[k] = std::complex<T>(buf[2 * k], buf[2 * k + 1]);
         return out;
+    }
+
+    /* Extension: samples [end - n, end) of the ring's channels become the
+       source rows (mfgpu_mf_set_window_ring; channel c of the object reads
+       row c % channels.size(), zero tail past n) */
+    void setWindowFromRing(const SignalRing<T> &ring, const std::vector<int> &channels, long long end, int n)
+    {
+        invalidate();
+        detail::check(mfgpu_mf_set_window_ring(mH, ring.handle(), (int) channels.size(), channels.data(), end, n));
     }
 
     /* the C-ABI handle, for the extensions in mfgpu.h */

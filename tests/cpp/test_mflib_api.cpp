@@ -178,6 +178,45 @@ void test_multichannel_float()
     require(e0 < 2e-6 && e1 < 2e-6, "FP32 vs two-pass Pearson (" + std::to_string(std::max(e0, e1)) + ")");
 }
 
+// extension: a window read from the device ring equals the same samples set
+// from the host
+void test_signal_ring()
+{
+    std::vector<double> x, x2, b, b2;
+    damped(x, x2, b, b2);
+    const int n = 400;
+    MFLib::MatchedFilterParameters p;
+    p.addTemplate(make_template(b, 1.0));
+    p.addTemplate(make_template(b2, 1.0));
+    p.setSignalSize(n);
+    MFLib::MatchedFilter<double> mf;
+    mf.initialize(p);
+    const long cap = 700;
+    MFLib::SignalRing<double> ring(2, cap);
+    const int total = (int) x.size();
+    std::vector<double> rows(2 * (size_t) total);
+    for (int i = 0; i < total; ++i) { rows[i] = x[i]; rows[total + i] = x2[i]; }
+    for (int a = 0; a < total; a += 130)
+    {
+        const int k = std::min(130, total - a);
+        std::vector<double> chunk(2 * (size_t) k);
+        for (int i = 0; i < k; ++i) { chunk[i] = rows[a + i]; chunk[k + i] = rows[total + a + i]; }
+        ring.append(k, chunk.data(), k);
+    }
+    require(ring.getHead() == total, "ring head counts every appended sample");
+    const long long end = total - 37;
+    mf.setWindowFromRing(ring, {1, 0}, end, n);
+    mf.apply();
+    const std::vector<double> r0 = mf.getMatchedFilteredSignal(0), r1 = mf.getMatchedFilteredSignal(1);
+    mf.setSignal(0, n, rows.data() + total + (end - n));
+    mf.setSignal(1, n, rows.data() + (end - n));
+    mf.apply();
+    require(r0 == mf.getMatchedFilteredSignal(0) && r1 == mf.getMatchedFilteredSignal(1),
+            "ring window equals the same samples set from the host");
+    require(throws_invalid([&] { mf.setWindowFromRing(ring, {0}, end - cap, n); }),
+            "a window no longer in the ring is refused");
+}
+
 void test_single_channel()
 {
     // testing/singleChannel.cpp:104-160: one signal, three templates cut from it
@@ -440,6 +479,7 @@ int main()
         test_value_types();
         test_multichannel_double();
         test_multichannel_float();
+        test_signal_ring();
         test_single_channel();
         test_shift_and_stack();
         test_peak_finder();
