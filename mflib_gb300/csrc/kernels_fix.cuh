@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(kThreads) den_robust_kernel(const float *x, lo
                 for (int q = 0; q < kDenRun; ++q)
                 {
                     const float M2 = fmaf(-S, S * invL, Q);
-                    o[q] = M2 > 0.f ? DenOps<float>::out(Lf * M2, sqrtL, tol) : 0.f;
+                    if (drow) o[q] = M2 > 0.f ? DenOps<float>::out(Lf * M2, sqrtL, tol) : 0.f;
                     if (M2 > 0.f) M2min = fminf(M2min, M2);
                     bad |= M2 < 0.f;
                     Smax = fmaxf(Smax, fabsf(S));
@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(kThreads) den_robust_kernel(const float *x, lo
                         b = fmaf(d, d, b);
                     }
                     const float M2 = fmaf(-a, a * invL, b);
-                    o[q] = M2 > 0.f ? DenOps<float>::out(Lf * M2, sqrtL, tol) : 0.f;
+                    if (drow) o[q] = M2 > 0.f ? DenOps<float>::out(Lf * M2, sqrtL, tol) : 0.f;
                     if (M2 > 0.f) M2min = fminf(M2min, M2);
                     if (q == 0) R0 = mu;
                     Smax = fmaxf(Smax, fabsf(mu - R0));
