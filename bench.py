@@ -743,6 +743,13 @@ def run_uneven_day(args, ctx):
     e2e_el = ctx.max(time.perf_counter() - t0)
     h2d = nch * n * 4
     d2h = int(4 * (c2.size + i2.size))
+    # the host link's rate for one step's upload alone (the e2e steps overlap
+    # it with the previous apply, so it bounds them when it is the longer)
+    f.synchronize()
+    t1 = time.perf_counter()
+    f.stage_channel_signals(host)
+    f.synchronize()
+    h2d_gbs = h2d / (time.perf_counter() - t1) / 1e9
 
     plan = f.get_plan()
     P = plan["fft_length"] // 2
@@ -768,6 +775,7 @@ def run_uneven_day(args, ctx):
                              % (4e-9 * nch * n, 4e-9 * lags)},
             "e2e": {"value": ctx.world * lags / (e2e_el / args.steps), "unit": METRIC, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * e2e_el / args.steps,
+                    "h2d_gbs_one_upload": h2d_gbs,
                     "api": "stage_channel_signals (async H2D of step i+1 under step i), apply, find_peaks, "
                            "get_all_peaks"},
             "roofline": roof, "gpu_launches": int(launches), "clocks": clk, "detections": int(idx.size),
