@@ -120,12 +120,12 @@ typedef struct
        length >= 4096; ignored otherwise).  0 = the static grid, which
        measured faster on GB300. */
     int persistent;
-    /* Extension, for precision comparison: 1 = the tensor-core correlator
-       splits its operands into BF16 hi + lo (about 16 bits of each FP32
-       value kept) instead of FP16 hi + lo (22 bits).  Its error bound then
-       exceeds the 2e-5 tolerance everywhere, so the accuracy fix-up
-       recomputes every run by direct correlation: correct but slow.
-       0 = FP16. */
+    /* Extension: 1 = the tensor-core correlator splits its operands into
+       BF16 hi + lo (about 16 bits of each FP32 value kept, no range
+       scaling needed) instead of FP16 hi + lo (22 bits).  The accuracy
+       fix-up's bound grows with the templates' largest coefficient
+       (independent roundings summed over the window), so more runs are
+       recomputed than with FP16.  0 = FP16. */
     int tc_bf16;
     /* Extension: the tensor-core correlator's tile shape, as templates per
        group Gp (the MMA's N = 16 Gp: the hi and lo columns of each): an even

@@ -284,6 +284,7 @@ struct mfgpu_mf
     int dev_smem = 0;                // opt-in shared memory per block of the device
     bool persistent = false;         // FFT correlator as a persistent work-queue launch (option)
     bool tc_bf16 = false;            // tensor-core operands split into BF16 instead of FP16 (option)
+    float tc_maxb = 0.f;             // largest coefficient of the unit-norm templates (tensor-core path)
     bool test_skip_fixup = false;    // mfgpu_mf_test_skip_fixup: flag runs but do not recompute them
 
     size_t esz() const { return (size_t) prec; }
@@ -925,6 +926,20 @@ try
                     tc_gtid.push_back(i + k < chan_t[c].size() ? chan_t[c][i + k] : -1);
             }
         mf->tc_Kp = Kp;
+        // largest coefficient of the demeaned unit-norm templates (the BF16
+        // split's error bound scales with it)
+        mf->tc_maxb = 0.f;
+        for (int t = 0; t < nt; ++t)
+        {
+            const double *b = &mf->tmpl[mf->toff[t]];
+            const int L = mf->lens[t];
+            double m = 0, q = 0, mx = 0;
+            for (int i = 0; i < L; ++i) m += b[i];
+            m /= L;
+            for (int i = 0; i < L; ++i) q += (b[i] - m) * (b[i] - m);
+            for (int i = 0; i < L; ++i) mx = std::max(mx, std::fabs(b[i] - m));
+            if (q > 0) mf->tc_maxb = std::max(mf->tc_maxb, (float) (mx / std::sqrt(q)));
+        }
         mf->tc_Gp = Gp;
         mf->tc_groups = (int) tc_gch.size();
         mf->tc_tiles = (std::max(1, maxvalid) + kTcLags - 1) / kTcLags;
@@ -1839,7 +1854,8 @@ template <class T> static mfgpu_status mf_launch_xcorr(mfgpu_mf *mf)
                                       mf->dead.as<unsigned char>(),
                                       mf->xrange.as<float>(), mf->tc_off.as<float>(),
                                       mf->fxbits.as<unsigned>(), mf->fxlist.as<int>(), mf->fxcount.as<int>(),
-                                      mf->tc_bf16 ? kFixTcC1Bf16 : kFixTcC1, mf->tc_bf16 ? kFixTcC2Bf16 : kFixTcC2,
+                                      mf->tc_bf16 ? kFixTcC1 + kFixTcC1Bf16Per * mf->tc_maxb : kFixTcC1,
+                                      mf->tc_bf16 ? kFixTcC2Bf16 : kFixTcC2,
                                       kFixTol, mf->stream));
                 ++mf->launches;
             }

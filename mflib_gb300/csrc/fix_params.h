@@ -20,10 +20,16 @@ constexpr float kFixTol = 2.0e-5f;
 constexpr float kFixFftK = 8.0f;
 constexpr float kFixTcC1 = 2.0e-6f;
 constexpr float kFixTcC2 = 0x1p-23f;
-// BF16 hi+lo keeps 2^-18 of each operand instead of 2^-22: C1 sixteen times
-// larger (above the tolerance itself, so every run is recomputed), and no
-// subnormal floor in BF16's exponent range
-constexpr float kFixTcC1Bf16 = 16 * kFixTcC1;
+// BF16 hi+lo leaves each operand with a representation error of at most
+// 2^-16 of its value (8-bit significands: 2^-8 for hi, again for lo; FP16:
+// 2^-22), and drops lo*lo products of the same order.  Like the FP16
+// subnormal term these are independent roundings: against a unit-norm
+// template b the three sums over a window have standard deviations of at
+// most 2^-16 max|b| ||y - off|| / sqrt(12) (the splits of y and b) and / 3
+// (the dropped products), 2^-16 max|b| ||y - off|| / 2 together.  Six of
+// those, 3 2^-16 max|b|, are added to the FP16 constant; the host takes
+// max|b| over the object's templates (kFixTcC1Bf16Per is its factor).
+constexpr float kFixTcC1Bf16Per = 3.f * 0x1p-16f;
 constexpr float kFixTcC2Bf16 = 0.f;
 
 // Fix-up batches: the templates of a channel sorted by length, kFixBatch per

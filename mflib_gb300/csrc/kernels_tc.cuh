@@ -32,11 +32,10 @@
 // Strips and accumulators are double-buffered (mbarriers, bounded waits);
 // the group's template operands stay resident in shared memory.
 //
-// BF16 operands (template flag BF, an option for precision comparison): the
-// same kernel with BF16 hi and lo (about 16 of the 24 bits kept, against 22
-// for FP16; BF16's exponent range needs no scaling but the powers of two
-// are kept), and the instruction descriptor's A and B format fields set to
-// BF16.
+// BF16 operands (template flag BF, an option): the same kernel with BF16 hi
+// and lo (about 16 of the 24 bits kept, against 22 for FP16; BF16's
+// exponent range needs no scaling but the powers of two are kept), and the
+// instruction descriptor's A and B format fields set to BF16.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>

@@ -236,8 +236,8 @@ class MatchedFilter:
         correlator as one persistent launch fed by a device work ticket
         (FP32, variants 3 and 6; the static grid is the default);
         ``tc_bf16`` splits the tensor-core correlator's operands into BF16
-        hi + lo instead of FP16 (precision comparison: every run is then
-        recomputed by the accuracy fix-up); ``tc_group`` sets the
+        hi + lo instead of FP16 (its error bound lists more runs for the
+        accuracy fix-up); ``tc_group`` sets the
         tensor-core tile shape as templates per group (even, 2..16, MMA N =
         16 per template; 0 automatic)."""
         if not isinstance(params, MatchedFilterParameters) or not params.is_valid():

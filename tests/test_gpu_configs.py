@@ -191,15 +191,16 @@ def test_tc_operand_splits_raw_error(gpu, oracle, capsys):
     block and window stay inside one envelope segment.  BF16 keeps about 16
     bits of each operand against FP16's 22, but the representation errors
     average out over the window: both raw errors sit at the FP32
-    accumulation's level, within the tolerance.  The BF16 worst-case bound
-    still flags every run, and with the fix-up on the object is
-    oracle-equal."""
+    accumulation's level, within the tolerance.  BF16's bound (independent
+    roundings, scaled by the templates' largest coefficient) lists more
+    runs than FP16's but not all, and with the fix-up on both objects are
+    oracle-equal on every sampled lag."""
     mf = gpu
     tp, chans, bounds = stress_case()
     n = chans[0].size
     rng = np.random.default_rng(9)
     lags = np.sort(rng.choice(n - tp.size + 1, 4000, replace=False))
-    raw = {}
+    raw, flagged = {}, {}
     for bf16 in (False, True):
         f = mf.MultiChannel.MatchedFilter(dtype=np.float32)
         f.initialize(_params(mf, [tp, tp], n), template_channels=[0, 1], n_channels=2, correlator_variant=4,
@@ -220,14 +221,15 @@ def test_tc_operand_splits_raw_error(gpu, oracle, capsys):
                 w_all = max(w_all, float(err.max()))
                 w_flat = max(w_flat, float(err[flat].max()))
             worst[skip] = (w_all, w_flat)
-            if bf16:
-                assert f.get_fixup_runs() >= 0.99 * 2 * ((n - tp.size + 1 + 31) // 32)
+            flagged[bf16] = f.get_fixup_runs()
         raw[bf16] = worst[True][1]
         assert worst[False][0] < 1e-4, (bf16, worst)
     with capsys.disabled():
-        print("\ntensor-core raw max|drho| away from envelope steps: fp16 hi+lo %.3g, bf16 hi+lo %.3g"
-              % (raw[False], raw[True]))
+        print("\ntensor-core raw max|drho| away from envelope steps: fp16 hi+lo %.3g, bf16 hi+lo %.3g;"
+              " runs over the bound: fp16 %d, bf16 %d" % (raw[False], raw[True], flagged[False], flagged[True]))
     assert raw[False] < 2e-5 and raw[True] < 2e-5, raw
+    total = 2 * ((n - tp.size + 1 + 31) // 32)
+    assert 0 < flagged[False] <= flagged[True] < 0.5 * total, (flagged, total)
 
 
 @pytest.mark.parametrize("variant", [0, 4])
