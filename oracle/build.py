@@ -16,12 +16,14 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-# Where this recipe reads the reference checkout: $MFLIB_REFERENCE_ROOT when
-# set, else the development host's read-only checkout below.  Only this
-# recipe names it; on a host without the checkout build_ref() is skipped and
-# the tests that need the compiled reference skip with it.
-DEV_HOST_REFERENCE = "/root/reference"
-REF_ROOT = os.environ.get("MFLIB_REFERENCE_ROOT") or DEV_HOST_REFERENCE
+# Where this recipe reads the reference checkout: $MFLIB_REFERENCE_ROOT (the
+# repository's build() sets it when the development host's checkout exists).
+# Without it build_ref() is skipped and the tests that need the compiled
+# reference skip with it.
+
+
+def ref_root():
+    return os.environ.get("MFLIB_REFERENCE_ROOT") or ""
 REF_SOURCES = [
     "src/matchedFilter.cpp",
     "src/matchedFilterParameters.cpp",
@@ -67,7 +69,8 @@ def build_oracle(force=False):
 
 
 def build_ref(force=False):
-    if not os.path.isdir(os.path.join(REF_ROOT, "src")):
+    REF_ROOT = ref_root()
+    if not REF_ROOT or not os.path.isdir(os.path.join(REF_ROOT, "src")):
         return None
     outdir = os.path.join(HERE, "_ref")
     os.makedirs(outdir, exist_ok=True)
