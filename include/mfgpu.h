@@ -446,8 +446,10 @@ mfgpu_status mfgpu_dbscan_segmented(mfgpu_dbscan *db, int n_segments, const int 
  * (a cudaStream_t, NULL = default stream); the caller synchronises.
  * Working memory is a fixed file-scope device array sized for at most
  * MFGPU_DBSCAN_NOALLOC_MAX_OBS observations and
- * MFGPU_DBSCAN_NOALLOC_MAX_SEGMENTS segments (about 1.4 MB, held on every
- * device that loads the library until the process exits); larger requests
+ * MFGPU_DBSCAN_NOALLOC_MAX_SEGMENTS segments (about 2.4 MB, held on every
+ * device that loads the library until the process exits; with one feature
+ * the segments are sorted there on the device, so each point visits its
+ * neighbours only); larger requests
  * fail with MFGPU_EINVAL.  Every call looks up the array's device address
  * in the current context (no allocation); the first call in a context also
  * loads the module that places the array, so make that first call before

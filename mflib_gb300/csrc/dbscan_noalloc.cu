@@ -37,7 +37,13 @@ constexpr size_t kOffCore = kOffIsRoot + align256(sizeof(int) * kMaxPoints);
 constexpr size_t kOffPos = kOffCore + align256(kMaxPoints);
 constexpr size_t kOffTiles = kOffPos + align256(sizeof(long long) * (kMaxPoints + 1));
 constexpr size_t kOffSegOff = kOffTiles + align256(sizeof(long long) * kTiles);
-constexpr size_t kScratchBytes = kOffSegOff + align256(sizeof(int) * (kMaxSegments + 1));
+// one feature: sorted values, permutation, positions, finite segment ends
+constexpr size_t kOffXs = kOffSegOff + align256(sizeof(int) * (kMaxSegments + 1));
+constexpr size_t kOffPerm = kOffXs + align256(sizeof(double) * kMaxPoints);
+constexpr size_t kOffRank = kOffPerm + align256(sizeof(int) * kMaxPoints);
+constexpr size_t kOffFend = kOffRank + align256(sizeof(int) * kMaxPoints);
+constexpr size_t kScratchBytes = kOffFend + align256(sizeof(int) * kMaxSegments);
+static_assert((kMaxPoints & (kMaxPoints - 1)) == 0, "the bitonic sort pads to a power of two within the scratch");
 
 __device__ __align__(256) unsigned char g_dbscan_scratch[kScratchBytes];
 
@@ -124,6 +130,10 @@ try
     long long *pos = reinterpret_cast<long long *>(sb + kOffPos);
     long long *tiles = reinterpret_cast<long long *>(sb + kOffTiles);
     int *seg_off = reinterpret_cast<int *>(sb + kOffSegOff);
+    double *xs = reinterpret_cast<double *>(sb + kOffXs);
+    int *perm = reinterpret_cast<int *>(sb + kOffPerm);
+    int *rank = reinterpret_cast<int *>(sb + kOffRank);
+    int *fend = reinterpret_cast<int *>(sb + kOffFend);
 
     if (n_obs == 0)
     {
@@ -138,14 +148,36 @@ try
     const unsigned wblocks = (unsigned) ((n_obs + kDbWarps - 1) / kDbWarps);
     sanitize_offsets_kernel<<<1, 1, 0, s>>>(n_obs, n_segments, d_seg_offsets, seg_off);
     seg_of_kernel<<<blocks, kDbThreads, 0, s>>>(n_obs, n_segments, seg_off, seg_of);
-    db_core_kernel<<<wblocks, kDbThreads, 0, s>>>(p, core, parent);
-    db_union_kernel<<<wblocks, kDbThreads, 0, s>>>(p, core, parent);
+    // one feature: every segment sorted on the device (bitonic network over
+    // the next power of two, at most the scratch's capacity), so each point
+    // visits its neighbours only
+    const bool sorted1 = n_features == 1;
+    const Db1Sorted q{xs, perm, rank, fend};
+    if (sorted1)
+    {
+        int n2 = 1;
+        while (n2 < n_obs) n2 <<= 1;
+        const unsigned b2 = (unsigned) ((n2 + kDbThreads - 1) / kDbThreads);
+        db1_iota_kernel<<<b2, kDbThreads, 0, s>>>(perm, n2);
+        for (int k = 2; k <= n2; k <<= 1)
+            for (int j = k >> 1; j > 0; j >>= 1) db1_bitonic_kernel<<<b2, kDbThreads, 0, s>>>(p, perm, n2, j, k);
+        db1_gather_kernel<<<blocks, kDbThreads, 0, s>>>(p, perm, xs, rank);
+        db1_fend_kernel<<<(n_segments + 127) / 128, 128, 0, s>>>(n_segments, seg_off, xs, fend);
+        db1_core_kernel<<<wblocks, kDbThreads, 0, s>>>(p, q, core, parent);
+        db1_union_kernel<<<wblocks, kDbThreads, 0, s>>>(p, q, core, parent);
+    }
+    else
+    {
+        db_core_kernel<<<wblocks, kDbThreads, 0, s>>>(p, core, parent);
+        db_union_kernel<<<wblocks, kDbThreads, 0, s>>>(p, core, parent);
+    }
     db_roots_kernel<<<blocks, kDbThreads, 0, s>>>(n_obs, core, parent, is_root);
     const long nt = (n_obs + kScanTile - 1) / kScanTile;
     scan_tile_sums_kernel<<<(unsigned) nt, kScanThreads, 0, s>>>(is_root, n_obs, tiles);
     scan_tile_offsets_kernel<<<1, kScanThreads, 0, s>>>(tiles, nt);
     scan_apply_kernel<<<(unsigned) nt, kScanThreads, 0, s>>>(is_root, n_obs, tiles, pos);
-    db_label_kernel<<<wblocks, kDbThreads, 0, s>>>(p, core, parent, pos, d_labels);
+    if (sorted1) db1_label_kernel<<<wblocks, kDbThreads, 0, s>>>(p, q, core, parent, pos, d_labels);
+    else db_label_kernel<<<wblocks, kDbThreads, 0, s>>>(p, core, parent, pos, d_labels);
     db_count_kernel<<<(n_segments + 127) / 128, 128, 0, s>>>(n_segments, seg_off, pos, d_n_clusters);
     e = cudaGetLastError();
     if (e != cudaSuccess) return fail(MFGPU_ECUDA, cudaGetErrorString(e));

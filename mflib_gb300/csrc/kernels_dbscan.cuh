@@ -219,7 +219,15 @@ struct Db1Sorted
     const double *xs;
     const int *perm;
     const int *rank;
+    // per segment, the end of its non-NaN values (NaN sorted last, no
+    // neighbour of anything); null when no value is NaN
+    const int *fend;
 };
+
+__device__ __forceinline__ int db1_end(const DbParams &p, const Db1Sorted &q, int s)
+{
+    return q.fend ? q.fend[s] : p.seg_off[s + 1];
+}
 
 // [lo, hi): positions of the segment [jb, je) within eps of the value xi
 __device__ __forceinline__ void db1_range(const double *xs, int jb, int je, double xi, double eps, int &lo, int &hi)
@@ -249,7 +257,7 @@ static __global__ void __launch_bounds__(kDbThreads) db1_core_kernel(DbParams p,
     if (i >= p.n) return;
     const int s = p.seg_of[i];
     int lo = 0, hi = 0;
-    if (lane == 0) db1_range(q.xs, p.seg_off[s], p.seg_off[s + 1], p.X[i], p.eps, lo, hi);
+    if (lane == 0) db1_range(q.xs, p.seg_off[s], db1_end(p, q, s), p.X[i], p.eps, lo, hi);
     lo = __shfl_sync(0xffffffffu, lo, 0);
     hi = __shfl_sync(0xffffffffu, hi, 0);
     double acc = 0;
@@ -298,7 +306,7 @@ static __global__ void __launch_bounds__(kDbThreads) db1_label_kernel(DbParams p
     const int i = blockIdx.x * kDbWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
     if (i >= p.n) return;
     const int s = p.seg_of[i];
-    const int jb = p.seg_off[s], je = p.seg_off[s + 1];
+    const int jb = p.seg_off[s], je = db1_end(p, q, s);
     const long long base = root_pos[jb];
     if (core[i])
     {
@@ -324,6 +332,71 @@ static __global__ void __launch_bounds__(kDbThreads) db1_label_kernel(DbParams p
         best = v < best ? v : best;
     }
     if (lane == 0) labels[i] = best == 0x7fffffffffffffffLL ? -1 : (int) best;
+}
+
+// Device-side preparation of Db1Sorted, for callers whose data are already
+// on the device: perm (n2 = a power of two >= n entries, padding indices
+// n .. n2-1 sorting last) sorted by (segment, value, index) with NaN after
+// every number in its segment, by a bitonic network (one launch per step),
+// then the sorted values, each point's position and every segment's end of
+// non-NaN values.
+__device__ __forceinline__ bool db1_less(const DbParams &p, int a, int b)
+{
+    if (a >= p.n) return b >= p.n && a < b;
+    if (b >= p.n) return true;
+    const int sa = p.seg_of[a], sb = p.seg_of[b];
+    if (sa != sb) return sa < sb;
+    const double xa = p.X[a], xb = p.X[b];
+    const bool na = isnan(xa), nb = isnan(xb);
+    if (na != nb) return nb;
+    if (!na && xa != xb) return xa < xb;
+    return a < b;
+}
+
+static __global__ void db1_iota_kernel(int *perm, int n2)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n2) perm[i] = i;
+}
+
+// one compare-exchange step (distance j, merge size k) of the bitonic network
+static __global__ void db1_bitonic_kernel(DbParams p, int *perm, int n2, int j, int k)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n2) return;
+    const int l = i ^ j;
+    if (l <= i) return;
+    const int a = perm[i], b = perm[l];
+    const bool up = (i & k) == 0;
+    if (up ? db1_less(p, b, a) : db1_less(p, a, b))
+    {
+        perm[i] = b;
+        perm[l] = a;
+    }
+}
+
+static __global__ void db1_gather_kernel(DbParams p, const int *perm, double *xs, int *rank)
+{
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= p.n) return;
+    const int i = perm[r];
+    xs[r] = p.X[i];
+    rank[i] = r;
+}
+
+// fend[s]: the first position of segment s holding NaN (its end if none)
+static __global__ void db1_fend_kernel(int nseg, const int *seg_off, const double *xs, int *fend)
+{
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nseg) return;
+    int a = seg_off[s], b = seg_off[s + 1];
+    while (a < b)
+    {
+        const int m = (a + b) >> 1;
+        if (isnan(xs[m])) b = m;
+        else a = m + 1;
+    }
+    fend[s] = a;
 }
 
 static __global__ void db_count_kernel(int nseg, const int *seg_off, const long long *root_pos, int *n_clusters)

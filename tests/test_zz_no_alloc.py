@@ -125,3 +125,39 @@ def test_noalloc_empty_and_malformed_offsets(gpu):
     # NaN epsilon is rejected before any work is enqueued
     st = lib.mfgpu_dbscan_segmented_noalloc(1, None, 10, 1, None, None, float("nan"), 2, None, None, None)
     assert st == _lib.MFGPU_EINVAL
+
+
+def test_noalloc_one_feature_sorted_on_device(gpu, oracle):
+    """One feature: the entry point sorts every segment on the device
+    (bitonic network) and visits neighbourhoods only.  Checked against the
+    oracle with ties at eps, +-inf and NaN values (a NaN is no neighbour of
+    anything), weights, and at the scratch's full capacity in one segment
+    against the sort-based restatement."""
+    from mflib_gb300 import _lib
+    from test_oracle import dbscan_1d
+    lib = _lib.lib()
+    rng = np.random.default_rng(11)
+    sizes = [700, 0, 1, 2500, 33]
+    x = np.round(rng.uniform(0, 300, sum(sizes)) * 4) / 4
+    x[rng.integers(0, x.size, 25)] = np.inf
+    x[rng.integers(0, x.size, 25)] = -np.inf
+    x[rng.integers(0, x.size, 25)] = np.nan
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int32)
+    w = rng.integers(1, 6, x.size) / 2.0
+    for eps, mo, weights in ((0.25, 2, None), (0.75, 4, w)):
+        labels, ncl = _noalloc(lib, x[:, None], off, eps, mo, weights)
+        for s in range(len(sizes)):
+            a, b = off[s], off[s + 1]
+            n_ref, lab_ref = oracle.dbscan(x[a:b], eps, mo, None if weights is None else weights[a:b])
+            assert ncl[s] == n_ref
+            np.testing.assert_array_equal(labels[a:b], lab_ref)
+    # the full capacity in one segment, and ragged segments up to it
+    n = 65_536
+    x = np.round(rng.uniform(0, 6000, n) * 8) / 8
+    for off in (np.array([0, n], np.int32), np.array([0, 17, 40_000, 40_001, n], np.int32)):
+        labels, ncl = _noalloc(lib, x[:, None], off, 0.125, 3)
+        for s in range(len(off) - 1):
+            a, b = off[s], off[s + 1]
+            n_ref, lab_ref = dbscan_1d(x[a:b], 0.125, 3)
+            assert ncl[s] == n_ref
+            np.testing.assert_array_equal(labels[a:b], lab_ref)
