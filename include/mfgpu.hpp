@@ -684,6 +684,16 @@ template <class T = double> class Detection
     }
     int getDetectedSignalLength() const { return (int) mSignal.size(); }
     bool haveDetectedSignal() const noexcept { return !mSignal.empty(); }
+    /* copies the detected signal into *x, which holds n >= its length */
+    void getDetectedSignal(int n, T *x[]) const
+    {
+        const T *src = getDetectedSignalPointer();
+        if (n < (int) mSignal.size())
+            throw std::invalid_argument("Signal length = " + std::to_string(n) + " must be at least = " +
+                                        std::to_string(mSignal.size()));
+        if (!x || !*x) throw std::invalid_argument("x is NULL");
+        std::copy(src, src + mSignal.size(), *x);
+    }
     void setDetectionTime(double t) { mT = t; mHaveT = true; }
     double getDetectionTime() const { return get(mT, mHaveT, "Detection time"); }
     bool haveDetectionTime() const noexcept { return mHaveT; }
@@ -716,6 +726,7 @@ template <class T = double> class Detection
         if (a <= 0) throw std::invalid_argument("Scaling factor must be positive");
         return std::log10(a);
     }
+    bool haveMagnitudePerturbation(RelativeMagnitudeType type) const noexcept { return haveAmplitudeScalingFactor(type); }
     void setPolarity(Polarity p) noexcept { mPol = p; }
     Polarity getPolarity() const noexcept { return mPol; }
 
@@ -753,6 +764,15 @@ template <class T = double> class Detector
         mInit = true;
     }
     bool isInitialized() const noexcept { return mInit; }
+    /* the traces detect() reduces: checks them and records their length
+       (detect runs the reduction and the detections in one device call) */
+    void setMatchedFilteredSignals(const MFLib::SingleChannel::MatchedFilter<T> &mf)
+    {
+        if (!mInit) throw std::runtime_error("Detector class not initialized");
+        if (!mf.haveMatchedFilteredSignals()) throw std::invalid_argument("Matched filtered signals not computed");
+        mLength = (int) mf.getMatchedFilteredSignal(0).size();
+    }
+    int getMatchedFilteredSignalLength() const noexcept { return mLength; }
     void detect(const MFLib::SingleChannel::MatchedFilter<T> &mf)
     {
         mDets.clear();
@@ -778,6 +798,7 @@ template <class T = double> class Detector
         detail::check(mfgpu_mf_get_detections(mf.handle(), n, raw.data(), &n));
         const T *signal = mP.wantDetectedWaveform() ? mf.getSignalPointer() : nullptr;
         const int ns = mf.getSignalLength();
+        mLength = ns - mf.getWaveformTemplate(0).getSignalLength() + 1;
         for (int i = 0; i < n; ++i)
         {
             const mfgpu_detection &r = raw[i];
@@ -815,6 +836,239 @@ template <class T = double> class Detector
   private:
     DetectorParameters mP;
     std::vector<Detection<T>> mDets;
+    bool mInit = false;
+    int mLength = 0;
+};
+
+/* MFLib::SingleChannel::convertAmplitudeScalingFactorToMagnitudePerturbation
+   (src/singleChannel/relativeMagnitude.cpp:399-420) */
+inline double convertAmplitudeScalingFactorToMagnitudePerturbation(double alpha)
+{
+    if (alpha <= 0) throw std::invalid_argument("Scaling factor = " + std::to_string(alpha) + " must be positive");
+    return std::log10(alpha);
+}
+inline float convertAmplitudeScalingFactorToMagnitudePerturbation(float alpha)
+{
+    if (alpha <= 0) throw std::invalid_argument("Scaling factor = " + std::to_string(alpha) + " must be positive");
+    return std::log10(alpha);
+}
+
+/* MFLib::SingleChannel::RelativeMagnitude<T>
+   (src/singleChannel/relativeMagnitude.cpp:260-396): the two amplitude
+   scaling factors of a detected window against the template, from
+   mfgpu_relative_amplitudes (which also takes many windows per call) */
+template <class T = double> class RelativeMagnitude
+{
+  public:
+    void clear() noexcept
+    {
+        mB.clear();
+        mHave = false;
+    }
+    void initialize(const WaveformTemplate &wt)
+    {
+        clear();
+        if (!wt.haveSignal()) throw std::invalid_argument("Template signal length = 0 must be positive");
+        const int L = wt.getSignalLength();
+        std::vector<double> b((size_t) L);
+        double *pb = b.data();
+        wt.getSignal(L, &pb);
+        bool constant = true;
+        for (int i = 1; i < L && constant; ++i) constant = b[i] == b[0];
+        if (constant) throw std::invalid_argument("Template signal cannot be constant");
+        mB = std::move(b);
+    }
+    bool isInitialized() const noexcept { return !mB.empty(); }
+    int getDetectedSignalLength() const
+    {
+        if (!isInitialized()) throw std::runtime_error("Class not initialized");
+        return (int) mB.size();
+    }
+    void setDetectedSignal(int n, const T y[])
+    {
+        mHave = false;
+        if (!isInitialized()) throw std::runtime_error("Class not initialized");
+        if (n != (int) mB.size())
+            throw std::invalid_argument("Signal length = " + std::to_string(n) + " must = " + std::to_string(mB.size()));
+        if (!y) throw std::invalid_argument("Signal is NULL");
+        int valid = 0;
+        detail::check(mfgpu_relative_amplitudes(detail::precision<T>::value, n, mB.data(), 1, y, n, &mAlpha[0],
+                                                &mAlpha[1], &valid));
+        if (!valid) throw std::invalid_argument("Detected signal cannot be constant");
+        mHave = true;
+    }
+    bool haveDetectedSignal() const noexcept { return mHave; }
+    T computeAmplitudeScalingFactor(RelativeMagnitudeType type) const
+    {
+        if (!isInitialized()) throw std::runtime_error("Class is not initialized");
+        if (!mHave) throw std::runtime_error("Detected waveform not set");
+        return (T) mAlpha[type == RelativeMagnitudeType::GIBBONS_RINGDAL_2006 ? 0 : 1];
+    }
+    T computeMagnitudePerturbation(RelativeMagnitudeType type) const
+    {
+        return convertAmplitudeScalingFactorToMagnitudePerturbation(computeAmplitudeScalingFactor(type));
+    }
+
+  private:
+    std::vector<double> mB;
+    double mAlpha[2] = {0, 0};
+    bool mHave = false;
+};
+
+/* MFLib::SingleChannel::AssociatorParameters
+   (src/singleChannel/associatorParameters.cpp, defaults :10-18) */
+class AssociatorParameters
+{
+  public:
+    void clear() noexcept { *this = AssociatorParameters(); }
+    void setOriginTimeTolerance(double tol)
+    {
+        if (tol < 0) throw std::invalid_argument("tolerance = " + std::to_string(tol) + " must be positive");
+        mTol = tol;
+    }
+    double getOriginTimeTolerance() const noexcept { return mTol; }
+    void setMinimumNumberOfPicksInEvent(int n)
+    {
+        if (n < 1) throw std::invalid_argument("minPicks = " + std::to_string(n) + " must be positive");
+        mMinPicks = n;
+    }
+    int getMinimumNumberOfPicksInEvent() const noexcept { return mMinPicks; }
+    void enableCorrelationCoefficientWeighting() noexcept { mWeight = true; }
+    void disableCorrelationCoefficientWeighting() noexcept { mWeight = false; }
+    bool useCorrelationCoefficientWeighting() const noexcept { return mWeight; }
+
+  private:
+    double mTol = 2.0;
+    int mMinPicks = 5;
+    bool mWeight = false;
+};
+
+/* MFLib::SingleChannel::Associator<T> (src/singleChannel/associator.cpp):
+   detections grouped by their template identifier's id, each group sorted
+   by phase onset time, the origin times (onset - travel time) of every
+   group clustered by DBSCAN with eps = the origin-time tolerance and
+   minPts = the minimum number of picks (weighted by the coefficients when
+   asked), all groups in one mfgpu_dbscan_segmented call; each cluster is an
+   event, events ordered by id, then cluster.  The sorts are stable (the
+   reference's std::sort leaves equal keys in unspecified order), and
+   getDetectionsInEvent checks the event index against the number of events. */
+template <class T = double> class Associator
+{
+  public:
+    Associator() = default;
+    ~Associator()
+    {
+        if (mDb) mfgpu_dbscan_destroy(mDb);
+    }
+    Associator(const Associator &) = delete;
+    Associator &operator=(const Associator &) = delete;
+    void clear() noexcept
+    {
+        mInit = false;
+        mDets.clear();
+        mEvents.clear();
+    }
+    void initialize(const AssociatorParameters &parameters)
+    {
+        clear();
+        mP = parameters;
+        mInit = true;
+    }
+    bool isInitialized() const noexcept { return mInit; }
+    void addDetection(const Detection<T> &det)
+    {
+        mEvents.clear();
+        if (!mInit) throw std::runtime_error("Class not initialized");
+        if (!det.haveTravelTime()) throw std::invalid_argument("Travel time must be set");
+        if (!det.haveTemplateIdentifier()) throw std::invalid_argument("Template identifier must be set");
+        if (mP.useCorrelationCoefficientWeighting() && !det.haveCorrelationCoefficient())
+            throw std::invalid_argument("XC coefficient must be set");
+        mDets.push_back(det);
+    }
+    int getNumberOfDetections() const noexcept { return (int) mDets.size(); }
+    void clearDetections() noexcept
+    {
+        mDets.clear();
+        mEvents.clear();
+    }
+    void associate()
+    {
+        mEvents.clear();
+        if (!mInit) throw std::runtime_error("Class is not intialized");
+        if (mDets.empty()) return;
+        const size_t n = mDets.size();
+        std::vector<uint64_t> id(n);
+        std::vector<double> onset(n), travel(n);
+        for (size_t i = 0; i < n; ++i)
+        {
+            id[i] = mDets[i].getTemplateIdentifier().second;
+            onset[i] = mDets[i].getPhaseOnsetTime();
+            travel[i] = mDets[i].getTravelTime();
+        }
+        std::vector<size_t> order(n);
+        for (size_t i = 0; i < n; ++i) order[i] = i;
+        std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) {
+            return id[a] < id[b] || (id[a] == id[b] && onset[a] < onset[b]);
+        });
+        std::vector<Detection<T>> sorted;
+        sorted.reserve(n);
+        std::vector<double> X(n), w;
+        std::vector<int> offs{0};
+        std::vector<uint64_t> ids;
+        for (size_t r = 0; r < n; ++r)
+        {
+            const size_t i = order[r];
+            if (r == 0 || id[i] != ids.back())
+            {
+                if (r > 0) offs.push_back((int) r);
+                ids.push_back(id[i]);
+            }
+            X[r] = onset[i] - travel[i];
+            sorted.push_back(mDets[i]);
+        }
+        offs.push_back((int) n);
+        if (mP.useCorrelationCoefficientWeighting())
+        {
+            w.resize(n);
+            for (size_t r = 0; r < n; ++r)
+            {
+                w[r] = sorted[r].getCorrelationCoefficient();
+                if (!(w[r] > 0)) throw std::invalid_argument("All weights must be positive");
+            }
+        }
+        mDets = std::move(sorted);
+        if (!mDb) detail::check(mfgpu_dbscan_create(&mDb));
+        detail::check(mfgpu_dbscan_initialize(mDb, mP.getOriginTimeTolerance(), mP.getMinimumNumberOfPicksInEvent()));
+        const int nseg = (int) ids.size();
+        std::vector<int> labels(n), ncl((size_t) nseg);
+        detail::check(mfgpu_dbscan_segmented(mDb, nseg, offs.data(), 1, X.data(), w.empty() ? nullptr : w.data(),
+                                             labels.data(), ncl.data()));
+        for (int s = 0; s < nseg; ++s)
+            for (int c = 0; c < ncl[s]; ++c)
+            {
+                std::vector<int> members;
+                for (int i = offs[s]; i < offs[s + 1]; ++i)
+                    if (labels[i] == c) members.push_back(i);
+                mEvents.push_back(std::move(members));
+            }
+    }
+    int getNumberOfEvents() const noexcept { return (int) mEvents.size(); }
+    std::vector<Detection<T>> getDetectionsInEvent(int iev) const
+    {
+        if (mEvents.empty()) throw std::runtime_error("No detections have been associated");
+        if (iev < 0 || iev >= (int) mEvents.size())
+            throw std::invalid_argument("iev = " + std::to_string(iev) + " must be in range [0," +
+                                        std::to_string(mEvents.size() - 1) + "]");
+        std::vector<Detection<T>> out;
+        for (int i : mEvents[iev]) out.push_back(mDets[i]);
+        return out;
+    }
+
+  private:
+    AssociatorParameters mP;
+    std::vector<Detection<T>> mDets;
+    std::vector<std::vector<int>> mEvents;
+    mfgpu_dbscan *mDb = nullptr;
     bool mInit = false;
 };
 }  // namespace SingleChannel

@@ -459,7 +459,84 @@ void test_detector()
                     std::abs(a.getAmplitudeScalingFactor(MFLib::RelativeMagnitudeType::SCHAFF_RICHARDS_2014) - 3.0) < 1e-9,
                 "detector: amplitude scaling factors of a copy scaled by 3");
         require(std::abs(a.getPhaseOnsetTime() - a.getDetectionTime()) < 1e-12, "detector: phase onset time");
+        require(det.getMatchedFilteredSignalLength() == n - L + 1, "detector: matched-filtered signal length");
+        require(a.haveMagnitudePerturbation(MFLib::RelativeMagnitudeType::GIBBONS_RINGDAL_2006) &&
+                    std::abs(a.getMagnitudePerturbation(MFLib::RelativeMagnitudeType::GIBBONS_RINGDAL_2006) -
+                             std::log10(3.0)) < 1e-9,
+                "detector: magnitude perturbation log10(3)");
     }
+    // the relative magnitude of a scaled, offset copy of template 0
+    MFLib::WaveformTemplate wt;
+    wt.setSignal(L, t0.data());
+    MFLib::SingleChannel::RelativeMagnitude<double> rm;
+    require(throws_runtime([&] { rm.getDetectedSignalLength(); }), "relative magnitude: not initialised");
+    rm.initialize(wt);
+    std::vector<double> y(L);
+    for (int i = 0; i < L; ++i) y[i] = 2.5 * t0[i] + 7.0;
+    rm.setDetectedSignal(L, y.data());
+    const double gr = rm.computeAmplitudeScalingFactor(MFLib::RelativeMagnitudeType::GIBBONS_RINGDAL_2006);
+    const double sr = rm.computeAmplitudeScalingFactor(MFLib::RelativeMagnitudeType::SCHAFF_RICHARDS_2014);
+    require(std::abs(gr - 2.5) < 1e-12 && std::abs(sr - 2.5) < 1e-12, "relative magnitude: both factors 2.5");
+    require(std::abs(rm.computeMagnitudePerturbation(MFLib::RelativeMagnitudeType::SCHAFF_RICHARDS_2014) -
+                     std::log10(2.5)) < 1e-12,
+            "relative magnitude: perturbation log10(2.5)");
+    std::vector<double> flat(L, 4.0);
+    require(throws_invalid([&] { rm.setDetectedSignal(L, flat.data()); }), "relative magnitude: constant window rejected");
+    require(throws_invalid([&] { rm.setDetectedSignal(L - 1, y.data()); }), "relative magnitude: wrong length rejected");
+    require(throws_invalid([&] { MFLib::SingleChannel::convertAmplitudeScalingFactorToMagnitudePerturbation(0.0); }),
+            "non-positive scaling factor rejected");
+}
+
+// Associator: detections grouped by their template id, origin times (onset -
+// travel time) clustered within the tolerance, isolated picks left out.
+void test_associator()
+{
+    using D = MFLib::SingleChannel::Detection<double>;
+    auto make = [](uint64_t id, double onset, double travel, double xc) {
+        D d;
+        d.setTemplateIdentifier({MFLib::NetworkStationPhase(), id});
+        d.setPhaseOnsetTime(onset);
+        d.setTravelTime(travel);
+        d.setCorrelationCoefficient(xc);
+        return d;
+    };
+    MFLib::SingleChannel::AssociatorParameters ap;
+    ap.setOriginTimeTolerance(1.0);
+    ap.setMinimumNumberOfPicksInEvent(2);
+    MFLib::SingleChannel::Associator<double> as;
+    require(throws_runtime([&] { as.addDetection(make(1, 0, 0, 0.5)); }), "associator: not initialised");
+    as.initialize(ap);
+    // id 2: origins 100.0, 100.4, 160 (noise); id 1: origins 20.1, 20.5, 20.9, 75 (noise)
+    as.addDetection(make(2, 103.0, 3.0, 0.8));
+    as.addDetection(make(1, 24.1, 4.0, 0.9));
+    as.addDetection(make(2, 102.4, 2.0, 0.7));
+    as.addDetection(make(1, 75.0, 0.0, 0.6));
+    as.addDetection(make(1, 21.5, 1.0, 0.8));
+    as.addDetection(make(2, 160.0, 0.0, 0.9));
+    as.addDetection(make(1, 22.9, 2.0, 0.5));
+    D bad;
+    bad.setTemplateIdentifier({MFLib::NetworkStationPhase(), 3});
+    require(throws_invalid([&] { as.addDetection(bad); }), "associator: travel time required");
+    as.associate();
+    require(as.getNumberOfDetections() == 7 && as.getNumberOfEvents() == 2, "associator: two events");
+    const auto e0 = as.getDetectionsInEvent(0), e1 = as.getDetectionsInEvent(1);
+    require(e0.size() == 3 && e0[0].getTemplateIdentifier().second == 1 &&
+                std::abs(e0[0].getPhaseOnsetTime() - e0[0].getTravelTime() - 20.5) < 1e-12,
+            "associator: first event is id 1's three picks, by onset time");
+    require(e1.size() == 2 && e1[0].getTemplateIdentifier().second == 2, "associator: second event is id 2's pair");
+    require(throws_invalid([&] { as.getDetectionsInEvent(2); }), "associator: event index checked");
+    ap.enableCorrelationCoefficientWeighting();
+    ap.setMinimumNumberOfPicksInEvent(3);
+    MFLib::SingleChannel::Associator<double> aw;
+    aw.initialize(ap);
+    // id 5: four picks of weight 0.9 (sum 3.6 >= 3) form an event; id 6:
+    // two of 0.95 (1.9) do not
+    for (const D &d : {make(5, 10.0, 0, 0.9), make(5, 10.3, 0, 0.9), make(5, 10.6, 0, 0.9), make(5, 10.2, 0, 0.9),
+                       make(6, 40.0, 0, 0.95), make(6, 40.5, 0, 0.95)})
+        aw.addDetection(d);
+    aw.associate();
+    require(aw.getNumberOfEvents() == 1 && aw.getDetectionsInEvent(0).size() == 4,
+            "associator: weighted picks need a weight sum of 3");
 }
 
 }  // namespace
@@ -485,6 +562,7 @@ int main()
         test_peak_finder();
         test_dbscan();
         test_detector();
+        test_associator();
     }
     catch (const std::exception &e)
     {
