@@ -126,15 +126,16 @@ template <class T, int LOG2P> struct XcorrLayout
     static constexpr size_t tw_bytes = tw_bytes_of(0);
     static constexpr size_t uv = sizeof(cx<T>) * 2 * P;
     static constexpr size_t brow = sizeof(cx<T>) * (P + 2);
-    // Without SHARED_DEN (modes 0, 1) the segment's region later holds the
-    // padded demeaned segment.  With SHARED_DEN, and in mode 3, the first
-    // work buffer overlays the segment; mode 3 builds the padded copy in the
-    // second team's buffer before the forward FFT.
+    // With SHARED_DEN, and in mode 3, the first work buffer overlays the
+    // segment; mode 3 builds a padded demeaned copy in the second team's
+    // buffer before the forward FFT.
     static constexpr size_t padded = sizeof(T) * (N + N / 32);
-    // mode 4: after the forward FFT the segment's region holds the in-chunk
-    // prefix sums of y and y^2, interleaved (2 N values, and a zero pair at
-    // position N: the prefix where the last lag's window ends), and each team
-    // keeps 8 values per 32-lag run of its template's window statistics
+    // Without SHARED_DEN (modes 0, 1, 4: templates of several lengths) the
+    // segment's region holds, after the forward FFT, the in-chunk prefix sums
+    // of y and y^2, interleaved (2 N values, and a zero pair at position N:
+    // the prefix where the last lag's window ends), and the CTA (each team in
+    // mode 4) keeps 8 values per 32-lag run of its template's window
+    // statistics
     static constexpr size_t q12 = sizeof(T) * 2 * (N + 2);
     static __host__ __device__ size_t rd_bytes(int S) { return up(8 * sizeof(T) * (size_t) (S / 32)); }
     static_assert(((sizeof(cx<T>) * spad_size(P) + 127) & ~size_t(127)) >= sizeof(T) * (N + N / 32),
@@ -143,7 +144,7 @@ template <class T, int LOG2P> struct XcorrLayout
     static constexpr bool teams(int mode) { return mode >= 2; }
     static constexpr size_t xs_region(bool sd, int mode)
     {
-        return up(overlay(sd, mode) ? (seg > fft ? seg : fft) : mode == 4 ? q12 : padded);
+        return up(overlay(sd, mode) ? (seg > fft ? seg : fft) : q12);
     }
     static constexpr size_t off_xs(bool sd, int mode = 0) { return head(sd, mode); }
     static constexpr size_t off_W0(bool sd, int mode)
@@ -158,17 +159,18 @@ template <class T, int LOG2P> struct XcorrLayout
     static constexpr size_t off_tw(bool sd, int mode) { return off_UV(sd, mode) + up(uv); }
     static constexpr size_t off_B(bool sd, int mode) { return off_tw(sd, mode) + up(tw_bytes_of(mode)); }
     static constexpr size_t off_invd(bool sd, int mode) { return off_B(sd, mode) + (mode == 1 ? 2 * up(brow) : 0); }
-    // one normalisation row (mode 4: a run-statistics row per team)
-    static __host__ __device__ size_t invd_bytes(int mode, int S)
+    // one normalisation row (one template length), else run statistics:
+    // one row, or one per team in mode 4
+    static __host__ __device__ size_t invd_bytes(bool sd, int mode, int S)
     {
-        return mode == 4 ? 2 * rd_bytes(S) : up(sizeof(T) * (size_t) S);
+        return overlay(sd, mode) ? up(sizeof(T) * (size_t) S) : (mode == 4 ? 2 : 1) * rd_bytes(S);
     }
     // fused peak candidates: per team two chunk masks (one bit per 64 lags,
     // P/32 chunks)
     static constexpr int mask_words = (P / 32 + 31) / 32;
     static __host__ __device__ size_t off_M(bool sd, int mode, int S)
     {
-        return off_invd(sd, mode) + invd_bytes(mode, S);
+        return off_invd(sd, mode) + invd_bytes(sd, mode, S);
     }
     static size_t bytes(bool sd, int mode, int S)
     {
@@ -784,6 +786,10 @@ __device__ __forceinline__ int xcorr_tile(const XcorrParams<T> &p, const int bx,
     // CTA (once, before the forward FFT) instead of read from den_kernel
     constexpr bool OWN_DEN = MODE == 3;
     static_assert(!(OWN_DEN && SHARED_DEN), "mode 3 computes its own normalisation");
+    // templates of several lengths (modes 0, 1, 4): each lag's normalisation
+    // computed in the last inverse pass from in-chunk prefix sums and the
+    // template's run statistics (inv_den_wide)
+    constexpr bool PERLAG = !SHARED_DEN && !OWN_DEN;
     constexpr int P = LY::P, N = LY::N, NCH = LY::NCH;
     const int tid = threadIdx.x;
     const int c = p.grp_chan[g];
@@ -862,7 +868,6 @@ __device__ __forceinline__ int xcorr_tile(const XcorrParams<T> &p, const int bx,
     st.xs = xs; st.yp = xs; st.m = m; st.c1 = c1; st.c2 = c2;
     st.p1 = reinterpret_cast<T *>(c2 + NCH + 1);
     st.p2 = st.p1 + NCH;
-    int Lcur = p.tlen[p.tids[t_begin]];
     if constexpr (!SHARED_DEN) seg_chunk_prefix<T, N, NTH>(st, tid);
     if constexpr (OWN_DEN)
     {
@@ -870,7 +875,7 @@ __device__ __forceinline__ int xcorr_tile(const XcorrParams<T> &p, const int bx,
         // demeaned copy there, then the CTA's one normalisation row
         st.yp = reinterpret_cast<T *>(W1);
         seg_make_padded<T, N>(st, tid);
-        seg_inv_den<T, N>(st, Lcur, S, p.tol, invd_s, tid);
+        seg_inv_den<T, N>(st, p.tlen[p.tids[t_begin]], S, p.tol, invd_s, tid);
     }
 
     // ---- forward real FFT of (x - m), read straight from the staged segment
@@ -921,19 +926,12 @@ __device__ __forceinline__ int xcorr_tile(const XcorrParams<T> &p, const int bx,
         __syncthreads();
     }
     cx<T> *q12 = reinterpret_cast<cx<T> *>(xs);
-    if constexpr (WIDE)
+    if constexpr (PERLAG)
     {
         // the segment's region is free now: in-chunk prefix sums of y and
-        // y^2; each team derives its templates' normalisation from them in
-        // the epilogue (inv_den_wide)
+        // y^2, from which the epilogue derives each template's normalisation
+        // (inv_den_wide)
         seg_prefix_q12<T, N, NTH>(st, q12, st.p1, st.p2, tid);
-    }
-    else if constexpr (!SHARED_DEN && !OWN_DEN)
-    {
-        // the segment's region is free now: padded demeaned copy, then the
-        // first template length's normalisation
-        seg_make_padded<T, N>(st, tid);
-        seg_inv_den<T, N>(st, Lcur, S, p.tol, invd_s, tid);
     }
 
     // ---- per template: fused conj-multiply + inverse FFT + Pearson epilogue
@@ -1008,9 +1006,9 @@ __device__ __forceinline__ int xcorr_tile(const XcorrParams<T> &p, const int bx,
             const int k = 2 * e;
             if (k >= kmax) return;
             // rows from den_kernel (TMA) are plain, rows from seg_inv_den
-            // swizzled; mode 4 derives the pair from its run statistics
+            // swizzled; several lengths: the pair from the run statistics
             cx<T> d;
-            if constexpr (WIDE) d = inv_den_wide<T>(q12, invd2, k, L, re, Lt, sqrtL, p.tol);
+            if constexpr (PERLAG) d = inv_den_wide<T>(q12, invd2, k, L, re, Lt, sqrtL, p.tol);
             else d = invd2[SHARED_DEN ? e : inv_den_pair<T>(e)];
             const T r0 = clamp_rho(z.x * d.x);
             const T r1 = clamp_rho(z.y * d.y);
@@ -1097,6 +1095,7 @@ __device__ __forceinline__ int xcorr_tile(const XcorrParams<T> &p, const int bx,
     }
     else
     {
+        int Lrd = -1;  // length of the run statistics in invd_s
         for (int j = 0; j < ntl; ++j)
         {
             const int t = p.tids[t_begin + j];
@@ -1132,14 +1131,16 @@ __device__ __forceinline__ int xcorr_tile(const XcorrParams<T> &p, const int bx,
             {
                 B = p.Bc + (long) t * p.ldb;
             }
-            if constexpr (!SHARED_DEN)
+            if constexpr (PERLAG)
             {
+                // run statistics of the template's length, read in the last
+                // inverse pass after the passes' barriers; the previous
+                // template's epilogue finished at the barrier above
                 const int L = p.tlen[t];
-                if (L != Lcur)
+                if (L != Lrd)
                 {
-                    seg_inv_den<T, N>(st, L, S, p.tol, invd_s, tid);
-                    Lcur = L;
-                    __syncthreads();
+                    seg_run_stats<T, kThreads>(st, q12, st.p1, st.p2, L, S, reinterpret_cast<cx<T> *>(invd_s), tid);
+                    Lrd = L;
                 }
             }
             template_body(std::integral_constant<int, 0>(), std::integral_constant<int, kThreads>(), j, B, W,

@@ -185,33 +185,39 @@ def test_precision_stress(gpu, oracle, dtype, variant, capsys):
         assert f.get_fixup_runs() > 0
 
 
-@pytest.mark.parametrize("fft_length", [4096, 8192])
-def test_several_lengths_chunk_edges(gpu, oracle, fft_length):
-    """The two-team correlator that normalises every template for its own
-    length (variant 6), at the lengths where its per-lag normalisation
+@pytest.mark.parametrize("dtype,variant,fft_length", [(np.float32, 6, 4096), (np.float32, 6, 8192),
+                                                    (np.float32, 1, 4096), (np.float32, 2, 2048),
+                                                    (np.float64, 1, 4096), (np.float64, 2, 2048)])
+def test_several_lengths_chunk_edges(gpu, oracle, dtype, variant, fft_length):
+    """The correlators that normalise every template for its own length
+    (variant 6: two teams; 1 and 2: the whole CTA, FP32 and FP64), at the
+    lengths where the per-lag normalisation
     changes form: shorter than one 32-sample chunk, exact multiples of 32
     (no partial chunk), and one sample either side of them, plus a template
     of the longest length the block leaves room for (the last lag's window
     then ends at the segment's end).  Two channels with a DC offset; every
     valid lag against the FP64 oracle."""
     mf = gpu
-    lens = [5, 31, 32, 33, 64, 95, 96, 97, 1024, 1025]
+    lens = [5, 31, 32, 33, 64, 95, 96, 97, 1024, 1025] if fft_length > 2048 else [5, 31, 32, 33, 64, 95, 96, 97]
     lens.append(fft_length - 2 * 32 * ((fft_length // 4) // 32) + 1)
     tps = [_template(2000 + i, L) for i, L in enumerate(lens)]
     nch, n = 2, 50_000
     chan = np.arange(len(lens)) % nch
     rng = np.random.default_rng(12)
-    sigs = np.stack([_bp(rng.standard_normal(n), 1.0, 10.0) + 30.0 * c for c in range(nch)]).astype(np.float32)
-    f = mf.MultiChannel.MatchedFilter(dtype=np.float32)
-    f.initialize(_params(mf, tps, n), template_channels=chan, n_channels=nch, correlator_variant=6,
+    sigs = np.stack([_bp(rng.standard_normal(n), 1.0, 10.0) + 30.0 * c for c in range(nch)]).astype(dtype)
+    f = mf.MultiChannel.MatchedFilter(dtype=dtype)
+    f.initialize(_params(mf, tps, n), template_channels=chan, n_channels=nch, correlator_variant=variant,
                  fft_length=fft_length)
-    assert f.get_plan()["correlator"] == 6 and f.get_plan()["fft_length"] == fft_length
+    assert f.get_plan()["correlator"] == variant and f.get_plan()["fft_length"] == fft_length
     f.set_channel_signals(sigs)
     f.apply()
-    ref = oracle.matched_filter(tps, [sigs[c] for c in chan], multi=True, fp64_from_f32=True)
+    if dtype == np.float32:
+        ref = oracle.matched_filter(tps, [sigs[c] for c in chan], multi=True, fp64_from_f32=True)
+    else:
+        ref = oracle.matched_filter(tps, [sigs[c] for c in chan], multi=True)
     worst = max(float(np.max(np.abs(f.get_valid_matched_filtered_signal(t).astype(np.float64) - ref[t])))
                 for t in range(len(tps)))
-    assert worst < 1e-5, worst
+    assert worst < (1e-5 if dtype == np.float32 else 1e-10), worst
 
 
 def test_tc_operand_splits_raw_error(gpu, oracle, capsys):
