@@ -402,9 +402,12 @@ template <> struct DenOps<double>
         vl = 0.0;
     }
     static __device__ __forceinline__ double hi(double a) { return a; }
+    // sqrt(L) / max(sqrt(V), tol) as in the reference; the common branch
+    // with one reciprocal square root instead of a square root and a
+    // division (FP64 arithmetic is costly on this GPU)
     static __device__ __forceinline__ double out(double var, double sqrtL, double tol)
     {
-        return var > 0.0 ? sqrtL / fmax(sqrt(var), tol) : 0.0;
+        return var > tol * tol ? sqrtL * rsqrt(var) : (var > 0.0 ? sqrtL / tol : 0.0);
     }
 };
 
