@@ -258,8 +258,8 @@ def cpu_baseline(w, minutes=None, threads=None):
             "seconds": dt}
 
 
-def cpu_baseline_uneven(w, channels=8, minutes=None, threads=None):
-    """The reference algorithm (oracle restatement, FP32) on a bounded sample
+def cpu_baseline_uneven(w, channels=8, minutes=None, threads=None, dtype=np.float32):
+    """The reference algorithm (oracle restatement, FP32 or dtype) on a bounded sample
     of the uneven bank: for each of the first `channels` channels, its
     templates against its first `minutes` of samples in SINGLE_CHANNEL mode
     (a MULTI_CHANNEL instance of the whole bank would hold one signal copy
@@ -279,14 +279,14 @@ def cpu_baseline_uneven(w, channels=8, minutes=None, threads=None):
             continue
         x = w["signals"][c, :n]
         t0 = time.perf_counter()
-        o.matched_filter(tps, [x], multi=False, dtype=np.float32, threads=threads)
+        o.matched_filter(tps, [x], multi=False, dtype=dtype, threads=threads)
         dt += time.perf_counter() - t0
         lags += sum(n - tp.size + 1 for tp in tps)
         nt += len(tps)
     return {"value": lags / dt, "unit": METRIC, "cores": threads, "kind": "port",
             "sample": "channels 0-%d (%d templates of the bank) x first %.0f min, SINGLE_CHANNEL mode per channel "
-                      "(%d template-lags); reference overlap-add algorithm restated in C, FFT by the oracle's "
-                      "radix-2 transform" % (channels - 1, nt, minutes, lags),
+                      "(%d template-lags, %s); reference overlap-add algorithm restated in C, FFT by the "
+                      "oracle's radix-2 transform" % (channels - 1, nt, minutes, lags, np.dtype(dtype).name),
             "seconds": dt}
 
 
@@ -662,9 +662,13 @@ def run_uneven_day(args, ctx):
     candidates gathered in the correlator (rho > 0.7, separation 250) and the
     peaks copied to the host.  value: K steps with the channels resident,
     CUDA events on the library's stream; e2e: the same K steps with every
-    step's channels staged from pinned host memory under the previous step."""
+    step's channels staged from pinned host memory under the previous step.
+    --fp64 runs the same bank in double precision (the reference's default
+    type)."""
     import torch
     import mflib_gb300 as mf
+    fp64 = bool(getattr(args, "fp64", False))
+    npt, tdt, es = (np.float64, torch.float64, 8) if fp64 else (np.float32, torch.float32, 4)
     w = make_uneven_workload(n_samples=args.samples)
     n, nch, lens = w["n"], w["nch"], w["lens"]
     nt = len(w["templates"])
@@ -675,10 +679,10 @@ def run_uneven_day(args, ctx):
         wt.set_sampling_rate(FS)
         p.add_template(wt)
     p.set_signal_size(n)
-    f = mf.MultiChannel.MatchedFilter(dtype=np.float32)
+    f = mf.MultiChannel.MatchedFilter(dtype=npt)
     f.initialize(p, template_channels=[int(c) for c in w["tchan"]], n_channels=nch,
                  correlator_variant=args.correlator_variant, length_buckets=args.length_buckets)
-    pinned = torch.empty((nch, n), dtype=torch.float32, pin_memory=True)
+    pinned = torch.empty((nch, n), dtype=tdt, pin_memory=True)
     pinned.numpy()[:] = w["signals"]
     host = pinned.numpy()
     f.set_channel_signals(host)
@@ -739,7 +743,7 @@ def run_uneven_day(args, ctx):
     t0 = time.perf_counter()
     (c2, i2), _ = run_steps(args.steps, stage=True)
     e2e_el = ctx.max(time.perf_counter() - t0)
-    h2d = nch * n * 4
+    h2d = nch * n * es
     d2h = int(4 * (c2.size + i2.size))
     # the host link's rate for one step's upload alone (the e2e steps overlap
     # it with the previous apply, so it bounds them when it is the longer)
@@ -752,17 +756,19 @@ def run_uneven_day(args, ctx):
     plan = f.get_plan()
     P = plan["fft_length"] // 2
     x_ms = float(np.mean(xms))
-    alg = 4.0 * lags + 4.0 * nch * n + 8.0 * (P + 1) * nt
+    alg = es * lags + es * nch * n + 2.0 * es * (P + 1) * nt
     peak, kind = measured_peak()
     traffic = profile_traffic("xcorr_fp32_uneven_traffic.txt")
-    default = n == N_SAMPLES and args.correlator_variant == 0 and args.length_buckets == 0 and not args.autotune
+    default = (n == N_SAMPLES and args.correlator_variant == 0 and args.length_buckets == 0 and not args.autotune
+               and not fp64)
     roof = {"bound": "hbm", "achieved": alg / (x_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
             "frac": alg / (x_ms * 1e-3) / 1e9 / peak, "traffic": traffic if default else None,
-            "kernel": "xcorr_kernel<float,%d,per-template normalisation>" % P, "kernel_ms": x_ms,
+            "kernel": "xcorr_kernel<%s,%d,per-template normalisation>" % ("double" if fp64 else "float", P),
+            "kernel_ms": x_ms,
             "algorithmic_bytes": alg, "peak_source": kind}
     line = {"metric": METRIC, "value": ctx.world * lags / (el / args.steps), "unit": METRIC, "n_gpus": ctx.world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64" if fp64 else "f32",
             "data": "synthetic seeded seismograms (band-passed noise, Hann-tapered band-passed templates)",
             "config": {"workload": "uneven bank: 2,000 templates of 200-3,000 samples on 96 channels x %d samples, "
                                    "peaks %.1f/%d" % (n, UNEVEN_THR, UNEVEN_SEP),
@@ -783,6 +789,11 @@ def run_uneven_day(args, ctx):
     # template's K padded to 16 (K = L + 7 for the 8 phases of a row), 2 flops
     # each; even at the measured dense BF16/FP16 peak that takes longer than
     # the FFT form's measured step.
+    if tune is not None:
+        line["config"]["autotune"] = tune
+    if fp64:  # the split-precision form is an FP32 path
+        f.clear()
+        return line, w
     kp = ((lens.astype(np.int64) + 7 + 15) // 16) * 16
     tc_flops = float(np.sum(3.0 * 2.0 * kp * (n - lens + 1)))
     bf16, bf16_kind = measured_peak("bf16_tflops")
@@ -790,8 +801,6 @@ def run_uneven_day(args, ctx):
     line["split_precision_ceiling"] = {
         "executed_flops": tc_flops, "ms_at_tensor_peak": tc_ms, "peak_tflops": bf16, "peak_source": bf16_kind,
         "fft_ms_per_step": 1e3 * el / args.steps, "best_possible_ratio_over_fft": (1e3 * el / args.steps) / tc_ms}
-    if tune is not None:
-        line["config"]["autotune"] = tune
     f.clear()
     return line, w
 
@@ -989,6 +998,7 @@ def main():
     ap.add_argument("--autotune", action="store_true",
                     help="uneven bank: measured per-bucket plan choice before timing")
     ap.add_argument("--uneven", action="store_true", help="the uneven bank alone (the default headline, no extras)")
+    ap.add_argument("--fp64", action="store_true", help="uneven bank: double precision (the reference's default type)")
     ap.add_argument("--detector", action="store_true", help="time the single-channel detector")
     ap.add_argument("--stress", action="store_true", help="precision stress: FFT and tensor-core paths")
     ap.add_argument("--length-buckets", type=int, default=0,
@@ -1038,8 +1048,9 @@ def main():
         if ctx.rank == 0 and ctx.world == 1 and not args.no_cpu_baseline:
             # a short warm-up, then the mean of three timed samples (a single
             # cold sample had read well below the reference arm's steady mean)
-            cpu_baseline_uneven(w, channels=1, minutes=10.0)
-            reps = [cpu_baseline_uneven(w) for _ in range(3)]
+            cdt = np.float64 if args.fp64 else np.float32
+            cpu_baseline_uneven(w, channels=1, minutes=10.0, dtype=cdt)
+            reps = [cpu_baseline_uneven(w, dtype=cdt) for _ in range(3)]
             cb = {k: v for k, v in reps[0].items() if k != "seconds"}
             cb["value"] = float(np.mean([r["value"] for r in reps]))
             cb["repeats"] = 3
