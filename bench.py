@@ -19,7 +19,8 @@ precision-stress bank on the FFT and split-precision tensor-core paths
 (`precision_stress`) and the serving loop at one arrival rate
 (`serving`).  `--impl reference` times the reference's algorithm (the CPU
 restatement in oracle/) on the host cores instead.  Other modes:
---day24, --stress, --serving, --detector.
+--uneven (the headline alone; with --fp64 in double precision), --day24,
+--stress, --serving, --detector.
 """
 import argparse
 import ctypes
