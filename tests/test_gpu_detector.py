@@ -155,6 +155,31 @@ def test_detector_errors_and_waveforms(gpu, rng):
         det.get_detection(det.get_number_of_detections())
 
 
+def test_detections_survive_wire_records(gpu, rng):
+    """The GPU detector's detections (detected waveforms, amplitudes,
+    interpolated times, polarities) through the MPI wire records
+    (mflib_gb300.mpi) come back field for field; float32 signals round to
+    float32."""
+    from mflib_gb300 import mpi
+    mf = gpu
+    tps, x = _case(rng, 3, [120, 200, 160], 20_000)
+    prm = mf.SingleChannel.DetectorParameters()
+    prm.set_detection_threshold(0.3)
+    prm.enable_save_detected_waveform()
+    det = mf.SingleChannel.Detector()
+    det.initialize(prm)
+    det.detect(_filter(mf, tps, x, np.float64, 100.0))
+    ds = det.get_detections()
+    assert len(ds) > 2 and all(d.have_detected_signal() for d in ds)
+    for dtype in (np.float64, np.float32):
+        recs, sig = mpi.pack_detections(ds, dtype)
+        got = mpi.unpack_detections(recs, sig)
+        for a, b in zip(ds, got):
+            sa, sb = a.__getstate__(), b.__getstate__()
+            sa["sig"] = np.asarray(sa["sig"], dtype).tolist()
+            assert sa == sb
+
+
 @pytest.mark.parametrize("dtype", [np.float32, np.float64])
 def test_relative_magnitude(gpu, oracle, rng, dtype):
     """RelativeMagnitude on the GPU against the restatement (pinned to the
