@@ -31,6 +31,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <stdexcept>
 #include <string>
 #include <utility>
@@ -151,7 +152,9 @@ template <class T> void fromRecord(const DetectionRecord &r, const T *signal, Si
         nsp.setPhase(detail::get64(r.phase));
         det->setTemplateIdentifier({nsp, r.templateID});
     }
-    det->setPolarity((Polarity) r.polarity);
+    /* a byte other than -1, 0, 1 (a sender's uninitialised padding) reads as unknown */
+    det->setPolarity(r.polarity == 1 ? Polarity::COMPRESSION
+                                     : (r.polarity == -1 ? Polarity::DILATATION : Polarity::UNKNOWN));
 }
 
 /* MPI::Send (src/mpi.cpp:386-414) */
@@ -275,6 +278,10 @@ std::vector<SingleChannel::Detection<T>> Gather(const std::vector<SingleChannel:
         if (d.haveDetectedSignal())
             sig.insert(sig.end(), d.getDetectedSignalPointer(), d.getDetectedSignalPointer() + d.getDetectedSignalLength());
     }
+    /* MPI counts are int: byte counts of the records and sample counts of the signals must fit */
+    if (recs.size() > (size_t) std::numeric_limits<int>::max() / sizeof(DetectionRecord) ||
+        sig.size() > (size_t) std::numeric_limits<int>::max())
+        throw std::invalid_argument("too many detections or detected samples for one gather");
     const int mine[2] = {(int) recs.size(), (int) sig.size()};
     std::vector<int> counts(me == root ? 2 * size : 0);
     detail::check(MPI_Gather(mine, 2, MPI_INT, counts.data(), 2, MPI_INT, root, comm), "MPI_Gather");
@@ -289,6 +296,8 @@ std::vector<SingleChannel::Detection<T>> Gather(const std::vector<SingleChannel:
             ns[r] = counts[2 * r + 1];
             ds[r] = totS;
             totS += counts[2 * r + 1];
+            if (totR > std::numeric_limits<int>::max() / (int) sizeof(DetectionRecord) || totS < 0)
+                throw std::runtime_error("gathered detections exceed one gather's int counts");
         }
     std::vector<DetectionRecord> allR(totR);
     std::vector<T> allS(totS);

@@ -150,7 +150,9 @@ def unpack_detection(rec, signal=None, det=None):
         nsp.set_station(_unstr(r["station"]))
         nsp.set_phase(_unstr(r["phase"]))
         det.set_template_identifier((nsp, int(r["template_id"])))
-    det.set_polarity(Polarity(int(r["polarity"])))
+    # a byte other than -1, 0, 1 (a sender's uninitialised padding) reads as unknown
+    pol = int(r["polarity"])
+    det.set_polarity(Polarity(pol) if pol in (-1, 0, 1) else Polarity.unknown)
     return det
 
 

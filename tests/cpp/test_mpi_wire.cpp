@@ -169,6 +169,10 @@ template <class T> void roundTrips(const char *name)
     require(id.first.getNetwork() == std::string(64, 'N') && id.first.getStation() == "STA" &&
                 id.first.getChannel().empty() && id.first.getLocationCode().empty() && id.second == 7,
             std::string(name) + " names truncated to 64 bytes; channel and location code not in the record");
+    MPI::DetectionRecord bad = MPI::toRecord(d);
+    bad.polarity = 77;
+    MPI::fromRecord<T>(bad, nullptr, &e);
+    require(e.getPolarity() == Polarity::UNKNOWN, std::string(name) + " a polarity byte outside -1, 0, 1 reads as unknown");
 }
 
 template <class T> void transport(const char *name)

@@ -107,6 +107,10 @@ def test_record_truncation_and_dropped_fields():
     assert not mpi.unpack_detection(mpi.pack_detection(d), det=tgt).have_detection_time()
     with pytest.raises(ValueError):
         mpi.unpack_detection(mpi.pack_detection(_dets(2, 1)[0]), None)  # its signal is missing
+    # a polarity byte outside -1, 0, 1 reads as unknown
+    r = mpi.pack_detection(_dets(3, 1)[0])
+    r["polarity"] = 77
+    assert mpi.unpack_detection(r, _dets(3, 1)[0].get_detected_signal()).get_polarity() == Polarity.unknown
     with pytest.raises(ValueError):
         mpi.pack_detections([Detection()], np.int32)
     with pytest.raises(ValueError):
