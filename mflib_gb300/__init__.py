@@ -17,6 +17,10 @@ from .detector import (DetectionTimeInterpolationType, MatchedFilteredSignalDete
                        MaximumMatchedFilterPolicy, RelativeMagnitudeType)
 from .matched_filter import _attach_detector
 
+# pymflib binds this enumeration under a misspelt name (python/pymflib.cpp:29);
+# code written against pymflib uses it
+MaxmimumMatchedFilterPolicy = MaximumMatchedFilterPolicy
+
 _attach_detector()
 
 __version__ = "1.0.0"
@@ -27,5 +31,6 @@ __all__ = [
     "PeakFinder", "Polarity", "SignalRing", "SingleChannel", "WaveformTemplate",
     "compute_optimal_fft_and_block_length",
     "DetectionTimeInterpolationType", "MatchedFilteredSignalDetectorPolicy", "MaximumMatchedFilterPolicy",
+    "MaxmimumMatchedFilterPolicy",
     "RelativeMagnitudeType",
 ]

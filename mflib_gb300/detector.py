@@ -253,12 +253,20 @@ class Detection:
         return self._poi is not None
 
     def set_amplitude_scaling_factor(self, value, mag_type):
+        """python/singleChannel/detection.cpp:333-343: the factor must be
+        positive."""
+        if not value > 0:
+            raise ValueError("Scaling factor = %g must be positive" % value)
         self._amp[RelativeMagnitudeType(int(mag_type))] = float(value)
 
     def get_amplitude_scaling_factor(self, mag_type):
         return self._get(self._amp.get(RelativeMagnitudeType(int(mag_type))), "Amplitude scaling factor")
 
-    def have_amplitude_scaling_factor(self, mag_type):
+    def have_amplitude_scaling_factor(self, mag_type=None):
+        """With a type: that factor is set.  Without one, as pymflib
+        (python/singleChannel/detection.cpp:353-362): both factors are set."""
+        if mag_type is None:
+            return len(self._amp) == len(RelativeMagnitudeType)
         return RelativeMagnitudeType(int(mag_type)) in self._amp
 
     def get_magnitude_perturbation(self, mag_type):

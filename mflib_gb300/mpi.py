@@ -133,7 +133,9 @@ def unpack_detection(rec, signal=None, det=None):
         r = np.frombuffer(r.tobytes(), DETECTION_RECORD)[0]
     for i, t in enumerate(_AMP):
         if r["have_amplitude%d" % (i + 1)]:
-            det.set_amplitude_scaling_factor(float(r["amplitude%d" % (i + 1)]), t)
+            # the sent value as it is (the detector may have computed a factor
+            # the public setter, which wants a positive one, would refuse)
+            det._amp[t] = float(r["amplitude%d" % (i + 1)])
     if r["have_correlation_coefficient"]:
         det.set_correlation_coefficient(float(r["correlation_coefficient"]))
     for f in _TIMES:

@@ -145,3 +145,78 @@ def test_single_channel_parameters(mflib, rng):
     assert p.get_number_of_templates() == 0
     p.clear()
     assert not p.is_valid()
+
+
+def test_single_channel_detection(mflib, rng):
+    # python/unit_tests.py:328-457: every field's have / set / get, the same
+    # object through an alias, and a pickle round trip (which here also
+    # carries the detected signal)
+    sc, rmt = mflib.SingleChannel, mflib.RelativeMagnitudeType
+    nsp = mflib.NetworkStationPhase()
+    nsp.set_network("UU")
+    nsp.set_station("CMU")
+    nsp.set_channel("EHZ")
+    nsp.set_location_code("01")
+    nsp.set_phase("P")
+    xt = rng.uniform(5, 7, 400)
+    d = sc.Detection()
+    fields = [("phase_onset_time", 4.0), ("interpolated_phase_onset_time", 9.0), ("detection_time", 2.0),
+              ("interpolated_detection_time", 3.0), ("travel_time", 13.0), ("correlation_coefficient", 0.3)]
+    assert not d.have_template_identifier()
+    d.set_template_identifier([nsp, 204])
+    for name, v in fields:
+        assert not getattr(d, "have_" + name)()
+        getattr(d, "set_" + name)(v)
+        assert getattr(d, "have_" + name)() and getattr(d, "get_" + name)() == v
+    assert not d.have_amplitude_scaling_factor()
+    d.set_amplitude_scaling_factor(9, rmt.gibbons_ringdal_2006)
+    assert not d.have_amplitude_scaling_factor()  # pymflib: true once both are set
+    d.set_amplitude_scaling_factor(10, rmt.schaff_richards_2014)
+    assert d.have_amplitude_scaling_factor() and d.have_amplitude_scaling_factor(rmt.schaff_richards_2014)
+    with pytest.raises(ValueError):
+        d.set_amplitude_scaling_factor(0.0, rmt.gibbons_ringdal_2006)
+    with pytest.raises(ValueError):
+        d.set_correlation_coefficient(1.5)
+    assert not d.have_detected_signal()
+    d.set_detected_signal(xt)
+    assert d.have_detected_signal() and np.max(np.abs(d.get_detected_signal() - xt)) < 1e-14
+    for e in (d, pickle.loads(pickle.dumps(d, 2))):
+        ident = e.get_template_identifier()
+        assert ident[1] == 204
+        assert [ident[0].get_network(), ident[0].get_station(), ident[0].get_channel(),
+                ident[0].get_location_code(), ident[0].get_phase()] == ["UU", "CMU", "EHZ", "01", "P"]
+        for name, v in fields:
+            assert getattr(e, "get_" + name)() == v
+        assert e.get_amplitude_scaling_factor(rmt.gibbons_ringdal_2006) == 9
+        assert e.get_amplitude_scaling_factor(rmt.schaff_richards_2014) == 10
+        assert np.max(np.abs(e.get_detected_signal() - xt)) < 1e-14
+
+
+def test_single_channel_detector_parameters(mflib):
+    # python/unit_tests.py:459-489, with pymflib's spelling of the maxima
+    # policy enumeration (python/pymflib.cpp:29)
+    p = mflib.SingleChannel.DetectorParameters()
+    p.set_maxima_policy(mflib.MaxmimumMatchedFilterPolicy.absolute_maximum)
+    p.set_matched_filtered_signal_detector_policy(mflib.MatchedFilteredSignalDetectorPolicy.single)
+    p.set_minimum_detection_spacing(5)
+    p.set_detection_threshold(0.5)
+    p.enable_save_detected_waveform()
+    p.disable_save_amplitude_scaling_factor()
+    for q in (p, p):
+        assert q.get_maxima_policy() == mflib.MaxmimumMatchedFilterPolicy.absolute_maximum
+        assert q.get_maxima_policy() == mflib.MaximumMatchedFilterPolicy.absolute_maximum
+        assert q.get_minimum_detection_spacing() == 5 and q.get_detection_threshold() == 0.5
+        assert q.want_detected_waveform() and not q.want_amplitude_scaling_factor()
+        assert q.get_matched_filtered_signal_detector_policy() == mflib.MatchedFilteredSignalDetectorPolicy.single
+
+
+def test_single_channel_associator_parameters(mflib):
+    # python/unit_tests.py:491-507
+    p = mflib.SingleChannel.AssociatorParameters()
+    p.set_origin_time_tolerance(0.5)
+    p.set_minimum_number_of_picks_in_event(8)
+    p.enable_correlation_coefficient_weighting()
+    for q in (p, p):
+        assert q.get_origin_time_tolerance() == 0.5
+        assert q.get_minimum_number_of_picks_in_event() == 8
+        assert q.use_correlation_coefficient_weighting()

@@ -155,6 +155,26 @@ def test_detector_errors_and_waveforms(gpu, rng):
         det.get_detection(det.get_number_of_detections())
 
 
+def test_pymflib_relative_magnitude(gpu, rng):
+    # python/unit_tests.py:301-326: both magnitude perturbations of random
+    # windows equal their closed forms over the demeaned signals to 1e-14
+    mf = gpu
+    xt, yt = rng.uniform(5, 7, 355), rng.uniform(-2, 1, 355)
+    wt = mf.WaveformTemplate()
+    wt.set_sampling_rate(100.0)
+    wt.set_signal(xt)
+    rm = mf.SingleChannel.RelativeMagnitude()
+    rm.initialize(wt)
+    assert rm.is_initialized() and rm.get_detected_signal_length() == 355
+    rm.set_detected_signal(yt)
+    assert rm.have_detected_signal()
+    xd, yd = xt - xt.mean(), yt - yt.mean()
+    gr = np.log10(abs(xd @ yd) / (xd @ xd))
+    sr = 0.5 * np.log10((yd @ yd) / (xd @ xd))
+    assert abs(rm.compute_magnitude_perturbation(mf.RelativeMagnitudeType.gibbons_ringdal_2006) - gr) < 1e-14
+    assert abs(rm.compute_magnitude_perturbation(mf.RelativeMagnitudeType.schaff_richards_2014) - sr) < 1e-14
+
+
 def test_detections_survive_wire_records(gpu, rng):
     """The GPU detector's detections (detected waveforms, amplitudes,
     interpolated times, polarities) through the MPI wire records
