@@ -148,3 +148,66 @@ class Associator:
         if iev < 0 or iev >= len(self._events):
             raise ValueError("iev out of range")
         return self._events[iev][0]
+
+
+# Summary statistics of an event's picks (include/private/weightedStatistics.hpp:
+# median, weightedMedian, mean, weightedMean).  Sums run left to right, as
+# std::accumulate does.
+def median(x):
+    """Median of x; 0 for no values (weightedStatistics.hpp:17-32)."""
+    x = np.sort(np.asarray(x, dtype=np.float64).ravel())
+    n = x.size
+    if n == 0:
+        return 0.0
+    return float(x[n // 2]) if n % 2 else float((x[n // 2 - 1] + x[n // 2]) / 2)
+
+
+def weighted_median(x, weights=None):
+    """Weighted median (weightedStatistics.hpp:42-85): the x at which the
+    weights' normalised cumulative sum, over x sorted ascending, reaches 1/2,
+    interpolated linearly between the two observations that straddle it; x
+    itself where the sum equals 1/2 exactly.  No weights: the median."""
+    x = np.asarray(x, dtype=np.float64).ravel()
+    n = x.size
+    if n == 0:
+        return 0.0
+    if n == 1:
+        return float(x[0])
+    if weights is None:
+        return median(x)
+    w = np.asarray(weights, dtype=np.float64).ravel()
+    if w.size != n:
+        raise ValueError("weights must have one value per observation")
+    order = np.argsort(x, kind="stable")
+    xs, cdf = x[order], np.cumsum(w[order] / np.cumsum(w)[-1])
+    if cdf[0] > 0.5:
+        return float(xs[0])
+    i = int(np.argmax(cdf[1:] >= 0.5)) + 1
+    if not cdf[i] >= 0.5:
+        return float(xs[0])
+    if cdf[i] == 0.5:
+        return float(xs[i])
+    return float(xs[i - 1] + (xs[i] - xs[i - 1]) * (0.5 - cdf[i - 1]) / (cdf[i] - cdf[i - 1]))
+
+
+def mean(x):
+    """Mean of x; 0 for no values (weightedStatistics.hpp:90-96)."""
+    x = np.asarray(x, dtype=np.float64).ravel()
+    return float(np.cumsum(x)[-1] / x.size) if x.size else 0.0
+
+
+def weighted_mean(x, weights=None):
+    """Sum of x w over the sum of w (weightedStatistics.hpp:106-115); no
+    weights: the mean."""
+    x = np.asarray(x, dtype=np.float64).ravel()
+    n = x.size
+    if n == 0:
+        return 0.0
+    if n == 1:
+        return float(x[0])
+    if weights is None:
+        return mean(x)
+    w = np.asarray(weights, dtype=np.float64).ravel()
+    if w.size != n:
+        raise ValueError("weights must have one value per observation")
+    return float(np.cumsum(x * w)[-1] / np.cumsum(w)[-1])

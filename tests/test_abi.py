@@ -220,3 +220,22 @@ def test_single_channel_associator_parameters(mflib):
         assert q.get_origin_time_tolerance() == 0.5
         assert q.get_minimum_number_of_picks_in_event() == 8
         assert q.use_correlation_coefficient_weighting()
+
+
+def test_weighted_statistics_known_answers(mflib):
+    # testing/associator.cpp:36-78 (values from R's spatstat weighted.median)
+    from mflib_gb300.associator import mean, median, weighted_mean, weighted_median
+    x = [1.1, 5.3, 3.7, 2.1, 7.0, 9.9]
+    w = [1.1, 0.4, 2.1, 3.5, 1.2, 0.8]
+    xp = [0.1, 0.35, 0.05, 0.1, 0.15, 0.05, 0.2]
+    assert abs(weighted_median(x, w) - 2.085714) < 1e-6
+    assert abs(weighted_median(xp, xp) - 0.1625) < 1e-6
+    assert abs(weighted_median(xp[:-1], xp[:-1]) - 0.1333333) < 1e-6
+    assert abs(weighted_median([1, 2], [1, 4]) - 1.375) < 1e-6
+    assert weighted_median(x[:1], w[:1]) == x[0]
+    assert abs(median(x) - 4.5) < 1e-6 and abs(median(x[:-1]) - 3.7) < 1e-6 and median(x[:1]) == x[0]
+    assert abs(weighted_mean(xp, xp) - 0.21) < 1e-6 and weighted_mean(x[:1], x[:1]) == x[0]
+    assert abs(mean(xp) - 0.1428571) < 1e-6 and mean(x[:1]) == x[0]
+    # empty input and no weights, as the reference's helpers
+    assert median([]) == mean([]) == weighted_median([], None) == weighted_mean([], None) == 0.0
+    assert weighted_median(x) == median(x) and weighted_mean(x) == mean(x)
