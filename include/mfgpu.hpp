@@ -661,6 +661,7 @@ class DetectorParameters
 template <class T = double> class Detection
 {
   public:
+    void clear() noexcept { *this = Detection(); }
     void setTemplateIdentifier(const std::pair<NetworkStationPhase, uint64_t> &id) { mId = id; mHaveId = true; }
     std::pair<NetworkStationPhase, uint64_t> getTemplateIdentifier() const
     {

@@ -2,7 +2,8 @@
 the C ABI, links against libmfgpu.so, and on a GPU passes the reference's
 known-answer checks (tests/cpp/test_mflib_api.cpp); the ABI's exception
 handler maps host exceptions to status codes (tests/cpp/test_abi_exceptions.cpp,
-no GPU)."""
+no GPU); the host-side classes pass the reference's C++ tests of them
+(tests/cpp/test_host_classes.cpp, no GPU)."""
 import os
 import shutil
 import subprocess
@@ -63,3 +64,16 @@ def test_abi_exception_mapping(tmp_path):
     assert run.returncode == 0, run.stdout + run.stderr
     assert "ALL PASSED" in run.stdout
 
+
+
+@pytest.mark.skipif(CXX is None, reason="g++ not found")
+def test_host_classes(tmp_path):
+    """The header's host-side classes against the reference's own C++ tests
+    of them (tests/cpp/test_host_classes.cpp); no GPU, no library."""
+    exe = str(tmp_path / "test_host_classes")
+    r = subprocess.run([CXX, "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        os.path.join(ROOT, "tests", "cpp", "test_host_classes.cpp"), "-o", exe],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    run = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert run.returncode == 0 and "ALL PASSED" in run.stdout, run.stdout + run.stderr

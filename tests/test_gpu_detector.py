@@ -156,8 +156,9 @@ def test_detector_errors_and_waveforms(gpu, rng):
 
 
 def test_pymflib_relative_magnitude(gpu, rng):
-    # python/unit_tests.py:301-326: both magnitude perturbations of random
-    # windows equal their closed forms over the demeaned signals to 1e-14
+    # python/unit_tests.py:301-326 (and testing/relativeMagnitude.cpp:21-62 at
+    # 1e-12): both magnitude perturbations of random windows equal their
+    # closed forms over the demeaned signals to 1e-14
     mf = gpu
     xt, yt = rng.uniform(5, 7, 355), rng.uniform(-2, 1, 355)
     wt = mf.WaveformTemplate()
