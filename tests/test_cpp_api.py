@@ -65,7 +65,6 @@ def test_abi_exception_mapping(tmp_path):
     assert "ALL PASSED" in run.stdout
 
 
-
 @pytest.mark.skipif(CXX is None, reason="g++ not found")
 def test_host_classes(tmp_path):
     """The header's host-side classes against the reference's own C++ tests
