@@ -137,8 +137,10 @@ class Associator:
         return len(self._events)
 
     def get_detections_in_event(self, iev):
+        """The detections of event iev; an empty list when there are no events
+        (pymflib, python/singleChannel/associator.cpp:127-133)."""
         if not self._events:
-            raise RuntimeError("No detections have been associated")
+            return []
         if iev < 0 or iev >= len(self._events):
             raise ValueError("iev = %d must be in range [0,%d]" % (iev, len(self._events) - 1))
         return [self._dets[i] for i in self._events[iev][1]]

@@ -156,6 +156,12 @@ class DetectorParameters:
         return self._interp
 
 
+def _non_negative(t, what):
+    # the pymflib setters refuse negative times (python/singleChannel/detection.cpp:191-290)
+    if t < 0:
+        raise ValueError("%s = %g must not be negative" % (what, t))
+
+
 class Detection:
     """src/singleChannel/detection.cpp: a detection's value fields, each with
     get / set / have."""
@@ -208,6 +214,7 @@ class Detection:
         return self._sig is not None
 
     def set_detection_time(self, t):
+        _non_negative(t, 'Detection time')
         self._t = float(t)
 
     def get_detection_time(self):
@@ -217,6 +224,7 @@ class Detection:
         return self._t is not None
 
     def set_interpolated_detection_time(self, t):
+        _non_negative(t, 'Detection time')
         self._ti = float(t)
 
     def get_interpolated_detection_time(self):
@@ -226,6 +234,7 @@ class Detection:
         return self._ti is not None
 
     def set_travel_time(self, t):
+        _non_negative(t, 'Travel time')
         self._tt = float(t)
 
     def get_travel_time(self):
@@ -235,6 +244,7 @@ class Detection:
         return self._tt is not None
 
     def set_phase_onset_time(self, t):
+        _non_negative(t, 'Onset time')
         self._po = float(t)
 
     def get_phase_onset_time(self):
@@ -244,6 +254,7 @@ class Detection:
         return self._po is not None
 
     def set_interpolated_phase_onset_time(self, t):
+        _non_negative(t, 'Onset time')
         self._poi = float(t)
 
     def get_interpolated_phase_onset_time(self):

@@ -67,6 +67,8 @@ TEMPLATE_HEADER = np.dtype({
 _AMP = (RelativeMagnitudeType.gibbons_ringdal_2006, RelativeMagnitudeType.schaff_richards_2014)
 _TIMES = ("detection_time", "interpolated_detection_time", "phase_onset_time", "interpolated_phase_onset_time",
           "travel_time")
+_TIME_ATTRS = (("detection_time", "_t"), ("interpolated_detection_time", "_ti"), ("phase_onset_time", "_po"),
+               ("interpolated_phase_onset_time", "_poi"), ("travel_time", "_tt"))
 
 
 def _str64(s):
@@ -131,16 +133,17 @@ def unpack_detection(rec, signal=None, det=None):
     r = np.asarray(rec)
     if r.dtype != DETECTION_RECORD:
         r = np.frombuffer(r.tobytes(), DETECTION_RECORD)[0]
+    # the sent values as they are, assigned directly: a detector's refined
+    # time may be slightly negative and its amplitude factor 0, which the
+    # public setters refuse
     for i, t in enumerate(_AMP):
         if r["have_amplitude%d" % (i + 1)]:
-            # the sent value as it is (the detector may have computed a factor
-            # the public setter, which wants a positive one, would refuse)
             det._amp[t] = float(r["amplitude%d" % (i + 1)])
     if r["have_correlation_coefficient"]:
-        det.set_correlation_coefficient(float(r["correlation_coefficient"]))
-    for f in _TIMES:
+        det._xc = float(r["correlation_coefficient"])
+    for f, attr in _TIME_ATTRS:
         if r["have_" + f]:
-            getattr(det, "set_" + f)(float(r[f]))
+            setattr(det, attr, float(r[f]))
     if r["have_detected_signal"]:
         n = int(r["signal_length"])
         if signal is None or len(signal) != n:

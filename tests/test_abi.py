@@ -177,6 +177,11 @@ def test_single_channel_detection(mflib, rng):
         d.set_amplitude_scaling_factor(0.0, rmt.gibbons_ringdal_2006)
     with pytest.raises(ValueError):
         d.set_correlation_coefficient(1.5)
+    # pymflib refuses negative times (python/singleChannel/detection.cpp:191-290)
+    for name in ("detection_time", "interpolated_detection_time", "phase_onset_time",
+                 "interpolated_phase_onset_time", "travel_time"):
+        with pytest.raises(ValueError):
+            getattr(d, "set_" + name)(-1.0)
     assert not d.have_detected_signal()
     d.set_detected_signal(xt)
     assert d.have_detected_signal() and np.max(np.abs(d.get_detected_signal() - xt)) < 1e-14

@@ -107,6 +107,11 @@ def test_record_truncation_and_dropped_fields():
     assert not mpi.unpack_detection(mpi.pack_detection(d), det=tgt).have_detection_time()
     with pytest.raises(ValueError):
         mpi.unpack_detection(mpi.pack_detection(_dets(2, 1)[0]), None)  # its signal is missing
+    # a record carries what the detector computed, even where the public
+    # setters would refuse it (a refined time just below 0)
+    r = mpi.pack_detection(Detection())
+    r["have_interpolated_detection_time"], r["interpolated_detection_time"] = True, -0.004
+    assert mpi.unpack_detection(r).get_interpolated_detection_time() == -0.004
     # a polarity byte outside -1, 0, 1 reads as unknown
     r = mpi.pack_detection(_dets(3, 1)[0])
     r["polarity"] = 77
