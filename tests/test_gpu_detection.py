@@ -162,6 +162,27 @@ def test_dbscan_random_vs_oracle(gpu, oracle, rng, nf):
             np.testing.assert_array_equal(db.get_labels(), lab)
 
 
+@pytest.mark.parametrize("nf", [1, 2])
+def test_dbscan_edge_cases_vs_oracle(gpu, oracle, rng, nf):
+    # eps = 0 (only exact duplicates are neighbours), every point the same,
+    # minPts = 1 (every point a core point) and a single observation, on the
+    # one-feature sorted path and the all-pairs path
+    db = gpu.DBSCAN()
+    dup = np.repeat(rng.integers(0, 40, (60, nf)).astype(np.float64), rng.integers(1, 5, 60), axis=0)
+    rng.shuffle(dup)
+    cases = [(dup, 0.0, 2), (dup, 0.0, 1), (dup, 0.0, 4), (np.full((500, nf), 7.5), 0.0, 3),
+             (np.full((500, nf), 7.5), 1.0, 501), (rng.uniform(0, 100, (300, nf)), 1.5, 1),
+             (np.array([[3.0] * nf]), 0.0, 1), (np.array([[3.0] * nf]), 2.0, 2)]
+    for X, eps, mo in cases:
+        for weights in (None, rng.integers(1, 4, X.shape[0]) / 2.0):
+            db.initialize(eps, mo)
+            db.set_weighted_data(X[:, 0] if nf == 1 else X, weights)
+            db.cluster()
+            ncl, lab = oracle.dbscan(X[:, 0] if nf == 1 else X, eps, mo, weights)
+            assert db.get_number_of_clusters() == ncl, (eps, mo, X.shape)
+            np.testing.assert_array_equal(db.get_labels(), lab)
+
+
 def test_dbscan_segmented(gpu, oracle, rng):
     mf = gpu
     db = mf.DBSCAN()
