@@ -54,6 +54,12 @@ mfgpu_status mfgpu_device_count(int *count);
  * Returns the reference's FFT length and overlap-add block length. */
 mfgpu_status mfgpu_fft_sizes(int nb, int nx, int *fft_length, int *block_length);
 
+/* MFLib::MatchedFilterParameters::getFFTLength / getBlockLength for a longest
+ * template of nb samples and a signal of nx (src/matchedFilterParameters.cpp:268-300,
+ * computeWindowLength :47-104): the same search as mfgpu_fft_sizes, an error
+ * only when nb > nx (a signal as long as the template is accepted). */
+mfgpu_status mfgpu_window_length(int nb, int nx, int *fft_length, int *block_length);
+
 /* ------------------------------------------------------------------------ */
 /* Matched filter: MFLib::MatchedFilter<T> (include/mflib/matchedFilter.hpp:28-178)
  * and its SINGLE_CHANNEL facade MFLib::SingleChannel::MatchedFilter<T>

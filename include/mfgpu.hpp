@@ -304,7 +304,10 @@ class MatchedFilterParameters
     {
         if (mTemplates.empty()) throw std::runtime_error("Templates must be set prior to calling this");
         if (mFFT > 0) return {mFFT, mBlock};
-        return computeOptimalFFTAndBlockLength(getMaxTemplateLength(), getSignalSize());
+        /* the window-length rule of getFFTLength (src/matchedFilterParameters.cpp:268-300) */
+        int n = 0, l = 0;
+        detail::check(mfgpu_window_length(getMaxTemplateLength(), getSignalSize(), &n, &l));
+        return {n, l};
     }
     std::vector<WaveformTemplate> mTemplates;
     double mFs = 0;

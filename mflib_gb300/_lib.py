@@ -86,6 +86,7 @@ _SIGS = {
     "mfgpu_version": ([], C.c_int),
     "mfgpu_device_count": ([_ip], C.c_int),
     "mfgpu_fft_sizes": ([C.c_int, C.c_int, _ip, _ip], C.c_int),
+    "mfgpu_window_length": ([C.c_int, C.c_int, _ip, _ip], C.c_int),
     "mfgpu_mf_create": ([C.c_int, C.POINTER(_vp)], C.c_int),
     "mfgpu_mf_destroy": ([_vp], C.c_int),
     "mfgpu_mf_initialize": ([_vp, C.POINTER(MfgpuParams)], C.c_int),

@@ -70,12 +70,14 @@ const double kFftFlops[21] = {18,       59,       138,       303,       660,    
                               6875,     14952,    32373,     69762,     149647,    319644,   680105,
                               1441974,  3047619,  6422736,   13500637,  28311786,  59244791, 59244791 * 2.09};
 
-mfgpu_status fft_sizes(int nb, int nx, int *nfft, int *L)
+// The FFT and block length minimising blocks x flops over the table
+// (src/matchedFilterParameters.cpp:47-104, computeWindowLength): the rule
+// MatchedFilterParameters::getFFTLength applies, an error only when the
+// template is longer than the signal.
+mfgpu_status window_length(int nb, int nx, int *nfft, int *L)
 {
     if (nb < 1) return fail(MFGPU_EINVAL, "Filter length must be positive");
-    if (nx <= nb)
-        return fail(MFGPU_EINVAL, "Signal length = " + std::to_string(nx) + " must exceed filter length = " +
-                                      std::to_string(nb));
+    if (nb > nx) return fail(MFGPU_EINVAL, "nb = " + std::to_string(nb) + " cannot exceed nx = " + std::to_string(nx));
     int start = -1;
     for (int i = 0; i < 21; ++i)
         if ((uint64_t) 1 << (i + 1) > (uint64_t) (nb - 1)) { start = i; break; }
@@ -99,6 +101,17 @@ mfgpu_status fft_sizes(int nb, int nx, int *nfft, int *L)
     *nfft = bn;
     *L = bl;
     return MFGPU_OK;
+}
+
+// computeOptimalFFTAndBlockLength (src/matchedFilterParameters.cpp:371-385):
+// the signal must be longer than the filter
+mfgpu_status fft_sizes(int nb, int nx, int *nfft, int *L)
+{
+    if (nb < 1) return fail(MFGPU_EINVAL, "Filter length must be positive");
+    if (nx <= nb)
+        return fail(MFGPU_EINVAL, "Signal length = " + std::to_string(nx) + " must exceed filter length = " +
+                                      std::to_string(nb));
+    return window_length(nb, nx, nfft, L);
 }
 
 }  // namespace
@@ -403,6 +416,17 @@ try
 {
     if (!fft_length || !block_length) return fail(MFGPU_EINVAL, "output is NULL");
     return fft_sizes(nb, nx, fft_length, block_length);
+}
+catch (...)
+{
+    return mfgpu::status_of_exception();
+}
+
+mfgpu_status mfgpu_window_length(int nb, int nx, int *fft_length, int *block_length)
+try
+{
+    if (!fft_length || !block_length) return fail(MFGPU_EINVAL, "output is NULL");
+    return window_length(nb, nx, fft_length, block_length);
 }
 catch (...)
 {

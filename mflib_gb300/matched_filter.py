@@ -93,11 +93,15 @@ class MatchedFilterParameters:
         self._block = self._fft - nb + 1
 
     def _sizes(self):
+        # getFFTLength / getBlockLength (src/matchedFilterParameters.cpp:268-300):
+        # the window-length rule, which accepts a signal as long as the template
         if not self._templates:
             raise RuntimeError("Templates must be set prior to calling this")
         if self._fft < 1:
-            self._fft, self._block = compute_optimal_fft_and_block_length(
-                self.get_max_template_length(), self.get_signal_size())
+            a, b = C.c_int(), C.c_int()
+            _lib.call("mfgpu_window_length", self.get_max_template_length(), self.get_signal_size(),
+                      C.byref(a), C.byref(b))
+            self._fft, self._block = a.value, b.value
         return self._fft, self._block
 
     def get_fft_length(self):

@@ -236,6 +236,7 @@ class Reference:
         self.lib = C.CDLL(path)
         L = self.lib
         L.ref_fft_sizes.argtypes = [C.c_int, C.c_int, _ip, _ip]
+        L.ref_window_length.argtypes = [C.c_int, C.c_int, _ip, _ip]
         L.ref_mf_d.argtypes = [C.c_int, C.c_int, _ip, C.c_void_p, C.c_int, C.c_void_p,
                                _dp, C.c_long]
         L.ref_mf_f.argtypes = [C.c_int, C.c_int, _ip, C.c_void_p, C.c_int, C.c_void_p,
@@ -288,6 +289,14 @@ class Reference:
     def fft_sizes(self, nb, nx):
         a, b = C.c_int(), C.c_int()
         if self.lib.ref_fft_sizes(nb, nx, C.byref(a), C.byref(b)) != 0:
+            raise ValueError("invalid sizes")
+        return a.value, b.value
+
+    def window_length(self, nb, nx):
+        """MatchedFilterParameters::getFFTLength / getBlockLength for a
+        template of nb samples and a signal of nx."""
+        a, b = C.c_int(), C.c_int()
+        if self.lib.ref_window_length(nb, nx, C.byref(a), C.byref(b)) != 0:
             raise ValueError("invalid sizes")
         return a.value, b.value
 

@@ -7,6 +7,7 @@
  *
  * Calls: MFLib::computeOptimalFFTAndBlockLength
  *        (include/mflib/matchedFilterParameters.hpp:208),
+ *        MFLib::MatchedFilterParameters::getFFTLength / getBlockLength,
  *        MFLib::MatchedFilter<T> (include/mflib/matchedFilter.hpp:28-178),
  *        MFLib::PeakFinder<T> (include/private/peakFinder.hpp:12-138),
  *        MFLib::SingleChannel::{MatchedFilter, Detector}<T>
@@ -41,6 +42,29 @@ REF_API int ref_fft_sizes(int nb, int nx, int *nfft, int *L)
         auto r = computeOptimalFFTAndBlockLength(nb, nx);
         *nfft = r.first;
         *L = r.second;
+        return 0;
+    }
+    catch (const std::exception &) { return -1; }
+}
+
+/* MatchedFilterParameters::getFFTLength / getBlockLength for one template
+ * of nb samples and a signal of nx samples: the window-length rule the
+ * parameters object applies (computeWindowLength), not the public
+ * function's stricter precondition. */
+REF_API int ref_window_length(int nb, int nx, int *nfft, int *L)
+{
+    try
+    {
+        std::vector<double> b(nb, 0.0);
+        for (int i = 0; i < nb; ++i) b[i] = (double) (i % 7) - 3.0;
+        WaveformTemplate wt;
+        wt.setSamplingRate(1.0);
+        wt.setSignal(nb, b.data());
+        MatchedFilterParameters p;
+        p.addTemplate(wt);
+        p.setSignalSize(nx);
+        *nfft = p.getFFTLength();
+        *L = p.getBlockLength();
         return 0;
     }
     catch (const std::exception &) { return -1; }

@@ -42,6 +42,33 @@ def test_fft_sizes_through_abi(mflib, oracle, rng):
         mflib.compute_optimal_fft_and_block_length(0, 10)
 
 
+def test_parameters_window_length_vs_reference(mflib, reference, rng):
+    """MatchedFilterParameters.get_fft_length / get_block_length follow the
+    reference's getFFTLength (computeWindowLength,
+    src/matchedFilterParameters.cpp:47-104, :268-300): a signal as long as the
+    longest template is accepted; only a shorter one is an error.  Checked
+    against the compiled reference's own parameters object."""
+    cases = [(100, 100), (1, 1), (2, 2), (4097, 4097), (512, 513), (3000, 2999), (7, 3)]
+    cases += [(int(a), int(a + rng.integers(0, 3))) for a in rng.integers(1, 300_000, 150)]
+    cases += [(int(a), int(b)) for a, b in zip(rng.integers(1, 5000, 100), rng.integers(1, 200_000, 100))]
+    for nb, nx in cases:
+        try:
+            want = reference.window_length(nb, nx)
+        except ValueError:
+            want = None
+        p = mflib.MultiChannel.MatchedFilterParameters()
+        wt = mflib.WaveformTemplate()
+        wt.set_signal(np.arange(nb) % 7 - 3.0)
+        wt.set_sampling_rate(1.0)
+        p.add_template(wt)
+        p.set_signal_size(nx)
+        if want is None:
+            with pytest.raises(ValueError):
+                p.get_fft_length()
+        else:
+            assert (p.get_fft_length(), p.get_block_length()) == want, (nb, nx)
+
+
 def test_network_station_phase(mflib):
     # python/unit_tests.py:8-35
     nsp = mflib.NetworkStationPhase()
