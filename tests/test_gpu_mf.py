@@ -381,6 +381,34 @@ def test_short_signal_edge(gpu, oracle, rng):
     assert f.get_valid_matched_filtered_signal(1).size == 0
 
 
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("mode", ["multi", "single"])
+def test_signal_as_long_as_the_template(gpu, oracle, rng, dtype, mode):
+    """A signal as long as the longest template (one valid lag) or one
+    sample longer (two): the reference sizes its FFT from (L, n + L - 1)
+    (src/matchedFilter.cpp:519-525), so both are legal; coefficients equal
+    the two-pass Pearson correlation."""
+    mf = gpu
+    tol = 1e-12 if dtype == np.float64 else 2e-5
+    for L in (2, 37, 500, 3000):
+        for extra in (0, 1):
+            n = L + extra
+            tp = rng.standard_normal(L)
+            sig = rng.standard_normal(n) + 3.0
+            f = mf.SingleChannel.MatchedFilter(dtype=dtype) if mode == "single" else \
+                mf.MultiChannel.MatchedFilter(dtype=dtype)
+            f.initialize(_params(mf, [tp], n, mode=mode))
+            if mode == "single":
+                f.set_signal(sig.astype(dtype))
+            else:
+                f.set_signal(0, sig.astype(dtype))
+            f.apply()
+            r = f.get_matched_filtered_signal(0)
+            assert r.size == extra + 1
+            ref = oracle.pearson_naive(tp, sig.astype(dtype).astype(np.float64))
+            assert np.max(np.abs(r - ref)) < tol, (L, n)
+
+
 def test_spectra_of_template(gpu, rng):
     """getSpectraOfTemplate is the reference's rfft of the reversed,
     demeaned, unit-norm template at its own FFT length."""
