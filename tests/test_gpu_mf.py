@@ -339,6 +339,21 @@ def test_dead_and_zero_signals(gpu, rng):
     f.apply()
     assert np.all(f.get_matched_filtered_signal(1) == 0)
     np.testing.assert_array_equal(f.get_signal(1), np.zeros(n))
+    # a live-looking signal whose extremes are +-5 is dead by the reference's
+    # rule too (|min| == |max|, src/matchedFilter.cpp:882-894); one sample
+    # less extreme makes it live again
+    x = np.clip(rng.standard_normal(n), -4, 4)
+    x[10], x[4000] = 5.0, -5.0
+    for dtype in (np.float64, np.float32):
+        g = mf.MultiChannel.MatchedFilter(dtype=dtype)
+        g.initialize(_params(mf, tps, n))
+        g.set_signal(0, x.astype(dtype))
+        x2 = x.copy()
+        x2[4000] = -4.5
+        g.set_signal(1, x2.astype(dtype))
+        g.apply()
+        assert np.all(g.get_matched_filtered_signal(0) == 0)
+        assert np.any(g.get_matched_filtered_signal(1) != 0)
 
 
 def test_errors(gpu, rng):
