@@ -312,6 +312,11 @@ class MatchedFilter:
         return v.value
 
     def get_number_of_templates(self):
+        """0 before initialize, as pymflib's binding returns
+        (python/multiChannelMatchedFilter.cpp and
+        python/singleChannel/matchedFilter.cpp:97-101); the C++ class throws."""
+        if not self.is_initialized():
+            return 0
         return self._int("mfgpu_mf_get_number_of_templates")
 
     def get_signal_length(self):
