@@ -78,6 +78,11 @@ class MatchedFilterParameters:
         self._signal_size = int(n)
 
     def get_signal_size(self):
+        """0 while no template is set, as pymflib's binding returns
+        (python/multiChannelMatchedFilterParameters.cpp:103-107,
+        python/singleChannel/matchedFilterParameters.cpp:99-103)."""
+        if not self._templates:
+            return 0
         if self._signal_size < 1:
             raise RuntimeError("Signal size not set")
         return self._signal_size
@@ -105,10 +110,12 @@ class MatchedFilterParameters:
         return self._fft, self._block
 
     def get_fft_length(self):
-        return self._sizes()[0]
+        """0 while no template is set, as pymflib's binding returns
+        (python/multiChannelMatchedFilterParameters.cpp:79-84)."""
+        return self._sizes()[0] if self._templates else 0
 
     def get_block_length(self):
-        return self._sizes()[1]
+        return self._sizes()[1] if self._templates else 0
 
     def block_length(self):
         """pymflib binds this name to getFFTLength (python/multiChannelMatchedFilterParameters.cpp:160-162);

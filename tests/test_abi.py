@@ -42,6 +42,26 @@ def test_fft_sizes_through_abi(mflib, oracle, rng):
         mflib.compute_optimal_fft_and_block_length(0, 10)
 
 
+def test_parameters_without_templates(mflib):
+    # pymflib's parameters return 0 for the sizes while no template is set
+    # (python/multiChannelMatchedFilterParameters.cpp:79-107,
+    # python/singleChannel/matchedFilterParameters.cpp:75-103)
+    for p in (mflib.MultiChannel.MatchedFilterParameters(), mflib.SingleChannel.MatchedFilterParameters()):
+        p.set_signal_size(1000)
+        assert p.get_fft_length() == 0 and p.block_length() == 0 and p.get_signal_size() == 0
+        wt = mflib.WaveformTemplate()
+        wt.set_signal(np.arange(50.0))
+        wt.set_sampling_rate(10.0)
+        p.add_template(wt)
+        assert p.get_signal_size() == 1000 and p.get_fft_length() > 0
+        p.clear()
+        p.add_template(wt)
+        with pytest.raises(RuntimeError):
+            p.get_signal_size()  # templates but no size: the reference's getSignalSize throws
+        with pytest.raises(RuntimeError):
+            p.get_fft_length()
+
+
 def test_parameters_window_length_vs_reference(mflib, reference, rng):
     """MatchedFilterParameters.get_fft_length / get_block_length follow the
     reference's getFFTLength (computeWindowLength,
