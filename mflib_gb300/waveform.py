@@ -165,8 +165,10 @@ class WaveformTemplate:
 
     # -- travel time (:326-350)
     def set_phase_travel_time(self, t):
+        # pymflib refuses a negative time as an invalid argument
+        # (python/waveformTemplate.cpp:151-160; the C++ class throws runtime_error)
         if t < 0:
-            raise RuntimeError("Travel time cannot be negative")
+            raise ValueError("travel time = %g must not be negative" % t)
         self._travel = float(t)
 
     def get_phase_travel_time(self):

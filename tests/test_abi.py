@@ -42,6 +42,20 @@ def test_fft_sizes_through_abi(mflib, oracle, rng):
         mflib.compute_optimal_fft_and_block_length(0, 10)
 
 
+def test_waveform_template_time_errors(mflib):
+    # python/waveformTemplate.cpp:135-160: negative onset and travel times are
+    # invalid arguments
+    wt = mflib.WaveformTemplate()
+    wt.set_signal(np.arange(10.0))
+    wt.set_sampling_rate(10.0)
+    with pytest.raises(ValueError):
+        wt.set_phase_travel_time(-1.0)
+    with pytest.raises(ValueError):
+        wt.set_phase_onset_time_in_signal(-0.1)
+    wt.set_phase_travel_time(0.0)
+    assert wt.have_travel_time() and wt.get_phase_travel_time() == 0.0
+
+
 def test_parameters_without_templates(mflib):
     # pymflib's parameters return 0 for the sizes while no template is set
     # (python/multiChannelMatchedFilterParameters.cpp:79-107,
