@@ -215,6 +215,27 @@ def max_over_ranks(value, dist, device="cpu"):
     return float(t.item())
 
 
+def gather_detections_to_rank0(counts, idx, fs, group):
+    """The multi-rank path's one exchange: every rank's detections (template
+    index and detection time of each peak of its last step) as the 280-byte
+    wire records of mflib_gb300.mpi, gathered on rank 0 over a host (gloo)
+    group for association there.  Returns the number of detections rank 0
+    received, None on the other ranks."""
+    from mflib_gb300 import NetworkStationPhase, mpi
+    from mflib_gb300.detector import Detection
+    nsp = NetworkStationPhase()
+    dets, o = [], 0
+    for t, c in enumerate(np.asarray(counts).tolist()):
+        for k in np.asarray(idx[o:o + c]).tolist():
+            d = Detection()
+            d.set_template_identifier((nsp, t))
+            d.set_detection_time(k / fs)
+            dets.append(d)
+        o += c
+    got = mpi.gather_detections(dets, dst=0, group=group)
+    return None if got is None else len(got)
+
+
 def measured_peak(key="hbm_gbs"):
     """Measured peak of the GB300s (HBM GB/s or dense BF16 TFLOP/s),
     else the fallback figure of an earlier GB300 measurement."""
@@ -648,6 +669,7 @@ class Ctx:
         self.rank = int(os.environ.get("RANK", "0"))
         self.local = int(os.environ.get("LOCAL_RANK", "0"))
         self.dist = None
+        self.gloo = None  # host-tensor group for the gather of detections
 
     def barrier(self):
         if self.dist is not None:
@@ -785,6 +807,8 @@ def run_uneven_day(args, ctx):
                            "get_all_peaks"},
             "roofline": roof, "gpu_launches": int(launches), "clocks": clk, "detections": int(idx.size),
             "graph_replays": f.graph_launches()}
+    if ctx.world > 1:  # after the timed regions; every rank takes part
+        line["gathered_detections"] = gather_detections_to_rank0(counts, idx, FS, ctx.gloo)
     # The split-precision tensor-core form on this bank, by arithmetic: per
     # template-lag it executes 3 products (hi*hi, hi*lo, lo*hi) over the
     # template's K padded to 16 (K = L + 7 for the 8 phases of a row), 2 flops
@@ -962,6 +986,8 @@ def run_day24(args, ctx, steps=None, warmup=None, cpu=True):
             "roofline": roof, "gpu_launches": int(launches), "clocks": clk,
             "detections": int(idx.size), "events_found": int(np.sum(ncl)),
             "events_injected": int(w["origins"].size)}
+    if ctx.world > 1:  # after the timed regions; every rank takes part
+        line["gathered_detections"] = gather_detections_to_rank0(counts, idx, FS, ctx.gloo)
     if cpu and ctx.rank == 0 and ctx.world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(w).items() if k != "seconds"}
     f.clear()
@@ -1030,6 +1056,8 @@ def main():
             torch.cuda.set_device(ctx.local)
         dist.init_process_group("nccl" if args.impl == "ours" else "gloo")
         ctx.dist = dist
+        if args.impl == "ours":
+            ctx.gloo = dist.new_group(backend="gloo")
 
     if args.impl == "reference":
         run_reference(args, ctx.rank)

@@ -1,6 +1,7 @@
 """Host logic of the N > 1 path on CPU: the max-over-ranks timing with the
-gloo backend (world size 2), and the reference arm under torchrun, where
-rank 0 alone runs and prints the one JSON line and rank 1 exits cleanly."""
+gloo backend (world size 2), the gather of every rank's detections to rank
+0, and the reference arm under torchrun, where rank 0 alone runs and prints
+the one JSON line and rank 1 exits cleanly."""
 import json
 import os
 import socket
@@ -62,3 +63,35 @@ def test_reference_arm_two_ranks():
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["value"] > 0 and d["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def _gather_rank(rank, world, port, q):
+    import numpy as np
+    import torch.distributed as dist
+    sys.path.insert(0, ROOT)
+    import bench
+    dist.init_process_group("gloo", init_method="tcp://127.0.0.1:%d" % port, rank=rank, world_size=world)
+    try:
+        counts = np.array([2, 0, 3], dtype=np.int32) if rank == 0 else np.array([1, 1, 0, 4], dtype=np.int32)
+        idx = np.arange(int(counts.sum()), dtype=np.int32) * 10 + rank
+        q.put((rank, bench.gather_detections_to_rank0(counts, idx, 100.0, None)))
+        dist.barrier()
+    finally:
+        dist.destroy_process_group()
+
+
+def test_gather_detections_to_rank0_gloo():
+    """The N > 1 path's one exchange: each rank's peaks as detection records
+    to rank 0 (world size 2, gloo)."""
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_gather_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = dict(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert got == {0: 5 + 6, 1: None}
